@@ -1,0 +1,202 @@
+/*
+ * efs_gb300.h — C ABI of the GB300 (sm_103a) Eulerian liquid step.
+ *
+ * One context (efs_ctx) holds one MAC grid resident in HBM, its own CUDA stream and the CUDA graphs
+ * that replay whole steps.  Every entry point returns an int status (EFS_OK == 0); the text of the
+ * last failure is available from efs_last_error().  Signatures use plain pointers and sizes only.
+ *
+ * The entry points replace the reference's simulator-backend interface for the liquid step
+ * (MarQMark/EulerianFluidSimulation):
+ *   - ISimulator::update()              include/simulation/simulator/ISimulator.h:12-38  -> efs_step
+ *   - the seven protected stage virtuals include/simulation/simulator/ISimulator.h:43-50 -> efs_stage
+ *   - ISolver3D/ISolver2D::solve(IGrid*) include/simulation/solver/ISolver.h:7-47        -> efs_solve
+ *   - IGrid3D/IGrid2D field accessors    include/simulation/data/IGrid.h:10-68            -> efs_upload_field /
+ *                                                                                         efs_download_field
+ *   - CudaGrid3D::upload()/download()    src/simulation/data/CudaGrid3D.cu:247-269        -> efs_upload_fields /
+ *                                                                                         efs_download_fields
+ *   - the Properties values the step reads include/simulation/Properties.h:136-218       -> efs_params
+ *
+ * Host field layout is the reference's: x fastest, then y, then z (index z*W*H + y*W + x, W/H/D include the
+ * one-cell wall border); velocity and forces are interleaved glm::vec3 (3D) or glm::vec2 (2D) floats;
+ * scalar fields are float; `boundary` is 1.0 for solid cells and 0.0 otherwise.
+ */
+#ifndef EFS_GB300_H
+#define EFS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EFS_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum efs_status {
+    EFS_OK = 0,
+    EFS_ERR_ARG = 1,            /* bad argument (size, pointer, enum, field value)                  */
+    EFS_ERR_CUDA = 2,           /* a CUDA runtime call failed                                      */
+    EFS_ERR_STATE = 3,          /* call not valid in the context's current state                   */
+    EFS_ERR_NO_DEVICE = 4,      /* no CUDA device visible                                          */
+    EFS_ERR_DEVICE_FAULT = 5,   /* a kernel reported an error through the device status word       */
+    EFS_ERR_NOT_CONVERGED = 6   /* efs_solve only: the pressure solve hit max_steps                */
+};
+
+/* ---- the seven stages, in ISimulator::update order (ISimulator.h:15-35) ---- */
+enum efs_stage {
+    EFS_STAGE_VEL_DECAY = 0,
+    EFS_STAGE_VEL_EXTRAPOLATE = 1,
+    EFS_STAGE_RHO_SHARPEN = 2,
+    EFS_STAGE_RHO_ADVECT = 3,
+    EFS_STAGE_VEL_ADVECT = 4,
+    EFS_STAGE_ADD_FORCE = 5,
+    EFS_STAGE_PROJECT = 6,
+    EFS_STAGE_COUNT = 7
+};
+#define EFS_STAGE_BIT(s) (1u << (s))
+#define EFS_STAGES_ALL 0x7Fu
+
+/* ---- pressure solvers (Properties::SolverType, Properties.h:476-482) ---- */
+enum efs_solver {
+    EFS_SOLVER_JACOBI = 0,      /* JacobiSolverCPU3D: max_steps/2 sweeps from p = 0                */
+    EFS_SOLVER_CG = 1           /* CGSolverCPU3D: p0 = b, true residual every 64 iterations        */
+};
+
+/* CG variants.  Both follow CGSolverCPU3D::solve (CGSolver.cpp:416-465): p0 = b, recurrence residual, the
+ * true residual recomputed when (i & 63) == 0, stop when r.r < threshold or after max_steps, FP64 dot
+ * products.  EFS_CG_MIXED keeps the pressure as an FP64 accumulator plus an FP32 increment that is folded in
+ * at every recomputation, and computes that true residual in FP64 (group-wise reliable updates); before
+ * stopping it recomputes the true residual once more and continues if it is above the threshold.  This
+ * reaches relative residuals below what any FP32 pressure field can represent (the rounded exact solution
+ * sits near 1e-5 on these grids).  EFS_CG_REFERENCE keeps the pressure in FP32 and recomputes the residual in
+ * FP32, like the reference. */
+enum efs_cg_variant {
+    EFS_CG_MIXED = 0,
+    EFS_CG_REFERENCE = 1
+};
+
+/* ---- fields (IGrid3D accessors, IGrid.h:44-68) ---- */
+enum efs_field {
+    EFS_FIELD_VEL = 0,          /* dim floats per cell (MAC faces: vel(x,y,z).x is the face between x-1 and x) */
+    EFS_FIELD_RHO = 1,
+    EFS_FIELD_GAMMA = 2,
+    EFS_FIELD_BETA = 3,
+    EFS_FIELD_DIVERGENCE = 4,
+    EFS_FIELD_PRESSURE = 5,
+    EFS_FIELD_FORCES = 6,       /* dim floats per cell */
+    EFS_FIELD_BOUNDARY = 7,     /* 0.0 or 1.0 */
+    EFS_FIELD_COUNT = 8
+};
+
+/* Density-sharpen scatter semantics.  The reference applies each cell's change and scatters its
+ * counter-mass while later cells of the same loop read the updated density
+ * (CPUSimulator3D.cpp:446-455).  The GPU applies every cell's change first, then traces all cells
+ * on that field, then scatters; the two differ only through the order of those updates. */
+enum efs_sharpen_mode {
+    EFS_SHARPEN_PARALLEL = 0
+};
+
+/* Values of the reference Properties the step reads (Properties.h:141-162, 186-192). */
+typedef struct efs_params {
+    float dt;                 /* DT                                                       */
+    float gravity_force;      /* GRAVITY_FORCE in cells/s^2 (= GRAVITY_FORCE_PHYSICAL / CELL_SIZE, Application.cpp:89) */
+    int   gravity_enabled;    /* GRAVITY_ENABLED                                          */
+    float vel_decay;          /* VEL_DECAY                                                */
+    float lambda_minus;       /* LAMBDA_MINUS                                             */
+    float lambda_plus;        /* LAMBDA_PLUS                                              */
+    float eta;                /* ETA                                                      */
+    float liquid_threshold;   /* LIQUID_THRESHOLD                                         */
+    float rho_d;              /* RHO_D (sharpen trace length, cells)                      */
+    int   solver;             /* enum efs_solver (SOLVER_TYPE)                            */
+    int   max_steps;          /* MAX_STEPS (CG iteration cap; Jacobi runs max_steps/2)    */
+    float solver_threshold;   /* SOLVER_THRESHOLD: absolute r.r stop, used when tol_rel <= 0 */
+    float tol_rel;            /* > 0: stop when r.r < tol_rel^2 * b.b (relative residual) */
+    unsigned disable_mask;    /* bit s set = DISABLE_<stage s> (Properties.h:114-120)     */
+    int   re_calc_div;        /* RE_CALC_DIV (2D only)                                    */
+    int   sharpen_mode;       /* enum efs_sharpen_mode                                    */
+    int   cg_variant;         /* enum efs_cg_variant                                      */
+    int   reserved[5];
+} efs_params;
+
+/* Per-context statistics (Properties SOLVE_STEPS / SOLVE_ERRORS / PAUSED / SIMULATION_FRAMES). */
+typedef struct efs_stats {
+    int64_t frames;           /* completed steps (SIMULATION_FRAMES)                      */
+    int     solve_steps;      /* iterations of the last pressure solve (SOLVE_STEPS)      */
+    int     converged;        /* last solve met its stop rule                             */
+    int     paused;           /* set when a solve did not converge (CPUSimulator3D.cpp:541-547) */
+    int     device_error;     /* device status word (0 = none)                            */
+    double  rr;               /* last solve: final r.r (FP64)                             */
+    double  bb;               /* last solve: b.b (FP64)                                   */
+    double  threshold;        /* last solve: the r.r threshold it used                    */
+    int64_t active_cells;     /* last solve: matrix rows (liquid, non-solid cells)        */
+    int64_t total_solve_steps;/* sum of solve_steps over all solves since create / reset  */
+    int64_t solves;           /* number of solves since create / reset                    */
+} efs_stats;
+
+typedef struct efs_ctx efs_ctx;
+
+/* ---- defaults ---- */
+/* Reference Properties defaults (Properties.h:141-162; gravity 10 / cell size 1). */
+void efs_params_default(efs_params* p);
+/* Dam-break constants of the reference scene assets/scenes/Dam128.json "properties": lambda- 50,
+ * lambda+ 10, eta 100, D 32, velocity decay disabled, liquid threshold 0.5, gravity 9.81 / cell_size,
+ * with the given dt, solver and relative tolerance. */
+void efs_params_dam(efs_params* p, float cell_size, float dt, int solver, float tol_rel);
+
+/* ---- lifetime ---- */
+int  efs_abi_version(void);
+int  efs_device_count(int* count);
+/* dim 2: depth must be 1.  width/height/depth >= 4 and include the one-cell border. */
+int  efs_create(int dim, int width, int height, int depth, const efs_params* params, efs_ctx** out);
+void efs_destroy(efs_ctx* ctx);
+/* Text of the last failure on this context (ctx == NULL: the last efs_create failure). */
+const char* efs_last_error(const efs_ctx* ctx);
+
+int  efs_set_params(efs_ctx* ctx, const efs_params* params);
+int  efs_get_params(const efs_ctx* ctx, efs_params* params);
+
+/* ---- fields (host buffers in the reference layout) ---- */
+int  efs_upload_field(efs_ctx* ctx, int field, const float* host);
+int  efs_download_field(efs_ctx* ctx, int field, float* host);
+/* CudaGrid3D::upload (CudaGrid3D.cu:247-256): NULL pointers are skipped. */
+int  efs_upload_fields(efs_ctx* ctx, const float* vel, const float* rho, const float* gamma,
+                       const float* boundary, const float* forces);
+/* CudaGrid3D::download (CudaGrid3D.cu:258-269): NULL pointers are skipped. */
+int  efs_download_fields(efs_ctx* ctx, float* vel, float* rho, float* gamma, float* beta,
+                         float* divergence, float* pressure);
+/* Grid3D/Grid2D constructor state (Grid3D.cpp:10-48): zero fields, gamma = 1, solid border, rho = 0 on it. */
+int  efs_reset_fields(efs_ctx* ctx);
+
+/* ---- the step ---- */
+/* One reference stage virtual, regardless of disable_mask. */
+int  efs_stage(efs_ctx* ctx, int stage);
+/* n_steps x ISimulator::update(): the stages not in params.disable_mask, replayed from one CUDA graph
+ * per configuration.  Returns after launching; efs_synchronize waits. */
+int  efs_step(efs_ctx* ctx, int n_steps);
+/* ISolver::solve on the context's current divergence / rho / boundary, into pressure. */
+int  efs_solve(efs_ctx* ctx, efs_stats* out);
+int  efs_synchronize(efs_ctx* ctx);
+int  efs_get_stats(efs_ctx* ctx, efs_stats* out);
+/* FP64 sum of rho over all cells (StatsView total, Grid3D.cpp:44-47 in float). */
+int  efs_total_mass(efs_ctx* ctx, double* out);
+
+/* ---- timing of the dominant kernel (the pressure solve) over replayed steps ---- */
+/* Arms a pool of `capacity` CUDA event pairs recorded around each pressure-solve launch on the
+ * context's stream during efs_step.  capacity 0 disarms. */
+int  efs_solve_timing_arm(efs_ctx* ctx, int capacity);
+/* Number of recorded launches, their summed device time (ms) and summed solver iterations. */
+int  efs_solve_timing_read(efs_ctx* ctx, int* launches, double* total_ms, int64_t* total_iterations,
+                           int64_t* total_active_cells);
+
+/* ---- host-only helpers (no device needed) ---- */
+/* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */
+int  efs_scene_dam3d(int w, int h, int d, int n_spheres_min, int n_spheres_max, uint64_t seed,
+                     float* boundary, float* rho);
+int  efs_scene_dam2d(int w, int h, float* boundary, float* rho);
+int  efs_scene_batch2d(uint64_t seed, int* side, float* boundary, float* rho, int capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EFS_GB300_H */

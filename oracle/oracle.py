@@ -1,0 +1,253 @@
+"""Python binding of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+``Oracle`` wraps the C restatement (``oracle/liborc.so`` built from ``efs_oracle.c``); ``RefOracle`` wraps the
+reference's own CPU backend compiled from its sources (``oracle/_ref/libefs_ref.so``, only where the
+reference tree exists).  Both expose the same calls as the product binding so tests can run the three side by
+side: ``set_field`` / ``field`` (reference layout), ``stage``, ``step``, ``stats``.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from eulerianfluidsimulation_gb300.abi import (EfsParams, EfsStats, FIELD_COUNT, VECTOR_FIELDS)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBORC = os.path.join(HERE, "liborc.so")
+LIBREF = os.path.join(HERE, "_ref", "libefs_ref.so")
+REFERENCE_TREE = "/root/reference"
+
+DOTS_FP64 = 1
+SHARPEN_PARALLEL = 2
+
+
+def build(reference=True):
+    """Build liborc.so and, when the reference tree is present, _ref/libefs_ref.so."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "oracle"])
+    if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "src")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_TREE])
+
+
+def reference_available():
+    return os.path.exists(LIBREF)
+
+
+_orc = None
+_ref = None
+_FP = ctypes.POINTER(ctypes.c_float)
+
+
+def _load_orc():
+    global _orc
+    if _orc is None:
+        if not os.path.exists(LIBORC):
+            build(reference=False)
+        lib = ctypes.CDLL(LIBORC)
+        lib.orc_create.restype = ctypes.c_void_p
+        lib.orc_create.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(EfsParams)]
+        lib.orc_destroy.argtypes = [ctypes.c_void_p]
+        lib.orc_set_params.argtypes = [ctypes.c_void_p, ctypes.POINTER(EfsParams)]
+        lib.orc_set_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_field.restype = _FP
+        lib.orc_field.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_reset.argtypes = [ctypes.c_void_p]
+        lib.orc_stage.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.orc_solve.restype = ctypes.c_float
+        lib.orc_solve.argtypes = [ctypes.c_void_p]
+        lib.orc_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(EfsStats)]
+        lib.orc_solve_fp64.restype = ctypes.c_int
+        lib.orc_solve_fp64.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.orc_relres_fp64.restype = ctypes.c_double
+        lib.orc_relres_fp64.argtypes = [ctypes.c_void_p, _FP]
+        lib.orc_total_mass.restype = ctypes.c_double
+        lib.orc_total_mass.argtypes = [ctypes.c_void_p]
+        lib.orc_params_default.argtypes = [ctypes.POINTER(EfsParams)]
+        lib.orc_scene_dam3d.restype = ctypes.c_int
+        lib.orc_scene_dam3d.argtypes = [ctypes.c_int] * 5 + [ctypes.c_uint64, _FP, _FP]
+        lib.orc_scene_dam2d.restype = ctypes.c_int
+        lib.orc_scene_dam2d.argtypes = [ctypes.c_int, ctypes.c_int, _FP, _FP]
+        lib.orc_scene_batch2d.restype = ctypes.c_int
+        lib.orc_scene_batch2d.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _FP, _FP]
+        _orc = lib
+    return _orc
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        lib = ctypes.CDLL(LIBREF)
+        lib.ref_create.restype = ctypes.c_void_p
+        lib.ref_create.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(EfsParams)]
+        lib.ref_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_set_params.argtypes = [ctypes.c_void_p, ctypes.POINTER(EfsParams)]
+        lib.ref_field.restype = _FP
+        lib.ref_field.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_stage.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(EfsStats)]
+        _ref = lib
+    return _ref
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_FP)
+
+
+def scene_dam3d(w, h, d, n_min, n_max, seed):
+    """Seeded 3D dam break with spheres (include/efs_scene.h) -> (boundary, rho) float32 arrays (d, h, w)."""
+    lib = _load_orc()
+    b = np.zeros((d, h, w), np.float32)
+    r = np.zeros((d, h, w), np.float32)
+    n = lib.orc_scene_dam3d(w, h, d, n_min, n_max, seed, _fptr(b), _fptr(r))
+    if n < 0:
+        raise ValueError("bad scene arguments")
+    return b, r
+
+
+def scene_dam2d(w, h):
+    lib = _load_orc()
+    b = np.zeros((h, w), np.float32)
+    r = np.zeros((h, w), np.float32)
+    if lib.orc_scene_dam2d(w, h, _fptr(b), _fptr(r)) < 0:
+        raise ValueError("bad scene arguments")
+    return b, r
+
+
+def scene_batch2d(seed):
+    lib = _load_orc()
+    side = ctypes.c_int(0)
+    lib.orc_scene_batch2d(seed, ctypes.byref(side), None, None)
+    s = side.value
+    b = np.zeros((s, s), np.float32)
+    r = np.zeros((s, s), np.float32)
+    lib.orc_scene_batch2d(seed, ctypes.byref(side), _fptr(b), _fptr(r))
+    return b, r
+
+
+class _Base:
+    def __init__(self, dim, w, h, d, params):
+        self.dim, self.w, self.h = dim, w, h
+        self.d = d if dim == 3 else 1
+        self.shape = (self.d, h, w) if dim == 3 else (h, w)
+        self.params = params.copy()
+
+    def _shape(self, f):
+        return self.shape + (self.dim,) if f in VECTOR_FIELDS else self.shape
+
+    def field(self, f):
+        n = int(np.prod(self._shape(f)))
+        ptr = self._ptr(f)
+        return np.ctypeslib.as_array(ptr, shape=(n,)).reshape(self._shape(f)).copy()
+
+    def set_field(self, f, arr):
+        n = int(np.prod(self._shape(f)))
+        src = np.ascontiguousarray(arr, dtype=np.float32).reshape(-1)
+        if src.size != n:
+            raise ValueError("field size mismatch")
+        ctypes.memmove(self._ptr(f), src.ctypes.data, n * 4)
+
+    def fields(self):
+        return {f: self.field(f) for f in range(FIELD_COUNT)}
+
+    def set_fields(self, fields):
+        for f, a in fields.items():
+            self.set_field(f, a)
+
+
+class Oracle(_Base):
+    """The C restatement of the reference CPU path (efs_oracle.c)."""
+
+    def __init__(self, dim, w, h, d=1, params=None, mode=0):
+        lib = _load_orc()
+        if params is None:
+            params = EfsParams()
+            lib.orc_params_default(ctypes.byref(params))
+        super().__init__(dim, w, h, d, params)
+        self._lib = lib
+        self._h = lib.orc_create(dim, w, h, self.d, ctypes.byref(self.params))
+        if not self._h:
+            raise ValueError("orc_create failed")
+        lib.orc_set_mode(self._h, mode)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.orc_destroy(self._h)
+            self._h = None
+
+    def _ptr(self, f):
+        return self._lib.orc_field(self._h, f)
+
+    def set_params(self, params):
+        self.params = params.copy()
+        self._lib.orc_set_params(self._h, ctypes.byref(self.params))
+
+    def set_mode(self, mode):
+        self._lib.orc_set_mode(self._h, mode)
+
+    def reset(self):
+        self._lib.orc_reset(self._h)
+
+    def stage(self, s):
+        self._lib.orc_stage(self._h, s)
+
+    def step(self, n=1):
+        self._lib.orc_step(self._h, n)
+
+    def solve(self):
+        return self._lib.orc_solve(self._h)
+
+    def stats(self):
+        s = EfsStats()
+        self._lib.orc_stats(self._h, ctypes.byref(s))
+        return s
+
+    def solve_fp64(self, tol=1e-12, maxit=100000):
+        p = np.zeros(self.shape, np.float64)
+        it = self._lib.orc_solve_fp64(self._h, tol, maxit, p.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return p, it
+
+    def relres_fp64(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        return self._lib.orc_relres_fp64(self._h, _fptr(p))
+
+    def total_mass(self):
+        return self._lib.orc_total_mass(self._h)
+
+
+class RefOracle(_Base):
+    """The reference's own CPUSimulator2D/3D compiled from its sources with the shim include directory."""
+
+    def __init__(self, dim, w, h, d=1, params=None):
+        if not reference_available():
+            raise RuntimeError("oracle/_ref/libefs_ref.so is not built (needs the reference tree)")
+        lib = _load_ref()
+        super().__init__(dim, w, h, d, params)
+        self._lib = lib
+        self._h = lib.ref_create(dim, w, h, self.d, ctypes.byref(self.params))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.ref_destroy(self._h)
+            self._h = None
+
+    def _ptr(self, f):
+        return self._lib.ref_field(self._h, f)
+
+    def set_params(self, params):
+        self.params = params.copy()
+        self._lib.ref_set_params(self._h, ctypes.byref(self.params))
+
+    def stage(self, s):
+        self._lib.ref_stage(self._h, s)
+
+    def step(self, n=1):
+        self._lib.ref_step(self._h, n)
+
+    def stats(self):
+        s = EfsStats()
+        self._lib.ref_stats(self._h, ctypes.byref(s))
+        return s

@@ -1,0 +1,46 @@
+// Shim for the reference build only (oracle/_ref): glm vector subset, see vec3.hpp.
+#pragma once
+#include <cmath>
+namespace glm {
+struct vec2 {
+    float x, y;
+    vec2() : x(0.f), y(0.f) {}
+    explicit vec2(float s) : x(s), y(s) {}
+    vec2(float a, float b) : x(a), y(b) {}
+    float& operator[](int i) { return i == 0 ? x : y; }
+    float operator[](int i) const { return i == 0 ? x : y; }
+    vec2& operator+=(const vec2& o) { x += o.x; y += o.y; return *this; }
+    vec2& operator-=(const vec2& o) { x -= o.x; y -= o.y; return *this; }
+    vec2& operator*=(float s) { x *= s; y *= s; return *this; }
+    vec2& operator/=(float s) { x /= s; y /= s; return *this; }
+};
+inline vec2 operator+(const vec2& a, const vec2& b) { return vec2(a.x + b.x, a.y + b.y); }
+inline vec2 operator-(const vec2& a, const vec2& b) { return vec2(a.x - b.x, a.y - b.y); }
+inline vec2 operator*(const vec2& a, float s) { return vec2(a.x * s, a.y * s); }
+inline vec2 operator*(float s, const vec2& a) { return vec2(s * a.x, s * a.y); }
+inline vec2 operator/(const vec2& a, float s) { return vec2(a.x / s, a.y / s); }
+inline float length(const vec2& v) { float t0 = v.x * v.x, t1 = v.y * v.y; return std::sqrt(t0 + t1); }
+
+struct vec3 {
+    float x, y, z;
+    vec3() : x(0.f), y(0.f), z(0.f) {}
+    explicit vec3(float s) : x(s), y(s), z(s) {}
+    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+    vec3& operator+=(const vec3& o) { x += o.x; y += o.y; z += o.z; return *this; }
+    vec3& operator-=(const vec3& o) { x -= o.x; y -= o.y; z -= o.z; return *this; }
+    vec3& operator*=(float s) { x *= s; y *= s; z *= s; return *this; }
+    vec3& operator/=(float s) { x /= s; y /= s; z /= s; return *this; }
+};
+inline vec3 operator+(const vec3& a, const vec3& b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline vec3 operator-(const vec3& a, const vec3& b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline vec3 operator*(const vec3& a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
+inline vec3 operator*(float s, const vec3& a) { return vec3(s * a.x, s * a.y, s * a.z); }
+inline vec3 operator/(const vec3& a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
+inline float length(const vec3& v) { float t0 = v.x * v.x, t1 = v.y * v.y, t2 = v.z * v.z; return std::sqrt(t0 + t1 + t2); }
+
+struct vec4 { float x, y, z, w; };
+struct mat4 { float m[16]; };
+static_assert(sizeof(vec2) == 8 && sizeof(vec3) == 12, "glm vectors are packed floats");
+}  // namespace glm

@@ -1,0 +1,77 @@
+"""Generate the golden fixtures in this folder from the reference's own CPU backend.
+
+Runs the unmodified reference sources (built by ``oracle/Makefile`` into ``oracle/_ref/libefs_ref.so``, which
+needs the reference tree) on small seeded scenes and stores, per case:
+  ``state``           all eight fields after ``warmup`` full steps from the seeded scene,
+  ``stage<s>``        all fields after running stage s alone from ``state`` (s = 0..6),
+  ``steps``           all fields after ``nsteps`` more full steps from ``state``,
+plus the parameters used.  Sizes are chosen so the reference's 32-bit advection-matrix key cannot wrap
+(3D: cells^2 < 2^32; 2D: side <= 256).
+
+Usage: python tests/golden/make_golden.py      (writes ref_3d_cg.npz, ref_2d_jacobi.npz, ref_2d_cg.npz)
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+sys.path.insert(0, ROOT)
+
+from eulerianfluidsimulation_gb300 import abi  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+CASES = {
+    # name: (dim, side, solver, dt, tol_rel, warmup, nsteps, spheres)
+    "ref_3d_cg": (3, 24, abi.SOLVER_CG, 0.004, 0.0, 4, 2, 6),
+    "ref_2d_jacobi": (2, 48, abi.SOLVER_JACOBI, 0.005, 0.0, 6, 3, 0),
+    "ref_2d_cg": (2, 40, abi.SOLVER_CG, 0.005, 0.0, 6, 3, 0),
+}
+
+
+def case_params(dim, side, solver, dt, tol_rel):
+    p = abi.params_dam(1.0 / side, dt, solver, tol_rel)
+    p.cg_variant = abi.CG_REFERENCE
+    if solver == abi.SOLVER_JACOBI:
+        p.max_steps = 200
+    return p
+
+
+def scene(dim, side, spheres, seed=1):
+    if dim == 3:
+        return oracle.scene_dam3d(side, side, side, spheres, spheres, seed)
+    return oracle.scene_dam2d(side, side)
+
+
+def make(name):
+    dim, side, solver, dt, tol, warmup, nsteps, spheres = CASES[name]
+    prm = case_params(dim, side, solver, dt, tol)
+    b, r = scene(dim, side, spheres)
+    ref = oracle.RefOracle(dim, side, side, side, prm)
+    ref.set_field(abi.FIELD_BOUNDARY, b)
+    ref.set_field(abi.FIELD_RHO, r)
+    ref.step(warmup)
+    state = ref.fields()
+    out = {"params": np.frombuffer(bytes(prm), np.uint8).copy(), "meta": np.array([dim, side, warmup, nsteps, spheres])}
+    for f, a in state.items():
+        out[f"state_{f}"] = a
+    for s in range(abi.STAGE_COUNT):
+        ref.set_fields(state)
+        ref.stage(s)
+        for f, a in ref.fields().items():
+            out[f"stage{s}_{f}"] = a
+    ref.set_fields(state)
+    ref.step(nsteps)
+    for f, a in ref.fields().items():
+        out[f"steps_{f}"] = a
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    oracle.build(reference=True)
+    if not oracle.reference_available():
+        sys.exit("the reference tree is needed to generate golden fixtures")
+    for n in CASES:
+        make(n)
