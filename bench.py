@@ -1,0 +1,305 @@
+#!/usr/bin/env python3
+"""bench.py — steps/s of the Eulerian liquid step on a 256^3 dam break with 16 seeded solid spheres.
+
+One step is one ISimulator::update(): the seven stages of the reference order (velocity decay disabled, as in
+the reference's dam-break scene) with the pressure solved by CG to relative residual 1e-6.  The grid (about
+2 GB of fields and temporaries) is larger than L2, so no flush is needed between steps.
+
+Lines printed (rank 0, one JSON object):
+  --impl gb300 (default): `value` = steps/s with the fields resident in HBM (CUDA events on the library's
+      stream around K replayed step graphs); `e2e` = the same through efs_upload_fields / efs_step /
+      efs_download_fields with pinned host buffers every step; `roofline` for the pressure solve (the
+      dominant kernel); `cpu_baseline` = the CPU oracle (a port of the reference CPU step) on a bounded sample.
+  --impl reference: the reference's CPU step on the host cores (the oracle port; the reference's own sources
+      need its build tree) on the same workload, bounded sample.
+With --gpus N (torchrun), every rank advances its own replica (weak scaling; the step has no data exchange).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s at 256^3 to rel-res 1e-6 (plain CG)"
+# Bytes the pressure solve must move, per matrix row: per CG iteration read d_prev, r, rowinfo and write d
+# (14 B), then read d, e, r, rowinfo and write e, r (22 B); per solve set-up read b, rowinfo and write p64, e,
+# r, d and finally p (30 B).  Neighbour reads of the stencils are cache hits and count 0.
+SOLVE_BYTES_PER_ROW_ITER = 36.0
+SOLVE_BYTES_PER_ROW_SETUP = 30.0
+# Mean CG iterations per step the CUDA path needs on this workload (measured by the gb300 arm over the first
+# steps of the dam break; printed in its JSON line as cg_iters_per_step).  The CPU-baseline sample times a
+# few CG iterations and scales them to this count instead of solving at 256^3 on one core for minutes.
+CG_ITERS_PER_STEP_REF = 400
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--spheres", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--dt", type=float, default=0.004)
+    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(a):
+    from eulerianfluidsimulation_gb300 import abi
+    solver = abi.SOLVER_CG if a.solver == "cg" else abi.SOLVER_JACOBI
+    prm = abi.params_dam(1.0 / a.size, a.dt, solver, 1e-6)
+    if solver == abi.SOLVER_JACOBI:
+        prm.max_steps = 200
+    return prm
+
+
+def config(a):
+    return {"workload": f"dam3d_{a.size}", "grid": [a.size] * 3, "spheres": a.spheres, "seed": a.seed, "dt": a.dt,
+            "solver": a.solver + (" rel-res 1e-6, FP32 fields, FP64 dots + FP64 residual replacement" if a.solver == "cg" else " 100 sweeps"),
+            "scene": "seeded synthetic: fluid x<0.4,y<0.6; spheres r~U[0.04,0.1], centres~U[0.2,0.8]^3 (PCG32)",
+            "l2": "working set ~2 GB > 129 MB L2 (no flush)"}
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(a, prm, cg_iters):
+    """Time the CPU oracle (port of the reference CPU step) on the same 256^3 state: stages 0-5 once, the project
+    set-up, and 8 CG iterations; the step time scales the CG part to `cg_iters` iterations."""
+    from eulerianfluidsimulation_gb300 import abi
+    from oracle import oracle
+    n = a.size
+    b, r = oracle.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
+    p = prm.copy()
+    o = oracle.Oracle(3, n, n, n, p)
+    o.set_field(abi.FIELD_BOUNDARY, b)
+    o.set_field(abi.FIELD_RHO, r)
+    t0 = time.perf_counter()
+    for s in range(abi.STAGE_PROJECT):
+        if not (p.disable_mask >> s) & 1:
+            o.stage(s)
+    t1 = time.perf_counter()
+    state = o.fields()
+    p0 = p.copy(); p0.max_steps = 0
+    o.set_params(p0)
+    ta = time.perf_counter(); o.stage(abi.STAGE_PROJECT); tb = time.perf_counter()
+    k = 8
+    pk = p.copy(); pk.max_steps = k
+    o.set_fields(state)
+    o.set_params(pk)
+    tc = time.perf_counter(); o.stage(abi.STAGE_PROJECT); td = time.perf_counter()
+    t_stages, t_setup = t1 - t0, tb - ta
+    t_iter = max((td - tc) - t_setup, 0.0) / k
+    step_s = t_stages + t_setup + cg_iters * t_iter
+    return {"value": 1.0 / step_s, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": (f"one {n}^3 step on 1 core: stages 0-5 {t_stages:.2f} s, project set-up {t_setup:.2f} s, "
+                       f"{k} CG iterations at {t_iter * 1e3:.1f} ms each scaled to {cg_iters:.0f} iterations/step"),
+            "step_s": step_s}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    prm = workload(a)
+    t = time.perf_counter()
+    cs = cpu_sample(a, prm, CG_ITERS_PER_STEP_REF)
+    wall = time.perf_counter() - t
+    line = {"metric": METRIC, "value": cs["value"], "unit": "steps/s", "n_gpus": a.gpus, "steps": 1, "warmup": 0,
+            "ms_per_step": cs["step_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": config(a), "impl": "reference",
+            "cpu_baseline": {"value": cs["value"], "unit": "steps/s", "cores": cs["cores"], "kind": cs["kind"],
+                             "sample": cs["sample"] + f"; CG count = the CUDA path's measured mean ({CG_ITERS_PER_STEP_REF})"},
+            "e2e": {"value": cs["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "sample_wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(a):
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    n = a.size
+    prm = workload(a)
+    b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed + rank)
+    N = n ** 3
+    sim = gb.GB300Simulator3D(n, n, n, prm)
+    sim.set_field(abi.FIELD_BOUNDARY, b)
+    sim.set_field(abi.FIELD_RHO, r)
+    for _ in range(a.warmup):
+        sim.update(1)
+    st0 = sim.stats()
+    sim.synchronize()
+    kernels = sim.kernels_per_step()
+    sim.solve_timing_arm(a.steps)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    with Clocks(local) as clk:
+        barrier()
+        sim.synchronize()
+        sim.mark(0)
+        sim.update(a.steps)
+        sim.mark(1)
+        ms = sim.elapsed_ms(0, 1)
+        barrier()
+    clocks = clk.summary()
+    st1 = sim.stats()
+    launches, solve_ms, row_iters, row_setups = sim.solve_timing_read()
+    iters = st1.total_solve_steps - st0.total_solve_steps
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    steps_per_s = a.steps / (ms / 1e3) * world
+    solve_bytes = row_iters * SOLVE_BYTES_PER_ROW_ITER + row_setups * SOLVE_BYTES_PER_ROW_SETUP
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (solve_bytes / launches) / ((solve_ms / launches) / 1e3) / 1e9 if launches and solve_ms > 0 else None
+    roofline = {"kernel": "k_solver (persistent CG)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                "solve_ms_per_step": solve_ms / max(launches, 1), "algorithmic_bytes_per_launch": solve_bytes / max(launches, 1)}
+
+    # e2e through the C ABI with pinned host buffers: upload, step, download every step
+    e2e = None
+    if not a.no_e2e:
+        import torch
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+        h = {k: pinned(s) for k, s in (("vel", (n, n, n, 3)), ("rho", (n, n, n)), ("gamma", (n, n, n)),
+                                        ("boundary", (n, n, n)), ("forces", (n, n, n, 3)), ("beta", (n, n, n)),
+                                        ("div", (n, n, n)), ("p", (n, n, n)))}
+        sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+        h["boundary"][...] = b
+        h["forces"][...] = 0
+        k_e2e = max(2, a.steps // 2)
+        sim.synchronize()
+        barrier()
+        sim.mark(2)
+        for _ in range(k_e2e):
+            sim.upload_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"])
+            sim.update(1)
+            sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+        sim.mark(3)
+        ms_e2e = sim.elapsed_ms(2, 3)
+        barrier()
+        e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
+               "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e,
+               "api": "efs_upload_fields(vel,rho,gamma,boundary,forces) + efs_step + efs_download_fields(vel,rho,gamma,beta,div,p)"}
+    st2 = sim.stats()
+    sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cg_mean = iters / a.steps if a.steps else CG_ITERS_PER_STEP_REF
+        cs = cpu_sample(a, prm, cg_mean if prm.solver == abi.SOLVER_CG else prm.max_steps // 2)
+        cpu = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(a),
+                "cell_updates_per_s": steps_per_s * (n - 2) ** 3, "cg_iters_per_step": iters / max(a.steps, 1),
+                "solve_converged": bool(st1.converged), "paused": bool(st2.paused), "active_rows": st1.active_cells,
+                "gpu_launches": kernels * a.steps, "kernels_per_step": kernels,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,528 @@
+// efs_api.cu — the C ABI of include/efs_gb300.h.
+//
+// A context owns its device buffers, one non-blocking stream and one instantiated CUDA graph per step
+// configuration (enabled stages, solver, CG variant).  efs_step replays that graph; the pressure solve
+// inside it is a single cooperative kernel, so a step never waits on the host.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "efs_internal.h"
+#include "../../include/efs_scene.h"
+
+using efs::DevCtl;
+
+namespace {
+
+std::string g_create_error;
+
+int fail(efs_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg; else g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(efs_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, EFS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_fail(c, e_, what); } while (0)
+
+bool params_valid(const efs_params* p, std::string& why) {
+    if (!p) { why = "params is NULL"; return false; }
+    if (!std::isfinite(p->dt) || !std::isfinite(p->gravity_force)) { why = "dt and gravity_force must be finite"; return false; }
+    if (p->solver != EFS_SOLVER_JACOBI && p->solver != EFS_SOLVER_CG) { why = "unknown solver"; return false; }
+    if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE) { why = "unknown cg_variant"; return false; }
+    if (p->sharpen_mode != EFS_SHARPEN_PARALLEL) { why = "unknown sharpen_mode"; return false; }
+    if (p->max_steps < 0) { why = "max_steps must be >= 0"; return false; }
+    if (p->disable_mask & ~EFS_STAGES_ALL) { why = "disable_mask has bits beyond the seven stages"; return false; }
+    return true;
+}
+
+void drop_graphs(efs_ctx* c) {
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    c->timing_nodes_begin.clear();
+    c->timing_nodes_end.clear();
+    c->kernel_nodes.clear();
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T));
+}
+
+// The launch sequence of one ISimulator::update() (include/simulation/simulator/ISimulator.h:12-38).
+cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
+    const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
+    for (int s = 0; s < EFS_STAGE_COUNT; s++) {
+        if (!(stages & EFS_STAGE_BIT(s))) continue;
+        if (s == EFS_STAGE_ADD_FORCE && fuse) continue;   // applied inside vel_advect's averaging pass
+        cudaError_t e;
+        if (s == EFS_STAGE_PROJECT) {
+            if ((e = efs::launch_project_pre(c)) != cudaSuccess) return e;
+            if (timing_events && (e = cudaEventRecordWithFlags(c->ev_solve_begin, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
+            if ((e = efs::launch_solver(c)) != cudaSuccess) return e;
+            if (timing_events && (e = cudaEventRecordWithFlags(c->ev_solve_end, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
+            if ((e = efs::launch_project_post(c)) != cudaSuccess) return e;
+        } else {
+            if ((e = efs::launch_stage(c, s, s == EFS_STAGE_VEL_ADVECT && fuse)) != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
+int build_graph(efs_ctx* c, const efs::GraphKey& key, cudaGraphExec_t* out) {
+    auto it = c->graphs.find(key);
+    if (it != c->graphs.end()) { *out = it->second; return EFS_OK; }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaError_t le = enqueue_step(c, key.stages, true);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(c, le, "step capture"); }
+    if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+    // locate the two event-record nodes around the solver so their events can be swapped per replay
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) cudaGraphGetNodes(graph, nodes.data(), &n);
+    int kernels = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) continue;
+        if (t == cudaGraphNodeTypeKernel) kernels++;
+        if (t != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev;
+        if (cudaGraphEventRecordNodeGetEvent(nd, &ev) != cudaSuccess) continue;
+        if (ev == c->ev_solve_begin) c->timing_nodes_begin[key] = nd;
+        if (ev == c->ev_solve_end) c->timing_nodes_end[key] = nd;
+    }
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_fail(c, ie, "cudaGraphInstantiate");
+    c->graphs[key] = exec;
+    c->kernel_nodes[key] = kernels;
+    *out = exec;
+    return EFS_OK;
+}
+
+int check_device_status(efs_ctx* c) {
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    CK(cudaMemcpy(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost), "read device status");
+    if (c->ctl_host->error) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device status word %d (1 barrier timeout, 2 boundary not 0/1, 4 list overflow)",
+                      c->ctl_host->error);
+        const int err = c->ctl_host->error;
+        int zero = 0;
+        cudaMemcpy(&c->ctl->error, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(c, err == efs::DEV_ERR_BAD_BOUNDARY ? EFS_ERR_ARG : EFS_ERR_DEVICE_FAULT, buf);
+    }
+    return EFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void efs_params_default(efs_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 0.0167f;
+    p->gravity_force = 10.f;
+    p->gravity_enabled = 1;
+    p->vel_decay = 0.8f;
+    p->lambda_minus = .5f;
+    p->lambda_plus = .1f;
+    p->eta = 1.f;
+    p->liquid_threshold = 0.5f;
+    p->rho_d = 3.f;
+    p->solver = EFS_SOLVER_CG;
+    p->max_steps = 2000;
+    p->solver_threshold = 1e-5f;
+    p->tol_rel = 0.f;
+    p->disable_mask = 0;
+    p->re_calc_div = 0;
+    p->sharpen_mode = EFS_SHARPEN_PARALLEL;
+    p->cg_variant = EFS_CG_MIXED;
+}
+
+void efs_params_dam(efs_params* p, float cell_size, float dt, int solver, float tol_rel) {
+    if (!p) return;
+    efs_params_default(p);
+    p->dt = dt;
+    p->gravity_force = 9.81f / cell_size;
+    p->lambda_minus = 50.f;
+    p->lambda_plus = 10.f;
+    p->eta = 100.f;
+    p->rho_d = 32.f;
+    p->solver = solver;
+    p->tol_rel = tol_rel;
+    p->disable_mask = EFS_STAGE_BIT(EFS_STAGE_VEL_DECAY);
+}
+
+int efs_abi_version(void) { return EFS_ABI_VERSION; }
+
+int efs_device_count(int* count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (count) *count = (e == cudaSuccess) ? n : 0;
+    return (e == cudaSuccess || e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? EFS_OK : EFS_ERR_CUDA;
+}
+
+const char* efs_last_error(const efs_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+void efs_destroy(efs_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->div, c->p, c->fx, c->fy, c->fz, c->solid,
+                    c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
+                    c->sh_idx, c->sh_val, c->sh_end, c->rowinfo, c->chunk_flag, c->chunk_list, c->block_count,
+                    c->r, c->d0, c->d1, c->e, c->p64, c->partials, c->ctl, c->mass_partials};
+    for (void* b : bufs) if (b) cudaFree(b);
+    if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    for (auto ev : c->ev_begin) cudaEventDestroy(ev);
+    for (auto ev : c->ev_end) cudaEventDestroy(ev);
+    for (auto ev : c->marks) if (ev) cudaEventDestroy(ev);
+    if (c->ev_solve_begin) cudaEventDestroy(c->ev_solve_begin);
+    if (c->ev_solve_end) cudaEventDestroy(c->ev_solve_end);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int efs_create(int dim, int width, int height, int depth, const efs_params* params, efs_ctx** out) {
+    if (!out) return fail(nullptr, EFS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return fail(nullptr, EFS_ERR_ARG, "dim must be 2 or 3");
+    if (dim == 2 && depth != 1) return fail(nullptr, EFS_ERR_ARG, "2D grids have depth 1");
+    if (width < 4 || height < 4 || (dim == 3 && depth < 4)) return fail(nullptr, EFS_ERR_ARG, "grid sides must be >= 4 (border included)");
+    const long long n = (long long)width * height * depth;
+    if (n >= (1LL << 31) / 8) return fail(nullptr, EFS_ERR_ARG, "grid too large for 32-bit cell indexing of 8-slot weights");
+    std::string why;
+    efs_params prm;
+    if (params) prm = *params; else efs_params_default(&prm);
+    if (!params_valid(&prm, why)) return fail(nullptr, EFS_ERR_ARG, why);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, EFS_ERR_NO_DEVICE, "no CUDA device visible");
+
+    efs_ctx* c = new efs_ctx();
+    c->dim = dim;
+    c->g.W = width; c->g.H = height; c->g.D = depth;
+    c->g.WH = width * height;
+    c->g.N = (int)n;
+    c->prm = prm;
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    const size_t N = (size_t)n;
+    const int K = (dim == 3) ? 8 : 4;
+    const int nchunks = (int)((N + 31) / 32);
+    auto bail = [&](cudaError_t e, const char* what) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+        efs_destroy(c);
+        return EFS_ERR_CUDA;
+    };
+    cudaError_t e;
+#define ALLOC(ptr, cnt) if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    ALLOC(c->u, N); ALLOC(c->v, N); ALLOC(c->w, N);
+    ALLOC(c->rho, N); ALLOC(c->gamma, N); ALLOC(c->beta, N); ALLOC(c->div, N); ALLOC(c->p, N);
+    ALLOC(c->fx, N); ALLOC(c->fy, N); ALLOC(c->fz, N); ALLOC(c->solid, N);
+    ALLOC(c->tvel, 3 * N); ALLOC(c->validA, N); ALLOC(c->validB, N);
+    ALLOC(c->wb, K * N); ALLOC(c->wf, K * N); ALLOC(c->bb, N); ALLOC(c->fb, N);
+    ALLOC(c->bsum, N); ALLOC(c->gsum, N); ALLOC(c->rho_acc, N);
+    ALLOC(c->sh_idx, N); ALLOC(c->sh_val, N); ALLOC(c->sh_end, 3 * N);
+    ALLOC(c->rowinfo, N); ALLOC(c->chunk_flag, nchunks); ALLOC(c->chunk_list, nchunks);
+    ALLOC(c->r, N); ALLOC(c->d0, N); ALLOC(c->d1, N); ALLOC(c->e, N); ALLOC(c->p64, N);
+    ALLOC(c->ctl, 1);
+    ALLOC(c->mass_partials, 256);
+#undef ALLOC
+    if ((e = efs::solver_configure(c)) != cudaSuccess) return bail(e, "solver occupancy");
+    if ((e = dalloc(&c->block_count, c->solver_blocks)) != cudaSuccess) return bail(e, "cudaMalloc block_count");
+    if ((e = dalloc(&c->partials, 6 * (size_t)c->solver_blocks)) != cudaSuccess) return bail(e, "cudaMalloc partials");
+    if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->ctl_host), sizeof(DevCtl))) != cudaSuccess) return bail(e, "cudaMallocHost");
+    if ((e = cudaEventCreate(&c->ev_solve_begin)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&c->ev_solve_end)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
+    if ((e = cudaMemsetAsync(c->validB, 0, N, c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
+    if ((e = cudaMemsetAsync(c->r, 0, N * sizeof(float), c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
+    if ((e = cudaMemsetAsync(c->e, 0, N * sizeof(float), c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
+    if ((e = efs::launch_reset_fields(c)) != cudaSuccess) return bail(e, "reset");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(e, "cudaStreamSynchronize");
+    *out = c;
+    return EFS_OK;
+}
+
+int efs_set_params(efs_ctx* c, const efs_params* p) {
+    if (!c) return EFS_ERR_ARG;
+    std::string why;
+    if (!params_valid(p, why)) return fail(c, EFS_ERR_ARG, why);
+    if (std::memcmp(&c->prm, p, sizeof(efs_params)) != 0) {
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+        drop_graphs(c);
+        c->prm = *p;
+    }
+    return EFS_OK;
+}
+
+int efs_get_params(const efs_ctx* c, efs_params* p) {
+    if (!c || !p) return EFS_ERR_ARG;
+    *p = c->prm;
+    return EFS_OK;
+}
+
+int efs_upload_field(efs_ctx* c, int field, const float* host) {
+    if (!c) return EFS_ERR_ARG;
+    if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
+    const size_t N = (size_t)c->g.N, bytes = N * sizeof(float);
+    switch (field) {
+        case EFS_FIELD_VEL:
+        case EFS_FIELD_FORCES: {
+            CK(cudaMemcpyAsync(c->tvel, host, bytes * c->dim, cudaMemcpyHostToDevice, c->stream), "upload");
+            if (field == EFS_FIELD_VEL) { CK(efs::launch_upload_vec(c, c->tvel, c->u, c->v, c->w), "split"); }
+            else { CK(efs::launch_upload_vec(c, c->tvel, c->fx, c->fy, c->fz), "split"); c->has_forces = true; }
+            break;
+        }
+        case EFS_FIELD_BOUNDARY:
+            CK(cudaMemcpyAsync(c->tvel, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload");
+            CK(efs::launch_boundary_to_solid(c, c->tvel), "boundary");
+            break;
+        case EFS_FIELD_RHO: CK(cudaMemcpyAsync(c->rho, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
+        case EFS_FIELD_GAMMA: CK(cudaMemcpyAsync(c->gamma, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
+        case EFS_FIELD_BETA: CK(cudaMemcpyAsync(c->beta, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
+        case EFS_FIELD_DIVERGENCE: CK(cudaMemcpyAsync(c->div, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
+        case EFS_FIELD_PRESSURE: CK(cudaMemcpyAsync(c->p, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
+        default: return fail(c, EFS_ERR_ARG, "unknown field");
+    }
+    if (field == EFS_FIELD_BOUNDARY) return check_device_status(c);
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_download_field(efs_ctx* c, int field, float* host) {
+    if (!c) return EFS_ERR_ARG;
+    if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
+    const size_t N = (size_t)c->g.N, bytes = N * sizeof(float);
+    switch (field) {
+        case EFS_FIELD_VEL:
+            CK(efs::launch_download_vec(c, c->tvel, c->u, c->v, c->w), "interleave");
+            CK(cudaMemcpyAsync(host, c->tvel, bytes * c->dim, cudaMemcpyDeviceToHost, c->stream), "download");
+            break;
+        case EFS_FIELD_FORCES:
+            CK(efs::launch_download_vec(c, c->tvel, c->fx, c->fy, c->fz), "interleave");
+            CK(cudaMemcpyAsync(host, c->tvel, bytes * c->dim, cudaMemcpyDeviceToHost, c->stream), "download");
+            break;
+        case EFS_FIELD_BOUNDARY:
+            CK(efs::launch_solid_to_boundary(c, c->tvel), "boundary");
+            CK(cudaMemcpyAsync(host, c->tvel, bytes, cudaMemcpyDeviceToHost, c->stream), "download");
+            break;
+        case EFS_FIELD_RHO: CK(cudaMemcpyAsync(host, c->rho, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
+        case EFS_FIELD_GAMMA: CK(cudaMemcpyAsync(host, c->gamma, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
+        case EFS_FIELD_BETA: CK(cudaMemcpyAsync(host, c->beta, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
+        case EFS_FIELD_DIVERGENCE: CK(cudaMemcpyAsync(host, c->div, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
+        case EFS_FIELD_PRESSURE: CK(cudaMemcpyAsync(host, c->p, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
+        default: return fail(c, EFS_ERR_ARG, "unknown field");
+    }
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_upload_fields(efs_ctx* c, const float* vel, const float* rho, const float* gamma, const float* boundary,
+                      const float* forces) {
+    if (!c) return EFS_ERR_ARG;
+    int s;
+    if (boundary && (s = efs_upload_field(c, EFS_FIELD_BOUNDARY, boundary)) != EFS_OK) return s;
+    if (vel && (s = efs_upload_field(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
+    if (rho && (s = efs_upload_field(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
+    if (gamma && (s = efs_upload_field(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
+    if (forces && (s = efs_upload_field(c, EFS_FIELD_FORCES, forces)) != EFS_OK) return s;
+    return EFS_OK;
+}
+
+int efs_download_fields(efs_ctx* c, float* vel, float* rho, float* gamma, float* beta, float* divergence,
+                        float* pressure) {
+    if (!c) return EFS_ERR_ARG;
+    int s;
+    if (vel && (s = efs_download_field(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
+    if (rho && (s = efs_download_field(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
+    if (gamma && (s = efs_download_field(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
+    if (beta && (s = efs_download_field(c, EFS_FIELD_BETA, beta)) != EFS_OK) return s;
+    if (divergence && (s = efs_download_field(c, EFS_FIELD_DIVERGENCE, divergence)) != EFS_OK) return s;
+    if (pressure && (s = efs_download_field(c, EFS_FIELD_PRESSURE, pressure)) != EFS_OK) return s;
+    return EFS_OK;
+}
+
+int efs_reset_fields(efs_ctx* c) {
+    if (!c) return EFS_ERR_ARG;
+    CK(efs::launch_reset_fields(c), "reset");
+    c->has_forces = false;
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_stage(efs_ctx* c, int stage) {
+    if (!c) return EFS_ERR_ARG;
+    if (stage < 0 || stage >= EFS_STAGE_COUNT) return fail(c, EFS_ERR_ARG, "unknown stage");
+    CK(efs::launch_stage(c, stage, false), "stage launch");
+    return EFS_OK;
+}
+
+int efs_step(efs_ctx* c, int n_steps) {
+    if (!c) return EFS_ERR_ARG;
+    if (n_steps < 0) return fail(c, EFS_ERR_ARG, "n_steps < 0");
+    if (n_steps == 0) return EFS_OK;
+    efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
+    cudaGraphExec_t exec = nullptr;
+    int s = build_graph(c, key, &exec);
+    if (s != EFS_OK) return s;
+    auto nb = c->timing_nodes_begin.find(key), ne = c->timing_nodes_end.find(key);
+    const bool can_time = nb != c->timing_nodes_begin.end() && ne != c->timing_nodes_end.end();
+    for (int k = 0; k < n_steps; k++) {
+        if (can_time && c->ev_used < (int)c->ev_begin.size()) {
+            CK(cudaGraphExecEventRecordNodeSetEvent(exec, nb->second, c->ev_begin[c->ev_used]), "timing event");
+            CK(cudaGraphExecEventRecordNodeSetEvent(exec, ne->second, c->ev_end[c->ev_used]), "timing event");
+            c->ev_used++;
+        } else if (can_time && !c->ev_begin.empty()) {
+            CK(cudaGraphExecEventRecordNodeSetEvent(exec, nb->second, c->ev_solve_begin), "timing event");
+            CK(cudaGraphExecEventRecordNodeSetEvent(exec, ne->second, c->ev_solve_end), "timing event");
+        }
+        CK(cudaGraphLaunch(exec, c->stream), "cudaGraphLaunch");
+    }
+    c->frames += n_steps;
+    return EFS_OK;
+}
+
+int efs_step_kernel_count(efs_ctx* c, int* count) {
+    if (!c || !count) return EFS_ERR_ARG;
+    efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
+    cudaGraphExec_t exec = nullptr;
+    int s = build_graph(c, key, &exec);
+    if (s != EFS_OK) return s;
+    *count = c->kernel_nodes[key];
+    return EFS_OK;
+}
+
+int efs_solve(efs_ctx* c, efs_stats* out) {
+    if (!c) return EFS_ERR_ARG;
+    CK(efs::launch_solver_prep(c), "solver prep");
+    CK(efs::launch_solver(c), "solver launch");
+    int s = efs_get_stats(c, out);
+    if (s != EFS_OK) return s;
+    if (!c->ctl_host->converged) return fail(c, EFS_ERR_NOT_CONVERGED, "pressure solve reached max_steps");
+    return EFS_OK;
+}
+
+int efs_synchronize(efs_ctx* c) {
+    if (!c) return EFS_ERR_ARG;
+    return check_device_status(c);
+}
+
+int efs_get_stats(efs_ctx* c, efs_stats* out) {
+    if (!c) return EFS_ERR_ARG;
+    int s = check_device_status(c);
+    if (s != EFS_OK) return s;
+    if (out) {
+        const DevCtl& h = *c->ctl_host;
+        std::memset(out, 0, sizeof(*out));
+        out->frames = c->frames;
+        out->solve_steps = h.iterations;
+        out->converged = h.converged;
+        out->paused = h.paused;
+        out->device_error = h.error;
+        out->rr = h.rr;
+        out->bb = h.bb;
+        out->threshold = h.thr;
+        out->active_cells = h.active_cells;
+        out->total_solve_steps = h.total_iterations;
+        out->solves = h.solves;
+    }
+    return EFS_OK;
+}
+
+int efs_total_mass(efs_ctx* c, double* out) {
+    if (!c || !out) return EFS_ERR_ARG;
+    CK(efs::launch_mass(c, c->mass_partials), "mass");
+    double part[256];
+    CK(cudaMemcpyAsync(part, c->mass_partials, sizeof part, cudaMemcpyDeviceToHost, c->stream), "mass readback");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    double s = 0;
+    for (double v : part) s += v;
+    *out = s;
+    return EFS_OK;
+}
+
+int efs_solve_timing_arm(efs_ctx* c, int capacity) {
+    if (!c || capacity < 0) return EFS_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    for (auto ev : c->ev_begin) cudaEventDestroy(ev);
+    for (auto ev : c->ev_end) cudaEventDestroy(ev);
+    c->ev_begin.clear();
+    c->ev_end.clear();
+    c->ev_used = 0;
+    for (int k = 0; k < capacity; k++) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a), "cudaEventCreate");
+        CK(cudaEventCreate(&b), "cudaEventCreate");
+        c->ev_begin.push_back(a);
+        c->ev_end.push_back(b);
+    }
+    // work counters restart with the pool
+    CK(cudaMemset(&c->ctl->sum_iter_rows, 0, 2 * sizeof(double)), "cudaMemset");
+    return EFS_OK;
+}
+
+int efs_solve_timing_read(efs_ctx* c, int* launches, double* total_ms, double* row_iterations,
+                          double* row_setups) {
+    if (!c) return EFS_ERR_ARG;
+    int s = check_device_status(c);
+    if (s != EFS_OK) return s;
+    double ms = 0;
+    for (int k = 0; k < c->ev_used; k++) {
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, c->ev_begin[k], c->ev_end[k]), "cudaEventElapsedTime");
+        ms += t;
+    }
+    if (launches) *launches = c->ev_used;
+    if (total_ms) *total_ms = ms;
+    if (row_iterations) *row_iterations = c->ctl_host->sum_iter_rows;
+    if (row_setups) *row_setups = c->ctl_host->sum_rows;
+    return EFS_OK;
+}
+
+int efs_timer_mark(efs_ctx* c, int slot) {
+    if (!c || slot < 0 || slot >= 8) return EFS_ERR_ARG;
+    if (!c->marks[slot]) CK(cudaEventCreate(&c->marks[slot]), "cudaEventCreate");
+    CK(cudaEventRecord(c->marks[slot], c->stream), "cudaEventRecord");
+    return EFS_OK;
+}
+
+int efs_timer_elapsed(efs_ctx* c, int a, int b, double* ms) {
+    if (!c || !ms || a < 0 || a >= 8 || b < 0 || b >= 8 || !c->marks[a] || !c->marks[b]) return EFS_ERR_ARG;
+    CK(cudaEventSynchronize(c->marks[b]), "cudaEventSynchronize");
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, c->marks[a], c->marks[b]), "cudaEventElapsedTime");
+    *ms = t;
+    return EFS_OK;
+}
+
+int efs_scene_dam3d(int w, int h, int d, int n_min, int n_max, uint64_t seed, float* boundary, float* rho) {
+    if (!boundary || !rho) return EFS_ERR_ARG;
+    return efs_scene_dam3d_fill(w, h, d, n_min, n_max, seed, boundary, rho) < 0 ? EFS_ERR_ARG : EFS_OK;
+}
+
+int efs_scene_dam2d(int w, int h, float* boundary, float* rho) {
+    if (!boundary || !rho) return EFS_ERR_ARG;
+    return efs_scene_dam2d_fill(w, h, boundary, rho) < 0 ? EFS_ERR_ARG : EFS_OK;
+}
+
+int efs_scene_batch2d(uint64_t seed, int* side, float* boundary, float* rho, int capacity) {
+    int s = 0;
+    efs_scene_batch2d_fill(seed, &s, nullptr, nullptr);
+    if (side) *side = s;
+    if (!boundary || !rho) return EFS_OK;
+    if (capacity < s * s) return EFS_ERR_ARG;
+    return efs_scene_batch2d_fill(seed, &s, boundary, rho) < 0 ? EFS_ERR_ARG : EFS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// efs_internal.h — the context behind the C ABI and the launch entry points shared by the translation units.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/efs_gb300.h"
+#include "efs_device.cuh"
+
+namespace efs {
+
+// Device error bits (efs_stats.device_error).
+enum DeviceError : int {
+    DEV_ERR_BARRIER_TIMEOUT = 1,   // a grid barrier of the persistent solver gave up waiting
+    DEV_ERR_BAD_BOUNDARY = 2,      // an uploaded boundary value was neither 0.0 nor 1.0
+    DEV_ERR_LIST_OVERFLOW = 4      // a compaction list exceeded its capacity
+};
+
+// Control block in device memory: grid barrier, solve results and counters.  Mirrored into pinned host
+// memory by efs_get_stats.
+struct DevCtl {
+    unsigned bar_count;        // grid barrier arrivals (reset before every solver launch)
+    int bar_abort;             // set when a barrier of the current launch gave up (reset before every launch)
+    unsigned bar_gen;          // grid barrier generation
+    int error;
+    int converged;
+    int iterations;
+    int paused;
+    int active_chunks;
+    int sh_count;              // density-sharpen active-cell count
+    long long active_cells;
+    long long total_iterations;
+    long long solves;
+    double rr, bb, thr;
+    double sum_iter_rows;      // sum over solves of iterations x matrix rows (since the timing pool was armed)
+    double sum_rows;           // sum over solves of matrix rows
+};
+
+// Arguments of the persistent pressure solver (efs_solver.cu).
+struct SolverArgs {
+    Geo g;
+    int dim;
+    int solver;                // efs_solver
+    int cg_variant;            // efs_cg_variant
+    int max_steps;
+    float tol_rel;
+    float solver_threshold;
+    int n_chunks;              // ceil(N / 32)
+    const float* b;            // divergence (right-hand side)
+    const uint16_t* rowinfo;   // per cell: bit 15 matrix row; bits 0-5 summed neighbours; bits 8-10 count
+    const uint8_t* chunk_flag; // per 32-cell chunk: 1 if it holds a matrix row or a non-zero b
+    int* chunk_list;           // compacted active chunks (capacity n_chunks)
+    int* block_count;          // per block: active chunks in its static range
+    float* p;                  // pressure (FP32 field)
+    double* p64;               // FP64 pressure accumulator (EFS_CG_MIXED)
+    float* e;                  // FP32 increment since the last fold (EFS_CG_MIXED) / Jacobi ping-pong buffer
+    float* r;
+    float* d0;
+    float* d1;
+    double* partials;          // 2 slots x 3 values per block
+    DevCtl* ctl;
+};
+
+struct GraphKey {
+    unsigned stages;
+    int solver, cg_variant;
+    bool operator<(const GraphKey& o) const {
+        if (stages != o.stages) return stages < o.stages;
+        if (solver != o.solver) return solver < o.solver;
+        return cg_variant < o.cg_variant;
+    }
+};
+
+}  // namespace efs
+
+struct efs_ctx {
+    int dim = 3;
+    efs::Geo g{};
+    efs_params prm{};
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+
+    // fields (SoA)
+    float *u = nullptr, *v = nullptr, *w = nullptr;
+    float *rho = nullptr, *gamma = nullptr, *beta = nullptr, *div = nullptr, *p = nullptr;
+    float *fx = nullptr, *fy = nullptr, *fz = nullptr;
+    uint8_t* solid = nullptr;
+    bool has_forces = false;
+
+    // temporaries
+    float* tvel = nullptr;                  // 3N: vel_advect / extrapolation ping-pong and host staging
+    uint8_t *validA = nullptr, *validB = nullptr;
+    float *wb = nullptr, *wf = nullptr;     // advection weights, slot-major (k * N + i)
+    int *bb = nullptr, *fb = nullptr;       // advection base cell (-1: no entries)
+    float *bsum = nullptr, *gsum = nullptr, *rho_acc = nullptr;
+    int* sh_idx = nullptr;                  // density-sharpen active cells
+    float* sh_val = nullptr;
+    float* sh_end = nullptr;                // 3 per active cell
+
+    // solver
+    uint16_t* rowinfo = nullptr;
+    uint8_t* chunk_flag = nullptr;
+    int* chunk_list = nullptr;
+    int* block_count = nullptr;
+    float *r = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr;
+    double* p64 = nullptr;
+    double* partials = nullptr;
+    int solver_blocks = 0;
+    int solver_threads = 0;
+
+    double* mass_partials = nullptr;
+    efs::DevCtl* ctl = nullptr;
+    efs::DevCtl* ctl_host = nullptr;        // pinned
+
+    std::map<efs::GraphKey, cudaGraphExec_t> graphs;
+    std::map<efs::GraphKey, cudaGraphNode_t> timing_nodes_begin, timing_nodes_end;
+    std::map<efs::GraphKey, int> kernel_nodes;
+
+    // solve timing pool
+    std::vector<cudaEvent_t> ev_begin, ev_end;
+    int ev_used = 0;
+    cudaEvent_t ev_solve_begin = nullptr, ev_solve_end = nullptr;   // recorded inside the graph
+
+    cudaEvent_t marks[8] = {};
+    int64_t frames = 0;
+    std::string err;
+};
+
+namespace efs {
+// efs_stages.cu
+cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force);
+cudaError_t launch_project_pre(efs_ctx* c);
+cudaError_t launch_project_post(efs_ctx* c);
+cudaError_t launch_solver_prep(efs_ctx* c);
+// efs_solver.cu
+cudaError_t solver_configure(efs_ctx* c);
+cudaError_t launch_solver(efs_ctx* c);
+// efs_fields.cu
+cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc);
+cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc);
+cudaError_t launch_boundary_to_solid(efs_ctx* c, const float* staged);
+cudaError_t launch_solid_to_boundary(efs_ctx* c, float* staged);
+cudaError_t launch_reset_fields(efs_ctx* c);
+cudaError_t launch_mass(efs_ctx* c, double* out_dev);
+}  // namespace efs

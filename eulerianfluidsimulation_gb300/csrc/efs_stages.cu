@@ -1,0 +1,951 @@
+// efs_stages.cu — the seven stages of the liquid step as sm_103a kernels (3D and 2D).
+//
+// Each kernel restates one loop of the reference CPU backend (src/simulation/simulator/CPUSimulator3D.cpp,
+// CPUSimulator2D.cpp); the comments give the lines.  Where the reference loop is order dependent the kernels
+// keep its result:
+//   - density diffusion sweeps are in place along one axis; rows along that axis are independent, so one
+//     thread walks one row sequentially (CPUSimulator3D.cpp:276-363);
+//   - the Chentanez-Mueller matrix A is stored as 8 backward weights per row plus 8 forward weights per
+//     column (no hash map); row and column sums that the reference forms by iterating over A become passes
+//     over those weights with atomic adds for the scattered part.
+// Density sharpening applies every cell's change, then traces every changed cell on that field, then
+// scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell.
+#include "efs_internal.h"
+
+namespace efs {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+__device__ __forceinline__ bool cell3(const Geo& g, int& x, int& y, int& z, int& i) {
+    x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    z = 1 + blockIdx.z;
+    if (x > g.W - 2 || y > g.H - 2) return false;
+    i = z * g.WH + y * g.W + x;
+    return true;
+}
+__device__ __forceinline__ bool cell2(const Geo& g, int& x, int& y, int& i) {
+    x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (x > g.W - 2 || y > g.H - 2) return false;
+    i = y * g.W + x;
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 0: vel_decay (CPUSimulator3D.cpp:54-59, CPUSimulator2D.cpp:65-70)
+// ------------------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_vel_decay(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                            const float* __restrict__ rho, float k) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if ((double)rho[i] < 0.5) {
+        u[i] *= k; v[i] *= k;
+        if (DIM == 3) w[i] *= k;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 1: vel_extrapolate (CPUSimulator3D.cpp:61-111, CPUSimulator2D.cpp:72-120)
+// ------------------------------------------------------------------------------------------------
+__global__ void k_extrap_init(Geo g, int dim, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                              uint8_t* __restrict__ valid) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    const int x = i % g.W, y = (i / g.W) % g.H, z = i / g.WH;
+    bool interior = x >= 1 && x <= g.W - 2 && y >= 1 && y <= g.H - 2;
+    if (dim == 3) interior = interior && z >= 1 && z <= g.D - 2;
+    valid[i] = (interior && rho[i] >= 0.5f && solid[i] == 0) ? 1 : 0;
+}
+
+template <int DIM>
+__global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* __restrict__ sv,
+                              const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du,
+                              float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV,
+                              const uint8_t* __restrict__ solid) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (solid[i]) {
+        du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
+        dV[i] = 0;
+        return;
+    }
+    if (sV[i]) {
+        du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
+        dV[i] = 1;
+        return;
+    }
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, n = 0;
+    const int nb[6] = {i - 1, i + 1, i - g.W, i + g.W, i - g.WH, i + g.WH};
+#pragma unroll
+    for (int k = 0; k < 2 * DIM; k++) {
+        const int j = nb[k];
+        if (sV[j]) {
+            s0 += su[j]; s1 += sv[j];
+            if (DIM == 3) s2 += sw[j];
+            n++;
+        }
+    }
+    if (n > 0) {
+        du[i] = s0 / n; dv[i] = s1 / n; if (DIM == 3) dw[i] = s2 / n;
+    } else {
+        du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
+    }
+    dV[i] = (n > 0) ? 1 : 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 2: rho_sharpen (CPUSimulator3D.cpp:366-456 with trace_along_field :568-607 and scatter_values
+// :609-655; 2D CPUSimulator2D.cpp:320-402, :526-595)
+// ------------------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_sharpen_calc(Geo g, const float* __restrict__ rho, float delT, int* __restrict__ idx,
+                               float* __restrict__ val, DevCtl* ctl, int cap) {
+    int x, y, z = 0, i;
+    bool ok;
+    if (DIM == 3) ok = cell3(g, x, y, z, i); else ok = cell2(g, x, y, i);
+    float dr = 0.f;
+    if (ok) {
+        const float r = rho[i];
+        const float rxm = rho[i - 1], rxp = rho[i + 1], rym = rho[i - g.W], ryp = rho[i + g.W];
+        const float dpx = -(r - rxm) * delT, dmx = -(rxp - r) * delT;
+        const float dpy = -(r - rym) * delT, dmy = -(ryp - r) * delT;
+        double inc = maxd(sq_d(maxf(dpx, 0.f)), sq_d(minf(dmx, 0.f))) + maxd(sq_d(maxf(dpy, 0.f)), sq_d(minf(dmy, 0.f)));
+        double dec = maxd(sq_d(minf(dpx, 0.f)), sq_d(maxf(dmx, 0.f))) + maxd(sq_d(minf(dpy, 0.f)), sq_d(maxf(dmy, 0.f)));
+        float mx = -INFINITY;
+        mx = maxf(mx, fabsf(r - rxm)); mx = maxf(mx, fabsf(r - rxp));
+        mx = maxf(mx, fabsf(r - rym)); mx = maxf(mx, fabsf(r - ryp));
+        if (DIM == 3) {
+            const float rzm = rho[i - g.WH], rzp = rho[i + g.WH];
+            const float dpz = -(r - rzm) * delT, dmz = -(rzp - r) * delT;
+            inc = inc + maxd(sq_d(maxf(dpz, 0.f)), sq_d(minf(dmz, 0.f)));
+            dec = dec + maxd(sq_d(minf(dpz, 0.f)), sq_d(maxf(dmz, 0.f)));
+            mx = maxf(mx, fabsf(r - rzm)); mx = maxf(mx, fabsf(r - rzp));
+        }
+        const float max_inc = (float)sqrt(inc), max_dec = (float)sqrt(dec);
+        const float wgt = cube_f(r - 0.5f) * (1 - minf(1.f, mx / 0.2f));
+        dr = (wgt >= 0) ? wgt * max_inc : wgt * max_dec;
+        if (r + dr < 0 || (double)r < 1e-5) dr = -r;
+        else if (r > 0.5f) dr = 0;
+    }
+    const bool active = ok && !(fabsf(dr) < 1e-6f);
+    // warp-aggregated append
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (mask == 0) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(mask) - 1) base = atomicAdd(&ctl->sh_count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (active) {
+        const int slot = base + __popc(mask & ((1u << lane) - 1u));
+        if (slot < cap) { idx[slot] = i; val[slot] = dr; }
+        else atomicOr(&ctl->error, DEV_ERR_LIST_OVERFLOW);
+    }
+}
+
+__global__ void k_sharpen_apply(float* __restrict__ rho, const int* __restrict__ idx, const float* __restrict__ val,
+                                const DevCtl* ctl, int cap) {
+    const int n = min(ctl->sh_count, cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int i = idx[s];
+        float r = rho[i] + val[s];
+        rho[i] = maxf(r, 0.f);
+    }
+}
+
+template <int DIM>
+__global__ void k_sharpen_trace(Geo g, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                                const int* __restrict__ idx, float* __restrict__ ends, float Dist,
+                                const DevCtl* ctl, int cap) {
+    const int n = min(ctl->sh_count, cap);
+    const float stepSize = Dist / (float)10;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int i = idx[s];
+        float px = (float)(i % g.W), py = (float)((i / g.W) % g.H), pz = (float)(i / g.WH);
+        for (int st = 0; st < 10; st++) {
+            const float sv = (DIM == 3) ? sinterp3(rho, g, px, py, pz) : sinterp2(rho, g, px, py);
+            if (sv >= 0.5f) break;
+            const int ix = clampi((int)px, 1, g.W - 2), iy = clampi((int)py, 1, g.H - 2);
+            const int iz = (DIM == 3) ? clampi((int)pz, 1, g.D - 2) : 0;
+            const int c = iz * g.WH + iy * g.W + ix;
+            const float gx = rho[c + 1] - rho[c - 1];
+            const float gy = rho[c + g.W] - rho[c - g.W];
+            const float gz = (DIM == 3) ? rho[c + g.WH] - rho[c - g.WH] : 0.f;
+            const float len = (DIM == 3) ? sqrtf(gx * gx + gy * gy + gz * gz) : sqrtf(gx * gx + gy * gy);
+            if (len < 1e-6f) break;
+            float nx = px + (gx / len) * stepSize, ny = py + (gy / len) * stepSize;
+            nx = clampf(nx, 1.f, (float)g.W - 2.f);
+            ny = clampf(ny, 1.f, (float)g.H - 2.f);
+            float nz = pz;
+            if (DIM == 3) { nz = pz + (gz / len) * stepSize; nz = clampf(nz, 1.f, (float)g.D - 2.f); }
+            const int ci = (DIM == 3 ? (int)nz * g.WH : 0) + (int)ny * g.W + (int)nx;
+            if (solid[ci]) break;
+            px = nx; py = ny; pz = nz;
+        }
+        ends[3 * s] = px; ends[3 * s + 1] = py; ends[3 * s + 2] = pz;
+    }
+}
+
+template <int DIM>
+__global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                                  const float* __restrict__ val, const float* __restrict__ ends, const DevCtl* ctl,
+                                  int cap) {
+    const int n = min(ctl->sh_count, cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const float px = ends[3 * s], py = ends[3 * s + 1], pz = ends[3 * s + 2];
+        const float value = -val[s];
+        const int x0 = clampi((int)px, 0, g.W - 1), y0 = clampi((int)py, 0, g.H - 1);
+        const int x1 = clampi((int)px + 1, 0, g.W - 1), y1 = clampi((int)py + 1, 0, g.H - 1);
+        const float fx = px - (float)(int)px, fy = py - (float)(int)py;
+        if (DIM == 3) {
+            const int z0 = clampi((int)pz, 0, g.D - 1), z1 = clampi((int)pz + 1, 0, g.D - 1);
+            const float fz = pz - (float)(int)pz;
+            float w[8];
+            w[0] = (1.f - fx) * (1.f - fy) * (1.f - fz);
+            w[1] = fx * (1.f - fy) * (1.f - fz);
+            w[2] = (1.f - fx) * fy * (1.f - fz);
+            w[3] = fx * fy * (1.f - fz);
+            w[4] = (1.f - fx) * (1.f - fy) * fz;
+            w[5] = fx * (1.f - fy) * fz;
+            w[6] = (1.f - fx) * fy * fz;
+            w[7] = fx * fy * fz;
+            int c[8];
+            c[0] = z0 * g.WH + y0 * g.W + x0; c[1] = z0 * g.WH + y0 * g.W + x1;
+            c[2] = z0 * g.WH + y1 * g.W + x0; c[3] = z0 * g.WH + y1 * g.W + x1;
+            c[4] = z1 * g.WH + y0 * g.W + x0; c[5] = z1 * g.WH + y0 * g.W + x1;
+            c[6] = z1 * g.WH + y1 * g.W + x0; c[7] = z1 * g.WH + y1 * g.W + x1;
+#pragma unroll
+            for (int k = 0; k < 8; k++) if (solid[c[k]]) w[k] = 0.f;
+            const float total = w[0] + w[1] + w[2] + w[3] + w[4] + w[5] + w[6] + w[7];
+            if (total < 1e-6f) continue;
+            const float inv = 1.f / total;
+#pragma unroll
+            for (int k = 0; k < 8; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+        } else {
+            float w[4];
+            w[0] = (1.f - fx) * (1.f - fy); w[1] = fx * (1.f - fy); w[2] = (1.f - fx) * fy; w[3] = fx * fy;
+            const int c[4] = {y0 * g.W + x0, y0 * g.W + x1, y1 * g.W + x0, y1 * g.W + x1};
+#pragma unroll
+            for (int k = 0; k < 4; k++) if (solid[c[k]]) w[k] = 0.f;
+            const float total = w[0] + w[1] + w[2] + w[3];
+            if (total < 1e-6f) continue;
+            const float inv = 1.f / total;
+#pragma unroll
+            for (int k = 0; k < 4; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 3: rho_advect (CPUSimulator3D.cpp:113-364, CPUSimulator2D.cpp:122-318)
+// ------------------------------------------------------------------------------------------------
+
+// Steps 1-4: back-trace (shared by steps 1 and 2, which trace the same point), gamma' at the trace end,
+// backward weights m_k / sum / gamma', column sums beta1.
+template <int DIM>
+__global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                               const float* __restrict__ w, const uint8_t* __restrict__ solid,
+                               const float* __restrict__ gamma, float dt, float* __restrict__ wb,
+                               int* __restrict__ bb, float* __restrict__ bsum) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (solid[i]) { bb[i] = -1; return; }     // step 1 skips solids; step 2 finds no free corner for them
+    float px, py, pz = 0.f, gp;
+    float m[K];
+    int base;
+    float sum;
+    if (DIM == 3) {
+        trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, -dt, 4, px, py, pz);
+        gp = sinterp3(gamma, g, px, py, pz);
+        sum = corner_weights3(solid, g, px, py, pz, base, m);
+    } else {
+        trace2(u, v, solid, g, (float)x, (float)y, -dt, 4, px, py);
+        gp = sinterp2(gamma, g, px, py);
+        sum = corner_weights2(solid, g, px, py, base, m);
+    }
+    if (sum == 0) { bb[i] = -1; return; }
+    bb[i] = base;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float val = m[k] / sum;
+        if (gp > 1.e-5f) val /= gp;
+        wb[k * g.N + i] = val;
+        const int c = base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k));
+        atomicAdd(&bsum[c], val);
+    }
+}
+
+// Step 5: forward trace for beta_j < 1; forward weights (1 - beta_j) m_k / sum; their row sums into gsum.
+template <int DIM>
+__global__ void k_adv_forward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ w, const uint8_t* __restrict__ solid,
+                              const float* __restrict__ bsum, float dt, float* __restrict__ wf, int* __restrict__ fb,
+                              float* __restrict__ gsum) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    int x, y, z = 0, j;
+    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    const float beta = bsum[j];
+    if (beta >= 1) { fb[j] = -1; return; }
+    float px, py, pz = 0.f;
+    float m[K];
+    int base;
+    float sum;
+    if (DIM == 3) {
+        trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, +dt, 4, px, py, pz);
+        sum = corner_weights3(solid, g, px, py, pz, base, m);
+    } else {
+        trace2(u, v, solid, g, (float)x, (float)y, +dt, 4, px, py);
+        sum = corner_weights2(solid, g, px, py, base, m);
+    }
+    if (sum == 0) { fb[j] = -1; return; }
+    fb[j] = base;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float val = (1 - beta) * (m[k] / sum);
+        wf[k * g.N + j] = val;
+        atomicAdd(&gsum[base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k))], val);
+    }
+}
+
+// Steps 6-8 for the backward rows: gamma2 = row sum, A /= gamma2, column sums beta2 (into beta).
+template <int DIM>
+__global__ void k_adv_rows(Geo g, float* __restrict__ wb, const int* __restrict__ bb, float* __restrict__ gsum,
+                           float* __restrict__ beta) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    const int base = bb[i];
+    float vals[K];
+    float local = 0;
+    if (base >= 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) { vals[k] = wb[k * g.N + i]; local += vals[k]; }
+    }
+    const float g2 = local + gsum[i];
+    gsum[i] = g2;
+    if (base < 0) return;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float val = vals[k];
+        if (g2 > 1.e-5f) val /= g2;
+        wb[k * g.N + i] = val;
+        atomicAdd(&beta[base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k))], val);
+    }
+}
+
+// Steps 7-8 for the forward entries: A /= gamma2 of their row, column sums into beta.
+template <int DIM>
+__global__ void k_adv_cols(Geo g, float* __restrict__ wf, const int* __restrict__ fb, const float* __restrict__ gsum,
+                           float* __restrict__ beta) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    int x, y, z = 0, j;
+    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    const int base = fb[j];
+    if (base < 0) return;
+    float local = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float val = wf[k * g.N + j];
+        const float g2 = gsum[base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k))];
+        if (g2 > 1.e-5f) val /= g2;
+        wf[k * g.N + j] = val;
+        local += val;
+    }
+    atomicAdd(&beta[j], local);
+}
+
+// Steps 9-11 for the backward rows, every cell: A /= beta2 of the column, gamma3 = row sum, rho' = A rho.
+// Cells without a backward row (border, solids) get 0, which the forward pass then adds to.
+template <int DIM>
+__global__ void k_adv_apply_rows(Geo g, const float* __restrict__ wb, const int* __restrict__ bb,
+                                 const float* __restrict__ beta, const float* __restrict__ rho,
+                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    const int x = i % g.W, y = (i / g.W) % g.H, z = i / g.WH;
+    bool interior = x >= 1 && x <= g.W - 2 && y >= 1 && y <= g.H - 2;
+    if (DIM == 3) interior = interior && z >= 1 && z <= g.D - 2;
+    float gs = 0, rs = 0;
+    const int base = interior ? bb[i] : -1;
+    if (base >= 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int c = base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k));
+            float val = wb[k * g.N + i];
+            const float b2 = beta[c];
+            if (b2 > 1.e-5f) val /= b2;
+            gs += val;
+            rs += val * rho[c];
+        }
+    }
+    gamma_out[i] = gs;
+    rho_out[i] = rs;
+}
+
+// Steps 9-11 for the forward entries: A /= beta2_j, scattered into gamma3 and rho'.
+template <int DIM>
+__global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int* __restrict__ fb,
+                                 const float* __restrict__ beta, const float* __restrict__ rho,
+                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+    constexpr int K = (DIM == 3) ? 8 : 4;
+    int x, y, z = 0, j;
+    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    const int base = fb[j];
+    if (base < 0) return;
+    const float b2 = beta[j];
+    const float rj = rho[j];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float val = wf[k * g.N + j];
+        if (b2 > 1.e-5f) val /= b2;
+        const int c = base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k));
+        atomicAdd(&gamma_out[c], val);
+        atomicAdd(&rho_out[c], val * rj);
+    }
+}
+
+// Step 12: one in-place sweep of pairwise gamma-equalising transfers along one axis
+// (CPUSimulator3D.cpp:277-362).  One thread walks one line sequentially; `stride` is the axis stride,
+// `n` the line length (cells), line start = `first`.
+__device__ __forceinline__ void diffuse_line(const float* __restrict__ rsrc, const float* __restrict__ gsrc,
+                                             float* __restrict__ rdst, float* __restrict__ gdst,
+                                             const uint8_t* __restrict__ solid, int first, int stride, int n) {
+    // cells first + stride * c for c = 1 .. n-2; pairs (c-1, c) for c = 2 .. n-2
+    int jj = first + stride;
+    float rj = rsrc[jj], gj = gsrc[jj];
+    uint8_t sj = solid[jj];
+    for (int c = 2; c <= n - 2; c++) {
+        const int ii = jj + stride;
+        float ri = rsrc[ii], gi = gsrc[ii];
+        const uint8_t si = solid[ii];
+        if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
+            const float avg = (gj + gi) / 2.f;
+            if (gj > gi) {
+                const float dif = rj * (gj - gi) / (2.f * gj);
+                rj -= dif; ri += dif;
+            } else {
+                const float dif = ri * (gi - gj) / (2.f * gi);
+                ri -= dif; rj += dif;
+            }
+            gj = avg; gi = avg;
+        }
+        rdst[jj] = rj; gdst[jj] = gj;
+        jj = ii; rj = ri; gj = gi; sj = si;
+    }
+    if (n >= 3) { rdst[jj] = rj; gdst[jj] = gj; }
+}
+
+// X sweep: one thread per (y, z) line.
+__global__ void k_diffuse_x(Geo g, int dim, const float* rsrc, const float* gsrc, float* rdst, float* gdst,
+                            const uint8_t* __restrict__ solid) {
+    const int y = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = (dim == 3) ? 1 + blockIdx.y : 0;
+    if (y > g.H - 2) return;
+    diffuse_line(rsrc, gsrc, rdst, gdst, solid, z * g.WH + y * g.W, 1, g.W);
+}
+// Y sweep: one thread per (x, z) line (consecutive threads = consecutive x: coalesced).
+__global__ void k_diffuse_y(Geo g, int dim, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
+    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = (dim == 3) ? 1 + blockIdx.y : 0;
+    if (x > g.W - 2) return;
+    diffuse_line(rho, gamma, rho, gamma, solid, z * g.WH + x, g.W, g.H);
+}
+// Z sweep: one thread per (x, y) line.
+__global__ void k_diffuse_z(Geo g, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
+    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = 1 + blockIdx.y;
+    if (x > g.W - 2) return;
+    diffuse_line(rho, gamma, rho, gamma, solid, y * g.W + x, g.WH, g.D);
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 4: vel_advect (CPUSimulator3D.cpp:478-504, CPUSimulator2D.cpp:427-448), optionally followed by
+// stage 5 add_force in the same pass.
+// ------------------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_vadv_trace(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                             const float* __restrict__ w, const uint8_t* __restrict__ solid, float dt,
+                             float* __restrict__ tu, float* __restrict__ tv, float* __restrict__ tw) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) {
+        float px, py, pz, a, b, c;
+        trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, -dt, 4, px, py, pz);
+        vinterp3(u, v, w, g, px - 0.5f, py - 0.5f, pz - 0.5f, a, b, c);
+        tu[i] = a; tv[i] = b; tw[i] = c;
+    } else {
+        float px, py, a, b;
+        trace2(u, v, solid, g, (float)x, (float)y, -dt, 4, px, py);
+        vinterp2(u, v, g, px - 0.5f, py - 0.5f, a, b);
+        tu[i] = a; tv[i] = b;
+    }
+}
+
+struct ForceArgs {
+    int enabled;          // fuse add_force after the averaging
+    int has_forces;       // forces field is not all zero
+    int gravity;
+    float dt, gforce;
+    const float *fx, *fy, *fz;
+};
+
+// 3D add_force on one cell (CPUSimulator3D.cpp:458-476)
+__device__ __forceinline__ void add_force_cell3(const ForceArgs& f, int i, bool solid_i, float& a, float& b, float& c) {
+    if (solid_i) return;
+    if (f.has_forces) { a += f.fx[i] * f.dt; b += f.fy[i] * f.dt; c += f.fz[i] * f.dt; }
+    if (f.gravity) b -= f.gforce * f.dt;
+}
+// 2D add_force on one cell, face based (CPUSimulator2D.cpp:404-425)
+__device__ __forceinline__ void add_force_cell2(const ForceArgs& f, int i, bool s_i, bool s_xm, bool s_ym, float& a,
+                                                float& b) {
+    if (!s_i || !s_xm) a += f.fx[i] * f.dt; else a = 0.f;
+    if (!s_i || !s_ym) {
+        b += f.fy[i] * f.dt;
+        if (f.gravity) b -= f.gforce * f.dt;
+    } else b = 0.f;
+}
+
+template <int DIM>
+__global__ void k_vadv_average(Geo g, const float* __restrict__ tu, const float* __restrict__ tv,
+                               const float* __restrict__ tw, const uint8_t* __restrict__ solid, float* __restrict__ u,
+                               float* __restrict__ v, float* __restrict__ w, ForceArgs f) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    const bool si = solid[i], sx = solid[i - 1], sy = solid[i - g.W];
+    float a = (x == 1 || si || sx) ? tu[i] : 0.5f * (tu[i] + tu[i - 1]);
+    float b = (y == 1 || si || sy) ? tv[i] : 0.5f * (tv[i] + tv[i - g.W]);
+    if (DIM == 3) {
+        const bool sz = solid[i - g.WH];
+        float c = (z == 1 || si || sz) ? tw[i] : 0.5f * (tw[i] + tw[i - g.WH]);
+        if (f.enabled) add_force_cell3(f, i, si, a, b, c);
+        w[i] = c;
+    } else {
+        if (f.enabled) add_force_cell2(f, i, si, sx, sy, a, b);
+    }
+    u[i] = a; v[i] = b;
+}
+
+template <int DIM>
+__global__ void k_add_force(Geo g, const uint8_t* __restrict__ solid, float* __restrict__ u, float* __restrict__ v,
+                            float* __restrict__ w, ForceArgs f) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    float a = u[i], b = v[i];
+    if (DIM == 3) {
+        float c = w[i];
+        add_force_cell3(f, i, solid[i] != 0, a, b, c);
+        w[i] = c;
+    } else {
+        add_force_cell2(f, i, solid[i] != 0, solid[i - 1] != 0, solid[i - g.W] != 0, a, b);
+    }
+    u[i] = a; v[i] = b;
+}
+
+// ------------------------------------------------------------------------------------------------
+// stage 6: project (CPUSimulator3D.cpp:506-566 with enforce_wall_boundaries :657-679;
+// CPUSimulator2D.cpp:450-524, :597-607)
+// ------------------------------------------------------------------------------------------------
+
+// wall rule of one face (3D: sign dependent; 2D: zero when either side is solid)
+template <int DIM>
+__device__ __forceinline__ float wall_face(float val, bool solid_here, bool solid_below) {
+    if (DIM == 3) {
+        if (solid_here && val > 0) val = 0.f;
+        if (solid_below && val < 0) val = 0.f;
+        return val;
+    } else {
+        return (solid_here || solid_below) ? 0.f : val;
+    }
+}
+
+struct ProjectArgs {
+    float thrL, lp, lm, eta;
+    int jacobi;          // p starts at 0 (Jacobi) or at b (CG)
+};
+
+// Walls on every face, divergence with the density correction, initial pressure, matrix-row description and
+// active-chunk flags.  One thread per cell, 1D over the linear index (a warp is one aligned 32-cell chunk).
+template <int DIM>
+__global__ void k_project_pre(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                              const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                              float* __restrict__ div, float* __restrict__ p, uint16_t* __restrict__ rowinfo,
+                              uint8_t* __restrict__ chunk_flag, ProjectArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < g.N;
+    bool active = false;
+    if (in) {
+        const int x = i % g.W, y = (i / g.W) % g.H, z = (DIM == 3) ? i / g.WH : 0;
+        const bool si = solid[i];
+        // enforce_wall_boundaries on this cell's faces
+        float fu = u[i], fv = v[i], fw = 0.f;
+        if (DIM == 3) {
+            if (x >= 1 && y >= 1 && z >= 1) {
+                fu = wall_face<3>(fu, si, solid[i - 1]);
+                fv = wall_face<3>(fv, si, solid[i - g.W]);
+                fw = wall_face<3>(w[i], si, solid[i - g.WH]);
+                u[i] = fu; v[i] = fv; w[i] = fw;
+            }
+        } else {
+            fu = wall_face<2>(fu, si, x > 0 && solid[i - (x > 0 ? 1 : 0)]);
+            fv = wall_face<2>(fv, si, y > 0 && solid[i - (y > 0 ? g.W : 0)]);
+            u[i] = fu; v[i] = fv;
+        }
+        bool interior = x >= 1 && x <= g.W - 2 && y >= 1 && y <= g.H - 2;
+        if (DIM == 3) interior = interior && z >= 1 && z <= g.D - 2;
+        float d = 0.f;
+        const float r = rho[i];
+        if (interior && !(r < a.thrL) && !si) {
+            const float up = wall_face<DIM>(u[i + 1], solid[i + 1], si);
+            const float vp = wall_face<DIM>(v[i + g.W], solid[i + g.W], si);
+            const float dx = up - fu, dy = vp - fv;
+            if (DIM == 3) {
+                const float wp = wall_face<3>(w[i + g.WH], solid[i + g.WH], si);
+                d = dx + dy + (wp - fw);
+            } else {
+                d = dx + dy;
+            }
+            if (r > 1.f) d -= minf(a.lm * (r - 1.f), a.eta);
+            if (r < 1.f) d += minf(a.lp * (1.f - r), a.eta);
+        }
+        div[i] = d;
+        p[i] = a.jacobi ? 0.f : d;
+        // matrix row (CGSolver.cpp:467-497): rho > 0.5 and not solid; neighbours counted when inside, off the
+        // border and not solid; summed when also rho > 0.5.  Bits: x-1, x+1, y-1, y+1, z-1, z+1.
+        uint16_t info = 0;
+        if (r > 0.5f && !si) {
+            const int nx[6] = {x - 1, x + 1, x, x, x, x}, ny[6] = {y, y, y - 1, y + 1, y, y};
+            const int nz[6] = {z, z, z, z, z - 1, z + 1};
+            const int off[6] = {-1, 1, -g.W, g.W, -g.WH, g.WH};
+            int cnt = 0;
+#pragma unroll
+            for (int k = 0; k < 2 * DIM; k++) {
+                if (nx[k] <= 0 || nx[k] >= g.W - 1 || ny[k] <= 0 || ny[k] >= g.H - 1) continue;
+                if (DIM == 3 && (nz[k] <= 0 || nz[k] >= g.D - 1)) continue;
+                const int j = i + off[k];
+                if (solid[j]) continue;
+                cnt++;
+                if (rho[j] > 0.5f) info |= (uint16_t)(1u << k);
+            }
+            info |= (uint16_t)(cnt << 8) | (uint16_t)0x8000u;
+        }
+        rowinfo[i] = info;
+        active = (info & 0x8000u) || d != 0.f;
+    }
+    const unsigned any = __ballot_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0 && (i >> 5) < ((g.N + 31) >> 5)) chunk_flag[i >> 5] = any ? 1 : 0;
+}
+
+// v -= grad p on non-solid interior cells, then walls on every face; skipped (with PAUSED set) when the solve
+// did not converge (CPUSimulator3D.cpp:541-566).
+template <int DIM>
+__global__ void k_project_post(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                               const float* __restrict__ p, const uint8_t* __restrict__ solid, DevCtl* ctl,
+                               int do_walls) {
+    if (!ctl->converged) {
+        if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->paused = 1;
+        return;
+    }
+    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = (DIM == 3) ? 1 + blockIdx.z : 0;
+    if (x > g.W - 1 || y > g.H - 1) return;
+    const int i = z * g.WH + y * g.W + x;
+    const bool si = solid[i];
+    const bool interior = x <= g.W - 2 && y <= g.H - 2 && (DIM == 2 || z <= g.D - 2);
+    float fu = u[i], fv = v[i], fw = (DIM == 3) ? w[i] : 0.f;
+    if (interior) {
+        if (DIM == 3) {
+            if (!si) {
+                float gx = 0, gy = 0, gz = 0;
+                if (x > 1) gx = p[i] - p[i - 1];
+                if (y > 1) gy = p[i] - p[i - g.W];
+                if (z > 1) gz = p[i] - p[i - g.WH];
+                fu -= gx; fv -= gy; fw -= gz;
+            }
+        } else {
+            if (!si && !solid[i - 1]) fu -= (p[i] - p[i - 1]); else fu = 0.f;
+            if (!si && !solid[i - g.W]) fv -= (p[i] - p[i - g.W]); else fv = 0.f;
+        }
+    }
+    if (do_walls) {
+        fu = wall_face<DIM>(fu, si, solid[i - 1]);
+        fv = wall_face<DIM>(fv, si, solid[i - g.W]);
+        if (DIM == 3) fw = wall_face<3>(fw, si, solid[i - g.WH]);
+    }
+    u[i] = fu; v[i] = fv;
+    if (DIM == 3) w[i] = fw;
+}
+
+// ISolver::solve on the current divergence: matrix-row description, active-chunk flags and the solver's
+// initial pressure (CG: p = b, CGSolver.cpp:429; Jacobi: the current p, JacobiSolver.cpp:159).
+template <int DIM>
+__global__ void k_solver_prep(Geo g, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                              const float* __restrict__ div, float* __restrict__ p, uint16_t* __restrict__ rowinfo,
+                              uint8_t* __restrict__ chunk_flag, int jacobi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = false;
+    if (i < g.N) {
+        const int x = i % g.W, y = (i / g.W) % g.H, z = (DIM == 3) ? i / g.WH : 0;
+        const float d = div[i];
+        if (!jacobi) p[i] = d;
+        uint16_t info = 0;
+        if (rho[i] > 0.5f && !solid[i]) {
+            const int nx[6] = {x - 1, x + 1, x, x, x, x}, ny[6] = {y, y, y - 1, y + 1, y, y};
+            const int nz[6] = {z, z, z, z, z - 1, z + 1};
+            const int off[6] = {-1, 1, -g.W, g.W, -g.WH, g.WH};
+            int cnt = 0;
+#pragma unroll
+            for (int k = 0; k < 2 * DIM; k++) {
+                if (nx[k] <= 0 || nx[k] >= g.W - 1 || ny[k] <= 0 || ny[k] >= g.H - 1) continue;
+                if (DIM == 3 && (nz[k] <= 0 || nz[k] >= g.D - 1)) continue;
+                const int j = i + off[k];
+                if (solid[j]) continue;
+                cnt++;
+                if (rho[j] > 0.5f) info |= (uint16_t)(1u << k);
+            }
+            info |= (uint16_t)(cnt << 8) | (uint16_t)0x8000u;
+        }
+        rowinfo[i] = info;
+        active = (info & 0x8000u) || d != 0.f || (jacobi && p[i] != 0.f);
+    }
+    const unsigned any = __ballot_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0 && (i >> 5) < ((g.N + 31) >> 5)) chunk_flag[i >> 5] = any ? 1 : 0;
+}
+
+// 2D RE_CALC_DIV (CPUSimulator2D.cpp:503-521) and the closing walls when it is on.
+__global__ void k_recalc_div2(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ rho, const uint8_t* __restrict__ solid, float* __restrict__ div,
+                              ProjectArgs a, const DevCtl* ctl) {
+    if (!ctl->converged) return;
+    int x, y, i;
+    if (!cell2(g, x, y, i)) return;
+    const float r = rho[i];
+    if (r < a.thrL || solid[i]) return;
+    float d = (u[i + 1] - u[i]) + (v[i + g.W] - v[i]);
+    if (r > 1.f) d -= minf(a.lm * (r - 1.f), a.eta);
+    if (r < 1.f) d += minf(a.lp * (1.f - r), a.eta);
+    div[i] = d;
+}
+__global__ void k_walls2(Geo g, float* __restrict__ u, float* __restrict__ v, const uint8_t* __restrict__ solid,
+                         const DevCtl* ctl) {
+    if (!ctl->converged) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.N) return;
+    const int x = i % g.W, y = i / g.W;
+    const bool si = solid[i];
+    if (si || (x > 0 && solid[i - 1])) u[i] = 0.f;
+    if (si || (y > 0 && solid[i - g.W])) v[i] = 0.f;
+}
+
+inline dim3 grid_interior(const Geo& g, int dim) {
+    return dim3((g.W - 2 + BX - 1) / BX, (g.H - 2 + BY - 1) / BY, dim == 3 ? g.D - 2 : 1);
+}
+inline dim3 grid_linear(int n, int threads) { return dim3((n + threads - 1) / threads); }
+
+}  // namespace
+
+#define EFS_LAUNCH_CHECK() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
+
+static cudaError_t stage_decay(efs_ctx* c) {
+    const dim3 b(BX, BY), gr = grid_interior(c->g, c->dim);
+    if (c->dim == 3) k_vel_decay<3><<<gr, b, 0, c->stream>>>(c->g, c->u, c->v, c->w, c->rho, c->prm.vel_decay);
+    else k_vel_decay<2><<<gr, b, 0, c->stream>>>(c->g, c->u, c->v, c->w, c->rho, c->prm.vel_decay);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+static cudaError_t stage_extrapolate(efs_ctx* c) {
+    const Geo& g = c->g;
+    float* tu = c->tvel; float* tv = c->tvel + g.N; float* tw = c->tvel + 2 * (size_t)g.N;
+    k_extrap_init<<<grid_linear(g.N, 256), 256, 0, c->stream>>>(g, c->dim, c->rho, c->solid, c->validA);
+    EFS_LAUNCH_CHECK();
+    const dim3 b(BX, BY), gr = grid_interior(g, c->dim);
+    for (int it = 0; it < 6; it++) {
+        const bool odd = it & 1;
+        const float* su = odd ? tu : c->u; const float* sv = odd ? tv : c->v; const float* sw = odd ? tw : c->w;
+        float* du = odd ? c->u : tu; float* dv = odd ? c->v : tv; float* dw = odd ? c->w : tw;
+        const uint8_t* sV = odd ? c->validB : c->validA;
+        uint8_t* dV = odd ? c->validA : c->validB;
+        if (c->dim == 3) k_extrap_pass<3><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid);
+        else k_extrap_pass<2><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid);
+        EFS_LAUNCH_CHECK();
+    }
+    return cudaSuccess;
+}
+
+static cudaError_t stage_sharpen(efs_ctx* c) {
+    const Geo& g = c->g;
+    cudaError_t e = cudaMemsetAsync(&c->ctl->sh_count, 0, sizeof(int), c->stream);
+    if (e != cudaSuccess) return e;
+    const dim3 b(BX, BY), gr = grid_interior(g, c->dim);
+    const float delT = c->prm.dt * 3;
+    const int cap = g.N;
+    const int lg = c->sm_count * 4;
+    if (c->dim == 3) k_sharpen_calc<3><<<gr, b, 0, c->stream>>>(g, c->rho, delT, c->sh_idx, c->sh_val, c->ctl, cap);
+    else k_sharpen_calc<2><<<gr, b, 0, c->stream>>>(g, c->rho, delT, c->sh_idx, c->sh_val, c->ctl, cap);
+    EFS_LAUNCH_CHECK();
+    k_sharpen_apply<<<lg, 256, 0, c->stream>>>(c->rho, c->sh_idx, c->sh_val, c->ctl, cap);
+    EFS_LAUNCH_CHECK();
+    if (c->dim == 3) {
+        k_sharpen_trace<3><<<lg, 256, 0, c->stream>>>(g, c->rho, c->solid, c->sh_idx, c->sh_end, c->prm.rho_d, c->ctl, cap);
+        EFS_LAUNCH_CHECK();
+        k_sharpen_scatter<3><<<lg, 256, 0, c->stream>>>(g, c->rho, c->solid, c->sh_val, c->sh_end, c->ctl, cap);
+    } else {
+        k_sharpen_trace<2><<<lg, 256, 0, c->stream>>>(g, c->rho, c->solid, c->sh_idx, c->sh_end, c->prm.rho_d, c->ctl, cap);
+        EFS_LAUNCH_CHECK();
+        k_sharpen_scatter<2><<<lg, 256, 0, c->stream>>>(g, c->rho, c->solid, c->sh_val, c->sh_end, c->ctl, cap);
+    }
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+template <int DIM>
+static cudaError_t stage_advect_t(efs_ctx* c) {
+    const Geo& g = c->g;
+    const size_t bytes = (size_t)g.N * sizeof(float);
+    const dim3 b(BX, BY), gr = grid_interior(g, DIM);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(c->bsum, 0, bytes, c->stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->gsum, 0, bytes, c->stream)) != cudaSuccess) return e;
+    k_adv_backward<DIM><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->gamma, c->prm.dt, c->wb, c->bb, c->bsum);
+    EFS_LAUNCH_CHECK();
+    k_adv_forward<DIM><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->bsum, c->prm.dt, c->wf, c->fb, c->gsum);
+    EFS_LAUNCH_CHECK();
+    if ((e = cudaMemsetAsync(c->beta, 0, bytes, c->stream)) != cudaSuccess) return e;
+    k_adv_rows<DIM><<<gr, b, 0, c->stream>>>(g, c->wb, c->bb, c->gsum, c->beta);
+    EFS_LAUNCH_CHECK();
+    k_adv_cols<DIM><<<gr, b, 0, c->stream>>>(g, c->wf, c->fb, c->gsum, c->beta);
+    EFS_LAUNCH_CHECK();
+    k_adv_apply_rows<DIM><<<grid_linear(g.N, 256), 256, 0, c->stream>>>(g, c->wb, c->bb, c->beta, c->rho, c->gamma, c->rho_acc);
+    EFS_LAUNCH_CHECK();
+    k_adv_apply_cols<DIM><<<gr, b, 0, c->stream>>>(g, c->wf, c->fb, c->beta, c->rho, c->gamma, c->rho_acc);
+    EFS_LAUNCH_CHECK();
+    // step 11's copy of rho' into the interior is folded into the first x sweep (it reads rho_acc and writes
+    // rho); step 12's sweeps follow
+    const int iters = (DIM == 3) ? 3 : 7;
+    for (int it = 0; it < iters; it++) {
+        const float* rs = (it == 0) ? c->rho_acc : c->rho;
+        k_diffuse_x<<<dim3((g.H - 2 + 127) / 128, DIM == 3 ? g.D - 2 : 1), 128, 0, c->stream>>>(g, DIM, rs, c->gamma, c->rho, c->gamma, c->solid);
+        EFS_LAUNCH_CHECK();
+        k_diffuse_y<<<dim3((g.W - 2 + 127) / 128, DIM == 3 ? g.D - 2 : 1), 128, 0, c->stream>>>(g, DIM, c->rho, c->gamma, c->solid);
+        EFS_LAUNCH_CHECK();
+        if (DIM == 3) {
+            k_diffuse_z<<<dim3((g.W - 2 + 127) / 128, g.H - 2), 128, 0, c->stream>>>(g, c->rho, c->gamma, c->solid);
+            EFS_LAUNCH_CHECK();
+        }
+    }
+    return cudaSuccess;
+}
+
+static ForceArgs force_args(efs_ctx* c, int enabled) {
+    ForceArgs f;
+    f.enabled = enabled;
+    f.has_forces = c->has_forces ? 1 : 0;
+    f.gravity = c->prm.gravity_enabled ? 1 : 0;
+    f.dt = c->prm.dt;
+    f.gforce = c->prm.gravity_force;
+    f.fx = c->fx; f.fy = c->fy; f.fz = c->fz;
+    return f;
+}
+
+static cudaError_t stage_vel_advect(efs_ctx* c, bool fuse_force) {
+    const Geo& g = c->g;
+    float* tu = c->tvel; float* tv = c->tvel + g.N; float* tw = c->tvel + 2 * (size_t)g.N;
+    const dim3 b(BX, BY), gr = grid_interior(g, c->dim);
+    const ForceArgs f = force_args(c, fuse_force ? 1 : 0);
+    if (c->dim == 3) {
+        k_vadv_trace<3><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
+        EFS_LAUNCH_CHECK();
+        k_vadv_average<3><<<gr, b, 0, c->stream>>>(g, tu, tv, tw, c->solid, c->u, c->v, c->w, f);
+    } else {
+        k_vadv_trace<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
+        EFS_LAUNCH_CHECK();
+        k_vadv_average<2><<<gr, b, 0, c->stream>>>(g, tu, tv, tw, c->solid, c->u, c->v, c->w, f);
+    }
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+static cudaError_t stage_add_force(efs_ctx* c) {
+    const dim3 b(BX, BY), gr = grid_interior(c->g, c->dim);
+    const ForceArgs f = force_args(c, 1);
+    if (c->dim == 3) k_add_force<3><<<gr, b, 0, c->stream>>>(c->g, c->solid, c->u, c->v, c->w, f);
+    else k_add_force<2><<<gr, b, 0, c->stream>>>(c->g, c->solid, c->u, c->v, c->w, f);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+static ProjectArgs project_args(efs_ctx* c) {
+    ProjectArgs a;
+    a.thrL = c->prm.liquid_threshold; a.lp = c->prm.lambda_plus; a.lm = c->prm.lambda_minus; a.eta = c->prm.eta;
+    a.jacobi = c->prm.solver == EFS_SOLVER_JACOBI;
+    return a;
+}
+
+cudaError_t launch_project_pre(efs_ctx* c) {
+    const Geo& g = c->g;
+    const ProjectArgs a = project_args(c);
+    const int nthreads = 256;
+    const int nblk = (((g.N + 31) / 32) * 32 + nthreads - 1) / nthreads;
+    if (c->dim == 3) k_project_pre<3><<<nblk, nthreads, 0, c->stream>>>(g, c->u, c->v, c->w, c->rho, c->solid, c->div, c->p, c->rowinfo, c->chunk_flag, a);
+    else k_project_pre<2><<<nblk, nthreads, 0, c->stream>>>(g, c->u, c->v, c->w, c->rho, c->solid, c->div, c->p, c->rowinfo, c->chunk_flag, a);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t launch_project_post(efs_ctx* c) {
+    const Geo& g = c->g;
+    const dim3 b(BX, BY);
+    const dim3 gr((g.W - 1 + BX - 1) / BX, (g.H - 1 + BY - 1) / BY, c->dim == 3 ? g.D - 1 : 1);
+    if (c->dim == 3) {
+        k_project_post<3><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->p, c->solid, c->ctl, 1);
+        EFS_LAUNCH_CHECK();
+    } else if (!c->prm.re_calc_div) {
+        k_project_post<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->p, c->solid, c->ctl, 1);
+        EFS_LAUNCH_CHECK();
+    } else {
+        k_project_post<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->p, c->solid, c->ctl, 0);
+        EFS_LAUNCH_CHECK();
+        k_recalc_div2<<<grid_interior(g, 2), b, 0, c->stream>>>(g, c->u, c->v, c->rho, c->solid, c->div, project_args(c), c->ctl);
+        EFS_LAUNCH_CHECK();
+        k_walls2<<<grid_linear(g.N, 256), 256, 0, c->stream>>>(g, c->u, c->v, c->solid, c->ctl);
+        EFS_LAUNCH_CHECK();
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_solver_prep(efs_ctx* c) {
+    const Geo& g = c->g;
+    const int nthreads = 256;
+    const int nblk = (((g.N + 31) / 32) * 32 + nthreads - 1) / nthreads;
+    const int jacobi = c->prm.solver == EFS_SOLVER_JACOBI;
+    if (c->dim == 3) k_solver_prep<3><<<nblk, nthreads, 0, c->stream>>>(g, c->rho, c->solid, c->div, c->p, c->rowinfo, c->chunk_flag, jacobi);
+    else k_solver_prep<2><<<nblk, nthreads, 0, c->stream>>>(g, c->rho, c->solid, c->div, c->p, c->rowinfo, c->chunk_flag, jacobi);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force) {
+    switch (stage) {
+        case EFS_STAGE_VEL_DECAY: return stage_decay(c);
+        case EFS_STAGE_VEL_EXTRAPOLATE: return stage_extrapolate(c);
+        case EFS_STAGE_RHO_SHARPEN: return stage_sharpen(c);
+        case EFS_STAGE_RHO_ADVECT: return c->dim == 3 ? stage_advect_t<3>(c) : stage_advect_t<2>(c);
+        case EFS_STAGE_VEL_ADVECT: return stage_vel_advect(c, fuse_add_force);
+        case EFS_STAGE_ADD_FORCE: return stage_add_force(c);
+        case EFS_STAGE_PROJECT: {
+            cudaError_t e = launch_project_pre(c);
+            if (e != cudaSuccess) return e;
+            if ((e = launch_solver(c)) != cudaSuccess) return e;
+            return launch_project_post(c);
+        }
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace efs

@@ -1,0 +1,241 @@
+"""Host-side mirror of the reference's simulator-backend interface, over the C ABI.
+
+``GB300Simulator3D`` / ``GB300Simulator2D`` stand where the reference's ``CPUSimulator3D`` / ``CudaSimulator3D``
+stand (include/simulation/simulator/ISimulator.h:8-53): ``update()`` runs the seven stages in the reference
+order with the ``DISABLE_*`` gates of ``params.disable_mask``; the protected stage virtuals are exposed under
+their reference names; ``solve()`` is ``ISolver::solve``; the grid accessors of ``IGrid3D``
+(include/simulation/data/IGrid.h:44-68) return host copies in the reference layout and the ``set_*``
+methods write them back, as the reference editor writes ``rho`` / ``boundary`` through those references.
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+from ._lib import EfsError, check, fptr, lib
+
+
+class _GB300Simulator:
+    def __init__(self, dim, width, height, depth, params=None):
+        self.dim = dim
+        self.width, self.height = width, height
+        self.depth = depth if dim == 3 else 1
+        self.shape = (self.depth, height, width) if dim == 3 else (height, width)
+        if params is None:
+            params = abi.params_default()
+        self._params = params.copy()
+        h = ctypes.c_void_p()
+        L = lib()
+        st = L.efs_create(dim, width, height, self.depth, ctypes.byref(self._params), ctypes.byref(h))
+        if st != 0:
+            raise EfsError(st, L.efs_last_error(None).decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().efs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- parameters (Properties values) ----
+    @property
+    def params(self):
+        return self._params.copy()
+
+    def set_params(self, params):
+        check(lib().efs_set_params(self._h, ctypes.byref(params)), self._h)
+        self._params = params.copy()
+
+    # ---- ISimulator ----
+    def update(self, n=1):
+        """ISimulator::update() n times (asynchronous; fields and stats synchronise)."""
+        check(lib().efs_step(self._h, n), self._h)
+
+    def stage(self, s):
+        check(lib().efs_stage(self._h, s), self._h)
+
+    def vel_decay(self):
+        self.stage(abi.STAGE_VEL_DECAY)
+
+    def vel_extrapolate(self):
+        self.stage(abi.STAGE_VEL_EXTRAPOLATE)
+
+    def rho_sharpen(self):
+        self.stage(abi.STAGE_RHO_SHARPEN)
+
+    def rho_advect(self):
+        self.stage(abi.STAGE_RHO_ADVECT)
+
+    def vel_advect(self):
+        self.stage(abi.STAGE_VEL_ADVECT)
+
+    def add_force(self):
+        self.stage(abi.STAGE_ADD_FORCE)
+
+    def project(self):
+        self.stage(abi.STAGE_PROJECT)
+
+    # ---- ISolver ----
+    def solve(self):
+        """ISolver::solve on the current divergence; returns the stats (raises EfsError if not converged)."""
+        s = abi.EfsStats()
+        check(lib().efs_solve(self._h, ctypes.byref(s)), self._h)
+        return s
+
+    def synchronize(self):
+        check(lib().efs_synchronize(self._h), self._h)
+
+    def stats(self):
+        s = abi.EfsStats()
+        check(lib().efs_get_stats(self._h, ctypes.byref(s)), self._h)
+        return s
+
+    def total_mass(self):
+        m = ctypes.c_double()
+        check(lib().efs_total_mass(self._h, ctypes.byref(m)), self._h)
+        return m.value
+
+    # ---- IGrid ----
+    def _fshape(self, f):
+        return self.shape + (self.dim,) if f in abi.VECTOR_FIELDS else self.shape
+
+    def field(self, f):
+        out = np.empty(self._fshape(f), np.float32)
+        check(lib().efs_download_field(self._h, f, fptr(out)), self._h)
+        return out
+
+    def set_field(self, f, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        if a.size != int(np.prod(self._fshape(f))):
+            raise ValueError(f"{abi.FIELD_NAMES[f]}: expected {self._fshape(f)}, got {a.shape}")
+        check(lib().efs_upload_field(self._h, f, fptr(a)), self._h)
+
+    def fields(self):
+        return {f: self.field(f) for f in range(abi.FIELD_COUNT)}
+
+    def set_fields(self, fields):
+        if abi.FIELD_BOUNDARY in fields:
+            self.set_field(abi.FIELD_BOUNDARY, fields[abi.FIELD_BOUNDARY])
+        for f, a in fields.items():
+            if f != abi.FIELD_BOUNDARY:
+                self.set_field(f, a)
+
+    def reset(self):
+        check(lib().efs_reset_fields(self._h), self._h)
+
+    def vel(self):
+        return self.field(abi.FIELD_VEL)
+
+    def rho(self):
+        return self.field(abi.FIELD_RHO)
+
+    def gamma(self):
+        return self.field(abi.FIELD_GAMMA)
+
+    def beta(self):
+        return self.field(abi.FIELD_BETA)
+
+    def divergence(self):
+        return self.field(abi.FIELD_DIVERGENCE)
+
+    def pressure(self):
+        return self.field(abi.FIELD_PRESSURE)
+
+    def forces(self):
+        return self.field(abi.FIELD_FORCES)
+
+    def boundary(self):
+        return self.field(abi.FIELD_BOUNDARY)
+
+    def kernels_per_step(self):
+        n = ctypes.c_int()
+        check(lib().efs_step_kernel_count(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+    def mark(self, slot):
+        """Record CUDA event `slot` on the simulator's stream."""
+        check(lib().efs_timer_mark(self._h, slot), self._h)
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_double()
+        check(lib().efs_timer_elapsed(self._h, a, b, ctypes.byref(ms)), self._h)
+        return ms.value
+
+    def upload_fields(self, vel=None, rho=None, gamma=None, boundary=None, forces=None):
+        """efs_upload_fields (CudaGrid3D::upload): host arrays in the reference layout; None skips."""
+        check(lib().efs_upload_fields(self._h, fptr(vel), fptr(rho), fptr(gamma), fptr(boundary), fptr(forces)), self._h)
+
+    def download_fields(self, vel=None, rho=None, gamma=None, beta=None, divergence=None, pressure=None):
+        """efs_download_fields (CudaGrid3D::download) into host arrays; None skips."""
+        check(lib().efs_download_fields(self._h, fptr(vel), fptr(rho), fptr(gamma), fptr(beta), fptr(divergence),
+                                        fptr(pressure)), self._h)
+
+    # ---- timing of the pressure solve ----
+    def solve_timing_arm(self, capacity):
+        check(lib().efs_solve_timing_arm(self._h, capacity), self._h)
+
+    def solve_timing_read(self):
+        n = ctypes.c_int()
+        ms = ctypes.c_double()
+        ri = ctypes.c_double()
+        rs = ctypes.c_double()
+        check(lib().efs_solve_timing_read(self._h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(ri), ctypes.byref(rs)), self._h)
+        return n.value, ms.value, ri.value, rs.value
+
+
+class GB300Simulator3D(_GB300Simulator):
+    """Drop-in for the reference's 3D backends (ISimulator3D(w, h, d), ISimulator3D.h:6-14)."""
+
+    def __init__(self, width, height, depth, params=None):
+        super().__init__(3, width, height, depth, params)
+
+
+class GB300Simulator2D(_GB300Simulator):
+    """Drop-in for the reference's 2D backends (ISimulator2D(w, h), ISimulator2D.h:6-13)."""
+
+    def __init__(self, width, height, params=None):
+        super().__init__(2, width, height, 1, params)
+
+
+def device_count():
+    n = ctypes.c_int()
+    check(lib().efs_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def scene_dam3d(w, h, d, n_min, n_max, seed):
+    b = np.zeros((d, h, w), np.float32)
+    r = np.zeros((d, h, w), np.float32)
+    check(lib().efs_scene_dam3d(w, h, d, n_min, n_max, seed, fptr(b), fptr(r)))
+    return b, r
+
+
+def scene_dam2d(w, h):
+    b = np.zeros((h, w), np.float32)
+    r = np.zeros((h, w), np.float32)
+    check(lib().efs_scene_dam2d(w, h, fptr(b), fptr(r)))
+    return b, r
+
+
+def scene_batch2d(seed):
+    s = ctypes.c_int()
+    check(lib().efs_scene_batch2d(seed, ctypes.byref(s), None, None, 0))
+    b = np.zeros((s.value, s.value), np.float32)
+    r = np.zeros((s.value, s.value), np.float32)
+    check(lib().efs_scene_batch2d(seed, ctypes.byref(s), fptr(b), fptr(r), b.size))
+    return b, r
+
+
+def params_dam(cell_size, dt, solver=abi.SOLVER_CG, tol_rel=1e-6):
+    """efs_params_dam from the library (the C preset)."""
+    p = abi.EfsParams()
+    lib().efs_params_dam(ctypes.byref(p), cell_size, dt, solver, tol_rel)
+    return p

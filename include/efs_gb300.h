@@ -181,13 +181,21 @@ int  efs_get_stats(efs_ctx* ctx, efs_stats* out);
 /* FP64 sum of rho over all cells (StatsView total, Grid3D.cpp:44-47 in float). */
 int  efs_total_mass(efs_ctx* ctx, double* out);
 
+/* Number of kernel launches one efs_step replays for the current parameters (kernel nodes of its graph). */
+int  efs_step_kernel_count(efs_ctx* ctx, int* count);
+
 /* ---- timing of the dominant kernel (the pressure solve) over replayed steps ---- */
 /* Arms a pool of `capacity` CUDA event pairs recorded around each pressure-solve launch on the
  * context's stream during efs_step.  capacity 0 disarms. */
 int  efs_solve_timing_arm(efs_ctx* ctx, int capacity);
-/* Number of recorded launches, their summed device time (ms) and summed solver iterations. */
-int  efs_solve_timing_read(efs_ctx* ctx, int* launches, double* total_ms, int64_t* total_iterations,
-                           int64_t* total_active_cells);
+/* Number of recorded launches and their summed device time (ms); the work those solves did since arming:
+ * the sum of iterations x matrix rows, and the sum of matrix rows (one per solve set-up). */
+int  efs_solve_timing_read(efs_ctx* ctx, int* launches, double* total_ms, double* row_iterations,
+                           double* row_setups);
+
+/* CUDA events on the context's stream: record slot (0..7); elapsed ms between two recorded slots (waits). */
+int  efs_timer_mark(efs_ctx* ctx, int slot);
+int  efs_timer_elapsed(efs_ctx* ctx, int slot_begin, int slot_end, double* ms);
 
 /* ---- host-only helpers (no device needed) ---- */
 /* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */
