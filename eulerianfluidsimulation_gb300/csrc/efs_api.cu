@@ -41,7 +41,9 @@ bool params_valid(const efs_params* p, std::string& why) {
 
 void drop_graphs(efs_ctx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : c->graph_defs) cudaGraphDestroy(kv.second);
     c->graphs.clear();
+    c->graph_defs.clear();
     c->timing_nodes_begin.clear();
     c->timing_nodes_end.clear();
     c->kernel_nodes.clear();
@@ -99,9 +101,9 @@ int build_graph(efs_ctx* c, const efs::GraphKey& key, cudaGraphExec_t* out) {
     }
     cudaGraphExec_t exec = nullptr;
     cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) return cuda_fail(c, ie, "cudaGraphInstantiate");
+    if (ie != cudaSuccess) { cudaGraphDestroy(graph); return cuda_fail(c, ie, "cudaGraphInstantiate"); }
     c->graphs[key] = exec;
+    c->graph_defs[key] = graph;
     c->kernel_nodes[key] = kernels;
     *out = exec;
     return EFS_OK;

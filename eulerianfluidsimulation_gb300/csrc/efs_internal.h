@@ -118,6 +118,7 @@ struct efs_ctx {
     efs::DevCtl* ctl_host = nullptr;        // pinned
 
     std::map<efs::GraphKey, cudaGraphExec_t> graphs;
+    std::map<efs::GraphKey, cudaGraph_t> graph_defs;    // kept alive: their node handles address the exec nodes
     std::map<efs::GraphKey, cudaGraphNode_t> timing_nodes_begin, timing_nodes_end;
     std::map<efs::GraphKey, int> kernel_nodes;
 

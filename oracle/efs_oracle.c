@@ -344,14 +344,19 @@ static void add_forward3(orc_grid* g, int32_t i, int32_t j, float val) {
     fent_push(g, i, j, val);
 }
 
-/* iterate every entry (i, j, &val) of A: backward rows in cell order, then forward entries */
+/* iterate every entry (i, j, &val) of A: backward rows in cell order, then forward entries; with
+ * ORC_REVERSE_SUMS the exact reverse order (a summation-order perturbation for drift bounds) */
 #define FOR_ENTRIES3(g, BODY) do { \
     const size_t W_ = (g)->W, WH_ = (size_t)(g)->W * (g)->H; \
-    for (size_t i_ = 0; i_ < (g)->N; i_++) { const int32_t b_ = (g)->bbase[i_]; if (b_ < 0) continue; \
-        for (int k_ = 0; k_ < 8; k_++) { const size_t ci = i_; \
+    const int rev_ = ((g)->mode & ORC_REVERSE_SUMS) != 0; \
+    if (rev_) for (size_t e2_ = (g)->nf; e2_-- > 0;) { const size_t ci = (size_t)(g)->fent[e2_].i, cj = (size_t)(g)->fent[e2_].j; \
+        float* cv = &(g)->fent[e2_].val; (void)ci; (void)cj; BODY } \
+    for (size_t t_ = 0; t_ < (g)->N; t_++) { const size_t i_ = rev_ ? (g)->N - 1 - t_ : t_; \
+        const int32_t b_ = (g)->bbase[i_]; if (b_ < 0) continue; \
+        for (int q_ = 0; q_ < 8; q_++) { const int k_ = rev_ ? 7 - q_ : q_; const size_t ci = i_; \
             const size_t cj = (size_t)b_ + (k_ & 1) + ((k_ >> 1) & 1) * W_ + ((k_ >> 2) & 1) * WH_; \
             float* cv = &(g)->wb[i_ * 8 + k_]; (void)ci; (void)cj; BODY } } \
-    for (size_t e_ = 0; e_ < (g)->nf; e_++) { const size_t ci = (size_t)(g)->fent[e_].i, cj = (size_t)(g)->fent[e_].j; \
+    if (!rev_) for (size_t e_ = 0; e_ < (g)->nf; e_++) { const size_t ci = (size_t)(g)->fent[e_].i, cj = (size_t)(g)->fent[e_].j; \
         float* cv = &(g)->fent[e_].val; (void)ci; (void)cj; BODY } } while (0)
 
 /* R3:113-364 Chentanez-Mueller density advection */
@@ -998,10 +1003,15 @@ static void add_forward2(orc_grid* g, int32_t i, int32_t j, float val) {
 
 #define FOR_ENTRIES2(g, BODY) do { \
     const size_t W_ = (g)->W; \
-    for (size_t i_ = 0; i_ < (g)->N; i_++) { const int32_t b_ = (g)->bbase[i_]; if (b_ < 0) continue; \
-        for (int k_ = 0; k_ < 4; k_++) { const size_t ci = i_; const size_t cj = (size_t)b_ + (k_ & 1) + ((k_ >> 1) & 1) * W_; \
+    const int rev_ = ((g)->mode & ORC_REVERSE_SUMS) != 0; \
+    if (rev_) for (size_t e2_ = (g)->nf; e2_-- > 0;) { const size_t ci = (size_t)(g)->fent[e2_].i, cj = (size_t)(g)->fent[e2_].j; \
+        float* cv = &(g)->fent[e2_].val; (void)ci; (void)cj; BODY } \
+    for (size_t t_ = 0; t_ < (g)->N; t_++) { const size_t i_ = rev_ ? (g)->N - 1 - t_ : t_; \
+        const int32_t b_ = (g)->bbase[i_]; if (b_ < 0) continue; \
+        for (int q_ = 0; q_ < 4; q_++) { const int k_ = rev_ ? 3 - q_ : q_; const size_t ci = i_; \
+            const size_t cj = (size_t)b_ + (k_ & 1) + ((k_ >> 1) & 1) * W_; \
             float* cv = &(g)->wb[i_ * 4 + k_]; (void)ci; (void)cj; BODY } } \
-    for (size_t e_ = 0; e_ < (g)->nf; e_++) { const size_t ci = (size_t)(g)->fent[e_].i, cj = (size_t)(g)->fent[e_].j; \
+    if (!rev_) for (size_t e_ = 0; e_ < (g)->nf; e_++) { const size_t ci = (size_t)(g)->fent[e_].i, cj = (size_t)(g)->fent[e_].j; \
         float* cv = &(g)->fent[e_].val; (void)ci; (void)cj; BODY } } while (0)
 
 /* R2:122-318 */

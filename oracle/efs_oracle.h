@@ -22,6 +22,8 @@
  *   - ORC_SHARPEN_PARALLEL applies all density changes, traces every active cell on that field, then
  *     scatters in cell order (the GPU's semantics); the default is the reference's sequential loop
  *     (CPUSimulator3D.cpp:446-455).
+ *   - ORC_REVERSE_SUMS sums the advection matrix in exactly the reverse entry order: a summation-order
+ *     perturbation used to ground multi-step drift bounds (oracle against perturbed oracle).
  *   - When params.tol_rel > 0 the solver threshold is (float)(tol_rel^2 * b.b) of the current right-hand
  *     side (FLT_MIN if that is 0), used both by the solver and by project's convergence check.
  */
@@ -38,6 +40,7 @@ extern "C" {
 
 #define ORC_DOTS_FP64 1
 #define ORC_SHARPEN_PARALLEL 2
+#define ORC_REVERSE_SUMS 4
 
 typedef struct orc_grid orc_grid;
 

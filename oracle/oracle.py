@@ -22,6 +22,7 @@ REFERENCE_TREE = "/root/reference"
 
 DOTS_FP64 = 1
 SHARPEN_PARALLEL = 2
+REVERSE_SUMS = 4
 
 
 def build(reference=True):

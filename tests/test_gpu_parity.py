@@ -131,30 +131,87 @@ def test_solver_against_fp64(dim, n):
     assert o.relres_fp64(p) < 3 * o.relres_fp64(pstar.astype(np.float32)) + 1e-6
 
 
-@pytest.mark.parametrize("dim,n,steps", [(3, 32, 1), (3, 32, 10), (2, 128, 1), (2, 128, 10)])
-def test_steps_match_oracle(dim, n, steps):
-    """Whole steps through the captured graph: fields within 1e-5 after 1 step; within the stated drift bound
-    after 10 (1e-4 for the velocity field, labels identical away from ties)."""
+def run_pair(dim, n, steps, extra_mode=0):
     prm = make_params(dim, n)
     prm.disable_mask = 1 << abi.STAGE_VEL_DECAY
     b, r = scene(dim, n)
-    o = oracle.Oracle(dim, n, n, n, prm, mode=GPU_MODE)
+    o = oracle.Oracle(dim, n, n, n, prm, mode=GPU_MODE | extra_mode)
     o.set_field(abi.FIELD_BOUNDARY, b)
     o.set_field(abi.FIELD_RHO, r)
+    return prm, b, r, o
+
+
+@pytest.mark.parametrize("dim,n", [(3, 32), (2, 128)])
+def test_one_step_matches_oracle(dim, n):
+    """One whole step through the captured graph: u/v/w, rho, gamma, p within relative L2 1e-5; labels and
+    flags identical."""
+    prm, b, r, o = run_pair(dim, n, 1)
+    with gpu_sim(dim, n, prm) as s:
+        s.set_field(abi.FIELD_BOUNDARY, b)
+        s.set_field(abi.FIELD_RHO, r)
+        s.update(1)
+        o.step(1)
+        got, want = s.fields(), o.fields()
+        st = s.stats()
+    assert st.frames == 1 and not st.paused and st.converged
+    assert_fields(got, want, 1e-5, fields=(abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_PRESSURE, abi.FIELD_GAMMA), what="1 step")
+    assert np.array_equal(labels(got[abi.FIELD_RHO]), labels(want[abi.FIELD_RHO]))
+    assert np.array_equal(got[abi.FIELD_BOUNDARY], want[abi.FIELD_BOUNDARY])
+
+
+@pytest.mark.parametrize("dim,n,steps", [(3, 32, 12), (2, 96, 12)])
+def test_every_stage_exact_along_gpu_trajectory(dim, n, steps):
+    """After `steps` GPU steps, each stage run from that GPU state matches the oracle run from the same state:
+    bit-exact, except rho_advect's atomically summed fields (relative L2 1e-6)."""
+    prm, b, r, _ = run_pair(dim, n, steps)
     with gpu_sim(dim, n, prm) as s:
         s.set_field(abi.FIELD_BOUNDARY, b)
         s.set_field(abi.FIELD_RHO, r)
         s.update(steps)
-        o.step(steps)
+        state = s.fields()
+        for stage in range(abi.STAGE_COUNT):
+            s.set_fields(state)
+            o = oracle.Oracle(dim, n, n, n, prm, mode=GPU_MODE)
+            o.set_fields(state)
+            s.stage(stage)
+            o.stage(stage)
+            got, want = s.fields(), o.fields()
+            if stage == abi.STAGE_RHO_ADVECT:
+                assert_fields(got, want, 1e-6, fields=(abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA), what="advect")
+                assert_fields(got, want, 0, fields=(abi.FIELD_VEL, abi.FIELD_PRESSURE), what="advect")
+            else:
+                assert_fields(got, want, 0, what=abi.STAGE_NAMES[stage])
+
+
+# Stated drift bounds after 200 steps (relative L2 of u/v/w, rho, p against the oracle on the same seeded
+# scene).  The step is chaotic at this level: the oracle itself, with only the summation order of its
+# advection matrix reversed, drifts by 1.6e-2 (3D 32^3) after 200 steps, because threshold decisions (the
+# sharpen trace stopping at rho = 0.5, the diffusion's exact-equality test) turn last-bit differences into
+# relocated mass.  The bounds are a small multiple of that measured oracle-against-oracle drift.
+DRIFT_200 = {(3, 32): 0.1, (2, 128): 1e-3}
+
+
+@pytest.mark.parametrize("dim,n", [(3, 32), (2, 128)])
+def test_drift_after_200_steps(dim, n):
+    prm, b, r, o = run_pair(dim, n, 200)
+    with gpu_sim(dim, n, prm) as s:
+        s.set_field(abi.FIELD_BOUNDARY, b)
+        s.set_field(abi.FIELD_RHO, r)
+        m0 = s.total_mass()
+        s.update(200)
+        o.step(200)
         got, want = s.fields(), o.fields()
         st = s.stats()
-    assert st.frames == steps and not st.paused
-    tol = 1e-5 if steps == 1 else 1e-4
-    assert_fields(got, want, tol, fields=(abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_PRESSURE, abi.FIELD_GAMMA), what=f"{steps} steps")
-    lg, lw = labels(got[abi.FIELD_RHO]), labels(want[abi.FIELD_RHO])
-    ties = np.abs(want[abi.FIELD_RHO] - 0.5) < 1e-5
-    assert np.array_equal(lg[~ties], lw[~ties])
-    assert np.array_equal(got[abi.FIELD_BOUNDARY], want[abi.FIELD_BOUNDARY])
+        m1 = s.total_mass()
+    assert st.frames == 200 and not st.paused
+    for f in (abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_PRESSURE):
+        d = rel_l2(got[f], want[f])
+        print(f"drift {dim}D {n}: {abi.FIELD_NAMES[f]} {d:.3e} (bound {DRIFT_200[(dim, n)]})")
+        assert d <= DRIFT_200[(dim, n)], (abi.FIELD_NAMES[f], d)
+    print(f"mass {m0:.6f} -> {m1:.6f} (rel {(m1 - m0) / m0:.3e}); oracle {o.total_mass():.6f}")
+    assert np.all(np.isfinite(got[abi.FIELD_VEL]))
+    # total liquid mass: the oracle drifts by -8e-7 (3D) / -4e-7 (2D) relative over these 200 steps
+    assert abs(m1 - m0) / m0 < 5e-6
 
 
 @pytest.mark.parametrize("case", ["ref_3d_cg", "ref_2d_jacobi", "ref_2d_cg"])
@@ -182,7 +239,7 @@ def test_stages_match_reference_golden(case):
             assert_fields(got, want, tol, fields=(abi.FIELD_PRESSURE, abi.FIELD_VEL), what=f"{case} project")
 
 
-def test_mass_and_finiteness_over_many_steps():
+def test_mass_and_finiteness_over_30_steps_64cubed():
     n = 64
     prm = make_params(3, n)
     prm.disable_mask = 1 << abi.STAGE_VEL_DECAY
