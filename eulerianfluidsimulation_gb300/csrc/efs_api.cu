@@ -54,6 +54,19 @@ cudaError_t dalloc(T** p, size_t count) {
     return cudaMalloc(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T));
 }
 
+// count elements plus c->halo_cells on each side (zeroed); *p points at element 0
+template <typename T>
+cudaError_t dalloc_halo(efs_ctx* c, T** p, size_t count) {
+    T* base = nullptr;
+    const size_t h = (size_t)c->halo_cells;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&base), (count + 2 * h) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    c->halo_bases.push_back(base);
+    e = cudaMemset(base, 0, (count + 2 * h) * sizeof(T));
+    *p = base + h;
+    return e;
+}
+
 // The launch sequence of one ISimulator::update() (include/simulation/simulator/ISimulator.h:12-38).
 cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
     const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
@@ -179,11 +192,12 @@ void efs_destroy(efs_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
-    void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->div, c->p, c->fx, c->fy, c->fz, c->solid,
+    void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->fx, c->fy, c->fz, c->solid,
                     c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
                     c->sh_idx, c->sh_val, c->sh_end, c->rowinfo, c->chunk_flag, c->chunk_list, c->block_count,
-                    c->r, c->d0, c->d1, c->e, c->p64, c->partials, c->ctl, c->mass_partials};
+                    c->partials, c->ctl, c->mass_partials};
     for (void* b : bufs) if (b) cudaFree(b);
+    for (void* b : c->halo_bases) cudaFree(b);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     for (auto ev : c->ev_begin) cudaEventDestroy(ev);
     for (auto ev : c->ev_end) cudaEventDestroy(ev);
@@ -229,14 +243,17 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
 #define ALLOC(ptr, cnt) if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
     ALLOC(c->u, N); ALLOC(c->v, N); ALLOC(c->w, N);
-    ALLOC(c->rho, N); ALLOC(c->gamma, N); ALLOC(c->beta, N); ALLOC(c->div, N); ALLOC(c->p, N);
+    c->halo_cells = (long long)width * height + 64;
+#define ALLOC_H(ptr, cnt) if ((e = dalloc_halo(c, &(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
+    ALLOC(c->rho, N); ALLOC(c->gamma, N); ALLOC(c->beta, N); ALLOC_H(c->div, N); ALLOC_H(c->p, N);
     ALLOC(c->fx, N); ALLOC(c->fy, N); ALLOC(c->fz, N); ALLOC(c->solid, N);
     ALLOC(c->tvel, 3 * N); ALLOC(c->validA, N); ALLOC(c->validB, N);
     ALLOC(c->wb, K * N); ALLOC(c->wf, K * N); ALLOC(c->bb, N); ALLOC(c->fb, N);
     ALLOC(c->bsum, N); ALLOC(c->gsum, N); ALLOC(c->rho_acc, N);
     ALLOC(c->sh_idx, N); ALLOC(c->sh_val, N); ALLOC(c->sh_end, 3 * N);
     ALLOC(c->rowinfo, N); ALLOC(c->chunk_flag, nchunks); ALLOC(c->chunk_list, nchunks);
-    ALLOC(c->r, N); ALLOC(c->d0, N); ALLOC(c->d1, N); ALLOC(c->e, N); ALLOC(c->p64, N);
+    ALLOC_H(c->r, N); ALLOC_H(c->d0, N); ALLOC_H(c->d1, N); ALLOC_H(c->e, N); ALLOC_H(c->p64, N);
+#undef ALLOC_H
     ALLOC(c->ctl, 1);
     ALLOC(c->mass_partials, 256);
 #undef ALLOC

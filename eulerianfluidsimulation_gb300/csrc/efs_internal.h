@@ -26,6 +26,8 @@ struct DevCtl {
     unsigned bar_count;        // grid barrier arrivals (reset before every solver launch)
     int bar_abort;             // set when a barrier of the current launch gave up (reset before every launch)
     unsigned bar_gen;          // grid barrier generation
+    int pad0;
+    double totals[2][3];       // grid totals published by the last block to reach a reducing barrier
     int error;
     int converged;
     int iterations;
@@ -112,8 +114,13 @@ struct efs_ctx {
     double* partials = nullptr;
     int solver_blocks = 0;
     int solver_threads = 0;
+    size_t solver_smem = 0;
 
     double* mass_partials = nullptr;
+    // arrays read at stencil offsets by the solver carry a halo of halo_cells on each side, so neighbour
+    // addresses of any cell of any active chunk stay inside the allocation without clamping
+    long long halo_cells = 0;
+    std::vector<void*> halo_bases;
     efs::DevCtl* ctl = nullptr;
     efs::DevCtl* ctl_host = nullptr;        // pinned
 

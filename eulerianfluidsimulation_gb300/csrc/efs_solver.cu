@@ -25,54 +25,129 @@ namespace {
 
 constexpr int SOLVER_THREADS = 512;
 constexpr int SOLVER_WARPS = SOLVER_THREADS / 32;
-constexpr long long BARRIER_SPIN_LIMIT = 1LL << 25;   // ~ several seconds with the back-off below
 
-// Grid-wide barrier for a cooperative launch.  Returns false when it (or another block) gave up.
-__device__ bool grid_barrier(DevCtl* ctl) {
+constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;   // 2 s per barrier
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).  Warp 0 of each block takes part; lane 0
+// arrives on the counter.  When `partials`/`slot` are given, the last block to arrive adds every block's
+// partials in block order and publishes the three totals in ctl->totals[slot] before releasing, so the
+// totals are identical in every block and reach them with the release.  Waiting is bounded by time: a
+// block that waits longer than BARRIER_TIMEOUT_NS sets DEV_ERR_BARRIER_TIMEOUT and bar_abort, and every
+// block returns false from then on.
+__device__ bool grid_barrier(DevCtl* ctl, const double* partials = nullptr, int slot = 0) {
     __shared__ int s_ok;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = &ctl->bar_gen;
-        volatile int* vabort = &ctl->bar_abort;
-        const unsigned gen = *vgen;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        unsigned gen = 0, arrived = 0;
+        if (lane == 0) {
+            gen = ld_acquire(&ctl->bar_gen);
+            __threadfence();
+            arrived = atomicAdd(&ctl->bar_count, 1u);
+        }
+        arrived = __shfl_sync(0xffffffffu, arrived, 0);
         __threadfence();
-        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
         int ok = 1;
         if (arrived == gridDim.x - 1) {
-            atomicExch(&ctl->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&ctl->bar_gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*vgen == gen) {
-                if (*vabort) { ok = 0; break; }
-                __nanosleep(40);
-                if (++spins > BARRIER_SPIN_LIMIT) {
-                    atomicOr(&ctl->error, DEV_ERR_BARRIER_TIMEOUT);
-                    atomicExch(&ctl->bar_abort, 1);
-                    ok = 0;
-                    break;
+            if (partials) {
+                const volatile double* src = partials + (size_t)slot * 3 * gridDim.x;
+                double ta = 0, tb = 0, tc = 0;
+                for (int k = lane; k < (int)gridDim.x; k += 32) { ta += src[3 * k]; tb += src[3 * k + 1]; tc += src[3 * k + 2]; }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    ta += __shfl_down_sync(0xffffffffu, ta, o);
+                    tb += __shfl_down_sync(0xffffffffu, tb, o);
+                    tc += __shfl_down_sync(0xffffffffu, tc, o);
+                }
+                if (lane == 0) { ctl->totals[slot][0] = ta; ctl->totals[slot][1] = tb; ctl->totals[slot][2] = tc; }
+            }
+            if (lane == 0) {
+                atomicExch(&ctl->bar_count, 0u);
+                __threadfence();
+                atomicAdd(&ctl->bar_gen, 1u);
+            }
+        } else if (lane == 0) {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            while (ld_acquire(&ctl->bar_gen) == gen) {
+                if ((++spins & 255u) == 0) {
+                    if (*(volatile int*)&ctl->bar_abort) { ok = 0; break; }
+                    if (globaltimer_ns() - t0 > BARRIER_TIMEOUT_NS) {
+                        atomicOr(&ctl->error, DEV_ERR_BARRIER_TIMEOUT);
+                        atomicExch(&ctl->bar_abort, 1);
+                        ok = 0;
+                        break;
+                    }
                 }
             }
         }
-        __threadfence();
-        s_ok = ok;
+        if (lane == 0) {
+            __threadfence();
+            s_ok = ok;
+        }
     }
     __syncthreads();
     return s_ok != 0;
 }
 
-// Block sums of three doubles; thread 0 stores them as this block's partials in `slot`.
-__device__ void block_partials(double a, double b, double c, double* partials, int slot) {
-    __shared__ double s_v[3][SOLVER_WARPS];
+// Dot-product accumulation.  GB300 executes FP64 at a small fraction of its FP32 rate, so per-thread sums are
+// kept as an unevaluated pair of floats (s + c): every product a*b is split exactly into p + e with one FMA,
+// and every addition into s is made exact with TwoSum (Knuth), the rounding error going into c.  The pair
+// carries about 48 significant bits; warps combine pairs with shuffles, and only per-warp partials, block
+// partials and grid totals are FP64.
+struct FSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = s + v;
+        const float z = t - s;
+        c += (s - (t - z)) + (v - z);
+        s = t;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);
+        add(p);
+        c += e;
+    }
+    __device__ __forceinline__ void add_pair(float s2, float c2) {
+        add(s2);
+        c += c2;
+    }
+};
+
+__device__ __forceinline__ FSum warp_sum(FSum v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-        c += __shfl_down_sync(0xffffffffu, c, o);
+        const float s2 = __shfl_down_sync(0xffffffffu, v.s, o);
+        const float c2 = __shfl_down_sync(0xffffffffu, v.c, o);
+        v.add_pair(s2, c2);
     }
+    return v;
+}
+
+// Block sums of two compensated sums and an integer count; thread 0 stores them as this block's partials.
+__device__ void block_partials(FSum a, FSum b, int n, double* partials, int slot) {
+    __shared__ double s_v[3][SOLVER_WARPS];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    n = __reduce_add_sync(0xffffffffu, n);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { s_v[0][warp] = a; s_v[1][warp] = b; s_v[2][warp] = c; }
+    if (lane == 0) {
+        s_v[0][warp] = (double)a.s + (double)a.c;
+        s_v[1][warp] = (double)b.s + (double)b.c;
+        s_v[2][warp] = (double)n;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         double ta = 0, tb = 0, tc = 0;
@@ -108,15 +183,25 @@ __device__ void grid_totals(const double* partials, int slot, double& a, double&
 struct Reduction {
     double* partials;
     int slot;
-    __device__ bool run(DevCtl* ctl, double a, double b, double c, double& ta, double& tb, double& tc);
+    __device__ bool run(DevCtl* ctl, FSum a, FSum b, int n, double& ta, double& tb, double& tc) {
+        block_partials(a, b, n, partials, slot);
+        if (!grid_barrier(ctl, partials, slot)) return false;
+        const volatile double* t = ctl->totals[slot];
+        ta = t[0]; tb = t[1]; tc = t[2];
+        slot ^= 1;
+        return true;
+    }
 };
 
-__device__ bool Reduction::run(DevCtl* ctl, double a, double b, double c, double& ta, double& tb, double& tc) {
-    block_partials(a, b, c, partials, slot);
-    if (!grid_barrier(ctl)) return false;
-    grid_totals(partials, slot, ta, tb, tc);
-    slot ^= 1;
-    return true;
+// A float computed by thread 0 from the grid totals and read by the whole block (keeps the FP64 divisions of
+// alpha = rr / dt and beta = rr / rr_old to one thread per block).
+__device__ __forceinline__ float block_scalar(float v_thread0) {
+    __shared__ float s_scalar;
+    if (threadIdx.x == 0) s_scalar = v_thread0;
+    __syncthreads();
+    const float v = s_scalar;
+    __syncthreads();
+    return v;
 }
 
 // Neighbour order of the reference matrix-vector product: x-1, x+1, y-1, y+1, z+1, z-1 (CGSolver.cpp:489-494)
@@ -166,17 +251,118 @@ __device__ __forceinline__ double lap_df(const float* x, uint16_t info, int i, c
     return sum - (double)((info >> 8) & 7) * (double)x[i];
 }
 
-// Iterate over this block's share of the active chunks: f(cell index) for every matrix row (rows only) or
-// every in-range cell (all).
+// This block's share of the active chunks, cached in shared memory for the whole solve (the compacted list
+// does not change between iterations).
+struct Chunks {
+    const int* ids;   // shared memory
+    int n;
+};
+
+// Iterate over this block's chunks: f(cell index) for every in-range cell.
 template <typename F>
-__device__ __forceinline__ void for_rows(const SolverArgs& a, int m, F f) {
-    const int per = (m + gridDim.x - 1) / gridDim.x;
-    const int c0 = blockIdx.x * per, c1 = min(m, c0 + per);
+__device__ __forceinline__ void for_rows(const SolverArgs& a, const Chunks& ch, F f) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = c0 + warp; c < c1; c += SOLVER_WARPS) {
-        const int i = a.chunk_list[c] * 32 + lane;
+    for (int c = warp; c < ch.n; c += SOLVER_WARPS) {
+        const int i = ch.ids[c] * 32 + lane;
         if (i < a.g.N) f(i);
     }
+}
+
+// The two hot phases of a CG iteration process U chunks per warp at once.  Neighbour addresses do not
+// depend on rowinfo (they are clamped into the grid and only summed where the row's bits say so), so all
+// loads of the U cells are independent and in flight together.
+constexpr int U = 2;
+
+// Phase A: d = beta * d_prev + r (it > 0) or d (it == 0), t = L d (reference float rounding), sum d.t.
+__device__ __forceinline__ FSum phase_a(const SolverArgs& a, const Chunks& ch, int it, float beta,
+                                        const float* __restrict__ dprev, float* __restrict__ dcur, const Nb& nb) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = 0, c1 = ch.n;
+    const int N = a.g.N;
+    const float* __restrict__ r = a.r;
+    FSum acc;
+    for (int cb = c0 + warp * U; cb < c1; cb += SOLVER_WARPS * U) {
+        int idx[U];
+        uint16_t f[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int c = cb + u;
+            idx[u] = (c < c1) ? ch.ids[c] * 32 + lane : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        float xv[U][7], rv[U][7];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = idx[u] < 0 ? 0 : idx[u];   // the vectors carry a halo: i + offset stays allocated
+            xv[u][6] = (it == 0) ? dcur[i] : dprev[i];
+            if (it != 0) rv[u][6] = r[i];
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                const int j = i + nb.o[k];
+                xv[u][k] = (it == 0) ? dcur[j] : dprev[j];
+                if (it != 0) rv[u][k] = r[j];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (!(f[u] & 0x8000u)) continue;
+            float sum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (f[u] & (1u << cg_bit(k))) sum += (it == 0) ? xv[u][k] : xv[u][k] * beta + rv[u][k];
+            const float di = (it == 0) ? xv[u][6] : xv[u][6] * beta + rv[u][6];
+            const float t = sum - (float)((f[u] >> 8) & 7) * di;
+            if (it != 0) dcur[idx[u]] = di;
+            acc.add_prod(di, t);
+        }
+    }
+    return acc;
+}
+
+// Phase B: x += alpha d (x = e or p), r += (-alpha) L d, sum r.r.
+__device__ __forceinline__ FSum phase_b(const SolverArgs& a, const Chunks& ch, float alpha, const float* __restrict__ dcur,
+                                        float* __restrict__ x, const Nb& nb) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = 0, c1 = ch.n;
+    const int N = a.g.N;
+    float* __restrict__ r = a.r;
+    FSum acc;
+    for (int cb = c0 + warp * U; cb < c1; cb += SOLVER_WARPS * U) {
+        int idx[U];
+        uint16_t f[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int c = cb + u;
+            idx[u] = (c < c1) ? ch.ids[c] * 32 + lane : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        float dv[U][7], xo[U], ro[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = idx[u] < 0 ? 0 : idx[u];
+            dv[u][6] = dcur[i];
+            xo[u] = x[i];
+            ro[u] = r[i];
+#pragma unroll
+            for (int k = 0; k < 6; k++) dv[u][k] = dcur[i + nb.o[k]];
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (!(f[u] & 0x8000u)) continue;
+            float sum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (f[u] & (1u << cg_bit(k))) sum += dv[u][k];
+            const float t = sum - (float)((f[u] >> 8) & 7) * dv[u][6];
+            x[idx[u]] = xo[u] + alpha * dv[u][6];
+            const float ri = ro[u] + (-alpha) * t;
+            r[idx[u]] = ri;
+            acc.add_prod(ri, ri);
+        }
+    }
+    return acc;
 }
 
 __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
@@ -229,6 +415,16 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     }
     const int M = s_total;
     if (!grid_barrier(ctl)) return;
+    extern __shared__ int s_chunks[];
+    Chunks ch;
+    {
+        const int per = (M + gridDim.x - 1) / gridDim.x;
+        const int c0 = blockIdx.x * per, c1 = min(M, c0 + per);
+        ch.ids = s_chunks;
+        ch.n = max(0, c1 - c0);
+        for (int k = threadIdx.x; k < ch.n; k += SOLVER_THREADS) s_chunks[k] = ((volatile int*)a.chunk_list)[c0 + k];
+        __syncthreads();
+    }
 
     const Nb nb = cg_order(a.g);
     const float* __restrict__ b = a.b;
@@ -241,14 +437,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     if (a.solver == EFS_SOLVER_JACOBI) {
         const int iters = a.max_steps / 2;
         const int jo[6] = {-1, 1, -a.g.W, a.g.W, -a.g.WH, a.g.WH};
-        double rows = 0;
-        for_rows(a, M, [&](int i) { if (info[i] & 0x8000u) rows += 1.0; });
+        int rows = 0;
+        for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) rows += 1; });
         double nrows;
-        if (!red.run(ctl, rows, 0.0, 0.0, nrows, u1, u2)) return;
+        if (!red.run(ctl, FSum(), FSum(), rows, u1, u2, nrows)) return;
         for (int it = 0; it < iters; it++) {
             const float* src = (it & 1) ? a.e : a.p;
             float* dst = (it & 1) ? a.p : a.e;
-            for_rows(a, M, [&](int i) {
+            for_rows(a, ch, [&](int i) {
                 const uint16_t f = info[i];
                 if (!(f & 0x8000u)) return;
                 float sum = 0.0f;
@@ -261,7 +457,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
             if (!grid_barrier(ctl)) return;
         }
         if (iters & 1) {
-            for_rows(a, M, [&](int i) { if (info[i] & 0x8000u) a.p[i] = a.e[i]; });
+            for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) a.p[i] = a.e[i]; });
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctl->converged = 1; ctl->iterations = iters; ctl->rr = 0; ctl->bb = 0; ctl->thr = 0;
@@ -282,13 +478,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     // initial residual r = b - L p0 with p0 = b (CGSolver.cpp:425-434); d = r
     double rr, bb, nrows;
     {
-        double rr_p = 0, bb_p = 0, rows = 0;
-        for_rows(a, M, [&](int i) {
+        FSum rr_p, bb_p;
+        int rows = 0;
+        for_rows(a, ch, [&](int i) {
             const float bi = b[i];
-            bb_p += (double)bi * (double)bi;
+            bb_p.add_prod(bi, bi);
             const uint16_t f = info[i];
             if (!(f & 0x8000u)) return;
-            rows += 1.0;
+            rows += 1;
             float ri;
             if (mixed) {
                 p64[i] = (double)bi;
@@ -299,7 +496,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
             }
             r[i] = ri;
             a.d0[i] = ri;
-            rr_p += (double)ri * (double)ri;
+            rr_p.add_prod(ri, ri);
         });
         if (!red.run(ctl, rr_p, bb_p, rows, rr, bb, nrows)) return;
     }
@@ -316,22 +513,22 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     // r = b - L p in FP32 (reference)
     auto replace = [&](double& rr_out) -> bool {
         if (mixed) {
-            for_rows(a, M, [&](int i) {
+            for_rows(a, ch, [&](int i) {
                 if (!(info[i] & 0x8000u)) return;
                 p64[i] += (double)e[i];
                 e[i] = 0.f;
             });
         }
         if (!grid_barrier(ctl)) return false;
-        double rp = 0;
-        for_rows(a, M, [&](int i) {
+        FSum rp;
+        for_rows(a, ch, [&](int i) {
             const uint16_t f = info[i];
             if (!(f & 0x8000u)) return;
             const float ri = mixed ? (float)((double)b[i] - lap_d(p64, f, i, nb)) : b[i] - lap_f(p, f, i, nb);
             r[i] = ri;
-            rp += (double)ri * (double)ri;
+            rp.add_prod(ri, ri);
         });
-        return red.run(ctl, rp, 0.0, 0.0, rr_out, u1, u2);
+        return red.run(ctl, rp, FSum(), 0, rr_out, u1, u2);
     };
 
     int conv = rr < thr;
@@ -343,36 +540,18 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
             float* dcur = (it & 1) ? a.d1 : a.d0;
             const float* dprev = (it & 1) ? a.d0 : a.d1;
             // A: d = beta d + r (it > 0; CGSolver.cpp:458-460), t = L d, d.t
-            double dt_p = 0;
-            for_rows(a, M, [&](int i) {
-                const uint16_t f = info[i];
-                if (!(f & 0x8000u)) return;
-                float di, t;
-                if (it == 0) { di = dcur[i]; t = lap_f(dcur, f, i, nb); }
-                else { t = lap_dir(dprev, r, beta, f, i, nb, di); dcur[i] = di; }
-                dt_p += (double)di * (double)t;
-            });
+            const FSum dt_p = phase_a(a, ch, it, beta, dprev, dcur, nb);
             double dt;
-            if (!red.run(ctl, dt_p, 0.0, 0.0, dt, u1, u2)) return;
-            const float alpha = (float)(rr / dt);
+            if (!red.run(ctl, dt_p, FSum(), 0, dt, u1, u2)) return;
+            const float alpha = block_scalar(threadIdx.x == 0 ? (float)(rr / dt) : 0.f);
             // B: p (or e) += alpha d; r -= alpha L d, or the true residual every 64 iterations (:442-451)
             const double old = rr;
             bool replaced = false;
             if (it & 0x3F) {
-                double rp = 0;
-                for_rows(a, M, [&](int i) {
-                    const uint16_t f = info[i];
-                    if (!(f & 0x8000u)) return;
-                    const float di = dcur[i];
-                    if (mixed) e[i] += alpha * di; else p[i] += alpha * di;
-                    const float t = lap_f(dcur, f, i, nb);
-                    const float ri = r[i] + (-alpha) * t;
-                    r[i] = ri;
-                    rp += (double)ri * (double)ri;
-                });
-                if (!red.run(ctl, rp, 0.0, 0.0, rr, u1, u2)) return;
+                const FSum rp = phase_b(a, ch, alpha, dcur, mixed ? e : p, nb);
+                if (!red.run(ctl, rp, FSum(), 0, rr, u1, u2)) return;
             } else {
-                for_rows(a, M, [&](int i) {
+                for_rows(a, ch, [&](int i) {
                     if (!(info[i] & 0x8000u)) return;
                     if (mixed) e[i] += alpha * dcur[i]; else p[i] += alpha * dcur[i];
                 });
@@ -386,12 +565,12 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
                 }
                 if (rr < thr) { conv = 1; break; }
             }
-            beta = (float)(rr / old);
+            beta = block_scalar(threadIdx.x == 0 ? (float)(rr / old) : 0.f);
         }
         iters = it + 1;
     }
     if (mixed) {
-        for_rows(a, M, [&](int i) {
+        for_rows(a, ch, [&](int i) {
             if (!(info[i] & 0x8000u)) return;
             p[i] = (float)(p64[i] + (double)e[i]);
         });
@@ -415,17 +594,23 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
 
 cudaError_t solver_configure(efs_ctx* c) {
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, 0);
+    const int n_chunks = (c->g.N + 31) / 32;
+    // shared memory for the chunk-id cache when every chunk is active and the grid has one block per SM
+    const size_t smem_max = (size_t)((n_chunks + c->sm_count - 1) / c->sm_count) * sizeof(int);
+    cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem_max);
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorLaunchOutOfResources;
-    const int n_chunks = (c->g.N + 31) / 32;
     int blocks = std::min(occ, 2) * c->sm_count;
     // small grids: about four chunks per warp so barrier cost stays proportionate
     const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
     blocks = std::max(1, std::min(blocks, want));
     c->solver_blocks = blocks;
     c->solver_threads = SOLVER_THREADS;
-    return cudaSuccess;
+    c->solver_smem = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
+    return cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::max(c->solver_smem, smem_max));
 }
 
 cudaError_t launch_solver(efs_ctx* c) {
@@ -454,7 +639,7 @@ cudaError_t launch_solver(efs_ctx* c) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c->solver_blocks);
     cfg.blockDim = dim3(SOLVER_THREADS);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = c->solver_smem;
     cfg.stream = c->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

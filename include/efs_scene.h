@@ -10,6 +10,10 @@
  * Geometry: the domain is the unit square / cube; cell (i,j,k) has centre ((i+0.5)/W, (j+0.5)/H, (k+0.5)/D).
  * A cell is solid when it is on the border or its centre lies in an obstacle; liquid when its centre
  * satisfies the fluid predicate and it is not solid (rho = 0 in solids, as Editor.cpp:256 does).
+ * Cavities: non-solid cells that are not connected (through faces of non-solid cells) to the open top row of
+ * the domain (y = H-2) become solid.  Overlapping obstacles can leave such cells; a liquid cell inside one
+ * gives the pressure matrix a row with no free neighbour (or a closed Neumann block), which no solver can
+ * satisfy once its divergence is non-zero, so the reference's project() would pause for good.
  *
  * Random numbers: PCG32 (M. E. O'Neill, "PCG: A Family of Simple Fast Space-Efficient Statistically Good
  * Algorithms for Random Number Generation", 2014), XSH-RR output, 64-bit LCG state with multiplier
@@ -19,7 +23,7 @@
  *
  * Draw order
  *   dam3d:   n = int[n_min, n_max]; then per sphere: cx, cy, cz = U(0.2, 0.8), r = U(0.04, 0.10).
- *            Fluid: x < 0.4 and y < 0.6 (all z).
+ *            Fluid: x < 0.4 and y < 0.6 (all z).  Cavities filled (all generators).
  *   dam2d:   no draws.  Fluid: x < 0.4 and y < 0.6.
  *   batch2d: side = {64, 96, 128, 192, 256}[int[0, 4]]; n_rect = int[1, 4]; per rectangle:
  *            x0 = U(0.05, 0.80), y0 = U(0.05, 0.60), wx = U(0.05, 0.25), wy = U(0.03, 0.15);
@@ -31,6 +35,7 @@
 
 #include <stdint.h>
 #include <stddef.h>
+#include <stdlib.h>
 
 #define EFS_SCENE_STREAM 0x0EF5u
 
@@ -63,6 +68,41 @@ static inline int efs_pcg32_int(efs_pcg32* g, int lo, int hi) {
 
 #define EFS_SCENE_MAX_OBJECTS 64
 
+/* Make every non-solid cell that cannot reach the top interior row through face neighbours solid (rho 0).
+ * Returns the number of cells filled, or -1 when the work queue cannot be allocated. */
+static inline long efs_scene_fill_cavities(int W, int H, int D, float* boundary, float* rho) {
+    const size_t N = (size_t)W * H * D, WH = (size_t)W * H;
+    unsigned char* seen = (unsigned char*)calloc(N, 1);
+    size_t* q = (size_t*)malloc(N * sizeof(size_t));
+    if (!seen || !q) { free(seen); free(q); return -1; }
+    size_t head = 0, tail = 0;
+    const int yt = H - 2;
+    for (int z = 0; z < D; z++)
+    for (int x = 0; x < W; x++) {
+        const size_t i = (size_t)z * WH + (size_t)yt * W + x;
+        if (boundary[i] != 1.0f && !seen[i]) { seen[i] = 1; q[tail++] = i; }
+    }
+    while (head < tail) {
+        const size_t i = q[head++];
+        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / WH);
+        const long nb[6][3] = {{x - 1, y, z}, {x + 1, y, z}, {x, y - 1, z}, {x, y + 1, z}, {x, y, z - 1}, {x, y, z + 1}};
+        for (int k = 0; k < 6; k++) {
+            const long nx = nb[k][0], ny = nb[k][1], nz = nb[k][2];
+            if (nx < 0 || ny < 0 || nz < 0 || nx >= W || ny >= H || nz >= D) continue;
+            const size_t j = (size_t)nz * WH + (size_t)ny * W + (size_t)nx;
+            if (seen[j] || boundary[j] == 1.0f) continue;
+            seen[j] = 1;
+            q[tail++] = j;
+        }
+    }
+    long filled = 0;
+    for (size_t i = 0; i < N; i++)
+        if (boundary[i] != 1.0f && !seen[i]) { boundary[i] = 1.0f; rho[i] = 0.0f; filled++; }
+    free(seen);
+    free(q);
+    return filled;
+}
+
 /* 3D dam break with seeded solid spheres.  Returns the number of spheres, or -1 on bad arguments. */
 static inline int efs_scene_dam3d_fill(int W, int H, int D, int n_min, int n_max, uint64_t seed,
                                        float* boundary, float* rho) {
@@ -91,6 +131,7 @@ static inline int efs_scene_dam3d_fill(int W, int H, int D, int n_min, int n_max
         boundary[i] = solid ? 1.0f : 0.0f;
         rho[i] = (!solid && fluid) ? 1.0f : 0.0f;
     }
+    if (efs_scene_fill_cavities(W, H, D, boundary, rho) < 0) return -1;
     return n;
 }
 
@@ -105,6 +146,7 @@ static inline int efs_scene_dam2d_fill(int W, int H, float* boundary, float* rho
         boundary[i] = solid ? 1.0f : 0.0f;
         rho[i] = (!solid && px < 0.4 && py < 0.6) ? 1.0f : 0.0f;
     }
+    if (efs_scene_fill_cavities(W, H, 1, boundary, rho) < 0) return -1;
     return 0;
 }
 
@@ -148,6 +190,7 @@ static inline int efs_scene_batch2d_fill(uint64_t seed, int* side, float* bounda
         boundary[i] = solid ? 1.0f : 0.0f;
         rho[i] = (!solid && fluid) ? 1.0f : 0.0f;
     }
+    if (efs_scene_fill_cavities(S, S, 1, boundary, rho) < 0) return -1;
     return 0;
 }
 
