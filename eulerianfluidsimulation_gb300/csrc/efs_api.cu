@@ -243,7 +243,7 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
 #define ALLOC(ptr, cnt) if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
     ALLOC(c->u, N); ALLOC(c->v, N); ALLOC(c->w, N);
-    c->halo_cells = (long long)width * height + 64;
+    c->halo_cells = (dim == 3 ? (long long)width * height : (long long)width) + 64;
 #define ALLOC_H(ptr, cnt) if ((e = dalloc_halo(c, &(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
     ALLOC(c->rho, N); ALLOC(c->gamma, N); ALLOC(c->beta, N); ALLOC_H(c->div, N); ALLOC_H(c->p, N);
     ALLOC(c->fx, N); ALLOC(c->fy, N); ALLOC(c->fz, N); ALLOC(c->solid, N);

@@ -14,8 +14,8 @@
 //   - d <- beta d + r is fused into the next matrix-vector product (d is double-buffered), and the
 //     product L d is recomputed in the update phase instead of being stored.
 // EFS_CG_MIXED additionally keeps p as an FP64 accumulator plus an FP32 increment (see efs_gb300.h).
-#include <cooperative_groups.h>
 #include <cfloat>
+#include <mutex>
 
 #include "efs_internal.h"
 
@@ -210,7 +210,12 @@ __device__ __forceinline__ float block_scalar(float v_thread0) {
 struct Nb {
     int o[6];
 };
-__device__ __forceinline__ Nb cg_order(const Geo& g) { return Nb{{-1, 1, -g.W, g.W, g.WH, -g.WH}}; }
+// In 2D (D == 1) the z offsets are 0: rowinfo never sets their bits, and the unconditional loads of the hot
+// phases then stay within one row of halo.
+__device__ __forceinline__ Nb cg_order(const Geo& g) {
+    const int oz = (g.D > 1) ? g.WH : 0;
+    return Nb{{-1, 1, -g.W, g.W, oz, -oz}};
+}
 __device__ __forceinline__ int cg_bit(int k) { return (k == 4) ? 5 : (k == 5 ? 4 : k); }
 
 // L x (float, reference rounding) on row i
@@ -590,6 +595,19 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     }
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel for the whole process: raise it when a grid
+// needs more than the 48 KB default, and never lower it (other contexts may need the larger value).
+std::mutex g_smem_mutex;
+size_t g_smem_limit = 48 * 1024;
+
+cudaError_t ensure_solver_smem(size_t bytes) {
+    std::lock_guard<std::mutex> lock(g_smem_mutex);
+    if (bytes <= g_smem_limit) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) g_smem_limit = bytes;
+    return e;
+}
+
 }  // namespace
 
 cudaError_t solver_configure(efs_ctx* c) {
@@ -597,7 +615,7 @@ cudaError_t solver_configure(efs_ctx* c) {
     const int n_chunks = (c->g.N + 31) / 32;
     // shared memory for the chunk-id cache when every chunk is active and the grid has one block per SM
     const size_t smem_max = (size_t)((n_chunks + c->sm_count - 1) / c->sm_count) * sizeof(int);
-    cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    cudaError_t e = ensure_solver_smem(smem_max);
     if (e != cudaSuccess) return e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem_max);
     if (e != cudaSuccess) return e;
@@ -609,8 +627,7 @@ cudaError_t solver_configure(efs_ctx* c) {
     c->solver_blocks = blocks;
     c->solver_threads = SOLVER_THREADS;
     c->solver_smem = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
-    return cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::max(c->solver_smem, smem_max));
+    return ensure_solver_smem(c->solver_smem);
 }
 
 cudaError_t launch_solver(efs_ctx* c) {
