@@ -43,6 +43,9 @@ SIGNATURES = {
                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "efs_timer_mark": (ctypes.c_int, [_CTX, ctypes.c_int]),
     "efs_timer_elapsed": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "efs_solve_noalloc": (ctypes.c_int, [ctypes.c_int] * 4 + [ctypes.POINTER(EfsParams), ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(EfsStats)]),
+    "efs_noalloc_last_error": (ctypes.c_char_p, []),
     "efs_scene_dam3d": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_uint64, _FP, _FP]),
     "efs_scene_dam2d": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _FP, _FP]),
     "efs_scene_batch2d": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _FP, _FP, ctypes.c_int]),

@@ -22,6 +22,7 @@ UNITS = {
     "efs_fields.cu": ["--fmad=false"],
     "efs_stages.cu": ["--fmad=false"],
     "efs_solver.cu": ["--fmad=false"],
+    "efs_noalloc.cu": ["--fmad=false"],
 }
 
 

@@ -669,4 +669,37 @@ cudaError_t launch_solver(efs_ctx* c) {
     return cudaLaunchKernelEx(&cfg, k_solver, a);
 }
 
+// Launch shape of the solver for a grid of n_chunks 32-cell chunks (the same rule as solver_configure),
+// for callers that hold their own SolverArgs.
+cudaError_t solver_launch_shape(int n_chunks, int sm_count, int* blocks_out, size_t* smem_out) {
+    int occ = 0;
+    const size_t smem_max = (size_t)((n_chunks + sm_count - 1) / sm_count) * sizeof(int);
+    cudaError_t e = ensure_solver_smem(smem_max);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem_max);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorLaunchOutOfResources;
+    int blocks = std::min(occ, 2) * sm_count;
+    const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
+    blocks = std::max(1, std::min(blocks, want));
+    *blocks_out = blocks;
+    *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
+    return ensure_solver_smem(*smem_out);
+}
+
+// Cooperative launch of the solver with caller-provided arguments and shape (no allocation).
+cudaError_t launch_solver_args(const SolverArgs& a, int blocks, size_t smem, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(SOLVER_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_solver, a);
+}
+
 }  // namespace efs

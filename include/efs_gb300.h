@@ -197,6 +197,23 @@ int  efs_solve_timing_read(efs_ctx* ctx, int* launches, double* total_ms, double
 int  efs_timer_mark(efs_ctx* ctx, int slot);
 int  efs_timer_elapsed(efs_ctx* ctx, int slot_begin, int slot_end, double* ms);
 
+/* ---- a pressure solve that allocates nothing ---- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc (a host that owns every device
+ * allocation of its plug-ins, a real-time loop that may not synchronise the device, work recorded into a CUDA
+ * graph): ISolver::solve on caller-owned device buffers rho, boundary, divergence and pressure (N floats each,
+ * reference layout), on `stream` (a cudaStream_t; NULL = the legacy default stream).  Working memory is one
+ * fixed file-scope device array of about 10 MB that every device loading the library keeps until exit, so
+ * grids are limited to EFS_NOALLOC_MAX_CELLS cells and larger ones are rejected with EFS_ERR_ARG.  The first
+ * call on each device looks up that array's address (make it before any stream capture).  All calls share
+ * the array: calls whose work overlaps on the GPU race.  With stats == NULL the call returns after queueing
+ * its work; otherwise it waits for the stream and fills stats (EFS_ERR_NOT_CONVERGED when max_steps ran out).
+ * Errors of this entry point are reported by efs_noalloc_last_error(). */
+#define EFS_NOALLOC_MAX_CELLS 262144
+int  efs_solve_noalloc(int dim, int width, int height, int depth, const efs_params* params,
+                       const float* rho, const float* boundary, const float* divergence, float* pressure,
+                       void* stream, efs_stats* stats);
+const char* efs_noalloc_last_error(void);
+
 /* ---- host-only helpers (no device needed) ---- */
 /* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */
 int  efs_scene_dam3d(int w, int h, int d, int n_spheres_min, int n_spheres_max, uint64_t seed,
