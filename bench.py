@@ -38,7 +38,7 @@ SOLVE_BYTES_PER_ROW_SETUP = 30.0
 # Mean CG iterations per step the CUDA path needs on this workload (measured by the gb300 arm over the first
 # steps of the dam break; printed in its JSON line as cg_iters_per_step).  The CPU-baseline sample times a
 # few CG iterations and scales them to this count instead of solving at 256^3 on one core for minutes.
-CG_ITERS_PER_STEP_REF = 400
+CG_ITERS_PER_STEP_REF = 934
 
 
 def parse():
