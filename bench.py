@@ -30,10 +30,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "steps/s at 256^3 to rel-res 1e-6 (plain CG)"
-# Bytes the pressure solve must move, per matrix row: per CG iteration read d_prev, r, rowinfo and write d
-# (14 B), then read d, e, r, rowinfo and write e, r (22 B); per solve set-up read b, rowinfo and write p64, e,
-# r, d and finally p (30 B).  Neighbour reads of the stencils are cache hits and count 0.
-SOLVE_BYTES_PER_ROW_ITER = 36.0
+# Bytes the pressure solve must move, per matrix row (CG in its recurrence form, the default variant): per
+# iteration read d, rowinfo and write t = L d (10 B), then read d, t, e, r, rowinfo and write e, r, d (30 B);
+# per solve set-up read b, rowinfo and write p64, e, r, d and finally p (30 B).  Neighbour reads of the stencil
+# are cache hits and count 0.
+SOLVE_BYTES_PER_ROW_ITER = 40.0
 SOLVE_BYTES_PER_ROW_SETUP = 30.0
 # Mean CG iterations per step the CUDA path needs on this workload (measured by the gb300 arm over the first
 # steps of the dam break; printed in its JSON line as cg_iters_per_step).  The CPU-baseline sample times a

@@ -22,6 +22,7 @@ SOLVER_CG = 1
 
 CG_MIXED = 0
 CG_REFERENCE = 1
+CG_MIXED_RECURRENCE = 2
 
 FIELD_VEL = 0
 FIELD_RHO = 1
@@ -115,7 +116,7 @@ def params_default():
     p.disable_mask = 0
     p.re_calc_div = 0
     p.sharpen_mode = 0
-    p.cg_variant = CG_MIXED
+    p.cg_variant = CG_MIXED_RECURRENCE
     return p
 
 

@@ -32,7 +32,10 @@ bool params_valid(const efs_params* p, std::string& why) {
     if (!p) { why = "params is NULL"; return false; }
     if (!std::isfinite(p->dt) || !std::isfinite(p->gravity_force)) { why = "dt and gravity_force must be finite"; return false; }
     if (p->solver != EFS_SOLVER_JACOBI && p->solver != EFS_SOLVER_CG) { why = "unknown solver"; return false; }
-    if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE) { why = "unknown cg_variant"; return false; }
+    if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE && p->cg_variant != EFS_CG_MIXED_RECURRENCE) {
+        why = "unknown cg_variant";
+        return false;
+    }
     if (p->sharpen_mode != EFS_SHARPEN_PARALLEL) { why = "unknown sharpen_mode"; return false; }
     if (p->max_steps < 0) { why = "max_steps must be >= 0"; return false; }
     if (p->disable_mask & ~EFS_STAGES_ALL) { why = "disable_mask has bits beyond the seven stages"; return false; }
@@ -160,7 +163,7 @@ void efs_params_default(efs_params* p) {
     p->disable_mask = 0;
     p->re_calc_div = 0;
     p->sharpen_mode = EFS_SHARPEN_PARALLEL;
-    p->cg_variant = EFS_CG_MIXED;
+    p->cg_variant = EFS_CG_MIXED_RECURRENCE;
 }
 
 void efs_params_dam(efs_params* p, float cell_size, float dt, int solver, float tol_rel) {
@@ -252,7 +255,7 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
     ALLOC(c->bsum, N); ALLOC(c->gsum, N); ALLOC(c->rho_acc, N);
     ALLOC(c->sh_idx, N); ALLOC(c->sh_val, N); ALLOC(c->sh_end, 3 * N);
     ALLOC(c->rowinfo, N); ALLOC(c->chunk_flag, nchunks); ALLOC(c->chunk_list, nchunks);
-    ALLOC_H(c->r, N); ALLOC_H(c->d0, N); ALLOC_H(c->d1, N); ALLOC_H(c->e, N); ALLOC_H(c->p64, N);
+    ALLOC_H(c->r, N); ALLOC_H(c->d0, N); ALLOC_H(c->d1, N); ALLOC_H(c->e, N); ALLOC_H(c->p64, N); ALLOC_H(c->t, N);
 #undef ALLOC_H
     ALLOC(c->ctl, 1);
     ALLOC(c->mass_partials, 256);

@@ -63,6 +63,7 @@ struct SolverArgs {
     float* r;
     float* d0;
     float* d1;
+    float* t;                  // L d of the current iteration (EFS_CG_MIXED_RECURRENCE)
     double* partials;          // 2 slots x 3 values per block
     DevCtl* ctl;
 };
@@ -109,7 +110,7 @@ struct efs_ctx {
     uint8_t* chunk_flag = nullptr;
     int* chunk_list = nullptr;
     int* block_count = nullptr;
-    float *r = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr;
+    float *r = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr, *t = nullptr;
     double* p64 = nullptr;
     double* partials = nullptr;
     int solver_blocks = 0;

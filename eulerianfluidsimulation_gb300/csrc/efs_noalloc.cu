@@ -46,9 +46,10 @@ constexpr size_t kOffD1 = align256(kOffD0 + kVec * sizeof(float));
 constexpr size_t kOffE = align256(kOffD1 + kVec * sizeof(float));
 constexpr size_t kOffP = align256(kOffE + kVec * sizeof(float));
 constexpr size_t kOffP64 = align256(kOffP + kVec * sizeof(float));
-constexpr size_t kScratchBytes = align256(kOffP64 + kVec * sizeof(double));
+constexpr size_t kOffT = align256(kOffP64 + kVec * sizeof(double));
+constexpr size_t kScratchBytes = align256(kOffT + kVec * sizeof(float));
 
-// The solver's working memory: about 10 MB, zero at load, shared by every call on a device.
+// The solver's working memory: about 12 MB, zero at load, shared by every call on a device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // Host code cannot use g_noalloc_scratch as an address: its device address is looked up once per device.
@@ -114,7 +115,9 @@ extern "C" int efs_solve_noalloc(int dim, int width, int height, int depth, cons
     if (halo > kMaxHalo) return nfail(EFS_ERR_ARG, "grid planes too large for the fixed solver scratch");
     if (!params || !rho || !boundary || !divergence || !pressure) return nfail(EFS_ERR_ARG, "NULL argument");
     if (params->solver != EFS_SOLVER_JACOBI && params->solver != EFS_SOLVER_CG) return nfail(EFS_ERR_ARG, "unknown solver");
-    if (params->cg_variant != EFS_CG_MIXED && params->cg_variant != EFS_CG_REFERENCE) return nfail(EFS_ERR_ARG, "unknown cg_variant");
+    if (params->cg_variant != EFS_CG_MIXED && params->cg_variant != EFS_CG_REFERENCE &&
+        params->cg_variant != EFS_CG_MIXED_RECURRENCE)
+        return nfail(EFS_ERR_ARG, "unknown cg_variant");
     if (params->max_steps < 0) return nfail(EFS_ERR_ARG, "max_steps must be >= 0");
 
     int dev = 0;
@@ -170,6 +173,7 @@ extern "C" int efs_solve_noalloc(int dim, int width, int height, int depth, cons
     a.e = reinterpret_cast<float*>(base + kOffE) + kMaxHalo;
     a.p = p_s;
     a.p64 = reinterpret_cast<double*>(base + kOffP64) + kMaxHalo;
+    a.t = reinterpret_cast<float*>(base + kOffT) + kMaxHalo;
     a.ctl = ctl;
 
     if ((e = cudaMemsetAsync(ctl, 0, sizeof(DevCtl), st)) != cudaSuccess) return nfail(EFS_ERR_CUDA, cudaGetErrorString(e));

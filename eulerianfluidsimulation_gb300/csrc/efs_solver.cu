@@ -370,7 +370,97 @@ __device__ __forceinline__ FSum phase_b(const SolverArgs& a, const Chunks& ch, f
     return acc;
 }
 
-__global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
+// EFS_CG_MIXED_RECURRENCE, pass 1: t = L d (reference float rounding), stored; sums d.t and t.t.
+constexpr int UA = 4;
+__device__ __forceinline__ void phase_t(const SolverArgs& a, const Chunks& ch, const float* __restrict__ d,
+                                        float* __restrict__ tout, const Nb& nb, FSum& dt, FSum& tt) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = a.g.N;
+    for (int cb = warp * UA; cb < ch.n; cb += SOLVER_WARPS * UA) {
+        int idx[UA];
+        uint16_t f[UA];
+#pragma unroll
+        for (int u = 0; u < UA; u++) idx[u] = (cb + u < ch.n) ? ch.ids[cb + u] * 32 + lane : -1;
+#pragma unroll
+        for (int u = 0; u < UA; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        float xv[UA][7];
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            const int i = idx[u] < 0 ? 0 : idx[u];
+            xv[u][6] = d[i];
+#pragma unroll
+            for (int k = 0; k < 6; k++) xv[u][k] = d[i + nb.o[k]];
+        }
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            if (!(f[u] & 0x8000u)) continue;
+            float sum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (f[u] & (1u << cg_bit(k))) sum += xv[u][k];
+            const float t = sum - (float)((f[u] >> 8) & 7) * xv[u][6];
+            tout[idx[u]] = t;
+            dt.add_prod(xv[u][6], t);
+            tt.add_prod(t, t);
+        }
+    }
+}
+
+// EFS_CG_MIXED_RECURRENCE, pass 2 (per cell, no neighbours): what = 3: e += alpha d, r += -alpha t,
+// d = d beta + r (sums r.r); what = 1: only e += alpha d; what = 2: only d = d beta + r.
+template <int WHAT>
+__device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& ch, float alpha, float beta) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = a.g.N;
+    float* __restrict__ d = a.d0;
+    float* __restrict__ r = a.r;
+    float* __restrict__ e = a.e;
+    const float* __restrict__ t = a.t;
+    FSum acc;
+    for (int cb = warp * UA; cb < ch.n; cb += SOLVER_WARPS * UA) {
+        int idx[UA];
+        uint16_t f[UA];
+#pragma unroll
+        for (int u = 0; u < UA; u++) idx[u] = (cb + u < ch.n) ? ch.ids[cb + u] * 32 + lane : -1;
+#pragma unroll
+        for (int u = 0; u < UA; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        float dv[UA], tv[UA], rv[UA], ev[UA];
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            const int i = idx[u] < 0 ? 0 : idx[u];
+            dv[u] = d[i];
+            if (WHAT & 1) { tv[u] = t[i]; ev[u] = e[i]; }
+            rv[u] = r[i];
+        }
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            if (!(f[u] & 0x8000u)) continue;
+            const int i = idx[u];
+            if (WHAT & 1) e[i] = ev[u] + alpha * dv[u];
+            if (WHAT == 3) {
+                const float rn = rv[u] + (-alpha) * tv[u];
+                r[i] = rn;
+                d[i] = dv[u] * beta + rn;
+                acc.add_prod(rn, rn);
+            } else if (WHAT == 2) {
+                d[i] = dv[u] * beta + rv[u];
+            }
+        }
+    }
+    return acc;
+}
+
+// Two floats computed by thread 0 and read by the whole block.
+__device__ __forceinline__ void block_scalars(float& v0, float& v1) {
+    __shared__ float s2[2];
+    if (threadIdx.x == 0) { s2[0] = v0; s2[1] = v1; }
+    __syncthreads();
+    v0 = s2[0];
+    v1 = s2[1];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
     DevCtl* ctl = a.ctl;
     __shared__ int s_scan[SOLVER_THREADS];
     // ---- phase 0: ordered compaction of the active chunks -------------------------------------------
@@ -474,7 +564,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     }
 
     // ---- CG ---------------------------------------------------------------------------------------------
-    const bool mixed = a.cg_variant == EFS_CG_MIXED;
+    const bool mixed = a.cg_variant == EFS_CG_MIXED || a.cg_variant == EFS_CG_MIXED_RECURRENCE;
     float* __restrict__ r = a.r;
     float* __restrict__ e = a.e;
     double* __restrict__ p64 = a.p64;
@@ -539,7 +629,47 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
     int conv = rr < thr;
     int iters = 0;
     float beta = 0.f;
-    if (!conv) {
+    if (!conv && a.cg_variant == EFS_CG_MIXED_RECURRENCE) {
+        int it;
+        for (it = 0; it < a.max_steps; it++) {
+            // pass 1: t = L d, d.t and t.t in one reduction
+            FSum dtp, ttp;
+            phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+            double dt, tt, u3;
+            if (!red.run(ctl, dtp, ttp, 0, dt, tt, u3)) return;
+            float alpha = 0.f, bet = 0.f;
+            if (threadIdx.x == 0) {
+                const double ad = rr / dt;
+                alpha = (float)ad;
+                bet = (float)((ad * ad * tt - rr) / rr);
+            }
+            block_scalars(alpha, bet);
+            const double old = rr;
+            bool replaced = false;
+            if (it & 0x3F) {
+                // pass 2: e, r, d per cell; exact r.r
+                const FSum rp = phase_update<3>(a, ch, alpha, bet);
+                if (!red.run(ctl, rp, FSum(), 0, rr, u1, u2)) return;
+            } else {
+                phase_update<1>(a, ch, alpha, 0.f);
+                __syncthreads();   // replace() folds e with another cell-to-thread mapping
+                if (!replace(rr)) return;
+                replaced = true;
+                float b2 = 0.f, unused = 0.f;
+                if (threadIdx.x == 0) b2 = (float)(rr / old);
+                block_scalars(b2, unused);
+                phase_update<2>(a, ch, 0.f, b2);
+                if (!grid_barrier(ctl)) return;
+            }
+            if (rr < thr) {
+                if (!replaced) {
+                    if (!replace(rr)) return;
+                }
+                if (rr < thr) { conv = 1; break; }
+            }
+        }
+        iters = it + 1;
+    } else if (!conv) {
         int it;
         for (it = 0; it < a.max_steps; it++) {
             float* dcur = (it & 1) ? a.d1 : a.d0;
@@ -600,8 +730,19 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solver(SolverArgs a) {
 std::mutex g_smem_mutex;
 size_t g_smem_limit = 48 * 1024;
 
+// The shared-memory carveout is set so that two blocks with this dynamic size fit on one SM (the driver's
+// default carveout held only one block of the 256^3 chunk cache); it too only rises.
+int g_carveout_pct = 0;
+
 cudaError_t ensure_solver_smem(size_t bytes) {
     std::lock_guard<std::mutex> lock(g_smem_mutex);
+    const size_t per_block = bytes + 4096 + 1024;   // dynamic + static + reserved, rounded up
+    const int pct = (int)std::min<size_t>(100, (2 * per_block * 100 + 228 * 1024 - 1) / (228 * 1024) + 1);
+    if (pct > g_carveout_pct) {
+        cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+        if (e != cudaSuccess) return e;
+        g_carveout_pct = pct;
+    }
     if (bytes <= g_smem_limit) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) g_smem_limit = bytes;
@@ -610,24 +751,32 @@ cudaError_t ensure_solver_smem(size_t bytes) {
 
 }  // namespace
 
-cudaError_t solver_configure(efs_ctx* c) {
-    int occ = 0;
-    const int n_chunks = (c->g.N + 31) / 32;
-    // shared memory for the chunk-id cache when every chunk is active and the grid has one block per SM
-    const size_t smem_max = (size_t)((n_chunks + c->sm_count - 1) / c->sm_count) * sizeof(int);
-    cudaError_t e = ensure_solver_smem(smem_max);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem_max);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) return cudaErrorLaunchOutOfResources;
-    int blocks = std::min(occ, 2) * c->sm_count;
-    // small grids: about four chunks per warp so barrier cost stays proportionate
+// Blocks per SM and the chunk-cache size: two blocks per SM when two blocks, each caching its share of the
+// chunks, fit (registers, threads, shared memory); otherwise one.  Small grids get fewer blocks (about four
+// chunks per warp) so barrier cost stays proportionate.
+cudaError_t solver_shape(int n_chunks, int sm_count, int* blocks_out, size_t* smem_out) {
+    int blocks = sm_count;
+    for (int bps = 2; bps >= 1; bps--) {
+        const size_t smem = (size_t)((n_chunks + bps * sm_count - 1) / (bps * sm_count)) * sizeof(int);
+        cudaError_t e = ensure_solver_smem(smem);
+        if (e != cudaSuccess) return e;
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem);
+        if (e != cudaSuccess) return e;
+        if (occ >= bps) { blocks = bps * sm_count; break; }
+        if (bps == 1 && occ < 1) return cudaErrorLaunchOutOfResources;
+    }
     const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
     blocks = std::max(1, std::min(blocks, want));
-    c->solver_blocks = blocks;
+    *blocks_out = blocks;
+    *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
+    return ensure_solver_smem(*smem_out);
+}
+
+cudaError_t solver_configure(efs_ctx* c) {
+    const int n_chunks = (c->g.N + 31) / 32;
     c->solver_threads = SOLVER_THREADS;
-    c->solver_smem = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
-    return ensure_solver_smem(c->solver_smem);
+    return solver_shape(n_chunks, c->sm_count, &c->solver_blocks, &c->solver_smem);
 }
 
 cudaError_t launch_solver(efs_ctx* c) {
@@ -651,6 +800,7 @@ cudaError_t launch_solver(efs_ctx* c) {
     a.r = c->r;
     a.d0 = c->d0;
     a.d1 = c->d1;
+    a.t = c->t;
     a.partials = c->partials;
     a.ctl = c->ctl;
     cudaLaunchConfig_t cfg = {};
@@ -672,19 +822,7 @@ cudaError_t launch_solver(efs_ctx* c) {
 // Launch shape of the solver for a grid of n_chunks 32-cell chunks (the same rule as solver_configure),
 // for callers that hold their own SolverArgs.
 cudaError_t solver_launch_shape(int n_chunks, int sm_count, int* blocks_out, size_t* smem_out) {
-    int occ = 0;
-    const size_t smem_max = (size_t)((n_chunks + sm_count - 1) / sm_count) * sizeof(int);
-    cudaError_t e = ensure_solver_smem(smem_max);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solver, SOLVER_THREADS, smem_max);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) return cudaErrorLaunchOutOfResources;
-    int blocks = std::min(occ, 2) * sm_count;
-    const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
-    blocks = std::max(1, std::min(blocks, want));
-    *blocks_out = blocks;
-    *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
-    return ensure_solver_smem(*smem_out);
+    return solver_shape(n_chunks, sm_count, blocks_out, smem_out);
 }
 
 // Cooperative launch of the solver with caller-provided arguments and shape (no allocation).

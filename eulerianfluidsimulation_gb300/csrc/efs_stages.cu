@@ -108,8 +108,14 @@ __global__ void k_sharpen_calc(Geo g, const float* __restrict__ rho, float delT,
     bool ok;
     if (DIM == 3) ok = cell3(g, x, y, z, i); else ok = cell2(g, x, y, i);
     float dr = 0.f;
-    if (ok) {
-        const float r = rho[i];
+    // Cells whose result is decided without the slope terms: rho < 1e-5 gives dr = -rho, and rho > 0.5 gives
+    // dr = 0 (there the weight is >= 0, so rho + dr >= rho > 0 and the reference's second branch applies).
+    // Only the interface band 1e-5 <= rho <= 0.5 (or NaN) evaluates the FP64 slope terms below.
+    const float r0 = ok ? rho[i] : 0.f;
+    const bool settled = ok && ((double)r0 < 1e-5 || r0 > 0.5f);
+    if (settled) dr = ((double)r0 < 1e-5) ? -r0 : 0.f;
+    if (ok && !settled) {
+        const float r = r0;
         const float rxm = rho[i - 1], rxp = rho[i + 1], rym = rho[i - g.W], ryp = rho[i + g.W];
         const float dpx = -(r - rxm) * delT, dmx = -(rxp - r) * delT;
         const float dpy = -(r - rym) * delT, dmy = -(ryp - r) * delT;

@@ -73,7 +73,13 @@ enum efs_solver {
  * FP32, like the reference. */
 enum efs_cg_variant {
     EFS_CG_MIXED = 0,
-    EFS_CG_REFERENCE = 1
+    EFS_CG_REFERENCE = 1,
+    /* EFS_CG_MIXED_RECURRENCE: EFS_CG_MIXED with the work of an iteration rearranged so that only one pass reads
+     * stencil neighbours.  Pass 1 forms t = L d, stores it and sums d.t and t.t; beta is taken from the
+     * residual-norm recurrence r'.r' = alpha^2 t.t - r.r (exact CG identity); pass 2 updates the increment, r and
+     * d in place per cell and sums the exact r'.r' for the stop test.  Every 64th iteration recomputes the
+     * residual in FP64 as the other variants do, and takes that iteration's beta from it. */
+    EFS_CG_MIXED_RECURRENCE = 2
 };
 
 /* ---- fields (IGrid3D accessors, IGrid.h:44-68) ---- */
@@ -137,7 +143,8 @@ typedef struct efs_stats {
 typedef struct efs_ctx efs_ctx;
 
 /* ---- defaults ---- */
-/* Reference Properties defaults (Properties.h:141-162; gravity 10 / cell size 1). */
+/* Reference Properties defaults (Properties.h:141-162; gravity 10 / cell size 1); the solver fields that
+ * Properties does not have: sharpen_mode EFS_SHARPEN_PARALLEL, cg_variant EFS_CG_MIXED_RECURRENCE. */
 void efs_params_default(efs_params* p);
 /* Dam-break constants of the reference scene assets/scenes/Dam128.json "properties": lambda- 50,
  * lambda+ 10, eta 100, D 32, velocity decay disabled, liquid threshold 0.5, gravity 9.81 / cell_size,

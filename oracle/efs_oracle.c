@@ -781,8 +781,74 @@ static float cg_solve_mixed(orc_grid* g, float thr) {
     return ((float)rr > thr) ? (float)rr : nextafterf(thr, INFINITY);
 }
 
+/* EFS_CG_MIXED_RECURRENCE: the iteration of cg_solve_mixed with beta from the residual-norm recurrence
+ * r'.r' = alpha^2 t.t - r.r, so that d, r and the increment are updated together once t = L d is known; the
+ * exact r'.r' is still summed for the stop test, and every 64th iteration recomputes the residual in FP64 and
+ * takes beta from it. */
+static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
+    const size_t N = g->N;
+    float *t = g->cg_t, *r = g->cg_r, *d = g->cg_d, *e = g->jac_tmp;
+    const float* b = g->div;
+    const int steps = g->prm.max_steps;
+    double* p64 = (double*)malloc(N * sizeof(double));
+    double* t64 = (double*)malloc(N * sizeof(double));
+    double rr;
+    #define ORC_REPLACE() do { \
+        for (size_t c = 0; c < N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
+        matmul_d(g, t64, p64); \
+        rr = 0; \
+        for (size_t c = 0; c < N; c++) { r[c] = (float)((double)b[c] - t64[c]); rr += (double)r[c] * (double)r[c]; } \
+    } while (0)
+    for (size_t c = 0; c < N; c++) { p64[c] = (double)b[c]; e[c] = 0.f; }
+    ORC_REPLACE();
+    memcpy(d, r, N * 4);
+    g->solve_steps = 0;
+    int conv = rr < (double)thr;
+    if (!conv) {
+        int i;
+        for (i = 0; i < steps; i++) {
+            matmul(g, t, d);
+            const double dt = ddot(g, d, t), tt = ddot(g, t, t);
+            const double ad = rr / dt;
+            const float alpha = (float)ad;
+            const double old = rr;
+            int replaced = 0;
+            if (i & 0x3F) {
+                const float beta = (float)((ad * ad * tt - old) / old);
+                for (size_t c = 0; c < N; c++) {
+                    e[c] += alpha * d[c];
+                    const float rn = r[c] + (-alpha) * t[c];
+                    r[c] = rn;
+                    d[c] = d[c] * beta + rn;
+                }
+                rr = ddot(g, r, r);
+            } else {
+                for (size_t c = 0; c < N; c++) e[c] += alpha * d[c];
+                ORC_REPLACE();
+                replaced = 1;
+                const float beta = (float)(rr / old);
+                for (size_t c = 0; c < N; c++) d[c] = d[c] * beta + r[c];
+            }
+            if (rr < (double)thr) {
+                if (!replaced) ORC_REPLACE();
+                if (rr < (double)thr) { conv = 1; break; }
+            }
+        }
+        g->solve_steps = i + 1;
+    }
+    #undef ORC_REPLACE
+    for (size_t c = 0; c < N; c++) g->p[c] = (float)(p64[c] + (double)e[c]);
+    free(p64); free(t64);
+    g->rr = rr;
+    g->converged = conv;
+    if (conv) return (float)rr;
+    return ((float)rr > thr) ? (float)rr : nextafterf(thr, INFINITY);
+}
+
 static float cg_solve(orc_grid* g, float thr) {
-    return (g->prm.cg_variant == EFS_CG_REFERENCE) ? cg_solve_reference(g, thr) : cg_solve_mixed(g, thr);
+    if (g->prm.cg_variant == EFS_CG_REFERENCE) return cg_solve_reference(g, thr);
+    if (g->prm.cg_variant == EFS_CG_MIXED_RECURRENCE) return cg_solve_mixed_recurrence(g, thr);
+    return cg_solve_mixed(g, thr);
 }
 
 /* JacobiSolverCPU3D::solve (JS:154-212) == JacobiSolverCPU2D::solve (JS:18-71): returns 0 */
@@ -1358,6 +1424,7 @@ void orc_params_default(efs_params* p) {
     p->lambda_minus = .5f; p->lambda_plus = .1f; p->eta = 1.f; p->liquid_threshold = 0.5f; p->rho_d = 3.f;
     p->solver = EFS_SOLVER_CG; p->max_steps = 2000; p->solver_threshold = 1e-5f; p->tol_rel = 0.f;
     p->disable_mask = 0; p->re_calc_div = 0; p->sharpen_mode = EFS_SHARPEN_PARALLEL;
+    p->cg_variant = EFS_CG_MIXED_RECURRENCE;
 }
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -88,9 +88,9 @@ def test_stage_matches_oracle(dim, n, stage):
 
 @pytest.mark.parametrize("dim,n", [(3, 32), (2, 64)])
 @pytest.mark.parametrize("solver,variant", [(abi.SOLVER_JACOBI, abi.CG_MIXED), (abi.SOLVER_CG, abi.CG_REFERENCE),
-                                            (abi.SOLVER_CG, abi.CG_MIXED)])
+                                            (abi.SOLVER_CG, abi.CG_MIXED), (abi.SOLVER_CG, abi.CG_MIXED_RECURRENCE)])
 def test_project_solvers(dim, n, solver, variant):
-    prm = make_params(dim, n, solver, variant, tol=1e-6 if variant == abi.CG_MIXED else 0.0)
+    prm = make_params(dim, n, solver, variant, tol=0.0 if variant == abi.CG_REFERENCE else 1e-6)
     state = warm_state(dim, n, prm, 2)
     o = oracle.Oracle(dim, n, n, n, prm, mode=GPU_MODE)
     o.set_fields(state)
@@ -111,9 +111,10 @@ def test_project_solvers(dim, n, solver, variant):
 
 
 @pytest.mark.parametrize("dim,n", [(3, 48), (2, 128)])
-def test_solver_against_fp64(dim, n):
+@pytest.mark.parametrize("variant", [abi.CG_MIXED, abi.CG_MIXED_RECURRENCE])
+def test_solver_against_fp64(dim, n, variant):
     """efs_solve alone (ISolver::solve): the mixed CG's pressure against an FP64 CG solve of the same system."""
-    prm = make_params(dim, n)
+    prm = make_params(dim, n, variant=variant)
     state = warm_state(dim, n, prm, 2)
     o = oracle.Oracle(dim, n, n, n, prm, mode=GPU_MODE)
     o.set_fields(state)

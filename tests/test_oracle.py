@@ -81,7 +81,7 @@ def test_mixed_cg_reaches_fp64_relative_residual():
     n = 128
     b, r = oracle.scene_dam2d(n, n)
     res = {}
-    for v in (abi.CG_MIXED, abi.CG_REFERENCE):
+    for v in (abi.CG_MIXED, abi.CG_REFERENCE, abi.CG_MIXED_RECURRENCE):
         prm = abi.params_dam(1.0 / n, 0.005, abi.SOLVER_CG, 1e-6)
         prm.cg_variant = v
         o = oracle.Oracle(2, n, n, 1, prm)
@@ -96,6 +96,10 @@ def test_mixed_cg_reaches_fp64_relative_residual():
     pstar, _ = o.solve_fp64(1e-13)
     assert rel_l2(p, pstar) < 1e-6
     assert not res[abi.CG_REFERENCE][0].converged
+    # the recurrence form (two passes per iteration) takes the same iterations to the same accuracy
+    st2, p2, _ = res[abi.CG_MIXED_RECURRENCE]
+    assert st2.converged and abs(st2.solve_steps - st.solve_steps) <= 2
+    assert rel_l2(p2, pstar) < 1e-6
 
 
 def test_scene_generators_are_seeded():
