@@ -23,11 +23,8 @@ enum DeviceError : int {
 // Control block in device memory: grid barrier, solve results and counters.  Mirrored into pinned host
 // memory by efs_get_stats.
 struct DevCtl {
-    unsigned bar_count;        // grid barrier arrivals (reset before every solver launch)
+    unsigned bar_count;        // grid barrier arrivals, counting up through the launch (reset before every launch)
     int bar_abort;             // set when a barrier of the current launch gave up (reset before every launch)
-    unsigned bar_gen;          // grid barrier generation
-    int pad0;
-    double totals[2][3];       // grid totals published by the last block to reach a reducing barrier
     int error;
     int converged;
     int iterations;

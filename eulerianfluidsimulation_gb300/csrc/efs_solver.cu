@@ -39,48 +39,36 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
-// Grid-wide barrier for a cooperative launch (all blocks co-resident).  Warp 0 of each block takes part; lane 0
-// arrives on the counter.  When `partials`/`slot` are given, the last block to arrive adds every block's
-// partials in block order and publishes the three totals in ctl->totals[slot] before releasing, so the
-// totals are identical in every block and reach them with the release.  Waiting is bounded by time: a
-// block that waits longer than BARRIER_TIMEOUT_NS sets DEV_ERR_BARRIER_TIMEOUT and bar_abort, and every
-// block returns false from then on.
-__device__ bool grid_barrier(DevCtl* ctl, const double* partials = nullptr, int slot = 0) {
+__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// Number of grid barriers this block has passed in the current launch (one per block, in shared memory).
+__device__ __forceinline__ unsigned& barrier_index() {
+    __shared__ unsigned s_index;
+    return s_index;
+}
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).  The arrival counter only counts up
+// during a launch: at its k-th barrier a block adds 1 (a release) and waits (acquire loads) until the
+// counter reaches k * gridDim.x, compared modulo 2^32.  No block resets anything, so the last arrival
+// releases everyone with its own add.  Waiting is bounded by time: a block that waits longer than
+// BARRIER_TIMEOUT_NS sets DEV_ERR_BARRIER_TIMEOUT and bar_abort, and every block returns false from then on.
+__device__ bool grid_barrier(DevCtl* ctl) {
     __shared__ int s_ok;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        unsigned gen = 0, arrived = 0;
-        if (lane == 0) {
-            gen = ld_acquire(&ctl->bar_gen);
-            __threadfence();
-            arrived = atomicAdd(&ctl->bar_count, 1u);
-        }
-        arrived = __shfl_sync(0xffffffffu, arrived, 0);
-        __threadfence();
+    if (threadIdx.x == 0) {
+        unsigned& k = barrier_index();
+        k += 1u;
+        const unsigned target = k * gridDim.x;
+        const unsigned old = atom_add_release(&ctl->bar_count, 1u);
         int ok = 1;
-        if (arrived == gridDim.x - 1) {
-            if (partials) {
-                const volatile double* src = partials + (size_t)slot * 3 * gridDim.x;
-                double ta = 0, tb = 0, tc = 0;
-                for (int k = lane; k < (int)gridDim.x; k += 32) { ta += src[3 * k]; tb += src[3 * k + 1]; tc += src[3 * k + 2]; }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    ta += __shfl_down_sync(0xffffffffu, ta, o);
-                    tb += __shfl_down_sync(0xffffffffu, tb, o);
-                    tc += __shfl_down_sync(0xffffffffu, tc, o);
-                }
-                if (lane == 0) { ctl->totals[slot][0] = ta; ctl->totals[slot][1] = tb; ctl->totals[slot][2] = tc; }
-            }
-            if (lane == 0) {
-                atomicExch(&ctl->bar_count, 0u);
-                __threadfence();
-                atomicAdd(&ctl->bar_gen, 1u);
-            }
-        } else if (lane == 0) {
+        if (old + 1u != target) {
             const unsigned long long t0 = globaltimer_ns();
             unsigned spins = 0;
-            while (ld_acquire(&ctl->bar_gen) == gen) {
+            while ((int)(ld_acquire(&ctl->bar_count) - target) < 0) {
                 if ((++spins & 255u) == 0) {
                     if (*(volatile int*)&ctl->bar_abort) { ok = 0; break; }
                     if (globaltimer_ns() - t0 > BARRIER_TIMEOUT_NS) {
@@ -92,20 +80,18 @@ __device__ bool grid_barrier(DevCtl* ctl, const double* partials = nullptr, int 
                 }
             }
         }
-        if (lane == 0) {
-            __threadfence();
-            s_ok = ok;
-        }
+        __threadfence();
+        s_ok = ok;
     }
     __syncthreads();
     return s_ok != 0;
 }
 
-// Dot-product accumulation.  GB300 executes FP64 at a small fraction of its FP32 rate, so per-thread sums are
-// kept as an unevaluated pair of floats (s + c): every product a*b is split exactly into p + e with one FMA,
-// and every addition into s is made exact with TwoSum (Knuth), the rounding error going into c.  The pair
-// carries about 48 significant bits; warps combine pairs with shuffles, and only per-warp partials, block
-// partials and grid totals are FP64.
+// Dot-product accumulation.  GB300 executes FP64 at a small fraction of its FP32 rate, so sums are kept as an
+// unevaluated pair of floats (s + c): every product a*b is split exactly into p + e with one FMA, and every
+// addition into s is made exact with TwoSum (Knuth), the rounding error going into c.  The pair carries about
+// 48 significant bits.  Threads, warps, blocks and the grid all combine pairs; only the grid total becomes a
+// double (s + c).
 struct FSum {
     float s = 0.f, c = 0.f;
     __device__ __forceinline__ void add(float v) {
@@ -136,60 +122,68 @@ __device__ __forceinline__ FSum warp_sum(FSum v) {
     return v;
 }
 
-// Block sums of two compensated sums and an integer count; thread 0 stores them as this block's partials.
-__device__ void block_partials(FSum a, FSum b, int n, double* partials, int slot) {
-    __shared__ double s_v[3][SOLVER_WARPS];
+// Sums three pairs over the block (fixed tree: lanes, then warps in order); the result is valid in warp 0.
+__device__ __forceinline__ void block_sum3(FSum& a, FSum& b, FSum& c) {
+    __shared__ float s_w[6][SOLVER_WARPS];
     a = warp_sum(a);
     b = warp_sum(b);
-    n = __reduce_add_sync(0xffffffffu, n);
+    c = warp_sum(c);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
-        s_v[0][warp] = (double)a.s + (double)a.c;
-        s_v[1][warp] = (double)b.s + (double)b.c;
-        s_v[2][warp] = (double)n;
+        s_w[0][warp] = a.s; s_w[1][warp] = a.c;
+        s_w[2][warp] = b.s; s_w[3][warp] = b.c;
+        s_w[4][warp] = c.s; s_w[5][warp] = c.c;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double ta = 0, tb = 0, tc = 0;
-        for (int k = 0; k < SOLVER_WARPS; k++) { ta += s_v[0][k]; tb += s_v[1][k]; tc += s_v[2][k]; }
-        double* dst = partials + (size_t)slot * 3 * gridDim.x + 3 * blockIdx.x;
-        dst[0] = ta; dst[1] = tb; dst[2] = tc;
+    if (warp == 0) {
+        const bool in = lane < SOLVER_WARPS;
+        a.s = in ? s_w[0][lane] : 0.f; a.c = in ? s_w[1][lane] : 0.f;
+        b.s = in ? s_w[2][lane] : 0.f; b.c = in ? s_w[3][lane] : 0.f;
+        c.s = in ? s_w[4][lane] : 0.f; c.c = in ? s_w[5][lane] : 0.f;
+        a = warp_sum(a);
+        b = warp_sum(b);
+        c = warp_sum(c);
     }
 }
 
-// Every block adds all blocks' partials of `slot` in the same order; totals returned to every thread.
-__device__ void grid_totals(const double* partials, int slot, double& a, double& b, double& c) {
-    __shared__ double s_tot[3];
-    const volatile double* src = partials + (size_t)slot * 3 * gridDim.x;
-    if (threadIdx.x < 32) {
-        double ta = 0, tb = 0, tc = 0;
-        for (int k = threadIdx.x; k < (int)gridDim.x; k += 32) { ta += src[3 * k]; tb += src[3 * k + 1]; tc += src[3 * k + 2]; }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            ta += __shfl_down_sync(0xffffffffu, ta, o);
-            tb += __shfl_down_sync(0xffffffffu, tb, o);
-            tc += __shfl_down_sync(0xffffffffu, tc, o);
-        }
-        if (threadIdx.x == 0) { s_tot[0] = ta; s_tot[1] = tb; s_tot[2] = tc; }
-    }
-    __syncthreads();
-    a = s_tot[0]; b = s_tot[1]; c = s_tot[2];
-    __syncthreads();
-}
-
-// Grid reduction with two alternating partial slots: put (block partials), grid barrier, get (totals).
-// A slot is rewritten two reductions later, after every block has passed the barrier of the reduction in
-// between, so no second barrier is needed.
+// Grid reduction of three pair sums with two alternating partial slots.  Each block stores its three pairs
+// (6 floats) in slot `slot`; after the barrier every block adds all blocks' partials in the same fixed order
+// (thread k loads block k's, then block_sum3), so every block obtains bit-identical totals and takes the same
+// branches.  A slot is rewritten two reductions later, after every block has passed the barrier between.
 struct Reduction {
-    double* partials;
+    float* partials;           // 2 slots x gridDim.x x 6 floats
     int slot;
-    __device__ bool run(DevCtl* ctl, FSum a, FSum b, int n, double& ta, double& tb, double& tc) {
-        block_partials(a, b, n, partials, slot);
-        if (!grid_barrier(ctl, partials, slot)) return false;
-        const volatile double* t = ctl->totals[slot];
-        ta = t[0]; tb = t[1]; tc = t[2];
+    __device__ bool run(DevCtl* ctl, FSum a, FSum b, FSum c, double& ta, double& tb, double& tc) {
+        __shared__ double s_tot[3];
+        block_sum3(a, b, c);
+        float* mine = partials + ((size_t)slot * gridDim.x + blockIdx.x) * 6;
+        if (threadIdx.x == 0) {
+            mine[0] = a.s; mine[1] = a.c; mine[2] = b.s; mine[3] = b.c; mine[4] = c.s; mine[5] = c.c;
+        }
+        if (!grid_barrier(ctl)) return false;
+        FSum x, y, z;
+        const volatile float* src = partials + (size_t)slot * gridDim.x * 6;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += SOLVER_THREADS) {
+            x.add_pair(src[6 * k + 0], src[6 * k + 1]);
+            y.add_pair(src[6 * k + 2], src[6 * k + 3]);
+            z.add_pair(src[6 * k + 4], src[6 * k + 5]);
+        }
+        block_sum3(x, y, z);
+        if (threadIdx.x == 0) {
+            s_tot[0] = (double)x.s + (double)x.c;
+            s_tot[1] = (double)y.s + (double)y.c;
+            s_tot[2] = (double)z.s + (double)z.c;
+        }
+        __syncthreads();
+        ta = s_tot[0]; tb = s_tot[1]; tc = s_tot[2];
+        __syncthreads();
         slot ^= 1;
         return true;
+    }
+    __device__ bool run(DevCtl* ctl, FSum a, FSum b, int n, double& ta, double& tb, double& tc) {
+        FSum c;
+        c.add((float)n);
+        return run(ctl, a, b, c, ta, tb, tc);
     }
 };
 
@@ -225,19 +219,6 @@ __device__ __forceinline__ float lap_f(const float* x, uint16_t info, int i, con
     for (int k = 0; k < 6; k++)
         if (info & (1u << cg_bit(k))) sum += x[i + nb.o[k]];
     return sum - (float)((info >> 8) & 7) * x[i];
-}
-// L d for d = beta * dp + r evaluated on the fly (the same float operations as forming d first)
-__device__ __forceinline__ float lap_dir(const float* dp, const float* r, float beta, uint16_t info, int i,
-                                         const Nb& nb, float& d_own) {
-    float sum = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 6; k++)
-        if (info & (1u << cg_bit(k))) {
-            const int j = i + nb.o[k];
-            sum += dp[j] * beta + r[j];
-        }
-    d_own = dp[i] * beta + r[i];
-    return sum - (float)((info >> 8) & 7) * d_own;
 }
 // L x in FP64 on row i
 __device__ __forceinline__ double lap_d(const double* x, uint16_t info, int i, const Nb& nb) {
@@ -462,6 +443,7 @@ __device__ __forceinline__ void block_scalars(float& v0, float& v1) {
 
 __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
     DevCtl* ctl = a.ctl;
+    if (threadIdx.x == 0) barrier_index() = 0u;
     __shared__ int s_scan[SOLVER_THREADS];
     // ---- phase 0: ordered compaction of the active chunks -------------------------------------------
     const int per_blk = (a.n_chunks + gridDim.x - 1) / gridDim.x;
@@ -525,7 +507,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
     const float* __restrict__ b = a.b;
     const uint16_t* __restrict__ info = a.rowinfo;
 
-    Reduction red{a.partials, 0};
+    Reduction red{reinterpret_cast<float*>(a.partials), 0};
     double u1, u2;
 
     // ---- Jacobi ---------------------------------------------------------------------------------------
