@@ -431,6 +431,19 @@ __device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& 
     return acc;
 }
 
+// a / b in FP64 without the FP64 division sequence (about 550 cycles of dependent latency on GB300): a
+// float reciprocal refined by two Newton steps in FP64, relative error near 1e-16.  Falls back to the
+// division when b is outside the range where the float reciprocal is finite and normal.
+__device__ __forceinline__ double div_fast(double a, double b) {
+    const float bf = (float)b;
+    float r0 = 1.0f / bf;
+    if (!(fabsf(r0) < 1e37f && fabsf(r0) > 1e-37f)) return a / b;
+    double r = (double)r0;
+    r = fma(r, fma(-b, r, 1.0), r);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+}
+
 // Two floats computed by thread 0 and read by the whole block.
 __device__ __forceinline__ void block_scalars(float& v0, float& v1) {
     __shared__ float s2[2];
@@ -612,42 +625,51 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
     int iters = 0;
     float beta = 0.f;
     if (!conv && a.cg_variant == EFS_CG_MIXED_RECURRENCE) {
-        int it;
-        for (it = 0; it < a.max_steps; it++) {
-            // pass 1: t = L d, d.t and t.t in one reduction
+        // Pass 1 (t = L d; d.t, t.t) and pass 2 (e, r, d per cell; exact r.r) alternate.  The r.r of pass 2
+        // only feeds the stop test, so its block partial travels with the next pass 1's reduction: one
+        // reduction and one plain barrier per iteration.  The stop test of iteration k is therefore taken
+        // after the pass 1 of iteration k+1, whose t is then unused; e, r and p are unaffected.
+        double dt, tt, u3;
+        {
             FSum dtp, ttp;
             phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
-            double dt, tt, u3;
-            if (!red.run(ctl, dtp, ttp, 0, dt, tt, u3)) return;
+            if (!red.run(ctl, FSum(), dtp, ttp, u3, dt, tt)) return;
+        }
+        int it;
+        for (it = 0; it < a.max_steps; it++) {
             float alpha = 0.f, bet = 0.f;
             if (threadIdx.x == 0) {
-                const double ad = rr / dt;
+                const double ad = div_fast(rr, dt);
                 alpha = (float)ad;
-                bet = (float)((ad * ad * tt - rr) / rr);
+                bet = (float)(ad * ad * tt * div_fast(1.0, rr) - 1.0);
             }
             block_scalars(alpha, bet);
             const double old = rr;
-            bool replaced = false;
             if (it & 0x3F) {
-                // pass 2: e, r, d per cell; exact r.r
                 const FSum rp = phase_update<3>(a, ch, alpha, bet);
-                if (!red.run(ctl, rp, FSum(), 0, rr, u1, u2)) return;
+                if (!grid_barrier(ctl)) return;
+                FSum dtp, ttp;
+                phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+                if (!red.run(ctl, rp, dtp, ttp, rr, dt, tt)) return;
+                if (rr < thr) {
+                    // confirm on the recomputed residual; if that is above the threshold, iterate on from it
+                    // (d.t and t.t of the current d stand)
+                    if (!replace(rr)) return;
+                    if (rr < thr) { conv = 1; break; }
+                }
             } else {
                 phase_update<1>(a, ch, alpha, 0.f);
                 __syncthreads();   // replace() folds e with another cell-to-thread mapping
                 if (!replace(rr)) return;
-                replaced = true;
+                if (rr < thr) { conv = 1; break; }
                 float b2 = 0.f, unused = 0.f;
                 if (threadIdx.x == 0) b2 = (float)(rr / old);
                 block_scalars(b2, unused);
                 phase_update<2>(a, ch, 0.f, b2);
                 if (!grid_barrier(ctl)) return;
-            }
-            if (rr < thr) {
-                if (!replaced) {
-                    if (!replace(rr)) return;
-                }
-                if (rr < thr) { conv = 1; break; }
+                FSum dtp, ttp;
+                phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+                if (!red.run(ctl, FSum(), dtp, ttp, u3, dt, tt)) return;
             }
         }
         iters = it + 1;
