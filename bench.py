@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--solver", default="cg", choices=["cg", "jacobi"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--study", default=None, choices=["precision"],
+                    help="instead of the throughput line: the precision study (every field against an FP64 "
+                         "pressure solve of the same right-hand side) at --size for --steps steps")
+    ap.add_argument("--study-out", default=None, help="precision study: also write the per-step records here (JSON)")
     return ap.parse_args()
 
 
@@ -295,8 +299,25 @@ def run_gb300(a):
         dist.destroy_process_group()
 
 
+def run_precision_study(a):
+    """One JSON line with the maxima of the per-step errors (the 3D dam break with --spheres spheres)."""
+    from eulerianfluidsimulation_gb300.precision import precision_study
+    t0 = time.time()
+    rep = precision_study(3, a.size, a.steps, spheres=a.spheres, seed=a.seed, dt=a.dt)
+    line = {"study": "precision", "workload": f"dam3d_{a.size}", "steps": a.steps, "spheres": a.spheres,
+            "seed": a.seed, "tol_rel": rep["tol_rel"], "tol_fp64": rep["tol_fp64"], "max": rep["max"],
+            "wall_s": round(time.time() - t0, 1)}
+    if a.study_out:
+        with open(a.study_out, "w") as f:
+            json.dump(rep, f)
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.study == "precision":
+        run_precision_study(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

@@ -30,6 +30,7 @@ SIGNATURES = {
     "efs_download_field": (ctypes.c_int, [_CTX, ctypes.c_int, _FP]),
     "efs_upload_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP]),
     "efs_download_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP, _FP]),
+    "efs_download_pressure_fp64": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_double)]),
     "efs_reset_fields": (ctypes.c_int, [_CTX]),
     "efs_stage": (ctypes.c_int, [_CTX, ctypes.c_int]),
     "efs_step": (ctypes.c_int, [_CTX, ctypes.c_int]),

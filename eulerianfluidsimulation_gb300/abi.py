@@ -23,6 +23,7 @@ SOLVER_CG = 1
 CG_MIXED = 0
 CG_REFERENCE = 1
 CG_MIXED_RECURRENCE = 2
+CG_FP64 = 3
 
 FIELD_VEL = 0
 FIELD_RHO = 1

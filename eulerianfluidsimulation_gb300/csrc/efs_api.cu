@@ -32,7 +32,8 @@ bool params_valid(const efs_params* p, std::string& why) {
     if (!p) { why = "params is NULL"; return false; }
     if (!std::isfinite(p->dt) || !std::isfinite(p->gravity_force)) { why = "dt and gravity_force must be finite"; return false; }
     if (p->solver != EFS_SOLVER_JACOBI && p->solver != EFS_SOLVER_CG) { why = "unknown solver"; return false; }
-    if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE && p->cg_variant != EFS_CG_MIXED_RECURRENCE) {
+    if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE && p->cg_variant != EFS_CG_MIXED_RECURRENCE &&
+        p->cg_variant != EFS_CG_FP64) {
         why = "unknown cg_variant";
         return false;
     }
@@ -137,6 +138,17 @@ int check_device_status(efs_ctx* c) {
         cudaMemcpy(&c->ctl->error, &zero, sizeof(int), cudaMemcpyHostToDevice);
         return fail(c, err == efs::DEV_ERR_BAD_BOUNDARY ? EFS_ERR_ARG : EFS_ERR_DEVICE_FAULT, buf);
     }
+    return EFS_OK;
+}
+
+// The FP64 vectors of EFS_CG_FP64, allocated the first time a context selects that variant.
+int ensure_fp64_vectors(efs_ctx* c) {
+    if (c->r64) return EFS_OK;
+    const size_t N = (size_t)c->g.N;
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    CK(dalloc_halo(c, &c->r64, N), "cudaMalloc r64");
+    CK(dalloc_halo(c, &c->d64, N), "cudaMalloc d64");
+    CK(dalloc_halo(c, &c->t64, N), "cudaMalloc t64");
     return EFS_OK;
 }
 
@@ -272,6 +284,10 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
     if ((e = cudaMemsetAsync(c->e, 0, N * sizeof(float), c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
     if ((e = efs::launch_reset_fields(c)) != cudaSuccess) return bail(e, "reset");
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(e, "cudaStreamSynchronize");
+    if (prm.cg_variant == EFS_CG_FP64) {
+        const int s = ensure_fp64_vectors(c);
+        if (s != EFS_OK) { efs_destroy(c); return s; }
+    }
     *out = c;
     return EFS_OK;
 }
@@ -280,12 +296,25 @@ int efs_set_params(efs_ctx* c, const efs_params* p) {
     if (!c) return EFS_ERR_ARG;
     std::string why;
     if (!params_valid(p, why)) return fail(c, EFS_ERR_ARG, why);
+    if (p->cg_variant == EFS_CG_FP64) {
+        const int s = ensure_fp64_vectors(c);
+        if (s != EFS_OK) return s;
+    }
     if (std::memcmp(&c->prm, p, sizeof(efs_params)) != 0) {
         CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
         drop_graphs(c);
         c->prm = *p;
     }
     return EFS_OK;
+}
+
+int efs_download_pressure_fp64(efs_ctx* c, double* host) {
+    if (!c) return EFS_ERR_ARG;
+    if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
+    if (c->prm.solver != EFS_SOLVER_CG || c->prm.cg_variant == EFS_CG_REFERENCE)
+        return fail(c, EFS_ERR_STATE, "no FP64 pressure: the solver is not CG with an FP64 accumulator");
+    CK(cudaMemcpyAsync(host, c->p64, (size_t)c->g.N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "download p64");
+    return check_device_status(c);
 }
 
 int efs_get_params(const efs_ctx* c, efs_params* p) {

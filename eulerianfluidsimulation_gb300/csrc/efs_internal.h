@@ -61,6 +61,9 @@ struct SolverArgs {
     float* d0;
     float* d1;
     float* t;                  // L d of the current iteration (EFS_CG_MIXED_RECURRENCE)
+    double* r64;               // EFS_CG_FP64 vectors (allocated when that variant is first selected)
+    double* d64;
+    double* t64;
     double* partials;          // 2 slots x 3 values per block
     DevCtl* ctl;
 };
@@ -108,6 +111,7 @@ struct efs_ctx {
     int* chunk_list = nullptr;
     int* block_count = nullptr;
     float *r = nullptr, *d0 = nullptr, *d1 = nullptr, *e = nullptr, *t = nullptr;
+    double *r64 = nullptr, *d64 = nullptr, *t64 = nullptr;
     double* p64 = nullptr;
     double* partials = nullptr;
     int solver_blocks = 0;

@@ -454,8 +454,114 @@ __device__ __forceinline__ void block_scalars(float& v0, float& v1) {
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
+// A per-thread FP64 sum as a float pair (about 48 significant bits), for the pair reductions.
+__device__ __forceinline__ FSum pair_of(double v) {
+    FSum f;
+    f.s = (float)v;
+    f.c = (float)(v - (double)f.s);
+    return f;
+}
+
+// EFS_CG_FP64: the reference CG iteration (CGSolver.cpp:416-465: p0 = b, r = b - L p, d = r; true residual
+// when (i & 63) == 0; stop on r.r < threshold) with p, r, d and t = L d all in FP64 and the threshold
+// tol_rel^2 b.b kept in FP64.  A study solver: it gives the FP64 pressure of the same right-hand side that the
+// FP32 solvers are measured against.  Rows outside the matrix keep p = b, as in the other variants.
+__device__ __forceinline__ void cg_fp64(const SolverArgs& a, const Chunks& ch, const Nb& nb, Reduction& red, int M) {
     DevCtl* ctl = a.ctl;
+    const float* b = a.b;
+    const uint16_t* info = a.rowinfo;
+    double* p = a.p64;
+    double* r = a.r64;
+    double* d = a.d64;
+    double* t = a.t64;
+    double u1, u2, rr, bb, nrows;
+    for_rows(a, ch, [&](int i) { p[i] = (double)b[i]; });
+    if (!grid_barrier(ctl)) return;
+    {
+        double acc_rr = 0.0, acc_bb = 0.0;
+        int rows = 0;
+        for_rows(a, ch, [&](int i) {
+            const double bi = (double)b[i];
+            acc_bb += bi * bi;
+            const uint16_t f = info[i];
+            if (!(f & 0x8000u)) return;
+            rows += 1;
+            const double ri = bi - lap_d(p, f, i, nb);
+            r[i] = ri;
+            d[i] = ri;
+            acc_rr += ri * ri;
+        });
+        if (!red.run(ctl, pair_of(acc_rr), pair_of(acc_bb), rows, rr, bb, nrows)) return;
+    }
+    const double thr = a.tol_rel > 0 ? (double)a.tol_rel * (double)a.tol_rel * bb : (double)a.solver_threshold;
+    int conv = rr < thr, it = 0;
+    if (!conv) {
+        for (it = 0; it < a.max_steps; it++) {
+            double acc = 0.0;
+            for_rows(a, ch, [&](int i) {
+                const uint16_t f = info[i];
+                if (!(f & 0x8000u)) return;
+                const double ti = lap_d(d, f, i, nb);
+                t[i] = ti;
+                acc += d[i] * ti;
+            });
+            double dt;
+            if (!red.run(ctl, pair_of(acc), FSum(), 0, dt, u1, u2)) return;
+            const double alpha = rr / dt;
+            const double old = rr;
+            acc = 0.0;
+            if (it & 0x3F) {
+                for_rows(a, ch, [&](int i) {
+                    if (!(info[i] & 0x8000u)) return;
+                    p[i] += alpha * d[i];
+                    const double ri = r[i] - alpha * t[i];
+                    r[i] = ri;
+                    acc += ri * ri;
+                });
+            } else {
+                for_rows(a, ch, [&](int i) {
+                    if (info[i] & 0x8000u) p[i] += alpha * d[i];
+                });
+                if (!grid_barrier(ctl)) return;
+                for_rows(a, ch, [&](int i) {
+                    const uint16_t f = info[i];
+                    if (!(f & 0x8000u)) return;
+                    const double ri = (double)b[i] - lap_d(p, f, i, nb);
+                    r[i] = ri;
+                    acc += ri * ri;
+                });
+            }
+            if (!red.run(ctl, pair_of(acc), FSum(), 0, rr, u1, u2)) return;
+            if (rr < thr) { conv = 1; break; }
+            const double beta = rr / old;
+            for_rows(a, ch, [&](int i) {
+                if (info[i] & 0x8000u) d[i] = r[i] + beta * d[i];
+            });
+            if (!grid_barrier(ctl)) return;
+        }
+        it += 1;
+    }
+    for_rows(a, ch, [&](int i) {
+        if (info[i] & 0x8000u) a.p[i] = (float)p[i];
+    });
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->converged = conv;
+        ctl->iterations = it;
+        ctl->rr = rr;
+        ctl->bb = bb;
+        ctl->thr = thr;
+        ctl->active_chunks = M;
+        ctl->active_cells = (long long)nrows;
+        ctl->total_iterations += it;
+        ctl->solves += 1;
+        ctl->sum_iter_rows += (double)it * nrows;
+        ctl->sum_rows += nrows;
+    }
+}
+
+// Start of both solver kernels: ordered compaction of the active chunks into a.chunk_list (two grid
+// barriers), then this block's share of the list cached in shared memory.  M = active chunks.
+__device__ __forceinline__ bool solver_prologue(const SolverArgs& a, Chunks& ch, int& M) {
     if (threadIdx.x == 0) barrier_index() = 0u;
     __shared__ int s_scan[SOLVER_THREADS];
     // ---- phase 0: ordered compaction of the active chunks -------------------------------------------
@@ -470,7 +576,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         for (int k = 0; k < SOLVER_THREADS; k++) t += s_scan[k];
         a.block_count[blockIdx.x] = t;
     }
-    if (!grid_barrier(ctl)) return;
+    if (!grid_barrier(a.ctl)) return false;
     __shared__ int s_off, s_total;
     if (threadIdx.x == 0) {
         int off = 0, tot = 0;
@@ -503,10 +609,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
             base += tile;
         }
     }
-    const int M = s_total;
-    if (!grid_barrier(ctl)) return;
+    M = s_total;
+    if (!grid_barrier(a.ctl)) return false;
     extern __shared__ int s_chunks[];
-    Chunks ch;
     {
         const int per = (M + gridDim.x - 1) / gridDim.x;
         const int c0 = blockIdx.x * per, c1 = min(M, c0 + per);
@@ -516,6 +621,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         __syncthreads();
     }
 
+    return true;
+}
+
+__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
+    DevCtl* ctl = a.ctl;
+    Chunks ch;
+    int M = 0;
+    if (!solver_prologue(a, ch, M)) return;
     const Nb nb = cg_order(a.g);
     const float* __restrict__ b = a.b;
     const uint16_t* __restrict__ info = a.rowinfo;
@@ -709,9 +822,13 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         iters = it + 1;
     }
     if (mixed) {
+        // fold the increment: p64 then holds the FP64 solution (efs_download_pressure_fp64)
         for_rows(a, ch, [&](int i) {
             if (!(info[i] & 0x8000u)) return;
-            p[i] = (float)(p64[i] + (double)e[i]);
+            const double v = p64[i] + (double)e[i];
+            p64[i] = v;
+            e[i] = 0.f;
+            p[i] = (float)v;
         });
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -729,6 +846,15 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
     }
 }
 
+// EFS_CG_FP64 runs in its own kernel so that the study solver does not weigh on k_solver's registers.
+__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver_fp64(SolverArgs a) {
+    Chunks ch;
+    int M = 0;
+    if (!solver_prologue(a, ch, M)) return;
+    Reduction red{reinterpret_cast<float*>(a.partials), 0};
+    cg_fp64(a, ch, cg_order(a.g), red, M);
+}
+
 // The dynamic shared-memory limit is an attribute of the kernel for the whole process: raise it when a grid
 // needs more than the 48 KB default, and never lower it (other contexts may need the larger value).
 std::mutex g_smem_mutex;
@@ -743,14 +869,19 @@ cudaError_t ensure_solver_smem(size_t bytes) {
     const size_t per_block = bytes + 4096 + 1024;   // dynamic + static + reserved, rounded up
     const int pct = (int)std::min<size_t>(100, (2 * per_block * 100 + 228 * 1024 - 1) / (228 * 1024) + 1);
     if (pct > g_carveout_pct) {
-        cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
-        if (e != cudaSuccess) return e;
+        for (auto k : {k_solver, k_solver_fp64}) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+            if (e != cudaSuccess) return e;
+        }
         g_carveout_pct = pct;
     }
     if (bytes <= g_smem_limit) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_solver, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) g_smem_limit = bytes;
-    return e;
+    for (auto k : {k_solver, k_solver_fp64}) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+    }
+    g_smem_limit = bytes;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -805,6 +936,9 @@ cudaError_t launch_solver(efs_ctx* c) {
     a.d0 = c->d0;
     a.d1 = c->d1;
     a.t = c->t;
+    a.r64 = c->r64;
+    a.d64 = c->d64;
+    a.t64 = c->t64;
     a.partials = c->partials;
     a.ctl = c->ctl;
     cudaLaunchConfig_t cfg = {};
@@ -820,7 +954,7 @@ cudaError_t launch_solver(efs_ctx* c) {
     // a fresh barrier for this launch (a previous launch may have aborted mid-barrier)
     cudaError_t e = cudaMemsetAsync(c->ctl, 0, 2 * sizeof(int), c->stream);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_solver, a);
+    return cudaLaunchKernelEx(&cfg, a.cg_variant == EFS_CG_FP64 && a.solver == EFS_SOLVER_CG ? k_solver_fp64 : k_solver, a);
 }
 
 // Launch shape of the solver for a grid of n_chunks 32-cell chunks (the same rule as solver_configure),

@@ -178,6 +178,12 @@ class _GB300Simulator:
         check(lib().efs_download_fields(self._h, fptr(vel), fptr(rho), fptr(gamma), fptr(beta), fptr(divergence),
                                         fptr(pressure)), self._h)
 
+    def pressure_fp64(self):
+        """efs_download_pressure_fp64: the FP64 pressure of the last CG solve, shaped like the fields."""
+        out = np.empty(self._fshape(abi.FIELD_PRESSURE), np.float64)
+        check(lib().efs_download_pressure_fp64(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), self._h)
+        return out
+
     # ---- timing of the pressure solve ----
     def solve_timing_arm(self, capacity):
         check(lib().efs_solve_timing_arm(self._h, capacity), self._h)

@@ -74,12 +74,18 @@ enum efs_solver {
 enum efs_cg_variant {
     EFS_CG_MIXED = 0,
     EFS_CG_REFERENCE = 1,
-    /* EFS_CG_MIXED_RECURRENCE: EFS_CG_MIXED with the work of an iteration rearranged so that only one pass reads
-     * stencil neighbours.  Pass 1 forms t = L d, stores it and sums d.t and t.t; beta is taken from the
-     * residual-norm recurrence r'.r' = alpha^2 t.t - r.r (exact CG identity); pass 2 updates the increment, r and
-     * d in place per cell and sums the exact r'.r' for the stop test.  Every 64th iteration recomputes the
-     * residual in FP64 as the other variants do, and takes that iteration's beta from it. */
-    EFS_CG_MIXED_RECURRENCE = 2
+    /* EFS_CG_MIXED_RECURRENCE (default): EFS_CG_MIXED with t = L d stored and beta taken from the
+     * residual-norm recurrence r'.r' = alpha^2 t.t - r.r (an exact CG identity), so that alpha and beta both
+     * follow from one reduction of d.t and t.t.  The iteration then updates the increment, r and d per cell
+     * and sums the exact r'.r' for the stop test (on the GPU that sum travels with the next iteration's
+     * reduction).  Every 64th iteration recomputes the residual in FP64 as the other variants do, and takes
+     * that iteration's beta from it. */
+    EFS_CG_MIXED_RECURRENCE = 2,
+    /* EFS_CG_FP64: a study solver, not a fast path.  The reference iteration with p, r, d and L d in FP64 and
+     * the threshold tol_rel^2 b.b kept in FP64 (set tol_rel to 1e-12 or so): the FP64 pressure solve of the
+     * same right-hand side that the FP32 results are measured against.  Its FP64 vectors are allocated when
+     * a context first selects it. */
+    EFS_CG_FP64 = 3
 };
 
 /* ---- fields (IGrid3D accessors, IGrid.h:44-68) ---- */
@@ -174,6 +180,11 @@ int  efs_download_fields(efs_ctx* ctx, float* vel, float* rho, float* gamma, flo
                          float* divergence, float* pressure);
 /* Grid3D/Grid2D constructor state (Grid3D.cpp:10-48): zero fields, gamma = 1, solid border, rho = 0 on it. */
 int  efs_reset_fields(efs_ctx* ctx);
+/* No counterpart in the reference.  The FP64 pressure of the last CG solve (N doubles, reference layout):
+ * the FP64 iterate for EFS_CG_FP64, the FP64 accumulator with its increment folded in for the mixed
+ * variants (the FP32 pressure field is this value rounded).  Matrix rows only; other cells hold stale
+ * values.  EFS_ERR_STATE for Jacobi and EFS_CG_REFERENCE, which keep no FP64 pressure. */
+int  efs_download_pressure_fp64(efs_ctx* ctx, double* host);
 
 /* ---- the step ---- */
 /* One reference stage virtual, regardless of disable_mask. */
