@@ -31,6 +31,16 @@ SIGNATURES = {
     "efs_upload_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP]),
     "efs_download_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP, _FP]),
     "efs_download_pressure_fp64": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_double)]),
+    "efs_unet_param_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
+    "efs_unet_init": (ctypes.c_int, [_CTX, ctypes.c_uint64, ctypes.c_int]),
+    "efs_unet_get_weights": (ctypes.c_int, [_CTX, _FP, ctypes.c_int64]),
+    "efs_unet_set_weights": (ctypes.c_int, [_CTX, _FP, ctypes.c_int64]),
+    "efs_unet_apply": (ctypes.c_int, [_CTX, _FP, _FP]),
+    "efs_unet_loss_grad": (ctypes.c_int, [_CTX, ctypes.c_int, _FP, _FP, _FP, _FP]),
+    "efs_unet_add_sample": (ctypes.c_int, [_CTX]),
+    "efs_unet_sample_count": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int)]),
+    "efs_unet_train": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_uint64, _FP]),
     "efs_reset_fields": (ctypes.c_int, [_CTX]),
     "efs_stage": (ctypes.c_int, [_CTX, ctypes.c_int]),
     "efs_step": (ctypes.c_int, [_CTX, ctypes.c_int]),

@@ -19,6 +19,7 @@ STAGE_NAMES = ("vel_decay", "vel_extrapolate", "rho_sharpen", "rho_advect", "vel
 
 SOLVER_JACOBI = 0
 SOLVER_CG = 1
+SOLVER_FCG_UNET = 2
 
 CG_MIXED = 0
 CG_REFERENCE = 1
@@ -88,6 +89,7 @@ class EfsStats(ctypes.Structure):
         ("active_cells", ctypes.c_int64),
         ("total_solve_steps", ctypes.c_int64),
         ("solves", ctypes.c_int64),
+        ("precond_steps", ctypes.c_int64),
     ]
 
     def as_dict(self):

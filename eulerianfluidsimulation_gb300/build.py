@@ -23,6 +23,7 @@ UNITS = {
     "efs_stages.cu": ["--fmad=false"],
     "efs_solver.cu": ["--fmad=false"],
     "efs_noalloc.cu": ["--fmad=false"],
+    "efs_unet.cu": [],
 }
 
 

@@ -31,7 +31,10 @@ int cuda_fail(efs_ctx* c, cudaError_t e, const char* what) {
 bool params_valid(const efs_params* p, std::string& why) {
     if (!p) { why = "params is NULL"; return false; }
     if (!std::isfinite(p->dt) || !std::isfinite(p->gravity_force)) { why = "dt and gravity_force must be finite"; return false; }
-    if (p->solver != EFS_SOLVER_JACOBI && p->solver != EFS_SOLVER_CG) { why = "unknown solver"; return false; }
+    if (p->solver != EFS_SOLVER_JACOBI && p->solver != EFS_SOLVER_CG && p->solver != EFS_SOLVER_FCG_UNET) {
+        why = "unknown solver";
+        return false;
+    }
     if (p->cg_variant != EFS_CG_MIXED && p->cg_variant != EFS_CG_REFERENCE && p->cg_variant != EFS_CG_MIXED_RECURRENCE &&
         p->cg_variant != EFS_CG_FP64) {
         why = "unknown cg_variant";
@@ -207,6 +210,7 @@ void efs_destroy(efs_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
+    efs::unet_free(c);
     void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->fx, c->fy, c->fz, c->solid,
                     c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
                     c->sh_idx, c->sh_val, c->sh_end, c->rowinfo, c->chunk_flag, c->chunk_list, c->block_count,
@@ -311,8 +315,9 @@ int efs_set_params(efs_ctx* c, const efs_params* p) {
 int efs_download_pressure_fp64(efs_ctx* c, double* host) {
     if (!c) return EFS_ERR_ARG;
     if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
-    if (c->prm.solver != EFS_SOLVER_CG || c->prm.cg_variant == EFS_CG_REFERENCE)
-        return fail(c, EFS_ERR_STATE, "no FP64 pressure: the solver is not CG with an FP64 accumulator");
+    const bool fcg = c->prm.solver == EFS_SOLVER_FCG_UNET;
+    if (!fcg && (c->prm.solver != EFS_SOLVER_CG || c->prm.cg_variant == EFS_CG_REFERENCE))
+        return fail(c, EFS_ERR_STATE, "no FP64 pressure: the solver is not CG with an FP64 accumulator, nor FCG");
     CK(cudaMemcpyAsync(host, c->p64, (size_t)c->g.N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "download p64");
     return check_device_status(c);
 }
@@ -415,6 +420,8 @@ int efs_reset_fields(efs_ctx* c) {
 int efs_stage(efs_ctx* c, int stage) {
     if (!c) return EFS_ERR_ARG;
     if (stage < 0 || stage >= EFS_STAGE_COUNT) return fail(c, EFS_ERR_ARG, "unknown stage");
+    if (stage == EFS_STAGE_PROJECT && c->prm.solver == EFS_SOLVER_FCG_UNET && !c->unet)
+        return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
     CK(efs::launch_stage(c, stage, false), "stage launch");
     return EFS_OK;
 }
@@ -423,6 +430,13 @@ int efs_step(efs_ctx* c, int n_steps) {
     if (!c) return EFS_ERR_ARG;
     if (n_steps < 0) return fail(c, EFS_ERR_ARG, "n_steps < 0");
     if (n_steps == 0) return EFS_OK;
+    if (c->prm.solver == EFS_SOLVER_FCG_UNET) {
+        // FCG reads its scalars on the host every iteration, so the step runs as direct launches
+        if (!c->unet) return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
+        for (int k = 0; k < n_steps; k++) CK(enqueue_step(c, EFS_STAGES_ALL & ~c->prm.disable_mask, false), "step");
+        c->frames += n_steps;
+        return EFS_OK;
+    }
     efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
     cudaGraphExec_t exec = nullptr;
     int s = build_graph(c, key, &exec);
@@ -446,6 +460,7 @@ int efs_step(efs_ctx* c, int n_steps) {
 
 int efs_step_kernel_count(efs_ctx* c, int* count) {
     if (!c || !count) return EFS_ERR_ARG;
+    if (c->prm.solver == EFS_SOLVER_FCG_UNET) return fail(c, EFS_ERR_STATE, "FCG steps are not captured in a graph");
     efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
     cudaGraphExec_t exec = nullptr;
     int s = build_graph(c, key, &exec);
@@ -456,6 +471,8 @@ int efs_step_kernel_count(efs_ctx* c, int* count) {
 
 int efs_solve(efs_ctx* c, efs_stats* out) {
     if (!c) return EFS_ERR_ARG;
+    if (c->prm.solver == EFS_SOLVER_FCG_UNET && !c->unet)
+        return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
     CK(efs::launch_solver_prep(c), "solver prep");
     CK(efs::launch_solver(c), "solver launch");
     int s = efs_get_stats(c, out);
@@ -487,6 +504,7 @@ int efs_get_stats(efs_ctx* c, efs_stats* out) {
         out->active_cells = h.active_cells;
         out->total_solve_steps = h.total_iterations;
         out->solves = h.solves;
+        out->precond_steps = h.precond_iterations;
     }
     return EFS_OK;
 }

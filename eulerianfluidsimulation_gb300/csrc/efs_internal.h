@@ -31,6 +31,7 @@ struct DevCtl {
     int paused;
     int active_chunks;
     int sh_count;              // density-sharpen active-cell count
+    int precond_iterations;    // FCG: iterations of the last solve that applied the preconditioner
     long long active_cells;
     long long total_iterations;
     long long solves;
@@ -79,6 +80,10 @@ struct GraphKey {
 };
 
 }  // namespace efs
+
+namespace efs {
+struct UNetState;
+}
 
 struct efs_ctx {
     int dim = 3;
@@ -139,6 +144,8 @@ struct efs_ctx {
     cudaEvent_t marks[8] = {};
     int64_t frames = 0;
     std::string err;
+
+    efs::UNetState* unet = nullptr;         // learned preconditioner (efs_unet.cu)
 };
 
 namespace efs {
@@ -150,6 +157,9 @@ cudaError_t launch_solver_prep(efs_ctx* c);
 // efs_solver.cu
 cudaError_t solver_configure(efs_ctx* c);
 cudaError_t launch_solver(efs_ctx* c);
+// efs_unet.cu: FCG with the U-Net preconditioner (host-driven, not graph-capturable), and teardown
+cudaError_t fcg_solve(efs_ctx* c);
+void unet_free(efs_ctx* c);
 // efs_fields.cu
 cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc);
 cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc);

@@ -554,6 +554,7 @@ __device__ __forceinline__ void cg_fp64(const SolverArgs& a, const Chunks& ch, c
         ctl->active_cells = (long long)nrows;
         ctl->total_iterations += it;
         ctl->solves += 1;
+        ctl->precond_iterations = 0;
         ctl->sum_iter_rows += (double)it * nrows;
         ctl->sum_rows += nrows;
     }
@@ -665,7 +666,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctl->converged = 1; ctl->iterations = iters; ctl->rr = 0; ctl->bb = 0; ctl->thr = 0;
             ctl->active_chunks = M; ctl->active_cells = (long long)nrows;
-            ctl->total_iterations += iters; ctl->solves += 1;
+            ctl->total_iterations += iters; ctl->solves += 1; ctl->precond_iterations = 0;
             ctl->sum_iter_rows += (double)iters * nrows; ctl->sum_rows += nrows;
         }
         return;
@@ -841,6 +842,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         ctl->active_cells = (long long)nrows;
         ctl->total_iterations += iters;
         ctl->solves += 1;
+        ctl->precond_iterations = 0;
         ctl->sum_iter_rows += (double)iters * nrows;
         ctl->sum_rows += nrows;
     }
@@ -915,6 +917,7 @@ cudaError_t solver_configure(efs_ctx* c) {
 }
 
 cudaError_t launch_solver(efs_ctx* c) {
+    if (c->prm.solver == EFS_SOLVER_FCG_UNET) return fcg_solve(c);
     SolverArgs a;
     a.g = c->g;
     a.dim = c->dim;

@@ -1,0 +1,387 @@
+// efs_tc.cuh — 5th-generation tensor-core (tcgen05) building blocks for sm_103a and the two GEMM-shaped
+// kernels of the U-Net preconditioner: the implicit-GEMM 3x3x3 convolution (forward, and input gradient
+// with flipped/transposed weights) and the weight-gradient GEMM.
+//
+// Operand staging.  Both operands of every tcgen05.mma are K-major BF16 tiles in shared memory in the
+// canonical no-swizzle layout: 8-row x 16-byte core matrices (8 rows of 8 BF16 along K, 128 contiguous
+// bytes).  A tile of R rows x 16 K-elements (one MMA K-step) is R/8 row groups x 2 K groups; core matrix
+// (row group g, K group k) sits at g * 256 + k * 128 bytes, i.e. leading (K) byte offset 128 and stride
+// (row group) byte offset 256 in the shared-memory descriptor.  Accumulators are FP32 in tensor memory
+// (TMEM): row i of the M = 128 tile is TMEM lane i, output channel n is column n.
+//
+// Every wait on an mbarrier is bounded in time; on expiry the kernel records an error, waits (bounded
+// again) for its own MMAs, frees its TMEM and returns.
+#pragma once
+#include <cstdint>
+#include <cuda_bf16.h>
+
+namespace efs {
+namespace tc {
+
+constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// ---- mbarrier -------------------------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Waits until the phase with the given parity has completed; false after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_test(bar, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    while (!mbar_test(bar, parity)) {
+        if (now_ns() - t0 > kWaitNs) return false;
+    }
+    return true;
+}
+
+// ---- tensor memory ----------------------------------------------------------------------------------------
+// Allocation by one whole warp; the TMEM address is written to *slot (shared memory).
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Generic-proxy shared-memory writes (plain stores, cp.async) made visible to the tensor cores' async proxy.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes: thread l of the warp gets lane (base + l).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- MMA ---------------------------------------------------------------------------------------------------
+// Shared-memory matrix descriptor: no swizzle, K-major, byte offsets as described at the top of this file.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version of the sm_100 family; base offset 0; layout: no swizzle
+    return d;
+}
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 accumulator, shape M x N (x K = 16).
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// D (TMEM) = A * B^T (+ D when accumulate != 0), issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// The mbarrier receives one arrival when every tcgen05 operation this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// ---- cp.async ----------------------------------------------------------------------------------------------
+// 16 bytes global -> shared; zero-filled when !valid (src must still be a mapped address).
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(valid ? 16u : 0u)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Byte offset of element (row, k) (k < 16) in a K-major no-swizzle tile (see the top of this file).
+__host__ __device__ __forceinline__ uint32_t tile_off(int row, int k) {
+    return (uint32_t)((row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// ============================================================================================================
+// Implicit-GEMM 3x3x3 convolution, zero padding ("same"), channel-last BF16 tensors.
+//   out[v][n] = sum_{tap, c} in[v + off(tap)][c] * w[tap][c][n]   (+ bias, ReLU, + skip)
+// GEMM view per block: M = 128 voxels (linear index v = (z*H + y)*W + x), N = COUT, K = 27 * CIN in steps of
+// one tap x 16 channels.  Weights are pre-arranged as wt[tap][c/16][n][16] (BF16) so a K-step's B tile is
+// COUT rows of 32 contiguous bytes.  Two operand buffers: the loads of step s+1 fly while MMA s runs.
+// ============================================================================================================
+struct ConvArgs {
+    const __nv_bfloat16* in;    // [V][cin]
+    const __nv_bfloat16* wt;    // [27][cin/16][COUT][16]
+    const float* bias;          // [COUT] or null
+    const __nv_bfloat16* skip;  // [V][COUT] added after the activation, or null
+    __nv_bfloat16* out;         // [V][COUT] (BF16) or null
+    float* out32;               // [V][COUT] (FP32) or null
+    __nv_bfloat16* pre;         // [V][COUT] pre-activation (BF16, for the ReLU mask of the backward pass) or null
+    int D, H, W, cin;
+    int relu;
+    int* err;                   // error word: bit 0 = an mbarrier wait gave up
+};
+
+constexpr int kConvThreads = 128;
+constexpr int kConvSmem = 32 * 1024;   // also caps residency at 7 blocks/SM: 7 x 64 TMEM columns <= 512
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
+    static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
+    constexpr int kABytes = 128 * 32, kBBytes = COUT * 32;
+    constexpr uint32_t kCols = COUT < 32 ? 32 : COUT;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* bufA[2] = {smem, smem + kABytes};
+    unsigned char* bufB[2] = {smem + 2 * kABytes, smem + 2 * kABytes + kBBytes};
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * kABytes + 2 * kBBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int V = a.D * a.H * a.W;
+    const int v = blockIdx.x * 128 + tid;
+    const bool vin = v < V;
+    const int x = vin ? v % a.W : 0, y = vin ? (v / a.W) % a.H : 0, z = vin ? v / (a.W * a.H) : 0;
+    const int chunks = a.cin >> 4;
+    const int S = 27 * chunks;
+
+    if (warp == 0) tmem_alloc(tslot, kCols);
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    auto load = [&](int s, int b) {
+        const int tap = s / chunks, cc = s - tap * chunks;
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const int nx = x + dx, ny = y + dy, nz = z + dz;
+        const bool ok = vin && nx >= 0 && nx < a.W && ny >= 0 && ny < a.H && nz >= 0 && nz < a.D;
+        const __nv_bfloat16* src = ok ? a.in + ((size_t)((nz * a.H + ny) * a.W + nx) * a.cin + cc * 16) : a.in;
+        cp_async16(bufA[b] + tile_off(tid, 0), src, ok);
+        cp_async16(bufA[b] + tile_off(tid, 8), src + 8, ok);
+        if (tid < 2 * COUT) {
+            const int n = tid >> 1, kg = tid & 1;
+            const __nv_bfloat16* w = a.wt + ((size_t)(tap * chunks + cc) * COUT + n) * 16 + kg * 8;
+            cp_async16(bufB[b] + tile_off(n, kg * 8), w, true);
+        }
+        cp_async_commit();
+    };
+
+    bool ok = true;
+    load(0, 0);
+    for (int s = 0; s < S && ok; s++) {
+        const int b = s & 1;
+        if (s + 1 < S) {
+            // buffer b^1 was read by MMA s-1: wait for it before refilling
+            if (s >= 1 && !mbar_wait(&mbar[b ^ 1], ((s - 1) >> 1) & 1)) { ok = false; break; }
+            load(s + 1, b ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint64_t ad = sdesc(smem_u32(bufA[b]), 128, 256);
+            const uint64_t bd = sdesc(smem_u32(bufB[b]), 128, 256);
+            mma_bf16(tmem, ad, bd, idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
+            mma_commit(&mbar[b]);
+        }
+    }
+    cp_async_wait<0>();
+    // all MMAs (the last commit covers every earlier one), and the other buffer's last arrival
+    const int last = S - 1;
+    if (ok && !mbar_wait(&mbar[last & 1], (last >> 1) & 1)) ok = false;
+    if (ok && last >= 1 && !mbar_wait(&mbar[(last - 1) & 1], ((last - 1) >> 1) & 1)) ok = false;
+    if (!ok) {
+        if (tid == 0) atomicOr(a.err, 1);
+        mbar_wait(&mbar[last & 1], (last >> 1) & 1);   // bounded: let MMAs in flight finish before freeing TMEM
+    }
+    tc_fence_after();
+    if (ok) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)c0, acc);
+            if (vin) {
+                __align__(16) __nv_bfloat16 o[16], pr[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
+                    pr[j] = __float2bfloat16(t);
+                    if (a.relu) t = fmaxf(t, 0.f);
+                    if (a.skip) t += __bfloat162float(a.skip[(size_t)v * COUT + c0 + j]);
+                    o[j] = __float2bfloat16(t);
+                    if (a.out32) a.out32[(size_t)v * COUT + c0 + j] = t;
+                }
+                if (a.out) {
+                    uint4* dst = reinterpret_cast<uint4*>(a.out + (size_t)v * COUT + c0);
+                    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                }
+                if (a.pre) {
+                    uint4* dst = reinterpret_cast<uint4*>(a.pre + (size_t)v * COUT + c0);
+                    dst[0] = reinterpret_cast<const uint4*>(pr)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+// ============================================================================================================
+// Weight gradient:  dw[tap][c][n] += sum_v in[v + off(tap)][c] * g[v][n]
+// GEMM view: M = 27 * CIN rows (row = tap * CIN + c), tiles of 128 (blockIdx.x); N = COUT; K = voxels, in
+// steps of 16, over the voxel range of blockIdx.y.  Operands are transposed into the K-major tiles with
+// plain shared stores.  Each block adds its FP32 partial into dw with atomics.
+// ============================================================================================================
+struct WgradArgs {
+    const __nv_bfloat16* in;   // [V][cin]
+    const __nv_bfloat16* g;    // [V][COUT]
+    float* dw;                 // [27 * cin][COUT] FP32, accumulated
+    int D, H, W, cin;
+    int vox_per_block;         // multiple of 16
+    int* err;
+};
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvThreads) k_wgrad3_tc(WgradArgs a) {
+    static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
+    constexpr int kABytes = 128 * 32, kBBytes = COUT * 32;
+    constexpr uint32_t kCols = COUT < 32 ? 32 : COUT;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* bufA[2] = {smem, smem + kABytes};
+    unsigned char* bufB[2] = {smem + 2 * kABytes, smem + 2 * kABytes + kBBytes};
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * kABytes + 2 * kBBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int V = a.D * a.H * a.W;
+    const int rows = 27 * a.cin;
+    const int row = blockIdx.x * 128 + tid;          // this thread's A row
+    const bool rin = row < rows;
+    const int tap = rin ? row / a.cin : 0, c = rin ? row - tap * a.cin : 0;
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    const int v0 = blockIdx.y * a.vox_per_block;
+    const int v1 = min(V, v0 + a.vox_per_block);
+    const int S = (v1 > v0) ? (v1 - v0 + 15) / 16 : 0;
+
+    if (warp == 0) tmem_alloc(tslot, kCols);
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    bool ok = true;
+    for (int s = 0; s < S && ok; s++) {
+        const int b = s & 1;
+        const int vs = v0 + s * 16;
+        // gather this step's operands into registers before waiting for the buffer
+        __align__(16) __nv_bfloat16 av[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int vv = vs + j;
+            __nv_bfloat16 t = __float2bfloat16(0.f);
+            if (rin && vv < v1) {
+                const int x = vv % a.W, y = (vv / a.W) % a.H, z = vv / (a.W * a.H);
+                const int nx = x + dx, ny = y + dy, nz = z + dz;
+                if (nx >= 0 && nx < a.W && ny >= 0 && ny < a.H && nz >= 0 && nz < a.D)
+                    t = a.in[(size_t)((nz * a.H + ny) * a.W + nx) * a.cin + c];
+            }
+            av[j] = t;
+        }
+        __align__(16) __nv_bfloat16 bv[16];
+        if (tid < COUT) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int vv = vs + j;
+                bv[j] = (vv < v1) ? a.g[(size_t)vv * COUT + tid] : __float2bfloat16(0.f);
+            }
+        }
+        if (s >= 2 && !mbar_wait(&mbar[b], ((s - 2) >> 1) & 1)) { ok = false; break; }
+        *reinterpret_cast<uint4*>(bufA[b] + tile_off(tid, 0)) = reinterpret_cast<const uint4*>(av)[0];
+        *reinterpret_cast<uint4*>(bufA[b] + tile_off(tid, 8)) = reinterpret_cast<const uint4*>(av)[1];
+        if (tid < COUT) {
+            *reinterpret_cast<uint4*>(bufB[b] + tile_off(tid, 0)) = reinterpret_cast<const uint4*>(bv)[0];
+            *reinterpret_cast<uint4*>(bufB[b] + tile_off(tid, 8)) = reinterpret_cast<const uint4*>(bv)[1];
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint64_t ad = sdesc(smem_u32(bufA[b]), 128, 256);
+            const uint64_t bd = sdesc(smem_u32(bufB[b]), 128, 256);
+            mma_bf16(tmem, ad, bd, idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
+            mma_commit(&mbar[b]);
+        }
+    }
+    if (S > 0) {
+        const int last = S - 1;
+        if (ok && !mbar_wait(&mbar[last & 1], (last >> 1) & 1)) ok = false;
+        if (ok && last >= 1 && !mbar_wait(&mbar[(last - 1) & 1], ((last - 1) >> 1) & 1)) ok = false;
+        if (!ok) {
+            if (tid == 0) atomicOr(a.err, 1);
+            mbar_wait(&mbar[last & 1], (last >> 1) & 1);
+        }
+    }
+    tc_fence_after();
+    if (ok && S > 0) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)c0, acc);
+            if (rin) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) atomicAdd(&a.dw[(size_t)row * COUT + c0 + j], acc[j]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+}  // namespace tc
+}  // namespace efs

@@ -1,0 +1,1128 @@
+// efs_unet.cu — the learned preconditioner: a 3-level 3D convolutional U-Net (16/32/64 channels, BF16
+// weights and activations, FP32 accumulation in tensor memory), its training on the GPU with the project's
+// own forward and backward kernels, and flexible preconditioned CG (FCG) with plain CG as the fallback.
+//
+// No counterpart in the reference (its solvers are CGSolverCPU3D / JacobiSolverCPU3D,
+// src/simulation/solver/CGSolver.cpp:416-497, JacobiSolver.cpp:154-212); FCG solves the same matrix
+// L p = b as those (rows: liquid, non-solid cells; see k_solver_prep) to the same stop rule.
+//
+// Network (all convolutions 3x3x3, zero padding; level l has the grid dimensions halved l times, rounded up):
+//   x0  = [r / rms(r), row mask, 0 x 14]                   level 0, 16 channels (BF16)
+//   e0  = relu(conv0(x0))            16 -> 16              level 0
+//   e1  = relu(conv1(pool(e0)))      16 -> 32              level 1 (pool: 2x2x2 mean)
+//   e2  = relu(conv2(pool(e1)))      32 -> 64              level 2
+//   d1  = relu(conv3(up(e2))) + e1   64 -> 32              level 1 (up: nearest)
+//   d0  = relu(conv4(up(d1))) + e0   32 -> 16              level 0
+//   y   = conv5(d0)[channel 0]       16 -> 16 (FP32)       level 0
+// Parameters: layer k's weights w[tap][cin][cout] then its bias[cout], layers in order (FP32 master copy;
+// BF16 copies in the tcgen05 operand layouts).  The preconditioner is z = y on matrix rows, 0 elsewhere.
+// FCG is invariant to the scale of z, so neither the input normalisation nor the output scale matters to it.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "efs_internal.h"
+#include "efs_tc.cuh"
+
+using bf16 = __nv_bfloat16;
+
+namespace efs {
+
+namespace {
+
+constexpr int kLayers = 6;
+struct LayerSpec {
+    int cin, cout, level;
+};
+constexpr LayerSpec kSpec[kLayers] = {{16, 16, 0}, {16, 32, 1}, {32, 64, 2}, {64, 32, 1}, {32, 16, 0}, {16, 16, 0}};
+
+long long param_count_host() {
+    long long n = 0;
+    for (const auto& s : kSpec) n += 27LL * s.cin * s.cout + s.cout;
+    return n;
+}
+
+struct Level {
+    int D, H, W;
+    long long V;
+};
+
+}  // namespace
+
+struct UNetState {
+    Level L[3];
+    long long woff[kLayers], boff[kLayers], nparam = 0;
+    float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
+    int adam_t = 0;
+    bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
+    // activations (level of each in brackets)
+    bf16 *x0 = nullptr, *e0 = nullptr, *p0 = nullptr, *e1 = nullptr, *p1 = nullptr, *e2 = nullptr, *u2 = nullptr,
+         *d1 = nullptr, *u1 = nullptr, *d0 = nullptr;
+    float* y32 = nullptr;
+    // training: pre-activations and gradients
+    bool train_ready = false;
+    bf16 *a0 = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *a4 = nullptr;
+    bf16 *g5 = nullptr, *gd0 = nullptr, *ga4 = nullptr, *gu1 = nullptr, *gd1 = nullptr, *ga3 = nullptr, *gu2 = nullptr,
+         *ge2 = nullptr, *ga2 = nullptr, *gp1 = nullptr, *ge1 = nullptr, *ga1 = nullptr, *gp0 = nullptr, *ge0 = nullptr,
+         *ga0 = nullptr;
+    // scalars and reductions
+    double* dscal = nullptr;     // [0] sum, [1] count, [2] 1/rms (input); [3..5] the same for the target; [8..10] dots
+    double* dpart = nullptr;     // block partials
+    double* dloss = nullptr;     // [0] loss
+    int* err = nullptr;
+    // training set: (b, p, rowinfo) per sample
+    int cap = 0, count = 0, next = 0;
+    float *sb = nullptr, *sp = nullptr;
+    uint16_t* srow = nullptr;
+    float* tmp_in = nullptr;     // one scalar field: input staging
+    float* tmp_t = nullptr;
+    float *tz = nullptr, *tq = nullptr;   // training: z = net output and L z (energy loss)
+    // FCG vectors
+    double* x64 = nullptr;
+    float *fr = nullptr, *fz = nullptr, *fd = nullptr, *fq = nullptr;
+    double* hdots = nullptr;     // pinned host copy of the dot products
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+constexpr int kRedBlocks = 512;
+
+// ---- small kernels -------------------------------------------------------------------------------------------
+// sum of x^2 and count over matrix rows -> block partials [2 * blockIdx]
+__global__ void k_sumsq_rows(const float* __restrict__ x, const uint16_t* __restrict__ rowinfo, long long n,
+                             double* __restrict__ part) {
+    double s = 0, c = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (rowinfo[i] & 0x8000u) {
+            const double v = x[i];
+            s += v * v;
+            c += 1;
+        }
+    }
+    __shared__ double ss[256], sc[256];
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { ss[threadIdx.x] += ss[threadIdx.x + o]; sc[threadIdx.x] += sc[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = ss[0]; part[2 * blockIdx.x + 1] = sc[0]; }
+}
+// out[0] = sum, out[1] = count, out[2] = 1 / sqrt(sum / count) (1 when the sum is 0)
+__global__ void k_finish_scale(const double* __restrict__ part, int nb, double* __restrict__ out) {
+    __shared__ double ss[256], sc[256];
+    double s = 0, c = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) { s += part[2 * b]; c += part[2 * b + 1]; }
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { ss[threadIdx.x] += ss[threadIdx.x + o]; sc[threadIdx.x] += sc[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = ss[0];
+        out[1] = sc[0];
+        out[2] = (ss[0] > 0 && sc[0] > 0) ? 1.0 / sqrt(ss[0] / sc[0]) : 1.0;
+    }
+}
+
+// x0[v] = [r * inv, mask, 0...] on rows, 0 elsewhere
+__global__ void k_pack(const float* __restrict__ r, const uint16_t* __restrict__ rowinfo, const double* __restrict__ scal,
+                       long long n, bf16* __restrict__ x0) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const bool row = rowinfo[v] & 0x8000u;
+    __align__(16) bf16 o[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) o[j] = __float2bfloat16(0.f);
+    if (row) {
+        o[0] = __float2bfloat16((float)((double)r[v] * scal[2]));
+        o[1] = __float2bfloat16(1.f);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(x0 + v * 16);
+    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+}
+
+__device__ __forceinline__ void unpack8(uint4 u, float (&f)[8]) {
+    const bf16* b = reinterpret_cast<const bf16*>(&u);
+#pragma unroll
+    for (int j = 0; j < 8; j++) f[j] = __bfloat162float(b[j]);
+}
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+    __align__(16) bf16 b[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) b[j] = __float2bfloat16(f[j]);
+    return *reinterpret_cast<const uint4*>(b);
+}
+
+// 2x2x2 mean over the children that exist; one thread per (parent voxel, 8 channels)
+__global__ void k_pool(const bf16* __restrict__ in, Level lc, bf16* __restrict__ out, Level lp, int C) {
+    const int g8 = C / 8;
+    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (item >= lp.V * g8) return;
+    const long long pv = item / g8;
+    const int g = (int)(item - pv * g8);
+    const int px = (int)(pv % lp.W), py = (int)((pv / lp.W) % lp.H), pz = (int)(pv / ((long long)lp.W * lp.H));
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int cnt = 0;
+    for (int dz = 0; dz < 2; dz++)
+        for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++) {
+                const int x = 2 * px + dx, y = 2 * py + dy, z = 2 * pz + dz;
+                if (x >= lc.W || y >= lc.H || z >= lc.D) continue;
+                float f[8];
+                unpack8(*reinterpret_cast<const uint4*>(in + (((long long)z * lc.H + y) * lc.W + x) * C + g * 8), f);
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[j] += f[j];
+                cnt++;
+            }
+    const float inv = 1.f / (float)cnt;
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] *= inv;
+    *reinterpret_cast<uint4*>(out + pv * C + g * 8) = pack8(acc);
+}
+// nearest up-sampling: out[child] = in[parent]
+__global__ void k_up(const bf16* __restrict__ in, Level lp, bf16* __restrict__ out, Level lc, int C) {
+    const int g8 = C / 8;
+    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (item >= lc.V * g8) return;
+    const long long v = item / g8;
+    const int g = (int)(item - v * g8);
+    const int x = (int)(v % lc.W), y = (int)((v / lc.W) % lc.H), z = (int)(v / ((long long)lc.W * lc.H));
+    const long long pv = ((long long)(z >> 1) * lp.H + (y >> 1)) * lp.W + (x >> 1);
+    *reinterpret_cast<uint4*>(out + v * C + g * 8) = *reinterpret_cast<const uint4*>(in + pv * C + g * 8);
+}
+// gradient of k_up: parent gets the sum of its children's gradients
+__global__ void k_up_bwd(const bf16* __restrict__ gc, Level lc, bf16* __restrict__ gp, Level lp, int C) {
+    const int g8 = C / 8;
+    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (item >= lp.V * g8) return;
+    const long long pv = item / g8;
+    const int g = (int)(item - pv * g8);
+    const int px = (int)(pv % lp.W), py = (int)((pv / lp.W) % lp.H), pz = (int)(pv / ((long long)lp.W * lp.H));
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dz = 0; dz < 2; dz++)
+        for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++) {
+                const int x = 2 * px + dx, y = 2 * py + dy, z = 2 * pz + dz;
+                if (x >= lc.W || y >= lc.H || z >= lc.D) continue;
+                float f[8];
+                unpack8(*reinterpret_cast<const uint4*>(gc + (((long long)z * lc.H + y) * lc.W + x) * C + g * 8), f);
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[j] += f[j];
+            }
+    *reinterpret_cast<uint4*>(gp + pv * C + g * 8) = pack8(acc);
+}
+// gradient of k_pool: child gets parent's gradient / (parent's child count), plus an optional skip gradient
+__global__ void k_pool_bwd(const bf16* __restrict__ gp, Level lp, bf16* __restrict__ gc, Level lc, int C,
+                           const bf16* __restrict__ skip) {
+    const int g8 = C / 8;
+    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (item >= lc.V * g8) return;
+    const long long v = item / g8;
+    const int g = (int)(item - v * g8);
+    const int x = (int)(v % lc.W), y = (int)((v / lc.W) % lc.H), z = (int)(v / ((long long)lc.W * lc.H));
+    const int px = x >> 1, py = y >> 1, pz = z >> 1;
+    const int nx = min(2, lc.W - 2 * px), ny = min(2, lc.H - 2 * py), nz = min(2, lc.D - 2 * pz);
+    const float inv = 1.f / (float)(nx * ny * nz);
+    float f[8];
+    unpack8(*reinterpret_cast<const uint4*>(gp + (((long long)pz * lp.H + py) * lp.W + px) * C + g * 8), f);
+#pragma unroll
+    for (int j = 0; j < 8; j++) f[j] *= inv;
+    if (skip) {
+        float s[8];
+        unpack8(*reinterpret_cast<const uint4*>(skip + v * C + g * 8), s);
+#pragma unroll
+        for (int j = 0; j < 8; j++) f[j] += s[j];
+    }
+    *reinterpret_cast<uint4*>(gc + v * C + g * 8) = pack8(f);
+}
+// out = g where pre > 0, else 0
+__global__ void k_relu_bwd(const bf16* __restrict__ g, const bf16* __restrict__ pre, long long n8, bf16* __restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n8) return;
+    float f[8], p[8];
+    unpack8(reinterpret_cast<const uint4*>(g)[i], f);
+    unpack8(reinterpret_cast<const uint4*>(pre)[i], p);
+#pragma unroll
+    for (int j = 0; j < 8; j++) f[j] = p[j] > 0.f ? f[j] : 0.f;
+    reinterpret_cast<uint4*>(out)[i] = pack8(f);
+}
+// db[c] += sum over voxels of g[v][c]
+__global__ void k_bias_grad(const bf16* __restrict__ g, long long V, int C, float* __restrict__ db) {
+    __shared__ float acc[256];
+    const int lanes = 256 / C;                           // voxels processed side by side per block
+    const int c = threadIdx.x % C, l = threadIdx.x / C;
+    float s = 0.f;
+    for (long long v = blockIdx.x * (long long)lanes + l; v < V; v += (long long)gridDim.x * lanes)
+        s += __bfloat162float(g[v * C + c]);
+    acc[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int k = 0; k < lanes; k++) t += acc[k * C + threadIdx.x];
+        atomicAdd(&db[threadIdx.x], t);
+    }
+}
+// loss = sum_rows (y - t)^2 / rows with t = p / rms(p); g5 = dloss/dy (channel 0), 0 on the other channels
+__global__ void k_loss(const float* __restrict__ y32, const float* __restrict__ p, const uint16_t* __restrict__ rowinfo,
+                       const double* __restrict__ tscal, long long n, bf16* __restrict__ g5, double* __restrict__ part) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double l = 0;
+    __align__(16) bf16 o[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) o[j] = __float2bfloat16(0.f);
+    if (v < n) {
+        if (rowinfo[v] & 0x8000u) {
+            const double t = (double)p[v] * tscal[2];
+            const double d = (double)y32[v * 16] - t;
+            l = d * d;
+            o[0] = __float2bfloat16((float)(2.0 * d / tscal[1]));
+        }
+        uint4* dst = reinterpret_cast<uint4*>(g5 + v * 16);
+        dst[0] = reinterpret_cast<const uint4*>(o)[0];
+        dst[1] = reinterpret_cast<const uint4*>(o)[1];
+    }
+    __shared__ double s[256];
+    s[threadIdx.x] = l;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+// Energy-norm alignment loss of the preconditioner output z (channel 0 of y32, on rows) for input r and
+// error e (L e = r):  loss = 1 - (z.r)^2 / ((z.Lz) (e.r)), the fraction of the error's energy norm that a
+// line search along z leaves.  dots = (a, c, k) = (z.r, z.Lz, e.r); q = L z.
+__global__ void k_energy_grad(const float* __restrict__ r, const float* __restrict__ q, const uint16_t* __restrict__ rowinfo,
+                              const double* __restrict__ dots, long long n, bf16* __restrict__ g5) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    __align__(16) bf16 o[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) o[j] = __float2bfloat16(0.f);
+    const double a = dots[0], cz = dots[1], k = dots[2];
+    if ((rowinfo[v] & 0x8000u) && cz != 0.0 && k != 0.0) {
+        const double g = -2.0 * a / (cz * k) * (double)r[v] + 2.0 * a * a / (cz * cz * k) * (double)q[v];
+        o[0] = __float2bfloat16((float)g);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(g5 + v * 16);
+    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+}
+__global__ void k_energy_loss(const double* __restrict__ dots, double* __restrict__ out) {
+    const double a = dots[0], cz = dots[1], k = dots[2];
+    out[0] += (cz != 0.0 && k != 0.0) ? 1.0 - a * a / (cz * k) : 1.0;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ part, int nb, const double* __restrict__ tscal, double* out) {
+    __shared__ double s[256];
+    double a = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) a += part[b];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) s[threadIdx.x] += s[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] += (tscal[1] > 0 ? s[0] / tscal[1] : 0.0);
+}
+// FP32 master weights -> BF16 operand layouts: forward wf[tap][cin/16][cout][16]; input gradient
+// wb[tap'][cout/16][cin][16] with tap' = 26 - tap (negated offsets) and the channel roles swapped.
+__global__ void k_w_to_bf16(const float* __restrict__ w, int cin, int cout, bf16* __restrict__ wf, bf16* __restrict__ wb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 27 * cin * cout) return;
+    const int co = i % cout, ci = (i / cout) % cin, tap = i / (cout * cin);
+    const bf16 v = __float2bfloat16(w[i]);
+    wf[(((size_t)tap * (cin / 16) + ci / 16) * cout + co) * 16 + ci % 16] = v;
+    wb[(((size_t)(26 - tap) * (cout / 16) + co / 16) * cin + ci) * 16 + co % 16] = v;
+}
+__global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2, float gscale) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * gscale;
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+// He-normal initial weights from a counter-based hash (Box-Muller), biases 0
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__global__ void k_init(float* __restrict__ w, long long n, long long nw, float stdv, unsigned long long seed,
+                       unsigned long long salt) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (i >= nw) { w[i] = 0.f; return; }
+    const unsigned long long h = mix64(seed ^ (salt << 32) ^ (unsigned long long)i);
+    const double u1 = ((h >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+    const double u2 = (mix64(h) >> 11) * (1.0 / 9007199254740992.0);
+    w[i] = (float)(stdv * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+}
+// Synthetic training pair: a random error field e on the rows, the sum over lattice spacings s of
+// amp[k] * (trilinear interpolation of hash values on the lattice of spacing s); r = L e is formed after.
+__device__ __forceinline__ float lattice_value(unsigned long long seed, int k, int ix, int iy, int iz) {
+    const unsigned long long h = mix64(seed ^ ((unsigned long long)k << 56) ^ ((unsigned long long)(unsigned)ix << 36) ^
+                                       ((unsigned long long)(unsigned)iy << 18) ^ (unsigned long long)(unsigned)iz);
+    return (float)((h >> 40) * (1.0 / 16777216.0)) * 2.f - 1.f;
+}
+struct SynthAmp {
+    float a[5];
+};
+__global__ void k_synth_error(Level L, const uint16_t* __restrict__ rowinfo, unsigned long long seed, SynthAmp amp,
+                              float* __restrict__ e) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (v >= L.V) return;
+    if (!(rowinfo[v] & 0x8000u)) { e[v] = 0.f; return; }
+    const int x = (int)(v % L.W), y = (int)((v / L.W) % L.H), z = (int)(v / ((long long)L.W * L.H));
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int s = 1 << k;
+        const float fx = (float)x / s, fy = (float)y / s, fz = (float)z / s;
+        const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+        const float tx = fx - ix, ty = fy - iy, tz = fz - iz;
+        float c = 0.f;
+#pragma unroll
+        for (int corner = 0; corner < 8; corner++) {
+            const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+            const float w = (dx ? tx : 1.f - tx) * (dy ? ty : 1.f - ty) * (dz ? tz : 1.f - tz);
+            c += w * lattice_value(seed, k, ix + dx, iy + dy, iz + dz);
+        }
+        acc += amp.a[k] * c;
+    }
+    e[v] = acc;
+}
+
+// z = y (channel 0) on rows, 0 elsewhere
+__global__ void k_unpack(const float* __restrict__ y32, const uint16_t* __restrict__ rowinfo, long long n, float* __restrict__ z) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    z[v] = (rowinfo[v] & 0x8000u) ? y32[v * 16] : 0.f;
+}
+
+// ---- FCG kernels (matrix of k_solver_prep: rowinfo bits x-1, x+1, y-1, y+1, z-1, z+1) -------------------------
+struct Off6 {
+    long long o[6];
+};
+__device__ __forceinline__ int fcg_bit(int k) { return (k == 4) ? 5 : (k == 5 ? 4 : k); }   // order x-1,x+1,y-1,y+1,z+1,z-1
+__global__ void k_fcg_matvec(const float* __restrict__ d, const uint16_t* __restrict__ rowinfo, long long n, Off6 off,
+                             float* __restrict__ q) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint16_t f = rowinfo[i];
+    if (!(f & 0x8000u)) { q[i] = 0.f; return; }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        if (f & (1u << fcg_bit(k))) s += d[i + off.o[fcg_bit(k)]];
+    q[i] = s - (float)((f >> 8) & 7) * d[i];
+}
+// r = b - L x in FP64, rounded to FP32 (rows), 0 elsewhere
+__global__ void k_fcg_resid(const float* __restrict__ b, const double* __restrict__ x, const uint16_t* __restrict__ rowinfo,
+                            long long n, Off6 off, float* __restrict__ r) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint16_t f = rowinfo[i];
+    if (!(f & 0x8000u)) { r[i] = 0.f; return; }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        if (f & (1u << fcg_bit(k))) s += x[i + off.o[fcg_bit(k)]];
+    r[i] = (float)((double)b[i] - (s - (double)((f >> 8) & 7) * x[i]));
+}
+// three dot products at once (pairs (a0,b0), (a1,b1), (a2,b2); null pairs give 0) -> block partials
+__global__ void k_dots3(const float* a0, const float* b0, const float* a1, const float* b1, const float* a2, const float* b2,
+                        long long n, double* __restrict__ part) {
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (a0) s0 += (double)a0[i] * b0[i];
+        if (a1) s1 += (double)a1[i] * b1[i];
+        if (a2) s2 += (double)a2[i] * b2[i];
+    }
+    __shared__ double sh[3][256];
+    sh[0][threadIdx.x] = s0;
+    sh[1][threadIdx.x] = s1;
+    sh[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + k];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + k];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = sh[0][0];
+        part[3 * blockIdx.x + 1] = sh[1][0];
+        part[3 * blockIdx.x + 2] = sh[2][0];
+    }
+}
+__global__ void k_dots3_finish(const double* __restrict__ part, int nb, double* __restrict__ out) {
+    __shared__ double sh[3][256];
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) { s0 += part[3 * b]; s1 += part[3 * b + 1]; s2 += part[3 * b + 2]; }
+    sh[0][threadIdx.x] = s0;
+    sh[1][threadIdx.x] = s1;
+    sh[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + k];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + k];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = sh[0][0]; out[1] = sh[1][0]; out[2] = sh[2][0]; }
+}
+__global__ void k_fcg_xr(double* __restrict__ x, float* __restrict__ r, const float* __restrict__ d, const float* __restrict__ q,
+                         long long n, double alpha) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] += alpha * (double)d[i];
+    r[i] = (float)((double)r[i] - alpha * (double)q[i]);
+}
+__global__ void k_fcg_dir(float* __restrict__ d, const float* __restrict__ z, long long n, double beta) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d[i] = (float)((double)z[i] + beta * (double)d[i]);
+}
+__global__ void k_fcg_init(const float* __restrict__ b, const uint16_t* __restrict__ rowinfo, long long n, double* __restrict__ x) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = 0.0;   // FCG starts from 0: its first residual is b, the kind of field the network was trained on
+}
+__global__ void k_fcg_out(const double* __restrict__ x, const uint16_t* __restrict__ rowinfo, long long n, float* __restrict__ p,
+                          double* __restrict__ p64) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (rowinfo[i] & 0x8000u) {
+        p[i] = (float)x[i];
+        p64[i] = x[i];
+    }
+}
+// statistics of an FCG solve; after a CG fallback (cg = 1) the CG launch has already counted the solve, its
+// iterations and its convergence, which are folded in here
+__global__ void k_fcg_stats(DevCtl* ctl, int conv, int iters, double rr, double bb, double thr, double rows, int cg) {
+    ctl->precond_iterations = iters;
+    if (cg) {
+        ctl->iterations += iters;
+        ctl->bb = bb;
+    } else {
+        ctl->converged = conv;
+        ctl->iterations = iters;
+        ctl->rr = rr;
+        ctl->bb = bb;
+        ctl->thr = thr;
+        ctl->active_cells = (long long)rows;
+        ctl->solves += 1;
+        ctl->sum_rows += rows;
+    }
+    ctl->total_iterations += iters;
+    ctl->sum_iter_rows += (double)iters * rows;
+}
+__global__ void k_add_rows(double* __restrict__ x, const float* __restrict__ e, const uint16_t* __restrict__ rowinfo, long long n) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n && (rowinfo[i] & 0x8000u)) x[i] += (double)e[i];
+}
+
+// ---- host helpers -------------------------------------------------------------------------------------------
+inline unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+template <typename T>
+cudaError_t ualloc(UNetState* u, T** p, long long count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), (size_t)count * sizeof(T));
+    if (e == cudaSuccess) u->allocs.push_back(*p);
+    return e;
+}
+
+Level level_of(const efs_ctx* c, int l) {
+    Level L{c->g.D, c->g.H, c->g.W, 0};
+    for (int k = 0; k < l; k++) L = Level{(L.D + 1) / 2, (L.H + 1) / 2, (L.W + 1) / 2, 0};
+    L.V = (long long)L.D * L.H * L.W;
+    return L;
+}
+
+Off6 offsets(const efs_ctx* c) {
+    const long long W = c->g.W, WH = (long long)c->g.W * c->g.H;
+    return Off6{{-1, 1, -W, W, c->dim == 3 ? -WH : 0, c->dim == 3 ? WH : 0}};
+}
+
+cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
+                 const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st) {
+    const Level& L = u->L[level];
+    tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err};
+    const unsigned grid = (unsigned)((L.V + 127) / 128);
+    (void)layer;
+    if (cout == 16) tc::k_conv3_tc<16><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    else if (cout == 32) tc::k_conv3_tc<32><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    else tc::k_conv3_tc<64><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t wgrad(UNetState* u, const bf16* in, const bf16* g, int cin, int cout, int level, float* dw, int sm_count,
+                  cudaStream_t st) {
+    const Level& L = u->L[level];
+    const int mt = (27 * cin + 127) / 128;
+    const long long want = std::max(1LL, (long long)(4 * sm_count + mt - 1) / mt);
+    const long long splits = std::min(want, (L.V + 15) / 16);
+    long long per = (L.V + splits - 1) / splits;
+    per = (per + 15) / 16 * 16;
+    const unsigned ny = (unsigned)((L.V + per - 1) / per);
+    tc::WgradArgs a{in, g, dw, L.D, L.H, L.W, cin, (int)per, u->err};
+    const dim3 grid((unsigned)mt, ny);
+    if (cout == 16) tc::k_wgrad3_tc<16><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    else if (cout == 32) tc::k_wgrad3_tc<32><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    else tc::k_wgrad3_tc<64><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+    return cudaGetLastError();
+}
+
+#define UCK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return e_; } while (0)
+
+cudaError_t refresh_bf16(UNetState* u, cudaStream_t st) {
+    for (int k = 0; k < kLayers; k++) {
+        const int n = 27 * kSpec[k].cin * kSpec[k].cout;
+        k_w_to_bf16<<<nblk(n), 256, 0, st>>>(u->w32 + u->woff[k], kSpec[k].cin, kSpec[k].cout, u->wf[k], u->wb[k]);
+        UCK(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+// rms scale of x over rows into scal[0..2]
+cudaError_t scale_rows(UNetState* u, const float* x, const uint16_t* rowinfo, long long n, double* scal, cudaStream_t st) {
+    k_sumsq_rows<<<kRedBlocks, 256, 0, st>>>(x, rowinfo, n, u->dpart);
+    UCK(cudaGetLastError());
+    k_finish_scale<<<1, 256, 0, st>>>(u->dpart, kRedBlocks, scal);
+    return cudaGetLastError();
+}
+
+// forward pass on the input field `r` (FP32, reference layout) with matrix rows `rowinfo`; y32 holds the output.
+// train: keep the pre-activations for the backward pass.
+cudaError_t forward(UNetState* u, const float* r, const uint16_t* rowinfo, bool train, cudaStream_t st) {
+    const Level *L = u->L;
+    UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
+    k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0);
+    UCK(cudaGetLastError());
+    const float* B[kLayers];
+    for (int k = 0; k < kLayers; k++) B[k] = u->w32 + u->boff[k];
+    UCK(conv(u, 0, u->x0, u->wf[0], 16, 16, 0, B[0], nullptr, u->e0, nullptr, train ? u->a0 : nullptr, 1, st));
+    k_pool<<<nblk(L[1].V * 2), 256, 0, st>>>(u->e0, L[0], u->p0, L[1], 16);
+    UCK(cudaGetLastError());
+    UCK(conv(u, 1, u->p0, u->wf[1], 16, 32, 1, B[1], nullptr, u->e1, nullptr, train ? u->a1 : nullptr, 1, st));
+    k_pool<<<nblk(L[2].V * 4), 256, 0, st>>>(u->e1, L[1], u->p1, L[2], 32);
+    UCK(cudaGetLastError());
+    UCK(conv(u, 2, u->p1, u->wf[2], 32, 64, 2, B[2], nullptr, u->e2, nullptr, train ? u->a2 : nullptr, 1, st));
+    k_up<<<nblk(L[1].V * 8), 256, 0, st>>>(u->e2, L[2], u->u2, L[1], 64);
+    UCK(cudaGetLastError());
+    UCK(conv(u, 3, u->u2, u->wf[3], 64, 32, 1, B[3], u->e1, u->d1, nullptr, train ? u->a3 : nullptr, 1, st));
+    k_up<<<nblk(L[0].V * 4), 256, 0, st>>>(u->d1, L[1], u->u1, L[0], 32);
+    UCK(cudaGetLastError());
+    UCK(conv(u, 4, u->u1, u->wf[4], 32, 16, 0, B[4], u->e0, u->d0, nullptr, train ? u->a4 : nullptr, 1, st));
+    UCK(conv(u, 5, u->d0, u->wf[5], 16, 16, 0, B[5], nullptr, nullptr, u->y32, nullptr, 0, st));
+    return cudaSuccess;
+}
+
+// The training losses (kind 0: mean squared error against the target field p normalised by its rms over
+// rows; kind 1: energy-norm alignment with the error p for input r, see k_energy_grad) and the gradients of
+// every parameter, accumulated into u->grad.  Requires a forward(train = true) on input r just before.
+cudaError_t backward(UNetState* u, const float* r, const float* p, const uint16_t* rowinfo, int kind, Off6 off,
+                     int sm_count, cudaStream_t st) {
+    const Level* L = u->L;
+    float* G = u->grad;
+    const unsigned nb = nblk(L[0].V);
+    if (kind == 0) {
+        UCK(scale_rows(u, p, rowinfo, L[0].V, u->dscal + 3, st));
+        k_loss<<<nb, 256, 0, st>>>(u->y32, p, rowinfo, u->dscal + 3, L[0].V, u->g5, u->dpart);
+        UCK(cudaGetLastError());
+        k_sum_partials<<<1, 256, 0, st>>>(u->dpart, (int)nb, u->dscal + 3, u->dloss);
+        UCK(cudaGetLastError());
+    } else {
+        k_unpack<<<nb, 256, 0, st>>>(u->y32, rowinfo, L[0].V, u->tz);
+        UCK(cudaGetLastError());
+        k_fcg_matvec<<<nb, 256, 0, st>>>(u->tz, rowinfo, L[0].V, off, u->tq);
+        UCK(cudaGetLastError());
+        k_dots3<<<kRedBlocks, 256, 0, st>>>(u->tz, r, u->tz, u->tq, p, r, L[0].V, u->dpart);
+        UCK(cudaGetLastError());
+        k_dots3_finish<<<1, 256, 0, st>>>(u->dpart, kRedBlocks, u->dscal + 8);
+        UCK(cudaGetLastError());
+        k_energy_grad<<<nb, 256, 0, st>>>(r, u->tq, rowinfo, u->dscal + 8, L[0].V, u->g5);
+        UCK(cudaGetLastError());
+        k_energy_loss<<<1, 1, 0, st>>>(u->dscal + 8, u->dloss);
+        UCK(cudaGetLastError());
+    }
+    auto bgrad = [&](const bf16* g, long long V, int C, int layer) {
+        k_bias_grad<<<256, 256, 0, st>>>(g, V, C, G + u->boff[layer]);
+        return cudaGetLastError();
+    };
+    // layer 5
+    UCK(wgrad(u, u->d0, u->g5, 16, 16, 0, G + u->woff[5], sm_count, st));
+    UCK(bgrad(u->g5, L[0].V, 16, 5));
+    UCK(conv(u, 5, u->g5, u->wb[5], 16, 16, 0, nullptr, nullptr, u->gd0, nullptr, nullptr, 0, st));
+    // layer 4: d0 = relu(a4) + e0
+    k_relu_bwd<<<nblk(L[0].V * 2), 256, 0, st>>>(u->gd0, u->a4, L[0].V * 2, u->ga4);
+    UCK(cudaGetLastError());
+    UCK(wgrad(u, u->u1, u->ga4, 32, 16, 0, G + u->woff[4], sm_count, st));
+    UCK(bgrad(u->ga4, L[0].V, 16, 4));
+    UCK(conv(u, 4, u->ga4, u->wb[4], 16, 32, 0, nullptr, nullptr, u->gu1, nullptr, nullptr, 0, st));
+    k_up_bwd<<<nblk(L[1].V * 4), 256, 0, st>>>(u->gu1, L[0], u->gd1, L[1], 32);
+    UCK(cudaGetLastError());
+    // layer 3: d1 = relu(a3) + e1
+    k_relu_bwd<<<nblk(L[1].V * 4), 256, 0, st>>>(u->gd1, u->a3, L[1].V * 4, u->ga3);
+    UCK(cudaGetLastError());
+    UCK(wgrad(u, u->u2, u->ga3, 64, 32, 1, G + u->woff[3], sm_count, st));
+    UCK(bgrad(u->ga3, L[1].V, 32, 3));
+    UCK(conv(u, 3, u->ga3, u->wb[3], 32, 64, 1, nullptr, nullptr, u->gu2, nullptr, nullptr, 0, st));
+    k_up_bwd<<<nblk(L[2].V * 8), 256, 0, st>>>(u->gu2, L[1], u->ge2, L[2], 64);
+    UCK(cudaGetLastError());
+    // layer 2
+    k_relu_bwd<<<nblk(L[2].V * 8), 256, 0, st>>>(u->ge2, u->a2, L[2].V * 8, u->ga2);
+    UCK(cudaGetLastError());
+    UCK(wgrad(u, u->p1, u->ga2, 32, 64, 2, G + u->woff[2], sm_count, st));
+    UCK(bgrad(u->ga2, L[2].V, 64, 2));
+    UCK(conv(u, 2, u->ga2, u->wb[2], 64, 32, 2, nullptr, nullptr, u->gp1, nullptr, nullptr, 0, st));
+    k_pool_bwd<<<nblk(L[1].V * 4), 256, 0, st>>>(u->gp1, L[2], u->ge1, L[1], 32, u->gd1);
+    UCK(cudaGetLastError());
+    // layer 1
+    k_relu_bwd<<<nblk(L[1].V * 4), 256, 0, st>>>(u->ge1, u->a1, L[1].V * 4, u->ga1);
+    UCK(cudaGetLastError());
+    UCK(wgrad(u, u->p0, u->ga1, 16, 32, 1, G + u->woff[1], sm_count, st));
+    UCK(bgrad(u->ga1, L[1].V, 32, 1));
+    UCK(conv(u, 1, u->ga1, u->wb[1], 32, 16, 1, nullptr, nullptr, u->gp0, nullptr, nullptr, 0, st));
+    k_pool_bwd<<<nblk(L[0].V * 2), 256, 0, st>>>(u->gp0, L[1], u->ge0, L[0], 16, u->gd0);
+    UCK(cudaGetLastError());
+    // layer 0
+    k_relu_bwd<<<nblk(L[0].V * 2), 256, 0, st>>>(u->ge0, u->a0, L[0].V * 2, u->ga0);
+    UCK(cudaGetLastError());
+    UCK(wgrad(u, u->x0, u->ga0, 16, 16, 0, G + u->woff[0], sm_count, st));
+    UCK(bgrad(u->ga0, L[0].V, 16, 0));
+    return cudaSuccess;
+}
+
+cudaError_t alloc_train(UNetState* u) {
+    if (u->train_ready) return cudaSuccess;
+    const Level* L = u->L;
+    UCK(ualloc(u, &u->a0, L[0].V * 16));
+    UCK(ualloc(u, &u->a1, L[1].V * 32));
+    UCK(ualloc(u, &u->a2, L[2].V * 64));
+    UCK(ualloc(u, &u->a3, L[1].V * 32));
+    UCK(ualloc(u, &u->a4, L[0].V * 16));
+    UCK(ualloc(u, &u->g5, L[0].V * 16));
+    UCK(ualloc(u, &u->gd0, L[0].V * 16));
+    UCK(ualloc(u, &u->ga4, L[0].V * 16));
+    UCK(ualloc(u, &u->gu1, L[0].V * 32));
+    UCK(ualloc(u, &u->gd1, L[1].V * 32));
+    UCK(ualloc(u, &u->ga3, L[1].V * 32));
+    UCK(ualloc(u, &u->gu2, L[1].V * 64));
+    UCK(ualloc(u, &u->ge2, L[2].V * 64));
+    UCK(ualloc(u, &u->ga2, L[2].V * 64));
+    UCK(ualloc(u, &u->gp1, L[2].V * 32));
+    UCK(ualloc(u, &u->ge1, L[1].V * 32));
+    UCK(ualloc(u, &u->ga1, L[1].V * 32));
+    UCK(ualloc(u, &u->gp0, L[1].V * 16));
+    UCK(ualloc(u, &u->ge0, L[0].V * 16));
+    UCK(ualloc(u, &u->ga0, L[0].V * 16));
+    UCK(ualloc(u, &u->tz, L[0].V));
+    UCK(ualloc(u, &u->tq, L[0].V));
+    UCK(ualloc(u, &u->grad, u->nparam));
+    UCK(ualloc(u, &u->am, u->nparam));
+    UCK(ualloc(u, &u->av, u->nparam));
+    UCK(cudaMemset(u->am, 0, u->nparam * sizeof(float)));
+    UCK(cudaMemset(u->av, 0, u->nparam * sizeof(float)));
+    u->adam_t = 0;
+    u->train_ready = true;
+    return cudaSuccess;
+}
+
+cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
+    UNetState* u = new UNetState();
+    *out = u;
+    for (int l = 0; l < 3; l++) u->L[l] = level_of(c, l);
+    long long off = 0;
+    for (int k = 0; k < kLayers; k++) {
+        u->woff[k] = off;
+        off += 27LL * kSpec[k].cin * kSpec[k].cout;
+        u->boff[k] = off;
+        off += kSpec[k].cout;
+    }
+    u->nparam = off;
+    const Level* L = u->L;
+    UCK(ualloc(u, &u->w32, u->nparam));
+    for (int k = 0; k < kLayers; k++) {
+        UCK(ualloc(u, &u->wf[k], 27LL * kSpec[k].cin * kSpec[k].cout));
+        UCK(ualloc(u, &u->wb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
+    }
+    UCK(ualloc(u, &u->x0, L[0].V * 16));
+    UCK(ualloc(u, &u->e0, L[0].V * 16));
+    UCK(ualloc(u, &u->p0, L[1].V * 16));
+    UCK(ualloc(u, &u->e1, L[1].V * 32));
+    UCK(ualloc(u, &u->p1, L[2].V * 32));
+    UCK(ualloc(u, &u->e2, L[2].V * 64));
+    UCK(ualloc(u, &u->u2, L[1].V * 64));
+    UCK(ualloc(u, &u->d1, L[1].V * 32));
+    UCK(ualloc(u, &u->u1, L[0].V * 32));
+    UCK(ualloc(u, &u->d0, L[0].V * 16));
+    UCK(ualloc(u, &u->y32, L[0].V * 16));
+    UCK(ualloc(u, &u->dscal, 12));
+    UCK(ualloc(u, &u->dpart, 3LL * std::max<long long>(kRedBlocks, nblk(L[0].V))));
+    UCK(ualloc(u, &u->dloss, 1));
+    UCK(ualloc(u, &u->err, 1));
+    UCK(ualloc(u, &u->tmp_in, L[0].V));
+    UCK(ualloc(u, &u->tmp_t, L[0].V));
+    UCK(cudaMemset(u->err, 0, sizeof(int)));
+    return cudaSuccess;
+}
+
+int check_err(efs_ctx* c, UNetState* u) {
+    int e = 0;
+    if (cudaMemcpy(&e, u->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return EFS_ERR_CUDA;
+    if (e) {
+        c->err = "tensor-core kernel: an mbarrier wait timed out";
+        return EFS_ERR_DEVICE_FAULT;
+    }
+    return EFS_OK;
+}
+
+int ufail(efs_ctx* c, int status, const std::string& msg) {
+    if (c) c->err = msg;
+    return status;
+}
+int ucuda(efs_ctx* c, cudaError_t e, const char* what) {
+    return ufail(c, EFS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define ACK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return efs::ucuda(c, e_, what); } while (0)
+
+// One dot-product round: up to three pairs, result in u->hdots[0..2] (host, after a synchronisation).
+cudaError_t dots3(efs_ctx* c, UNetState* u, const float* a0, const float* b0, const float* a1, const float* b1,
+                  const float* a2, const float* b2) {
+    const long long n = c->g.N;
+    k_dots3<<<kRedBlocks, 256, 0, c->stream>>>(a0, b0, a1, b1, a2, b2, n, u->dpart);
+    UCK(cudaGetLastError());
+    k_dots3_finish<<<1, 256, 0, c->stream>>>(u->dpart, kRedBlocks, u->dscal + 8);
+    UCK(cudaGetLastError());
+    UCK(cudaMemcpyAsync(u->hdots, u->dscal + 8, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return cudaStreamSynchronize(c->stream);
+}
+
+}  // namespace
+
+void unet_free(efs_ctx* c) {
+    if (!c || !c->unet) return;
+    for (void* p : c->unet->allocs) cudaFree(p);
+    if (c->unet->hdots) cudaFreeHost(c->unet->hdots);
+    delete c->unet;
+    c->unet = nullptr;
+}
+
+// Flexible preconditioned CG (Notay's FCG with truncation 1: beta = -(z'.q) / (d.q)) on the matrix of the
+// current rowinfo, from p0 = 0 (the CG solvers start from b), to the stop rule of the CG solvers
+// (r.r < tol_rel^2 b.b, or the absolute threshold), with x in FP64 and the true residual recomputed in FP64
+// every 32 iterations and before stopping.  Plain CG is the fallback: when the residual norm has not halved
+// over 10 iterations, or d.Ld is not negative (L is negative definite on the rows), the rest of the solve is
+// handed to the
+// persistent CG kernel (EFS_CG_MIXED_RECURRENCE) on the residual system L e = r with the same absolute
+// threshold, and x += e.
+cudaError_t fcg_solve(efs_ctx* c) {
+    UNetState* u = c->unet;
+    if (!u) return cudaErrorInvalidValue;
+    const long long n = c->g.N;
+    if (!u->x64) {
+        UCK(ualloc(u, &u->x64, n));
+        UCK(ualloc(u, &u->fr, n));
+        UCK(ualloc(u, &u->fz, n));
+        UCK(ualloc(u, &u->fd, n));
+        UCK(ualloc(u, &u->fq, n));
+        UCK(cudaMallocHost(reinterpret_cast<void**>(&u->hdots), 4 * sizeof(double)));
+    }
+    cudaStream_t st = c->stream;
+    const Off6 off = offsets(c);
+    const unsigned nb = nblk(n);
+    const uint16_t* R = c->rowinfo;
+    k_fcg_init<<<nb, 256, 0, st>>>(c->div, R, n, u->x64);
+    UCK(cudaGetLastError());
+    k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
+    UCK(cudaGetLastError());
+    UCK(dots3(c, u, u->fr, u->fr, c->div, c->div, nullptr, nullptr));
+    double rr = u->hdots[0];
+    const double bb = u->hdots[1];
+    UCK(scale_rows(u, c->div, R, n, u->dscal, st));
+    double hs[2];
+    UCK(cudaMemcpyAsync(hs, u->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    UCK(cudaStreamSynchronize(st));
+    const double rows = hs[1];
+    double thr = c->prm.tol_rel > 0 ? (double)(float)((double)c->prm.tol_rel * c->prm.tol_rel * bb)
+                                    : (double)c->prm.solver_threshold;
+    int conv = rr < thr, it = 0;
+    bool fallback = false;
+    if (!conv) {
+        UCK(forward(u, u->fr, R, false, st));
+        k_unpack<<<nb, 256, 0, st>>>(u->y32, R, n, u->fz);
+        UCK(cudaGetLastError());
+        UCK(cudaMemcpyAsync(u->fd, u->fz, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        UCK(dots3(c, u, u->fr, u->fz, nullptr, nullptr, nullptr, nullptr));
+        double rz = u->hdots[0];
+        double rr_window = rr;
+        for (it = 0; it < c->prm.max_steps; it++) {
+            k_fcg_matvec<<<nb, 256, 0, st>>>(u->fd, R, n, off, u->fq);
+            UCK(cudaGetLastError());
+            UCK(dots3(c, u, u->fd, u->fq, nullptr, nullptr, nullptr, nullptr));
+            const double dq = u->hdots[0];
+            // d.Ld < 0 for any direction on the rows; the sign of r.z does not matter (alpha follows it)
+            if (!(dq < 0.0) || !std::isfinite(rz / dq)) { fallback = true; break; }
+            const double alpha = rz / dq;
+            k_fcg_xr<<<nb, 256, 0, st>>>(u->x64, u->fr, u->fd, u->fq, n, alpha);
+            UCK(cudaGetLastError());
+            if (((it + 1) & 31) == 0) {
+                k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
+                UCK(cudaGetLastError());
+            }
+            UCK(dots3(c, u, u->fr, u->fr, nullptr, nullptr, nullptr, nullptr));
+            rr = u->hdots[0];
+            if (rr < thr) {
+                k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
+                UCK(cudaGetLastError());
+                UCK(dots3(c, u, u->fr, u->fr, nullptr, nullptr, nullptr, nullptr));
+                rr = u->hdots[0];
+                if (rr < thr) { conv = 1; it++; break; }
+            }
+            if (((it + 1) % 10) == 0) {
+                if (rr > 0.5 * rr_window) { fallback = true; it++; break; }
+                rr_window = rr;
+            }
+            UCK(forward(u, u->fr, R, false, st));
+            k_unpack<<<nb, 256, 0, st>>>(u->y32, R, n, u->fz);
+            UCK(cudaGetLastError());
+            UCK(dots3(c, u, u->fz, u->fq, u->fr, u->fz, nullptr, nullptr));
+            const double beta = -u->hdots[0] / dq;
+            rz = u->hdots[1];
+            k_fcg_dir<<<nb, 256, 0, st>>>(u->fd, u->fz, n, beta);
+            UCK(cudaGetLastError());
+        }
+    }
+    if (fallback) {
+        // plain CG on L e = r (true residual of x), absolute threshold thr; then x += e
+        k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
+        UCK(cudaGetLastError());
+        UCK(cudaMemcpyAsync(u->tmp_t, c->div, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        UCK(cudaMemcpyAsync(c->div, u->fr, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        const efs_params saved = c->prm;
+        c->prm.solver = EFS_SOLVER_CG;
+        c->prm.cg_variant = EFS_CG_MIXED_RECURRENCE;
+        c->prm.tol_rel = 0.f;
+        c->prm.solver_threshold = (float)thr;
+        c->prm.max_steps = std::max(0, saved.max_steps - it);
+        cudaError_t e = launch_solver(c);
+        c->prm = saved;
+        UCK(e);
+        k_add_rows<<<nb, 256, 0, st>>>(u->x64, c->p, R, n);
+        UCK(cudaGetLastError());
+        UCK(cudaMemcpyAsync(c->div, u->tmp_t, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    }
+    k_fcg_out<<<nb, 256, 0, st>>>(u->x64, R, n, c->p, c->p64);
+    UCK(cudaGetLastError());
+    k_fcg_stats<<<1, 1, 0, st>>>(c->ctl, conv, it, rr, bb, thr, rows, fallback ? 1 : 0);
+    UCK(cudaGetLastError());
+    return cudaSuccess;
+}
+
+}  // namespace efs
+
+using efs::UNetState;
+
+extern "C" {
+
+int efs_unet_param_count(int64_t* n) {
+    if (!n) return EFS_ERR_ARG;
+    *n = efs::param_count_host();
+    return EFS_OK;
+}
+
+int efs_unet_init(efs_ctx* c, uint64_t seed, int sample_capacity) {
+    if (!c) return EFS_ERR_ARG;
+    if (c->dim != 3) return efs::ufail(c, EFS_ERR_ARG, "the U-Net preconditioner is 3D only");
+    if (sample_capacity < 0) return efs::ufail(c, EFS_ERR_ARG, "sample_capacity < 0");
+    ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    efs::unet_free(c);
+    UNetState* u = nullptr;
+    cudaError_t e = efs::alloc_net(c, &u);
+    c->unet = u;
+    if (e != cudaSuccess) { efs::unet_free(c); return efs::ucuda(c, e, "U-Net allocation"); }
+    for (int k = 0; k < efs::kLayers; k++) {
+        const long long nw = 27LL * efs::kSpec[k].cin * efs::kSpec[k].cout;
+        const long long nk = nw + efs::kSpec[k].cout;
+        const float stdv = (float)std::sqrt(2.0 / (27.0 * efs::kSpec[k].cin));
+        efs::k_init<<<efs::nblk(nk), 256, 0, c->stream>>>(u->w32 + u->woff[k], nk, nw, stdv, seed, (unsigned long long)k);
+        ACK(cudaGetLastError(), "U-Net init");
+    }
+    ACK(efs::refresh_bf16(u, c->stream), "U-Net weights");
+    if (sample_capacity > 0) {
+        const long long N = c->g.N;
+        ACK(efs::ualloc(u, &u->sb, N * sample_capacity), "sample buffer");
+        ACK(efs::ualloc(u, &u->sp, N * sample_capacity), "sample buffer");
+        ACK(efs::ualloc(u, &u->srow, N * sample_capacity), "sample buffer");
+        u->cap = sample_capacity;
+    }
+    ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_unet_get_weights(efs_ctx* c, float* host, int64_t n) {
+    if (!c) return EFS_ERR_ARG;
+    if (!c->unet) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (!host || n != c->unet->nparam) return efs::ufail(c, EFS_ERR_ARG, "host buffer must hold efs_unet_param_count floats");
+    ACK(cudaMemcpyAsync(host, c->unet->w32, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "download weights");
+    ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_unet_set_weights(efs_ctx* c, const float* host, int64_t n) {
+    if (!c) return EFS_ERR_ARG;
+    if (!c->unet) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (!host || n != c->unet->nparam) return efs::ufail(c, EFS_ERR_ARG, "host buffer must hold efs_unet_param_count floats");
+    for (int64_t i = 0; i < n; i++)
+        if (!std::isfinite(host[i])) return efs::ufail(c, EFS_ERR_ARG, "weights must be finite");
+    ACK(cudaMemcpyAsync(c->unet->w32, host, n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload weights");
+    ACK(efs::refresh_bf16(c->unet, c->stream), "U-Net weights");
+    if (c->unet->train_ready) {   // new weights: fresh optimiser state
+        ACK(cudaMemsetAsync(c->unet->am, 0, n * sizeof(float), c->stream), "memset");
+        ACK(cudaMemsetAsync(c->unet->av, 0, n * sizeof(float), c->stream), "memset");
+        c->unet->adam_t = 0;
+    }
+    ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_unet_apply(efs_ctx* c, const float* r_host, float* z_host) {
+    if (!c) return EFS_ERR_ARG;
+    UNetState* u = c->unet;
+    if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (!r_host || !z_host) return efs::ufail(c, EFS_ERR_ARG, "NULL field");
+    const long long N = c->g.N;
+    ACK(efs::launch_solver_prep(c), "solver prep");
+    ACK(cudaMemcpyAsync(u->tmp_in, r_host, N * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload");
+    ACK(efs::forward(u, u->tmp_in, c->rowinfo, false, c->stream), "U-Net forward");
+    efs::k_unpack<<<efs::nblk(N), 256, 0, c->stream>>>(u->y32, c->rowinfo, N, u->tmp_t);
+    ACK(cudaGetLastError(), "unpack");
+    ACK(cudaMemcpyAsync(z_host, u->tmp_t, N * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "download");
+    ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return efs::check_err(c, u);
+}
+
+int efs_unet_loss_grad(efs_ctx* c, int loss_kind, const float* b_host, const float* p_host, float* loss, float* grads_host) {
+    if (!c) return EFS_ERR_ARG;
+    UNetState* u = c->unet;
+    if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (!b_host || !p_host) return efs::ufail(c, EFS_ERR_ARG, "NULL field");
+    if (loss_kind != 0 && loss_kind != 1) return efs::ufail(c, EFS_ERR_ARG, "loss_kind: 0 (pressure MSE) or 1 (energy)");
+    const long long N = c->g.N;
+    cudaStream_t st = c->stream;
+    ACK(efs::alloc_train(u), "U-Net training buffers");
+    ACK(efs::launch_solver_prep(c), "solver prep");
+    ACK(cudaMemcpyAsync(u->tmp_in, b_host, N * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
+    ACK(cudaMemcpyAsync(u->tmp_t, p_host, N * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
+    ACK(cudaMemsetAsync(u->grad, 0, u->nparam * sizeof(float), st), "memset");
+    ACK(cudaMemsetAsync(u->dloss, 0, sizeof(double), st), "memset");
+    ACK(efs::forward(u, u->tmp_in, c->rowinfo, true, st), "U-Net forward");
+    ACK(efs::backward(u, u->tmp_in, u->tmp_t, c->rowinfo, loss_kind, efs::offsets(c), c->sm_count, st), "U-Net backward");
+    double l = 0;
+    ACK(cudaMemcpyAsync(&l, u->dloss, sizeof(double), cudaMemcpyDeviceToHost, st), "download");
+    if (grads_host) ACK(cudaMemcpyAsync(grads_host, u->grad, u->nparam * sizeof(float), cudaMemcpyDeviceToHost, st), "download");
+    ACK(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (loss) *loss = (float)l;
+    return efs::check_err(c, u);
+}
+
+int efs_unet_add_sample(efs_ctx* c) {
+    if (!c) return EFS_ERR_ARG;
+    UNetState* u = c->unet;
+    if (!u || u->cap == 0) return efs::ufail(c, EFS_ERR_STATE, "no sample buffer: efs_unet_init with sample_capacity > 0");
+    const long long N = c->g.N;
+    const int slot = u->next;
+    ACK(cudaMemcpyAsync(u->sb + (size_t)slot * N, c->div, N * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "sample");
+    ACK(cudaMemcpyAsync(u->sp + (size_t)slot * N, c->p, N * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "sample");
+    ACK(cudaMemcpyAsync(u->srow + (size_t)slot * N, c->rowinfo, N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, c->stream),
+        "sample");
+    u->next = (u->next + 1) % u->cap;
+    u->count = std::min(u->count + 1, u->cap);
+    return EFS_OK;
+}
+
+int efs_unet_sample_count(efs_ctx* c, int* count) {
+    if (!c || !count) return EFS_ERR_ARG;
+    *count = c->unet ? c->unet->count : 0;
+    return EFS_OK;
+}
+
+int efs_unet_train(efs_ctx* c, int loss_kind, int iterations, int batch, float lr, float synthetic, uint64_t seed,
+                   float* last_loss) {
+    if (!c) return EFS_ERR_ARG;
+    UNetState* u = c->unet;
+    if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (u->count == 0) return efs::ufail(c, EFS_ERR_STATE, "no training samples: efs_unet_add_sample after a projection");
+    if (iterations < 0 || batch < 1 || !(lr > 0) || !(synthetic >= 0.f && synthetic <= 1.f) ||
+        (loss_kind != 0 && loss_kind != 1))
+        return efs::ufail(c, EFS_ERR_ARG, "loss_kind 0/1, iterations >= 0, batch >= 1, lr > 0, 0 <= synthetic <= 1");
+    cudaStream_t st = c->stream;
+    const long long N = c->g.N;
+    ACK(efs::alloc_train(u), "U-Net training buffers");
+    unsigned long long rng = seed * 6364136223846793005ull + 1442695040888963407ull;
+    double l = 0;
+    for (int it = 0; it < iterations; it++) {
+        ACK(cudaMemsetAsync(u->grad, 0, u->nparam * sizeof(float), st), "memset");
+        ACK(cudaMemsetAsync(u->dloss, 0, sizeof(double), st), "memset");
+        for (int b = 0; b < batch; b++) {
+            rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+            const int s = (int)((rng >> 33) % (unsigned long long)u->count);
+            const float* sb = u->sb + (size_t)s * N;
+            const float* sp = u->sp + (size_t)s * N;
+            const uint16_t* sr = u->srow + (size_t)s * N;
+            rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+            if ((float)((rng >> 40) * (1.0 / 16777216.0)) < synthetic) {
+                // synthetic pair on this sample's geometry: e random and multi-scale, input L e, target e
+                efs::SynthAmp amp;
+                rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+                const float gam = (float)((rng >> 40) * (2.0 / 16777216.0));
+                for (int k = 0; k < 5; k++) {
+                    rng = rng * 6364136223846793005ull + 1442695040888963407ull;
+                    amp.a[k] = std::pow((float)(1 << k), gam) * (0.25f + 0.75f * (float)((rng >> 40) * (1.0 / 16777216.0)));
+                }
+                efs::k_synth_error<<<efs::nblk(N), 256, 0, st>>>(u->L[0], sr, rng, amp, u->tmp_t);
+                ACK(cudaGetLastError(), "synthetic error");
+                efs::k_fcg_matvec<<<efs::nblk(N), 256, 0, st>>>(u->tmp_t, sr, N, efs::offsets(c), u->tmp_in);
+                ACK(cudaGetLastError(), "synthetic residual");
+                sb = u->tmp_in;
+                sp = u->tmp_t;
+            }
+            ACK(efs::forward(u, sb, sr, true, st), "U-Net forward");
+            ACK(efs::backward(u, sb, sp, sr, loss_kind, efs::offsets(c), c->sm_count, st), "U-Net backward");
+        }
+        u->adam_t += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float bc1 = 1.f - std::pow(b1, (float)u->adam_t), bc2 = 1.f - std::pow(b2, (float)u->adam_t);
+        efs::k_adam<<<efs::nblk(u->nparam), 256, 0, st>>>(u->nparam, u->w32, u->grad, u->am, u->av, lr, b1, b2, 1e-8f, bc1,
+                                                          bc2, 1.f / (float)batch);
+        ACK(cudaGetLastError(), "adam");
+        ACK(efs::refresh_bf16(u, st), "U-Net weights");
+        if (it == iterations - 1) {
+            ACK(cudaMemcpyAsync(&l, u->dloss, sizeof(double), cudaMemcpyDeviceToHost, st), "download");
+        }
+    }
+    ACK(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (last_loss) *last_loss = (float)(l / batch);
+    return efs::check_err(c, u);
+}
+
+}  // extern "C"

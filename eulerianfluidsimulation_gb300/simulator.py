@@ -184,6 +184,47 @@ class _GB300Simulator:
         check(lib().efs_download_pressure_fp64(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), self._h)
         return out
 
+    # ---- learned preconditioner (3D) ----
+    def unet_init(self, seed=0, sample_capacity=0):
+        check(lib().efs_unet_init(self._h, seed, sample_capacity), self._h)
+
+    def unet_weights(self):
+        out = np.empty(unet_param_count(), np.float32)
+        check(lib().efs_unet_get_weights(self._h, fptr(out), out.size), self._h)
+        return out
+
+    def unet_set_weights(self, w):
+        a = np.ascontiguousarray(w, dtype=np.float32)
+        check(lib().efs_unet_set_weights(self._h, fptr(a), a.size), self._h)
+
+    def unet_apply(self, r):
+        a = np.ascontiguousarray(r, dtype=np.float32)
+        z = np.empty_like(a)
+        check(lib().efs_unet_apply(self._h, fptr(a), fptr(z)), self._h)
+        return z
+
+    def unet_loss_grad(self, b, p, grads=True, loss_kind=0):
+        bb = np.ascontiguousarray(b, dtype=np.float32)
+        pp = np.ascontiguousarray(p, dtype=np.float32)
+        loss = ctypes.c_float()
+        g = np.empty(unet_param_count(), np.float32) if grads else None
+        check(lib().efs_unet_loss_grad(self._h, loss_kind, fptr(bb), fptr(pp), ctypes.byref(loss), fptr(g)), self._h)
+        return loss.value, g
+
+    def unet_add_sample(self):
+        check(lib().efs_unet_add_sample(self._h), self._h)
+
+    def unet_sample_count(self):
+        n = ctypes.c_int()
+        check(lib().efs_unet_sample_count(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+    def unet_train(self, iterations, batch=4, lr=1e-3, synthetic=0.5, seed=0, loss_kind=1):
+        loss = ctypes.c_float()
+        check(lib().efs_unet_train(self._h, loss_kind, iterations, batch, lr, synthetic, seed, ctypes.byref(loss)),
+              self._h)
+        return loss.value
+
     # ---- timing of the pressure solve ----
     def solve_timing_arm(self, capacity):
         check(lib().efs_solve_timing_arm(self._h, capacity), self._h)
@@ -209,6 +250,12 @@ class GB300Simulator2D(_GB300Simulator):
 
     def __init__(self, width, height, params=None):
         super().__init__(2, width, height, 1, params)
+
+
+def unet_param_count():
+    n = ctypes.c_int64()
+    check(lib().efs_unet_param_count(ctypes.byref(n)))
+    return n.value
 
 
 def device_count():

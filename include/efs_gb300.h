@@ -60,7 +60,12 @@ enum efs_stage {
 /* ---- pressure solvers (Properties::SolverType, Properties.h:476-482) ---- */
 enum efs_solver {
     EFS_SOLVER_JACOBI = 0,      /* JacobiSolverCPU3D: max_steps/2 sweeps from p = 0                */
-    EFS_SOLVER_CG = 1           /* CGSolverCPU3D: p0 = b, true residual every 64 iterations        */
+    EFS_SOLVER_CG = 1,          /* CGSolverCPU3D: p0 = b, true residual every 64 iterations        */
+    /* No counterpart in the reference: flexible preconditioned CG with the context's learned U-Net
+     * preconditioner (3D; efs_unet_*), same matrix, start p0 = b and stop rule as EFS_SOLVER_CG; when the
+     * residual stalls it hands the remaining residual system to plain CG.  Steps with this solver run as
+     * direct launches (the iteration reads scalars on the host), not as a replayed graph. */
+    EFS_SOLVER_FCG_UNET = 2
 };
 
 /* CG variants.  Both follow CGSolverCPU3D::solve (CGSolver.cpp:416-465): p0 = b, recurrence residual, the
@@ -144,6 +149,8 @@ typedef struct efs_stats {
     int64_t active_cells;     /* last solve: matrix rows (liquid, non-solid cells)        */
     int64_t total_solve_steps;/* sum of solve_steps over all solves since create / reset  */
     int64_t solves;           /* number of solves since create / reset                    */
+    int64_t precond_steps;    /* EFS_SOLVER_FCG_UNET: iterations of the last solve that applied the
+                                 preconditioner (the rest of solve_steps were plain CG); 0 otherwise */
 } efs_stats;
 
 typedef struct efs_ctx efs_ctx;
@@ -231,6 +238,37 @@ int  efs_solve_noalloc(int dim, int width, int height, int depth, const efs_para
                        const float* rho, const float* boundary, const float* divergence, float* pressure,
                        void* stream, efs_stats* stats);
 const char* efs_noalloc_last_error(void);
+
+/* ---- learned preconditioner: 3D U-Net (3 levels, 16/32/64 channels, BF16 weights, FP32 accumulation) ----
+ * No counterpart in the reference.  A context holds at most one network, sized for its grid; the FP32
+ * master parameters are laid out layer by layer as weights [27 taps][cin][cout] then bias [cout] (layers:
+ * 16->16, 16->32, 32->64, 64->32, 32->16, 16->16).  The network maps a residual field r to z on the matrix
+ * rows; FCG (EFS_SOLVER_FCG_UNET) applies it every iteration.  Training runs on the device on samples
+ * (divergence, pressure, matrix rows) the context stored after its own projections.  The matrix rows used
+ * by efs_unet_apply and efs_unet_loss_grad are those of the context's current rho and boundary; both
+ * entry points overwrite the pressure field with the divergence (the solver's start). */
+int  efs_unet_param_count(int64_t* count);
+/* Fresh network with He-normal weights from `seed`; room for `sample_capacity` training samples (0: none). */
+int  efs_unet_init(efs_ctx* ctx, uint64_t seed, int sample_capacity);
+int  efs_unet_get_weights(efs_ctx* ctx, float* host, int64_t count);
+/* Loading weights also resets the optimiser state of efs_unet_train. */
+int  efs_unet_set_weights(efs_ctx* ctx, const float* host, int64_t count);
+/* z = net(r) on host fields (N floats each). */
+int  efs_unet_apply(efs_ctx* ctx, const float* r, float* z);
+/* Training losses, for input b and target p (p solves L p = b; host fields):
+ *   loss_kind 0: sum over rows of (net(b)_v - p_v / rms(p))^2 / rows (the pressure, normalised);
+ *   loss_kind 1: 1 - (z.b)^2 / ((z.Lz)(p.b)) with z = net(b): the share of p's energy norm (-L) that a line
+ *                search along z leaves, i.e. how far z is from a perfect preconditioned direction.
+ * efs_unet_loss_grad gives the loss and the gradient of every parameter for one sample (grads may be NULL). */
+int  efs_unet_loss_grad(efs_ctx* ctx, int loss_kind, const float* b, const float* p, float* loss, float* grads);
+/* Stores the current (divergence, pressure, matrix rows) as a training sample (ring buffer). */
+int  efs_unet_add_sample(efs_ctx* ctx);
+int  efs_unet_sample_count(efs_ctx* ctx, int* count);
+/* `iterations` Adam steps (beta 0.9/0.999) of `batch` samples drawn with `seed`; mean loss of the last batch.
+ * A fraction `synthetic` of the batch are synthetic pairs on a stored sample's matrix rows: a random
+ * multi-scale error field e (hash-valued lattices of spacing 1..16, random spectral slope) and input L e. */
+int  efs_unet_train(efs_ctx* ctx, int loss_kind, int iterations, int batch, float lr, float synthetic, uint64_t seed,
+                    float* last_loss);
 
 /* ---- host-only helpers (no device needed) ---- */
 /* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */

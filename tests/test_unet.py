@@ -1,0 +1,118 @@
+"""The learned preconditioner on the GPU (through the C ABI), against the CPU oracle of the network.
+
+- forward pass: the GPU output against the oracle with BF16 rounding at the same points, relative L2 1e-2
+  on the matrix rows (what remains is the FP32 order of tensor-core sums, which can flip a BF16 rounding);
+- gradients: the loss within 1e-3 relative and every layer's weight and bias gradient within 3e-2
+  relative L2 of the oracle's;
+- training on the device lowers the loss on the samples it was given;
+- FCG with the trained network reaches the same stop rule as CG, its pressure within 1e-5 of CG's, in
+  fewer iterations than plain CG (the gain of the network over the method without it).
+"""
+import numpy as np
+import pytest
+
+from eulerianfluidsimulation_gb300 import abi
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+gb = pytest.importorskip("eulerianfluidsimulation_gb300")
+from oracle import oracle, unet_oracle as U  # noqa: E402
+
+
+def _scene(n, seed=3):
+    b, r = oracle.scene_dam3d(n, n, n, 4, 4, seed)
+    rows = (r > 0.5) & (b == 0.0)
+    return b, r, rows
+
+
+def _ctx(n, seed=11, cap=0, solver=abi.SOLVER_CG):
+    prm = abi.params_dam(1.0 / n, 0.004, solver, 1e-6)
+    prm.max_steps = 20000
+    s = gb.GB300Simulator3D(n, n, n, prm)
+    s.unet_init(seed, cap)
+    return s
+
+
+def test_unet_forward_matches_oracle():
+    n = 12
+    bnd, rho, rows = _scene(n)
+    rng = np.random.default_rng(1)
+    r = rng.normal(size=(n, n, n)).astype(np.float32)
+    with _ctx(n) as s:
+        s.set_field(abi.FIELD_BOUNDARY, bnd)
+        s.set_field(abi.FIELD_RHO, rho)
+        z = s.unet_apply(r)
+        w = s.unet_weights()
+    y, _ = U.forward(w, r, rows, bf16=True)
+    assert np.all(z[~rows] == 0)
+    assert rel_l2(z[rows], y[rows]) < 1e-2, rel_l2(z[rows], y[rows])
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_unet_gradients_match_oracle(kind):
+    n = 12
+    bnd, rho, rows = _scene(n)
+    apply_L, rows_l = U.matrix(rho, bnd)
+    assert np.array_equal(rows, rows_l)
+    rng = np.random.default_rng(2)
+    p = np.where(rows, rng.normal(size=(n, n, n)), 0.0).astype(np.float32)
+    b = apply_L(p).astype(np.float32) if kind == 1 else rng.normal(size=(n, n, n)).astype(np.float32)
+    with _ctx(n, seed=5) as s:
+        s.set_field(abi.FIELD_BOUNDARY, bnd)
+        s.set_field(abi.FIELD_RHO, rho)
+        loss, g = s.unet_loss_grad(b, p, loss_kind=kind)
+        w = s.unet_weights()
+    lo, go = U.loss_grad(w, b, p, rows, bf16=True, kind=kind, apply_L=apply_L)
+    assert abs(loss - lo) <= 1e-3 * lo, (loss, lo)
+    for name, sl in U.layer_slices():
+        assert rel_l2(g[sl], go[sl]) < 3e-2, (name, rel_l2(g[sl], go[sl]))
+
+
+def _collect(s, steps):
+    for _ in range(steps):
+        s.update(1)
+        s.unet_add_sample()
+    s.synchronize()
+
+
+def test_training_lowers_the_loss():
+    n = 32
+    bnd, rho, _ = _scene(n, seed=4)
+    with _ctx(n, seed=9, cap=16) as s:
+        s.set_field(abi.FIELD_BOUNDARY, bnd)
+        s.set_field(abi.FIELD_RHO, rho)
+        _collect(s, 16)
+        assert s.unet_sample_count() == 16
+        first = s.unet_train(1, batch=8, lr=1e-3, synthetic=0.0, seed=1, loss_kind=0)
+        last = s.unet_train(150, batch=4, lr=1e-3, synthetic=0.0, seed=2, loss_kind=0)
+    assert np.isfinite(last) and last < 0.7 * first, (first, last)
+
+
+def test_fcg_converges_and_the_trained_network_saves_iterations():
+    n = 32
+    bnd, rho, rows0 = _scene(n, seed=4)
+    with _ctx(n, seed=9, cap=24) as s:
+        s.set_field(abi.FIELD_BOUNDARY, bnd)
+        s.set_field(abi.FIELD_RHO, rho)
+        _collect(s, 24)
+        s.unet_train(400, batch=4, lr=1e-3, synthetic=0.5, seed=3)
+        s.update(2)                                  # a state the network was not trained on
+        state = s.fields()
+        cg = s.params
+        s.project()
+        st_cg = s.stats()
+        p_cg = s.pressure()
+        fcg = cg.copy()
+        fcg.solver = abi.SOLVER_FCG_UNET
+        s.set_params(fcg)
+        s.set_fields(state)
+        s.project()
+        st_fcg = s.stats()
+        p_fcg = s.pressure()
+    rows = (state[abi.FIELD_RHO] > 0.5) & (state[abi.FIELD_BOUNDARY] == 0.0)
+    assert st_cg.converged and st_fcg.converged
+    assert st_fcg.rr < st_fcg.threshold
+    assert rel_l2(p_fcg[rows], p_cg[rows]) < 1e-5
+    print(f"\nFCG {st_fcg.solve_steps} iterations ({st_fcg.precond_steps} preconditioned), CG {st_cg.solve_steps}")
+    assert st_fcg.solve_steps < st_cg.solve_steps, (st_fcg.solve_steps, st_fcg.precond_steps, st_cg.solve_steps)
