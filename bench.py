@@ -29,7 +29,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "steps/s at 256^3 to rel-res 1e-6 (plain CG)"
+METRIC = "steps/s at 256\u00b3 to rel-res 1e-6: learned-PCG vs plain CG/Jacobi, HBM GB/s"
 # Bytes the pressure solve must move, per matrix row (CG in its recurrence form, the default variant): per
 # iteration read d, rowinfo and write t = L d (10 B), then read d, t, e, r, rowinfo and write e, r, d (30 B);
 # per solve set-up read b, rowinfo and write p64, e, r, d and finally p (30 B).  Neighbour reads of the stencil
@@ -52,7 +52,10 @@ def parse():
     ap.add_argument("--spheres", type=int, default=16)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--dt", type=float, default=0.004)
-    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi"])
+    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi", "fcg"],
+                    help="fcg: learned U-Net preconditioner (trained first at --fcg-train-size, outside the timed region)")
+    ap.add_argument("--fcg-train-size", type=int, default=64)
+    ap.add_argument("--fcg-train-iters", type=int, default=2000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--study", default=None, choices=["precision"],
@@ -71,7 +74,7 @@ def dist_env():
 
 def workload(a):
     from eulerianfluidsimulation_gb300 import abi
-    solver = abi.SOLVER_CG if a.solver == "cg" else abi.SOLVER_JACOBI
+    solver = abi.SOLVER_JACOBI if a.solver == "jacobi" else abi.SOLVER_CG
     prm = abi.params_dam(1.0 / a.size, a.dt, solver, 1e-6)
     # the reference's MAX_STEPS default (2000) is too small for plain CG to reach 1e-6 at 256^3; the cap
     # only guards against non-convergence here
@@ -299,6 +302,120 @@ def run_gb300(a):
         dist.destroy_process_group()
 
 
+UNET_LAYERS = ((16, 16, 0), (16, 32, 1), (32, 64, 2), (64, 32, 1), (32, 16, 0), (16, 16, 0))
+
+
+def unet_flops(n):
+    """Dense FLOPs of one U-Net forward pass on an n^3 grid (2 * 27 * cin * cout per output voxel and layer)."""
+    vox = [n ** 3]
+    m = n
+    for _ in range(2):
+        m = (m + 1) // 2
+        vox.append(m ** 3)
+    return [2 * 27 * ci * co * vox[lv] for ci, co, lv in UNET_LAYERS]
+
+
+def run_fcg(a):
+    """The learned-preconditioner line: FCG with the U-Net on the same 256^3 dam break.  The network is trained
+    first on the device (outside the timed region) on samples of other seeds at --fcg-train-size."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    n, nt = a.size, a.fcg_train_size
+    prm_t = abi.params_dam(1.0 / nt, a.dt, abi.SOLVER_CG, 1e-6)
+    prm_t.max_steps = 20000
+    T = gb.GB300Simulator3D(nt, nt, nt, prm_t)
+    T.unet_init(a.seed + 7, 48)
+    t0 = time.perf_counter()
+    for sd in (a.seed + 1, a.seed + 2):
+        bt, rt = gb.scene_dam3d(nt, nt, nt, a.spheres, a.spheres, sd)
+        T.reset()
+        T.set_field(abi.FIELD_BOUNDARY, bt)
+        T.set_field(abi.FIELD_RHO, rt)
+        for _ in range(24):
+            T.update(1)
+            T.unet_add_sample()
+    T.synchronize()
+    t1 = time.perf_counter()
+    loss0 = T.unet_train(1, 8, 1e-3, 0.5, 1, loss_kind=1)
+    loss = T.unet_train(a.fcg_train_iters, 4, 1e-3, 0.5, 2, loss_kind=1)
+    t2 = time.perf_counter()
+    W = T.unet_weights()
+    T.close()
+
+    prm = workload(a)
+    prm.solver = abi.SOLVER_FCG_UNET
+    b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
+    sim = gb.GB300Simulator3D(n, n, n, prm)
+    sim.set_field(abi.FIELD_BOUNDARY, b)
+    sim.set_field(abi.FIELD_RHO, r)
+    sim.unet_init(0, 0)
+    sim.unet_set_weights(W)
+    for _ in range(a.warmup):
+        sim.update(1)
+    sim.synchronize()
+    st0 = sim.stats()
+    precond = []
+    with Clocks(local) as clk:
+        sim.mark(0)
+        for _ in range(a.steps):
+            sim.update(1)
+            precond.append(sim.stats().precond_steps)
+        sim.mark(1)
+        ms = sim.elapsed_ms(0, 1)
+    clocks = clk.summary()
+    st1 = sim.stats()
+    iters = (st1.total_solve_steps - st0.total_solve_steps) / max(a.steps, 1)
+    # plain CG on the continuation of the same trajectory, for the iteration and time comparison
+    cg = prm.copy()
+    cg.solver = abi.SOLVER_CG
+    sim.set_params(cg)
+    sim.update(1)
+    sim.synchronize()
+    sc0 = sim.stats()
+    sim.mark(2)
+    sim.update(3)
+    sim.mark(3)
+    ms_cg = sim.elapsed_ms(2, 3) / 3
+    sc1 = sim.stats()
+    # the dominant kernel: the implicit-GEMM convolutions of one forward pass, timed on the device
+    sim.set_params(prm)
+    ms_fwd, ms_layers = sim.unet_time_forward(3)
+    sim.close()
+    flops = unet_flops(n)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    conv_ms = float(sum(ms_layers))
+    achieved = sum(flops) / (conv_ms / 1e3) / 1e12 if conv_ms > 0 else None
+    roofline = {"kernel": "k_conv3_tc (6 implicit-GEMM convolutions of one U-Net forward pass)", "bound": "tensor",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                "traffic": None, "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if "bf16_tflops" in peaks
+                else "fallback 1900 TFLOP/s", "flop_per_forward": sum(flops), "ms_per_forward": ms_fwd,
+                "ms_per_layer": [round(float(x), 4) for x in ms_layers]}
+    steps_per_s = a.steps / (ms / 1e3)
+    cfg = config(a)
+    cfg["solver"] = "fcg_unet rel-res 1e-6 (flexible PCG, U-Net 16/32/64 BF16, FP64 x, CG fallback on stall)"
+    line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cell_updates_per_s": steps_per_s * (n - 2) ** 3, "solve_iters_per_step": iters,
+            "precond_iters_per_step": float(np.mean(precond)) if precond else 0.0,
+            "fcg_converged": bool(st1.converged),
+            "plain_cg_same_trajectory": {"iters_per_step": (sc1.total_solve_steps - sc0.total_solve_steps) / 3,
+                                         "ms_per_step": ms_cg},
+            "training": {"grid": [nt] * 3, "samples": 48, "scenes": 2, "iterations": a.fcg_train_iters, "batch": 4,
+                         "loss": "energy-norm alignment", "synthetic_fraction": 0.5, "loss_first": loss0,
+                         "loss_last": loss, "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)},
+            "roofline": roofline, "clocks": clocks, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_precision_study(a):
     """One JSON line with the maxima of the per-step errors (the 3D dam break with --spheres spheres)."""
     from eulerianfluidsimulation_gb300.precision import precision_study
@@ -320,6 +437,8 @@ def main():
         return
     if a.impl == "reference":
         run_reference(a)
+    elif a.solver == "fcg":
+        run_fcg(a)
     else:
         run_gb300(a)
 

@@ -612,27 +612,42 @@ cudaError_t scale_rows(UNetState* u, const float* x, const uint16_t* rowinfo, lo
 
 // forward pass on the input field `r` (FP32, reference layout) with matrix rows `rowinfo`; y32 holds the output.
 // train: keep the pre-activations for the backward pass.
-cudaError_t forward(UNetState* u, const float* r, const uint16_t* rowinfo, bool train, cudaStream_t st) {
+cudaError_t forward(UNetState* u, const float* r, const uint16_t* rowinfo, bool train, cudaStream_t st,
+                    cudaEvent_t* ev = nullptr) {
     const Level *L = u->L;
+    // ev (optional): 12 events recorded before and after each of the six convolutions
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
     k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0);
     UCK(cudaGetLastError());
     const float* B[kLayers];
     for (int k = 0; k < kLayers; k++) B[k] = u->w32 + u->boff[k];
+    mark(0);
     UCK(conv(u, 0, u->x0, u->wf[0], 16, 16, 0, B[0], nullptr, u->e0, nullptr, train ? u->a0 : nullptr, 1, st));
+    mark(1);
     k_pool<<<nblk(L[1].V * 2), 256, 0, st>>>(u->e0, L[0], u->p0, L[1], 16);
     UCK(cudaGetLastError());
+    mark(2);
     UCK(conv(u, 1, u->p0, u->wf[1], 16, 32, 1, B[1], nullptr, u->e1, nullptr, train ? u->a1 : nullptr, 1, st));
+    mark(3);
     k_pool<<<nblk(L[2].V * 4), 256, 0, st>>>(u->e1, L[1], u->p1, L[2], 32);
     UCK(cudaGetLastError());
+    mark(4);
     UCK(conv(u, 2, u->p1, u->wf[2], 32, 64, 2, B[2], nullptr, u->e2, nullptr, train ? u->a2 : nullptr, 1, st));
+    mark(5);
     k_up<<<nblk(L[1].V * 8), 256, 0, st>>>(u->e2, L[2], u->u2, L[1], 64);
     UCK(cudaGetLastError());
+    mark(6);
     UCK(conv(u, 3, u->u2, u->wf[3], 64, 32, 1, B[3], u->e1, u->d1, nullptr, train ? u->a3 : nullptr, 1, st));
+    mark(7);
     k_up<<<nblk(L[0].V * 4), 256, 0, st>>>(u->d1, L[1], u->u1, L[0], 32);
     UCK(cudaGetLastError());
+    mark(8);
     UCK(conv(u, 4, u->u1, u->wf[4], 32, 16, 0, B[4], u->e0, u->d0, nullptr, train ? u->a4 : nullptr, 1, st));
+    mark(9);
+    mark(10);
     UCK(conv(u, 5, u->d0, u->wf[5], 16, 16, 0, B[5], nullptr, nullptr, u->y32, nullptr, 0, st));
+    mark(11);
     return cudaSuccess;
 }
 
@@ -1042,6 +1057,44 @@ int efs_unet_loss_grad(efs_ctx* c, int loss_kind, const float* b_host, const flo
     if (grads_host) ACK(cudaMemcpyAsync(grads_host, u->grad, u->nparam * sizeof(float), cudaMemcpyDeviceToHost, st), "download");
     ACK(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     if (loss) *loss = (float)l;
+    return efs::check_err(c, u);
+}
+
+int efs_unet_time_forward(efs_ctx* c, int reps, float* ms_forward, float* ms_layers) {
+    if (!c) return EFS_ERR_ARG;
+    UNetState* u = c->unet;
+    if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (reps < 1) return efs::ufail(c, EFS_ERR_ARG, "reps >= 1");
+    cudaStream_t st = c->stream;
+    cudaEvent_t ev[12], e0, e1;
+    for (auto& e : ev) ACK(cudaEventCreate(&e), "cudaEventCreate");
+    ACK(cudaEventCreate(&e0), "cudaEventCreate");
+    ACK(cudaEventCreate(&e1), "cudaEventCreate");
+    ACK(efs::launch_solver_prep(c), "solver prep");
+    ACK(efs::forward(u, c->div, c->rowinfo, false, st), "U-Net forward");   // warm-up
+    double lay[6] = {0, 0, 0, 0, 0, 0};
+    float total = 0.f;
+    cudaError_t err = cudaSuccess;
+    for (int k = 0; k < reps && err == cudaSuccess; k++) {
+        cudaEventRecord(e0, st);
+        err = efs::forward(u, c->div, c->rowinfo, false, st, ev);
+        cudaEventRecord(e1, st);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (err == cudaSuccess) { cudaEventElapsedTime(&ms, e0, e1); total += ms; }
+        for (int l = 0; l < 6 && err == cudaSuccess; l++) {
+            float m = 0.f;
+            cudaEventElapsedTime(&m, ev[2 * l], ev[2 * l + 1]);
+            lay[l] += m;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ACK(err, "U-Net timing");
+    if (ms_forward) *ms_forward = total / reps;
+    if (ms_layers)
+        for (int l = 0; l < 6; l++) ms_layers[l] = (float)(lay[l] / reps);
     return efs::check_err(c, u);
 }
 

@@ -211,6 +211,13 @@ class _GB300Simulator:
         check(lib().efs_unet_loss_grad(self._h, loss_kind, fptr(bb), fptr(pp), ctypes.byref(loss), fptr(g)), self._h)
         return loss.value, g
 
+    def unet_time_forward(self, reps=5):
+        """(ms per forward pass, ms per convolution layer [6]) on the device."""
+        ms = np.zeros(1, np.float32)
+        lay = np.zeros(6, np.float32)
+        check(lib().efs_unet_time_forward(self._h, reps, fptr(ms), fptr(lay)), self._h)
+        return float(ms[0]), lay
+
     def unet_add_sample(self):
         check(lib().efs_unet_add_sample(self._h), self._h)
 

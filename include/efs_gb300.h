@@ -261,6 +261,10 @@ int  efs_unet_apply(efs_ctx* ctx, const float* r, float* z);
  *                search along z leaves, i.e. how far z is from a perfect preconditioned direction.
  * efs_unet_loss_grad gives the loss and the gradient of every parameter for one sample (grads may be NULL). */
 int  efs_unet_loss_grad(efs_ctx* ctx, int loss_kind, const float* b, const float* p, float* loss, float* grads);
+/* Device time of the network's forward pass on the current divergence field (CUDA events on the context's
+ * stream, `reps` passes after one warm-up): mean ms per pass and per convolution layer (ms_layers[6], may
+ * be NULL).  A measurement entry point: the pressure field is overwritten with the divergence. */
+int  efs_unet_time_forward(efs_ctx* ctx, int reps, float* ms_forward, float* ms_layers);
 /* Stores the current (divergence, pressure, matrix rows) as a training sample (ring buffer). */
 int  efs_unet_add_sample(efs_ctx* ctx);
 int  efs_unet_sample_count(efs_ctx* ctx, int* count);
