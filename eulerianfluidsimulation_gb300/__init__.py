@@ -7,8 +7,9 @@ The compute path is ``libefs_gb300.so`` (hand-written CUDA kernels behind the C 
 from . import abi
 from .abi import EfsParams, EfsStats, params_default
 from ._lib import EfsError, LIB_PATH
-from .simulator import (GB300Simulator2D, GB300Simulator3D, device_count, params_dam, scene_batch2d,
-                        scene_dam2d, scene_dam3d)
+from .simulator import (GB300Batch2D, GB300Simulator2D, GB300Simulator3D, device_count, params_dam, scene_batch2d,
+                        scene_dam2d, scene_dam3d, unet_param_count)
 
-__all__ = ["abi", "EfsParams", "EfsStats", "EfsError", "LIB_PATH", "GB300Simulator2D", "GB300Simulator3D",
-           "device_count", "params_dam", "params_default", "scene_batch2d", "scene_dam2d", "scene_dam3d"]
+__all__ = ["abi", "EfsParams", "EfsStats", "EfsError", "LIB_PATH", "GB300Batch2D", "GB300Simulator2D",
+           "GB300Simulator3D", "device_count", "params_dam", "params_default", "scene_batch2d", "scene_dam2d",
+           "scene_dam3d", "unet_param_count"]

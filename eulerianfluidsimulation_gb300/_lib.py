@@ -7,7 +7,7 @@ no CPU fallback.  Build it with ``python -c "import __graft_entry__ as g; g.buil
 import ctypes
 import os
 
-from .abi import EfsParams, EfsStats, STATUS_NAMES
+from .abi import EfsBatchTuning, EfsParams, EfsStats, STATUS_NAMES
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libefs_gb300.so")
@@ -31,6 +31,21 @@ SIGNATURES = {
     "efs_upload_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP]),
     "efs_download_fields": (ctypes.c_int, [_CTX, _FP, _FP, _FP, _FP, _FP, _FP]),
     "efs_download_pressure_fp64": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_double)]),
+    "efs_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(EfsParams), _FP, ctypes.POINTER(_CTX)]),
+    "efs_batch_destroy": (None, [_CTX]),
+    "efs_batch_last_error": (ctypes.c_char_p, [_CTX]),
+    "efs_batch_scene_count": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int)]),
+    "efs_batch_upload_field": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _FP]),
+    "efs_batch_download_field": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _FP]),
+    "efs_batch_stage": (ctypes.c_int, [_CTX, ctypes.c_int]),
+    "efs_batch_step": (ctypes.c_int, [_CTX, ctypes.c_int]),
+    "efs_batch_synchronize": (ctypes.c_int, [_CTX]),
+    "efs_batch_stats": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.POINTER(EfsStats)]),
+    "efs_batch_kernel_count": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int)]),
+    "efs_batch_get_tuning": (ctypes.c_int, [_CTX, ctypes.POINTER(EfsBatchTuning)]),
+    "efs_batch_set_tuning": (ctypes.c_int, [_CTX, ctypes.POINTER(EfsBatchTuning)]),
+    "efs_batch_autotune": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.POINTER(EfsBatchTuning)]),
     "efs_unet_param_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     "efs_unet_init": (ctypes.c_int, [_CTX, ctypes.c_uint64, ctypes.c_int]),
     "efs_unet_get_weights": (ctypes.c_int, [_CTX, _FP, ctypes.c_int64]),

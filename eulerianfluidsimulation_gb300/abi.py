@@ -96,6 +96,20 @@ class EfsStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class EfsBatchTuning(ctypes.Structure):
+    """``efs_batch_tuning``: launch configuration of a batch of 2D scenes."""
+    _fields_ = [
+        ("tile_x", ctypes.c_int),
+        ("tile_y", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int),
+        ("solver_threads", ctypes.c_int),
+        ("ms_per_step", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 def _f32(x):
     return ctypes.c_float(x).value
 

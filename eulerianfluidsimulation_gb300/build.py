@@ -24,6 +24,7 @@ UNITS = {
     "efs_solver.cu": ["--fmad=false"],
     "efs_noalloc.cu": ["--fmad=false"],
     "efs_unet.cu": [],
+    "efs_batch.cu": ["--fmad=false"],
 }
 
 

@@ -1,0 +1,721 @@
+// efs_batch.cu — many independent 2D scenes of uneven sizes advanced together (efs_batch_* entry points).
+//
+// Every scene is a full reference 2D simulation (CPUSimulator2D: the seven stages of ISimulator::update,
+// include/simulation/simulator/ISimulator.h:12-38, and CGSolverCPU2D::solve, src/simulation/solver/
+// CGSolver.cpp:32-111) with its own grid size and cell size; the batch shares one set of parameters except
+// GRAVITY_FORCE, which is per scene (9.81 / dx in cells/s^2).  One step of all scenes is one CUDA graph: each
+// stage kernel is a single persistent launch over a table of (scene, block) entries (efs_stages.cu), and the
+// pressure solves are one persistent launch in which each block solves whole scenes (block-level CG, scenes
+// in descending size), so no scene waits on another and no grid-wide barrier is needed.  The tile shape of
+// the stage kernels, their blocks per SM and the solver's block size are chosen by efs_batch_autotune from
+// timed trial steps.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "efs_batch.h"
+
+using namespace efs;
+
+struct efs_batch {
+    int n = 0;
+    efs_params prm{};
+    int device = 0, sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<BScene> sc;
+    BScene* d_sc = nullptr;
+    std::vector<int> order;            // scenes by descending cell count (solver assignment)
+    int* d_order = nullptr;
+    long long total = 0;
+    BFields F{};
+    double* p64 = nullptr;
+    float *r = nullptr, *d = nullptr, *t = nullptr, *e = nullptr;
+    std::vector<void*> allocs;
+    BEntry* d_tab[5] = {};
+    int ntab[5] = {};
+    // tuning
+    int bx = 32, by = 8, bps = 4, cg_threads = 512;
+    cudaGraphExec_t graph = nullptr;
+    cudaGraph_t graph_def = nullptr;
+    unsigned graph_stages = 0;
+    int graph_kernels = 0;
+    int64_t frames = 0;
+    std::string err;
+};
+
+namespace {
+
+std::string g_batch_create_error;
+
+int bfail(efs_batch* b, int status, const std::string& msg) {
+    if (b) b->err = msg; else g_batch_create_error = msg;
+    return status;
+}
+int bcuda(efs_batch* b, cudaError_t e, const char* what) {
+    return bfail(b, EFS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define BCK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return bcuda(b, e_, what); } while (0)
+
+template <typename T>
+cudaError_t balloc(efs_batch* b, T** p, long long count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), (size_t)std::max<long long>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    b->allocs.push_back(*p);
+    return cudaMemset(*p, 0, (size_t)std::max<long long>(count, 1) * sizeof(T));
+}
+
+// ---- block-level CG: EFS_CG_MIXED_RECURRENCE on one scene per block (CGSolver.cpp:32-83 with the mixed
+// precision and recurrence of the persistent solver; see efs_gb300.h) ----------------------------------------
+struct BSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = s + v;
+        const float z = t - s;
+        c += (s - (t - z)) + (v - z);
+        s = t;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);
+        add(p);
+        c += e;
+    }
+};
+
+// block sums of up to three pair sums, returned as doubles to every thread
+__device__ void block_reduce3(BSum a, BSum b, BSum c, double& ta, double& tb, double& tc) {
+    __shared__ double sh[3][32];
+    __shared__ double tot[3];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float as = __shfl_down_sync(0xffffffffu, a.s, o), ac = __shfl_down_sync(0xffffffffu, a.c, o);
+        const float bs = __shfl_down_sync(0xffffffffu, b.s, o), bc = __shfl_down_sync(0xffffffffu, b.c, o);
+        const float cs = __shfl_down_sync(0xffffffffu, c.s, o), cc = __shfl_down_sync(0xffffffffu, c.c, o);
+        a.add(as); a.c += ac;
+        b.add(bs); b.c += bc;
+        c.add(cs); c.c += cc;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        sh[0][warp] = (double)a.s + (double)a.c;
+        sh[1][warp] = (double)b.s + (double)b.c;
+        sh[2][warp] = (double)c.s + (double)c.c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0, y = 0, z = 0;
+        for (int w = 0; w < nw; w++) { x += sh[0][w]; y += sh[1][w]; z += sh[2][w]; }
+        tot[0] = x; tot[1] = y; tot[2] = z;
+    }
+    __syncthreads();
+    ta = tot[0]; tb = tot[1]; tc = tot[2];
+    __syncthreads();
+}
+
+__device__ __forceinline__ float lap2_f(const float* x, uint16_t f, int i, int W) {
+    float s = 0.f;
+    if (f & 1u) s += x[i - 1];
+    if (f & 2u) s += x[i + 1];
+    if (f & 4u) s += x[i - W];
+    if (f & 8u) s += x[i + W];
+    return s - (float)((f >> 8) & 7) * x[i];
+}
+template <typename T>
+__device__ __forceinline__ double lap2_d(const T* x, uint16_t f, int i, int W) {
+    double s = 0.0;
+    if (f & 1u) s += (double)x[i - 1];
+    if (f & 2u) s += (double)x[i + 1];
+    if (f & 4u) s += (double)x[i - W];
+    if (f & 8u) s += (double)x[i + W];
+    return s - (double)((f >> 8) & 7) * (double)x[i];
+}
+
+struct BCGArgs {
+    const BScene* sc;
+    const int* order;
+    int n;
+    BFields F;
+    double* p64;
+    float *r, *d, *t, *e;
+    int max_steps;
+    float tol_rel, solver_threshold;
+};
+
+__global__ void k_batch_cg(BCGArgs A) {
+    for (int k = blockIdx.x; k < A.n; k += gridDim.x) {
+        const int s = A.order[k];
+        const BScene S = A.sc[s];
+        const long long o = S.base;
+        const int N = S.g.N, W = S.g.W;
+        const float* b = A.F.div + o;
+        const uint16_t* info = A.F.rowinfo + o;
+        float* p = A.F.p + o;
+        double* p64 = A.p64 + o;
+        float *r = A.r + o, *d = A.d + o, *t = A.t + o, *e = A.e + o;
+        DevCtl* ctl = A.F.sctl + s;
+        // r = b - L p0 with p0 = b (CGSolver.cpp:63-72), in FP64; d = r
+        BSum rr_p, bb_p, rows_p;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const float bi = b[i];
+            bb_p.add_prod(bi, bi);
+            const uint16_t f = info[i];
+            if (!(f & 0x8000u)) continue;
+            rows_p.add(1.f);
+            p64[i] = (double)bi;
+            e[i] = 0.f;
+            const float ri = (float)((double)bi - lap2_d(b, f, i, W));
+            r[i] = ri;
+            d[i] = ri;
+            rr_p.add_prod(ri, ri);
+        }
+        double rr, bb, rows;
+        block_reduce3(rr_p, bb_p, rows_p, rr, bb, rows);
+        float thr_f = A.tol_rel > 0 ? (float)((double)A.tol_rel * (double)A.tol_rel * bb) : A.solver_threshold;
+        if (A.tol_rel > 0 && !(thr_f > 0)) thr_f = FLT_MIN;
+        const double thr = (double)thr_f;
+        // true residual: fold e into p64, r = b - L p64 in FP64 (CGSolver.cpp:46-50)
+        auto replace = [&](double& rr_out) {
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                if (!(info[i] & 0x8000u)) continue;
+                p64[i] += (double)e[i];
+                e[i] = 0.f;
+            }
+            __syncthreads();
+            BSum rp;
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                const uint16_t f = info[i];
+                if (!(f & 0x8000u)) continue;
+                const float ri = (float)((double)b[i] - lap2_d(p64, f, i, W));
+                r[i] = ri;
+                rp.add_prod(ri, ri);
+            }
+            double u1, u2;
+            block_reduce3(rp, BSum(), BSum(), rr_out, u1, u2);
+        };
+        int conv = rr < thr, it = 0;
+        if (!conv) {
+            for (it = 0; it < A.max_steps; it++) {
+                BSum dtp, ttp;
+                for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                    const uint16_t f = info[i];
+                    if (!(f & 0x8000u)) continue;
+                    const float ti = lap2_f(d, f, i, W);
+                    t[i] = ti;
+                    dtp.add_prod(d[i], ti);
+                    ttp.add_prod(ti, ti);
+                }
+                double dt, tt, u3;
+                block_reduce3(dtp, ttp, BSum(), dt, tt, u3);
+                const double ad = rr / dt;
+                const float alpha = (float)ad;
+                const double old = rr;
+                bool replaced = false;
+                if (it & 0x3F) {
+                    const float beta = (float)((ad * ad * tt - rr) / rr);
+                    BSum rp;
+                    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                        if (!(info[i] & 0x8000u)) continue;
+                        const float di = d[i];
+                        e[i] += alpha * di;
+                        const float rn = r[i] + (-alpha) * t[i];
+                        r[i] = rn;
+                        d[i] = di * beta + rn;
+                        rp.add_prod(rn, rn);
+                    }
+                    double u1, u2;
+                    block_reduce3(rp, BSum(), BSum(), rr, u1, u2);
+                } else {
+                    for (int i = threadIdx.x; i < N; i += blockDim.x)
+                        if (info[i] & 0x8000u) e[i] += alpha * d[i];
+                    __syncthreads();
+                    replace(rr);
+                    replaced = true;
+                    const float beta = (float)(rr / old);
+                    for (int i = threadIdx.x; i < N; i += blockDim.x)
+                        if (info[i] & 0x8000u) d[i] = d[i] * beta + r[i];
+                    __syncthreads();
+                }
+                if (rr < thr) {
+                    if (!replaced) replace(rr);
+                    if (rr < thr) { conv = 1; break; }
+                }
+            }
+            it = min(it + 1, A.max_steps);
+        }
+        // p = p64 + e (FP64 accumulator folded), rows only
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            if (!(info[i] & 0x8000u)) continue;
+            const double v = p64[i] + (double)e[i];
+            p64[i] = v;
+            e[i] = 0.f;
+            p[i] = (float)v;
+        }
+        if (threadIdx.x == 0) {
+            ctl->converged = conv;
+            ctl->iterations = it;
+            ctl->rr = rr;
+            ctl->bb = bb;
+            ctl->thr = thr;
+            ctl->active_cells = (long long)rows;
+            ctl->total_iterations += it;
+            ctl->solves += 1;
+            ctl->precond_iterations = 0;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- host side --------------------------------------------------------------------------------------------
+void build_tables(efs_batch* b, std::vector<BEntry> (&tab)[5]) {
+    for (auto& t : tab) t.clear();
+    for (int s = 0; s < b->n; s++) {
+        const Geo& g = b->sc[s].g;
+        const int ix = (g.W - 2 + b->bx - 1) / b->bx, iy = (g.H - 2 + b->by - 1) / b->by;
+        for (int y = 0; y < iy; y++)
+            for (int x = 0; x < ix; x++) tab[0].push_back(BEntry{s, x, y, 0});
+        const int px = (g.W - 1 + b->bx - 1) / b->bx, py = (g.H - 1 + b->by - 1) / b->by;
+        for (int y = 0; y < py; y++)
+            for (int x = 0; x < px; x++) tab[1].push_back(BEntry{s, x, y, 0});
+        const int nl = (((g.N + 31) / 32) * 32 + 255) / 256;
+        for (int x = 0; x < nl; x++) tab[2].push_back(BEntry{s, x, 0, 0});
+        for (int x = 0; x < (g.H - 2 + 127) / 128; x++) tab[3].push_back(BEntry{s, x, 0, 0});
+        for (int x = 0; x < (g.W - 2 + 127) / 128; x++) tab[4].push_back(BEntry{s, x, 0, 0});
+    }
+}
+
+int upload_tables(efs_batch* b) {
+    std::vector<BEntry> tab[5];
+    build_tables(b, tab);
+    for (int k = 0; k < 5; k++) {
+        if (b->d_tab[k]) cudaFree(b->d_tab[k]);
+        b->d_tab[k] = nullptr;
+        BCK(cudaMalloc(reinterpret_cast<void**>(&b->d_tab[k]), std::max<size_t>(1, tab[k].size()) * sizeof(BEntry)), "cudaMalloc table");
+        if (!tab[k].empty())
+            BCK(cudaMemcpy(b->d_tab[k], tab[k].data(), tab[k].size() * sizeof(BEntry), cudaMemcpyHostToDevice), "upload table");
+        b->ntab[k] = (int)tab[k].size();
+    }
+    return EFS_OK;
+}
+
+BLaunch launch_of(const efs_batch* b) {
+    BLaunch L{};
+    L.interior = BView{b->d_tab[0], b->ntab[0], b->d_sc};
+    L.post = BView{b->d_tab[1], b->ntab[1], b->d_sc};
+    L.linear = BView{b->d_tab[2], b->ntab[2], b->d_sc};
+    L.dx = BView{b->d_tab[3], b->ntab[3], b->d_sc};
+    L.dy = BView{b->d_tab[4], b->ntab[4], b->d_sc};
+    L.bx_dim = b->bx;
+    L.by_dim = b->by;
+    L.grid = b->sm_count * b->bps;
+    L.list_grid = b->sm_count * 4;
+    L.total_cells = b->total;
+    L.F = b->F;
+    L.dt = b->prm.dt;
+    L.vel_decay = b->prm.vel_decay;
+    L.rho_d = b->prm.rho_d;
+    L.thrL = b->prm.liquid_threshold;
+    L.lp = b->prm.lambda_plus;
+    L.lm = b->prm.lambda_minus;
+    L.eta = b->prm.eta;
+    L.gravity = b->prm.gravity_enabled ? 1 : 0;
+    L.stream = b->stream;
+    return L;
+}
+
+cudaError_t launch_cg(const efs_batch* b) {
+    BCGArgs A;
+    A.sc = b->d_sc;
+    A.order = b->d_order;
+    A.n = b->n;
+    A.F = b->F;
+    A.p64 = b->p64;
+    A.r = b->r; A.d = b->d; A.t = b->t; A.e = b->e;
+    A.max_steps = b->prm.max_steps;
+    A.tol_rel = b->prm.tol_rel;
+    A.solver_threshold = b->prm.solver_threshold;
+    const int grid = std::min(b->n, b->sm_count * (1024 / b->cg_threads));
+    k_batch_cg<<<std::max(1, grid), b->cg_threads, 0, b->stream>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_stage(const efs_batch* b, int stage, bool fuse) {
+    const BLaunch L = launch_of(b);
+    if (stage == EFS_STAGE_PROJECT) {
+        cudaError_t e = batch_project_pre(L);
+        if (e != cudaSuccess) return e;
+        if ((e = launch_cg(b)) != cudaSuccess) return e;
+        return batch_project_post(L);
+    }
+    return batch_stage(L, stage, fuse);
+}
+
+cudaError_t enqueue_step(const efs_batch* b, unsigned stages) {
+    const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
+    for (int s = 0; s < EFS_STAGE_COUNT; s++) {
+        if (!(stages & EFS_STAGE_BIT(s))) continue;
+        if (s == EFS_STAGE_ADD_FORCE && fuse) continue;
+        cudaError_t e = enqueue_stage(b, s, s == EFS_STAGE_VEL_ADVECT && fuse);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void drop_graph(efs_batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph_def) cudaGraphDestroy(b->graph_def);
+    b->graph = nullptr;
+    b->graph_def = nullptr;
+}
+
+int build_graph(efs_batch* b) {
+    const unsigned stages = EFS_STAGES_ALL & ~b->prm.disable_mask;
+    if (b->graph && b->graph_stages == stages) return EFS_OK;
+    drop_graph(b);
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaError_t le = enqueue_step(b, stages);
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess) { if (g) cudaGraphDestroy(g); return bcuda(b, le, "batch step capture"); }
+    if (ce != cudaSuccess) return bcuda(b, ce, "cudaStreamEndCapture");
+    size_t n = 0;
+    cudaGraphGetNodes(g, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) cudaGraphGetNodes(g, nodes.data(), &n);
+    int kernels = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels++;
+    }
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+    if (ie != cudaSuccess) { cudaGraphDestroy(g); return bcuda(b, ie, "cudaGraphInstantiate"); }
+    b->graph = ex;
+    b->graph_def = g;
+    b->graph_stages = stages;
+    b->graph_kernels = kernels;
+    return EFS_OK;
+}
+
+int check_status(efs_batch* b) {
+    BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    DevCtl h;
+    BCK(cudaMemcpy(&h, b->F.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost), "read device status");
+    if (h.error) return bfail(b, EFS_ERR_DEVICE_FAULT, "device error word " + std::to_string(h.error));
+    return EFS_OK;
+}
+
+bool field_ok(int f) {
+    return f == EFS_FIELD_VEL || f == EFS_FIELD_RHO || f == EFS_FIELD_GAMMA || f == EFS_FIELD_BETA ||
+           f == EFS_FIELD_DIVERGENCE || f == EFS_FIELD_PRESSURE || f == EFS_FIELD_FORCES || f == EFS_FIELD_BOUNDARY;
+}
+
+float* scalar_field(efs_batch* b, int f) {
+    switch (f) {
+        case EFS_FIELD_RHO: return b->F.rho;
+        case EFS_FIELD_GAMMA: return b->F.gamma;
+        case EFS_FIELD_BETA: return b->F.beta;
+        case EFS_FIELD_DIVERGENCE: return b->F.div;
+        case EFS_FIELD_PRESSURE: return b->F.p;
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* efs_batch_last_error(const efs_batch* b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+void efs_batch_destroy(efs_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    for (auto& t : b->d_tab) if (t) cudaFree(t);
+    for (void* p : b->allocs) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int efs_batch_create(int n_scenes, const int* widths, const int* heights, const efs_params* params,
+                     const float* gravity_force, efs_batch** out) {
+    if (!out) return bfail(nullptr, EFS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (n_scenes < 1 || !widths || !heights || !params) return bfail(nullptr, EFS_ERR_ARG, "n_scenes >= 1 and non-NULL arrays");
+    if (params->solver != EFS_SOLVER_CG || params->cg_variant != EFS_CG_MIXED_RECURRENCE)
+        return bfail(nullptr, EFS_ERR_ARG, "batched scenes use the CG solver (EFS_CG_MIXED_RECURRENCE)");
+    if (params->re_calc_div) return bfail(nullptr, EFS_ERR_ARG, "RE_CALC_DIV is not supported in batches");
+    if (params->max_steps < 0 || !std::isfinite(params->dt)) return bfail(nullptr, EFS_ERR_ARG, "bad params");
+    for (int s = 0; s < n_scenes; s++)
+        if (widths[s] < 4 || heights[s] < 4 || (long long)widths[s] * heights[s] > (1LL << 26))
+            return bfail(nullptr, EFS_ERR_ARG, "scene sizes must be 4..2^26 cells");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return bfail(nullptr, EFS_ERR_NO_DEVICE, "no CUDA device");
+    efs_batch* b = new efs_batch();
+    b->n = n_scenes;
+    b->prm = *params;
+    cudaGetDevice(&b->device);
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+    cudaError_t e;
+    auto bail = [&](cudaError_t er, const char* what) {
+        const int st = bcuda(nullptr, er, what);
+        efs_batch_destroy(b);
+        return st;
+    };
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    long long off = 0;
+    for (int s = 0; s < n_scenes; s++) {
+        BScene S{};
+        S.g = Geo{widths[s], heights[s], 1, widths[s] * heights[s], widths[s] * heights[s]};
+        S.base = off;
+        S.gforce = gravity_force ? gravity_force[s] : params->gravity_force;
+        off += ((long long)S.g.N + 31) / 32 * 32;
+        b->sc.push_back(S);
+    }
+    b->total = off;
+    b->order.resize(n_scenes);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return b->sc[x].g.N > b->sc[y].g.N; });
+    const long long T = b->total;
+    BFields& F = b->F;
+#define BA(ptr, cnt) if ((e = balloc(b, &(ptr), (cnt))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr)
+    BA(b->d_sc, n_scenes); BA(b->d_order, n_scenes);
+    BA(F.u, T); BA(F.v, T); BA(F.rho, T); BA(F.gamma, T); BA(F.beta, T); BA(F.div, T); BA(F.p, T); BA(F.fx, T); BA(F.fy, T);
+    BA(F.solid, T); BA(F.tu, T); BA(F.tv, T); BA(F.validA, T); BA(F.validB, T);
+    BA(F.wb, 4 * T); BA(F.wf, 4 * T); BA(F.bb, T); BA(F.fb, T); BA(F.bsum, T); BA(F.gsum, T); BA(F.rho_acc, T);
+    BA(F.sh_idx, T); BA(F.sh_sid, T); BA(F.sh_val, T); BA(F.sh_end, 3 * T);
+    BA(F.rowinfo, T); BA(F.chunk_flag, T / 32 + 1); BA(F.ctl, 1); BA(F.sctl, n_scenes);
+    BA(b->p64, T); BA(b->r, T); BA(b->d, T); BA(b->t, T); BA(b->e, T);
+#undef BA
+    F.list_cap = (int)std::min<long long>(T, 1LL << 30);
+    if ((e = cudaMemcpy(b->d_sc, b->sc.data(), n_scenes * sizeof(BScene), cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "upload scenes");
+    if ((e = cudaMemcpy(b->d_order, b->order.data(), n_scenes * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "upload order");
+    // Grid2D constructor state (Grid2D.cpp:11-66): zero fields, gamma = 1, solid border
+    std::vector<float> ones(T, 1.f);
+    std::vector<uint8_t> solid(T, 0);
+    for (const auto& S : b->sc)
+        for (int y = 0; y < S.g.H; y++)
+            for (int x = 0; x < S.g.W; x++)
+                if (x == 0 || y == 0 || x == S.g.W - 1 || y == S.g.H - 1) solid[S.base + (long long)y * S.g.W + x] = 1;
+    if ((e = cudaMemcpy(F.gamma, ones.data(), T * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "init");
+    if ((e = cudaMemcpy(F.solid, solid.data(), T, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "init");
+    const int ts = upload_tables(b);
+    if (ts != EFS_OK) { efs_batch_destroy(b); return ts; }
+    *out = b;
+    return EFS_OK;
+}
+
+int efs_batch_scene_count(const efs_batch* b, int* n) {
+    if (!b || !n) return EFS_ERR_ARG;
+    *n = b->n;
+    return EFS_OK;
+}
+
+int efs_batch_upload_field(efs_batch* b, int scene, int field, const float* host) {
+    if (!b) return EFS_ERR_ARG;
+    if (scene < 0 || scene >= b->n || !field_ok(field) || !host) return bfail(b, EFS_ERR_ARG, "bad scene, field or pointer");
+    const BScene& S = b->sc[scene];
+    const long long N = S.g.N, o = S.base;
+    BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    if (field == EFS_FIELD_VEL || field == EFS_FIELD_FORCES) {
+        std::vector<float> a(N), c(N);
+        for (long long i = 0; i < N; i++) { a[i] = host[2 * i]; c[i] = host[2 * i + 1]; }
+        float* da = field == EFS_FIELD_VEL ? b->F.u : b->F.fx;
+        float* dc = field == EFS_FIELD_VEL ? b->F.v : b->F.fy;
+        BCK(cudaMemcpy(da + o, a.data(), N * sizeof(float), cudaMemcpyHostToDevice), "upload");
+        BCK(cudaMemcpy(dc + o, c.data(), N * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    } else if (field == EFS_FIELD_BOUNDARY) {
+        std::vector<uint8_t> s8(N);
+        for (long long i = 0; i < N; i++) {
+            if (host[i] != 0.f && host[i] != 1.f) return bfail(b, EFS_ERR_ARG, "boundary values must be 0.0 or 1.0");
+            s8[i] = host[i] == 1.f ? 1 : 0;
+        }
+        BCK(cudaMemcpy(b->F.solid + o, s8.data(), N, cudaMemcpyHostToDevice), "upload");
+    } else {
+        BCK(cudaMemcpy(scalar_field(b, field) + o, host, N * sizeof(float), cudaMemcpyHostToDevice), "upload");
+    }
+    return EFS_OK;
+}
+
+int efs_batch_download_field(efs_batch* b, int scene, int field, float* host) {
+    if (!b) return EFS_ERR_ARG;
+    if (scene < 0 || scene >= b->n || !field_ok(field) || !host) return bfail(b, EFS_ERR_ARG, "bad scene, field or pointer");
+    const BScene& S = b->sc[scene];
+    const long long N = S.g.N, o = S.base;
+    const int st = check_status(b);
+    if (st != EFS_OK) return st;
+    if (field == EFS_FIELD_VEL || field == EFS_FIELD_FORCES) {
+        std::vector<float> a(N), c(N);
+        const float* da = field == EFS_FIELD_VEL ? b->F.u : b->F.fx;
+        const float* dc = field == EFS_FIELD_VEL ? b->F.v : b->F.fy;
+        BCK(cudaMemcpy(a.data(), da + o, N * sizeof(float), cudaMemcpyDeviceToHost), "download");
+        BCK(cudaMemcpy(c.data(), dc + o, N * sizeof(float), cudaMemcpyDeviceToHost), "download");
+        for (long long i = 0; i < N; i++) { host[2 * i] = a[i]; host[2 * i + 1] = c[i]; }
+    } else if (field == EFS_FIELD_BOUNDARY) {
+        std::vector<uint8_t> s8(N);
+        BCK(cudaMemcpy(s8.data(), b->F.solid + o, N, cudaMemcpyDeviceToHost), "download");
+        for (long long i = 0; i < N; i++) host[i] = s8[i] ? 1.f : 0.f;
+    } else {
+        BCK(cudaMemcpy(host, scalar_field(b, field) + o, N * sizeof(float), cudaMemcpyDeviceToHost), "download");
+    }
+    return EFS_OK;
+}
+
+int efs_batch_stage(efs_batch* b, int stage) {
+    if (!b) return EFS_ERR_ARG;
+    if (stage < 0 || stage >= EFS_STAGE_COUNT) return bfail(b, EFS_ERR_ARG, "unknown stage");
+    BCK(enqueue_stage(b, stage, false), "batch stage");
+    return EFS_OK;
+}
+
+int efs_batch_step(efs_batch* b, int n_steps) {
+    if (!b) return EFS_ERR_ARG;
+    if (n_steps < 0) return bfail(b, EFS_ERR_ARG, "n_steps < 0");
+    if (n_steps == 0) return EFS_OK;
+    const int s = build_graph(b);
+    if (s != EFS_OK) return s;
+    for (int k = 0; k < n_steps; k++) BCK(cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
+    b->frames += n_steps;
+    return EFS_OK;
+}
+
+int efs_batch_synchronize(efs_batch* b) {
+    if (!b) return EFS_ERR_ARG;
+    return check_status(b);
+}
+
+int efs_batch_stats(efs_batch* b, int scene, efs_stats* out) {
+    if (!b || !out) return EFS_ERR_ARG;
+    if (scene < 0 || scene >= b->n) return bfail(b, EFS_ERR_ARG, "bad scene");
+    const int st = check_status(b);
+    if (st != EFS_OK) return st;
+    DevCtl h, g;
+    BCK(cudaMemcpy(&h, b->F.sctl + scene, sizeof(DevCtl), cudaMemcpyDeviceToHost), "download stats");
+    BCK(cudaMemcpy(&g, b->F.ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost), "download stats");
+    std::memset(out, 0, sizeof(*out));
+    out->frames = b->frames;
+    out->solve_steps = h.iterations;
+    out->converged = h.converged;
+    out->paused = h.paused;
+    out->device_error = g.error;
+    out->rr = h.rr;
+    out->bb = h.bb;
+    out->threshold = h.thr;
+    out->active_cells = h.active_cells;
+    out->total_solve_steps = h.total_iterations;
+    out->solves = h.solves;
+    return EFS_OK;
+}
+
+int efs_batch_kernel_count(efs_batch* b, int* count) {
+    if (!b || !count) return EFS_ERR_ARG;
+    const int s = build_graph(b);
+    if (s != EFS_OK) return s;
+    *count = b->graph_kernels;
+    return EFS_OK;
+}
+
+int efs_batch_get_tuning(const efs_batch* b, efs_batch_tuning* t) {
+    if (!b || !t) return EFS_ERR_ARG;
+    t->tile_x = b->bx;
+    t->tile_y = b->by;
+    t->blocks_per_sm = b->bps;
+    t->solver_threads = b->cg_threads;
+    t->ms_per_step = 0.f;
+    return EFS_OK;
+}
+
+int efs_batch_set_tuning(efs_batch* b, const efs_batch_tuning* t) {
+    if (!b || !t) return EFS_ERR_ARG;
+    if (t->tile_x < 1 || t->tile_y < 1 || t->tile_x * t->tile_y > 1024 || (t->tile_x * t->tile_y) % 32 != 0 ||
+        t->blocks_per_sm < 1 || t->blocks_per_sm > 32 ||
+        (t->solver_threads != 128 && t->solver_threads != 256 && t->solver_threads != 512 && t->solver_threads != 1024))
+        return bfail(b, EFS_ERR_ARG, "tile_x * tile_y a multiple of 32 up to 1024; blocks_per_sm 1..32; solver_threads 128..1024 (power of 2)");
+    BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    b->bx = t->tile_x;
+    b->by = t->tile_y;
+    b->bps = t->blocks_per_sm;
+    b->cg_threads = t->solver_threads;
+    drop_graph(b);
+    return upload_tables(b);
+}
+
+// Coordinate search over the tile shape, the blocks per SM of the stage kernels and the solver's block size:
+// each candidate runs `trial_steps` timed steps from the same saved state (the state is restored after every
+// trial), and the fastest is kept.
+int efs_batch_autotune(efs_batch* b, int trial_steps, efs_batch_tuning* best_out) {
+    if (!b) return EFS_ERR_ARG;
+    if (trial_steps < 1) return bfail(b, EFS_ERR_ARG, "trial_steps >= 1");
+    BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    const long long T = b->total;
+    // save the state every step reads or writes across steps
+    struct Saved { void* dev; size_t bytes; std::vector<unsigned char> host; };
+    std::vector<Saved> sv = {{b->F.u, (size_t)T * 4, {}}, {b->F.v, (size_t)T * 4, {}}, {b->F.rho, (size_t)T * 4, {}},
+                             {b->F.gamma, (size_t)T * 4, {}}, {b->F.beta, (size_t)T * 4, {}}, {b->F.p, (size_t)T * 4, {}},
+                             {b->F.div, (size_t)T * 4, {}}, {b->F.sctl, (size_t)b->n * sizeof(DevCtl), {}}};
+    for (auto& x : sv) {
+        x.host.resize(x.bytes);
+        BCK(cudaMemcpy(x.host.data(), x.dev, x.bytes, cudaMemcpyDeviceToHost), "save state");
+    }
+    const int64_t frames0 = b->frames;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0), "cudaEventCreate");
+    BCK(cudaEventCreate(&e1), "cudaEventCreate");
+    auto restore = [&]() -> int {
+        for (auto& x : sv) BCK(cudaMemcpy(x.dev, x.host.data(), x.bytes, cudaMemcpyHostToDevice), "restore state");
+        b->frames = frames0;
+        return EFS_OK;
+    };
+    auto trial = [&](const efs_batch_tuning& t, float& ms) -> int {
+        int s = efs_batch_set_tuning(b, &t);
+        if (s != EFS_OK) return s;
+        if ((s = restore()) != EFS_OK) return s;
+        if ((s = efs_batch_step(b, 1)) != EFS_OK) return s;   // warm-up and graph build
+        BCK(cudaEventRecord(e0, b->stream), "cudaEventRecord");
+        if ((s = efs_batch_step(b, trial_steps)) != EFS_OK) return s;
+        BCK(cudaEventRecord(e1, b->stream), "cudaEventRecord");
+        BCK(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        BCK(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        ms /= trial_steps;
+        return check_status(b);
+    };
+    efs_batch_tuning best{b->bx, b->by, b->bps, b->cg_threads, 0.f};
+    float best_ms = FLT_MAX;
+    int s = trial(best, best_ms);
+    if (s != EFS_OK) return s;
+    const int tiles[][2] = {{32, 8}, {32, 4}, {64, 4}, {16, 8}, {32, 16}, {128, 2}};
+    for (const auto& tl : tiles) {
+        efs_batch_tuning c = best;
+        c.tile_x = tl[0];
+        c.tile_y = tl[1];
+        float ms;
+        if ((s = trial(c, ms)) != EFS_OK) return s;
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    for (int bps : {2, 4, 8, 16}) {
+        efs_batch_tuning c = best;
+        c.blocks_per_sm = bps;
+        float ms;
+        if ((s = trial(c, ms)) != EFS_OK) return s;
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    for (int th : {256, 512, 1024}) {
+        efs_batch_tuning c = best;
+        c.solver_threads = th;
+        float ms;
+        if ((s = trial(c, ms)) != EFS_OK) return s;
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if ((s = efs_batch_set_tuning(b, &best)) != EFS_OK) return s;
+    if ((s = restore()) != EFS_OK) return s;
+    best.ms_per_step = best_ms;
+    if (best_out) *best_out = best;
+    return EFS_OK;
+}
+
+}  // extern "C"

@@ -10,6 +10,7 @@
 //     over those weights with atomic adds for the scattered part.
 // Density sharpening applies every cell's change, then traces every changed cell on that field, then
 // scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell.
+#include "efs_batch.h"
 #include "efs_internal.h"
 
 namespace efs {
@@ -18,17 +19,17 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 
-__device__ __forceinline__ bool cell3(const Geo& g, int& x, int& y, int& z, int& i) {
-    x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    z = 1 + blockIdx.z;
+__device__ __forceinline__ bool cell3(const Geo& g, int bx, int by, int bz, int& x, int& y, int& z, int& i) {
+    x = 1 + bx * blockDim.x + threadIdx.x;
+    y = 1 + by * blockDim.y + threadIdx.y;
+    z = 1 + bz;
     if (x > g.W - 2 || y > g.H - 2) return false;
     i = z * g.WH + y * g.W + x;
     return true;
 }
-__device__ __forceinline__ bool cell2(const Geo& g, int& x, int& y, int& i) {
-    x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ bool cell2(const Geo& g, int bx, int by, int& x, int& y, int& i) {
+    x = 1 + bx * blockDim.x + threadIdx.x;
+    y = 1 + by * blockDim.y + threadIdx.y;
     if (x > g.W - 2 || y > g.H - 2) return false;
     i = y * g.W + x;
     return true;
@@ -38,36 +39,40 @@ __device__ __forceinline__ bool cell2(const Geo& g, int& x, int& y, int& i) {
 // stage 0: vel_decay (CPUSimulator3D.cpp:54-59, CPUSimulator2D.cpp:65-70)
 // ------------------------------------------------------------------------------------------------
 template <int DIM>
-__global__ void k_vel_decay(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                            const float* __restrict__ rho, float k) {
+__device__ __forceinline__ void d_vel_decay(const Geo& g, int bx, int by, int bz, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, const float* __restrict__ rho, float k) {
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if ((double)rho[i] < 0.5) {
         u[i] *= k; v[i] *= k;
         if (DIM == 3) w[i] *= k;
     }
 }
+template <int DIM>
+__global__ void k_vel_decay(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                            const float* __restrict__ rho, float k) {
+    d_vel_decay<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, rho, k);
+}
 
 // ------------------------------------------------------------------------------------------------
 // stage 1: vel_extrapolate (CPUSimulator3D.cpp:61-111, CPUSimulator2D.cpp:72-120)
 // ------------------------------------------------------------------------------------------------
-__global__ void k_extrap_init(Geo g, int dim, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
-                              uint8_t* __restrict__ valid) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void d_extrap_init(const Geo& g, int bx, int by, int bz, int dim, const float* __restrict__ rho, const uint8_t* __restrict__ solid, uint8_t* __restrict__ valid) {
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     const int x = i % g.W, y = (i / g.W) % g.H, z = i / g.WH;
     bool interior = x >= 1 && x <= g.W - 2 && y >= 1 && y <= g.H - 2;
     if (dim == 3) interior = interior && z >= 1 && z <= g.D - 2;
     valid[i] = (interior && rho[i] >= 0.5f && solid[i] == 0) ? 1 : 0;
 }
+__global__ void k_extrap_init(Geo g, int dim, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                              uint8_t* __restrict__ valid) {
+    d_extrap_init(g, blockIdx.x, blockIdx.y, blockIdx.z, dim, rho, solid, valid);
+}
 
 template <int DIM>
-__global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* __restrict__ sv,
-                              const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du,
-                              float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV,
-                              const uint8_t* __restrict__ solid) {
+__device__ __forceinline__ void d_extrap_pass(const Geo& g, int bx, int by, int bz, const float* __restrict__ su, const float* __restrict__ sv, const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du, float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV, const uint8_t* __restrict__ solid) {
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if (solid[i]) {
         du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
         dV[i] = 0;
@@ -96,17 +101,26 @@ __global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* 
     }
     dV[i] = (n > 0) ? 1 : 0;
 }
+template <int DIM>
+__global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* __restrict__ sv,
+                              const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du,
+                              float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV,
+                              const uint8_t* __restrict__ solid) {
+    d_extrap_pass<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, su, sv, sw, sV, du, dv, dw, dV, solid);
+}
 
 // ------------------------------------------------------------------------------------------------
 // stage 2: rho_sharpen (CPUSimulator3D.cpp:366-456 with trace_along_field :568-607 and scatter_values
 // :609-655; 2D CPUSimulator2D.cpp:320-402, :526-595)
 // ------------------------------------------------------------------------------------------------
 template <int DIM>
-__global__ void k_sharpen_calc(Geo g, const float* __restrict__ rho, float delT, int* __restrict__ idx,
-                               float* __restrict__ val, DevCtl* ctl, int cap) {
+// (batched scenes: the list holds packed cell indices i + ibase and, in sid, the scene of each entry)
+__device__ __forceinline__ void d_sharpen_calc(const Geo& g, int bx, int by, int bz, const float* __restrict__ rho,
+                                               float delT, int* __restrict__ idx, float* __restrict__ val, DevCtl* ctl,
+                                               int cap, int ibase = 0, int scene = 0, int* __restrict__ sid = nullptr) {
     int x, y, z = 0, i;
     bool ok;
-    if (DIM == 3) ok = cell3(g, x, y, z, i); else ok = cell2(g, x, y, i);
+    if (DIM == 3) ok = cell3(g, bx, by, bz, x, y, z, i); else ok = cell2(g, bx, by, x, y, i);
     float dr = 0.f;
     // Cells whose result is decided without the slope terms: rho < 1e-5 gives dr = -rho, and rho > 0.5 gives
     // dr = 0 (there the weight is >= 0, so rho + dr >= rho > 0 and the reference's second branch applies).
@@ -147,9 +161,18 @@ __global__ void k_sharpen_calc(Geo g, const float* __restrict__ rho, float delT,
     base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
     if (active) {
         const int slot = base + __popc(mask & ((1u << lane) - 1u));
-        if (slot < cap) { idx[slot] = i; val[slot] = dr; }
+        if (slot < cap) {
+            idx[slot] = i + ibase;
+            val[slot] = dr;
+            if (sid) sid[slot] = scene;
+        }
         else atomicOr(&ctl->error, DEV_ERR_LIST_OVERFLOW);
     }
+}
+template <int DIM>
+__global__ void k_sharpen_calc(Geo g, const float* __restrict__ rho, float delT, int* __restrict__ idx,
+                               float* __restrict__ val, DevCtl* ctl, int cap) {
+    d_sharpen_calc<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, rho, delT, idx, val, ctl, cap);
 }
 
 __global__ void k_sharpen_apply(float* __restrict__ rho, const int* __restrict__ idx, const float* __restrict__ val,
@@ -162,35 +185,88 @@ __global__ void k_sharpen_apply(float* __restrict__ rho, const int* __restrict__
     }
 }
 
+// Trace of one changed cell up the density gradient (trace_along_field, CPUSimulator3D.cpp:568-607).
+template <int DIM>
+__device__ __forceinline__ void sharpen_trace_one(const Geo& g, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                                                  int i, float Dist, float& px, float& py, float& pz) {
+    const float stepSize = Dist / (float)10;
+    px = (float)(i % g.W); py = (float)((i / g.W) % g.H); pz = (float)(i / g.WH);
+    for (int st = 0; st < 10; st++) {
+        const float sv = (DIM == 3) ? sinterp3(rho, g, px, py, pz) : sinterp2(rho, g, px, py);
+        if (sv >= 0.5f) break;
+        const int ix = clampi((int)px, 1, g.W - 2), iy = clampi((int)py, 1, g.H - 2);
+        const int iz = (DIM == 3) ? clampi((int)pz, 1, g.D - 2) : 0;
+        const int c = iz * g.WH + iy * g.W + ix;
+        const float gx = rho[c + 1] - rho[c - 1];
+        const float gy = rho[c + g.W] - rho[c - g.W];
+        const float gz = (DIM == 3) ? rho[c + g.WH] - rho[c - g.WH] : 0.f;
+        const float len = (DIM == 3) ? sqrtf(gx * gx + gy * gy + gz * gz) : sqrtf(gx * gx + gy * gy);
+        if (len < 1e-6f) break;
+        float nx = px + (gx / len) * stepSize, ny = py + (gy / len) * stepSize;
+        nx = clampf(nx, 1.f, (float)g.W - 2.f);
+        ny = clampf(ny, 1.f, (float)g.H - 2.f);
+        float nz = pz;
+        if (DIM == 3) { nz = pz + (gz / len) * stepSize; nz = clampf(nz, 1.f, (float)g.D - 2.f); }
+        const int ci = (DIM == 3 ? (int)nz * g.WH : 0) + (int)ny * g.W + (int)nx;
+        if (solid[ci]) break;
+        px = nx; py = ny; pz = nz;
+    }
+}
+
+// Trilinear scatter of `value` at (px, py, pz) onto the non-solid corners (scatter_values,
+// CPUSimulator3D.cpp:609-655).
+template <int DIM>
+__device__ __forceinline__ void sharpen_scatter_one(const Geo& g, float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                                                    float px, float py, float pz, float value) {
+    const int x0 = clampi((int)px, 0, g.W - 1), y0 = clampi((int)py, 0, g.H - 1);
+    const int x1 = clampi((int)px + 1, 0, g.W - 1), y1 = clampi((int)py + 1, 0, g.H - 1);
+    const float fx = px - (float)(int)px, fy = py - (float)(int)py;
+    if (DIM == 3) {
+        const int z0 = clampi((int)pz, 0, g.D - 1), z1 = clampi((int)pz + 1, 0, g.D - 1);
+        const float fz = pz - (float)(int)pz;
+        float w[8];
+        w[0] = (1.f - fx) * (1.f - fy) * (1.f - fz);
+        w[1] = fx * (1.f - fy) * (1.f - fz);
+        w[2] = (1.f - fx) * fy * (1.f - fz);
+        w[3] = fx * fy * (1.f - fz);
+        w[4] = (1.f - fx) * (1.f - fy) * fz;
+        w[5] = fx * (1.f - fy) * fz;
+        w[6] = (1.f - fx) * fy * fz;
+        w[7] = fx * fy * fz;
+        int c[8];
+        c[0] = z0 * g.WH + y0 * g.W + x0; c[1] = z0 * g.WH + y0 * g.W + x1;
+        c[2] = z0 * g.WH + y1 * g.W + x0; c[3] = z0 * g.WH + y1 * g.W + x1;
+        c[4] = z1 * g.WH + y0 * g.W + x0; c[5] = z1 * g.WH + y0 * g.W + x1;
+        c[6] = z1 * g.WH + y1 * g.W + x0; c[7] = z1 * g.WH + y1 * g.W + x1;
+#pragma unroll
+        for (int k = 0; k < 8; k++) if (solid[c[k]]) w[k] = 0.f;
+        const float total = w[0] + w[1] + w[2] + w[3] + w[4] + w[5] + w[6] + w[7];
+        if (total < 1e-6f) return;
+        const float inv = 1.f / total;
+#pragma unroll
+        for (int k = 0; k < 8; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+    } else {
+        float w[4];
+        w[0] = (1.f - fx) * (1.f - fy); w[1] = fx * (1.f - fy); w[2] = (1.f - fx) * fy; w[3] = fx * fy;
+        const int c[4] = {y0 * g.W + x0, y0 * g.W + x1, y1 * g.W + x0, y1 * g.W + x1};
+#pragma unroll
+        for (int k = 0; k < 4; k++) if (solid[c[k]]) w[k] = 0.f;
+        const float total = w[0] + w[1] + w[2] + w[3];
+        if (total < 1e-6f) return;
+        const float inv = 1.f / total;
+#pragma unroll
+        for (int k = 0; k < 4; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+    }
+}
+
 template <int DIM>
 __global__ void k_sharpen_trace(Geo g, const float* __restrict__ rho, const uint8_t* __restrict__ solid,
                                 const int* __restrict__ idx, float* __restrict__ ends, float Dist,
                                 const DevCtl* ctl, int cap) {
     const int n = min(ctl->sh_count, cap);
-    const float stepSize = Dist / (float)10;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-        const int i = idx[s];
-        float px = (float)(i % g.W), py = (float)((i / g.W) % g.H), pz = (float)(i / g.WH);
-        for (int st = 0; st < 10; st++) {
-            const float sv = (DIM == 3) ? sinterp3(rho, g, px, py, pz) : sinterp2(rho, g, px, py);
-            if (sv >= 0.5f) break;
-            const int ix = clampi((int)px, 1, g.W - 2), iy = clampi((int)py, 1, g.H - 2);
-            const int iz = (DIM == 3) ? clampi((int)pz, 1, g.D - 2) : 0;
-            const int c = iz * g.WH + iy * g.W + ix;
-            const float gx = rho[c + 1] - rho[c - 1];
-            const float gy = rho[c + g.W] - rho[c - g.W];
-            const float gz = (DIM == 3) ? rho[c + g.WH] - rho[c - g.WH] : 0.f;
-            const float len = (DIM == 3) ? sqrtf(gx * gx + gy * gy + gz * gz) : sqrtf(gx * gx + gy * gy);
-            if (len < 1e-6f) break;
-            float nx = px + (gx / len) * stepSize, ny = py + (gy / len) * stepSize;
-            nx = clampf(nx, 1.f, (float)g.W - 2.f);
-            ny = clampf(ny, 1.f, (float)g.H - 2.f);
-            float nz = pz;
-            if (DIM == 3) { nz = pz + (gz / len) * stepSize; nz = clampf(nz, 1.f, (float)g.D - 2.f); }
-            const int ci = (DIM == 3 ? (int)nz * g.WH : 0) + (int)ny * g.W + (int)nx;
-            if (solid[ci]) break;
-            px = nx; py = ny; pz = nz;
-        }
+        float px, py, pz;
+        sharpen_trace_one<DIM>(g, rho, solid, idx[s], Dist, px, py, pz);
         ends[3 * s] = px; ends[3 * s + 1] = py; ends[3 * s + 2] = pz;
     }
 }
@@ -200,49 +276,8 @@ __global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t*
                                   const float* __restrict__ val, const float* __restrict__ ends, const DevCtl* ctl,
                                   int cap) {
     const int n = min(ctl->sh_count, cap);
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-        const float px = ends[3 * s], py = ends[3 * s + 1], pz = ends[3 * s + 2];
-        const float value = -val[s];
-        const int x0 = clampi((int)px, 0, g.W - 1), y0 = clampi((int)py, 0, g.H - 1);
-        const int x1 = clampi((int)px + 1, 0, g.W - 1), y1 = clampi((int)py + 1, 0, g.H - 1);
-        const float fx = px - (float)(int)px, fy = py - (float)(int)py;
-        if (DIM == 3) {
-            const int z0 = clampi((int)pz, 0, g.D - 1), z1 = clampi((int)pz + 1, 0, g.D - 1);
-            const float fz = pz - (float)(int)pz;
-            float w[8];
-            w[0] = (1.f - fx) * (1.f - fy) * (1.f - fz);
-            w[1] = fx * (1.f - fy) * (1.f - fz);
-            w[2] = (1.f - fx) * fy * (1.f - fz);
-            w[3] = fx * fy * (1.f - fz);
-            w[4] = (1.f - fx) * (1.f - fy) * fz;
-            w[5] = fx * (1.f - fy) * fz;
-            w[6] = (1.f - fx) * fy * fz;
-            w[7] = fx * fy * fz;
-            int c[8];
-            c[0] = z0 * g.WH + y0 * g.W + x0; c[1] = z0 * g.WH + y0 * g.W + x1;
-            c[2] = z0 * g.WH + y1 * g.W + x0; c[3] = z0 * g.WH + y1 * g.W + x1;
-            c[4] = z1 * g.WH + y0 * g.W + x0; c[5] = z1 * g.WH + y0 * g.W + x1;
-            c[6] = z1 * g.WH + y1 * g.W + x0; c[7] = z1 * g.WH + y1 * g.W + x1;
-#pragma unroll
-            for (int k = 0; k < 8; k++) if (solid[c[k]]) w[k] = 0.f;
-            const float total = w[0] + w[1] + w[2] + w[3] + w[4] + w[5] + w[6] + w[7];
-            if (total < 1e-6f) continue;
-            const float inv = 1.f / total;
-#pragma unroll
-            for (int k = 0; k < 8; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
-        } else {
-            float w[4];
-            w[0] = (1.f - fx) * (1.f - fy); w[1] = fx * (1.f - fy); w[2] = (1.f - fx) * fy; w[3] = fx * fy;
-            const int c[4] = {y0 * g.W + x0, y0 * g.W + x1, y1 * g.W + x0, y1 * g.W + x1};
-#pragma unroll
-            for (int k = 0; k < 4; k++) if (solid[c[k]]) w[k] = 0.f;
-            const float total = w[0] + w[1] + w[2] + w[3];
-            if (total < 1e-6f) continue;
-            const float inv = 1.f / total;
-#pragma unroll
-            for (int k = 0; k < 4; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
-        }
-    }
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        sharpen_scatter_one<DIM>(g, rho, solid, ends[3 * s], ends[3 * s + 1], ends[3 * s + 2], -val[s]);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -252,13 +287,10 @@ __global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t*
 // Steps 1-4: back-trace (shared by steps 1 and 2, which trace the same point), gamma' at the trace end,
 // backward weights m_k / sum / gamma', column sums beta1.
 template <int DIM>
-__global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
-                               const float* __restrict__ w, const uint8_t* __restrict__ solid,
-                               const float* __restrict__ gamma, float dt, float* __restrict__ wb,
-                               int* __restrict__ bb, float* __restrict__ bsum) {
+__device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ gamma, float dt, float* __restrict__ wb, int* __restrict__ bb, float* __restrict__ bsum) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if (solid[i]) { bb[i] = -1; return; }     // step 1 skips solids; step 2 finds no free corner for them
     float px, py, pz = 0.f, gp;
     float m[K];
@@ -284,16 +316,20 @@ __global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* 
         atomicAdd(&bsum[c], val);
     }
 }
+template <int DIM>
+__global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                               const float* __restrict__ w, const uint8_t* __restrict__ solid,
+                               const float* __restrict__ gamma, float dt, float* __restrict__ wb,
+                               int* __restrict__ bb, float* __restrict__ bsum) {
+    d_adv_backward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, gamma, dt, wb, bb, bsum);
+}
 
 // Step 5: forward trace for beta_j < 1; forward weights (1 - beta_j) m_k / sum; their row sums into gsum.
 template <int DIM>
-__global__ void k_adv_forward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
-                              const float* __restrict__ w, const uint8_t* __restrict__ solid,
-                              const float* __restrict__ bsum, float dt, float* __restrict__ wf, int* __restrict__ fb,
-                              float* __restrict__ gsum) {
+__device__ __forceinline__ void d_adv_forward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ bsum, float dt, float* __restrict__ wf, int* __restrict__ fb, float* __restrict__ gsum) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, j;
-    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, j)) return; } else { if (!cell2(g, bx, by, x, y, j)) return; }
     const float beta = bsum[j];
     if (beta >= 1) { fb[j] = -1; return; }
     float px, py, pz = 0.f;
@@ -316,14 +352,20 @@ __global__ void k_adv_forward(Geo g, const float* __restrict__ u, const float* _
         atomicAdd(&gsum[base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k))], val);
     }
 }
+template <int DIM>
+__global__ void k_adv_forward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ w, const uint8_t* __restrict__ solid,
+                              const float* __restrict__ bsum, float dt, float* __restrict__ wf, int* __restrict__ fb,
+                              float* __restrict__ gsum) {
+    d_adv_forward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, bsum, dt, wf, fb, gsum);
+}
 
 // Steps 6-8 for the backward rows: gamma2 = row sum, A /= gamma2, column sums beta2 (into beta).
 template <int DIM>
-__global__ void k_adv_rows(Geo g, float* __restrict__ wb, const int* __restrict__ bb, float* __restrict__ gsum,
-                           float* __restrict__ beta) {
+__device__ __forceinline__ void d_adv_rows(const Geo& g, int bx, int by, int bz, float* __restrict__ wb, const int* __restrict__ bb, float* __restrict__ gsum, float* __restrict__ beta) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     const int base = bb[i];
     float vals[K];
     float local = 0;
@@ -342,14 +384,18 @@ __global__ void k_adv_rows(Geo g, float* __restrict__ wb, const int* __restrict_
         atomicAdd(&beta[base + (DIM == 3 ? corner_offset3(g, k) : corner_offset2(g, k))], val);
     }
 }
+template <int DIM>
+__global__ void k_adv_rows(Geo g, float* __restrict__ wb, const int* __restrict__ bb, float* __restrict__ gsum,
+                           float* __restrict__ beta) {
+    d_adv_rows<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, wb, bb, gsum, beta);
+}
 
 // Steps 7-8 for the forward entries: A /= gamma2 of their row, column sums into beta.
 template <int DIM>
-__global__ void k_adv_cols(Geo g, float* __restrict__ wf, const int* __restrict__ fb, const float* __restrict__ gsum,
-                           float* __restrict__ beta) {
+__device__ __forceinline__ void d_adv_cols(const Geo& g, int bx, int by, int bz, float* __restrict__ wf, const int* __restrict__ fb, const float* __restrict__ gsum, float* __restrict__ beta) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, j;
-    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, j)) return; } else { if (!cell2(g, bx, by, x, y, j)) return; }
     const int base = fb[j];
     if (base < 0) return;
     float local = 0;
@@ -363,15 +409,18 @@ __global__ void k_adv_cols(Geo g, float* __restrict__ wf, const int* __restrict_
     }
     atomicAdd(&beta[j], local);
 }
+template <int DIM>
+__global__ void k_adv_cols(Geo g, float* __restrict__ wf, const int* __restrict__ fb, const float* __restrict__ gsum,
+                           float* __restrict__ beta) {
+    d_adv_cols<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, wf, fb, gsum, beta);
+}
 
 // Steps 9-11 for the backward rows, every cell: A /= beta2 of the column, gamma3 = row sum, rho' = A rho.
 // Cells without a backward row (border, solids) get 0, which the forward pass then adds to.
 template <int DIM>
-__global__ void k_adv_apply_rows(Geo g, const float* __restrict__ wb, const int* __restrict__ bb,
-                                 const float* __restrict__ beta, const float* __restrict__ rho,
-                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+__device__ __forceinline__ void d_adv_apply_rows(const Geo& g, int bx, int by, int bz, const float* __restrict__ wb, const int* __restrict__ bb, const float* __restrict__ beta, const float* __restrict__ rho, float* __restrict__ gamma_out, float* __restrict__ rho_out) {
     constexpr int K = (DIM == 3) ? 8 : 4;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= g.N) return;
     const int x = i % g.W, y = (i / g.W) % g.H, z = i / g.WH;
     bool interior = x >= 1 && x <= g.W - 2 && y >= 1 && y <= g.H - 2;
@@ -392,15 +441,19 @@ __global__ void k_adv_apply_rows(Geo g, const float* __restrict__ wb, const int*
     gamma_out[i] = gs;
     rho_out[i] = rs;
 }
+template <int DIM>
+__global__ void k_adv_apply_rows(Geo g, const float* __restrict__ wb, const int* __restrict__ bb,
+                                 const float* __restrict__ beta, const float* __restrict__ rho,
+                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+    d_adv_apply_rows<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, wb, bb, beta, rho, gamma_out, rho_out);
+}
 
 // Steps 9-11 for the forward entries: A /= beta2_j, scattered into gamma3 and rho'.
 template <int DIM>
-__global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int* __restrict__ fb,
-                                 const float* __restrict__ beta, const float* __restrict__ rho,
-                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+__device__ __forceinline__ void d_adv_apply_cols(const Geo& g, int bx, int by, int bz, const float* __restrict__ wf, const int* __restrict__ fb, const float* __restrict__ beta, const float* __restrict__ rho, float* __restrict__ gamma_out, float* __restrict__ rho_out) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, j;
-    if (DIM == 3) { if (!cell3(g, x, y, z, j)) return; } else { if (!cell2(g, x, y, j)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, j)) return; } else { if (!cell2(g, bx, by, x, y, j)) return; }
     const int base = fb[j];
     if (base < 0) return;
     const float b2 = beta[j];
@@ -413,6 +466,12 @@ __global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int*
         atomicAdd(&gamma_out[c], val);
         atomicAdd(&rho_out[c], val * rj);
     }
+}
+template <int DIM>
+__global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int* __restrict__ fb,
+                                 const float* __restrict__ beta, const float* __restrict__ rho,
+                                 float* __restrict__ gamma_out, float* __restrict__ rho_out) {
+    d_adv_apply_cols<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, wf, fb, beta, rho, gamma_out, rho_out);
 }
 
 // Step 12: one in-place sweep of pairwise gamma-equalising transfers along one axis
@@ -447,19 +506,25 @@ __device__ __forceinline__ void diffuse_line(const float* __restrict__ rsrc, con
 }
 
 // X sweep: one thread per (y, z) line.
-__global__ void k_diffuse_x(Geo g, int dim, const float* rsrc, const float* gsrc, float* rdst, float* gdst,
-                            const uint8_t* __restrict__ solid) {
-    const int y = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = (dim == 3) ? 1 + blockIdx.y : 0;
+__device__ __forceinline__ void d_diffuse_x(const Geo& g, int bx, int by, int bz, int dim, const float* rsrc, const float* gsrc, float* rdst, float* gdst, const uint8_t* __restrict__ solid) {
+    const int y = 1 + bx * blockDim.x + threadIdx.x;
+    const int z = (dim == 3) ? 1 + by : 0;
     if (y > g.H - 2) return;
     diffuse_line(rsrc, gsrc, rdst, gdst, solid, z * g.WH + y * g.W, 1, g.W);
 }
+__global__ void k_diffuse_x(Geo g, int dim, const float* rsrc, const float* gsrc, float* rdst, float* gdst,
+                            const uint8_t* __restrict__ solid) {
+    d_diffuse_x(g, blockIdx.x, blockIdx.y, blockIdx.z, dim, rsrc, gsrc, rdst, gdst, solid);
+}
 // Y sweep: one thread per (x, z) line (consecutive threads = consecutive x: coalesced).
-__global__ void k_diffuse_y(Geo g, int dim, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
-    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = (dim == 3) ? 1 + blockIdx.y : 0;
+__device__ __forceinline__ void d_diffuse_y(const Geo& g, int bx, int by, int bz, int dim, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
+    const int x = 1 + bx * blockDim.x + threadIdx.x;
+    const int z = (dim == 3) ? 1 + by : 0;
     if (x > g.W - 2) return;
     diffuse_line(rho, gamma, rho, gamma, solid, z * g.WH + x, g.W, g.H);
+}
+__global__ void k_diffuse_y(Geo g, int dim, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
+    d_diffuse_y(g, blockIdx.x, blockIdx.y, blockIdx.z, dim, rho, gamma, solid);
 }
 // Z sweep: one thread per (x, y) line.
 __global__ void k_diffuse_z(Geo g, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
@@ -474,11 +539,9 @@ __global__ void k_diffuse_z(Geo g, float* rho, float* gamma, const uint8_t* __re
 // stage 5 add_force in the same pass.
 // ------------------------------------------------------------------------------------------------
 template <int DIM>
-__global__ void k_vadv_trace(Geo g, const float* __restrict__ u, const float* __restrict__ v,
-                             const float* __restrict__ w, const uint8_t* __restrict__ solid, float dt,
-                             float* __restrict__ tu, float* __restrict__ tv, float* __restrict__ tw) {
+__device__ __forceinline__ void d_vadv_trace(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, float dt, float* __restrict__ tu, float* __restrict__ tv, float* __restrict__ tw) {
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if (DIM == 3) {
         float px, py, pz, a, b, c;
         trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, -dt, 4, px, py, pz);
@@ -490,6 +553,12 @@ __global__ void k_vadv_trace(Geo g, const float* __restrict__ u, const float* __
         vinterp2(u, v, g, px - 0.5f, py - 0.5f, a, b);
         tu[i] = a; tv[i] = b;
     }
+}
+template <int DIM>
+__global__ void k_vadv_trace(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                             const float* __restrict__ w, const uint8_t* __restrict__ solid, float dt,
+                             float* __restrict__ tu, float* __restrict__ tv, float* __restrict__ tw) {
+    d_vadv_trace<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, dt, tu, tv, tw);
 }
 
 struct ForceArgs {
@@ -517,11 +586,9 @@ __device__ __forceinline__ void add_force_cell2(const ForceArgs& f, int i, bool 
 }
 
 template <int DIM>
-__global__ void k_vadv_average(Geo g, const float* __restrict__ tu, const float* __restrict__ tv,
-                               const float* __restrict__ tw, const uint8_t* __restrict__ solid, float* __restrict__ u,
-                               float* __restrict__ v, float* __restrict__ w, ForceArgs f) {
+__device__ __forceinline__ void d_vadv_average(const Geo& g, int bx, int by, int bz, const float* __restrict__ tu, const float* __restrict__ tv, const float* __restrict__ tw, const uint8_t* __restrict__ solid, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, ForceArgs f) {
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     const bool si = solid[i], sx = solid[i - 1], sy = solid[i - g.W];
     float a = (x == 1 || si || sx) ? tu[i] : 0.5f * (tu[i] + tu[i - 1]);
     float b = (y == 1 || si || sy) ? tv[i] : 0.5f * (tv[i] + tv[i - g.W]);
@@ -535,12 +602,17 @@ __global__ void k_vadv_average(Geo g, const float* __restrict__ tu, const float*
     }
     u[i] = a; v[i] = b;
 }
+template <int DIM>
+__global__ void k_vadv_average(Geo g, const float* __restrict__ tu, const float* __restrict__ tv,
+                               const float* __restrict__ tw, const uint8_t* __restrict__ solid, float* __restrict__ u,
+                               float* __restrict__ v, float* __restrict__ w, ForceArgs f) {
+    d_vadv_average<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, tu, tv, tw, solid, u, v, w, f);
+}
 
 template <int DIM>
-__global__ void k_add_force(Geo g, const uint8_t* __restrict__ solid, float* __restrict__ u, float* __restrict__ v,
-                            float* __restrict__ w, ForceArgs f) {
+__device__ __forceinline__ void d_add_force(const Geo& g, int bx, int by, int bz, const uint8_t* __restrict__ solid, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, ForceArgs f) {
     int x, y, z = 0, i;
-    if (DIM == 3) { if (!cell3(g, x, y, z, i)) return; } else { if (!cell2(g, x, y, i)) return; }
+    if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     float a = u[i], b = v[i];
     if (DIM == 3) {
         float c = w[i];
@@ -550,6 +622,11 @@ __global__ void k_add_force(Geo g, const uint8_t* __restrict__ solid, float* __r
         add_force_cell2(f, i, solid[i] != 0, solid[i - 1] != 0, solid[i - g.W] != 0, a, b);
     }
     u[i] = a; v[i] = b;
+}
+template <int DIM>
+__global__ void k_add_force(Geo g, const uint8_t* __restrict__ solid, float* __restrict__ u, float* __restrict__ v,
+                            float* __restrict__ w, ForceArgs f) {
+    d_add_force<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, solid, u, v, w, f);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -577,11 +654,8 @@ struct ProjectArgs {
 // Walls on every face, divergence with the density correction, initial pressure, matrix-row description and
 // active-chunk flags.  One thread per cell, 1D over the linear index (a warp is one aligned 32-cell chunk).
 template <int DIM>
-__global__ void k_project_pre(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                              const float* __restrict__ rho, const uint8_t* __restrict__ solid,
-                              float* __restrict__ div, float* __restrict__ p, uint16_t* __restrict__ rowinfo,
-                              uint8_t* __restrict__ chunk_flag, ProjectArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void d_project_pre(const Geo& g, int bx, int by, int bz, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, const float* __restrict__ rho, const uint8_t* __restrict__ solid, float* __restrict__ div, float* __restrict__ p, uint16_t* __restrict__ rowinfo, uint8_t* __restrict__ chunk_flag, ProjectArgs a) {
+    const int i = bx * blockDim.x + threadIdx.x;
     const bool in = i < g.N;
     bool active = false;
     if (in) {
@@ -645,20 +719,25 @@ __global__ void k_project_pre(Geo g, float* __restrict__ u, float* __restrict__ 
     const unsigned any = __ballot_sync(0xffffffffu, active);
     if ((threadIdx.x & 31) == 0 && (i >> 5) < ((g.N + 31) >> 5)) chunk_flag[i >> 5] = any ? 1 : 0;
 }
+template <int DIM>
+__global__ void k_project_pre(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                              const float* __restrict__ rho, const uint8_t* __restrict__ solid,
+                              float* __restrict__ div, float* __restrict__ p, uint16_t* __restrict__ rowinfo,
+                              uint8_t* __restrict__ chunk_flag, ProjectArgs a) {
+    d_project_pre<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, rho, solid, div, p, rowinfo, chunk_flag, a);
+}
 
 // v -= grad p on non-solid interior cells, then walls on every face; skipped (with PAUSED set) when the solve
 // did not converge (CPUSimulator3D.cpp:541-566).
 template <int DIM>
-__global__ void k_project_post(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                               const float* __restrict__ p, const uint8_t* __restrict__ solid, DevCtl* ctl,
-                               int do_walls) {
+__device__ __forceinline__ void d_project_post(const Geo& g, int bx, int by, int bz, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, const float* __restrict__ p, const uint8_t* __restrict__ solid, DevCtl* ctl, int do_walls) {
     if (!ctl->converged) {
-        if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->paused = 1;
+        if (bx == 0 && by == 0 && bz == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->paused = 1;
         return;
     }
-    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = (DIM == 3) ? 1 + blockIdx.z : 0;
+    const int x = 1 + bx * blockDim.x + threadIdx.x;
+    const int y = 1 + by * blockDim.y + threadIdx.y;
+    const int z = (DIM == 3) ? 1 + bz : 0;
     if (x > g.W - 1 || y > g.H - 1) return;
     const int i = z * g.WH + y * g.W + x;
     const bool si = solid[i];
@@ -685,6 +764,12 @@ __global__ void k_project_post(Geo g, float* __restrict__ u, float* __restrict__
     }
     u[i] = fu; v[i] = fv;
     if (DIM == 3) w[i] = fw;
+}
+template <int DIM>
+__global__ void k_project_post(Geo g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                               const float* __restrict__ p, const uint8_t* __restrict__ solid, DevCtl* ctl,
+                               int do_walls) {
+    d_project_post<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, p, solid, ctl, do_walls);
 }
 
 // ISolver::solve on the current divergence: matrix-row description, active-chunk flags and the solver's
@@ -729,7 +814,7 @@ __global__ void k_recalc_div2(Geo g, const float* __restrict__ u, const float* _
                               ProjectArgs a, const DevCtl* ctl) {
     if (!ctl->converged) return;
     int x, y, i;
-    if (!cell2(g, x, y, i)) return;
+    if (!cell2(g, blockIdx.x, blockIdx.y, x, y, i)) return;
     const float r = rho[i];
     if (r < a.thrL || solid[i]) return;
     float d = (u[i + 1] - u[i]) + (v[i + g.W] - v[i]);
@@ -951,6 +1036,267 @@ cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force) {
             return launch_project_post(c);
         }
         default: return cudaErrorInvalidValue;
+    }
+}
+
+// ================================================================================================
+// Batched 2D scenes (efs_batch.h): the per-block code of the kernels above, run by persistent launches that
+// walk a table of (scene, virtual block) entries, on each scene's geometry and packed field pointers.
+// ================================================================================================
+namespace {
+
+template <class F>
+__device__ __forceinline__ void for_entries(const BView& t, F f) {
+    for (int k = blockIdx.x; k < t.n; k += gridDim.x) {
+        const BEntry E = t.e[k];
+        f(t.sc[E.scene], E);
+    }
+}
+
+__global__ void kb_vel_decay(BView t, BFields F, float k) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_vel_decay<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.rho + o, k);
+    });
+}
+__global__ void kb_extrap_init(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_extrap_init(S.g, E.bx, 0, 0, 2, F.rho + o, F.solid + o, F.validA + o);
+    });
+}
+__global__ void kb_extrap_pass(BView t, BFields F, int odd) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        const float* su = (odd ? F.tu : F.u) + o;
+        const float* sv = (odd ? F.tv : F.v) + o;
+        float* du = (odd ? F.u : F.tu) + o;
+        float* dv = (odd ? F.v : F.tv) + o;
+        const uint8_t* sV = (odd ? F.validB : F.validA) + o;
+        uint8_t* dV = (odd ? F.validA : F.validB) + o;
+        d_extrap_pass<2>(S.g, E.bx, E.by, 0, su, sv, nullptr, sV, du, dv, nullptr, dV, F.solid + o);
+    });
+}
+__global__ void kb_sharpen_calc(BView t, BFields F, float delT) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        d_sharpen_calc<2>(S.g, E.bx, E.by, 0, F.rho + S.base, delT, F.sh_idx, F.sh_val, F.ctl, F.list_cap, (int)S.base,
+                          E.scene, F.sh_sid);
+    });
+}
+__global__ void kb_sharpen_apply(BFields F) {
+    const int n = min(F.ctl->sh_count, F.list_cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int i = F.sh_idx[s];
+        F.rho[i] = maxf(F.rho[i] + F.sh_val[s], 0.f);
+    }
+}
+__global__ void kb_sharpen_trace(BFields F, const BScene* __restrict__ sc, float Dist) {
+    const int n = min(F.ctl->sh_count, F.list_cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const BScene S = sc[F.sh_sid[s]];
+        float px, py, pz;
+        sharpen_trace_one<2>(S.g, F.rho + S.base, F.solid + S.base, F.sh_idx[s] - (int)S.base, Dist, px, py, pz);
+        F.sh_end[3 * s] = px; F.sh_end[3 * s + 1] = py; F.sh_end[3 * s + 2] = pz;
+    }
+}
+__global__ void kb_sharpen_scatter(BFields F, const BScene* __restrict__ sc) {
+    const int n = min(F.ctl->sh_count, F.list_cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const BScene S = sc[F.sh_sid[s]];
+        sharpen_scatter_one<2>(S.g, F.rho + S.base, F.solid + S.base, F.sh_end[3 * s], F.sh_end[3 * s + 1],
+                               F.sh_end[3 * s + 2], -F.sh_val[s]);
+    }
+}
+__global__ void kb_adv_backward(BView t, BFields F, float dt) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_backward<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.solid + o, F.gamma + o, dt, F.wb + 4 * o,
+                          F.bb + o, F.bsum + o);
+    });
+}
+__global__ void kb_adv_forward(BView t, BFields F, float dt) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_forward<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.solid + o, F.bsum + o, dt, F.wf + 4 * o,
+                         F.fb + o, F.gsum + o);
+    });
+}
+__global__ void kb_adv_rows(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_rows<2>(S.g, E.bx, E.by, 0, F.wb + 4 * o, F.bb + o, F.gsum + o, F.beta + o);
+    });
+}
+__global__ void kb_adv_cols(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_cols<2>(S.g, E.bx, E.by, 0, F.wf + 4 * o, F.fb + o, F.gsum + o, F.beta + o);
+    });
+}
+__global__ void kb_adv_apply_rows(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_apply_rows<2>(S.g, E.bx, 0, 0, F.wb + 4 * o, F.bb + o, F.beta + o, F.rho + o, F.gamma + o, F.rho_acc + o);
+    });
+}
+__global__ void kb_adv_apply_cols(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_adv_apply_cols<2>(S.g, E.bx, E.by, 0, F.wf + 4 * o, F.fb + o, F.beta + o, F.rho + o, F.gamma + o, F.rho_acc + o);
+    });
+}
+__global__ void kb_diffuse_x(BView t, BFields F, int first) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_diffuse_x(S.g, E.bx, 0, 0, 2, (first ? F.rho_acc : F.rho) + o, F.gamma + o, F.rho + o, F.gamma + o, F.solid + o);
+    });
+}
+__global__ void kb_diffuse_y(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_diffuse_y(S.g, E.bx, 0, 0, 2, F.rho + o, F.gamma + o, F.solid + o);
+    });
+}
+__global__ void kb_vadv_trace(BView t, BFields F, float dt) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_vadv_trace<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.solid + o, dt, F.tu + o, F.tv + o, nullptr);
+    });
+}
+__global__ void kb_vadv_average(BView t, BFields F, ForceArgs f0) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        ForceArgs f = f0;
+        f.gforce = S.gforce;
+        f.fx = F.fx + o;
+        f.fy = F.fy + o;
+        d_vadv_average<2>(S.g, E.bx, E.by, 0, F.tu + o, F.tv + o, nullptr, F.solid + o, F.u + o, F.v + o, nullptr, f);
+    });
+}
+__global__ void kb_add_force(BView t, BFields F, ForceArgs f0) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        ForceArgs f = f0;
+        f.gforce = S.gforce;
+        f.fx = F.fx + o;
+        f.fy = F.fy + o;
+        d_add_force<2>(S.g, E.bx, E.by, 0, F.solid + o, F.u + o, F.v + o, nullptr, f);
+    });
+}
+__global__ void kb_project_pre(BView t, BFields F, ProjectArgs a) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_project_pre<2>(S.g, E.bx, 0, 0, F.u + o, F.v + o, nullptr, F.rho + o, F.solid + o, F.div + o, F.p + o,
+                         F.rowinfo + o, F.chunk_flag + (o >> 5), a);
+    });
+}
+__global__ void kb_project_post(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        d_project_post<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.p + o, F.solid + o, F.sctl + E.scene, 1);
+    });
+}
+
+inline unsigned bgrid(const BView& t, int grid) { return (unsigned)std::max(1, std::min(t.n, grid)); }
+
+}  // namespace
+
+cudaError_t batch_project_pre(const BLaunch& L) {
+    ProjectArgs a;
+    a.thrL = L.thrL; a.lp = L.lp; a.lm = L.lm; a.eta = L.eta; a.jacobi = 0;
+    kb_project_pre<<<bgrid(L.linear, L.grid), 256, 0, L.stream>>>(L.linear, L.F, a);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t batch_project_post(const BLaunch& L) {
+    kb_project_post<<<bgrid(L.post, L.grid), dim3(L.bx_dim, L.by_dim), 0, L.stream>>>(L.post, L.F);
+    EFS_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+// One stage (0-5) of every scene; the project stage is batch_project_pre + the solve + batch_project_post.
+cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force) {
+    const dim3 blk(L.bx_dim, L.by_dim);
+    const unsigned gi = bgrid(L.interior, L.grid);
+    cudaStream_t st = L.stream;
+    const BFields& F = L.F;
+    switch (stage) {
+        case EFS_STAGE_VEL_DECAY:
+            kb_vel_decay<<<gi, blk, 0, st>>>(L.interior, F, L.vel_decay);
+            EFS_LAUNCH_CHECK();
+            return cudaSuccess;
+        case EFS_STAGE_VEL_EXTRAPOLATE:
+            kb_extrap_init<<<bgrid(L.linear, L.grid), 256, 0, st>>>(L.linear, F);
+            EFS_LAUNCH_CHECK();
+            for (int it = 0; it < 6; it++) {
+                kb_extrap_pass<<<gi, blk, 0, st>>>(L.interior, F, it & 1);
+                EFS_LAUNCH_CHECK();
+            }
+            return cudaSuccess;
+        case EFS_STAGE_RHO_SHARPEN: {
+            cudaError_t e = cudaMemsetAsync(&F.ctl->sh_count, 0, sizeof(int), st);
+            if (e != cudaSuccess) return e;
+            kb_sharpen_calc<<<gi, blk, 0, st>>>(L.interior, F, L.dt * 3);
+            EFS_LAUNCH_CHECK();
+            kb_sharpen_apply<<<L.list_grid, 256, 0, st>>>(F);
+            EFS_LAUNCH_CHECK();
+            kb_sharpen_trace<<<L.list_grid, 256, 0, st>>>(F, L.interior.sc, L.rho_d);
+            EFS_LAUNCH_CHECK();
+            kb_sharpen_scatter<<<L.list_grid, 256, 0, st>>>(F, L.interior.sc);
+            EFS_LAUNCH_CHECK();
+            return cudaSuccess;
+        }
+        case EFS_STAGE_RHO_ADVECT: {
+            const size_t bytes = (size_t)L.total_cells * sizeof(float);
+            cudaError_t e;
+            if ((e = cudaMemsetAsync(F.bsum, 0, bytes, st)) != cudaSuccess) return e;
+            if ((e = cudaMemsetAsync(F.gsum, 0, bytes, st)) != cudaSuccess) return e;
+            kb_adv_backward<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
+            EFS_LAUNCH_CHECK();
+            kb_adv_forward<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
+            EFS_LAUNCH_CHECK();
+            if ((e = cudaMemsetAsync(F.beta, 0, bytes, st)) != cudaSuccess) return e;
+            kb_adv_rows<<<gi, blk, 0, st>>>(L.interior, F);
+            EFS_LAUNCH_CHECK();
+            kb_adv_cols<<<gi, blk, 0, st>>>(L.interior, F);
+            EFS_LAUNCH_CHECK();
+            kb_adv_apply_rows<<<bgrid(L.linear, L.grid), 256, 0, st>>>(L.linear, F);
+            EFS_LAUNCH_CHECK();
+            kb_adv_apply_cols<<<gi, blk, 0, st>>>(L.interior, F);
+            EFS_LAUNCH_CHECK();
+            for (int it = 0; it < 7; it++) {
+                kb_diffuse_x<<<bgrid(L.dx, L.grid), 128, 0, st>>>(L.dx, F, it == 0 ? 1 : 0);
+                EFS_LAUNCH_CHECK();
+                kb_diffuse_y<<<bgrid(L.dy, L.grid), 128, 0, st>>>(L.dy, F);
+                EFS_LAUNCH_CHECK();
+            }
+            return cudaSuccess;
+        }
+        case EFS_STAGE_VEL_ADVECT: {
+            ForceArgs f{};
+            f.enabled = fuse_add_force ? 1 : 0;
+            f.has_forces = 1;
+            f.gravity = L.gravity;
+            f.dt = L.dt;
+            kb_vadv_trace<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
+            EFS_LAUNCH_CHECK();
+            kb_vadv_average<<<gi, blk, 0, st>>>(L.interior, F, f);
+            EFS_LAUNCH_CHECK();
+            return cudaSuccess;
+        }
+        case EFS_STAGE_ADD_FORCE: {
+            ForceArgs f{};
+            f.enabled = 1;
+            f.has_forces = 1;
+            f.gravity = L.gravity;
+            f.dt = L.dt;
+            kb_add_force<<<gi, blk, 0, st>>>(L.interior, F, f);
+            EFS_LAUNCH_CHECK();
+            return cudaSuccess;
+        }
+        default:
+            return cudaErrorInvalidValue;
     }
 }
 

@@ -259,6 +259,96 @@ class GB300Simulator2D(_GB300Simulator):
         super().__init__(2, width, height, 1, params)
 
 
+class GB300Batch2D:
+    """Many independent 2D scenes of uneven sizes advanced together (efs_batch_*): scene s is a
+    ``widths[s] x heights[s]`` grid (border included); all share ``params`` except the optional per-scene
+    ``gravity`` (GRAVITY_FORCE in cells/s^2)."""
+
+    def __init__(self, widths, heights, params, gravity=None):
+        self.widths = [int(w) for w in widths]
+        self.heights = [int(h) for h in heights]
+        n = len(self.widths)
+        W = (ctypes.c_int * n)(*self.widths)
+        H = (ctypes.c_int * n)(*self.heights)
+        g = None if gravity is None else np.ascontiguousarray(gravity, np.float32)
+        self._params = params.copy()
+        h = ctypes.c_void_p()
+        L = lib()
+        st = L.efs_batch_create(n, W, H, ctypes.byref(self._params), fptr(g), ctypes.byref(h))
+        if st != 0:
+            raise EfsError(st, L.efs_batch_last_error(None).decode())
+        self._h = h
+
+    def _check(self, st):
+        if st != 0:
+            raise EfsError(st, lib().efs_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().efs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def n(self):
+        return len(self.widths)
+
+    def _shape(self, s, f):
+        shp = (self.heights[s], self.widths[s])
+        return shp + (2,) if f in abi.VECTOR_FIELDS else shp
+
+    def set_field(self, s, f, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        if a.size != int(np.prod(self._shape(s, f))):
+            raise ValueError(f"scene {s} {abi.FIELD_NAMES[f]}: expected {self._shape(s, f)}, got {a.shape}")
+        self._check(lib().efs_batch_upload_field(self._h, s, f, fptr(a)))
+
+    def field(self, s, f):
+        out = np.empty(self._shape(s, f), np.float32)
+        self._check(lib().efs_batch_download_field(self._h, s, f, fptr(out)))
+        return out
+
+    def stage(self, st):
+        self._check(lib().efs_batch_stage(self._h, st))
+
+    def update(self, n=1):
+        self._check(lib().efs_batch_step(self._h, n))
+
+    def synchronize(self):
+        self._check(lib().efs_batch_synchronize(self._h))
+
+    def stats(self, s):
+        out = abi.EfsStats()
+        self._check(lib().efs_batch_stats(self._h, s, ctypes.byref(out)))
+        return out
+
+    def kernels_per_step(self):
+        n = ctypes.c_int()
+        self._check(lib().efs_batch_kernel_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def tuning(self):
+        t = abi.EfsBatchTuning()
+        self._check(lib().efs_batch_get_tuning(self._h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, t):
+        self._check(lib().efs_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, trial_steps=3):
+        t = abi.EfsBatchTuning()
+        self._check(lib().efs_batch_autotune(self._h, trial_steps, ctypes.byref(t)))
+        return t
+
+
 def unet_param_count():
     n = ctypes.c_int64()
     check(lib().efs_unet_param_count(ctypes.byref(n)))

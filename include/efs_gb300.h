@@ -274,6 +274,43 @@ int  efs_unet_sample_count(efs_ctx* ctx, int* count);
 int  efs_unet_train(efs_ctx* ctx, int loss_kind, int iterations, int batch, float lr, float synthetic, uint64_t seed,
                     float* last_loss);
 
+/* ---- many independent 2D scenes of uneven sizes, advanced together ----
+ * No counterpart in the reference (each reference simulator owns one grid).  Every scene is a full 2D
+ * simulation (CPUSimulator2D stages, CGSolverCPU2D pressure solve with EFS_CG_MIXED_RECURRENCE) on its own
+ * grid (W x H, border included); all scenes share `params` except GRAVITY_FORCE, which may be given per
+ * scene (cells/s^2 for that scene's cell size).  One step of all scenes is one CUDA graph in which every
+ * stage kernel is a single persistent launch over a table of (scene, block) entries, and the pressure solves
+ * are a single launch whose blocks each solve whole scenes, largest first.  Fields use the single-context
+ * layouts (vel and forces: interleaved vec2).  A new batch holds the Grid2D constructor state: zero fields,
+ * gamma = 1, solid border. */
+typedef struct efs_batch efs_batch;
+typedef struct efs_batch_tuning {
+    int   tile_x, tile_y;     /* stage-kernel block: tile_x x tile_y cells (product a multiple of 32)   */
+    int   blocks_per_sm;      /* persistent blocks per SM of the stage kernels                          */
+    int   solver_threads;     /* threads of a solver block (128, 256, 512 or 1024)                      */
+    float ms_per_step;        /* efs_batch_autotune: measured step time of the chosen configuration     */
+} efs_batch_tuning;
+int  efs_batch_create(int n_scenes, const int* widths, const int* heights, const efs_params* params,
+                      const float* gravity_force, efs_batch** out);
+void efs_batch_destroy(efs_batch* batch);
+/* NULL: the error of the last failed efs_batch_create. */
+const char* efs_batch_last_error(const efs_batch* batch);
+int  efs_batch_scene_count(const efs_batch* batch, int* n);
+int  efs_batch_upload_field(efs_batch* batch, int scene, int field, const float* host);
+int  efs_batch_download_field(efs_batch* batch, int scene, int field, float* host);
+/* One stage of every scene (direct launches). */
+int  efs_batch_stage(efs_batch* batch, int stage);
+/* n_steps whole steps of every scene (graph replays; asynchronous). */
+int  efs_batch_step(efs_batch* batch, int n_steps);
+int  efs_batch_synchronize(efs_batch* batch);
+int  efs_batch_stats(efs_batch* batch, int scene, efs_stats* out);
+int  efs_batch_kernel_count(efs_batch* batch, int* count);
+int  efs_batch_get_tuning(const efs_batch* batch, efs_batch_tuning* tuning);
+int  efs_batch_set_tuning(efs_batch* batch, const efs_batch_tuning* tuning);
+/* Times trial steps of candidate tile shapes, blocks per SM and solver block sizes from the current state
+ * (restored after every trial) and keeps the fastest; `best` (may be NULL) receives it. */
+int  efs_batch_autotune(efs_batch* batch, int trial_steps, efs_batch_tuning* best);
+
 /* ---- host-only helpers (no device needed) ---- */
 /* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */
 int  efs_scene_dam3d(int w, int h, int d, int n_spheres_min, int n_spheres_max, uint64_t seed,

@@ -1,0 +1,126 @@
+"""Batched uneven 2D scenes (efs_batch_*) against the single-scene path and the oracle.
+
+- every stage of every scene, from the same state, against a single context running that scene: bit-exact
+  for the per-cell stages; rho_sharpen / rho_advect within 1e-6 (float atomics); the pressure within 1e-5
+  (the batch solves each scene with a block-level CG whose sums run in another order) and velocity after
+  projection within 1e-5;
+- one full step of each scene against the oracle within the single-context step tolerances;
+- a step is the same number of kernel launches whatever the number of scenes (one persistent launch per
+  stage kernel for all scenes), the autotuner returns a valid configuration, and stepping after it keeps
+  every scene converging with its liquid mass within 1e-5.
+"""
+import numpy as np
+import pytest
+
+from eulerianfluidsimulation_gb300 import abi
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+gb = pytest.importorskip("eulerianfluidsimulation_gb300")
+from oracle import oracle  # noqa: E402
+
+FIELDS = (abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA, abi.FIELD_DIVERGENCE, abi.FIELD_PRESSURE)
+
+
+def _scenes(seeds):
+    out = []
+    for sd in seeds:
+        b, r = gb.scene_batch2d(sd)
+        out.append((b, r))
+    return out
+
+
+def _params(side):
+    p = abi.params_dam(1.0 / side, 0.005, abi.SOLVER_CG, 1e-6)
+    p.max_steps = 20000
+    p.disable_mask = 0
+    return p
+
+
+def _batch(scenes):
+    sides = [b.shape[0] for b, _ in scenes]
+    prm = _params(sides[0])
+    grav = np.array([9.81 * s for s in sides], np.float32)
+    B = gb.GB300Batch2D(sides, sides, prm, grav)
+    for s, (b, r) in enumerate(scenes):
+        B.set_field(s, abi.FIELD_BOUNDARY, b)
+        B.set_field(s, abi.FIELD_RHO, r)
+    return B
+
+
+def _state(B, s):
+    st = {f: B.field(s, f) for f in FIELDS}
+    st[abi.FIELD_BOUNDARY] = B.field(s, abi.FIELD_BOUNDARY)
+    return st
+
+
+def test_every_stage_matches_the_single_context():
+    scenes = _scenes([0, 1, 2, 5])
+    with _batch(scenes) as B:
+        B.update(4)
+        B.synchronize()
+        singles = []
+        for s in range(B.n):
+            side = B.widths[s]
+            S = gb.GB300Simulator2D(side, side, _params(side))
+            S.set_fields(_state(B, s))
+            singles.append(S)
+        try:
+            for stage in range(abi.STAGE_COUNT):
+                B.stage(stage)
+                for s, S in enumerate(singles):
+                    S.stage(stage)
+                for s, S in enumerate(singles):
+                    for f in FIELDS:
+                        got, want = B.field(s, f), S.field(f)
+                        what = f"stage {abi.STAGE_NAMES[stage]} scene {s} field {abi.FIELD_NAMES[f]}"
+                        if stage == abi.STAGE_PROJECT and f in (abi.FIELD_PRESSURE, abi.FIELD_VEL):
+                            assert rel_l2(got, want) <= 1e-5, (what, rel_l2(got, want))
+                        elif stage in (abi.STAGE_RHO_SHARPEN, abi.STAGE_RHO_ADVECT) and f in (abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA):
+                            assert rel_l2(got, want) <= 1e-6, (what, rel_l2(got, want))
+                        else:
+                            assert np.array_equal(got, want), (what, int(np.sum(got != want)))
+                    # continue from identical states
+                    S.set_fields(_state(B, s))
+        finally:
+            for S in singles:
+                S.close()
+
+
+def test_one_step_of_each_scene_matches_the_oracle():
+    scenes = _scenes([3, 4, 6])
+    with _batch(scenes) as B:
+        B.update(1)
+        B.synchronize()
+        for s, (b, r) in enumerate(scenes):
+            side = b.shape[0]
+            o = oracle.Oracle(2, side, side, 1, _params(side), mode=oracle.SHARPEN_PARALLEL | oracle.DOTS_FP64)
+            o.set_field(abi.FIELD_BOUNDARY, b)
+            o.set_field(abi.FIELD_RHO, r)
+            o.step(1)
+            for f in (abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_PRESSURE):
+                assert rel_l2(B.field(s, f), o.field(f)) <= 1e-5, (s, abi.FIELD_NAMES[f])
+            st = B.stats(s)
+            assert st.converged and st.solves == 1
+
+
+def test_one_launch_per_stage_kernel_whatever_the_scene_count():
+    with _batch(_scenes([0, 1])) as A, _batch(_scenes(list(range(10)))) as B:
+        assert A.kernels_per_step() == B.kernels_per_step()
+
+
+def test_autotune_and_mass():
+    scenes = _scenes(list(range(8)))
+    with _batch(scenes) as B:
+        t = B.autotune(2)
+        assert t.ms_per_step > 0 and t.tile_x * t.tile_y % 32 == 0
+        assert B.tuning().tile_x == t.tile_x and B.tuning().solver_threads == t.solver_threads
+        m0 = [float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64)) for s in range(B.n)]
+        B.update(20)
+        B.synchronize()
+        for s in range(B.n):
+            st = B.stats(s)
+            assert st.converged and not st.paused
+            m = float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64))
+            assert abs(m - m0[s]) <= 1e-5 * m0[s], (s, m, m0[s])
