@@ -62,6 +62,9 @@ def parse():
                     help="instead of the throughput line: the precision study (every field against an FP64 "
                          "pressure solve of the same right-hand side) at --size for --steps steps")
     ap.add_argument("--study-out", default=None, help="precision study: also write the per-step records here (JSON)")
+    ap.add_argument("--workload", default="dam3d", choices=["dam3d", "batch2d"],
+                    help="batch2d: 64 independent 2D scenes of uneven sizes advanced together (efs_batch_*)")
+    ap.add_argument("--scenes", type=int, default=64)
     return ap.parse_args()
 
 
@@ -416,6 +419,93 @@ def run_fcg(a):
     print(json.dumps(line), flush=True)
 
 
+def run_batch2d(a):
+    """Many uneven 2D scenes advanced together: sides from {64, 96, 128, 192, 256}, 1-4 rectangles, 1-3 fluid
+    circles (seeded, efs_scene.h), dx = 1/side, gravity 9.81/dx, CG to rel-res 1e-6.  Autotuned first (outside
+    the timed region); the same scenes as separate single-scene simulators on their own streams are timed
+    beside it."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    scenes = [gb.scene_batch2d(a.seed + k) for k in range(a.scenes)]
+    sides = [b.shape[0] for b, _ in scenes]
+    dt = 0.005
+    prm = abi.params_dam(1.0 / sides[0], dt, abi.SOLVER_CG, 1e-6)
+    prm.max_steps = 20000
+    grav = np.array([9.81 * s for s in sides], np.float32)
+    B = gb.GB300Batch2D(sides, sides, prm, grav)
+    for k, (b, r) in enumerate(scenes):
+        B.set_field(k, abi.FIELD_BOUNDARY, b)
+        B.set_field(k, abi.FIELD_RHO, r)
+    for _ in range(a.warmup):
+        B.update(1)
+    B.synchronize()
+    tune = B.autotune(3)
+    st0 = [B.stats(k) for k in range(B.n)]
+    with Clocks(local) as clk:
+        ms = B.time_steps(a.steps)
+    clocks = clk.summary()
+    st1 = [B.stats(k) for k in range(B.n)]
+    kernels = B.kernels_per_step()
+    iters = [(st1[k].total_solve_steps - st0[k].total_solve_steps) / a.steps for k in range(B.n)]
+    rows = [st1[k].active_cells for k in range(B.n)]
+    conv = all(st1[k].converged for k in range(B.n))
+    B.close()
+    interior = sum((s - 2) ** 2 for s in sides)
+    # algorithmic bytes: 618 B per interior cell for the 2D stages, 40 B per matrix row and CG iteration + 30 B
+    # per row per solve
+    step_bytes = 618.0 * interior + sum(40.0 * rows[k] * iters[k] + 30.0 * rows[k] for k in range(len(sides)))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = step_bytes / (ms / a.steps / 1e3) / 1e9
+    # the same scenes as separate simulators, one stream each
+    sims = []
+    for k, (b, r) in enumerate(scenes):
+        p = abi.params_dam(1.0 / sides[k], dt, abi.SOLVER_CG, 1e-6)
+        p.max_steps = 20000
+        S = gb.GB300Simulator2D(sides[k], sides[k], p)
+        S.set_field(abi.FIELD_BOUNDARY, b)
+        S.set_field(abi.FIELD_RHO, r)
+        sims.append(S)
+    for S in sims:
+        S.update(a.warmup)
+    for S in sims:
+        S.synchronize()
+    k_sep = max(3, a.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(k_sep):
+        for S in sims:
+            S.update(1)
+    for S in sims:
+        S.synchronize()
+    sep_ms = (time.perf_counter() - t0) * 1e3 / k_sep
+    for S in sims:
+        S.close()
+    line = {"metric": f"scene-steps/s, {a.scenes} uneven 2D scenes (sides 64-256) to rel-res 1e-6",
+            "value": a.scenes * a.steps / (ms / 1e3), "unit": "scene-steps/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch2d", "scenes": a.scenes, "seeds": [a.seed, a.seed + a.scenes - 1],
+                       "sides": {str(s): sides.count(s) for s in sorted(set(sides))}, "dt": dt,
+                       "solver": "cg rel-res 1e-6 (block-level, one scene per block)", "l2": "working set below L2"},
+            "cell_updates_per_s": interior * a.steps / (ms / 1e3), "cg_iters_per_scene_step": float(np.mean(iters)),
+            "cg_iters_max": float(np.max(iters)), "all_converged": conv, "gpu_launches": kernels * a.steps,
+            "kernels_per_step": kernels, "tuning": tune.as_dict(),
+            "separate_simulators": {"ms_per_step_all_scenes": sep_ms, "host_timed": True,
+                                    "note": "one GB300Simulator2D per scene, each on its own stream"},
+            "roofline": {"kernel": "whole batched step", "bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "algorithmic_bytes_per_step": step_bytes},
+            "clocks": clocks, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_precision_study(a):
     """One JSON line with the maxima of the per-step errors (the 3D dam break with --spheres spheres)."""
     from eulerianfluidsimulation_gb300.precision import precision_study
@@ -434,6 +524,9 @@ def main():
     a = parse()
     if a.study == "precision":
         run_precision_study(a)
+        return
+    if a.workload == "batch2d":
+        run_batch2d(a)
         return
     if a.impl == "reference":
         run_reference(a)

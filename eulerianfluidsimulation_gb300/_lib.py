@@ -41,6 +41,7 @@ SIGNATURES = {
     "efs_batch_stage": (ctypes.c_int, [_CTX, ctypes.c_int]),
     "efs_batch_step": (ctypes.c_int, [_CTX, ctypes.c_int]),
     "efs_batch_synchronize": (ctypes.c_int, [_CTX]),
+    "efs_batch_time_steps": (ctypes.c_int, [_CTX, ctypes.c_int, _FP]),
     "efs_batch_stats": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.POINTER(EfsStats)]),
     "efs_batch_kernel_count": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int)]),
     "efs_batch_get_tuning": (ctypes.c_int, [_CTX, ctypes.POINTER(EfsBatchTuning)]),

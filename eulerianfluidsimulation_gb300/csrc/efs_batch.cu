@@ -210,12 +210,14 @@ __global__ void k_batch_cg(BCGArgs A) {
                 }
                 double dt, tt, u3;
                 block_reduce3(dtp, ttp, BSum(), dt, tt, u3);
+                if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown (singular block): not converged
                 const double ad = rr / dt;
                 const float alpha = (float)ad;
                 const double old = rr;
+                const double est = ad * ad * tt - rr;            // r'.r' from the CG recurrence
                 bool replaced = false;
-                if (it & 0x3F) {
-                    const float beta = (float)((ad * ad * tt - rr) / rr);
+                if ((it & 0x3F) && est > 0.0) {
+                    const float beta = (float)(est / rr);
                     BSum rp;
                     for (int i = threadIdx.x; i < N; i += blockDim.x) {
                         if (!(info[i] & 0x8000u)) continue;
@@ -240,7 +242,15 @@ __global__ void k_batch_cg(BCGArgs A) {
                     __syncthreads();
                 }
                 if (rr < thr) {
-                    if (!replaced) replace(rr);
+                    if (!replaced) {
+                        replace(rr);
+                        // d was formed from the recurrence residual: restart it from the recomputed one
+                        if (!(rr < thr)) {
+                            for (int i = threadIdx.x; i < N; i += blockDim.x)
+                                if (info[i] & 0x8000u) d[i] = r[i];
+                            __syncthreads();
+                        }
+                    }
                     if (rr < thr) { conv = 1; break; }
                 }
             }
@@ -580,6 +590,26 @@ int efs_batch_step(efs_batch* b, int n_steps) {
     for (int k = 0; k < n_steps; k++) BCK(cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
     b->frames += n_steps;
     return EFS_OK;
+}
+
+int efs_batch_time_steps(efs_batch* b, int n_steps, float* ms) {
+    if (!b || !ms) return EFS_ERR_ARG;
+    if (n_steps < 1) return bfail(b, EFS_ERR_ARG, "n_steps >= 1");
+    const int s = build_graph(b);
+    if (s != EFS_OK) return s;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0), "cudaEventCreate");
+    BCK(cudaEventCreate(&e1), "cudaEventCreate");
+    BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    BCK(cudaEventRecord(e0, b->stream), "cudaEventRecord");
+    for (int k = 0; k < n_steps; k++) BCK(cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
+    BCK(cudaEventRecord(e1, b->stream), "cudaEventRecord");
+    BCK(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    BCK(cudaEventElapsedTime(ms, e0, e1), "cudaEventElapsedTime");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->frames += n_steps;
+    return check_status(b);
 }
 
 int efs_batch_synchronize(efs_batch* b) {

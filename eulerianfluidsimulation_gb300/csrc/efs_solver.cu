@@ -444,13 +444,15 @@ __device__ __forceinline__ double div_fast(double a, double b) {
     return a * r;
 }
 
-// Two floats computed by thread 0 and read by the whole block.
-__device__ __forceinline__ void block_scalars(float& v0, float& v1) {
+// Two floats and a flag computed by thread 0 and read by the whole block.
+__device__ __forceinline__ void block_scalars(float& v0, float& v1, int* flag = nullptr) {
     __shared__ float s2[2];
-    if (threadIdx.x == 0) { s2[0] = v0; s2[1] = v1; }
+    __shared__ int s_flag;
+    if (threadIdx.x == 0) { s2[0] = v0; s2[1] = v1; s_flag = flag ? *flag : 0; }
     __syncthreads();
     v0 = s2[0];
     v1 = s2[1];
+    if (flag) *flag = s_flag;
     __syncthreads();
 }
 
@@ -507,6 +509,7 @@ __device__ __forceinline__ void cg_fp64(const SolverArgs& a, const Chunks& ch, c
             });
             double dt;
             if (!red.run(ctl, pair_of(acc), FSum(), 0, dt, u1, u2)) return;
+            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown: stop, not converged
             const double alpha = rr / dt;
             const double old = rr;
             acc = 0.0;
@@ -751,25 +754,35 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
         }
         int it;
         for (it = 0; it < a.max_steps; it++) {
+            // breakdown (a singular block: a liquid region with no air neighbour): stop, not converged
+            if (!(dt != 0.0) || !isfinite(rr / dt)) break;
             float alpha = 0.f, bet = 0.f;
+            int recur = 0;
             if (threadIdx.x == 0) {
                 const double ad = div_fast(rr, dt);
                 alpha = (float)ad;
-                bet = (float)(ad * ad * tt * div_fast(1.0, rr) - 1.0);
+                const double est = ad * ad * tt * div_fast(1.0, rr) - 1.0;   // r'.r' / r.r from the recurrence
+                recur = (it & 0x3F) && est > 0.0;
+                bet = (float)est;
             }
-            block_scalars(alpha, bet);
+            block_scalars(alpha, bet, &recur);
             const double old = rr;
-            if (it & 0x3F) {
+            if (recur) {
                 const FSum rp = phase_update<3>(a, ch, alpha, bet);
                 if (!grid_barrier(ctl)) return;
                 FSum dtp, ttp;
                 phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
                 if (!red.run(ctl, rp, dtp, ttp, rr, dt, tt)) return;
                 if (rr < thr) {
-                    // confirm on the recomputed residual; if that is above the threshold, iterate on from it
-                    // (d.t and t.t of the current d stand)
+                    // confirm on the recomputed residual; if that is above the threshold, the direction (formed
+                    // from the recurrence residual, so r.d != r.r now) restarts from it: d = r, t = L d
                     if (!replace(rr)) return;
                     if (rr < thr) { conv = 1; break; }
+                    for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) a.d0[i] = r[i]; });
+                    if (!grid_barrier(ctl)) return;
+                    FSum dtp2, ttp2;
+                    phase_t(a, ch, a.d0, a.t, nb, dtp2, ttp2);
+                    if (!red.run(ctl, FSum(), dtp2, ttp2, u3, dt, tt)) return;
                 }
             } else {
                 phase_update<1>(a, ch, alpha, 0.f);
@@ -796,6 +809,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
             const FSum dt_p = phase_a(a, ch, it, beta, dprev, dcur, nb);
             double dt;
             if (!red.run(ctl, dt_p, FSum(), 0, dt, u1, u2)) return;
+            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown: stop, not converged
             const float alpha = block_scalar(threadIdx.x == 0 ? (float)(rr / dt) : 0.f);
             // B: p (or e) += alpha d; r -= alpha L d, or the true residual every 64 iterations (:442-451)
             const double old = rr;

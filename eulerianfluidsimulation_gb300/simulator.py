@@ -325,6 +325,12 @@ class GB300Batch2D:
     def synchronize(self):
         self._check(lib().efs_batch_synchronize(self._h))
 
+    def time_steps(self, n):
+        """n steps timed with CUDA events on the batch's stream; device milliseconds."""
+        ms = np.zeros(1, np.float32)
+        self._check(lib().efs_batch_time_steps(self._h, n, fptr(ms)))
+        return float(ms[0])
+
     def stats(self, s):
         out = abi.EfsStats()
         self._check(lib().efs_batch_stats(self._h, s, ctypes.byref(out)))

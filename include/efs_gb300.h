@@ -303,6 +303,8 @@ int  efs_batch_stage(efs_batch* batch, int stage);
 /* n_steps whole steps of every scene (graph replays; asynchronous). */
 int  efs_batch_step(efs_batch* batch, int n_steps);
 int  efs_batch_synchronize(efs_batch* batch);
+/* n_steps steps with CUDA events recorded around them on the batch's stream; *ms = their device time. */
+int  efs_batch_time_steps(efs_batch* batch, int n_steps, float* ms);
 int  efs_batch_stats(efs_batch* batch, int scene, efs_stats* out);
 int  efs_batch_kernel_count(efs_batch* batch, int* count);
 int  efs_batch_get_tuning(const efs_batch* batch, efs_batch_tuning* tuning);

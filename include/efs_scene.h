@@ -13,7 +13,9 @@
  * Cavities: non-solid cells that are not connected (through faces of non-solid cells) to the open top row of
  * the domain (y = H-2) become solid.  Overlapping obstacles can leave such cells; a liquid cell inside one
  * gives the pressure matrix a row with no free neighbour (or a closed Neumann block), which no solver can
- * satisfy once its divergence is non-zero, so the reference's project() would pause for good.
+ * satisfy once its divergence is non-zero, so the reference's project() would pause for good.  For the same
+ * reason a connected set of non-solid cells that holds no air cell (rho <= 0.5) at all, such as a pocket the
+ * obstacles close off that a fluid blob fills, becomes solid as well (rho 0).
  *
  * Random numbers: PCG32 (M. E. O'Neill, "PCG: A Family of Simple Fast Space-Efficient Statistically Good
  * Algorithms for Random Number Generation", 2014), XSH-RR output, 64-bit LCG state with multiplier
@@ -68,8 +70,9 @@ static inline int efs_pcg32_int(efs_pcg32* g, int lo, int hi) {
 
 #define EFS_SCENE_MAX_OBJECTS 64
 
-/* Make every non-solid cell that cannot reach the top interior row through face neighbours solid (rho 0).
- * Returns the number of cells filled, or -1 when the work queue cannot be allocated. */
+/* Make every non-solid cell that cannot reach the top interior row through face neighbours solid (rho 0),
+ * and every connected set of non-solid cells without an air cell.  Returns the number of cells filled, or -1
+ * when the work queue cannot be allocated. */
 static inline long efs_scene_fill_cavities(int W, int H, int D, float* boundary, float* rho) {
     const size_t N = (size_t)W * H * D, WH = (size_t)W * H;
     unsigned char* seen = (unsigned char*)calloc(N, 1);
@@ -98,6 +101,30 @@ static inline long efs_scene_fill_cavities(int W, int H, int D, float* boundary,
     long filled = 0;
     for (size_t i = 0; i < N; i++)
         if (boundary[i] != 1.0f && !seen[i]) { boundary[i] = 1.0f; rho[i] = 0.0f; filled++; }
+    /* components of non-solid cells without an air cell: seen[] is reused as 2 = labelled */
+    for (size_t s0 = 0; s0 < N; s0++) {
+        if (boundary[s0] == 1.0f || seen[s0] == 2) continue;
+        head = tail = 0;
+        seen[s0] = 2;
+        q[tail++] = s0;
+        int air = 0;
+        while (head < tail) {
+            const size_t i = q[head++];
+            if (!(rho[i] > 0.5f)) air = 1;
+            const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / WH);
+            const long nb[6][3] = {{x - 1, y, z}, {x + 1, y, z}, {x, y - 1, z}, {x, y + 1, z}, {x, y, z - 1}, {x, y, z + 1}};
+            for (int k = 0; k < 6; k++) {
+                const long nx = nb[k][0], ny = nb[k][1], nz = nb[k][2];
+                if (nx < 0 || ny < 0 || nz < 0 || nx >= W || ny >= H || nz >= D) continue;
+                const size_t j = (size_t)nz * WH + (size_t)ny * W + (size_t)nx;
+                if (seen[j] == 2 || boundary[j] == 1.0f) continue;
+                seen[j] = 2;
+                q[tail++] = j;
+            }
+        }
+        if (!air)
+            for (size_t k = 0; k < tail; k++) { boundary[q[k]] = 1.0f; rho[q[k]] = 0.0f; filled++; }
+    }
     free(seen);
     free(q);
     return filled;

@@ -783,8 +783,10 @@ static float cg_solve_mixed(orc_grid* g, float thr) {
 
 /* EFS_CG_MIXED_RECURRENCE: the iteration of cg_solve_mixed with beta from the residual-norm recurrence
  * r'.r' = alpha^2 t.t - r.r, so that d, r and the increment are updated together once t = L d is known; the
- * exact r'.r' is still summed for the stop test, and every 64th iteration recomputes the residual in FP64 and
- * takes beta from it. */
+ * exact r'.r' is still summed for the stop test.  Every 64th iteration, and any iteration whose recurrence
+ * value is not positive, recomputes the residual in FP64 and takes beta from it.  When the stop test is met by the recurrence residual but not by the recomputed one, the
+ * search direction restarts from the recomputed residual.  A non-finite alpha (a singular block) stops the
+ * solve, not converged. */
 static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
     const size_t N = g->N;
     float *t = g->cg_t, *r = g->cg_r, *d = g->cg_d, *e = g->jac_tmp;
@@ -809,12 +811,14 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
         for (i = 0; i < steps; i++) {
             matmul(g, t, d);
             const double dt = ddot(g, d, t), tt = ddot(g, t, t);
+            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   /* breakdown: stop, not converged */
             const double ad = rr / dt;
             const float alpha = (float)ad;
             const double old = rr;
+            const double est = ad * ad * tt - old;            /* r'.r' from the CG recurrence */
             int replaced = 0;
-            if (i & 0x3F) {
-                const float beta = (float)((ad * ad * tt - old) / old);
+            if ((i & 0x3F) && est > 0.0) {
+                const float beta = (float)(est / old);
                 for (size_t c = 0; c < N; c++) {
                     e[c] += alpha * d[c];
                     const float rn = r[c] + (-alpha) * t[c];
@@ -830,7 +834,12 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
                 for (size_t c = 0; c < N; c++) d[c] = d[c] * beta + r[c];
             }
             if (rr < (double)thr) {
-                if (!replaced) ORC_REPLACE();
+                if (!replaced) {
+                    ORC_REPLACE();
+                    /* d was formed from the recurrence residual; after the replacement r.d != r.r, so the
+                     * direction restarts from the true residual */
+                    if (!(rr < (double)thr)) memcpy(d, r, N * 4);
+                }
                 if (rr < (double)thr) { conv = 1; break; }
             }
         }
