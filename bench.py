@@ -36,10 +36,24 @@ METRIC = "steps/s at 256\u00b3 to rel-res 1e-6: learned-PCG vs plain CG/Jacobi, 
 # are cache hits and count 0.
 SOLVE_BYTES_PER_ROW_ITER = 40.0
 SOLVE_BYTES_PER_ROW_SETUP = 30.0
+# Jacobi (ping-pong): per row and sweep read rowinfo, p, b and write the other p (14 B).
+JACOBI_BYTES_PER_ROW_ITER = 14.0
+# DRAM bytes (read + write) the solver moved per matrix row and CG iteration in one ncu capture of k_solver on
+# this workload (one launch: 958 iterations over 3,778,681 rows, 22.25 GB read + 41.77 GB written; the
+# active vectors only partly fit in L2 at 256^3).  `traffic` scales it by this run's row-iterations per launch.
+SOLVE_DRAM_BYTES_PER_ROW_ITER = 64.02e9 / (958 * 3778681)
+# Algorithmic bytes per interior cell of the stages other than the pressure solve, 3D (each field read once and
+# written once per pass: extrapolation 30 + 162, sharpen 21, advection 61 + 12 + 76 + 52, diffusion 153,
+# velocity advection 50, add_force 25, divergence 22, gradient and walls 29).
+STEP_BYTES_PER_CELL_3D = 693.0
+# The same for 2D (vel 8 B, 4 advection weights; the 2D diffusion runs 7 iterations x 2 axes).
+STEP_BYTES_PER_CELL_2D = 618.0
 # Mean CG iterations per step the CUDA path needs on this workload (measured by the gb300 arm over the first
 # steps of the dam break; printed in its JSON line as cg_iters_per_step).  The CPU-baseline sample times a
 # few CG iterations and scales them to this count instead of solving at 256^3 on one core for minutes.
 CG_ITERS_PER_STEP_REF = 934
+# The same for the other dam-break workloads the gb300 arm has measured (grid side, spheres) -> iterations/step.
+CG_ITERS_MEASURED = {(256, 16): 934, (128, 8): 459}
 
 
 def parse():
@@ -48,11 +62,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--size", type=int, default=None, help="grid side (default 256 for dam3d, 128 for dam2d)")
     ap.add_argument("--spheres", type=int, default=16)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--dt", type=float, default=0.004)
-    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi", "fcg"],
+    ap.add_argument("--solver", default=None, choices=["cg", "jacobi", "fcg"],
                     help="fcg: learned U-Net preconditioner (trained first at --fcg-train-size, outside the timed region)")
     ap.add_argument("--fcg-train-size", type=int, default=64)
     ap.add_argument("--fcg-train-iters", type=int, default=2000)
@@ -62,10 +76,18 @@ def parse():
                     help="instead of the throughput line: the precision study (every field against an FP64 "
                          "pressure solve of the same right-hand side) at --size for --steps steps")
     ap.add_argument("--study-out", default=None, help="precision study: also write the per-step records here (JSON)")
-    ap.add_argument("--workload", default="dam3d", choices=["dam3d", "batch2d"],
-                    help="batch2d: 64 independent 2D scenes of uneven sizes advanced together (efs_batch_*)")
+    ap.add_argument("--workload", default="dam3d", choices=["dam3d", "dam2d", "batch2d"],
+                    help="dam2d: the 2D dam break on one grid (Jacobi 100 sweeps unless --solver cg); batch2d: 64 "
+                         "independent 2D scenes of uneven sizes advanced together (efs_batch_*)")
     ap.add_argument("--scenes", type=int, default=64)
-    return ap.parse_args()
+    ap.add_argument("--batch-tuning", default=None,
+                    help="batch2d: tile_x,tile_y,blocks_per_sm,solver_threads instead of running the autotuner")
+    a = ap.parse_args()
+    if a.size is None:
+        a.size = 128 if a.workload == "dam2d" else 256
+    if a.solver is None:
+        a.solver = "jacobi" if a.workload == "dam2d" else "cg"
+    return a
 
 
 def dist_env():
@@ -183,14 +205,16 @@ def run_reference(a):
     if rank != 0:
         return
     prm = workload(a)
+    # unmeasured sizes: plain CG's iteration count grows about linearly with the grid side
+    cg_iters = CG_ITERS_MEASURED.get((a.size, a.spheres), round(CG_ITERS_PER_STEP_REF * a.size / 256))
     t = time.perf_counter()
-    cs = cpu_sample(a, prm, CG_ITERS_PER_STEP_REF)
+    cs = cpu_sample(a, prm, cg_iters)
     wall = time.perf_counter() - t
     line = {"metric": METRIC, "value": cs["value"], "unit": "steps/s", "n_gpus": a.gpus, "steps": 1, "warmup": 0,
             "ms_per_step": cs["step_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "config": config(a), "impl": "reference",
             "cpu_baseline": {"value": cs["value"], "unit": "steps/s", "cores": cs["cores"], "kind": cs["kind"],
-                             "sample": cs["sample"] + f"; CG count = the CUDA path's measured mean ({CG_ITERS_PER_STEP_REF})"},
+                             "sample": cs["sample"] + f"; CG count = the CUDA path's measured mean ({cg_iters})"},
             "e2e": {"value": cs["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "sample_wall_s": wall}
     print(json.dumps(line), flush=True)
@@ -243,7 +267,10 @@ def run_gb300(a):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     steps_per_s = a.steps / (ms / 1e3) * world
-    solve_bytes = row_iters * SOLVE_BYTES_PER_ROW_ITER + row_setups * SOLVE_BYTES_PER_ROW_SETUP
+    if prm.solver == abi.SOLVER_JACOBI:
+        solve_bytes = row_iters * JACOBI_BYTES_PER_ROW_ITER
+    else:
+        solve_bytes = row_iters * SOLVE_BYTES_PER_ROW_ITER + row_setups * SOLVE_BYTES_PER_ROW_SETUP
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -251,10 +278,22 @@ def run_gb300(a):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = (solve_bytes / launches) / ((solve_ms / launches) / 1e3) / 1e9 if launches and solve_ms > 0 else None
-    roofline = {"kernel": "k_solver (persistent CG)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": None,
+    traffic = None
+    if a.size == 256 and a.spheres == 16 and prm.solver == abi.SOLVER_CG and launches:
+        traffic = SOLVE_DRAM_BYTES_PER_ROW_ITER * row_iters / launches
+    roofline = {"kernel": "k_solver (persistent " + ("Jacobi)" if prm.solver == abi.SOLVER_JACOBI else "CG)"), "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_solver launch on this "
+                                  "workload, scaled by row-iterations" if traffic else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
                 "solve_ms_per_step": solve_ms / max(launches, 1), "algorithmic_bytes_per_launch": solve_bytes / max(launches, 1)}
+    # the whole step: the stages' algorithmic bytes per interior cell plus the solve's per matrix row
+    step_bytes = STEP_BYTES_PER_CELL_3D * (n - 2) ** 3 + solve_bytes / max(launches, 1)
+    step_achieved = step_bytes / (ms / a.steps / 1e3) / 1e9
+    step_roofline = {"bound": "hbm", "achieved": step_achieved, "peak": peak, "unit": "GB/s", "frac": step_achieved / peak,
+                     "algorithmic_bytes_per_step": step_bytes,
+                     "stages_bytes_per_interior_cell": STEP_BYTES_PER_CELL_3D,
+                     "stages_ms_per_step": ms / a.steps - solve_ms / max(launches, 1)}
 
     # e2e through the C ABI with pinned host buffers: upload, step, download every step
     e2e = None
@@ -298,7 +337,8 @@ def run_gb300(a):
                 "cell_updates_per_s": steps_per_s * (n - 2) ** 3, "cg_iters_per_step": iters / max(a.steps, 1),
                 "solve_converged": bool(st1.converged), "paused": bool(st2.paused), "active_rows": st1.active_cells,
                 "gpu_launches": kernels * a.steps, "kernels_per_step": kernels,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+                "roofline": roofline, "step_roofline": step_roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -442,7 +482,14 @@ def run_batch2d(a):
     for _ in range(a.warmup):
         B.update(1)
     B.synchronize()
-    tune = B.autotune(3)
+    if a.batch_tuning:
+        tx, ty, bps, th = (int(v) for v in a.batch_tuning.split(","))
+        tune = B.tuning()
+        tune.tile_x, tune.tile_y, tune.blocks_per_sm, tune.solver_threads = tx, ty, bps, th
+        B.set_tuning(tune)
+        tune.ms_per_step = 0.0
+    else:
+        tune = B.autotune(3)
     st0 = [B.stats(k) for k in range(B.n)]
     with Clocks(local) as clk:
         ms = B.time_steps(a.steps)
@@ -487,6 +534,9 @@ def run_batch2d(a):
     sep_ms = (time.perf_counter() - t0) * 1e3 / k_sep
     for S in sims:
         S.close()
+    cpu = None
+    if not a.no_cpu:
+        cpu = cpu_sample_batch([a.seed + k for k in range(a.scenes)], dt, 10)
     line = {"metric": f"scene-steps/s, {a.scenes} uneven 2D scenes (sides 64-256) to rel-res 1e-6",
             "value": a.scenes * a.steps / (ms / 1e3), "unit": "scene-steps/s", "n_gpus": 1, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -502,8 +552,137 @@ def run_batch2d(a):
             "roofline": {"kernel": "whole batched step", "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "algorithmic_bytes_per_step": step_bytes},
-            "clocks": clocks, "cpu_baseline": None, "e2e": None}
+            "clocks": clocks, "cpu_baseline": cpu, "e2e": None}
     print(json.dumps(line), flush=True)
+
+
+def _cpu_batch_scene(job):
+    """Worker of cpu_sample_batch: `steps` oracle steps of one batch scene; returns the seconds they took."""
+    seed, steps, dt = job
+    from eulerianfluidsimulation_gb300 import abi
+    from oracle import oracle
+    b, r = oracle.scene_batch2d(seed)
+    side = b.shape[0]
+    prm = abi.params_dam(1.0 / side, dt, abi.SOLVER_CG, 1e-6)
+    prm.max_steps = 20000
+    o = oracle.Oracle(2, side, side, 1, prm, mode=oracle.SHARPEN_PARALLEL | oracle.DOTS_FP64)
+    o.set_field(abi.FIELD_BOUNDARY, b)
+    o.set_field(abi.FIELD_RHO, r)
+    t0 = time.perf_counter()
+    o.step(steps)
+    return time.perf_counter() - t0
+
+
+def _cpu_batch_warm(_):
+    from oracle import oracle  # noqa: F401
+    return 0
+
+
+def cpu_sample_batch(seeds, dt, steps):
+    """The CPU oracle (port of the reference CPUSimulator2D step) on every scene of the batch, one process per
+    scene across the host cores (the reference's singletons forbid threads): `steps` steps of each scene."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    jobs = [(s, steps, dt) for s in seeds]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_cpu_batch_warm, range(cores), chunksize=1)      # worker start-up and imports, untimed
+        t0 = time.perf_counter()
+        per_scene = pool.map(_cpu_batch_scene, jobs, chunksize=1)
+        wall = time.perf_counter() - t0
+    return {"value": len(seeds) * steps / wall, "unit": "scene-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of each of the {len(seeds)} scenes, one process per scene on {cores} cores "
+                      f"({wall:.1f} s wall, {sum(per_scene):.1f} s of scene time)"}
+
+
+def run_dam2d(a):
+    """The 2D dam break on one 128^2 grid (dx = 1/128, dt = 0.005, fluid x < 0.4, y < 0.6, Jacobi 100 sweeps
+    per step as MAX_STEPS = 200): steps/s with the fields resident, e2e through upload/step/download, and the
+    CPU oracle timed on real steps of the same trajectory."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    n = a.size
+    solver = abi.SOLVER_CG if a.solver == "cg" else abi.SOLVER_JACOBI
+    prm = abi.params_dam(1.0 / n, 0.005, solver, 1e-6)
+    prm.max_steps = 200 if solver == abi.SOLVER_JACOBI else 20000
+    b, r = gb.scene_dam2d(n, n)
+    sim = gb.GB300Simulator2D(n, n, prm)
+    sim.set_field(abi.FIELD_BOUNDARY, b)
+    sim.set_field(abi.FIELD_RHO, r)
+    sim.update(a.warmup)
+    sim.synchronize()
+    kernels = sim.kernels_per_step()
+    st0 = sim.stats()
+    with Clocks(local) as clk:
+        sim.mark(0)
+        sim.update(a.steps)
+        sim.mark(1)
+        ms = sim.elapsed_ms(0, 1)
+    clocks = clk.summary()
+    st1 = sim.stats()
+    iters = (st1.total_solve_steps - st0.total_solve_steps) / max(a.steps, 1)
+    e2e = None
+    if not a.no_e2e:
+        import torch
+        h = {k: torch.empty(s, dtype=torch.float32, pin_memory=True).numpy()
+             for k, s in (("vel", (n, n, 2)), ("rho", (n, n)), ("gamma", (n, n)), ("boundary", (n, n)),
+                          ("forces", (n, n, 2)), ("beta", (n, n)), ("div", (n, n)), ("p", (n, n)))}
+        sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+        h["boundary"][...] = b
+        h["forces"][...] = 0
+        sim.synchronize()
+        sim.mark(2)
+        for _ in range(a.steps):
+            sim.upload_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"])
+            sim.update(1)
+            sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+        sim.mark(3)
+        ms_e2e = sim.elapsed_ms(2, 3)
+        e2e = {"value": a.steps / (ms_e2e / 1e3), "unit": "steps/s", "h2d_bytes_per_step": 4 * n * n * 7,
+               "d2h_bytes_per_step": 4 * n * n * 7, "steps": a.steps,
+               "api": "efs_upload_fields(vel,rho,gamma,boundary,forces) + efs_step + efs_download_fields(vel,rho,gamma,beta,div,p)"}
+    sim.close()
+    cpu = None
+    if not a.no_cpu:
+        cpu = cpu_sample_2d(n, prm, b, r, min(a.steps + a.warmup, 200))
+    interior = (n - 2) ** 2
+    per_iter = JACOBI_BYTES_PER_ROW_ITER if solver == abi.SOLVER_JACOBI else SOLVE_BYTES_PER_ROW_ITER
+    step_bytes = STEP_BYTES_PER_CELL_2D * interior + per_iter * st1.active_cells * iters
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = step_bytes / (ms / a.steps / 1e3) / 1e9
+    line = {"metric": f"steps/s, 2D dam break {n}^2 ({'Jacobi 100 sweeps' if solver == abi.SOLVER_JACOBI else 'CG rel-res 1e-6'})",
+            "value": a.steps / (ms / 1e3), "unit": "steps/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"dam2d_{n}", "grid": [n, n], "dt": 0.005, "solver": a.solver,
+                       "scene": "fluid x<0.4, y<0.6, solid border", "l2": "working set below L2 (no flush)"},
+            "cell_updates_per_s": interior * a.steps / (ms / 1e3), "solve_iters_per_step": iters,
+            "gpu_launches": kernels * a.steps, "kernels_per_step": kernels,
+            "roofline": {"kernel": "whole step", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_step": step_bytes},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_sample_2d(n, prm, b, r, steps):
+    """The CPU oracle (port of the reference CPUSimulator2D step) on the same scene, `steps` real steps."""
+    from eulerianfluidsimulation_gb300 import abi
+    from oracle import oracle
+    o = oracle.Oracle(2, n, n, 1, prm.copy())
+    o.set_field(abi.FIELD_BOUNDARY, b)
+    o.set_field(abi.FIELD_RHO, r)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} steps of the {n}^2 dam break on 1 core ({dt:.2f} s)"}
 
 
 def run_precision_study(a):
@@ -527,6 +706,9 @@ def main():
         return
     if a.workload == "batch2d":
         run_batch2d(a)
+        return
+    if a.workload == "dam2d":
+        run_dam2d(a)
         return
     if a.impl == "reference":
         run_reference(a)

@@ -337,7 +337,12 @@ int efs_upload_field(efs_ctx* c, int field, const float* host) {
         case EFS_FIELD_FORCES: {
             CK(cudaMemcpyAsync(c->tvel, host, bytes * c->dim, cudaMemcpyHostToDevice, c->stream), "upload");
             if (field == EFS_FIELD_VEL) { CK(efs::launch_upload_vec(c, c->tvel, c->u, c->v, c->w), "split"); }
-            else { CK(efs::launch_upload_vec(c, c->tvel, c->fx, c->fy, c->fz), "split"); c->has_forces = true; }
+            else {
+                CK(efs::launch_upload_vec(c, c->tvel, c->fx, c->fy, c->fz), "split");
+                // the step graphs were captured without the force term: recapture them with it
+                if (!c->has_forces) { CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"); drop_graphs(c); }
+                c->has_forces = true;
+            }
             break;
         }
         case EFS_FIELD_BOUNDARY:
