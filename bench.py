@@ -76,7 +76,7 @@ def parse():
                     help="instead of the throughput line: the precision study (every field against an FP64 "
                          "pressure solve of the same right-hand side) at --size for --steps steps")
     ap.add_argument("--study-out", default=None, help="precision study: also write the per-step records here (JSON)")
-    ap.add_argument("--workload", default="dam3d", choices=["dam3d", "dam2d", "batch2d"],
+    ap.add_argument("--workload", default="dam3d", choices=["dam3d", "dam2d", "batch2d", "scene", "unet"],
                     help="dam2d: the 2D dam break on one grid (Jacobi 100 sweeps unless --solver cg); batch2d: 64 "
                          "independent 2D scenes of uneven sizes advanced together (efs_batch_*)")
     ap.add_argument("--scenes", type=int, default=64)
@@ -685,6 +685,120 @@ def cpu_sample_2d(n, prm, b, r, steps):
             "sample": f"{steps} steps of the {n}^2 dam break on 1 core ({dt:.2f} s)"}
 
 
+def run_unet(a):
+    """The U-Net preconditioner's forward pass alone on a --size^3 dam break (untrained weights; the FLOPs do
+    not depend on them): ms per pass and per layer from CUDA events, TFLOP/s against the measured bf16 peak.
+    One warm-up pass, then --steps timed passes of 6 convolutions each."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    n = a.size
+    b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
+    sim = gb.GB300Simulator3D(n, n, n, workload(a))
+    sim.set_field(abi.FIELD_BOUNDARY, b)
+    sim.set_field(abi.FIELD_RHO, r)
+    sim.update(1)
+    sim.unet_init(a.seed + 7, 0)
+    with Clocks(local) as clk:
+        ms_fwd, ms_layers = sim.unet_time_forward(max(1, a.steps))
+    clocks = clk.summary()
+    sim.close()
+    flops = unet_flops(n)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    conv_ms = float(sum(ms_layers))
+    achieved = sum(flops) / (conv_ms / 1e3) / 1e12
+    per_layer = [{"layer": k, "cin_cout": list(UNET_LAYERS[k][:2]), "level": UNET_LAYERS[k][2], "ms": float(ms_layers[k]),
+                  "TFLOP/s": flops[k] / (float(ms_layers[k]) / 1e3) / 1e12 if ms_layers[k] > 0 else None}
+                 for k in range(len(UNET_LAYERS))]
+    line = {"metric": f"U-Net forward TFLOP/s at {n}^3 (implicit-GEMM tcgen05 convolutions)", "value": achieved,
+            "unit": "TFLOP/s", "n_gpus": 1, "steps": max(1, a.steps), "warmup": 1, "ms_per_step": ms_fwd,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"unet_{n}", "channels": [16, 32, 64], "levels": 3, "kernel": "3x3x3"},
+            "layers": per_layer,
+            "roofline": {"kernel": "k_conv3_tc (6 convolutions of one forward pass)", "bound": "tensor",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "flop_per_forward": sum(flops)},
+            "gpu_launches": None, "clocks": clocks, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
+def run_scene(a):
+    """The scene kernels on a --size^3 grid: the mesh label (sdf.comp's test of every cell against every
+    triangle of a closed sphere mesh) in cell-triangle tests/s, and the QueryNode box reduction over the whole
+    grid in GB/s (rho, u, v, w, p: 20 B per cell, every cell counted).  CUDA events on the context's stream."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    n = a.size
+    b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
+    sim = gb.GB300Simulator3D(n, n, n, workload(a))
+    sim.set_field(abi.FIELD_BOUNDARY, b)
+    sim.set_field(abi.FIELD_RHO, r)
+    sim.update(2)
+    sim.synchronize()
+    # a closed UV sphere of 64 x 32 bands (4032 triangles) in the unit-cube domain
+    nl, nm = 32, 64
+    th = np.linspace(0, np.pi, nl + 1)
+    ph = np.linspace(0, 2 * np.pi, nm + 1) + 0.1
+    P = lambda i, j: 0.5 + 0.3 * np.array([np.sin(th[i]) * np.cos(ph[j]), np.cos(th[i]), np.sin(th[i]) * np.sin(ph[j])])
+    tris = []
+    for i in range(nl):
+        for j in range(nm):
+            if i > 0:
+                tris.append((P(i, j), P(i + 1, j + 1), P(i, j + 1)))
+            if i < nl - 1:
+                tris.append((P(i, j), P(i + 1, j), P(i + 1, j + 1)))
+    tris = np.asarray(tris, np.float32)
+    center, size = (0.5, 0.5, 0.5), (1.0, 1.0, 1.0)
+    sim.mesh_label(abi.FIELD_GAMMA, tris, center, size, 1.0, 1.0)       # warm-up
+    reps = max(1, min(a.steps, 5))
+    with Clocks(local) as clk:
+        sim.mark(0)
+        for _ in range(reps):
+            sim.mesh_label(abi.FIELD_GAMMA, tris, center, size, 1.0, 1.0)
+        sim.mark(1)
+        ms_label = sim.elapsed_ms(0, 1) / reps
+        for _ in range(3):
+            sim.query_box((0, 0, 0), (n, n, n), False)
+        qreps = max(3, a.steps)
+        sim.mark(2)
+        for _ in range(qreps):
+            m = sim.query_box((0, 0, 0), (n, n, n), False)
+        sim.mark(3)
+        ms_query = sim.elapsed_ms(2, 3) / qreps
+    clocks = clk.summary()
+    sim.close()
+    pairs = float((n - 1) ** 3) * len(tris)
+    qcells = float((n - 1) ** 3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    q_gbs = 20.0 * qcells / (ms_query / 1e3) / 1e9
+    line = {"metric": f"mesh label cell-triangle tests/s and query-box GB/s at {n}^3", "value": pairs / (ms_label / 1e3),
+            "unit": "cell-triangle tests/s", "n_gpus": 1, "steps": reps, "warmup": 1, "ms_per_step": ms_label,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"scene_{n}", "triangles": len(tris), "cells": (n - 1) ** 3,
+                       "mesh": "closed UV sphere r=0.3 in the unit domain", "l2": "grid fields > L2 (query)"},
+            "mesh_label_ms": ms_label, "query_box": {"ms": ms_query, "count": m.count, "GB/s": q_gbs,
+                                                     "bytes_per_cell": 20},
+            "roofline": {"kernel": "k_query (box reduction, every cell counted)", "bound": "hbm", "achieved": q_gbs,
+                         "peak": peak, "unit": "GB/s", "frac": q_gbs / peak, "traffic": None},
+            "gpu_launches": reps + 2 * qreps, "clocks": clocks, "cpu_baseline": None, "e2e": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_precision_study(a):
     """One JSON line with the maxima of the per-step errors (the 3D dam break with --spheres spheres)."""
     from eulerianfluidsimulation_gb300.precision import precision_study
@@ -709,6 +823,12 @@ def main():
         return
     if a.workload == "dam2d":
         run_dam2d(a)
+        return
+    if a.workload == "scene":
+        run_scene(a)
+        return
+    if a.workload == "unet":
+        run_unet(a)
         return
     if a.impl == "reference":
         run_reference(a)

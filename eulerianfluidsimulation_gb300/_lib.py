@@ -7,7 +7,7 @@ no CPU fallback.  Build it with ``python -c "import __graft_entry__ as g; g.buil
 import ctypes
 import os
 
-from .abi import EfsBatchTuning, EfsParams, EfsStats, STATUS_NAMES
+from .abi import EfsBatchTuning, EfsParams, EfsQueryMetrics, EfsStats, STATUS_NAMES
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libefs_gb300.so")
@@ -77,6 +77,14 @@ SIGNATURES = {
     "efs_scene_dam3d": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_uint64, _FP, _FP]),
     "efs_scene_dam2d": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _FP, _FP]),
     "efs_scene_batch2d": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _FP, _FP, ctypes.c_int]),
+    "efs_mesh_label": (ctypes.c_int, [_CTX, ctypes.c_int, _FP, ctypes.c_int, _FP, _FP, ctypes.c_float, ctypes.c_float]),
+    "efs_mesh_cells": (ctypes.c_int, [_CTX, _FP, ctypes.c_int, _FP, _FP, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong,
+                                      ctypes.POINTER(ctypes.c_longlong)]),
+    "efs_fill_box": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _FP]),
+    "efs_set_cells": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong, _FP]),
+    "efs_seal_boundary": (ctypes.c_int, [_CTX]),
+    "efs_query_box": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                     ctypes.POINTER(EfsQueryMetrics)]),
 }
 
 

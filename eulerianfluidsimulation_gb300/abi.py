@@ -110,6 +110,25 @@ class EfsBatchTuning(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class EfsQueryMetrics(ctypes.Structure):
+    """``efs_query_metrics``: QueryNode's Metrics (include/simulation/scene/nodes/QueryNode.h:10-17) plus the
+    number of cells that counted."""
+    _fields_ = [
+        ("max_position", ctypes.c_float * 3),
+        ("min_position", ctypes.c_float * 3),
+        ("avg_position", ctypes.c_float * 3),
+        ("velocity", ctypes.c_float * 3),
+        ("pressure", ctypes.c_float),
+        ("pad", ctypes.c_int),
+        ("count", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {"max_position": list(self.max_position), "min_position": list(self.min_position),
+                "avg_position": list(self.avg_position), "velocity": list(self.velocity),
+                "pressure": self.pressure, "count": self.count}
+
+
 def _f32(x):
     return ctypes.c_float(x).value
 

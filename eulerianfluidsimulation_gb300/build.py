@@ -25,6 +25,7 @@ UNITS = {
     "efs_noalloc.cu": ["--fmad=false"],
     "efs_unet.cu": [],
     "efs_batch.cu": ["--fmad=false"],
+    "efs_scene.cu": ["--fmad=false"],
 }
 
 

@@ -3,6 +3,7 @@
 // A context owns its device buffers, one non-blocking stream and one instantiated CUDA graph per step
 // configuration (enabled stages, solver, CG variant).  efs_step replays that graph; the pressure solve
 // inside it is a single cooperative kernel, so a step never waits on the host.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -134,12 +135,22 @@ int check_device_status(efs_ctx* c) {
     CK(cudaMemcpy(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost), "read device status");
     if (c->ctl_host->error) {
         char buf[160];
-        std::snprintf(buf, sizeof buf, "device status word %d (1 barrier timeout, 2 boundary not 0/1, 4 list overflow)",
+        std::snprintf(buf, sizeof buf, "device status word %d (1 barrier timeout, 2 boundary not 0/1, 4 list overflow, 8 bad cell index)",
                       c->ctl_host->error);
         const int err = c->ctl_host->error;
         int zero = 0;
         cudaMemcpy(&c->ctl->error, &zero, sizeof(int), cudaMemcpyHostToDevice);
         return fail(c, err == efs::DEV_ERR_BAD_BOUNDARY ? EFS_ERR_ARG : EFS_ERR_DEVICE_FAULT, buf);
+    }
+    return EFS_OK;
+}
+
+// The step graphs bake in whether the forces field is used: recapture them the first time it is.
+int note_forces(efs_ctx* c) {
+    if (!c->has_forces) {
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+        drop_graphs(c);
+        c->has_forces = true;
     }
     return EFS_OK;
 }
@@ -214,7 +225,7 @@ void efs_destroy(efs_ctx* c) {
     void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->fx, c->fy, c->fz, c->solid,
                     c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
                     c->sh_idx, c->sh_val, c->sh_end, c->rowinfo, c->chunk_flag, c->chunk_list, c->block_count,
-                    c->partials, c->ctl, c->mass_partials};
+                    c->partials, c->ctl, c->mass_partials, c->query_scratch};
     for (void* b : bufs) if (b) cudaFree(b);
     for (void* b : c->halo_bases) cudaFree(b);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
@@ -339,9 +350,8 @@ int efs_upload_field(efs_ctx* c, int field, const float* host) {
             if (field == EFS_FIELD_VEL) { CK(efs::launch_upload_vec(c, c->tvel, c->u, c->v, c->w), "split"); }
             else {
                 CK(efs::launch_upload_vec(c, c->tvel, c->fx, c->fy, c->fz), "split");
-                // the step graphs were captured without the force term: recapture them with it
-                if (!c->has_forces) { CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"); drop_graphs(c); }
-                c->has_forces = true;
+                const int s = note_forces(c);
+                if (s != EFS_OK) return s;
             }
             break;
         }
@@ -577,6 +587,129 @@ int efs_timer_elapsed(efs_ctx* c, int a, int b, double* ms) {
     float t = 0;
     CK(cudaEventElapsedTime(&t, c->marks[a], c->marks[b]), "cudaEventElapsedTime");
     *ms = t;
+    return EFS_OK;
+}
+
+// ---- scene construction and queries (efs_scene.cu) --------------------------------------------------------
+
+int efs_mesh_label(efs_ctx* c, int field, const float* tris, int ntri, const float center[3], const float size[3],
+                   float vin, float vout) {
+    if (!c) return EFS_ERR_ARG;
+    if (c->dim != 3) return fail(c, EFS_ERR_ARG, "mesh labels are 3D only");
+    if ((ntri > 0 && !tris) || ntri < 0 || !center || !size) return fail(c, EFS_ERR_ARG, "bad triangles or domain");
+    efs::FieldPtrsOut o;
+    if (!efs::scene_field_ptrs(c, field, o) || o.ncomp != 1) return fail(c, EFS_ERR_ARG, "field must be scalar or the boundary");
+    if (field == EFS_FIELD_BOUNDARY && !((vin == 0.0f || vin == 1.0f) && (vout == 0.0f || vout == 1.0f)))
+        return fail(c, EFS_ERR_ARG, "boundary values are 0.0 or 1.0");
+    float* d_tris = nullptr;
+    const size_t bytes = (size_t)std::max(ntri, 1) * 12 * sizeof(float);
+    CK(cudaMalloc(&d_tris, bytes), "cudaMalloc triangles");
+    cudaError_t e = ntri > 0 ? cudaMemcpyAsync(d_tris, tris, (size_t)ntri * 12 * sizeof(float), cudaMemcpyHostToDevice, c->stream)
+                             : cudaSuccess;
+    if (e == cudaSuccess) e = efs::launch_mesh_label(c, d_tris, ntri, center, size, vin, vout, field, nullptr);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_tris);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mesh label");
+    return EFS_OK;
+}
+
+int efs_mesh_cells(efs_ctx* c, const float* tris, int ntri, const float center[3], const float size[3], int* cells,
+                   long long capacity, long long* count) {
+    if (!c) return EFS_ERR_ARG;
+    if (c->dim != 3) return fail(c, EFS_ERR_ARG, "mesh labels are 3D only");
+    if ((ntri > 0 && !tris) || ntri < 0 || !center || !size || !count || capacity < 0 || (capacity > 0 && !cells))
+        return fail(c, EFS_ERR_ARG, "bad arguments");
+    const long long N = c->g.N, tiles = efs::mask_tiles(c), cap = std::min(capacity, N);
+    float* d_tris = nullptr;
+    uint8_t* mask = nullptr;
+    int *counts = nullptr, *out = nullptr;
+    long long* offsets = nullptr;
+    cudaError_t e = cudaMalloc(&d_tris, (size_t)std::max(ntri, 1) * 12 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&mask, (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc(&counts, (size_t)tiles * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&offsets, (size_t)(tiles + 1) * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&out, (size_t)std::max(cap, 1LL) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(mask, 0, (size_t)N, c->stream);
+    if (e == cudaSuccess && ntri > 0)
+        e = cudaMemcpyAsync(d_tris, tris, (size_t)ntri * 12 * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = efs::launch_mesh_label(c, d_tris, ntri, center, size, 1.0f, 0.0f, EFS_FIELD_RHO, mask);
+    if (e == cudaSuccess) e = efs::launch_mask_compact(c, mask, out, cap, counts, offsets);
+    long long total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, offsets + tiles, sizeof(long long), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && cap > 0 && total > 0)
+        e = cudaMemcpy(cells, out, (size_t)std::min(total, cap) * sizeof(int), cudaMemcpyDeviceToHost);
+    for (void* b : {(void*)d_tris, (void*)mask, (void*)counts, (void*)offsets, (void*)out}) if (b) cudaFree(b);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mesh cells");
+    *count = total;
+    return EFS_OK;
+}
+
+int efs_fill_box(efs_ctx* c, int field, const int lo[3], const int hi[3], const float* value) {
+    if (!c) return EFS_ERR_ARG;
+    if (!lo || !hi || !value) return fail(c, EFS_ERR_ARG, "lo, hi and value must not be NULL");
+    efs::FieldPtrsOut o;
+    if (!efs::scene_field_ptrs(c, field, o)) return fail(c, EFS_ERR_ARG, "unknown field");
+    if (field == EFS_FIELD_BOUNDARY && !(value[0] == 0.0f || value[0] == 1.0f))
+        return fail(c, EFS_ERR_ARG, "boundary values are 0.0 or 1.0");
+    const int dims[3] = {c->g.W, c->g.H, c->dim == 3 ? c->g.D : 1};
+    int l[3], h[3];
+    for (int d = 0; d < 3; d++) { l[d] = std::max(0, lo[d]); h[d] = std::min(dims[d], hi[d]); }
+    if (c->dim == 2) { l[2] = 0; h[2] = 1; }
+    CK(efs::launch_fill_box(c, field, l, h, value), "fill box");
+    if (field == EFS_FIELD_FORCES) { const int s = note_forces(c); if (s != EFS_OK) return s; }
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_set_cells(efs_ctx* c, int field, const int* cells, long long n, const float* value) {
+    if (!c) return EFS_ERR_ARG;
+    if (n < 0 || (n > 0 && !cells) || !value) return fail(c, EFS_ERR_ARG, "bad cell list or value");
+    efs::FieldPtrsOut o;
+    if (!efs::scene_field_ptrs(c, field, o)) return fail(c, EFS_ERR_ARG, "unknown field");
+    if (field == EFS_FIELD_BOUNDARY && !(value[0] == 0.0f || value[0] == 1.0f))
+        return fail(c, EFS_ERR_ARG, "boundary values are 0.0 or 1.0");
+    if (n == 0) return EFS_OK;
+    int* d_cells = nullptr;
+    CK(cudaMalloc(&d_cells, (size_t)n * sizeof(int)), "cudaMalloc cells");
+    cudaError_t e = cudaMemcpyAsync(d_cells, cells, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = efs::launch_set_cells(c, field, d_cells, n, value);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_cells);
+    if (e != cudaSuccess) return cuda_fail(c, e, "set cells");
+    if (field == EFS_FIELD_FORCES) { const int s = note_forces(c); if (s != EFS_OK) return s; }
+    CK(cudaMemcpy(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost), "read device status");
+    if (c->ctl_host->error & efs::DEV_ERR_BAD_INDEX) {
+        const int cleared = c->ctl_host->error & ~efs::DEV_ERR_BAD_INDEX;
+        cudaMemcpy(&c->ctl->error, &cleared, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(c, EFS_ERR_ARG, "a cell index is outside the grid");
+    }
+    return EFS_OK;
+}
+
+int efs_seal_boundary(efs_ctx* c) {
+    if (!c) return EFS_ERR_ARG;
+    CK(efs::launch_seal_boundary(c), "seal boundary");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return EFS_OK;
+}
+
+int efs_query_box(efs_ctx* c, const int position[3], const int scale[3], int only_fluid, efs_query_metrics* out) {
+    if (!c) return EFS_ERR_ARG;
+    if (!position || !scale || !out) return fail(c, EFS_ERR_ARG, "position, scale and out must not be NULL");
+    const int dims[3] = {c->g.W, c->g.H, c->dim == 3 ? c->g.D : 2};
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = std::max(0, position[d]);
+        hi[d] = std::min(dims[d] - 1, position[d] + scale[d]);
+    }
+    if (c->dim == 2) { lo[2] = 0; hi[2] = 1; }
+    if (!c->query_scratch) CK(cudaMalloc(&c->query_scratch, efs::query_scratch_bytes()), "cudaMalloc query scratch");
+    const size_t res_off = efs::query_scratch_bytes() - sizeof(efs_query_metrics) - 64;
+    efs_query_metrics* d_out = reinterpret_cast<efs_query_metrics*>(static_cast<char*>(c->query_scratch) + res_off);
+    CK(efs::launch_query_box(c, lo, hi, only_fluid, c->query_scratch, d_out), "query box");
+    CK(cudaMemcpyAsync(out, d_out, sizeof(efs_query_metrics), cudaMemcpyDeviceToHost, c->stream), "download metrics");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     return EFS_OK;
 }
 

@@ -17,7 +17,8 @@ namespace efs {
 enum DeviceError : int {
     DEV_ERR_BARRIER_TIMEOUT = 1,   // a grid barrier of the persistent solver gave up waiting
     DEV_ERR_BAD_BOUNDARY = 2,      // an uploaded boundary value was neither 0.0 nor 1.0
-    DEV_ERR_LIST_OVERFLOW = 4      // a compaction list exceeded its capacity
+    DEV_ERR_LIST_OVERFLOW = 4,     // a compaction list exceeded its capacity
+    DEV_ERR_BAD_INDEX = 8          // a listed cell index was outside the grid
 };
 
 // Control block in device memory: grid barrier, solve results and counters.  Mirrored into pinned host
@@ -146,6 +147,7 @@ struct efs_ctx {
     std::string err;
 
     efs::UNetState* unet = nullptr;         // learned preconditioner (efs_unet.cu)
+    void* query_scratch = nullptr;          // efs_query_box block partials and result (efs_scene.cu)
 };
 
 namespace efs {
@@ -167,4 +169,22 @@ cudaError_t launch_boundary_to_solid(efs_ctx* c, const float* staged);
 cudaError_t launch_solid_to_boundary(efs_ctx* c, float* staged);
 cudaError_t launch_reset_fields(efs_ctx* c);
 cudaError_t launch_mass(efs_ctx* c, double* out_dev);
+// efs_scene.cu: scene construction and queries
+struct FieldPtrsOut {
+    float* f[3] = {nullptr, nullptr, nullptr};
+    uint8_t* solid = nullptr;
+    int ncomp = 0;
+};
+bool scene_field_ptrs(efs_ctx* c, int field, FieldPtrsOut& out);
+cudaError_t launch_mesh_label(efs_ctx* c, const float* d_tris, int ntri, const float center[3], const float size[3],
+                              float vin, float vout, int field, uint8_t* mask);
+cudaError_t launch_mask_compact(efs_ctx* c, const uint8_t* mask, int* d_out, long long cap, int* d_counts,
+                                long long* d_offsets);
+long long mask_tiles(const efs_ctx* c);
+cudaError_t launch_fill_box(efs_ctx* c, int field, const int lo[3], const int hi[3], const float* value);
+cudaError_t launch_set_cells(efs_ctx* c, int field, const int* d_cells, long long n, const float* value);
+cudaError_t launch_seal_boundary(efs_ctx* c);
+size_t query_scratch_bytes();
+cudaError_t launch_query_box(efs_ctx* c, const int lo[3], const int hi[3], int only_fluid, void* scratch,
+                             efs_query_metrics* d_out);
 }  // namespace efs

@@ -131,6 +131,65 @@ class _GB300Simulator:
     def reset(self):
         check(lib().efs_reset_fields(self._h), self._h)
 
+    # ---- scene construction and queries (Editor / scene nodes) ----
+    @staticmethod
+    def _tris(triangles):
+        """[n, 3, 3] world-space vertices -> the reference Triangle layout (12 floats per triangle)."""
+        t = np.asarray(triangles, np.float32).reshape(-1, 3, 3)
+        out = np.zeros((len(t), 3, 4), np.float32)
+        out[:, :, :3] = t
+        return out
+
+    @staticmethod
+    def _vec3(v):
+        return np.ascontiguousarray(np.asarray(v, np.float32).reshape(3))
+
+    @staticmethod
+    def _ivec3(v):
+        return (ctypes.c_int * 3)(*[int(x) for x in v])
+
+    def mesh_label(self, field, triangles, domain_center, domain_size, value_inside=1.0, value_outside=0.0):
+        t = self._tris(triangles)
+        c, s = self._vec3(domain_center), self._vec3(domain_size)
+        check(lib().efs_mesh_label(self._h, field, fptr(t), len(t), fptr(c), fptr(s), value_inside, value_outside),
+              self._h)
+
+    def mesh_cells(self, triangles, domain_center, domain_size, capacity=None):
+        """Inside cells (ascending linear indices) and their total number (which may exceed capacity)."""
+        t = self._tris(triangles)
+        c, s = self._vec3(domain_center), self._vec3(domain_size)
+        cap = int(np.prod(self.shape)) if capacity is None else int(capacity)
+        cells = np.zeros(max(cap, 1), np.int32)
+        n = ctypes.c_longlong()
+        check(lib().efs_mesh_cells(self._h, fptr(t), len(t), fptr(c), fptr(s),
+                                   cells.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap, ctypes.byref(n)), self._h)
+        return cells[:min(n.value, cap)], n.value
+
+    def _value(self, field, value):
+        comps = self.dim if field in abi.VECTOR_FIELDS else 1
+        v = np.zeros(3, np.float32)
+        v[:comps] = np.broadcast_to(np.asarray(value, np.float32), (comps,))
+        return v
+
+    def fill_box(self, field, lo, hi, value):
+        v = self._value(field, value)
+        check(lib().efs_fill_box(self._h, field, self._ivec3(lo), self._ivec3(hi), fptr(v)), self._h)
+
+    def set_cells(self, field, cells, value):
+        idx = np.ascontiguousarray(np.asarray(cells, np.int64).astype(np.int32))
+        v = self._value(field, value)
+        check(lib().efs_set_cells(self._h, field, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(idx), fptr(v)),
+              self._h)
+
+    def seal_boundary(self):
+        check(lib().efs_seal_boundary(self._h), self._h)
+
+    def query_box(self, position, scale, only_fluid=True):
+        m = abi.EfsQueryMetrics()
+        check(lib().efs_query_box(self._h, self._ivec3(position), self._ivec3(scale), int(only_fluid), ctypes.byref(m)),
+              self._h)
+        return m
+
     def vel(self):
         return self.field(abi.FIELD_VEL)
 

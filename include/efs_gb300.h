@@ -313,6 +313,50 @@ int  efs_batch_set_tuning(efs_batch* batch, const efs_batch_tuning* tuning);
  * (restored after every trial) and keeps the fastest; `best` (may be NULL) receives it. */
 int  efs_batch_autotune(efs_batch* batch, int trial_steps, efs_batch_tuning* best);
 
+/* ---- scene construction and queries (the editor and scene-node side; between steps) --------------------
+ * These write or read a context's device fields directly, on its stream, and return after the work is done.
+ * Triangles use the reference Triangle layout (include/assets/Triangle.h:10-19): 12 floats per triangle,
+ * v0.xyz, pad, v1.xyz, pad, v2.xyz, pad, in world coordinates; the domain is the simulation domain's
+ * world box (SimulationDomainNode / BoundingBoxNode::getWorldBoundingBox: centre and size), which the grid,
+ * border included, divides into W x H x D cells.  Mesh operations are 3D only. */
+
+/* The inside/outside label of sdf.comp (assets/shaders/sdf.comp:29-114) for every cell of
+ * [0, W-1) x [0, H-1) x [0, D-1): `value_inside` where the cell centre is on a triangle or the mesh's winding
+ * number exceeds pi in magnitude, else `value_outside`.  Other cells keep their value.  `field` is a scalar
+ * field or EFS_FIELD_BOUNDARY (values 0.0/1.0).  Replaces the sdf.comp dispatches of Editor::initFluid and
+ * Editor::initBoundaries (src/core/Editor.cpp:118-137, :199-218). */
+int  efs_mesh_label(efs_ctx* ctx, int field, const float* triangles, int n_triangles, const float domain_center[3],
+                    const float domain_size[3], float value_inside, float value_outside);
+/* The cells that efs_mesh_label labels inside, as ascending linear indices (forcefield_cells.comp:90-111,
+ * which appends them in dispatch order).  *count receives their number; at most `capacity` are written. */
+int  efs_mesh_cells(efs_ctx* ctx, const float* triangles, int n_triangles, const float domain_center[3],
+                    const float domain_size[3], int* cells, long long capacity, long long* count);
+/* `value` (1 float, or dim floats for EFS_FIELD_VEL / EFS_FIELD_FORCES) in every cell of the box
+ * [lo, hi), clipped to the grid (2D: z ignored).  The box fluid spawn (Editor.cpp:155-161), the initial fill
+ * (baseFluidFill.comp:24-35), DeletionNode::update (DeletionNode.cpp:27-33). */
+int  efs_fill_box(efs_ctx* ctx, int field, const int lo[3], const int hi[3], const float* value);
+/* `value` at the n listed linear cell indices (Scene2D::loadScene, Scene2D.cpp:59-62; the force-field cells,
+ * Editor.cpp:325-330).  An index outside the grid is EFS_ERR_ARG (the rest are written). */
+int  efs_set_cells(efs_ctx* ctx, int field, const int* cells, long long n, const float* value);
+/* The outer layer of cells becomes solid, and rho is 0 in every solid cell (Editor.cpp:220-229). */
+int  efs_seal_boundary(efs_ctx* ctx);
+
+/* QueryNode metrics (include/simulation/scene/nodes/QueryNode.h:10-17) over the box of cells
+ * [max(0, position), min(dim - 1, position + scale)) per axis (QueryNode.cpp:47-66; 2D: z ignored), only
+ * cells with rho >= 0.5 when only_fluid: the largest, smallest and mean cell coordinates, and the mean
+ * velocity (the MAC face values stored at each cell) and pressure.  All zero when no cell counts.  Sums are
+ * exact (coordinates) or FP64 (velocity, pressure), in a fixed order. */
+typedef struct efs_query_metrics {
+    float max_position[3];
+    float min_position[3];
+    float avg_position[3];
+    float velocity[3];
+    float pressure;
+    int   pad;
+    long long count;
+} efs_query_metrics;
+int  efs_query_box(efs_ctx* ctx, const int position[3], const int scale[3], int only_fluid, efs_query_metrics* out);
+
 /* ---- host-only helpers (no device needed) ---- */
 /* Seeded synthetic scenes; see efs_scene.h for the generators and their draw order. */
 int  efs_scene_dam3d(int w, int h, int d, int n_spheres_min, int n_spheres_max, uint64_t seed,

@@ -73,6 +73,11 @@ def _load_orc():
         lib.orc_scene_dam2d.argtypes = [ctypes.c_int, ctypes.c_int, _FP, _FP]
         lib.orc_scene_batch2d.restype = ctypes.c_int
         lib.orc_scene_batch2d.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _FP, _FP]
+        lib.orc_mesh_label.argtypes = [ctypes.c_int] * 3 + [_FP, ctypes.c_int, _FP, _FP, ctypes.c_float,
+                                                            ctypes.c_float, _FP]
+        lib.orc_query_box.restype = ctypes.c_longlong
+        lib.orc_query_box.argtypes = [ctypes.c_int] * 4 + [_FP] * 5 + [ctypes.POINTER(ctypes.c_int)] * 2 + \
+            [ctypes.c_int, _FP]
         _orc = lib
     return _orc
 
@@ -252,3 +257,37 @@ class RefOracle(_Base):
         s = EfsStats()
         self._lib.ref_stats(self._h, ctypes.byref(s))
         return s
+
+
+def mesh_label(shape, triangles, center, size, value_inside=1.0, value_outside=0.0, out=None):
+    """sdf.comp's label of every cell of [0, W-1) x [0, H-1) x [0, D-1) (restated in scene_oracle.c).
+    shape = (D, H, W); triangles: [n, 3, 3] world coordinates; other cells of `out` (default zeros) kept."""
+    D, H, W = shape
+    t = np.zeros((len(triangles), 3, 4), np.float32)
+    t[:, :, :3] = np.asarray(triangles, np.float32).reshape(-1, 3, 3)
+    o = np.zeros(shape, np.float32) if out is None else np.ascontiguousarray(out, np.float32).copy()
+    c = np.asarray(center, np.float32)
+    s = np.asarray(size, np.float32)
+    _load_orc().orc_mesh_label(W, H, D, _fptr(t), len(t), _fptr(c), _fptr(s), value_inside, value_outside, _fptr(o))
+    return o
+
+
+def query_box(rho, vel, pressure, position, scale, only_fluid=True):
+    """QueryNode::update's metrics (restated in scene_oracle.c).  rho, pressure: [D, H, W] or [H, W];
+    vel: [..., dim].  Returns (dict of floats, count)."""
+    rho = np.ascontiguousarray(rho, np.float32)
+    dim = rho.ndim
+    shape = rho.shape if dim == 3 else (1,) + rho.shape
+    vel = np.asarray(vel, np.float32)
+    u = np.ascontiguousarray(vel[..., 0])
+    v = np.ascontiguousarray(vel[..., 1])
+    w = np.ascontiguousarray(vel[..., 2]) if dim == 3 else None
+    p = np.ascontiguousarray(pressure, np.float32)
+    out = np.zeros(13, np.float32)
+    pos = (ctypes.c_int * 3)(*[int(x) for x in position])
+    sc = (ctypes.c_int * 3)(*[int(x) for x in scale])
+    n = _load_orc().orc_query_box(dim, shape[2], shape[1], shape[0], _fptr(rho), _fptr(u), _fptr(v),
+                                  _fptr(w) if w is not None else None, _fptr(p), pos, sc, int(only_fluid), _fptr(out))
+    m = {"max_position": out[0:3].copy(), "min_position": out[3:6].copy(), "avg_position": out[6:9].copy(),
+         "velocity": out[9:12].copy(), "pressure": float(out[12])}
+    return m, int(n)

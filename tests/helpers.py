@@ -32,3 +32,39 @@ def load_golden(name):
 def labels(rho):
     """Fluid labels as the step reads them: liquid where rho >= 0.5."""
     return np.asarray(rho) >= 0.5
+
+
+def sphere_mesh(center, radius, n_lat=12, n_lon=24):
+    """A closed UV sphere as triangles [n, 3, 3] (outward-facing), vertices placed off the cell-centre grid
+    so no cell centre lies exactly on a face unless a test asks for it."""
+    c = np.asarray(center, np.float64)
+    pts = lambda th, ph: c + radius * np.array([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)])
+    tris = []
+    for i in range(n_lat):
+        t0, t1 = np.pi * i / n_lat, np.pi * (i + 1) / n_lat
+        for j in range(n_lon):
+            p0, p1 = 2 * np.pi * j / n_lon + 0.1, 2 * np.pi * (j + 1) / n_lon + 0.1
+            a, b, cc, d = pts(t0, p0), pts(t0, p1), pts(t1, p1), pts(t1, p0)
+            if i > 0:
+                tris.append((a, cc, b))
+            if i < n_lat - 1:
+                tris.append((a, d, cc))
+    return np.asarray(tris, np.float32)
+
+
+def box_mesh(lo, hi):
+    """An axis-aligned box [lo, hi] as 12 triangles."""
+    from eulerianfluidsimulation_gb300.scene import cube_triangles
+    lo, hi = np.asarray(lo, np.float32), np.asarray(hi, np.float32)
+    t = cube_triangles() > 0          # each corner takes lo or hi exactly
+    return np.where(t, hi, lo).astype(np.float32)
+
+
+def write_obj(path, triangles):
+    """Triangles [n, 3, 3] as an OBJ file (one vertex per corner)."""
+    with open(path, "w") as fh:
+        for tri in np.asarray(triangles, np.float32):
+            for v in tri:
+                fh.write(f"v {float(v[0])!r} {float(v[1])!r} {float(v[2])!r}\n")
+        for k in range(len(triangles)):
+            fh.write(f"f {3 * k + 1} {3 * k + 2} {3 * k + 3}\n")
