@@ -81,7 +81,7 @@ def parse():
                          "independent 2D scenes of uneven sizes advanced together (efs_batch_*)")
     ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--batch-tuning", default=None,
-                    help="batch2d: tile_x,tile_y,blocks_per_sm,solver_threads instead of running the autotuner")
+                    help="batch2d: tile_x,tile_y,blocks_per_sm,solver_threads[,solver_cluster] instead of running the autotuner")
     a = ap.parse_args()
     if a.size is None:
         a.size = 128 if a.workload == "dam2d" else 256
@@ -483,9 +483,10 @@ def run_batch2d(a):
         B.update(1)
     B.synchronize()
     if a.batch_tuning:
-        tx, ty, bps, th = (int(v) for v in a.batch_tuning.split(","))
+        vals = [int(v) for v in a.batch_tuning.split(",")]
         tune = B.tuning()
-        tune.tile_x, tune.tile_y, tune.blocks_per_sm, tune.solver_threads = tx, ty, bps, th
+        tune.tile_x, tune.tile_y, tune.blocks_per_sm, tune.solver_threads = vals[:4]
+        tune.solver_cluster = vals[4] if len(vals) > 4 else 1
         B.set_tuning(tune)
         tune.ms_per_step = 0.0
     else:

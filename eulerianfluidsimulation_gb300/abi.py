@@ -39,6 +39,12 @@ FIELD_NAMES = ("vel", "rho", "gamma", "beta", "divergence", "pressure", "forces"
 VECTOR_FIELDS = (FIELD_VEL, FIELD_FORCES)
 
 EFS_OK = 0
+EFS_ERR_ARG = 1
+EFS_ERR_CUDA = 2
+EFS_ERR_STATE = 3
+EFS_ERR_NO_DEVICE = 4
+EFS_ERR_DEVICE_FAULT = 5
+EFS_ERR_NOT_CONVERGED = 6
 STATUS_NAMES = {0: "EFS_OK", 1: "EFS_ERR_ARG", 2: "EFS_ERR_CUDA", 3: "EFS_ERR_STATE", 4: "EFS_ERR_NO_DEVICE",
                 5: "EFS_ERR_DEVICE_FAULT", 6: "EFS_ERR_NOT_CONVERGED"}
 
@@ -103,6 +109,7 @@ class EfsBatchTuning(ctypes.Structure):
         ("tile_y", ctypes.c_int),
         ("blocks_per_sm", ctypes.c_int),
         ("solver_threads", ctypes.c_int),
+        ("solver_cluster", ctypes.c_int),
         ("ms_per_step", ctypes.c_float),
     ]
 

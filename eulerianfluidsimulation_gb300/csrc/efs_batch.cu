@@ -17,7 +17,11 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "efs_batch.h"
+
+namespace cg = cooperative_groups;
 
 using namespace efs;
 
@@ -38,7 +42,9 @@ struct efs_batch {
     BEntry* d_tab[5] = {};
     int ntab[5] = {};
     // tuning
-    int bx = 32, by = 8, bps = 4, cg_threads = 512;
+    int bx = 32, by = 8, bps = 4, cg_threads = 512, cg_cluster = 1;
+    int cg_clusters_max = 0;           // co-resident clusters of k_batch_cg_cluster at the current tuning
+    unsigned* fetch = nullptr;         // k_batch_cg*: next scene
     cudaGraphExec_t graph = nullptr;
     cudaGraph_t graph_def = nullptr;
     unsigned graph_stages = 0;
@@ -143,140 +149,236 @@ struct BCGArgs {
     float *r, *d, *t, *e;
     int max_steps;
     float tol_rel, solver_threshold;
+    unsigned* fetch;      // next scene to take (reset to 0 before every launch)
 };
 
-__global__ void k_batch_cg(BCGArgs A) {
-    for (int k = blockIdx.x; k < A.n; k += gridDim.x) {
-        const int s = A.order[k];
-        const BScene S = A.sc[s];
-        const long long o = S.base;
-        const int N = S.g.N, W = S.g.W;
-        const float* b = A.F.div + o;
-        const uint16_t* info = A.F.rowinfo + o;
-        float* p = A.F.p + o;
-        double* p64 = A.p64 + o;
-        float *r = A.r + o, *d = A.d + o, *t = A.t + o, *e = A.e + o;
-        DevCtl* ctl = A.F.sctl + s;
-        // r = b - L p0 with p0 = b (CGSolver.cpp:63-72), in FP64; d = r
-        BSum rr_p, bb_p, rows_p;
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            const float bi = b[i];
-            bb_p.add_prod(bi, bi);
-            const uint16_t f = info[i];
-            if (!(f & 0x8000u)) continue;
-            rows_p.add(1.f);
-            p64[i] = (double)bi;
-            e[i] = 0.f;
-            const float ri = (float)((double)bi - lap2_d(b, f, i, W));
-            r[i] = ri;
-            d[i] = ri;
-            rr_p.add_prod(ri, ri);
-        }
-        double rr, bb, rows;
-        block_reduce3(rr_p, bb_p, rows_p, rr, bb, rows);
-        float thr_f = A.tol_rel > 0 ? (float)((double)A.tol_rel * (double)A.tol_rel * bb) : A.solver_threshold;
-        if (A.tol_rel > 0 && !(thr_f > 0)) thr_f = FLT_MIN;
-        const double thr = (double)thr_f;
-        // true residual: fold e into p64, r = b - L p64 in FP64 (CGSolver.cpp:46-50)
-        auto replace = [&](double& rr_out) {
-            for (int i = threadIdx.x; i < N; i += blockDim.x) {
-                if (!(info[i] & 0x8000u)) continue;
-                p64[i] += (double)e[i];
-                e[i] = 0.f;
-            }
-            __syncthreads();
-            BSum rp;
-            for (int i = threadIdx.x; i < N; i += blockDim.x) {
-                const uint16_t f = info[i];
-                if (!(f & 0x8000u)) continue;
-                const float ri = (float)((double)b[i] - lap2_d(p64, f, i, W));
-                r[i] = ri;
-                rp.add_prod(ri, ri);
-            }
-            double u1, u2;
-            block_reduce3(rp, BSum(), BSum(), rr_out, u1, u2);
-        };
-        int conv = rr < thr, it = 0;
-        if (!conv) {
-            for (it = 0; it < A.max_steps; it++) {
-                BSum dtp, ttp;
-                for (int i = threadIdx.x; i < N; i += blockDim.x) {
-                    const uint16_t f = info[i];
-                    if (!(f & 0x8000u)) continue;
-                    const float ti = lap2_f(d, f, i, W);
-                    t[i] = ti;
-                    dtp.add_prod(d[i], ti);
-                    ttp.add_prod(ti, ti);
-                }
-                double dt, tt, u3;
-                block_reduce3(dtp, ttp, BSum(), dt, tt, u3);
-                if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown (singular block): not converged
-                const double ad = rr / dt;
-                const float alpha = (float)ad;
-                const double old = rr;
-                const double est = ad * ad * tt - rr;            // r'.r' from the CG recurrence
-                bool replaced = false;
-                if ((it & 0x3F) && est > 0.0) {
-                    const float beta = (float)(est / rr);
-                    BSum rp;
-                    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-                        if (!(info[i] & 0x8000u)) continue;
-                        const float di = d[i];
-                        e[i] += alpha * di;
-                        const float rn = r[i] + (-alpha) * t[i];
-                        r[i] = rn;
-                        d[i] = di * beta + rn;
-                        rp.add_prod(rn, rn);
-                    }
-                    double u1, u2;
-                    block_reduce3(rp, BSum(), BSum(), rr, u1, u2);
-                } else {
-                    for (int i = threadIdx.x; i < N; i += blockDim.x)
-                        if (info[i] & 0x8000u) e[i] += alpha * d[i];
-                    __syncthreads();
-                    replace(rr);
-                    replaced = true;
-                    const float beta = (float)(rr / old);
-                    for (int i = threadIdx.x; i < N; i += blockDim.x)
-                        if (info[i] & 0x8000u) d[i] = d[i] * beta + r[i];
-                    __syncthreads();
-                }
-                if (rr < thr) {
-                    if (!replaced) {
-                        replace(rr);
-                        // d was formed from the recurrence residual: restart it from the recomputed one
-                        if (!(rr < thr)) {
-                            for (int i = threadIdx.x; i < N; i += blockDim.x)
-                                if (info[i] & 0x8000u) d[i] = r[i];
-                            __syncthreads();
-                        }
-                    }
-                    if (rr < thr) { conv = 1; break; }
-                }
-            }
-            it = min(it + 1, A.max_steps);
-        }
-        // p = p64 + e (FP64 accumulator folded), rows only
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            if (!(info[i] & 0x8000u)) continue;
-            const double v = p64[i] + (double)e[i];
-            p64[i] = v;
-            e[i] = 0.f;
-            p[i] = (float)v;
-        }
+// The threads that solve one scene: one block, or the CTAs of one thread-block cluster.  A pass that reads
+// stencil neighbours written by another thread of the group is preceded by sync(); reduce3 returns the same
+// group totals to every thread (block partials added in rank order).
+struct BlockGroup {
+    __device__ __forceinline__ int rank() const { return 0; }
+    __device__ __forceinline__ int ranks() const { return 1; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z) {
+        block_reduce3(a, b, c, x, y, z);
+    }
+    __device__ __forceinline__ int next_scene(unsigned* fetch) {
+        __shared__ int s_k;
+        if (threadIdx.x == 0) s_k = (int)atomicAdd(fetch, 1u);
+        __syncthreads();
+        const int k = s_k;
+        __syncthreads();
+        return k;
+    }
+    __device__ __forceinline__ void finish() const {}
+};
+
+struct ClusterGroup {
+    double* slots;        // this CTA's shared memory: 2 x 3 doubles (alternating per reduction)
+    int* next;            // this CTA's shared memory: 2 ints (alternating per fetch)
+    int parity = 0, fparity = 0;
+    __device__ __forceinline__ int rank() const { return (int)cg::this_cluster().block_rank(); }
+    __device__ __forceinline__ int ranks() const { return (int)cg::this_cluster().num_blocks(); }
+    __device__ __forceinline__ void sync() const { cg::this_cluster().sync(); }
+    __device__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z) {
+        __shared__ double tot[3];
+        double bx, by, bz;
+        block_reduce3(a, b, c, bx, by, bz);
+        cg::cluster_group cl = cg::this_cluster();
         if (threadIdx.x == 0) {
-            ctl->converged = conv;
-            ctl->iterations = it;
-            ctl->rr = rr;
-            ctl->bb = bb;
-            ctl->thr = thr;
-            ctl->active_cells = (long long)rows;
-            ctl->total_iterations += it;
-            ctl->solves += 1;
-            ctl->precond_iterations = 0;
+            slots[3 * parity] = bx;
+            slots[3 * parity + 1] = by;
+            slots[3 * parity + 2] = bz;
+        }
+        cl.sync();
+        if (threadIdx.x == 0) {
+            double X = 0.0, Y = 0.0, Z = 0.0;
+            const int n = (int)cl.num_blocks();
+            for (int r = 0; r < n; r++) {
+                const double* rs = cl.map_shared_rank(slots + 3 * parity, r);
+                X += rs[0];
+                Y += rs[1];
+                Z += rs[2];
+            }
+            tot[0] = X; tot[1] = Y; tot[2] = Z;
         }
         __syncthreads();
+        x = tot[0]; y = tot[1]; z = tot[2];
+        parity ^= 1;
+        __syncthreads();
     }
+    // The slot written at one reduction (fetch) is written again two reductions (fetches) later, after a
+    // cluster barrier that every CTA reaches only once it has read the slot.
+    __device__ int next_scene(unsigned* fetch) {
+        cg::cluster_group cl = cg::this_cluster();
+        if (cl.block_rank() == 0 && threadIdx.x == 0) next[fparity] = (int)atomicAdd(fetch, 1u);
+        cl.sync();
+        const int k = *cl.map_shared_rank(next + fparity, 0);
+        fparity ^= 1;
+        return k;
+    }
+    // no CTA leaves while another may still read its shared memory
+    __device__ __forceinline__ void finish() const { cg::this_cluster().sync(); }
+};
+
+// Block-level CG (EFS_CG_MIXED_RECURRENCE) of one scene by group G (CGSolver.cpp:32-83 with the mixed precision
+// and recurrence of the persistent solver; see efs_gb300.h).
+template <class G>
+__device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
+    const BScene S = A.sc[s];
+    const long long o = S.base;
+    const int N = S.g.N, W = S.g.W;
+    const float* b = A.F.div + o;
+    const uint16_t* info = A.F.rowinfo + o;
+    float* p = A.F.p + o;
+    double* p64 = A.p64 + o;
+    float *r = A.r + o, *d = A.d + o, *t = A.t + o, *e = A.e + o;
+    DevCtl* ctl = A.F.sctl + s;
+    const int i0 = grp.rank() * blockDim.x + threadIdx.x, stride = grp.ranks() * blockDim.x;
+    // r = b - L p0 with p0 = b (CGSolver.cpp:63-72), in FP64; d = r
+    BSum rr_p, bb_p, rows_p;
+    for (int i = i0; i < N; i += stride) {
+        const float bi = b[i];
+        bb_p.add_prod(bi, bi);
+        const uint16_t f = info[i];
+        if (!(f & 0x8000u)) continue;
+        rows_p.add(1.f);
+        p64[i] = (double)bi;
+        e[i] = 0.f;
+        const float ri = (float)((double)bi - lap2_d(b, f, i, W));
+        r[i] = ri;
+        d[i] = ri;
+        rr_p.add_prod(ri, ri);
+    }
+    double rr, bb, rows;
+    grp.reduce3(rr_p, bb_p, rows_p, rr, bb, rows);
+    float thr_f = A.tol_rel > 0 ? (float)((double)A.tol_rel * (double)A.tol_rel * bb) : A.solver_threshold;
+    if (A.tol_rel > 0 && !(thr_f > 0)) thr_f = FLT_MIN;
+    const double thr = (double)thr_f;
+    // true residual: fold e into p64, r = b - L p64 in FP64 (CGSolver.cpp:46-50)
+    auto replace = [&](double& rr_out) {
+        for (int i = i0; i < N; i += stride) {
+            if (!(info[i] & 0x8000u)) continue;
+            p64[i] += (double)e[i];
+            e[i] = 0.f;
+        }
+        grp.sync();
+        BSum rp;
+        for (int i = i0; i < N; i += stride) {
+            const uint16_t f = info[i];
+            if (!(f & 0x8000u)) continue;
+            const float ri = (float)((double)b[i] - lap2_d(p64, f, i, W));
+            r[i] = ri;
+            rp.add_prod(ri, ri);
+        }
+        double u1, u2;
+        grp.reduce3(rp, BSum(), BSum(), rr_out, u1, u2);
+    };
+    int conv = rr < thr, it = 0;
+    if (!conv) {
+        for (it = 0; it < A.max_steps; it++) {
+            BSum dtp, ttp;
+            for (int i = i0; i < N; i += stride) {
+                const uint16_t f = info[i];
+                if (!(f & 0x8000u)) continue;
+                const float ti = lap2_f(d, f, i, W);
+                t[i] = ti;
+                dtp.add_prod(d[i], ti);
+                ttp.add_prod(ti, ti);
+            }
+            double dt, tt, u3;
+            grp.reduce3(dtp, ttp, BSum(), dt, tt, u3);
+            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown (singular block): not converged
+            const double ad = rr / dt;
+            const float alpha = (float)ad;
+            const double old = rr;
+            const double est = ad * ad * tt - rr;            // r'.r' from the CG recurrence
+            bool replaced = false;
+            if ((it & 0x3F) && est > 0.0) {
+                const float beta = (float)(est / rr);
+                BSum rp;
+                for (int i = i0; i < N; i += stride) {
+                    if (!(info[i] & 0x8000u)) continue;
+                    const float di = d[i];
+                    e[i] += alpha * di;
+                    const float rn = r[i] + (-alpha) * t[i];
+                    r[i] = rn;
+                    d[i] = di * beta + rn;
+                    rp.add_prod(rn, rn);
+                }
+                double u1, u2;
+                grp.reduce3(rp, BSum(), BSum(), rr, u1, u2);
+            } else {
+                for (int i = i0; i < N; i += stride)
+                    if (info[i] & 0x8000u) e[i] += alpha * d[i];
+                grp.sync();
+                replace(rr);
+                replaced = true;
+                const float beta = (float)(rr / old);
+                for (int i = i0; i < N; i += stride)
+                    if (info[i] & 0x8000u) d[i] = d[i] * beta + r[i];
+                grp.sync();
+            }
+            if (rr < thr) {
+                if (!replaced) {
+                    replace(rr);
+                    // d was formed from the recurrence residual: restart it from the recomputed one
+                    if (!(rr < thr)) {
+                        for (int i = i0; i < N; i += stride)
+                            if (info[i] & 0x8000u) d[i] = r[i];
+                        grp.sync();
+                    }
+                }
+                if (rr < thr) { conv = 1; break; }
+            }
+        }
+        it = min(it + 1, A.max_steps);
+    }
+    // p = p64 + e (FP64 accumulator folded), rows only
+    for (int i = i0; i < N; i += stride) {
+        if (!(info[i] & 0x8000u)) continue;
+        const double v = p64[i] + (double)e[i];
+        p64[i] = v;
+        e[i] = 0.f;
+        p[i] = (float)v;
+    }
+    if (grp.rank() == 0 && threadIdx.x == 0) {
+        ctl->converged = conv;
+        ctl->iterations = it;
+        ctl->rr = rr;
+        ctl->bb = bb;
+        ctl->thr = thr;
+        ctl->active_cells = (long long)rows;
+        ctl->total_iterations += it;
+        ctl->solves += 1;
+        ctl->precond_iterations = 0;
+    }
+    grp.sync();
+}
+
+// One block per scene; blocks take scenes largest first.
+__global__ void __launch_bounds__(1024) k_batch_cg(BCGArgs A) {
+    BlockGroup grp;
+    for (;;) {
+        const int k = grp.next_scene(A.fetch);
+        if (k >= A.n) break;
+        solve_scene(A, A.order[k], grp);
+    }
+}
+
+// One thread-block cluster per scene; clusters take scenes largest first.
+__global__ void __launch_bounds__(1024) k_batch_cg_cluster(BCGArgs A) {
+    __shared__ double slots[6];
+    __shared__ int next[2];
+    ClusterGroup grp;
+    grp.slots = slots;
+    grp.next = next;
+    for (;;) {
+        const int k = grp.next_scene(A.fetch);
+        if (k >= A.n) break;
+        solve_scene(A, A.order[k], grp);
+    }
+    grp.finish();
 }
 
 // ---- host side --------------------------------------------------------------------------------------------
@@ -347,9 +449,27 @@ cudaError_t launch_cg(const efs_batch* b) {
     A.max_steps = b->prm.max_steps;
     A.tol_rel = b->prm.tol_rel;
     A.solver_threshold = b->prm.solver_threshold;
-    const int grid = std::min(b->n, b->sm_count * (1024 / b->cg_threads));
-    k_batch_cg<<<std::max(1, grid), b->cg_threads, 0, b->stream>>>(A);
-    return cudaGetLastError();
+    A.fetch = b->fetch;
+    cudaError_t e = cudaMemsetAsync(b->fetch, 0, sizeof(unsigned), b->stream);
+    if (e != cudaSuccess) return e;
+    if (b->cg_cluster <= 1) {
+        const int grid = std::min(b->n, b->sm_count * (1024 / b->cg_threads));
+        k_batch_cg<<<std::max(1, grid), b->cg_threads, 0, b->stream>>>(A);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)b->cg_cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(b->cg_cluster * std::max(1, std::min(b->n, b->cg_clusters_max))));
+    cfg.blockDim = dim3((unsigned)b->cg_threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = b->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_batch_cg_cluster, A);
 }
 
 cudaError_t enqueue_stage(const efs_batch* b, int stage, bool fuse) {
@@ -498,7 +618,7 @@ int efs_batch_create(int n_scenes, const int* widths, const int* heights, const 
     BA(F.wb, 4 * T); BA(F.wf, 4 * T); BA(F.bb, T); BA(F.fb, T); BA(F.bsum, T); BA(F.gsum, T); BA(F.rho_acc, T);
     BA(F.sh_idx, T); BA(F.sh_sid, T); BA(F.sh_val, T); BA(F.sh_end, 3 * T);
     BA(F.rowinfo, T); BA(F.chunk_flag, T / 32 + 1); BA(F.ctl, 1); BA(F.sctl, n_scenes);
-    BA(b->p64, T); BA(b->r, T); BA(b->d, T); BA(b->t, T); BA(b->e, T);
+    BA(b->p64, T); BA(b->r, T); BA(b->d, T); BA(b->t, T); BA(b->e, T); BA(b->fetch, 1);
 #undef BA
     F.list_cap = (int)std::min<long long>(T, 1LL << 30);
     if ((e = cudaMemcpy(b->d_sc, b->sc.data(), n_scenes * sizeof(BScene), cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "upload scenes");
@@ -654,6 +774,7 @@ int efs_batch_get_tuning(const efs_batch* b, efs_batch_tuning* t) {
     t->tile_y = b->by;
     t->blocks_per_sm = b->bps;
     t->solver_threads = b->cg_threads;
+    t->solver_cluster = b->cg_cluster;
     t->ms_per_step = 0.f;
     return EFS_OK;
 }
@@ -662,13 +783,35 @@ int efs_batch_set_tuning(efs_batch* b, const efs_batch_tuning* t) {
     if (!b || !t) return EFS_ERR_ARG;
     if (t->tile_x < 1 || t->tile_y < 1 || t->tile_x * t->tile_y > 1024 || (t->tile_x * t->tile_y) % 32 != 0 ||
         t->blocks_per_sm < 1 || t->blocks_per_sm > 32 ||
-        (t->solver_threads != 128 && t->solver_threads != 256 && t->solver_threads != 512 && t->solver_threads != 1024))
-        return bfail(b, EFS_ERR_ARG, "tile_x * tile_y a multiple of 32 up to 1024; blocks_per_sm 1..32; solver_threads 128..1024 (power of 2)");
+        (t->solver_threads != 128 && t->solver_threads != 256 && t->solver_threads != 512 && t->solver_threads != 1024) ||
+        (t->solver_cluster != 1 && t->solver_cluster != 2 && t->solver_cluster != 4 && t->solver_cluster != 8 &&
+         t->solver_cluster != 16))
+        return bfail(b, EFS_ERR_ARG, "tile_x * tile_y a multiple of 32 up to 1024; blocks_per_sm 1..32; solver_threads "
+                                     "128..1024 (power of 2); solver_cluster 1, 2, 4, 8 or 16");
     BCK(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    int clusters = 0;
+    if (t->solver_cluster > 1) {
+        if (t->solver_cluster > 8)
+            BCK(cudaFuncSetAttribute(k_batch_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1), "cluster size attribute");
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)t->solver_cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)t->solver_cluster);
+        cfg.blockDim = dim3((unsigned)t->solver_threads);
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        BCK(cudaOccupancyMaxActiveClusters(&clusters, k_batch_cg_cluster, &cfg), "cudaOccupancyMaxActiveClusters");
+        if (clusters < 1) return bfail(b, EFS_ERR_ARG, "this solver cluster shape cannot be resident on the device");
+    }
     b->bx = t->tile_x;
     b->by = t->tile_y;
     b->bps = t->blocks_per_sm;
     b->cg_threads = t->solver_threads;
+    b->cg_cluster = t->solver_cluster;
+    b->cg_clusters_max = clusters;
     drop_graph(b);
     return upload_tables(b);
 }
@@ -712,7 +855,7 @@ int efs_batch_autotune(efs_batch* b, int trial_steps, efs_batch_tuning* best_out
         ms /= trial_steps;
         return check_status(b);
     };
-    efs_batch_tuning best{b->bx, b->by, b->bps, b->cg_threads, 0.f};
+    efs_batch_tuning best{b->bx, b->by, b->bps, b->cg_threads, b->cg_cluster, 0.f};
     float best_ms = FLT_MAX;
     int s = trial(best, best_ms);
     if (s != EFS_OK) return s;
@@ -732,12 +875,17 @@ int efs_batch_autotune(efs_batch* b, int trial_steps, efs_batch_tuning* best_out
         if ((s = trial(c, ms)) != EFS_OK) return s;
         if (ms < best_ms) { best_ms = ms; best = c; }
     }
-    for (int th : {256, 512, 1024}) {
-        efs_batch_tuning c = best;
-        c.solver_threads = th;
-        float ms;
-        if ((s = trial(c, ms)) != EFS_OK) return s;
-        if (ms < best_ms) { best_ms = ms; best = c; }
+    for (int cl : {1, 4, 8, 16}) {
+        for (int th : {256, 512, 1024}) {
+            efs_batch_tuning c = best;
+            c.solver_threads = th;
+            c.solver_cluster = cl;
+            float ms;
+            s = trial(c, ms);
+            if (s == EFS_ERR_ARG && cl > 1) continue;      // shape not resident on this device
+            if (s != EFS_OK) return s;
+            if (ms < best_ms) { best_ms = ms; best = c; }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -288,6 +288,8 @@ typedef struct efs_batch_tuning {
     int   tile_x, tile_y;     /* stage-kernel block: tile_x x tile_y cells (product a multiple of 32)   */
     int   blocks_per_sm;      /* persistent blocks per SM of the stage kernels                          */
     int   solver_threads;     /* threads of a solver block (128, 256, 512 or 1024)                      */
+    int   solver_cluster;     /* solver blocks per scene: 1 (one block), or a thread-block cluster of   */
+                              /* 2, 4, 8 or 16 blocks exchanging partial sums in distributed shared mem */
     float ms_per_step;        /* efs_batch_autotune: measured step time of the chosen configuration     */
 } efs_batch_tuning;
 int  efs_batch_create(int n_scenes, const int* widths, const int* heights, const efs_params* params,
@@ -309,7 +311,7 @@ int  efs_batch_stats(efs_batch* batch, int scene, efs_stats* out);
 int  efs_batch_kernel_count(efs_batch* batch, int* count);
 int  efs_batch_get_tuning(const efs_batch* batch, efs_batch_tuning* tuning);
 int  efs_batch_set_tuning(efs_batch* batch, const efs_batch_tuning* tuning);
-/* Times trial steps of candidate tile shapes, blocks per SM and solver block sizes from the current state
+/* Times trial steps of candidate tile shapes, blocks per SM, solver block sizes and solver clusters from the current state
  * (restored after every trial) and keeps the fastest; `best` (may be NULL) receives it. */
 int  efs_batch_autotune(efs_batch* batch, int trial_steps, efs_batch_tuning* best);
 

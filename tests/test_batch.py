@@ -124,3 +124,53 @@ def test_autotune_and_mass():
             assert st.converged and not st.paused
             m = float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64))
             assert abs(m - m0[s]) <= 1e-5 * m0[s], (s, m, m0[s])
+
+
+@pytest.mark.parametrize("cluster,threads", [(4, 256), (8, 512)])
+def test_cluster_solver_matches_the_single_context(cluster, threads):
+    """The pressure solve by a thread-block cluster per scene (partial sums exchanged in distributed shared
+    memory) gives the single-context pressure within the same 1e-5 as one block per scene."""
+    scenes = _scenes([0, 1, 2, 5])
+    with _batch(scenes) as B:
+        t = B.tuning()
+        t.solver_threads, t.solver_cluster = threads, cluster
+        B.set_tuning(t)
+        assert B.tuning().solver_cluster == cluster
+        B.update(3)
+        B.synchronize()
+        singles = []
+        for s in range(B.n):
+            side = B.widths[s]
+            S = gb.GB300Simulator2D(side, side, _params(side))
+            S.set_fields(_state(B, s))
+            singles.append(S)
+        try:
+            for stage in range(abi.STAGE_COUNT):
+                B.stage(stage)
+                for S in singles:
+                    S.stage(stage)
+            for s, S in enumerate(singles):
+                for f in (abi.FIELD_PRESSURE, abi.FIELD_VEL):
+                    assert rel_l2(B.field(s, f), S.field(f)) <= 1e-5, (s, abi.FIELD_NAMES[f])
+                assert B.stats(s).converged
+        finally:
+            for S in singles:
+                S.close()
+        B.update(5)
+        B.synchronize()
+        assert all(B.stats(s).converged for s in range(B.n))
+
+
+def test_cluster_of_16_or_refused():
+    scenes = _scenes([3, 4])
+    with _batch(scenes) as B:
+        t = B.tuning()
+        t.solver_threads, t.solver_cluster = 256, 16
+        try:
+            B.set_tuning(t)
+        except gb.EfsError as e:
+            assert e.status == abi.EFS_ERR_ARG          # not resident on this device
+            return
+        B.update(2)
+        B.synchronize()
+        assert all(B.stats(s).converged for s in range(B.n))
