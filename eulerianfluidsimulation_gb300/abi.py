@@ -25,6 +25,7 @@ CG_MIXED = 0
 CG_REFERENCE = 1
 CG_MIXED_RECURRENCE = 2
 CG_FP64 = 3
+CG_PIPELINED = 4
 
 FIELD_VEL = 0
 FIELD_RHO = 1

@@ -476,31 +476,60 @@ __global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int*
 
 // Step 12: one in-place sweep of pairwise gamma-equalising transfers along one axis
 // (CPUSimulator3D.cpp:277-362).  One thread walks one line sequentially; `stride` is the axis stride,
-// `n` the line length (cells), line start = `first`.
+// `n` the line length (cells), line start = `first`.  Only the carried pair (rho, gamma) of the previous cell
+// depends on earlier steps: every cell is read from memory before this thread writes it, and lines are
+// disjoint, so the loads of the next kPf cells are issued while the current kPf cells are processed.
+constexpr int kPf = 16;
+struct LineBlock {
+    float r[kPf], g[kPf];
+    unsigned solid;   // bit k: cell k of the block is solid
+};
+__device__ __forceinline__ void load_block(LineBlock& b, const float* __restrict__ rsrc, const float* __restrict__ gsrc,
+                                           const uint8_t* __restrict__ solid, int first, int stride, int c0, int last) {
+    b.solid = 0;
+#pragma unroll
+    for (int k = 0; k < kPf; k++) {
+        if (c0 + k <= last) {
+            const int i = first + stride * (c0 + k);
+            b.r[k] = rsrc[i];
+            b.g[k] = gsrc[i];
+            b.solid |= (unsigned)(solid[i] != 0) << k;
+        }
+    }
+}
 __device__ __forceinline__ void diffuse_line(const float* __restrict__ rsrc, const float* __restrict__ gsrc,
                                              float* __restrict__ rdst, float* __restrict__ gdst,
                                              const uint8_t* __restrict__ solid, int first, int stride, int n) {
     // cells first + stride * c for c = 1 .. n-2; pairs (c-1, c) for c = 2 .. n-2
+    const int last = n - 2;
     int jj = first + stride;
     float rj = rsrc[jj], gj = gsrc[jj];
-    uint8_t sj = solid[jj];
-    for (int c = 2; c <= n - 2; c++) {
-        const int ii = jj + stride;
-        float ri = rsrc[ii], gi = gsrc[ii];
-        const uint8_t si = solid[ii];
-        if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
-            const float avg = (gj + gi) / 2.f;
-            if (gj > gi) {
-                const float dif = rj * (gj - gi) / (2.f * gj);
-                rj -= dif; ri += dif;
-            } else {
-                const float dif = ri * (gi - gj) / (2.f * gi);
-                ri -= dif; rj += dif;
+    bool sj = solid[jj] != 0;
+    LineBlock cur, nxt;
+    load_block(cur, rsrc, gsrc, solid, first, stride, 2, last);
+    for (int c0 = 2; c0 <= last; c0 += kPf) {
+        load_block(nxt, rsrc, gsrc, solid, first, stride, c0 + kPf, last);
+#pragma unroll
+        for (int k = 0; k < kPf; k++) {
+            if (c0 + k > last) break;
+            const int ii = jj + stride;
+            float ri = cur.r[k], gi = cur.g[k];
+            const bool si = (cur.solid >> k) & 1u;
+            if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
+                const float avg = (gj + gi) / 2.f;
+                if (gj > gi) {
+                    const float dif = rj * (gj - gi) / (2.f * gj);
+                    rj -= dif; ri += dif;
+                } else {
+                    const float dif = ri * (gi - gj) / (2.f * gi);
+                    ri -= dif; rj += dif;
+                }
+                gj = avg; gi = avg;
             }
-            gj = avg; gi = avg;
+            rdst[jj] = rj; gdst[jj] = gj;
+            jj = ii; rj = ri; gj = gi; sj = si;
         }
-        rdst[jj] = rj; gdst[jj] = gj;
-        jj = ii; rj = ri; gj = gi; sj = si;
+        cur = nxt;
     }
     if (n >= 3) { rdst[jj] = rj; gdst[jj] = gj; }
 }

@@ -13,6 +13,7 @@
 // again) for its own MMAs, frees its TMEM and returns.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 namespace efs {
@@ -381,6 +382,176 @@ __global__ void __launch_bounds__(kConvThreads) k_wgrad3_tc(WgradArgs a) {
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+// ---- TMA and bulk copies ------------------------------------------------------------------------------------
+// The arrival of this thread plus `bytes` of expected transaction count on the mbarrier.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Tiled 4D tensor load (box of the tensor map) into shared memory; elements outside the tensor read as zero.
+// The innermost coordinate c0 is always 0 here (whole 16-byte channel groups).
+__device__ __forceinline__ void tma_load_4d(void* sdst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        ::"r"(smem_u32(sdst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+// Contiguous global -> shared copy (addresses and size multiples of 16 bytes).
+__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// ============================================================================================================
+// Halo-tile 3x3x3 convolution: the same function as k_conv3_tc, for grids at least one tile wide.
+// A CTA computes kHaloRows output rows (2 in y x 2 in z) of one 128-voxel segment along x.  Per 16 input
+// channels it loads, with two TMA tensor copies (one per 8-channel group), the input box of
+// 130 x 4 x 4 voxels that covers those rows and their one-voxel halo (zero outside the grid), and with one
+// bulk copy the 27 weight tiles of those channels.  Every tap of every row is then one tcgen05.mma whose A
+// operand starts at the tap's shifted voxel inside the box: shared memory holds each channel group as
+// [z][y][x][8 channels], so 8 consecutive x voxels of one group are one 128-byte core matrix (SBO 128 B
+// between voxel groups, LBO = one group plane between the two K halves).  Each input voxel is staged once
+// per CTA instead of once per tap.  Row r accumulates in TMEM columns [r * COUT, (r + 1) * COUT).
+// ============================================================================================================
+constexpr int kHaloSeg = 128, kHaloX = kHaloSeg + 2, kHaloRY = 2, kHaloRZ = 2, kHaloRows = kHaloRY * kHaloRZ;
+constexpr int kHaloBoxY = kHaloRY + 2, kHaloBoxZ = kHaloRZ + 2;
+constexpr int kHaloPlane = 16 * kHaloX * kHaloBoxY * kHaloBoxZ;     // bytes of one 8-channel group box
+constexpr int kHaloMaxGroups = 8;                                    // cin <= 64
+
+struct HaloArgs {
+    CUtensorMap map[kHaloMaxGroups];   // input group g: dims (8 channels, W, H, D), base in + 8 g
+    const __nv_bfloat16* wh;           // [cin/16][27][COUT x 16 in the K-major core-matrix order]
+    const float* bias;
+    const __nv_bfloat16* skip;
+    __nv_bfloat16* out;
+    float* out32;
+    __nv_bfloat16* pre;
+    int D, H, W, cin;
+    int relu;
+    int* err;
+};
+
+template <int COUT>
+constexpr int halo_smem_bytes() { return 2 * kHaloPlane + 27 * COUT * 32 + 64; }
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvThreads) k_conv3_halo(const __grid_constant__ HaloArgs a) {
+    static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
+    constexpr int kWBytes = 27 * COUT * 32;
+    constexpr uint32_t kCols = kHaloRows * COUT;      // 64, 128 or 256
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* box = smem;                        // 2 group planes (128-byte aligned)
+    unsigned char* wts = smem + 2 * kHaloPlane;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(wts + kWBytes);   // [0] loads, [1] MMAs
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int x0 = blockIdx.x * kHaloSeg, y0 = blockIdx.y * kHaloRY, z0 = blockIdx.z * kHaloRZ;
+    const int chunks = a.cin >> 4;
+
+    if (warp == 0) tmem_alloc(tslot, kCols);
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    // thread 0 stages and issues; its outcome reaches the block through shared memory
+    __shared__ int s_ok;
+    if (tid == 0) {
+        int ok = 1;
+        for (int c = 0; c < chunks && ok; c++) {
+            // the previous chunk's MMAs read the box and weights: wait before overwriting them
+            if (c > 0 && !mbar_wait(&mbar[1], (c - 1) & 1)) { ok = 0; break; }
+            mbar_expect_tx(&mbar[0], 2 * kHaloPlane + kWBytes);
+            tma_load_4d(box, &a.map[2 * c], 0, x0 - 1, y0 - 1, z0 - 1, &mbar[0]);
+            tma_load_4d(box + kHaloPlane, &a.map[2 * c + 1], 0, x0 - 1, y0 - 1, z0 - 1, &mbar[0]);
+            bulk_load(wts, a.wh + (size_t)c * 27 * COUT * 16, kWBytes, &mbar[0]);
+            if (!mbar_wait(&mbar[0], c & 1)) { ok = 0; break; }
+            tc_fence_after();
+            const uint32_t sbox = smem_u32(box), swts = smem_u32(wts);
+#pragma unroll 1
+            for (int r = 0; r < kHaloRows; r++) {
+                const int ry = r % kHaloRY, rz = r / kHaloRY;
+#pragma unroll 1
+                for (int tap = 0; tap < 27; tap++) {
+                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;      // offsets + 1
+                    const uint32_t off = (uint32_t)((((rz + dz) * kHaloBoxY + (ry + dy)) * kHaloX + dx) * 16);
+                    const uint64_t ad = sdesc(sbox + off, (uint32_t)kHaloPlane, 128);
+                    const uint64_t bd = sdesc(swts + (uint32_t)(tap * COUT * 32), 128, 256);
+                    mma_bf16(tmem + (uint32_t)(r * COUT), ad, bd, idesc_bf16(128, COUT), (c > 0 || tap > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(&mbar[1]);
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    bool ok = s_ok != 0;
+    const int last = chunks - 1;
+    if (ok && !mbar_wait(&mbar[1], last & 1)) ok = false;
+    if (!ok) {
+        if (tid == 0) atomicOr(a.err, 1);
+        mbar_wait(&mbar[1], last & 1);     // bounded: let MMAs in flight finish before freeing TMEM
+    }
+    tc_fence_after();
+    if (ok) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        const int x = x0 + tid;
+#pragma unroll 1
+        for (int r = 0; r < kHaloRows; r++) {
+            const int y = y0 + r % kHaloRY, z = z0 + r / kHaloRY;
+            const bool vin = x < a.W && y < a.H && z < a.D;
+            const size_t v = ((size_t)z * a.H + y) * a.W + x;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                float acc[16];
+                tmem_ld16(tmem + lane_base + (uint32_t)(r * COUT + c0), acc);
+                if (vin) {
+                    __align__(16) __nv_bfloat16 o[16], pr[16];
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
+                        pr[j] = __float2bfloat16(t);
+                        if (a.relu) t = fmaxf(t, 0.f);
+                        if (a.skip) t += __bfloat162float(a.skip[v * COUT + c0 + j]);
+                        o[j] = __float2bfloat16(t);
+                        if (a.out32) a.out32[v * COUT + c0 + j] = t;
+                    }
+                    if (a.out) {
+                        uint4* dst = reinterpret_cast<uint4*>(a.out + v * COUT + c0);
+                        dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                        dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                    }
+                    if (a.pre) {
+                        uint4* dst = reinterpret_cast<uint4*>(a.pre + v * COUT + c0);
+                        dst[0] = reinterpret_cast<const uint4*>(pr)[0];
+                        dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+// Weights wt[tap][cin/16][cout][16] (the k_conv3_tc layout) -> wh[cin/16][27][core-matrix tile of cout x 16].
+__global__ void k_pack_halo_weights(const __nv_bfloat16* __restrict__ wt, int cin, int cout, __nv_bfloat16* __restrict__ wh) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 27 * cin * cout) return;
+    const int chunks = cin >> 4;
+    const int k = i & 15, n = (i >> 4) % cout, cc = (i / (16 * cout)) % chunks, tap = i / (16 * cout * chunks);
+    const size_t dst = ((size_t)cc * 27 + tap) * cout * 16 + tile_off(n, k) / 2;
+    wh[dst] = wt[i];
 }
 
 }  // namespace tc

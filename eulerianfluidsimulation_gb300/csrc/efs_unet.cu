@@ -22,6 +22,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "efs_internal.h"
 #include "efs_tc.cuh"
 
@@ -56,6 +58,7 @@ struct UNetState {
     float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
     int adam_t = 0;
     bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
+    bf16* wh = nullptr;          // weights of the convolution in flight, packed for k_conv3_halo
     // activations (level of each in brackets)
     bf16 *x0 = nullptr, *e0 = nullptr, *p0 = nullptr, *e1 = nullptr, *p1 = nullptr, *e2 = nullptr, *u2 = nullptr,
          *d1 = nullptr, *u1 = nullptr, *d0 = nullptr;
@@ -562,9 +565,73 @@ Off6 offsets(const efs_ctx* c) {
     return Off6{{-1, 1, -W, W, c->dim == 3 ? -WH : 0, c->dim == 3 ? WH : 0}};
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (no link against the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// Grids this wide or wider use the halo-tile convolution (a CTA covers 128 voxels along x).
+constexpr int kHaloMinWidth = 96;
+
+template <int COUT>
+cudaError_t launch_halo(const tc::HaloArgs& a, int W, int H, int D, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(tc::k_conv3_halo<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tc::halo_smem_bytes<COUT>());
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const dim3 grid((unsigned)((W + tc::kHaloSeg - 1) / tc::kHaloSeg), (unsigned)((H + tc::kHaloRY - 1) / tc::kHaloRY),
+                    (unsigned)((D + tc::kHaloRZ - 1) / tc::kHaloRZ));
+    tc::k_conv3_halo<COUT><<<grid, tc::kConvThreads, tc::halo_smem_bytes<COUT>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t conv_halo(UNetState* u, const bf16* in, const bf16* wt, int cin, int cout, const Level& L, const float* bias,
+                      const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st) {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const int n = 27 * cin * cout;
+    tc::k_pack_halo_weights<<<nblk(n), 256, 0, st>>>(wt, cin, cout, u->wh);
+    const cudaError_t pe = cudaGetLastError();
+    if (pe != cudaSuccess) return pe;
+    tc::HaloArgs a;
+    std::memset(&a, 0, sizeof(a));
+    // input channel group g: (8 channels, W, H, D) at in + 8 g; strides in bytes include the channel padding
+    const cuuint64_t dims[4] = {8, (cuuint64_t)L.W, (cuuint64_t)L.H, (cuuint64_t)L.D};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)L.W * cin * 2, (cuuint64_t)L.H * L.W * cin * 2};
+    const cuuint32_t boxd[4] = {8, (cuuint32_t)tc::kHaloX, (cuuint32_t)tc::kHaloBoxY, (cuuint32_t)tc::kHaloBoxZ};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    for (int g = 0; g < cin / 8; g++) {
+        const CUresult r = encode(&a.map[g], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)(in + 8 * g), dims, strides, boxd,
+                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    }
+    a.wh = u->wh;
+    a.bias = bias; a.skip = skip; a.out = out; a.out32 = out32; a.pre = pre;
+    a.D = L.D; a.H = L.H; a.W = L.W; a.cin = cin; a.relu = relu; a.err = u->err;
+    if (cout == 16) return launch_halo<16>(a, L.W, L.H, L.D, st);
+    if (cout == 32) return launch_halo<32>(a, L.W, L.H, L.D, st);
+    return launch_halo<64>(a, L.W, L.H, L.D, st);
+}
+
 cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
                  const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st) {
     const Level& L = u->L[level];
+    if (L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64)
+        return conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st);
     tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err};
     const unsigned grid = (unsigned)((L.V + 127) / 128);
     (void)layer;
@@ -780,6 +847,7 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
         UCK(ualloc(u, &u->wf[k], 27LL * kSpec[k].cin * kSpec[k].cout));
         UCK(ualloc(u, &u->wb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
     }
+    UCK(ualloc(u, &u->wh, 27LL * 64 * 64));
     UCK(ualloc(u, &u->x0, L[0].V * 16));
     UCK(ualloc(u, &u->e0, L[0].V * 16));
     UCK(ualloc(u, &u->p0, L[1].V * 16));

@@ -90,7 +90,13 @@ enum efs_cg_variant {
      * the threshold tol_rel^2 b.b kept in FP64 (set tol_rel to 1e-12 or so): the FP64 pressure solve of the
      * same right-hand side that the FP32 results are measured against.  Its FP64 vectors are allocated when
      * a context first selects it. */
-    EFS_CG_FP64 = 3
+    EFS_CG_FP64 = 3,
+    /* EFS_CG_PIPELINED: pipelined CG (Ghysels and Vanroose 2014) with the FP64 accumulator and FP64 residual
+     * replacement of EFS_CG_MIXED: w = L r, s = L p and z = L s are carried by recurrences, so one sweep per
+     * iteration computes q = L w, updates every vector and sums the next iteration's r.r and w.r; on the GPU
+     * that is one pass and one grid reduction per iteration.  Every 64th iteration, and before stopping,
+     * r is recomputed in FP64 and w, s, z from r and p. */
+    EFS_CG_PIPELINED = 4
 };
 
 /* ---- fields (IGrid3D accessors, IGrid.h:44-68) ---- */

@@ -854,8 +854,81 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
     return ((float)rr > thr) ? (float)rr : nextafterf(thr, INFINITY);
 }
 
+/* EFS_CG_PIPELINED: pipelined CG (P. Ghysels and W. Vanroose, Parallel Computing 40, 2014, Alg. 4) on the same
+ * matrix and start (p0 = b), with the pressure held as p64 + e as in cg_solve_mixed.  Auxiliary vectors
+ * w = L r, s = L p, z = L s are carried by recurrences, so that one sweep per iteration computes q = L w and
+ * updates z, s, p, e, r, w, and the two dot products gamma = r.r and delta = w.r of the next iteration:
+ *   beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old)   (beta = 0 at a restart)
+ *   z = q + beta z; s = w + beta s; p = r + beta p; e += alpha p; r -= alpha s; w -= alpha z.
+ * Every 64th iteration, and before stopping, the residual is recomputed in FP64 from p64 and w, s, z are
+ * recomputed from r and p (residual replacement, S. Cools et al., SIAM J. Sci. Comput. 40, 2018); a stop test
+ * that the recomputed residual does not confirm restarts the recurrences (beta = 0). */
+static float cg_solve_pipelined(orc_grid* g, float thr) {
+    const size_t N = g->N;
+    float *r = g->cg_r, *e = g->jac_tmp;
+    const float* b = g->div;
+    const int steps = g->prm.max_steps;
+    float* w = (float*)calloc(N, 4);
+    float* p = (float*)calloc(N, 4);
+    float* s = (float*)calloc(N, 4);
+    float* z = (float*)calloc(N, 4);
+    float* q = (float*)calloc(N, 4);
+    double* p64 = (double*)malloc(N * sizeof(double));
+    double* t64 = (double*)malloc(N * sizeof(double));
+    double gamma = 0, delta = 0;
+    #define ORC_PREPLACE() do { \
+        for (size_t c = 0; c < N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
+        matmul_d(g, t64, p64); \
+        for (size_t c = 0; c < N; c++) r[c] = (float)((double)b[c] - t64[c]); \
+        matmul(g, w, r); matmul(g, s, p); matmul(g, z, s); \
+        gamma = ddot(g, r, r); delta = ddot(g, w, r); \
+    } while (0)
+    for (size_t c = 0; c < N; c++) { p64[c] = (double)b[c]; e[c] = 0.f; }
+    ORC_PREPLACE();
+    g->solve_steps = 0;
+    int conv = gamma < (double)thr;
+    if (!conv) {
+        int i, restart = 1;
+        double gamma_old = 0, alpha_old = 0;
+        for (i = 0; i < steps; i++) {
+            double alpha, beta;
+            if (restart) { beta = 0.0; alpha = gamma / delta; }
+            else { beta = gamma / gamma_old; alpha = gamma / (delta - beta * gamma / alpha_old); }
+            if (!isfinite(alpha) || alpha == 0.0) break;    /* breakdown: stop, not converged */
+            const float a = (float)alpha, bt = (float)beta;
+            matmul(g, q, w);
+            for (size_t c = 0; c < N; c++) {
+                z[c] = q[c] + bt * z[c];
+                s[c] = w[c] + bt * s[c];
+                p[c] = r[c] + bt * p[c];
+                e[c] += a * p[c];
+                r[c] = r[c] + (-a) * s[c];
+                w[c] = w[c] + (-a) * z[c];
+            }
+            gamma_old = gamma; alpha_old = alpha; restart = 0;
+            gamma = ddot(g, r, r); delta = ddot(g, w, r);
+            int replaced = 0;
+            if (((i + 1) & 0x1F) == 0) { ORC_PREPLACE(); replaced = 1; }
+            if (gamma < (double)thr) {
+                if (!replaced) ORC_PREPLACE();
+                if (gamma < (double)thr) { conv = 1; break; }
+                restart = 1;
+            }
+        }
+        g->solve_steps = i + 1 > steps ? steps : i + 1;
+    }
+    #undef ORC_PREPLACE
+    for (size_t c = 0; c < N; c++) g->p[c] = (float)(p64[c] + (double)e[c]);
+    free(w); free(p); free(s); free(z); free(q); free(p64); free(t64);
+    g->rr = gamma;
+    g->converged = conv;
+    if (conv) return (float)gamma;
+    return ((float)gamma > thr) ? (float)gamma : nextafterf(thr, INFINITY);
+}
+
 static float cg_solve(orc_grid* g, float thr) {
     if (g->prm.cg_variant == EFS_CG_REFERENCE) return cg_solve_reference(g, thr);
+    if (g->prm.cg_variant == EFS_CG_PIPELINED) return cg_solve_pipelined(g, thr);
     if (g->prm.cg_variant == EFS_CG_MIXED_RECURRENCE) return cg_solve_mixed_recurrence(g, thr);
     return cg_solve_mixed(g, thr);
 }
