@@ -91,11 +91,11 @@ enum efs_cg_variant {
      * same right-hand side that the FP32 results are measured against.  Its FP64 vectors are allocated when
      * a context first selects it. */
     EFS_CG_FP64 = 3,
-    /* EFS_CG_PIPELINED: pipelined CG (Ghysels and Vanroose 2014) with the FP64 accumulator and FP64 residual
-     * replacement of EFS_CG_MIXED: w = L r, s = L p and z = L s are carried by recurrences, so one sweep per
-     * iteration computes q = L w, updates every vector and sums the next iteration's r.r and w.r; on the GPU
-     * that is one pass and one grid reduction per iteration.  Every 64th iteration, and before stopping,
-     * r is recomputed in FP64 and w, s, z from r and p. */
+    /* EFS_CG_PIPELINED (reserved; contexts reject it with EFS_ERR_ARG): pipelined CG (Ghysels and Vanroose
+     * 2014) with the FP64 accumulator and FP64 residual replacement of EFS_CG_MIXED, w = L r, s = L p and
+     * z = L s carried by recurrences (one sweep and one reduction per iteration).  Only the CPU oracle
+     * implements it, as a studied alternative: with FP32 vectors it needs a replacement every 32 iterations
+     * and 9-29 % more iterations than EFS_CG_MIXED_RECURRENCE, which cancels the saved synchronisation. */
     EFS_CG_PIPELINED = 4
 };
 
