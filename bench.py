@@ -312,15 +312,16 @@ def run_gb300(a):
         barrier()
         sim.mark(2)
         for _ in range(k_e2e):
-            sim.upload_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"])
-            sim.update(1)
-            sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+            sim.step_host(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"],
+                          vel_out=h["vel"], rho_out=h["rho"], gamma_out=h["gamma"], beta_out=h["beta"],
+                          divergence_out=h["div"], pressure_out=h["p"])
         sim.mark(3)
         ms_e2e = sim.elapsed_ms(2, 3)
         barrier()
         e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
                "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e,
-               "api": "efs_upload_fields(vel,rho,gamma,boundary,forces) + efs_step + efs_download_fields(vel,rho,gamma,beta,div,p)"}
+               "api": "efs_step_host: upload vel,rho,gamma,boundary,forces + one step + download vel,rho,gamma,beta,div,p "
+                      "(page-locked buffers; gamma/forces up and rho/gamma/beta down overlap the step)"}
     st2 = sim.stats()
     sim.close()
 

@@ -77,6 +77,7 @@ SIGNATURES = {
     "efs_scene_dam3d": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_uint64, _FP, _FP]),
     "efs_scene_dam2d": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _FP, _FP]),
     "efs_scene_batch2d": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _FP, _FP, ctypes.c_int]),
+    "efs_step_host": (ctypes.c_int, [_CTX] + [_FP] * 11),
     "efs_mesh_label": (ctypes.c_int, [_CTX, ctypes.c_int, _FP, ctypes.c_int, _FP, _FP, ctypes.c_float, ctypes.c_float]),
     "efs_mesh_cells": (ctypes.c_int, [_CTX, _FP, ctypes.c_int, _FP, _FP, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong,
                                       ctypes.POINTER(ctypes.c_longlong)]),

@@ -79,6 +79,16 @@ cudaError_t dalloc_halo(efs_ctx* c, T** p, size_t count) {
 cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
     const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
     for (int s = 0; s < EFS_STAGE_COUNT; s++) {
+        // captured steps: gamma and forces uploaded by efs_step_host on the transfer stream are first read by
+        // rho_advect; rho, gamma and beta are final after it (the later stages do not write them)
+        if (timing_events && s == EFS_STAGE_RHO_ADVECT) {
+            cudaError_t e = cudaStreamWaitEvent(c->stream, c->ev_late, cudaEventWaitExternal);
+            if (e != cudaSuccess) return e;
+        }
+        if (timing_events && s == EFS_STAGE_VEL_ADVECT) {
+            cudaError_t e = cudaEventRecordWithFlags(c->ev_advected, c->stream, cudaEventRecordExternal);
+            if (e != cudaSuccess) return e;
+        }
         if (!(stages & EFS_STAGE_BIT(s))) continue;
         if (s == EFS_STAGE_ADD_FORCE && fuse) continue;   // applied inside vel_advect's averaging pass
         cudaError_t e;
@@ -225,7 +235,7 @@ void efs_destroy(efs_ctx* c) {
     void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->fx, c->fy, c->fz, c->solid,
                     c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
                     c->sh_idx, c->sh_val, c->sh_end, c->rowinfo, c->chunk_flag, c->chunk_list, c->block_count,
-                    c->partials, c->ctl, c->mass_partials, c->query_scratch};
+                    c->partials, c->ctl, c->mass_partials, c->query_scratch, c->fstage};
     for (void* b : bufs) if (b) cudaFree(b);
     for (void* b : c->halo_bases) cudaFree(b);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
@@ -233,6 +243,10 @@ void efs_destroy(efs_ctx* c) {
     for (auto ev : c->ev_end) cudaEventDestroy(ev);
     for (auto ev : c->marks) if (ev) cudaEventDestroy(ev);
     if (c->ev_solve_begin) cudaEventDestroy(c->ev_solve_begin);
+    if (c->xfer) { cudaStreamSynchronize(c->xfer); cudaStreamDestroy(c->xfer); }
+    if (c->ev_late) cudaEventDestroy(c->ev_late);
+    if (c->ev_advected) cudaEventDestroy(c->ev_advected);
+    if (c->ev_early) cudaEventDestroy(c->ev_early);
     if (c->ev_solve_end) cudaEventDestroy(c->ev_solve_end);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -292,6 +306,10 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
     if ((e = dalloc(&c->partials, 6 * (size_t)c->solver_blocks)) != cudaSuccess) return bail(e, "cudaMalloc partials");
     if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->ctl_host), sizeof(DevCtl))) != cudaSuccess) return bail(e, "cudaMallocHost");
     if ((e = cudaEventCreate(&c->ev_solve_begin)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_late, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_advected, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
     if ((e = cudaEventCreate(&c->ev_solve_end)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
     if ((e = cudaMemsetAsync(c->validB, 0, N, c->stream)) != cudaSuccess) return bail(e, "cudaMemset");
@@ -339,33 +357,104 @@ int efs_get_params(const efs_ctx* c, efs_params* p) {
     return EFS_OK;
 }
 
-int efs_upload_field(efs_ctx* c, int field, const float* host) {
-    if (!c) return EFS_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// The device address of a page-locked host buffer (which the GPU addresses directly: on GB300 over NVLink-C2C),
+// or null for pageable memory.  Kernels read such buffers at the link's rate (the velocity and force split
+// and the boundary conversion read them in place), but writing the interleaved velocity into one from a
+// kernel runs at half of it; downloads therefore go through device staging and the copy engine.
+void* mapped(const void* host) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
+float* scalar_field(efs_ctx* c, int field) {
+    switch (field) {
+        case EFS_FIELD_RHO: return c->rho;
+        case EFS_FIELD_GAMMA: return c->gamma;
+        case EFS_FIELD_BETA: return c->beta;
+        case EFS_FIELD_DIVERGENCE: return c->div;
+        case EFS_FIELD_PRESSURE: return c->p;
+        default: return nullptr;
+    }
+}
+
+// Enqueue one field's upload on the context's stream (no host synchronisation).
+int enqueue_upload(efs_ctx* c, int field, const float* host) {
     if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
     const size_t N = (size_t)c->g.N, bytes = N * sizeof(float);
     switch (field) {
         case EFS_FIELD_VEL:
         case EFS_FIELD_FORCES: {
-            CK(cudaMemcpyAsync(c->tvel, host, bytes * c->dim, cudaMemcpyHostToDevice, c->stream), "upload");
-            if (field == EFS_FIELD_VEL) { CK(efs::launch_upload_vec(c, c->tvel, c->u, c->v, c->w), "split"); }
+            const float* src = static_cast<const float*>(mapped(host));
+            if (!src) {
+                CK(cudaMemcpyAsync(c->tvel, host, bytes * c->dim, cudaMemcpyHostToDevice, c->stream), "upload");
+                src = c->tvel;
+            }
+            if (field == EFS_FIELD_VEL) { CK(efs::launch_upload_vec(c, src, c->u, c->v, c->w), "split"); }
             else {
-                CK(efs::launch_upload_vec(c, c->tvel, c->fx, c->fy, c->fz), "split");
+                CK(efs::launch_upload_vec(c, src, c->fx, c->fy, c->fz), "split");
                 const int s = note_forces(c);
                 if (s != EFS_OK) return s;
             }
-            break;
+            return EFS_OK;
         }
-        case EFS_FIELD_BOUNDARY:
-            CK(cudaMemcpyAsync(c->tvel, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload");
-            CK(efs::launch_boundary_to_solid(c, c->tvel), "boundary");
-            break;
-        case EFS_FIELD_RHO: CK(cudaMemcpyAsync(c->rho, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
-        case EFS_FIELD_GAMMA: CK(cudaMemcpyAsync(c->gamma, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
-        case EFS_FIELD_BETA: CK(cudaMemcpyAsync(c->beta, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
-        case EFS_FIELD_DIVERGENCE: CK(cudaMemcpyAsync(c->div, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
-        case EFS_FIELD_PRESSURE: CK(cudaMemcpyAsync(c->p, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload"); break;
-        default: return fail(c, EFS_ERR_ARG, "unknown field");
+        case EFS_FIELD_BOUNDARY: {
+            const float* src = static_cast<const float*>(mapped(host));
+            if (!src) {
+                CK(cudaMemcpyAsync(c->tvel, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload");
+                src = c->tvel;
+            }
+            CK(efs::launch_boundary_to_solid(c, src), "boundary");
+            return EFS_OK;
+        }
+        default: {
+            float* dst = scalar_field(c, field);
+            if (!dst) return fail(c, EFS_ERR_ARG, "unknown field");
+            CK(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload");
+            return EFS_OK;
+        }
     }
+}
+
+// Enqueue one field's download on stream `st` (default: the context's; no host synchronisation).
+int enqueue_download(efs_ctx* c, int field, float* host, cudaStream_t st = nullptr) {
+    if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
+    if (!st) st = c->stream;
+    const size_t N = (size_t)c->g.N, bytes = N * sizeof(float);
+    switch (field) {
+        case EFS_FIELD_VEL:
+        case EFS_FIELD_FORCES: {
+            if (field == EFS_FIELD_VEL) { CK(efs::launch_download_vec(c, c->tvel, c->u, c->v, c->w, st), "interleave"); }
+            else { CK(efs::launch_download_vec(c, c->tvel, c->fx, c->fy, c->fz, st), "interleave"); }
+            CK(cudaMemcpyAsync(host, c->tvel, bytes * c->dim, cudaMemcpyDeviceToHost, st), "download");
+            return EFS_OK;
+        }
+        case EFS_FIELD_BOUNDARY: {      // converted on the context's stream
+            CK(efs::launch_solid_to_boundary(c, c->tvel), "boundary");
+            CK(cudaMemcpyAsync(host, c->tvel, bytes, cudaMemcpyDeviceToHost, c->stream), "download");
+            return EFS_OK;
+        }
+        default: {
+            const float* src = scalar_field(c, field);
+            if (!src) return fail(c, EFS_ERR_ARG, "unknown field");
+            CK(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, st), "download");
+            return EFS_OK;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int efs_upload_field(efs_ctx* c, int field, const float* host) {
+    if (!c) return EFS_ERR_ARG;
+    const int s = enqueue_upload(c, field, host);
+    if (s != EFS_OK) return s;
     if (field == EFS_FIELD_BOUNDARY) return check_device_status(c);
     CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     return EFS_OK;
@@ -373,55 +462,91 @@ int efs_upload_field(efs_ctx* c, int field, const float* host) {
 
 int efs_download_field(efs_ctx* c, int field, float* host) {
     if (!c) return EFS_ERR_ARG;
-    if (!host) return fail(c, EFS_ERR_ARG, "host pointer is NULL");
-    const size_t N = (size_t)c->g.N, bytes = N * sizeof(float);
-    switch (field) {
-        case EFS_FIELD_VEL:
-            CK(efs::launch_download_vec(c, c->tvel, c->u, c->v, c->w), "interleave");
-            CK(cudaMemcpyAsync(host, c->tvel, bytes * c->dim, cudaMemcpyDeviceToHost, c->stream), "download");
-            break;
-        case EFS_FIELD_FORCES:
-            CK(efs::launch_download_vec(c, c->tvel, c->fx, c->fy, c->fz), "interleave");
-            CK(cudaMemcpyAsync(host, c->tvel, bytes * c->dim, cudaMemcpyDeviceToHost, c->stream), "download");
-            break;
-        case EFS_FIELD_BOUNDARY:
-            CK(efs::launch_solid_to_boundary(c, c->tvel), "boundary");
-            CK(cudaMemcpyAsync(host, c->tvel, bytes, cudaMemcpyDeviceToHost, c->stream), "download");
-            break;
-        case EFS_FIELD_RHO: CK(cudaMemcpyAsync(host, c->rho, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
-        case EFS_FIELD_GAMMA: CK(cudaMemcpyAsync(host, c->gamma, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
-        case EFS_FIELD_BETA: CK(cudaMemcpyAsync(host, c->beta, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
-        case EFS_FIELD_DIVERGENCE: CK(cudaMemcpyAsync(host, c->div, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
-        case EFS_FIELD_PRESSURE: CK(cudaMemcpyAsync(host, c->p, bytes, cudaMemcpyDeviceToHost, c->stream), "download"); break;
-        default: return fail(c, EFS_ERR_ARG, "unknown field");
-    }
+    const int s = enqueue_download(c, field, host);
+    if (s != EFS_OK) return s;
     CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     return EFS_OK;
 }
 
+// All given fields are enqueued on the stream, then one synchronisation (and the boundary check).  The
+// staging buffer is reused between fields only in stream order, so no host wait is needed in between.
 int efs_upload_fields(efs_ctx* c, const float* vel, const float* rho, const float* gamma, const float* boundary,
                       const float* forces) {
     if (!c) return EFS_ERR_ARG;
     int s;
-    if (boundary && (s = efs_upload_field(c, EFS_FIELD_BOUNDARY, boundary)) != EFS_OK) return s;
-    if (vel && (s = efs_upload_field(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
-    if (rho && (s = efs_upload_field(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
-    if (gamma && (s = efs_upload_field(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
-    if (forces && (s = efs_upload_field(c, EFS_FIELD_FORCES, forces)) != EFS_OK) return s;
-    return EFS_OK;
+    if (boundary && (s = enqueue_upload(c, EFS_FIELD_BOUNDARY, boundary)) != EFS_OK) return s;
+    if (vel && (s = enqueue_upload(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
+    if (rho && (s = enqueue_upload(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
+    if (gamma && (s = enqueue_upload(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
+    if (forces && (s = enqueue_upload(c, EFS_FIELD_FORCES, forces)) != EFS_OK) return s;
+    return check_device_status(c);
 }
 
 int efs_download_fields(efs_ctx* c, float* vel, float* rho, float* gamma, float* beta, float* divergence,
                         float* pressure) {
     if (!c) return EFS_ERR_ARG;
     int s;
-    if (vel && (s = efs_download_field(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
-    if (rho && (s = efs_download_field(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
-    if (gamma && (s = efs_download_field(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
-    if (beta && (s = efs_download_field(c, EFS_FIELD_BETA, beta)) != EFS_OK) return s;
-    if (divergence && (s = efs_download_field(c, EFS_FIELD_DIVERGENCE, divergence)) != EFS_OK) return s;
-    if (pressure && (s = efs_download_field(c, EFS_FIELD_PRESSURE, pressure)) != EFS_OK) return s;
+    if (vel && (s = enqueue_download(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
+    if (rho && (s = enqueue_download(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
+    if (gamma && (s = enqueue_download(c, EFS_FIELD_GAMMA, gamma)) != EFS_OK) return s;
+    if (beta && (s = enqueue_download(c, EFS_FIELD_BETA, beta)) != EFS_OK) return s;
+    if (divergence && (s = enqueue_download(c, EFS_FIELD_DIVERGENCE, divergence)) != EFS_OK) return s;
+    if (pressure && (s = enqueue_download(c, EFS_FIELD_PRESSURE, pressure)) != EFS_OK) return s;
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     return EFS_OK;
+}
+
+// One step with host fields in and out (the upload / update / download of a host-mirrored grid,
+// CudaGrid3D::upload and download around ISimulator::update).  With page-locked buffers the transfers that do
+// not block a stage overlap the step: gamma and forces are uploaded on the transfer stream while
+// vel_extrapolate and rho_sharpen run (the step graph waits for them before rho_advect), and rho, gamma and
+// beta, final after rho_advect, are downloaded on it while vel_advect and the pressure solve run.
+int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* gamma, const float* boundary,
+                  const float* forces, float* vel_out, float* rho_out, float* gamma_out, float* beta_out, float* div_out,
+                  float* p_out) {
+    if (!c) return EFS_ERR_ARG;
+    auto locked = [](const void* p) { return !p || mapped(p) != nullptr; };
+    // the copy engine overlaps only page-locked transfers with kernels
+    const bool overlap = c->prm.solver != EFS_SOLVER_FCG_UNET && locked(gamma) && locked(forces) && locked(rho_out) &&
+                         locked(gamma_out) && locked(beta_out);
+    int s;
+    if (!overlap) {
+        if ((s = efs_upload_fields(c, vel, rho, gamma, boundary, forces)) != EFS_OK) return s;
+        if ((s = efs_step(c, 1)) != EFS_OK) return s;
+        return efs_download_fields(c, vel_out, rho_out, gamma_out, beta_out, div_out, p_out);
+    }
+    const size_t bytes = (size_t)c->g.N * sizeof(float);
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");     // nothing of an earlier call still reads
+    if (forces && (s = note_forces(c)) != EFS_OK) return s;
+    // inputs of the first stages, on the compute stream
+    if (boundary && (s = enqueue_upload(c, EFS_FIELD_BOUNDARY, boundary)) != EFS_OK) return s;
+    if (vel && (s = enqueue_upload(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
+    if (rho && (s = enqueue_upload(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
+    // inputs first read by rho_advect (gamma) and add_force (forces), on the transfer stream once the first
+    // stages' inputs are up (the host link is the bottleneck: sharing it would delay the first stage)
+    CK(cudaEventRecord(c->ev_early, c->stream), "cudaEventRecord");
+    CK(cudaStreamWaitEvent(c->xfer, c->ev_early, 0), "cudaStreamWaitEvent");
+    if (gamma) CK(cudaMemcpyAsync(c->gamma, gamma, bytes, cudaMemcpyHostToDevice, c->xfer), "upload gamma");
+    if (forces) {
+        // the copy engine brings the interleaved forces up; a short split kernel follows (a kernel reading the
+        // host buffer itself would wait for SMs behind the first stages)
+        if (!c->fstage) CK(cudaMalloc(&c->fstage, bytes * c->dim), "cudaMalloc force staging");
+        CK(cudaMemcpyAsync(c->fstage, forces, bytes * c->dim, cudaMemcpyHostToDevice, c->xfer), "upload forces");
+        CK(efs::launch_upload_vec(c, c->fstage, c->fx, c->fy, c->fz, c->xfer), "split forces");
+    }
+    CK(cudaEventRecord(c->ev_late, c->xfer), "cudaEventRecord");
+    if ((s = efs_step(c, 1)) != EFS_OK) return s;
+    // rho, gamma, beta: on the transfer stream once rho_advect is done
+    CK(cudaStreamWaitEvent(c->xfer, c->ev_advected, 0), "cudaStreamWaitEvent");
+    if (rho_out && (s = enqueue_download(c, EFS_FIELD_RHO, rho_out, c->xfer)) != EFS_OK) return s;
+    if (gamma_out && (s = enqueue_download(c, EFS_FIELD_GAMMA, gamma_out, c->xfer)) != EFS_OK) return s;
+    if (beta_out && (s = enqueue_download(c, EFS_FIELD_BETA, beta_out, c->xfer)) != EFS_OK) return s;
+    // the fields of the last stages, after the step on the compute stream
+    if (vel_out && (s = enqueue_download(c, EFS_FIELD_VEL, vel_out)) != EFS_OK) return s;
+    if (div_out && (s = enqueue_download(c, EFS_FIELD_DIVERGENCE, div_out)) != EFS_OK) return s;
+    if (p_out && (s = enqueue_download(c, EFS_FIELD_PRESSURE, p_out)) != EFS_OK) return s;
+    CK(cudaStreamSynchronize(c->xfer), "cudaStreamSynchronize");
+    return check_device_status(c);
 }
 
 int efs_reset_fields(efs_ctx* c) {

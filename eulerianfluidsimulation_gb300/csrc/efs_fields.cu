@@ -4,6 +4,9 @@
 // include/simulation/data/VecField3D.h:93) and are split into one array per component; the boundary field
 // (float 0/1, ScalField3D) becomes one byte per cell.  Scalar fields share the reference layout and are
 // copied as they are.
+#include <algorithm>
+#include <cstdint>
+
 #include "efs_internal.h"
 
 namespace efs {
@@ -70,15 +73,39 @@ __global__ void k_mass(int n, const float* __restrict__ rho, double* __restrict_
 
 inline int nblk(int n) { return (n + 255) / 256; }
 
+// dst[i] = src[i]; 16 bytes per thread where both pointers allow it.  Either side may be page-locked host
+// memory that the GPU addresses directly.
+__global__ void k_copy(long long n, const float* __restrict__ src, float* __restrict__ dst, int vec4) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    if (vec4) {
+        const long long n4 = n >> 2;
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4; k += stride) d4[k] = s4[k];
+        for (long long k = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k];
+    } else {
+        for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += stride) dst[k] = src[k];
+    }
+}
+
 }  // namespace
 
-cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc) {
-    k_split<<<nblk(c->g.N), 256, 0, c->stream>>>(c->g.N, c->dim, staged, a, b, cc);
+cudaError_t launch_copy(efs_ctx* c, const float* src, float* dst, long long n) {
+    const int vec4 = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+    const long long work = vec4 ? (n + 3) / 4 : n;
+    const int blocks = (int)std::min<long long>(std::max<long long>(1, (work + 255) / 256), (long long)c->sm_count * 8);
+    k_copy<<<blocks, 256, 0, c->stream>>>(n, src, dst, vec4);
     return cudaGetLastError();
 }
 
-cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc) {
-    k_interleave<<<nblk(c->g.N), 256, 0, c->stream>>>(c->g.N, c->dim, staged, a, b, cc);
+cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc, cudaStream_t st) {
+    k_split<<<nblk(c->g.N), 256, 0, st ? st : c->stream>>>(c->g.N, c->dim, staged, a, b, cc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc,
+                                cudaStream_t st) {
+    k_interleave<<<nblk(c->g.N), 256, 0, st ? st : c->stream>>>(c->g.N, c->dim, staged, a, b, cc);
     return cudaGetLastError();
 }
 

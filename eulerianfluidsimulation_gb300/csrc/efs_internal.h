@@ -148,6 +148,12 @@ struct efs_ctx {
 
     efs::UNetState* unet = nullptr;         // learned preconditioner (efs_unet.cu)
     void* query_scratch = nullptr;          // efs_query_box block partials and result (efs_scene.cu)
+    // efs_step_host: transfers that overlap the step run on `xfer`; the step graph waits for `ev_late` (late
+    // inputs) before rho_advect and records `ev_advected` after it
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t ev_late = nullptr, ev_advected = nullptr;
+    cudaEvent_t ev_early = nullptr;         // the first stages' inputs are on the device
+    float* fstage = nullptr;                // efs_step_host: staging of the forces (dim floats a cell)
 };
 
 namespace efs {
@@ -163,11 +169,13 @@ cudaError_t launch_solver(efs_ctx* c);
 cudaError_t fcg_solve(efs_ctx* c);
 void unet_free(efs_ctx* c);
 // efs_fields.cu
-cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc);
-cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc);
+cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc, cudaStream_t st = nullptr);
+cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc,
+                                cudaStream_t st = nullptr);
 cudaError_t launch_boundary_to_solid(efs_ctx* c, const float* staged);
 cudaError_t launch_solid_to_boundary(efs_ctx* c, float* staged);
 cudaError_t launch_reset_fields(efs_ctx* c);
+cudaError_t launch_copy(efs_ctx* c, const float* src, float* dst, long long n);
 cudaError_t launch_mass(efs_ctx* c, double* out_dev);
 // efs_scene.cu: scene construction and queries
 struct FieldPtrsOut {

@@ -23,7 +23,10 @@ namespace efs {
 
 namespace {
 
-constexpr int SOLVER_THREADS = 512;
+// One block of 1024 threads per SM (64 registers a thread): half the grid-barrier arrivals and block partials
+// of two 512-thread blocks with the same warps per SM (measured at 256^3: 40.4 against 41.4 ms per solve).
+constexpr int SOLVER_THREADS = 1024;
+constexpr int SOLVER_MIN_BLOCKS = 1024 / SOLVER_THREADS;      // 64 registers a thread: 1024 threads per SM
 constexpr int SOLVER_WARPS = SOLVER_THREADS / 32;
 
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;   // 2 s per barrier
@@ -628,7 +631,7 @@ __device__ __forceinline__ bool solver_prologue(const SolverArgs& a, Chunks& ch,
     return true;
 }
 
-__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
+__global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(SolverArgs a) {
     DevCtl* ctl = a.ctl;
     Chunks ch;
     int M = 0;
@@ -863,7 +866,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver(SolverArgs a) {
 }
 
 // EFS_CG_FP64 runs in its own kernel so that the study solver does not weigh on k_solver's registers.
-__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_solver_fp64(SolverArgs a) {
+__global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver_fp64(SolverArgs a) {
     Chunks ch;
     int M = 0;
     if (!solver_prologue(a, ch, M)) return;

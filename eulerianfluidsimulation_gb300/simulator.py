@@ -237,6 +237,14 @@ class _GB300Simulator:
         check(lib().efs_download_fields(self._h, fptr(vel), fptr(rho), fptr(gamma), fptr(beta), fptr(divergence),
                                         fptr(pressure)), self._h)
 
+    def step_host(self, vel=None, rho=None, gamma=None, boundary=None, forces=None, vel_out=None, rho_out=None,
+                  gamma_out=None, beta_out=None, divergence_out=None, pressure_out=None):
+        """efs_step_host: upload, one step, download in one call (transfers overlap the step when the buffers
+        are page-locked); None skips a field."""
+        check(lib().efs_step_host(self._h, fptr(vel), fptr(rho), fptr(gamma), fptr(boundary), fptr(forces),
+                                  fptr(vel_out), fptr(rho_out), fptr(gamma_out), fptr(beta_out), fptr(divergence_out),
+                                  fptr(pressure_out)), self._h)
+
     def pressure_fp64(self):
         """efs_download_pressure_fp64: the FP64 pressure of the last CG solve, shaped like the fields."""
         out = np.empty(self._fshape(abi.FIELD_PRESSURE), np.float64)

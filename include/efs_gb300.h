@@ -191,6 +191,16 @@ int  efs_upload_fields(efs_ctx* ctx, const float* vel, const float* rho, const f
 /* CudaGrid3D::download (CudaGrid3D.cu:258-269): NULL pointers are skipped. */
 int  efs_download_fields(efs_ctx* ctx, float* vel, float* rho, float* gamma, float* beta,
                          float* divergence, float* pressure);
+/* One step with host fields in and out: efs_upload_fields, efs_step(ctx, 1) and efs_download_fields in one
+ * call (the upload / update / download of a host-mirrored grid, CudaGrid3D::upload and download,
+ * src/simulation/data/CudaGrid3D.cu:247-269, around ISimulator::update).  Any pointer may be NULL (skipped).
+ * When gamma, forces and the rho / gamma / beta outputs are page-locked host memory, the transfers overlap the
+ * step: gamma and forces go up while the stages before rho_advect run, and rho, gamma and beta come down while
+ * vel_advect and the pressure solve run; otherwise the three calls run in order.  Returns when the outputs are
+ * written. */
+int  efs_step_host(efs_ctx* ctx, const float* vel, const float* rho, const float* gamma, const float* boundary,
+                   const float* forces, float* vel_out, float* rho_out, float* gamma_out, float* beta_out,
+                   float* divergence_out, float* pressure_out);
 /* Grid3D/Grid2D constructor state (Grid3D.cpp:10-48): zero fields, gamma = 1, solid border, rho = 0 on it. */
 int  efs_reset_fields(efs_ctx* ctx);
 /* No counterpart in the reference.  The FP64 pressure of the last CG solve (N doubles, reference layout):

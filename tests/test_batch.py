@@ -174,3 +174,59 @@ def test_cluster_of_16_or_refused():
         B.update(2)
         B.synchronize()
         assert all(B.stats(s).converged for s in range(B.n))
+
+
+TILES = [(32, 8), (32, 4), (64, 4), (16, 8), (32, 16), (128, 2)]
+
+
+def _check_stages(B, tol_solve=1e-5):
+    singles = []
+    for s in range(B.n):
+        side = B.widths[s]
+        S = gb.GB300Simulator2D(side, side, _params(side))
+        S.set_fields(_state(B, s))
+        singles.append(S)
+    bad = []
+    try:
+        for stage in range(abi.STAGE_COUNT):
+            B.stage(stage)
+            for S in singles:
+                S.stage(stage)
+            for s, S in enumerate(singles):
+                for f in FIELDS:
+                    got, want = B.field(s, f), S.field(f)
+                    if stage == abi.STAGE_PROJECT and f in (abi.FIELD_PRESSURE, abi.FIELD_VEL):
+                        ok = rel_l2(got, want) <= tol_solve
+                    elif stage in (abi.STAGE_RHO_SHARPEN, abi.STAGE_RHO_ADVECT) and f in (abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA):
+                        ok = rel_l2(got, want) <= 1e-6
+                    else:
+                        ok = np.array_equal(got, want)
+                    if not ok:
+                        bad.append((abi.STAGE_NAMES[stage], s, abi.FIELD_NAMES[f]))
+                S.set_fields(_state(B, s))
+    finally:
+        for S in singles:
+            S.close()
+    return bad
+
+
+@pytest.mark.parametrize("tile", TILES)
+def test_every_tuning_the_autotuner_may_pick(tile):
+    """Each stage tile shape, at each blocks-per-SM count the autotuner tries, gives every stage of every scene
+    as the single context does; the liquid mass holds over 10 steps."""
+    scenes = _scenes([0, 1, 2, 5])
+    for bps in (2, 4, 8, 16):
+        with _batch(scenes) as B:
+            t = B.tuning()
+            t.tile_x, t.tile_y, t.blocks_per_sm = tile[0], tile[1], bps
+            B.set_tuning(t)
+            B.update(3)
+            B.synchronize()
+            bad = _check_stages(B)
+            assert not bad, (tile, bps, bad[:5])
+            m0 = [float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64)) for s in range(B.n)]
+            B.update(10)
+            B.synchronize()
+            for s in range(B.n):
+                m = float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64))
+                assert abs(m - m0[s]) <= 1e-5 * m0[s], (tile, bps, s, m, m0[s])
