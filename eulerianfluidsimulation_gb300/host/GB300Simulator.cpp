@@ -126,10 +126,17 @@ void GB300Simulator3D::readStats() {
 void GB300Simulator3D::update() {
     if (!_ctx) return;
     syncParams();
-    const bool udload = !PROPERTY_B(DISABLE_UDLOAD);
-    if (udload) upload();
-    report(_ctx, efs_step(_ctx, 1), "efs_step");
-    if (udload) download();
+    if (!PROPERTY_B(DISABLE_UDLOAD)) {
+        // upload, one step and download in one call; with page-locked host storage the transfers that no stage
+        // waits for overlap the step
+        float* vel = reinterpret_cast<float*>(_grid->vel().data());
+        report(_ctx, efs_step_host(_ctx, vel, _grid->rho().data(), _grid->gamma().data(), _grid->boundary().data(),
+                                   reinterpret_cast<const float*>(_grid->forces().data()), vel, _grid->rho().data(),
+                                   _grid->gamma().data(), _grid->beta().data(), _grid->divergence().data(),
+                                   _grid->pressure().data()), "efs_step_host");
+    } else {
+        report(_ctx, efs_step(_ctx, 1), "efs_step");
+    }
     readStats();
     ADD_PROPERTY_I(SIMULATION_FRAMES, 1);
 }
@@ -200,10 +207,17 @@ void GB300Simulator2D::readStats() {
 void GB300Simulator2D::update() {
     if (!_ctx) return;
     syncParams();
-    const bool udload = !PROPERTY_B(DISABLE_UDLOAD);
-    if (udload) upload();
-    report(_ctx, efs_step(_ctx, 1), "efs_step");
-    if (udload) download();
+    if (!PROPERTY_B(DISABLE_UDLOAD)) {
+        // upload, one step and download in one call; with page-locked host storage the transfers that no stage
+        // waits for overlap the step
+        float* vel = reinterpret_cast<float*>(_grid->vel().data());
+        report(_ctx, efs_step_host(_ctx, vel, _grid->rho().data(), _grid->gamma().data(), _grid->boundary().data(),
+                                   reinterpret_cast<const float*>(_grid->forces().data()), vel, _grid->rho().data(),
+                                   _grid->gamma().data(), _grid->beta().data(), _grid->divergence().data(),
+                                   _grid->pressure().data()), "efs_step_host");
+    } else {
+        report(_ctx, efs_step(_ctx, 1), "efs_step");
+    }
     readStats();
     ADD_PROPERTY_I(SIMULATION_FRAMES, 1);
 }
