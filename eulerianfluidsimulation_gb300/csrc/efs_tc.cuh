@@ -143,7 +143,7 @@ struct ConvArgs {
     const float* bias;          // [COUT] or null
     const __nv_bfloat16* skip;  // [V][COUT] added after the activation, or null
     __nv_bfloat16* out;         // [V][COUT] (BF16) or null
-    float* out32;               // [V][COUT] (FP32) or null
+    float* out32;               // [V] FP32: output channel 0 only, or null
     __nv_bfloat16* pre;         // [V][COUT] pre-activation (BF16, for the ReLU mask of the backward pass) or null
     int D, H, W, cin;
     int relu;
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
                     if (a.relu) t = fmaxf(t, 0.f);
                     if (a.skip) t += __bfloat162float(a.skip[(size_t)v * COUT + c0 + j]);
                     o[j] = __float2bfloat16(t);
-                    if (a.out32) a.out32[(size_t)v * COUT + c0 + j] = t;
+                    if (a.out32 && c0 + j == 0) a.out32[v] = t;
                 }
                 if (a.out) {
                     uint4* dst = reinterpret_cast<uint4*>(a.out + (size_t)v * COUT + c0);
@@ -406,7 +406,8 @@ __device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t
 }
 
 // ============================================================================================================
-// Halo-tile 3x3x3 convolution: the same function as k_conv3_tc, for grids at least one tile wide.
+// Halo-tile 3x3x3 convolution (k_conv3_halo_ws below): the same function as k_conv3_tc, for grids at least
+// one tile wide.
 // A CTA computes kHaloRows output rows (2 in y x 2 in z) of one 128-voxel segment along x.  Per 16 input
 // channels it loads, with two TMA tensor copies (one per 8-channel group), the input box of
 // 130 x 4 x 4 voxels that covers those rows and their one-voxel halo (zero outside the grid), and with one
@@ -427,120 +428,202 @@ struct HaloArgs {
     const float* bias;
     const __nv_bfloat16* skip;
     __nv_bfloat16* out;
-    float* out32;
+    float* out32;                      // [V] FP32: output channel 0 only, or null
     __nv_bfloat16* pre;
     int D, H, W, cin;
     int relu;
     int* err;
 };
 
-template <int COUT>
-constexpr int halo_smem_bytes() { return 2 * kHaloPlane + 27 * COUT * 32 + 64; }
+// ---- persistent, warp-specialised halo convolution ---------------------------------------------------------
+// One CTA per SM walking tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// Roles: warp 0 (one lane) streams (tile, 16-channel chunk) items into kWsStages shared-memory stages with TMA;
+// warp 1 (one lane) issues each item's 108 MMAs into one of two TMEM accumulator buffers; warps 2-5 (one per
+// TMEM lane quarter) run a tile's epilogue while the next tile's MMAs run.  full/empty mbarriers hand stages
+// between producer and MMA warp, acc_full/acc_empty accumulator buffers between MMA warp and epilogue.  Every
+// wait is bounded and also gives up as soon as another role has given up (shared abort flag), so a failure
+// ends the kernel within one wait limit; the MMA warp then drains its MMAs and the producer its copies before
+// TMEM is freed.
+constexpr int kWsThreads = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// mbar_wait that also returns false as soon as *abort is set; sets *abort itself when it gives up.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
+    if (mbar_test(bar, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    while (!mbar_test(bar, parity)) {
+        if (*abort) return false;
+        if (now_ns() - t0 > kWaitNs) { *abort = 1; return false; }
+    }
+    return true;
+}
+
+template <int COUT> __host__ __device__ constexpr int ws_stages() { return COUT == 64 ? 1 : 2; }
+template <int COUT> __host__ __device__ constexpr int ws_stage_bytes() { return 2 * kHaloPlane + 27 * COUT * 32; }
+template <int COUT> __host__ __device__ constexpr int ws_smem_bytes() { return ws_stages<COUT>() * ws_stage_bytes<COUT>() + 128; }
 
 template <int COUT>
-__global__ void __launch_bounds__(kConvThreads) k_conv3_halo(const __grid_constant__ HaloArgs a) {
+__global__ void __launch_bounds__(kWsThreads, 1) k_conv3_halo_ws(const __grid_constant__ HaloArgs a) {
     static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
+    constexpr int S = ws_stages<COUT>();
+    constexpr int kStage = ws_stage_bytes<COUT>();
     constexpr int kWBytes = 27 * COUT * 32;
-    constexpr uint32_t kCols = kHaloRows * COUT;      // 64, 128 or 256
+    constexpr uint32_t kAcc = kHaloRows * COUT;       // TMEM columns of one accumulator buffer
+    constexpr uint32_t kCols = 2 * kAcc;              // 128, 256 or 512
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* box = smem;                        // 2 group planes (128-byte aligned)
-    unsigned char* wts = smem + 2 * kHaloPlane;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(wts + kWBytes);   // [0] loads, [1] MMAs
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * kStage);
+    uint64_t* full = bars;              // [2]
+    uint64_t* empty = bars + 2;         // [2]
+    uint64_t* acc_full = bars + 4;      // [2]
+    uint64_t* acc_empty = bars + 6;     // [2]
+    uint64_t* drained = bars + 8;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 10);
+    __shared__ int s_abort;
 
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int x0 = blockIdx.x * kHaloSeg, y0 = blockIdx.y * kHaloRY, z0 = blockIdx.z * kHaloRZ;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nx = (a.W + kHaloSeg - 1) / kHaloSeg, ny = (a.H + kHaloRY - 1) / kHaloRY;
+    const int nz = (a.D + kHaloRZ - 1) / kHaloRZ;
+    const int ntiles = nx * ny * nz;
     const int chunks = a.cin >> 4;
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
     if (warp == 0) tmem_alloc(tslot, kCols);
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int q = 0; q < 2; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], 1);
+            mbar_init(&acc_full[q], 1);
+            mbar_init(&acc_empty[q], 4);
+        }
+        mbar_init(drained, 1);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    volatile int* abort = &s_abort;
+    auto origin = [&](int j, int& x0, int& y0, int& z0) {
+        const int t = (int)blockIdx.x + j * (int)gridDim.x;
+        x0 = (t % nx) * kHaloSeg;
+        y0 = ((t / nx) % ny) * kHaloRY;
+        z0 = (t / (nx * ny)) * kHaloRZ;
+    };
 
-    // thread 0 stages and issues; its outcome reaches the block through shared memory
-    __shared__ int s_ok;
-    if (tid == 0) {
-        int ok = 1;
-        for (int c = 0; c < chunks && ok; c++) {
-            // the previous chunk's MMAs read the box and weights: wait before overwriting them
-            if (c > 0 && !mbar_wait(&mbar[1], (c - 1) & 1)) { ok = 0; break; }
-            mbar_expect_tx(&mbar[0], 2 * kHaloPlane + kWBytes);
-            tma_load_4d(box, &a.map[2 * c], 0, x0 - 1, y0 - 1, z0 - 1, &mbar[0]);
-            tma_load_4d(box + kHaloPlane, &a.map[2 * c + 1], 0, x0 - 1, y0 - 1, z0 - 1, &mbar[0]);
-            bulk_load(wts, a.wh + (size_t)c * 27 * COUT * 16, kWBytes, &mbar[0]);
-            if (!mbar_wait(&mbar[0], c & 1)) { ok = 0; break; }
+    if (warp == 0 && lane == 0) {
+        // ---- producer ----
+        int k = 0;
+        for (int j = 0; j < my_tiles && !*abort; j++) {
+            int x0, y0, z0;
+            origin(j, x0, y0, z0);
+            bool ok = true;
+            for (int c = 0; c < chunks; c++) {
+                const int s = k % S;
+                if (k >= S && !mbar_wait_or_abort(&empty[s], ((k / S) - 1) & 1, abort)) { ok = false; break; }
+                unsigned char* box = smem + s * kStage;
+                mbar_expect_tx(&full[s], 2 * kHaloPlane + kWBytes);
+                tma_load_4d(box, &a.map[2 * c], 0, x0 - 1, y0 - 1, z0 - 1, &full[s]);
+                tma_load_4d(box + kHaloPlane, &a.map[2 * c + 1], 0, x0 - 1, y0 - 1, z0 - 1, &full[s]);
+                bulk_load(box + 2 * kHaloPlane, a.wh + (size_t)c * 27 * COUT * 16, kWBytes, &full[s]);
+                k++;
+            }
+            if (!ok) break;
+        }
+        // the last S items' copies have landed before the CTA may exit (bounded; no-ops when consumed)
+        for (int q = k - S; q < k; q++)
+            if (q >= 0) mbar_wait(&full[q % S], (q / S) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issue ----
+        int k = 0;
+        for (int j = 0; j < my_tiles && !*abort; j++) {
+            const int ab = j & 1;
+            if (j >= 2 && !mbar_wait_or_abort(&acc_empty[ab], ((j / 2) - 1) & 1, abort)) break;
             tc_fence_after();
-            const uint32_t sbox = smem_u32(box), swts = smem_u32(wts);
+            const uint32_t acc = tmem + (uint32_t)ab * kAcc;
+            bool ok = true;
+            for (int c = 0; c < chunks; c++) {
+                const int s = k % S;
+                if (!mbar_wait_or_abort(&full[s], (k / S) & 1, abort)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t sbox = smem_u32(smem + s * kStage), swts = sbox + 2 * kHaloPlane;
+                // all 108 operand addresses are constant offsets from the two base descriptors (the start
+                // address field is addr >> 4 and shared memory stays below 256 KB, so the addition cannot carry)
+                const uint64_t abase = sdesc(sbox, (uint32_t)kHaloPlane, 128), bbase = sdesc(swts, 128, 256);
+                const uint32_t first = c > 0 ? 1u : 0u;
+#pragma unroll
+                for (int r = 0; r < kHaloRows; r++) {
+#pragma unroll
+                    for (int tap = 0; tap < 27; tap++) {
+                        const int ry = r % kHaloRY, rz = r / kHaloRY;
+                        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                        const uint32_t off = (uint32_t)((((rz + dz) * kHaloBoxY + (ry + dy)) * kHaloX + dx) * 16);
+                        mma_bf16(acc + (uint32_t)(r * COUT), abase + (off >> 4), bbase + (uint32_t)((tap * COUT * 32) >> 4),
+                                 idesc_bf16(128, COUT), tap > 0 ? 1u : first);
+                    }
+                }
+                mma_commit(&empty[s]);
+                k++;
+            }
+            if (!ok) break;
+            mma_commit(&acc_full[ab]);
+        }
+        mma_commit(drained);                 // arrives when every MMA issued above has completed
+        mbar_wait(drained, 0);
+    } else if (warp >= 2) {
+        // ---- epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 ----
+        const int quarter = warp & 3;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        for (int j = 0; j < my_tiles; j++) {
+            const int ab = j & 1;
+            if (!mbar_wait_or_abort(&acc_full[ab], (j / 2) & 1, abort)) break;
+            tc_fence_after();
+            int x0, y0, z0;
+            origin(j, x0, y0, z0);
+            const int x = x0 + quarter * 32 + lane;
 #pragma unroll 1
             for (int r = 0; r < kHaloRows; r++) {
-                const int ry = r % kHaloRY, rz = r / kHaloRY;
-#pragma unroll 1
-                for (int tap = 0; tap < 27; tap++) {
-                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;      // offsets + 1
-                    const uint32_t off = (uint32_t)((((rz + dz) * kHaloBoxY + (ry + dy)) * kHaloX + dx) * 16);
-                    const uint64_t ad = sdesc(sbox + off, (uint32_t)kHaloPlane, 128);
-                    const uint64_t bd = sdesc(swts + (uint32_t)(tap * COUT * 32), 128, 256);
-                    mma_bf16(tmem + (uint32_t)(r * COUT), ad, bd, idesc_bf16(128, COUT), (c > 0 || tap > 0) ? 1u : 0u);
+                const int y = y0 + r % kHaloRY, z = z0 + r / kHaloRY;
+                const bool vin = x < a.W && y < a.H && z < a.D;
+                const size_t v = ((size_t)z * a.H + y) * a.W + x;
+#pragma unroll
+                for (int c0 = 0; c0 < COUT; c0 += 16) {
+                    float accv[16];
+                    tmem_ld16(tmem + lane_base + (uint32_t)ab * kAcc + (uint32_t)(r * COUT + c0), accv);
+                    if (vin) {
+                        __align__(16) __nv_bfloat16 o[16], pr[16];
+#pragma unroll
+                        for (int q = 0; q < 16; q++) {
+                            float t = accv[q] + (a.bias ? a.bias[c0 + q] : 0.f);
+                            pr[q] = __float2bfloat16(t);
+                            if (a.relu) t = fmaxf(t, 0.f);
+                            if (a.skip) t += __bfloat162float(a.skip[v * COUT + c0 + q]);
+                            o[q] = __float2bfloat16(t);
+                            if (a.out32 && c0 + q == 0) a.out32[v] = t;
+                        }
+                        if (a.out) {
+                            uint4* dst = reinterpret_cast<uint4*>(a.out + v * COUT + c0);
+                            dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                            dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                        }
+                        if (a.pre) {
+                            uint4* dst = reinterpret_cast<uint4*>(a.pre + v * COUT + c0);
+                            dst[0] = reinterpret_cast<const uint4*>(pr)[0];
+                            dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+                        }
+                    }
                 }
             }
-            mma_commit(&mbar[1]);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[ab]);
         }
-        s_ok = ok;
     }
     __syncthreads();
-    bool ok = s_ok != 0;
-    const int last = chunks - 1;
-    if (ok && !mbar_wait(&mbar[1], last & 1)) ok = false;
-    if (!ok) {
-        if (tid == 0) atomicOr(a.err, 1);
-        mbar_wait(&mbar[1], last & 1);     // bounded: let MMAs in flight finish before freeing TMEM
-    }
+    if (tid == 0 && *abort) atomicOr(a.err, 1);
     tc_fence_after();
-    if (ok) {
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-        const int x = x0 + tid;
-#pragma unroll 1
-        for (int r = 0; r < kHaloRows; r++) {
-            const int y = y0 + r % kHaloRY, z = z0 + r / kHaloRY;
-            const bool vin = x < a.W && y < a.H && z < a.D;
-            const size_t v = ((size_t)z * a.H + y) * a.W + x;
-#pragma unroll
-            for (int c0 = 0; c0 < COUT; c0 += 16) {
-                float acc[16];
-                tmem_ld16(tmem + lane_base + (uint32_t)(r * COUT + c0), acc);
-                if (vin) {
-                    __align__(16) __nv_bfloat16 o[16], pr[16];
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
-                        pr[j] = __float2bfloat16(t);
-                        if (a.relu) t = fmaxf(t, 0.f);
-                        if (a.skip) t += __bfloat162float(a.skip[v * COUT + c0 + j]);
-                        o[j] = __float2bfloat16(t);
-                        if (a.out32) a.out32[v * COUT + c0 + j] = t;
-                    }
-                    if (a.out) {
-                        uint4* dst = reinterpret_cast<uint4*>(a.out + v * COUT + c0);
-                        dst[0] = reinterpret_cast<const uint4*>(o)[0];
-                        dst[1] = reinterpret_cast<const uint4*>(o)[1];
-                    }
-                    if (a.pre) {
-                        uint4* dst = reinterpret_cast<uint4*>(a.pre + v * COUT + c0);
-                        dst[0] = reinterpret_cast<const uint4*>(pr)[0];
-                        dst[1] = reinterpret_cast<const uint4*>(pr)[1];
-                    }
-                }
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, kCols);
 }
 

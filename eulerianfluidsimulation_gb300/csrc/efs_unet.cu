@@ -58,11 +58,11 @@ struct UNetState {
     float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
     int adam_t = 0;
     bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
-    bf16* wh = nullptr;          // weights of the convolution in flight, packed for k_conv3_halo
+    bf16* wh = nullptr;          // weights of the convolution in flight, packed for k_conv3_halo_ws
     // activations (level of each in brackets)
     bf16 *x0 = nullptr, *e0 = nullptr, *p0 = nullptr, *e1 = nullptr, *p1 = nullptr, *e2 = nullptr, *u2 = nullptr,
          *d1 = nullptr, *u1 = nullptr, *d0 = nullptr;
-    float* y32 = nullptr;
+    float* y32 = nullptr;        // network output, channel 0 (FP32)
     // training: pre-activations and gradients
     bool train_ready = false;
     bf16 *a0 = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *a4 = nullptr;
@@ -283,7 +283,7 @@ __global__ void k_loss(const float* __restrict__ y32, const float* __restrict__ 
     if (v < n) {
         if (rowinfo[v] & 0x8000u) {
             const double t = (double)p[v] * tscal[2];
-            const double d = (double)y32[v * 16] - t;
+            const double d = (double)y32[v] - t;
             l = d * d;
             o[0] = __float2bfloat16((float)(2.0 * d / tscal[1]));
         }
@@ -413,7 +413,7 @@ __global__ void k_synth_error(Level L, const uint16_t* __restrict__ rowinfo, uns
 __global__ void k_unpack(const float* __restrict__ y32, const uint16_t* __restrict__ rowinfo, long long n, float* __restrict__ z) {
     const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (v >= n) return;
-    z[v] = (rowinfo[v] & 0x8000u) ? y32[v * 16] : 0.f;
+    z[v] = (rowinfo[v] & 0x8000u) ? y32[v] : 0.f;
 }
 
 // ---- FCG kernels (matrix of k_solver_prep: rowinfo bits x-1, x+1, y-1, y+1, z-1, z+1) -------------------------
@@ -584,17 +584,18 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 constexpr int kHaloMinWidth = 96;
 
 template <int COUT>
-cudaError_t launch_halo(const tc::HaloArgs& a, int W, int H, int D, cudaStream_t st) {
+cudaError_t launch_halo(const tc::HaloArgs& a, int W, int H, int D, int sm_count, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(tc::k_conv3_halo<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             tc::halo_smem_bytes<COUT>());
+        cudaError_t e = cudaFuncSetAttribute(tc::k_conv3_halo_ws<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tc::ws_smem_bytes<COUT>());
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    const dim3 grid((unsigned)((W + tc::kHaloSeg - 1) / tc::kHaloSeg), (unsigned)((H + tc::kHaloRY - 1) / tc::kHaloRY),
-                    (unsigned)((D + tc::kHaloRZ - 1) / tc::kHaloRZ));
-    tc::k_conv3_halo<COUT><<<grid, tc::kConvThreads, tc::halo_smem_bytes<COUT>(), st>>>(a);
+    const long long tiles = (long long)((W + tc::kHaloSeg - 1) / tc::kHaloSeg) * ((H + tc::kHaloRY - 1) / tc::kHaloRY) *
+                            ((D + tc::kHaloRZ - 1) / tc::kHaloRZ);
+    const unsigned grid = (unsigned)std::max(1LL, std::min<long long>(tiles, sm_count));
+    tc::k_conv3_halo_ws<COUT><<<grid, tc::kWsThreads, tc::ws_smem_bytes<COUT>(), st>>>(a);
     return cudaGetLastError();
 }
 
@@ -622,9 +623,11 @@ cudaError_t conv_halo(UNetState* u, const bf16* in, const bf16* wt, int cin, int
     a.wh = u->wh;
     a.bias = bias; a.skip = skip; a.out = out; a.out32 = out32; a.pre = pre;
     a.D = L.D; a.H = L.H; a.W = L.W; a.cin = cin; a.relu = relu; a.err = u->err;
-    if (cout == 16) return launch_halo<16>(a, L.W, L.H, L.D, st);
-    if (cout == 32) return launch_halo<32>(a, L.W, L.H, L.D, st);
-    return launch_halo<64>(a, L.W, L.H, L.D, st);
+    int sm_count = 0;
+    cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, 0);
+    if (cout == 16) return launch_halo<16>(a, L.W, L.H, L.D, sm_count, st);
+    if (cout == 32) return launch_halo<32>(a, L.W, L.H, L.D, sm_count, st);
+    return launch_halo<64>(a, L.W, L.H, L.D, sm_count, st);
 }
 
 cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
@@ -858,7 +861,7 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
     UCK(ualloc(u, &u->d1, L[1].V * 32));
     UCK(ualloc(u, &u->u1, L[0].V * 32));
     UCK(ualloc(u, &u->d0, L[0].V * 16));
-    UCK(ualloc(u, &u->y32, L[0].V * 16));
+    UCK(ualloc(u, &u->y32, L[0].V));
     UCK(ualloc(u, &u->dscal, 12));
     UCK(ualloc(u, &u->dpart, 3LL * std::max<long long>(kRedBlocks, nblk(L[0].V))));
     UCK(ualloc(u, &u->dloss, 1));
