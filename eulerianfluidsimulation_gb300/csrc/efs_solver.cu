@@ -243,7 +243,8 @@ __device__ __forceinline__ double lap_df(const float* x, uint16_t info, int i, c
 // This block's share of the active chunks, cached in shared memory for the whole solve (the compacted list
 // does not change between iterations).
 struct Chunks {
-    const int* ids;   // shared memory
+    const int* ids;        // shared memory
+    const unsigned* mask;  // shared memory: per chunk, bit l set when cell (chunk, lane l) is a matrix row
     int n;
 };
 
@@ -359,25 +360,30 @@ constexpr int UA = 4;
 __device__ __forceinline__ void phase_t(const SolverArgs& a, const Chunks& ch, const float* __restrict__ d,
                                         float* __restrict__ tout, const Nb& nb, FSum& dt, FSum& tt) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int N = a.g.N;
     for (int cb = warp * UA; cb < ch.n; cb += SOLVER_WARPS * UA) {
         int idx[UA];
+        bool act[UA];
         uint16_t f[UA];
 #pragma unroll
-        for (int u = 0; u < UA; u++) idx[u] = (cb + u < ch.n) ? ch.ids[cb + u] * 32 + lane : -1;
+        for (int u = 0; u < UA; u++) {
+            const int c = cb + u;
+            act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
+            idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
+        }
 #pragma unroll
-        for (int u = 0; u < UA; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        for (int u = 0; u < UA; u++) f[u] = a.rowinfo[idx[u]];
+        // lanes without a row all read cell 0's neighbourhood (inside the vectors' halo): one cached line
         float xv[UA][7];
 #pragma unroll
         for (int u = 0; u < UA; u++) {
-            const int i = idx[u] < 0 ? 0 : idx[u];
+            const int i = idx[u];
             xv[u][6] = d[i];
 #pragma unroll
             for (int k = 0; k < 6; k++) xv[u][k] = d[i + nb.o[k]];
         }
 #pragma unroll
         for (int u = 0; u < UA; u++) {
-            if (!(f[u] & 0x8000u)) continue;
+            if (!act[u]) continue;
             float sum = 0.0f;
 #pragma unroll
             for (int k = 0; k < 6; k++)
@@ -395,7 +401,6 @@ __device__ __forceinline__ void phase_t(const SolverArgs& a, const Chunks& ch, c
 template <int WHAT>
 __device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& ch, float alpha, float beta) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int N = a.g.N;
     float* __restrict__ d = a.d0;
     float* __restrict__ r = a.r;
     float* __restrict__ e = a.e;
@@ -403,22 +408,24 @@ __device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& 
     FSum acc;
     for (int cb = warp * UA; cb < ch.n; cb += SOLVER_WARPS * UA) {
         int idx[UA];
-        uint16_t f[UA];
+        bool act[UA];
 #pragma unroll
-        for (int u = 0; u < UA; u++) idx[u] = (cb + u < ch.n) ? ch.ids[cb + u] * 32 + lane : -1;
-#pragma unroll
-        for (int u = 0; u < UA; u++) f[u] = (idx[u] >= 0 && idx[u] < N) ? a.rowinfo[idx[u]] : 0;
+        for (int u = 0; u < UA; u++) {
+            const int c = cb + u;
+            act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
+            idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
+        }
         float dv[UA], tv[UA], rv[UA], ev[UA];
 #pragma unroll
         for (int u = 0; u < UA; u++) {
-            const int i = idx[u] < 0 ? 0 : idx[u];
+            const int i = idx[u];   // 0 for lanes without a row: one cached line
             dv[u] = d[i];
             if (WHAT & 1) { tv[u] = t[i]; ev[u] = e[i]; }
             rv[u] = r[i];
         }
 #pragma unroll
         for (int u = 0; u < UA; u++) {
-            if (!(f[u] & 0x8000u)) continue;
+            if (!act[u]) continue;
             const int i = idx[u];
             if (WHAT & 1) e[i] = ev[u] + alpha * dv[u];
             if (WHAT == 3) {
@@ -625,6 +632,19 @@ __device__ __forceinline__ bool solver_prologue(const SolverArgs& a, Chunks& ch,
         ch.ids = s_chunks;
         ch.n = max(0, c1 - c0);
         for (int k = threadIdx.x; k < ch.n; k += SOLVER_THREADS) s_chunks[k] = ((volatile int*)a.chunk_list)[c0 + k];
+        __syncthreads();
+        // Row lanes of every chunk (rowinfo is fixed during the solve).  The hot passes load and store only
+        // these lanes, so the sectors of a chunk that hold no row are never fetched: a liquid region whose x
+        // extent ends inside a chunk costs its touched 32-byte sectors, not the whole chunk.
+        unsigned* s_mask = reinterpret_cast<unsigned*>(s_chunks + ch.n);
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int c = warp; c < ch.n; c += SOLVER_WARPS) {
+            const int i = s_chunks[c] * 32 + lane;
+            const bool row = i < a.g.N && (a.rowinfo[i] & 0x8000u);
+            const unsigned m = __ballot_sync(0xffffffffu, row);
+            if (lane == 0) s_mask[c] = m;
+        }
+        ch.mask = s_mask;
         __syncthreads();
     }
 
@@ -911,7 +931,7 @@ cudaError_t ensure_solver_smem(size_t bytes) {
 cudaError_t solver_shape(int n_chunks, int sm_count, int* blocks_out, size_t* smem_out) {
     int blocks = sm_count;
     for (int bps = 2; bps >= 1; bps--) {
-        const size_t smem = (size_t)((n_chunks + bps * sm_count - 1) / (bps * sm_count)) * sizeof(int);
+        const size_t smem = (size_t)((n_chunks + bps * sm_count - 1) / (bps * sm_count)) * 2 * sizeof(int);
         cudaError_t e = ensure_solver_smem(smem);
         if (e != cudaSuccess) return e;
         int occ = 0;
@@ -923,7 +943,7 @@ cudaError_t solver_shape(int n_chunks, int sm_count, int* blocks_out, size_t* sm
     const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
     blocks = std::max(1, std::min(blocks, want));
     *blocks_out = blocks;
-    *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * sizeof(int);
+    *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * 2 * sizeof(int);   // chunk ids and row masks
     return ensure_solver_smem(*smem_out);
 }
 
