@@ -153,11 +153,16 @@ __device__ __forceinline__ void block_sum3(FSum& a, FSum& b, FSum& c) {
 // (6 floats) in slot `slot`; after the barrier every block adds all blocks' partials in the same fixed order
 // (thread k loads block k's, then block_sum3), so every block obtains bit-identical totals and takes the same
 // branches.  A slot is rewritten two reductions later, after every block has passed the barrier between.
+// Thread 0 also compares the first total with `below` and every thread reads the result as `lt`, so the
+// stop test costs the block one integer instead of an FP64 comparison per warp.
 struct Reduction {
     float* partials;           // 2 slots x gridDim.x x 6 floats
     int slot;
+    double below = 0.0;
+    int lt = 0;                // ta < below, for the last run
     __device__ bool run(DevCtl* ctl, FSum a, FSum b, FSum c, double& ta, double& tb, double& tc) {
         __shared__ double s_tot[3];
+        __shared__ int s_lt;
         block_sum3(a, b, c);
         float* mine = partials + ((size_t)slot * gridDim.x + blockIdx.x) * 6;
         if (threadIdx.x == 0) {
@@ -176,9 +181,11 @@ struct Reduction {
             s_tot[0] = (double)x.s + (double)x.c;
             s_tot[1] = (double)y.s + (double)y.c;
             s_tot[2] = (double)z.s + (double)z.c;
+            s_lt = s_tot[0] < below;
         }
         __syncthreads();
         ta = s_tot[0]; tb = s_tot[1]; tc = s_tot[2];
+        lt = s_lt;
         __syncthreads();
         slot ^= 1;
         return true;
@@ -738,6 +745,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         thr_f = a.solver_threshold;
     }
     const double thr = (double)thr_f;
+    red.below = thr;
 
     // residual recomputation (CGSolver.cpp:447-451): fold e into p64 and r = b - L p64 in FP64 (mixed), or
     // r = b - L p in FP32 (reference)
@@ -777,18 +785,23 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         }
         int it;
         for (it = 0; it < a.max_steps; it++) {
-            // breakdown (a singular block: a liquid region with no air neighbour): stop, not converged
-            if (!(dt != 0.0) || !isfinite(rr / dt)) break;
+            // The FP64 scalar work of an iteration is thread 0's: GB300 runs FP64 at a small fraction of its
+            // FP32 rate, and a division in every thread cost the whole block microseconds per iteration.
             float alpha = 0.f, bet = 0.f;
             int recur = 0;
             if (threadIdx.x == 0) {
                 const double ad = div_fast(rr, dt);
-                alpha = (float)ad;
-                const double est = ad * ad * tt * div_fast(1.0, rr) - 1.0;   // r'.r' / r.r from the recurrence
-                recur = (it & 0x3F) && est > 0.0;
-                bet = (float)est;
+                if (!(dt != 0.0) || !isfinite(ad)) {
+                    recur = -1;   // breakdown (a singular block: a liquid region with no air neighbour)
+                } else {
+                    alpha = (float)ad;
+                    const double est = ad * ad * tt * div_fast(1.0, rr) - 1.0;   // r'.r' / r.r from the recurrence
+                    recur = (it & 0x3F) && est > 0.0;
+                    bet = (float)est;
+                }
             }
             block_scalars(alpha, bet, &recur);
+            if (recur < 0) break;   // stop, not converged
             const double old = rr;
             if (recur) {
                 const FSum rp = phase_update<3>(a, ch, alpha, bet);
@@ -796,11 +809,11 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
                 FSum dtp, ttp;
                 phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
                 if (!red.run(ctl, rp, dtp, ttp, rr, dt, tt)) return;
-                if (rr < thr) {
+                if (red.lt) {
                     // confirm on the recomputed residual; if that is above the threshold, the direction (formed
                     // from the recurrence residual, so r.d != r.r now) restarts from it: d = r, t = L d
                     if (!replace(rr)) return;
-                    if (rr < thr) { conv = 1; break; }
+                    if (red.lt) { conv = 1; break; }
                     for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) a.d0[i] = r[i]; });
                     if (!grid_barrier(ctl)) return;
                     FSum dtp2, ttp2;
@@ -811,7 +824,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
                 phase_update<1>(a, ch, alpha, 0.f);
                 __syncthreads();   // replace() folds e with another cell-to-thread mapping
                 if (!replace(rr)) return;
-                if (rr < thr) { conv = 1; break; }
+                if (red.lt) { conv = 1; break; }
                 float b2 = 0.f, unused = 0.f;
                 if (threadIdx.x == 0) b2 = (float)(rr / old);
                 block_scalars(b2, unused);
@@ -832,8 +845,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
             const FSum dt_p = phase_a(a, ch, it, beta, dprev, dcur, nb);
             double dt;
             if (!red.run(ctl, dt_p, FSum(), 0, dt, u1, u2)) return;
-            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown: stop, not converged
-            const float alpha = block_scalar(threadIdx.x == 0 ? (float)(rr / dt) : 0.f);
+            float alpha = 0.f, unused = 0.f;
+            int brk = 0;
+            if (threadIdx.x == 0) {
+                const double q = rr / dt;
+                if (!(dt != 0.0) || !isfinite(q)) brk = 1; else alpha = (float)q;
+            }
+            block_scalars(alpha, unused, &brk);
+            if (brk) break;   // breakdown: stop, not converged
             // B: p (or e) += alpha d; r -= alpha L d, or the true residual every 64 iterations (:442-451)
             const double old = rr;
             bool replaced = false;
