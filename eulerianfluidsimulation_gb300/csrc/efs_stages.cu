@@ -155,9 +155,11 @@ __device__ __forceinline__ void d_sharpen_calc(const Geo& g, int bx, int by, int
     // warp-aggregated append
     const unsigned mask = __ballot_sync(0xffffffffu, active);
     if (mask == 0) return;
-    const int lane = threadIdx.x & 31;
+    // the lane within the warp: blocks are 2D (tile_x x tile_y) and tile_x may be below 32, so threadIdx.x is not it
+    unsigned lane;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
     int base = 0;
-    if (lane == __ffs(mask) - 1) base = atomicAdd(&ctl->sh_count, __popc(mask));
+    if ((int)lane == __ffs(mask) - 1) base = atomicAdd(&ctl->sh_count, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
     if (active) {
         const int slot = base + __popc(mask & ((1u << lane) - 1u));
@@ -480,6 +482,20 @@ __global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int*
 // depends on earlier steps: every cell is read from memory before this thread writes it, and lines are
 // disjoint, so the loads of the next kPf cells are issued while the current kPf cells are processed.
 constexpr int kPf = 16;
+// One pairwise transfer between the carried cell j and the next cell i along the line.
+__device__ __forceinline__ void diffuse_pair(float& rj, float& gj, bool sj, float& ri, float& gi, bool si) {
+    if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
+        const float avg = (gj + gi) / 2.f;
+        if (gj > gi) {
+            const float dif = rj * (gj - gi) / (2.f * gj);
+            rj -= dif; ri += dif;
+        } else {
+            const float dif = ri * (gi - gj) / (2.f * gi);
+            ri -= dif; rj += dif;
+        }
+        gj = avg; gi = avg;
+    }
+}
 struct LineBlock {
     float r[kPf], g[kPf];
     unsigned solid;   // bit k: cell k of the block is solid
@@ -515,17 +531,7 @@ __device__ __forceinline__ void diffuse_line(const float* __restrict__ rsrc, con
             const int ii = jj + stride;
             float ri = cur.r[k], gi = cur.g[k];
             const bool si = (cur.solid >> k) & 1u;
-            if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
-                const float avg = (gj + gi) / 2.f;
-                if (gj > gi) {
-                    const float dif = rj * (gj - gi) / (2.f * gj);
-                    rj -= dif; ri += dif;
-                } else {
-                    const float dif = ri * (gi - gj) / (2.f * gi);
-                    ri -= dif; rj += dif;
-                }
-                gj = avg; gi = avg;
-            }
+            diffuse_pair(rj, gj, sj, ri, gi, si);
             rdst[jj] = rj; gdst[jj] = gj;
             jj = ii; rj = ri; gj = gi; sj = si;
         }
@@ -541,9 +547,71 @@ __device__ __forceinline__ void d_diffuse_x(const Geo& g, int bx, int by, int bz
     if (y > g.H - 2) return;
     diffuse_line(rsrc, gsrc, rdst, gdst, solid, z * g.WH + y * g.W, 1, g.W);
 }
-__global__ void k_diffuse_x(Geo g, int dim, const float* rsrc, const float* gsrc, float* rdst, float* gdst,
-                            const uint8_t* __restrict__ solid) {
-    d_diffuse_x(g, blockIdx.x, blockIdx.y, blockIdx.z, dim, rsrc, gsrc, rdst, gdst, solid);
+// X sweep of a single grid through shared memory.  Along x a thread's line is contiguous, so one thread per
+// line reads 32 different lines per warp instruction.  Here a warp owns 32 lines (consecutive y, one plane)
+// and walks them in 32-cell tiles: each tile comes in row by row (one 128-byte row per instruction) into a
+// padded shared tile, lane l runs the sequential transfers of line l out of shared memory, and the tile goes
+// back row by row.  Cell x0 - 1, which becomes final at the first pair of a tile after its own tile was
+// stored, and the last cell of the line are written by the lane directly.  Same arithmetic and order as
+// diffuse_line.
+constexpr int kDxWarps = 4;
+__global__ void __launch_bounds__(kDxWarps * 32) k_diffuse_x(Geo g, int dim, const float* rsrc, const float* gsrc,
+                                                               float* rdst, float* gdst, const uint8_t* __restrict__ solid) {
+    __shared__ float s_r[kDxWarps][32][33], s_g[kDxWarps][32][33];
+    __shared__ unsigned s_m[kDxWarps][32];   // per line: bit p = cell x0 + p is solid
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y0 = 1 + (blockIdx.x * kDxWarps + warp) * 32;
+    const int z = (dim == 3) ? 1 + blockIdx.y : 0;
+    const int nlines = min(32, g.H - 1 - y0);   // lines y0 .. y0 + nlines - 1 (y <= H - 2)
+    if (nlines <= 0) return;                    // warp-uniform
+    const int n = g.W;
+    const size_t plane = (size_t)z * g.WH;
+    float (*tr)[33] = s_r[warp];
+    float (*tg)[33] = s_g[warp];
+    unsigned* tm = s_m[warp];
+    const size_t mine = plane + (size_t)(y0 + lane) * n;   // start of lane's own line (valid for lane < nlines)
+    float rj = 0.f, gj = 0.f;
+    bool sj = false;
+    for (int x0 = 0; x0 <= n - 2; x0 += 32) {
+        const int x = x0 + lane;
+        for (int j = 0; j < nlines; j++) {
+            const size_t i = plane + (size_t)(y0 + j) * n + x;
+            bool sol = false;
+            if (x <= n - 2) {
+                tr[j][lane] = rsrc[i];
+                tg[j][lane] = gsrc[i];
+                sol = solid[i] != 0;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, sol);
+            if (lane == 0) tm[j] = m;
+        }
+        __syncwarp();
+        if (lane < nlines) {
+            const unsigned m = tm[lane];
+            int p = 0;
+            if (x0 == 0) { rj = tr[lane][1]; gj = tg[lane][1]; sj = (m >> 1) & 1u; p = 2; }
+            const int pend = min(31, n - 2 - x0);   // last cell of this tile that is processed
+            for (; p <= pend; p++) {
+                float ri = tr[lane][p], gi = tg[lane][p];
+                const bool si = (m >> p) & 1u;
+                diffuse_pair(rj, gj, sj, ri, gi, si);
+                if (p == 0) { rdst[mine + x0 - 1] = rj; gdst[mine + x0 - 1] = gj; }
+                else { tr[lane][p - 1] = rj; tg[lane][p - 1] = gj; }
+                rj = ri; gj = gi; sj = si;
+            }
+            if (x0 + 31 >= n - 2 && n >= 3) { rdst[mine + n - 2] = rj; gdst[mine + n - 2] = gj; }
+        }
+        __syncwarp();
+        // cells finalised in this tile: x in [max(1, x0), min(n - 3, x0 + 30)]
+        if (lane <= 30 && x >= 1 && x <= n - 3) {
+            for (int j = 0; j < nlines; j++) {
+                const size_t i = plane + (size_t)(y0 + j) * n + x;
+                rdst[i] = tr[j][lane];
+                gdst[i] = tg[j][lane];
+            }
+        }
+        __syncwarp();
+    }
 }
 // Y sweep: one thread per (x, z) line (consecutive threads = consecutive x: coalesced).
 __device__ __forceinline__ void d_diffuse_y(const Geo& g, int bx, int by, int bz, int dim, float* rho, float* gamma, const uint8_t* __restrict__ solid) {
@@ -950,7 +1018,8 @@ static cudaError_t stage_advect_t(efs_ctx* c) {
     const int iters = (DIM == 3) ? 3 : 7;
     for (int it = 0; it < iters; it++) {
         const float* rs = (it == 0) ? c->rho_acc : c->rho;
-        k_diffuse_x<<<dim3((g.H - 2 + 127) / 128, DIM == 3 ? g.D - 2 : 1), 128, 0, c->stream>>>(g, DIM, rs, c->gamma, c->rho, c->gamma, c->solid);
+        k_diffuse_x<<<dim3((g.H - 2 + kDxWarps * 32 - 1) / (kDxWarps * 32), DIM == 3 ? g.D - 2 : 1), kDxWarps * 32, 0,
+                      c->stream>>>(g, DIM, rs, c->gamma, c->rho, c->gamma, c->solid);
         EFS_LAUNCH_CHECK();
         k_diffuse_y<<<dim3((g.W - 2 + 127) / 128, DIM == 3 ? g.D - 2 : 1), 128, 0, c->stream>>>(g, DIM, c->rho, c->gamma, c->solid);
         EFS_LAUNCH_CHECK();

@@ -7,7 +7,9 @@
 - one full step of each scene against the oracle within the single-context step tolerances;
 - a step is the same number of kernel launches whatever the number of scenes (one persistent launch per
   stage kernel for all scenes), the autotuner returns a valid configuration, and stepping after it keeps
-  every scene converging with its liquid mass within 1e-5.
+  every scene converging with its liquid mass within 1e-5;
+- every tile shape and blocks-per-SM count the autotuner may pick gives the single context's stages and keeps
+  the liquid mass within 2e-6 over 10 steps.
 """
 import numpy as np
 import pytest
@@ -213,7 +215,9 @@ def _check_stages(B, tol_solve=1e-5):
 @pytest.mark.parametrize("tile", TILES)
 def test_every_tuning_the_autotuner_may_pick(tile):
     """Each stage tile shape, at each blocks-per-SM count the autotuner tries, gives every stage of every scene
-    as the single context does; the liquid mass holds over 10 steps."""
+    as the single context does; the liquid mass holds over 10 steps within 2e-6 (the default tiles drift about
+    1e-7).  Tiles narrower than a warp put two rows in one warp: the density-sharpen list append once took
+    the lane from threadIdx.x there, lost list entries and replayed stale ones, a drift of +1e-5 per 10 steps."""
     scenes = _scenes([0, 1, 2, 5])
     for bps in (2, 4, 8, 16):
         with _batch(scenes) as B:
@@ -229,4 +233,4 @@ def test_every_tuning_the_autotuner_may_pick(tile):
             B.synchronize()
             for s in range(B.n):
                 m = float(np.sum(B.field(s, abi.FIELD_RHO), dtype=np.float64))
-                assert abs(m - m0[s]) <= 1e-5 * m0[s], (tile, bps, s, m, m0[s])
+                assert abs(m - m0[s]) <= 2e-6 * m0[s], (tile, bps, s, (m - m0[s]) / m0[s])
