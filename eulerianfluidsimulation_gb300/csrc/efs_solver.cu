@@ -403,6 +403,57 @@ __device__ __forceinline__ void phase_t(const SolverArgs& a, const Chunks& ch, c
     }
 }
 
+// Pass 1 with 128-bit accesses, the layout of phase_update4: lane l computes t for cells 4 (l & 7) .. +3 of
+// chunk cb + l / 8.  The y and z neighbours are whole groups at +-W and +-W*H; the x neighbours inside a
+// group are its own components, across groups the next lane's (warp shuffles), and at a chunk's two ends
+// single loads.  A group without a row reads cell 0's neighbourhood and stores nothing.  Same per-cell
+// arithmetic and neighbour order as phase_t.  Needs d and t 16-byte aligned, rowinfo 8-byte aligned and W a
+// multiple of 4.
+__device__ __forceinline__ void phase_t4(const SolverArgs& a, const Chunks& ch, const Nb& nb, FSum& dt, FSum& tt) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane >> 3, q = (lane & 7) * 4;
+    const float* __restrict__ d = a.d0;
+    const float4* __restrict__ d4 = reinterpret_cast<const float4*>(a.d0);
+    float4* __restrict__ t4 = reinterpret_cast<float4*>(a.t);
+    const uint2* __restrict__ info4 = reinterpret_cast<const uint2*>(a.rowinfo);
+    const int oy = nb.o[3] >> 2, oz = nb.o[4] >> 2;   // +W / 4 and +W*H / 4 (0 in 2D)
+    for (int cb = warp * 4; cb < ch.n; cb += SOLVER_WARPS * 4) {
+        const int c = cb + sub;
+        const unsigned m = c < ch.n ? (ch.mask[c] >> q) & 0xFu : 0u;
+        const int i = m ? ch.ids[c] * 32 + q : 0;
+        const int g = i >> 2;
+        const uint2 fi = info4[g];
+        const float4 xc = d4[g], ym = d4[g - oy], yp = d4[g + oy], zp = d4[g + oz], zm = d4[g - oz];
+        float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
+        float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
+        if ((lane & 7) == 0) left = d[i - 1];
+        if ((lane & 7) == 7) right = d[i + 4];
+        if (!m) continue;
+        const float cx[4] = {xc.x, xc.y, xc.z, xc.w};
+        const float cym[4] = {ym.x, ym.y, ym.z, ym.w}, cyp[4] = {yp.x, yp.y, yp.z, yp.w};
+        const float czp[4] = {zp.x, zp.y, zp.z, zp.w}, czm[4] = {zm.x, zm.y, zm.z, zm.w};
+        const unsigned fw[4] = {fi.x & 0xFFFFu, fi.x >> 16, fi.y & 0xFFFFu, fi.y >> 16};
+        float to[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            to[k] = 0.f;
+            if (!((m >> k) & 1u)) continue;
+            const unsigned f = fw[k];
+            const float nv[6] = {k == 0 ? left : cx[k > 0 ? k - 1 : 0], k == 3 ? right : cx[k < 3 ? k + 1 : 3],
+                                 cym[k], cyp[k], czp[k], czm[k]};
+            float sum = 0.0f;
+#pragma unroll
+            for (int n = 0; n < 6; n++)
+                if (f & (1u << cg_bit(n))) sum += nv[n];
+            const float tv = sum - (float)((f >> 8) & 7) * cx[k];
+            to[k] = tv;
+            dt.add_prod(cx[k], tv);
+            tt.add_prod(tv, tv);
+        }
+        t4[g] = make_float4(to[0], to[1], to[2], to[3]);
+    }
+}
+
 // EFS_CG_MIXED_RECURRENCE, pass 2 (per cell, no neighbours): what = 3: e += alpha d, r += -alpha t,
 // d = d beta + r (sums r.r); what = 1: only e += alpha d; what = 2: only d = d beta + r.
 template <int WHAT>
@@ -443,6 +494,63 @@ __device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& 
             } else if (WHAT == 2) {
                 d[i] = dv[u] * beta + rv[u];
             }
+        }
+    }
+    return acc;
+}
+
+// Pass 2 (what = 3) with 128-bit accesses: lane l handles cells 4 (l & 7) .. 4 (l & 7) + 3 of chunk
+// cb + l / 8, so one warp instruction covers four chunks.  A group of four cells without a row reads cell 0's
+// group (one cached line) and stores nothing; in a group with rows, the cells that are not rows are written back
+// as read.  Same per-cell arithmetic as phase_update<3>.  Needs d, t, r and e 16-byte aligned.
+#ifndef EFS_SOLVER_UV
+#define EFS_SOLVER_UV 2
+#endif
+constexpr int UV = EFS_SOLVER_UV;
+__device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks& ch, float alpha, float beta) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane >> 3, q = (lane & 7) * 4;
+    float4* __restrict__ d = reinterpret_cast<float4*>(a.d0);
+    float4* __restrict__ r = reinterpret_cast<float4*>(a.r);
+    float4* __restrict__ e = reinterpret_cast<float4*>(a.e);
+    const float4* __restrict__ t = reinterpret_cast<const float4*>(a.t);
+    FSum acc;
+    for (int cb = warp * UV * 4; cb < ch.n; cb += SOLVER_WARPS * UV * 4) {
+        int idx[UV];
+        unsigned m[UV];
+#pragma unroll
+        for (int v = 0; v < UV; v++) {
+            const int c = cb + v * 4 + sub;
+            m[v] = c < ch.n ? (ch.mask[c] >> q) & 0xFu : 0u;
+            idx[v] = m[v] ? (ch.ids[c] * 32 + q) >> 2 : 0;
+        }
+        float4 dv[UV], tv[UV], rv[UV], ev[UV];
+#pragma unroll
+        for (int v = 0; v < UV; v++) {
+            dv[v] = d[idx[v]];
+            tv[v] = t[idx[v]];
+            rv[v] = r[idx[v]];
+            ev[v] = e[idx[v]];
+        }
+#pragma unroll
+        for (int v = 0; v < UV; v++) {
+            if (!m[v]) continue;
+            float* dd = &dv[v].x;
+            float* tt = &tv[v].x;
+            float* rr = &rv[v].x;
+            float* ee = &ev[v].x;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (!((m[v] >> k) & 1u)) continue;
+                ee[k] = ee[k] + alpha * dd[k];
+                const float rn = rr[k] + (-alpha) * tt[k];
+                rr[k] = rn;
+                dd[k] = dd[k] * beta + rn;
+                acc.add_prod(rn, rn);
+            }
+            e[idx[v]] = ev[v];
+            r[idx[v]] = rv[v];
+            d[idx[v]] = dv[v];
         }
     }
     return acc;
@@ -778,9 +886,13 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         // reduction and one plain barrier per iteration.  The stop test of iteration k is therefore taken
         // after the pass 1 of iteration k+1, whose t is then unused; e, r and p are unaffected.
         double dt, tt, u3;
+        // 128-bit passes when the vectors allow them (always for the context's own allocations)
+        const bool vec4 = ((reinterpret_cast<uintptr_t>(a.d0) | reinterpret_cast<uintptr_t>(a.r) |
+                            reinterpret_cast<uintptr_t>(a.e) | reinterpret_cast<uintptr_t>(a.t)) & 15u) == 0 &&
+                          (reinterpret_cast<uintptr_t>(a.rowinfo) & 7u) == 0 && (a.g.W & 3) == 0;
         {
             FSum dtp, ttp;
-            phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+            if (vec4) phase_t4(a, ch, nb, dtp, ttp); else phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
             if (!red.run(ctl, FSum(), dtp, ttp, u3, dt, tt)) return;
         }
         int it;
@@ -804,10 +916,10 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
             if (recur < 0) break;   // stop, not converged
             const double old = rr;
             if (recur) {
-                const FSum rp = phase_update<3>(a, ch, alpha, bet);
+                const FSum rp = vec4 ? phase_update4(a, ch, alpha, bet) : phase_update<3>(a, ch, alpha, bet);
                 if (!grid_barrier(ctl)) return;
                 FSum dtp, ttp;
-                phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+                if (vec4) phase_t4(a, ch, nb, dtp, ttp); else phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
                 if (!red.run(ctl, rp, dtp, ttp, rr, dt, tt)) return;
                 if (red.lt) {
                     // confirm on the recomputed residual; if that is above the threshold, the direction (formed
@@ -817,7 +929,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
                     for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) a.d0[i] = r[i]; });
                     if (!grid_barrier(ctl)) return;
                     FSum dtp2, ttp2;
-                    phase_t(a, ch, a.d0, a.t, nb, dtp2, ttp2);
+                    if (vec4) phase_t4(a, ch, nb, dtp2, ttp2); else phase_t(a, ch, a.d0, a.t, nb, dtp2, ttp2);
                     if (!red.run(ctl, FSum(), dtp2, ttp2, u3, dt, tt)) return;
                 }
             } else {
@@ -831,7 +943,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
                 phase_update<2>(a, ch, 0.f, b2);
                 if (!grid_barrier(ctl)) return;
                 FSum dtp, ttp;
-                phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
+                if (vec4) phase_t4(a, ch, nb, dtp, ttp); else phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
                 if (!red.run(ctl, FSum(), dtp, ttp, u3, dt, tt)) return;
             }
         }
