@@ -288,14 +288,34 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
             }
             double dt, tt, u3;
             grp.reduce3(dtp, ttp, BSum(), dt, tt, u3);
-            if (!(dt != 0.0) || !isfinite(rr / dt)) break;   // breakdown (singular block): not converged
-            const double ad = rr / dt;
-            const float alpha = (float)ad;
+            // The FP64 scalar work is one thread's per CTA (GB300 runs FP64 divisions slowly; in every thread
+            // they cost the scene's group microseconds per iteration).  Every CTA of a cluster computes the same
+            // values from the same totals.
+            __shared__ float s_sc[2];
+            __shared__ int s_mode;
+            if (threadIdx.x == 0) {
+                int mode = 0;
+                float al = 0.f, be = 0.f;
+                if (!(dt != 0.0) || !isfinite(rr / dt)) {
+                    mode = -1;                                 // breakdown (singular block): not converged
+                } else {
+                    const double ad = rr / dt;
+                    al = (float)ad;
+                    const double est = ad * ad * tt - rr;     // r'.r' from the CG recurrence
+                    if ((it & 0x3F) && est > 0.0) { mode = 1; be = (float)(est / rr); }
+                }
+                s_sc[0] = al;
+                s_sc[1] = be;
+                s_mode = mode;
+            }
+            __syncthreads();
+            const int mode = s_mode;
+            const float alpha = s_sc[0];
+            if (mode < 0) break;
             const double old = rr;
-            const double est = ad * ad * tt - rr;            // r'.r' from the CG recurrence
             bool replaced = false;
-            if ((it & 0x3F) && est > 0.0) {
-                const float beta = (float)(est / rr);
+            if (mode == 1) {
+                const float beta = s_sc[1];
                 BSum rp;
                 for (int i = i0; i < N; i += stride) {
                     if (!(info[i] & 0x8000u)) continue;
@@ -314,7 +334,10 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
                 grp.sync();
                 replace(rr);
                 replaced = true;
-                const float beta = (float)(rr / old);
+                __shared__ float s_b2;
+                if (threadIdx.x == 0) s_b2 = (float)(rr / old);
+                __syncthreads();
+                const float beta = s_b2;
                 for (int i = i0; i < N; i += stride)
                     if (info[i] & 0x8000u) d[i] = d[i] * beta + r[i];
                 grp.sync();
