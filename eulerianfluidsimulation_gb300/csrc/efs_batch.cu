@@ -275,16 +275,60 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
         grp.reduce3(rp, BSum(), BSum(), rr_out, u1, u2);
     };
     int conv = rr < thr, it = 0;
+    // 128-bit passes: a thread takes groups of four cells (consecutive lanes, consecutive groups), x
+    // neighbours across groups by warp shuffles.  Needs W (so N) a multiple of 4 and 16-byte aligned vectors.
+    const bool vec4 = (W & 3) == 0 && ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(t) |
+                                       reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(e)) & 15u) == 0 &&
+                      (reinterpret_cast<uintptr_t>(info) & 7u) == 0;
+    const int N4 = N >> 2, W4 = W >> 2, lane = threadIdx.x & 31;
     if (!conv) {
         for (it = 0; it < A.max_steps; it++) {
             BSum dtp, ttp;
-            for (int i = i0; i < N; i += stride) {
-                const uint16_t f = info[i];
-                if (!(f & 0x8000u)) continue;
-                const float ti = lap2_f(d, f, i, W);
-                t[i] = ti;
-                dtp.add_prod(d[i], ti);
-                ttp.add_prod(ti, ti);
+            if (vec4) {
+                // t = L d on rows (same neighbour order and rounding as lap2_f), d.t and t.t
+                const float4* d4 = reinterpret_cast<const float4*>(d);
+                float4* t4 = reinterpret_cast<float4*>(t);
+                for (int gb = i0 - lane; gb < N4; gb += stride) {
+                    const int g = gb + lane;
+                    const uint2 fi = g < N4 ? reinterpret_cast<const uint2*>(info)[g] : make_uint2(0u, 0u);
+                    const unsigned fw[4] = {fi.x & 0xFFFFu, fi.x >> 16, fi.y & 0xFFFFu, fi.y >> 16};
+                    const bool any = ((fw[0] | fw[1] | fw[2] | fw[3]) & 0x8000u) != 0;
+                    float4 xc = make_float4(0.f, 0.f, 0.f, 0.f), ym = xc, yp = xc;
+                    if (any) { xc = d4[g]; ym = d4[g - W4]; yp = d4[g + W4]; }   // rows are interior cells
+                    float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
+                    float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
+                    if (lane == 0 && (fw[0] & 0x8000u) && (fw[0] & 1u)) left = d[4 * g - 1];
+                    if (lane == 31 && (fw[3] & 0x8000u) && (fw[3] & 2u)) right = d[4 * g + 4];
+                    if (!any) continue;
+                    const float cx[4] = {xc.x, xc.y, xc.z, xc.w};
+                    const float cym[4] = {ym.x, ym.y, ym.z, ym.w}, cyp[4] = {yp.x, yp.y, yp.z, yp.w};
+                    float to[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        to[k] = 0.f;
+                        const unsigned f = fw[k];
+                        if (!(f & 0x8000u)) continue;
+                        float sm = 0.f;
+                        if (f & 1u) sm += (k == 0) ? left : cx[k > 0 ? k - 1 : 0];
+                        if (f & 2u) sm += (k == 3) ? right : cx[k < 3 ? k + 1 : 3];
+                        if (f & 4u) sm += cym[k];
+                        if (f & 8u) sm += cyp[k];
+                        const float ti = sm - (float)((f >> 8) & 7) * cx[k];
+                        to[k] = ti;
+                        dtp.add_prod(cx[k], ti);
+                        ttp.add_prod(ti, ti);
+                    }
+                    t4[g] = make_float4(to[0], to[1], to[2], to[3]);
+                }
+            } else {
+                for (int i = i0; i < N; i += stride) {
+                    const uint16_t f = info[i];
+                    if (!(f & 0x8000u)) continue;
+                    const float ti = lap2_f(d, f, i, W);
+                    t[i] = ti;
+                    dtp.add_prod(d[i], ti);
+                    ttp.add_prod(ti, ti);
+                }
             }
             double dt, tt, u3;
             grp.reduce3(dtp, ttp, BSum(), dt, tt, u3);
@@ -317,14 +361,43 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
             if (mode == 1) {
                 const float beta = s_sc[1];
                 BSum rp;
-                for (int i = i0; i < N; i += stride) {
-                    if (!(info[i] & 0x8000u)) continue;
-                    const float di = d[i];
-                    e[i] += alpha * di;
-                    const float rn = r[i] + (-alpha) * t[i];
-                    r[i] = rn;
-                    d[i] = di * beta + rn;
-                    rp.add_prod(rn, rn);
+                if (vec4) {
+                    for (int g = i0; g < N4; g += stride) {
+                        const uint2 fi = reinterpret_cast<const uint2*>(info)[g];
+                        const unsigned rows = ((fi.x >> 15) & 1u) | ((fi.x >> 30) & 2u) | (((fi.y >> 15) & 1u) << 2) |
+                                              ((fi.y >> 31) << 3);
+                        if (!rows) continue;
+                        float4 dv = reinterpret_cast<float4*>(d)[g], ev = reinterpret_cast<float4*>(e)[g];
+                        float4 rv = reinterpret_cast<float4*>(r)[g];
+                        const float4 tv = reinterpret_cast<const float4*>(t)[g];
+                        float* dd = &dv.x;
+                        float* ee = &ev.x;
+                        float* rr4 = &rv.x;
+                        const float* tt4 = &tv.x;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            if (!((rows >> k) & 1u)) continue;
+                            const float di = dd[k];
+                            ee[k] += alpha * di;
+                            const float rn = rr4[k] + (-alpha) * tt4[k];
+                            rr4[k] = rn;
+                            dd[k] = di * beta + rn;
+                            rp.add_prod(rn, rn);
+                        }
+                        reinterpret_cast<float4*>(e)[g] = ev;
+                        reinterpret_cast<float4*>(r)[g] = rv;
+                        reinterpret_cast<float4*>(d)[g] = dv;
+                    }
+                } else {
+                    for (int i = i0; i < N; i += stride) {
+                        if (!(info[i] & 0x8000u)) continue;
+                        const float di = d[i];
+                        e[i] += alpha * di;
+                        const float rn = r[i] + (-alpha) * t[i];
+                        r[i] = rn;
+                        d[i] = di * beta + rn;
+                        rp.add_prod(rn, rn);
+                    }
                 }
                 double u1, u2;
                 grp.reduce3(rp, BSum(), BSum(), rr, u1, u2);
