@@ -409,6 +409,10 @@ __device__ __forceinline__ void phase_t(const SolverArgs& a, const Chunks& ch, c
 // single loads.  A group without a row reads cell 0's neighbourhood and stores nothing.  Same per-cell
 // arithmetic and neighbour order as phase_t.  Needs d and t 16-byte aligned, rowinfo 8-byte aligned and W a
 // multiple of 4.
+#ifndef EFS_SOLVER_UVT
+#define EFS_SOLVER_UVT 1
+#endif
+constexpr int UVT = EFS_SOLVER_UVT;
 __device__ __forceinline__ void phase_t4(const SolverArgs& a, const Chunks& ch, const Nb& nb, FSum& dt, FSum& tt) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane >> 3, q = (lane & 7) * 4;
@@ -417,40 +421,105 @@ __device__ __forceinline__ void phase_t4(const SolverArgs& a, const Chunks& ch, 
     float4* __restrict__ t4 = reinterpret_cast<float4*>(a.t);
     const uint2* __restrict__ info4 = reinterpret_cast<const uint2*>(a.rowinfo);
     const int oy = nb.o[3] >> 2, oz = nb.o[4] >> 2;   // +W / 4 and +W*H / 4 (0 in 2D)
+    for (int cb = warp * 4 * UVT; cb < ch.n; cb += SOLVER_WARPS * 4 * UVT) {
+        unsigned m[UVT];
+        int i[UVT];
+        uint2 fi[UVT];
+        float4 xc[UVT], ym[UVT], yp[UVT], zp[UVT], zm[UVT];
+        float left[UVT], right[UVT];
+#pragma unroll
+        for (int v = 0; v < UVT; v++) {
+            const int c = cb + 4 * v + sub;
+            m[v] = c < ch.n ? (ch.mask[c] >> q) & 0xFu : 0u;
+            i[v] = m[v] ? ch.ids[c] * 32 + q : 0;
+            const int g = i[v] >> 2;
+            fi[v] = info4[g];
+            xc[v] = d4[g]; ym[v] = d4[g - oy]; yp[v] = d4[g + oy]; zp[v] = d4[g + oz]; zm[v] = d4[g - oz];
+        }
+#pragma unroll
+        for (int v = 0; v < UVT; v++) {
+            left[v] = __shfl_up_sync(0xffffffffu, xc[v].w, 1);
+            right[v] = __shfl_down_sync(0xffffffffu, xc[v].x, 1);
+            if ((lane & 7) == 0) left[v] = d[i[v] - 1];
+            if ((lane & 7) == 7) right[v] = d[i[v] + 4];
+        }
+#pragma unroll
+        for (int v = 0; v < UVT; v++) {
+            if (!m[v]) continue;
+            const float cx[4] = {xc[v].x, xc[v].y, xc[v].z, xc[v].w};
+            const float cym[4] = {ym[v].x, ym[v].y, ym[v].z, ym[v].w}, cyp[4] = {yp[v].x, yp[v].y, yp[v].z, yp[v].w};
+            const float czp[4] = {zp[v].x, zp[v].y, zp[v].z, zp[v].w}, czm[4] = {zm[v].x, zm[v].y, zm[v].z, zm[v].w};
+            const unsigned fw[4] = {fi[v].x & 0xFFFFu, fi[v].x >> 16, fi[v].y & 0xFFFFu, fi[v].y >> 16};
+            float to[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                to[k] = 0.f;
+                if (!((m[v] >> k) & 1u)) continue;
+                const unsigned f = fw[k];
+                const float nv[6] = {k == 0 ? left[v] : cx[k > 0 ? k - 1 : 0], k == 3 ? right[v] : cx[k < 3 ? k + 1 : 3],
+                                     cym[k], cyp[k], czp[k], czm[k]};
+                float sum = 0.0f;
+#pragma unroll
+                for (int n = 0; n < 6; n++)
+                    if (f & (1u << cg_bit(n))) sum += nv[n];
+                const float tv = sum - (float)((f >> 8) & 7) * cx[k];
+                to[k] = tv;
+                dt.add_prod(cx[k], tv);
+                tt.add_prod(tv, tv);
+            }
+            t4[i[v] >> 2] = make_float4(to[0], to[1], to[2], to[3]);
+        }
+    }
+}
+
+// One Jacobi sweep (JacobiSolver.cpp:176-205) with 128-bit accesses, the layout of phase_t4: dst = (sum of
+// the summed neighbours of src - b) / count on rows, neighbours in the reference order x-1, x+1, y-1, y+1,
+// z-1, z+1.  Cells that are not rows keep their dst value (per-cell stores in a group that is not all rows).
+// Needs src, dst and b 16-byte aligned, rowinfo 8-byte aligned and W a multiple of 4.
+__device__ __forceinline__ void jacobi_sweep4(const SolverArgs& a, const Chunks& ch, const float* __restrict__ src,
+                                              float* __restrict__ dst) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane >> 3, q = (lane & 7) * 4;
+    const float4* __restrict__ s4 = reinterpret_cast<const float4*>(src);
+    const float4* __restrict__ b4 = reinterpret_cast<const float4*>(a.b);
+    const uint2* __restrict__ info4 = reinterpret_cast<const uint2*>(a.rowinfo);
+    const int oy = a.g.W >> 2, oz = (a.g.D > 1) ? (a.g.WH >> 2) : 0;
     for (int cb = warp * 4; cb < ch.n; cb += SOLVER_WARPS * 4) {
         const int c = cb + sub;
         const unsigned m = c < ch.n ? (ch.mask[c] >> q) & 0xFu : 0u;
         const int i = m ? ch.ids[c] * 32 + q : 0;
         const int g = i >> 2;
         const uint2 fi = info4[g];
-        const float4 xc = d4[g], ym = d4[g - oy], yp = d4[g + oy], zp = d4[g + oz], zm = d4[g - oz];
+        const float4 xc = s4[g], ym = s4[g - oy], yp = s4[g + oy], zm = s4[g - oz], zp = s4[g + oz], bv = b4[g];
         float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
         float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
-        if ((lane & 7) == 0) left = d[i - 1];
-        if ((lane & 7) == 7) right = d[i + 4];
+        if ((lane & 7) == 0) left = src[i - 1];
+        if ((lane & 7) == 7) right = src[i + 4];
         if (!m) continue;
-        const float cx[4] = {xc.x, xc.y, xc.z, xc.w};
+        const float cx[4] = {xc.x, xc.y, xc.z, xc.w}, cb4[4] = {bv.x, bv.y, bv.z, bv.w};
         const float cym[4] = {ym.x, ym.y, ym.z, ym.w}, cyp[4] = {yp.x, yp.y, yp.z, yp.w};
-        const float czp[4] = {zp.x, zp.y, zp.z, zp.w}, czm[4] = {zm.x, zm.y, zm.z, zm.w};
+        const float czm[4] = {zm.x, zm.y, zm.z, zm.w}, czp[4] = {zp.x, zp.y, zp.z, zp.w};
         const unsigned fw[4] = {fi.x & 0xFFFFu, fi.x >> 16, fi.y & 0xFFFFu, fi.y >> 16};
-        float to[4];
+        float out[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            to[k] = 0.f;
-            if (!((m >> k) & 1u)) continue;
             const unsigned f = fw[k];
             const float nv[6] = {k == 0 ? left : cx[k > 0 ? k - 1 : 0], k == 3 ? right : cx[k < 3 ? k + 1 : 3],
-                                 cym[k], cyp[k], czp[k], czm[k]};
+                                 cym[k], cyp[k], czm[k], czp[k]};
             float sum = 0.0f;
 #pragma unroll
             for (int n = 0; n < 6; n++)
-                if (f & (1u << cg_bit(n))) sum += nv[n];
-            const float tv = sum - (float)((f >> 8) & 7) * cx[k];
-            to[k] = tv;
-            dt.add_prod(cx[k], tv);
-            tt.add_prod(tv, tv);
+                if (f & (1u << n)) sum += nv[n];
+            const int cnt = (f >> 8) & 7;
+            out[k] = cnt > 0 ? (sum - cb4[k]) / (float)cnt : 0.0f;
         }
-        t4[g] = make_float4(to[0], to[1], to[2], to[3]);
+        if (m == 0xFu) {
+            reinterpret_cast<float4*>(dst)[g] = make_float4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if ((m >> k) & 1u) dst[i + k] = out[k];
+        }
     }
 }
 
@@ -786,9 +855,17 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         for_rows(a, ch, [&](int i) { if (info[i] & 0x8000u) rows += 1; });
         double nrows;
         if (!red.run(ctl, FSum(), FSum(), rows, u1, u2, nrows)) return;
+        const bool vec4 = ((reinterpret_cast<uintptr_t>(a.p) | reinterpret_cast<uintptr_t>(a.e) |
+                            reinterpret_cast<uintptr_t>(a.b)) & 15u) == 0 &&
+                          (reinterpret_cast<uintptr_t>(a.rowinfo) & 7u) == 0 && (a.g.W & 3) == 0;
         for (int it = 0; it < iters; it++) {
             const float* src = (it & 1) ? a.e : a.p;
             float* dst = (it & 1) ? a.p : a.e;
+            if (vec4) {
+                jacobi_sweep4(a, ch, src, dst);
+                if (!grid_barrier(ctl)) return;
+                continue;
+            }
             for_rows(a, ch, [&](int i) {
                 const uint16_t f = info[i];
                 if (!(f & 0x8000u)) return;
