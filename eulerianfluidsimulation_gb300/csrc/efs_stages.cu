@@ -70,15 +70,21 @@ __global__ void k_extrap_init(Geo g, int dim, const float* __restrict__ rho, con
 }
 
 template <int DIM>
-__device__ __forceinline__ void d_extrap_pass(const Geo& g, int bx, int by, int bz, const float* __restrict__ su, const float* __restrict__ sv, const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du, float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV, const uint8_t* __restrict__ solid) {
+// From the second pass on (`settled`), the destination of a pass is the source of the pass before, so it
+// already holds every cell that pass copied: solid cells, cells that stayed invalid, and cells that were
+// valid in that pass's source mask, which is what dV holds before this pass writes it.  Those cells are
+// skipped; only cells that became valid in the last two passes are written.  Valid cells stay valid.
+__device__ __forceinline__ void d_extrap_pass(const Geo& g, int bx, int by, int bz, const float* __restrict__ su, const float* __restrict__ sv, const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du, float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV, const uint8_t* __restrict__ solid, bool settled = false) {
     int x, y, z = 0, i;
     if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if (solid[i]) {
+        if (settled) return;
         du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
         dV[i] = 0;
         return;
     }
     if (sV[i]) {
+        if (settled && dV[i]) return;
         du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
         dV[i] = 1;
         return;
@@ -97,6 +103,7 @@ __device__ __forceinline__ void d_extrap_pass(const Geo& g, int bx, int by, int 
     if (n > 0) {
         du[i] = s0 / n; dv[i] = s1 / n; if (DIM == 3) dw[i] = s2 / n;
     } else {
+        if (settled) return;
         du[i] = su[i]; dv[i] = sv[i]; if (DIM == 3) dw[i] = sw[i];
     }
     dV[i] = (n > 0) ? 1 : 0;
@@ -105,8 +112,8 @@ template <int DIM>
 __global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* __restrict__ sv,
                               const float* __restrict__ sw, const uint8_t* __restrict__ sV, float* __restrict__ du,
                               float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV,
-                              const uint8_t* __restrict__ solid) {
-    d_extrap_pass<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, su, sv, sw, sV, du, dv, dw, dV, solid);
+                              const uint8_t* __restrict__ solid, int settled) {
+    d_extrap_pass<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, su, sv, sw, sV, du, dv, dw, dV, solid, settled != 0);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -959,8 +966,8 @@ static cudaError_t stage_extrapolate(efs_ctx* c) {
         float* du = odd ? c->u : tu; float* dv = odd ? c->v : tv; float* dw = odd ? c->w : tw;
         const uint8_t* sV = odd ? c->validB : c->validA;
         uint8_t* dV = odd ? c->validA : c->validB;
-        if (c->dim == 3) k_extrap_pass<3><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid);
-        else k_extrap_pass<2><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid);
+        if (c->dim == 3) k_extrap_pass<3><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
+        else k_extrap_pass<2><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
         EFS_LAUNCH_CHECK();
     }
     return cudaSuccess;
@@ -1163,7 +1170,7 @@ __global__ void kb_extrap_init(BView t, BFields F) {
         d_extrap_init(S.g, E.bx, 0, 0, 2, F.rho + o, F.solid + o, F.validA + o);
     });
 }
-__global__ void kb_extrap_pass(BView t, BFields F, int odd) {
+__global__ void kb_extrap_pass(BView t, BFields F, int odd, int settled) {
     for_entries(t, [&](const BScene& S, const BEntry& E) {
         const long long o = S.base;
         const float* su = (odd ? F.tu : F.u) + o;
@@ -1172,7 +1179,7 @@ __global__ void kb_extrap_pass(BView t, BFields F, int odd) {
         float* dv = (odd ? F.v : F.tv) + o;
         const uint8_t* sV = (odd ? F.validB : F.validA) + o;
         uint8_t* dV = (odd ? F.validA : F.validB) + o;
-        d_extrap_pass<2>(S.g, E.bx, E.by, 0, su, sv, nullptr, sV, du, dv, nullptr, dV, F.solid + o);
+        d_extrap_pass<2>(S.g, E.bx, E.by, 0, su, sv, nullptr, sV, du, dv, nullptr, dV, F.solid + o, settled != 0);
     });
 }
 __global__ void kb_sharpen_calc(BView t, BFields F, float delT) {
@@ -1328,7 +1335,7 @@ cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force) {
             kb_extrap_init<<<bgrid(L.linear, L.grid), 256, 0, st>>>(L.linear, F);
             EFS_LAUNCH_CHECK();
             for (int it = 0; it < 6; it++) {
-                kb_extrap_pass<<<gi, blk, 0, st>>>(L.interior, F, it & 1);
+                kb_extrap_pass<<<gi, blk, 0, st>>>(L.interior, F, it & 1, it >= 1);
                 EFS_LAUNCH_CHECK();
             }
             return cudaSuccess;
