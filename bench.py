@@ -321,7 +321,7 @@ def run_gb300(a):
         e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
                "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e,
                "api": "efs_step_host: upload vel,rho,gamma,boundary,forces + one step + download vel,rho,gamma,beta,div,p "
-                      "(page-locked buffers; gamma/forces up and rho/gamma/beta down overlap the step)"}
+                      "(page-locked buffers; gamma/forces up and rho/gamma/beta/div down overlap the step)"}
     st2 = sim.stats()
     sim.close()
 

@@ -94,6 +94,7 @@ cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
         cudaError_t e;
         if (s == EFS_STAGE_PROJECT) {
             if ((e = efs::launch_project_pre(c)) != cudaSuccess) return e;
+            if (timing_events && (e = cudaEventRecordWithFlags(c->ev_projected, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
             if (timing_events && (e = cudaEventRecordWithFlags(c->ev_solve_begin, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
             if ((e = efs::launch_solver(c)) != cudaSuccess) return e;
             if (timing_events && (e = cudaEventRecordWithFlags(c->ev_solve_end, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
@@ -246,6 +247,7 @@ void efs_destroy(efs_ctx* c) {
     if (c->xfer) { cudaStreamSynchronize(c->xfer); cudaStreamDestroy(c->xfer); }
     if (c->ev_late) cudaEventDestroy(c->ev_late);
     if (c->ev_advected) cudaEventDestroy(c->ev_advected);
+    if (c->ev_projected) cudaEventDestroy(c->ev_projected);
     if (c->ev_early) cudaEventDestroy(c->ev_early);
     if (c->ev_solve_end) cudaEventDestroy(c->ev_solve_end);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -308,6 +310,7 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
     if ((e = cudaEventCreate(&c->ev_solve_begin)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_late, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_advected, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_projected, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
     if ((e = cudaEventCreate(&c->ev_solve_end)) != cudaSuccess) return bail(e, "cudaEventCreate");
@@ -499,8 +502,9 @@ int efs_download_fields(efs_ctx* c, float* vel, float* rho, float* gamma, float*
 // One step with host fields in and out (the upload / update / download of a host-mirrored grid,
 // CudaGrid3D::upload and download around ISimulator::update).  With page-locked buffers the transfers that do
 // not block a stage overlap the step: gamma and forces are uploaded on the transfer stream while
-// vel_extrapolate and rho_sharpen run (the step graph waits for them before rho_advect), and rho, gamma and
-// beta, final after rho_advect, are downloaded on it while vel_advect and the pressure solve run.
+// vel_extrapolate and rho_sharpen run (the step graph waits for them before rho_advect), rho, gamma and
+// beta, final after rho_advect, are downloaded on it while vel_advect and the pressure solve run, and the
+// divergence, final after project_pre, while the solve runs.
 int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* gamma, const float* boundary,
                   const float* forces, float* vel_out, float* rho_out, float* gamma_out, float* beta_out, float* div_out,
                   float* p_out) {
@@ -508,7 +512,7 @@ int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* g
     auto locked = [](const void* p) { return !p || mapped(p) != nullptr; };
     // the copy engine overlaps only page-locked transfers with kernels
     const bool overlap = c->prm.solver != EFS_SOLVER_FCG_UNET && locked(gamma) && locked(forces) && locked(rho_out) &&
-                         locked(gamma_out) && locked(beta_out);
+                         locked(gamma_out) && locked(beta_out) && locked(div_out);
     int s;
     if (!overlap) {
         if ((s = efs_upload_fields(c, vel, rho, gamma, boundary, forces)) != EFS_OK) return s;
@@ -541,9 +545,11 @@ int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* g
     if (rho_out && (s = enqueue_download(c, EFS_FIELD_RHO, rho_out, c->xfer)) != EFS_OK) return s;
     if (gamma_out && (s = enqueue_download(c, EFS_FIELD_GAMMA, gamma_out, c->xfer)) != EFS_OK) return s;
     if (beta_out && (s = enqueue_download(c, EFS_FIELD_BETA, beta_out, c->xfer)) != EFS_OK) return s;
+    // the divergence, final after project_pre, while the pressure solve runs
+    CK(cudaStreamWaitEvent(c->xfer, c->ev_projected, 0), "cudaStreamWaitEvent");
+    if (div_out && (s = enqueue_download(c, EFS_FIELD_DIVERGENCE, div_out, c->xfer)) != EFS_OK) return s;
     // the fields of the last stages, after the step on the compute stream
     if (vel_out && (s = enqueue_download(c, EFS_FIELD_VEL, vel_out)) != EFS_OK) return s;
-    if (div_out && (s = enqueue_download(c, EFS_FIELD_DIVERGENCE, div_out)) != EFS_OK) return s;
     if (p_out && (s = enqueue_download(c, EFS_FIELD_PRESSURE, p_out)) != EFS_OK) return s;
     CK(cudaStreamSynchronize(c->xfer), "cudaStreamSynchronize");
     return check_device_status(c);

@@ -152,6 +152,7 @@ struct efs_ctx {
     // inputs) before rho_advect and records `ev_advected` after it
     cudaStream_t xfer = nullptr;
     cudaEvent_t ev_late = nullptr, ev_advected = nullptr;
+    cudaEvent_t ev_projected = nullptr;   // recorded after project_pre: the divergence is final
     cudaEvent_t ev_early = nullptr;         // the first stages' inputs are on the device
     float* fstage = nullptr;                // efs_step_host: staging of the forces (dim floats a cell)
 };
