@@ -489,19 +489,23 @@ __global__ void k_adv_apply_cols(Geo g, const float* __restrict__ wf, const int*
 // depends on earlier steps: every cell is read from memory before this thread writes it, and lines are
 // disjoint, so the loads of the next kPf cells are issued while the current kPf cells are processed.
 constexpr int kPf = 16;
-// One pairwise transfer between the carried cell j and the next cell i along the line.
+// One pairwise transfer between the carried cell j and the next cell i along the line.  The sweep is a
+// sequential chain per line, so its speed is this function's latency: both directions share one division,
+// formed from selected operands (the same operations in the same order as either branch), and the result is
+// applied by selects, so no lane of a warp waits on another lane's branch.
 __device__ __forceinline__ void diffuse_pair(float& rj, float& gj, bool sj, float& ri, float& gi, bool si) {
-    if (!(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi)) {
-        const float avg = (gj + gi) / 2.f;
-        if (gj > gi) {
-            const float dif = rj * (gj - gi) / (2.f * gj);
-            rj -= dif; ri += dif;
-        } else {
-            const float dif = ri * (gi - gj) / (2.f * gi);
-            ri -= dif; rj += dif;
-        }
-        gj = avg; gi = avg;
-    }
+    const bool act = !(si || sj) && !(gj < 1e-5f || gi < 1e-5f) && !(gj == gi);
+    const bool down = gj > gi;   // mass moves from j to i
+    const float avg = (gj + gi) / 2.f;
+    const float num = down ? rj * (gj - gi) : ri * (gi - gj);
+    const float den = 2.f * (down ? gj : gi);
+    const float dif = num / den;
+    const float rjn = down ? rj - dif : rj + dif;
+    const float rin = down ? ri + dif : ri - dif;
+    rj = act ? rjn : rj;
+    ri = act ? rin : ri;
+    gj = act ? avg : gj;
+    gi = act ? avg : gi;
 }
 struct LineBlock {
     float r[kPf], g[kPf];
