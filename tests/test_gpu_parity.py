@@ -86,7 +86,8 @@ def test_stage_matches_oracle(dim, n, stage):
         assert_fields(got, want, 1e-5, fields=(abi.FIELD_PRESSURE, abi.FIELD_VEL), what="project")
 
 
-@pytest.mark.parametrize("dim,n", [(3, 32), (2, 64)])
+# widths that are not a multiple of 4 (30, 62) run the solver's scalar passes, the others its 128-bit passes
+@pytest.mark.parametrize("dim,n", [(3, 32), (2, 64), (3, 30), (2, 62)])
 @pytest.mark.parametrize("solver,variant", [(abi.SOLVER_JACOBI, abi.CG_MIXED), (abi.SOLVER_CG, abi.CG_REFERENCE),
                                             (abi.SOLVER_CG, abi.CG_MIXED), (abi.SOLVER_CG, abi.CG_MIXED_RECURRENCE)])
 def test_project_solvers(dim, n, solver, variant):
