@@ -576,6 +576,7 @@ __device__ __forceinline__ FSum phase_update(const SolverArgs& a, const Chunks& 
 #define EFS_SOLVER_UV 2
 #endif
 constexpr int UV = EFS_SOLVER_UV;
+template <int WHAT = 3>
 __device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks& ch, float alpha, float beta) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane >> 3, q = (lane & 7) * 4;
@@ -597,9 +598,9 @@ __device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks&
 #pragma unroll
         for (int v = 0; v < UV; v++) {
             dv[v] = d[idx[v]];
-            tv[v] = t[idx[v]];
-            rv[v] = r[idx[v]];
-            ev[v] = e[idx[v]];
+            if (WHAT == 3) tv[v] = t[idx[v]];
+            if (WHAT & 2) rv[v] = r[idx[v]];
+            if (WHAT & 1) ev[v] = e[idx[v]];
         }
 #pragma unroll
         for (int v = 0; v < UV; v++) {
@@ -611,15 +612,19 @@ __device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks&
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 if (!((m[v] >> k) & 1u)) continue;
-                ee[k] = ee[k] + alpha * dd[k];
-                const float rn = rr[k] + (-alpha) * tt[k];
-                rr[k] = rn;
-                dd[k] = dd[k] * beta + rn;
-                acc.add_prod(rn, rn);
+                if (WHAT & 1) ee[k] = ee[k] + alpha * dd[k];
+                if (WHAT == 3) {
+                    const float rn = rr[k] + (-alpha) * tt[k];
+                    rr[k] = rn;
+                    dd[k] = dd[k] * beta + rn;
+                    acc.add_prod(rn, rn);
+                } else if (WHAT == 2) {
+                    dd[k] = dd[k] * beta + rr[k];
+                }
             }
-            e[idx[v]] = ev[v];
-            r[idx[v]] = rv[v];
-            d[idx[v]] = dv[v];
+            if (WHAT & 1) e[idx[v]] = ev[v];
+            if (WHAT == 3) r[idx[v]] = rv[v];
+            if (WHAT & 2) d[idx[v]] = dv[v];
         }
     }
     return acc;
@@ -1010,14 +1015,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
                     if (!red.run(ctl, FSum(), dtp2, ttp2, u3, dt, tt)) return;
                 }
             } else {
-                phase_update<1>(a, ch, alpha, 0.f);
+                if (vec4) phase_update4<1>(a, ch, alpha, 0.f); else phase_update<1>(a, ch, alpha, 0.f);
                 __syncthreads();   // replace() folds e with another cell-to-thread mapping
                 if (!replace(rr)) return;
                 if (red.lt) { conv = 1; break; }
                 float b2 = 0.f, unused = 0.f;
                 if (threadIdx.x == 0) b2 = (float)(rr / old);
                 block_scalars(b2, unused);
-                phase_update<2>(a, ch, 0.f, b2);
+                if (vec4) phase_update4<2>(a, ch, 0.f, b2); else phase_update<2>(a, ch, 0.f, b2);
                 if (!grid_barrier(ctl)) return;
                 FSum dtp, ttp;
                 if (vec4) phase_t4(a, ch, nb, dtp, ttp); else phase_t(a, ch, a.d0, a.t, nb, dtp, ttp);
