@@ -630,6 +630,77 @@ __device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks&
     return acc;
 }
 
+// Residual replacement of the mixed-precision variants, in rounds of several chunks per warp whose loads do not
+// depend on rowinfo (a chunk at a time, each row's loads waiting for its rowinfo, made every replacement a
+// chain of dependent L2 round trips: about 145 µs at 256^3, 16 times a solve).  Same per-row arithmetic as
+// the per-row loops: p64 += e, e = 0, then r = b - L p64 in FP64 with the neighbours summed in order.
+#ifndef EFS_SOLVER_UR
+#define EFS_SOLVER_UR 1
+#endif
+constexpr int UR = EFS_SOLVER_UR;   // chunks per round of the FP64 residual (7 doubles a row: more would spill)
+__device__ __forceinline__ void fold_rows(const SolverArgs& a, const Chunks& ch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int cb = warp * UA; cb < ch.n; cb += SOLVER_WARPS * UA) {
+        int idx[UA];
+        bool act[UA];
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            const int c = cb + u;
+            act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
+            idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
+        }
+        double pv[UA];
+        float ev[UA];
+#pragma unroll
+        for (int u = 0; u < UA; u++) { pv[u] = a.p64[idx[u]]; ev[u] = a.e[idx[u]]; }
+#pragma unroll
+        for (int u = 0; u < UA; u++) {
+            if (!act[u]) continue;
+            a.p64[idx[u]] = pv[u] + (double)ev[u];
+            a.e[idx[u]] = 0.f;
+        }
+    }
+}
+__device__ __forceinline__ FSum residual_rows(const SolverArgs& a, const Chunks& ch, const Nb& nb) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    FSum acc;
+    for (int cb = warp * UR; cb < ch.n; cb += SOLVER_WARPS * UR) {
+        int idx[UR];
+        bool act[UR];
+#pragma unroll
+        for (int u = 0; u < UR; u++) {
+            const int c = cb + u;
+            act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
+            idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
+        }
+        uint16_t f[UR];
+        float bv[UR];
+        double xv[UR][7];
+#pragma unroll
+        for (int u = 0; u < UR; u++) {
+            const int i = idx[u];
+            f[u] = a.rowinfo[i];
+            bv[u] = a.b[i];
+            xv[u][6] = a.p64[i];
+#pragma unroll
+            for (int k = 0; k < 6; k++) xv[u][k] = a.p64[i + nb.o[k]];
+        }
+#pragma unroll
+        for (int u = 0; u < UR; u++) {
+            if (!act[u]) continue;
+            double sum = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (f[u] & (1u << cg_bit(k))) sum += xv[u][k];
+            const double lap = sum - (double)((f[u] >> 8) & 7) * xv[u][6];
+            const float ri = (float)((double)bv[u] - lap);
+            a.r[idx[u]] = ri;
+            acc.add_prod(ri, ri);
+        }
+    }
+    return acc;
+}
+
 // a / b in FP64 without the FP64 division sequence (about 550 cycles of dependent latency on GB300): a
 // float reciprocal refined by two Newton steps in FP64, relative error near 1e-16.  Falls back to the
 // division when b is outside the range where the float reciprocal is finite and normal.
@@ -940,22 +1011,22 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
     // residual recomputation (CGSolver.cpp:447-451): fold e into p64 and r = b - L p64 in FP64 (mixed), or
     // r = b - L p in FP32 (reference)
     auto replace = [&](double& rr_out) -> bool {
-        if (mixed) {
-            for_rows(a, ch, [&](int i) {
-                if (!(info[i] & 0x8000u)) return;
-                p64[i] += (double)e[i];
-                e[i] = 0.f;
-            });
-        }
+        // the fold reads e with its own chunk-to-warp mapping: every warp's update of e comes first
+        __syncthreads();
+        if (mixed) fold_rows(a, ch);
         if (!grid_barrier(ctl)) return false;
         FSum rp;
-        for_rows(a, ch, [&](int i) {
-            const uint16_t f = info[i];
-            if (!(f & 0x8000u)) return;
-            const float ri = mixed ? (float)((double)b[i] - lap_d(p64, f, i, nb)) : b[i] - lap_f(p, f, i, nb);
-            r[i] = ri;
-            rp.add_prod(ri, ri);
-        });
+        if (mixed) {
+            rp = residual_rows(a, ch, nb);
+        } else {
+            for_rows(a, ch, [&](int i) {
+                const uint16_t f = info[i];
+                if (!(f & 0x8000u)) return;
+                const float ri = b[i] - lap_f(p, f, i, nb);
+                r[i] = ri;
+                rp.add_prod(ri, ri);
+            });
+        }
         return red.run(ctl, rp, FSum(), 0, rr_out, u1, u2);
     };
 
