@@ -75,6 +75,10 @@ __device__ __forceinline__ void vinterp3(const float* __restrict__ u, const floa
     }
 }
 
+// a / d for d the distance of two (clamped) cell centres, which is exactly 1 or 0: a / 1 is a exactly, so only
+// other values divide (IEEE division is a long instruction sequence and the scalar samples run once per cell).
+__device__ __forceinline__ float div_spacing(float a, float d) { return d == 1.0f ? a : a / d; }
+
 // ScalField3D::interpolate (src/simulation/data/ScalField3D.cpp:18-107): samples at i + 0.5, clamped.
 __device__ __forceinline__ float sinterp3(const float* __restrict__ f, const Geo& g, float px, float py, float pz) {
     const int x = (int)px, y = (int)py, z = (int)pz;
@@ -98,7 +102,7 @@ __device__ __forceinline__ float sinterp3(const float* __restrict__ f, const Geo
     float f00, f01, f10, f11;
     if (dz2z1 < 1e-9f) { f00 = v1; f01 = v3; f10 = v5; f11 = v7; }
     else {
-        const float wz1 = (z2 - pz) / dz2z1, wz2 = (pz - z1) / dz2z1;
+        const float wz1 = div_spacing(z2 - pz, dz2z1), wz2 = div_spacing(pz - z1, dz2z1);
         f00 = wz1 * v0 + wz2 * v1; f01 = wz1 * v2 + wz2 * v3;
         f10 = wz1 * v4 + wz2 * v5; f11 = wz1 * v6 + wz2 * v7;
     }
@@ -106,12 +110,12 @@ __device__ __forceinline__ float sinterp3(const float* __restrict__ f, const Geo
     float fx1, fx2;
     if (dy2y1 < 1e-9f) { fx1 = f01; fx2 = f11; }
     else {
-        const float wy1 = (y2 - py) / dy2y1, wy2 = (py - y1) / dy2y1;
+        const float wy1 = div_spacing(y2 - py, dy2y1), wy2 = div_spacing(py - y1, dy2y1);
         fx1 = wy1 * f00 + wy2 * f01; fx2 = wy1 * f10 + wy2 * f11;
     }
     const float dx2x1 = x2 - x1;
     if (dx2x1 < 1e-9f) return fx2;
-    const float wx1 = (x2 - px) / dx2x1, wx2 = (px - x1) / dx2x1;
+    const float wx1 = div_spacing(x2 - px, dx2x1), wx2 = div_spacing(px - x1, dx2x1);
     return wx1 * fx1 + wx2 * fx2;
 }
 
@@ -219,11 +223,11 @@ __device__ __forceinline__ float sinterp2(const float* __restrict__ f, const Geo
     const float v0 = f[iy1 * g.W + ix1], v1 = f[iy2 * g.W + ix1], v2 = f[iy1 * g.W + ix2], v3 = f[iy2 * g.W + ix2];
     const float x1 = (float)ix1 + 0.5f, x2 = (float)ix2 + 0.5f, y1 = (float)iy1 + 0.5f, y2 = (float)iy2 + 0.5f;
     const float dx2x1 = x2 - x1;
-    float fxy1 = ((x2 - px) / dx2x1) * v0 + ((px - x1) / dx2x1) * v2;
-    float fxy2 = ((x2 - px) / dx2x1) * v1 + ((px - x1) / dx2x1) * v3;
+    float fxy1 = (div_spacing(x2 - px, dx2x1)) * v0 + (div_spacing(px - x1, dx2x1)) * v2;
+    float fxy2 = (div_spacing(x2 - px, dx2x1)) * v1 + (div_spacing(px - x1, dx2x1)) * v3;
     if ((double)dx2x1 < 1e-9) { fxy1 = v1; fxy2 = v3; }
     const float dy2y1 = y2 - y1;
-    float fxy = ((y2 - py) / dy2y1) * fxy1 + ((py - y1) / dy2y1) * fxy2;
+    float fxy = (div_spacing(y2 - py, dy2y1)) * fxy1 + (div_spacing(py - y1, dy2y1)) * fxy2;
     if ((double)dy2y1 < 1e-9) fxy = fxy1;
     return fxy;
 }
