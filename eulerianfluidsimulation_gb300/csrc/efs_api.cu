@@ -78,6 +78,7 @@ cudaError_t dalloc_halo(efs_ctx* c, T** p, size_t count) {
 // The launch sequence of one ISimulator::update() (include/simulation/simulator/ISimulator.h:12-38).
 cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
     const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
+    const bool chain = (stages & EFS_STAGE_BIT(EFS_STAGE_RHO_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT));
     for (int s = 0; s < EFS_STAGE_COUNT; s++) {
         // captured steps: gamma and forces uploaded by efs_step_host on the transfer stream are first read by
         // rho_advect; rho, gamma and beta are final after it (the later stages do not write them)
@@ -100,7 +101,7 @@ cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
             if (timing_events && (e = cudaEventRecordWithFlags(c->ev_solve_end, c->stream, cudaEventRecordExternal)) != cudaSuccess) return e;
             if ((e = efs::launch_project_post(c)) != cudaSuccess) return e;
         } else {
-            if ((e = efs::launch_stage(c, s, s == EFS_STAGE_VEL_ADVECT && fuse)) != cudaSuccess) return e;
+            if ((e = efs::launch_stage(c, s, s == EFS_STAGE_VEL_ADVECT && fuse, chain)) != cudaSuccess) return e;
         }
     }
     return cudaSuccess;

@@ -159,7 +159,9 @@ struct efs_ctx {
 
 namespace efs {
 // efs_stages.cu
-cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force);
+// chain_traces: rho_advect and vel_advect run back to back in this step; rho_advect keeps its back-trace ends
+// (tvel) and vel_advect samples at them instead of tracing again.
+cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force, bool chain_traces = false);
 cudaError_t launch_project_pre(efs_ctx* c);
 cudaError_t launch_project_post(efs_ctx* c);
 cudaError_t launch_solver_prep(efs_ctx* c);

@@ -296,21 +296,30 @@ __global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t*
 // Steps 1-4: back-trace (shared by steps 1 and 2, which trace the same point), gamma' at the trace end,
 // backward weights m_k / sum / gamma', column sums beta1.
 template <int DIM>
-__device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ gamma, float dt, float* __restrict__ wb, int* __restrict__ bb, float* __restrict__ bsum) {
+// `tend` (optional, 3 x N floats): the trace end of every interior cell, kept for vel_advect, whose back-trace
+// from the cell (CPUSimulator3D.cpp:478-504) is this one: same start, velocity, dt and substeps, and the
+// velocity does not change in between (a trace from a solid cell ends at its start).
+__device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ gamma, float dt, float* __restrict__ wb, int* __restrict__ bb, float* __restrict__ bsum, float* __restrict__ tend = nullptr) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, i;
     if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
-    if (solid[i]) { bb[i] = -1; return; }     // step 1 skips solids; step 2 finds no free corner for them
+    if (solid[i]) {                           // step 1 skips solids; step 2 finds no free corner for them
+        bb[i] = -1;
+        if (tend) { tend[i] = (float)x; tend[g.N + i] = (float)y; if (DIM == 3) tend[2 * (size_t)g.N + i] = (float)z; }
+        return;
+    }
     float px, py, pz = 0.f, gp;
     float m[K];
     int base;
     float sum;
     if (DIM == 3) {
         trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, -dt, 4, px, py, pz);
+        if (tend) { tend[i] = px; tend[g.N + i] = py; tend[2 * (size_t)g.N + i] = pz; }
         gp = sinterp3(gamma, g, px, py, pz);
         sum = corner_weights3(solid, g, px, py, pz, base, m);
     } else {
         trace2(u, v, solid, g, (float)x, (float)y, -dt, 4, px, py);
+        if (tend) { tend[i] = px; tend[g.N + i] = py; }
         gp = sinterp2(gamma, g, px, py);
         sum = corner_weights2(solid, g, px, py, base, m);
     }
@@ -329,8 +338,8 @@ template <int DIM>
 __global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* __restrict__ v,
                                const float* __restrict__ w, const uint8_t* __restrict__ solid,
                                const float* __restrict__ gamma, float dt, float* __restrict__ wb,
-                               int* __restrict__ bb, float* __restrict__ bsum) {
-    d_adv_backward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, gamma, dt, wb, bb, bsum);
+                               int* __restrict__ bb, float* __restrict__ bsum, float* __restrict__ tend) {
+    d_adv_backward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, gamma, dt, wb, bb, bsum, tend);
 }
 
 // Step 5: forward trace for beta_j < 1; forward weights (1 - beta_j) m_k / sum; their row sums into gsum.
@@ -669,6 +678,27 @@ __global__ void k_vadv_trace(Geo g, const float* __restrict__ u, const float* __
     d_vadv_trace<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, dt, tu, tv, tw);
 }
 
+// vel_advect's sample at a trace end kept by rho_advect (k_adv_backward's `tend`, in tu/tv/tw, read and
+// overwritten per cell).
+template <int DIM>
+__global__ void k_vadv_sample(Geo g, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ w, float* tu, float* tv, float* tw) {
+    int x, y, z = 0, i;
+    if (DIM == 3) { if (!cell3(g, blockIdx.x, blockIdx.y, blockIdx.z, x, y, z, i)) return; }
+    else { if (!cell2(g, blockIdx.x, blockIdx.y, x, y, i)) return; }
+    if (DIM == 3) {
+        const float px = tu[i], py = tv[i], pz = tw[i];
+        float a, b, c;
+        vinterp3(u, v, w, g, px - 0.5f, py - 0.5f, pz - 0.5f, a, b, c);
+        tu[i] = a; tv[i] = b; tw[i] = c;
+    } else {
+        const float px = tu[i], py = tv[i];
+        float a, b;
+        vinterp2(u, v, g, px - 0.5f, py - 0.5f, a, b);
+        tu[i] = a; tv[i] = b;
+    }
+}
+
 struct ForceArgs {
     int enabled;          // fuse add_force after the averaging
     int has_forces;       // forces field is not all zero
@@ -1004,14 +1034,15 @@ static cudaError_t stage_sharpen(efs_ctx* c) {
 }
 
 template <int DIM>
-static cudaError_t stage_advect_t(efs_ctx* c) {
+static cudaError_t stage_advect_t(efs_ctx* c, bool keep_trace = false) {
     const Geo& g = c->g;
     const size_t bytes = (size_t)g.N * sizeof(float);
     const dim3 b(BX, BY), gr = grid_interior(g, DIM);
     cudaError_t e;
     if ((e = cudaMemsetAsync(c->bsum, 0, bytes, c->stream)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(c->gsum, 0, bytes, c->stream)) != cudaSuccess) return e;
-    k_adv_backward<DIM><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->gamma, c->prm.dt, c->wb, c->bb, c->bsum);
+    k_adv_backward<DIM><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->gamma, c->prm.dt, c->wb, c->bb, c->bsum,
+                                                  keep_trace ? c->tvel : nullptr);
     EFS_LAUNCH_CHECK();
     k_adv_forward<DIM><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->bsum, c->prm.dt, c->wf, c->fb, c->gsum);
     EFS_LAUNCH_CHECK();
@@ -1053,17 +1084,21 @@ static ForceArgs force_args(efs_ctx* c, int enabled) {
     return f;
 }
 
-static cudaError_t stage_vel_advect(efs_ctx* c, bool fuse_force) {
+// `traced`: rho_advect of the same step left every interior cell's trace end in tvel (the step runs the
+// two stages back to back), so only the samples at the ends are taken.
+static cudaError_t stage_vel_advect(efs_ctx* c, bool fuse_force, bool traced = false) {
     const Geo& g = c->g;
     float* tu = c->tvel; float* tv = c->tvel + g.N; float* tw = c->tvel + 2 * (size_t)g.N;
     const dim3 b(BX, BY), gr = grid_interior(g, c->dim);
     const ForceArgs f = force_args(c, fuse_force ? 1 : 0);
     if (c->dim == 3) {
-        k_vadv_trace<3><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
+        if (traced) k_vadv_sample<3><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, tu, tv, tw);
+        else k_vadv_trace<3><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
         EFS_LAUNCH_CHECK();
         k_vadv_average<3><<<gr, b, 0, c->stream>>>(g, tu, tv, tw, c->solid, c->u, c->v, c->w, f);
     } else {
-        k_vadv_trace<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
+        if (traced) k_vadv_sample<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, tu, tv, tw);
+        else k_vadv_trace<2><<<gr, b, 0, c->stream>>>(g, c->u, c->v, c->w, c->solid, c->prm.dt, tu, tv, tw);
         EFS_LAUNCH_CHECK();
         k_vadv_average<2><<<gr, b, 0, c->stream>>>(g, tu, tv, tw, c->solid, c->u, c->v, c->w, f);
     }
@@ -1130,13 +1165,13 @@ cudaError_t launch_solver_prep(efs_ctx* c) {
     return cudaSuccess;
 }
 
-cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force) {
+cudaError_t launch_stage(efs_ctx* c, int stage, bool fuse_add_force, bool chain_traces) {
     switch (stage) {
         case EFS_STAGE_VEL_DECAY: return stage_decay(c);
         case EFS_STAGE_VEL_EXTRAPOLATE: return stage_extrapolate(c);
         case EFS_STAGE_RHO_SHARPEN: return stage_sharpen(c);
-        case EFS_STAGE_RHO_ADVECT: return c->dim == 3 ? stage_advect_t<3>(c) : stage_advect_t<2>(c);
-        case EFS_STAGE_VEL_ADVECT: return stage_vel_advect(c, fuse_add_force);
+        case EFS_STAGE_RHO_ADVECT: return c->dim == 3 ? stage_advect_t<3>(c, chain_traces) : stage_advect_t<2>(c, chain_traces);
+        case EFS_STAGE_VEL_ADVECT: return stage_vel_advect(c, fuse_add_force, chain_traces);
         case EFS_STAGE_ADD_FORCE: return stage_add_force(c);
         case EFS_STAGE_PROJECT: {
             cudaError_t e = launch_project_pre(c);
