@@ -568,7 +568,7 @@ cudaError_t launch_cg(const efs_batch* b) {
     return cudaLaunchKernelEx(&cfg, k_batch_cg_cluster, A);
 }
 
-cudaError_t enqueue_stage(const efs_batch* b, int stage, bool fuse) {
+cudaError_t enqueue_stage(const efs_batch* b, int stage, bool fuse, bool chain = false) {
     const BLaunch L = launch_of(b);
     if (stage == EFS_STAGE_PROJECT) {
         cudaError_t e = batch_project_pre(L);
@@ -576,15 +576,16 @@ cudaError_t enqueue_stage(const efs_batch* b, int stage, bool fuse) {
         if ((e = launch_cg(b)) != cudaSuccess) return e;
         return batch_project_post(L);
     }
-    return batch_stage(L, stage, fuse);
+    return batch_stage(L, stage, fuse, chain);
 }
 
 cudaError_t enqueue_step(const efs_batch* b, unsigned stages) {
     const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
+    const bool chain = (stages & EFS_STAGE_BIT(EFS_STAGE_RHO_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT));
     for (int s = 0; s < EFS_STAGE_COUNT; s++) {
         if (!(stages & EFS_STAGE_BIT(s))) continue;
         if (s == EFS_STAGE_ADD_FORCE && fuse) continue;
-        cudaError_t e = enqueue_stage(b, s, s == EFS_STAGE_VEL_ADVECT && fuse);
+        cudaError_t e = enqueue_stage(b, s, s == EFS_STAGE_VEL_ADVECT && fuse, chain);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -65,7 +65,9 @@ struct BLaunch {
 };
 
 // efs_stages.cu: one stage of every scene (project: walls, divergence, rows; the solve is separate)
-cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force);
+// chain_traces: rho_advect and vel_advect run back to back in this step (rho_advect keeps its back-trace ends in
+// tu, tv; vel_advect samples at them instead of tracing again)
+cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force, bool chain_traces = false);
 cudaError_t batch_project_pre(const BLaunch& L);
 cudaError_t batch_project_post(const BLaunch& L);
 

@@ -296,16 +296,16 @@ __global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t*
 // Steps 1-4: back-trace (shared by steps 1 and 2, which trace the same point), gamma' at the trace end,
 // backward weights m_k / sum / gamma', column sums beta1.
 template <int DIM>
-// `tend` (optional, 3 x N floats): the trace end of every interior cell, kept for vel_advect, whose back-trace
+// tex, tey, tez (optional): the trace end of every interior cell, kept for vel_advect, whose back-trace
 // from the cell (CPUSimulator3D.cpp:478-504) is this one: same start, velocity, dt and substeps, and the
 // velocity does not change in between (a trace from a solid cell ends at its start).
-__device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ gamma, float dt, float* __restrict__ wb, int* __restrict__ bb, float* __restrict__ bsum, float* __restrict__ tend = nullptr) {
+__device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int bz, const float* __restrict__ u, const float* __restrict__ v, const float* __restrict__ w, const uint8_t* __restrict__ solid, const float* __restrict__ gamma, float dt, float* __restrict__ wb, int* __restrict__ bb, float* __restrict__ bsum, float* __restrict__ tex = nullptr, float* __restrict__ tey = nullptr, float* __restrict__ tez = nullptr) {
     constexpr int K = (DIM == 3) ? 8 : 4;
     int x, y, z = 0, i;
     if (DIM == 3) { if (!cell3(g, bx, by, bz, x, y, z, i)) return; } else { if (!cell2(g, bx, by, x, y, i)) return; }
     if (solid[i]) {                           // step 1 skips solids; step 2 finds no free corner for them
         bb[i] = -1;
-        if (tend) { tend[i] = (float)x; tend[g.N + i] = (float)y; if (DIM == 3) tend[2 * (size_t)g.N + i] = (float)z; }
+        if (tex) { tex[i] = (float)x; tey[i] = (float)y; if (DIM == 3) tez[i] = (float)z; }
         return;
     }
     float px, py, pz = 0.f, gp;
@@ -314,12 +314,12 @@ __device__ __forceinline__ void d_adv_backward(const Geo& g, int bx, int by, int
     float sum;
     if (DIM == 3) {
         trace3(u, v, w, solid, g, (float)x, (float)y, (float)z, -dt, 4, px, py, pz);
-        if (tend) { tend[i] = px; tend[g.N + i] = py; tend[2 * (size_t)g.N + i] = pz; }
+        if (tex) { tex[i] = px; tey[i] = py; tez[i] = pz; }
         gp = sinterp3(gamma, g, px, py, pz);
         sum = corner_weights3(solid, g, px, py, pz, base, m);
     } else {
         trace2(u, v, solid, g, (float)x, (float)y, -dt, 4, px, py);
-        if (tend) { tend[i] = px; tend[g.N + i] = py; }
+        if (tex) { tex[i] = px; tey[i] = py; }
         gp = sinterp2(gamma, g, px, py);
         sum = corner_weights2(solid, g, px, py, base, m);
     }
@@ -339,7 +339,8 @@ __global__ void k_adv_backward(Geo g, const float* __restrict__ u, const float* 
                                const float* __restrict__ w, const uint8_t* __restrict__ solid,
                                const float* __restrict__ gamma, float dt, float* __restrict__ wb,
                                int* __restrict__ bb, float* __restrict__ bsum, float* __restrict__ tend) {
-    d_adv_backward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, gamma, dt, wb, bb, bsum, tend);
+    d_adv_backward<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, u, v, w, solid, gamma, dt, wb, bb, bsum, tend,
+                        tend ? tend + g.N : nullptr, tend ? tend + 2 * (size_t)g.N : nullptr);
 }
 
 // Step 5: forward trace for beta_j < 1; forward weights (1 - beta_j) m_k / sum; their row sums into gsum.
@@ -1251,11 +1252,11 @@ __global__ void kb_sharpen_scatter(BFields F, const BScene* __restrict__ sc) {
                                F.sh_end[3 * s + 2], -F.sh_val[s]);
     }
 }
-__global__ void kb_adv_backward(BView t, BFields F, float dt) {
+__global__ void kb_adv_backward(BView t, BFields F, float dt, int keep_trace) {
     for_entries(t, [&](const BScene& S, const BEntry& E) {
         const long long o = S.base;
         d_adv_backward<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.solid + o, F.gamma + o, dt, F.wb + 4 * o,
-                          F.bb + o, F.bsum + o);
+                          F.bb + o, F.bsum + o, keep_trace ? F.tu + o : nullptr, keep_trace ? F.tv + o : nullptr);
     });
 }
 __global__ void kb_adv_forward(BView t, BFields F, float dt) {
@@ -1305,6 +1306,20 @@ __global__ void kb_vadv_trace(BView t, BFields F, float dt) {
     for_entries(t, [&](const BScene& S, const BEntry& E) {
         const long long o = S.base;
         d_vadv_trace<2>(S.g, E.bx, E.by, 0, F.u + o, F.v + o, nullptr, F.solid + o, dt, F.tu + o, F.tv + o, nullptr);
+    });
+}
+// vel_advect's samples at the trace ends kb_adv_backward kept in tu, tv (see k_vadv_sample)
+__global__ void kb_vadv_sample(BView t, BFields F) {
+    for_entries(t, [&](const BScene& S, const BEntry& E) {
+        const long long o = S.base;
+        int x, y, i;
+        if (!cell2(S.g, E.bx, E.by, x, y, i)) return;
+        float* tu = F.tu + o;
+        float* tv = F.tv + o;
+        float a, b;
+        vinterp2(F.u + o, F.v + o, S.g, tu[i] - 0.5f, tv[i] - 0.5f, a, b);
+        tu[i] = a;
+        tv[i] = b;
     });
 }
 __global__ void kb_vadv_average(BView t, BFields F, ForceArgs f0) {
@@ -1360,7 +1375,7 @@ cudaError_t batch_project_post(const BLaunch& L) {
 }
 
 // One stage (0-5) of every scene; the project stage is batch_project_pre + the solve + batch_project_post.
-cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force) {
+cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force, bool chain_traces) {
     const dim3 blk(L.bx_dim, L.by_dim);
     const unsigned gi = bgrid(L.interior, L.grid);
     cudaStream_t st = L.stream;
@@ -1396,7 +1411,7 @@ cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force) {
             cudaError_t e;
             if ((e = cudaMemsetAsync(F.bsum, 0, bytes, st)) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(F.gsum, 0, bytes, st)) != cudaSuccess) return e;
-            kb_adv_backward<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
+            kb_adv_backward<<<gi, blk, 0, st>>>(L.interior, F, L.dt, chain_traces ? 1 : 0);
             EFS_LAUNCH_CHECK();
             kb_adv_forward<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
             EFS_LAUNCH_CHECK();
@@ -1423,7 +1438,8 @@ cudaError_t batch_stage(const BLaunch& L, int stage, bool fuse_add_force) {
             f.has_forces = 1;
             f.gravity = L.gravity;
             f.dt = L.dt;
-            kb_vadv_trace<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
+            if (chain_traces) kb_vadv_sample<<<gi, blk, 0, st>>>(L.interior, F);
+            else kb_vadv_trace<<<gi, blk, 0, st>>>(L.interior, F, L.dt);
             EFS_LAUNCH_CHECK();
             kb_vadv_average<<<gi, blk, 0, st>>>(L.interior, F, f);
             EFS_LAUNCH_CHECK();
