@@ -6,14 +6,17 @@
 //   - the whole iteration runs inside one kernel: phases are separated by a grid barrier (bounded spin; a
 //     barrier that gives up sets DEV_ERR_BARRIER_TIMEOUT and every block returns), the stop test is made on
 //     the device, and no scalar goes to the host;
-//   - dot products are accumulated in FP64: per-block partial sums, then every block adds the partials in
-//     the same fixed order, so all blocks take the same branch and results do not depend on timing;
-//   - only 32-cell chunks that hold a matrix row or a non-zero right-hand side are visited.  Rows outside
-//     the matrix are the identity in the reference (result = x), start at p = b and keep r = d = 0, so
-//     skipping them changes nothing;
-//   - d <- beta d + r is fused into the next matrix-vector product (d is double-buffered), and the
-//     product L d is recomputed in the update phase instead of being stored.
-// EFS_CG_MIXED additionally keeps p as an FP64 accumulator plus an FP32 increment (see efs_gb300.h).
+//   - dot products are accumulated with FP64-class accuracy (compensated float pairs, see FSum): per-block
+//     partial sums, then every block adds the partials in the same fixed order, so all blocks take the same
+//     branch and results do not depend on timing;
+//   - only 32-cell chunks that hold a matrix row or a non-zero right-hand side are visited, and within them
+//     only the lanes that hold a row load or store.  Rows outside the matrix are the identity in the
+//     reference (result = x), start at p = b and keep r = d = 0, so skipping them changes nothing;
+//   - EFS_CG_MIXED_RECURRENCE (the default) runs an iteration as two passes, t = L d and a per-cell update,
+//     both with 128-bit accesses when the vectors allow it, and one grid reduction; EFS_CG_MIXED and
+//     EFS_CG_REFERENCE fuse d <- beta d + r into the next matrix-vector product (d double-buffered) and
+//     recompute L d in the update phase instead of storing it.
+// The mixed variants keep p as an FP64 accumulator plus an FP32 increment (see efs_gb300.h).
 #include <cfloat>
 #include <mutex>
 
