@@ -173,11 +173,13 @@ struct Reduction {
         }
         if (!grid_barrier(ctl)) return false;
         FSum x, y, z;
-        const volatile float* src = partials + (size_t)slot * gridDim.x * 6;
+        // L2 reads (the barrier's acquire orders them after every block's partial), three 8-byte pairs a block
+        const float2* src = reinterpret_cast<const float2*>(partials + (size_t)slot * gridDim.x * 6);
         for (int k = threadIdx.x; k < (int)gridDim.x; k += SOLVER_THREADS) {
-            x.add_pair(src[6 * k + 0], src[6 * k + 1]);
-            y.add_pair(src[6 * k + 2], src[6 * k + 3]);
-            z.add_pair(src[6 * k + 4], src[6 * k + 5]);
+            const float2 p0 = __ldcg(src + 3 * k), p1 = __ldcg(src + 3 * k + 1), p2 = __ldcg(src + 3 * k + 2);
+            x.add_pair(p0.x, p0.y);
+            y.add_pair(p1.x, p1.y);
+            z.add_pair(p2.x, p2.y);
         }
         block_sum3(x, y, z);
         if (threadIdx.x == 0) {
