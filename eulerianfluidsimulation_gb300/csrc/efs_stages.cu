@@ -10,6 +10,8 @@
 //     over those weights with atomic adds for the scattered part.
 // Density sharpening applies every cell's change, then traces every changed cell on that field, then
 // scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell.
+#include <mutex>
+
 #include "efs_batch.h"
 #include "efs_internal.h"
 
@@ -568,6 +570,63 @@ __device__ __forceinline__ void d_diffuse_x(const Geo& g, int bx, int by, int bz
     if (y > g.H - 2) return;
     diffuse_line(rsrc, gsrc, rdst, gdst, solid, z * g.WH + y * g.W, 1, g.W);
 }
+// All of step 12 for a 2D grid small enough for one SM's shared memory (rho, gamma and the solid bytes of the
+// whole grid, rows padded to W + 1 so that neither a row walk nor a column walk has bank conflicts): one block
+// loads the grid (rho from rho_acc on the interior, folding step 11's copy), runs the `iters` x and y sweeps
+// with a block barrier between sweeps, and writes the interior back.  A 2D grid has only H - 2 (W - 2) lines
+// a sweep, each a sequential chain, so a sweep is bound by the chain's latency: from shared memory that is a
+// few cycles a load instead of an L2 round trip per step, and 14 launches become one.  Same order and
+// arithmetic as diffuse_line; only interior cells are read or written, as there.
+constexpr int kD2Threads = 256;
+__global__ void __launch_bounds__(kD2Threads) k_diffuse_2d_smem(Geo g, const float* __restrict__ rho_acc, float* rho,
+                                                                 float* gamma, const uint8_t* __restrict__ solid,
+                                                                 int iters) {
+    extern __shared__ float sm[];
+    const int W = g.W, H = g.H, P = W + 1;
+    float* sr = sm;
+    float* sg = sm + (size_t)H * P;
+    uint8_t* ss = reinterpret_cast<uint8_t*>(sg + (size_t)H * P);
+    for (int k = threadIdx.x; k < W * H; k += blockDim.x) {
+        const int y = k / W, x = k - y * W;
+        const bool in = x >= 1 && x <= W - 2 && y >= 1 && y <= H - 2;
+        sr[y * P + x] = in ? rho_acc[k] : rho[k];
+        sg[y * P + x] = gamma[k];
+        ss[y * P + x] = solid[k];
+    }
+    __syncthreads();
+    for (int it = 0; it < iters; it++) {
+        for (int axis = 0; axis < 2; axis++) {
+            // axis 0: x sweep, line y = 1 + t (stride 1, n = W); axis 1: y sweep, line x = 1 + t (stride P, n = H)
+            const int lines = axis == 0 ? H - 2 : W - 2;
+            const int n = axis == 0 ? W : H;
+            const int stride = axis == 0 ? 1 : P;
+            for (int t = threadIdx.x; t < lines; t += blockDim.x) {
+                const int first = axis == 0 ? (1 + t) * P : 1 + t;
+                int jj = first + stride;
+                float rj = sr[jj], gj = sg[jj];
+                bool sj = ss[jj] != 0;
+                for (int c = 2; c <= n - 2; c++) {
+                    const int ii = jj + stride;
+                    float ri = sr[ii], gi = sg[ii];
+                    const bool si = ss[ii] != 0;
+                    diffuse_pair(rj, gj, sj, ri, gi, si);
+                    sr[jj] = rj; sg[jj] = gj;
+                    jj = ii; rj = ri; gj = gi; sj = si;
+                }
+                if (n >= 3) { sr[jj] = rj; sg[jj] = gj; }
+            }
+            __syncthreads();
+        }
+    }
+    for (int k = threadIdx.x; k < W * H; k += blockDim.x) {
+        const int y = k / W, x = k - y * W;
+        if (x >= 1 && x <= W - 2 && y >= 1 && y <= H - 2) { rho[k] = sr[y * P + x]; gamma[k] = sg[y * P + x]; }
+    }
+}
+// Shared memory of k_diffuse_2d_smem for a W x H grid, and the largest it takes.
+inline size_t diffuse_2d_smem_bytes(const Geo& g) { return (size_t)g.H * (g.W + 1) * (2 * sizeof(float) + 1); }
+constexpr size_t kD2MaxSmem = 200 * 1024;
+
 // X sweep of a 2D grid: one thread per line.  A 2D grid has too few lines (H - 2) for the tiled kernel below,
 // whose load and store phases then stand between the sequential steps of one block's lines (measured at 128^2:
 // 92 against 45 us per sweep); its few lines stay in L1.
@@ -1067,6 +1126,18 @@ static cudaError_t stage_advect_t(efs_ctx* c, bool keep_trace = false) {
     // step 11's copy of rho' into the interior is folded into the first x sweep (it reads rho_acc and writes
     // rho); step 12's sweeps follow
     const int iters = (DIM == 3) ? 3 : 7;
+    if (DIM == 2 && diffuse_2d_smem_bytes(g) <= kD2MaxSmem) {
+        static std::once_flag attr_once;
+        static cudaError_t attr_err = cudaSuccess;
+        std::call_once(attr_once, [] {
+            attr_err = cudaFuncSetAttribute(k_diffuse_2d_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kD2MaxSmem);
+        });
+        if (attr_err != cudaSuccess) return attr_err;
+        k_diffuse_2d_smem<<<1, kD2Threads, diffuse_2d_smem_bytes(g), c->stream>>>(g, c->rho_acc, c->rho, c->gamma, c->solid,
+                                                                                 iters);
+        EFS_LAUNCH_CHECK();
+        return cudaSuccess;
+    }
     for (int it = 0; it < iters; it++) {
         const float* rs = (it == 0) ? c->rho_acc : c->rho;
         if (DIM == 3) {
