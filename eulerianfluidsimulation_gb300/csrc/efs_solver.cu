@@ -65,6 +65,7 @@ __device__ __forceinline__ unsigned& barrier_index() {
 __device__ bool grid_barrier(DevCtl* ctl) {
     __shared__ int s_ok;
     __syncthreads();
+    if (gridDim.x == 1) return true;   // one block: the block barrier orders everything (small grids)
     if (threadIdx.x == 0) {
         unsigned& k = barrier_index();
         k += 1u;
@@ -1229,7 +1230,11 @@ cudaError_t solver_shape(int n_chunks, int sm_count, int* blocks_out, size_t* sm
         if (occ >= bps) { blocks = bps * sm_count; break; }
         if (bps == 1 && occ < 1) return cudaErrorLaunchOutOfResources;
     }
-    const int want = (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
+    // Small grids get fewer blocks (about four chunks per warp) so that barrier cost stays proportionate, and
+    // one block (block barriers instead of grid barriers) up to kOneBlockChunks chunks: at 2D 128^2 (512 chunks)
+    // a pass of one block's 32 warps takes less than a grid barrier of four blocks.
+    constexpr int kOneBlockChunks = 640;
+    const int want = n_chunks <= kOneBlockChunks ? 1 : (n_chunks + SOLVER_WARPS * 4 - 1) / (SOLVER_WARPS * 4);
     blocks = std::max(1, std::min(blocks, want));
     *blocks_out = blocks;
     *smem_out = (size_t)((n_chunks + blocks - 1) / blocks) * 2 * sizeof(int);   // chunk ids and row masks
