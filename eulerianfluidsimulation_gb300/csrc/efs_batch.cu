@@ -92,10 +92,10 @@ struct BSum {
     }
 };
 
-// block sums of up to three pair sums, returned as doubles to every thread
-__device__ void block_reduce3(BSum a, BSum b, BSum c, double& ta, double& tb, double& tc) {
+// Block totals of up to three pair sums, in thread 0 only (warp partials added in warp order).  One block
+// barrier; the next call writes `sh` only after a barrier every thread reaches after this one's reads.
+__device__ void block_partial3(BSum a, BSum b, BSum c, double& ta, double& tb, double& tc) {
     __shared__ double sh[3][32];
-    __shared__ double tot[3];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float as = __shfl_down_sync(0xffffffffu, a.s, o), ac = __shfl_down_sync(0xffffffffu, a.c, o);
@@ -115,12 +115,14 @@ __device__ void block_reduce3(BSum a, BSum b, BSum c, double& ta, double& tb, do
     if (threadIdx.x == 0) {
         double x = 0, y = 0, z = 0;
         for (int w = 0; w < nw; w++) { x += sh[0][w]; y += sh[1][w]; z += sh[2][w]; }
-        tot[0] = x; tot[1] = y; tot[2] = z;
+        ta = x; tb = y; tc = z;
     }
-    __syncthreads();
-    ta = tot[0]; tb = tot[1]; tc = tot[2];
-    __syncthreads();
 }
+
+// No work for thread 0 between a reduction and its broadcast.
+struct NoEpilogue {
+    __device__ __forceinline__ void operator()(double, double, double) const {}
+};
 
 __device__ __forceinline__ float lap2_f(const float* x, uint16_t f, int i, int W) {
     float s = 0.f;
@@ -153,14 +155,29 @@ struct BCGArgs {
 };
 
 // The threads that solve one scene: one block, or the CTAs of one thread-block cluster.  A pass that reads
-// stencil neighbours written by another thread of the group is preceded by sync(); reduce3 returns the same
-// group totals to every thread (block partials added in rank order).
+// stencil neighbours written by another thread of the group is preceded by sync().  reduce3 returns the same
+// group totals to every thread (block partials added in rank order); before the block barrier that publishes
+// them, thread 0 of every CTA runs `t0` on the totals, so scalars it derives and stores in shared memory
+// are published by the same barrier.  `tot` is written again only after the next reduction's first block
+// barrier, which every thread reaches after reading it.
 struct BlockGroup {
     __device__ __forceinline__ int rank() const { return 0; }
     __device__ __forceinline__ int ranks() const { return 1; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
+    template <class T0>
+    __device__ __forceinline__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z, T0&& t0) {
+        __shared__ double tot[3];
+        double bx, by, bz;
+        block_partial3(a, b, c, bx, by, bz);
+        if (threadIdx.x == 0) {
+            t0(bx, by, bz);
+            tot[0] = bx; tot[1] = by; tot[2] = bz;
+        }
+        __syncthreads();
+        x = tot[0]; y = tot[1]; z = tot[2];
+    }
     __device__ __forceinline__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z) {
-        block_reduce3(a, b, c, x, y, z);
+        reduce3(a, b, c, x, y, z, NoEpilogue());
     }
     __device__ __forceinline__ int next_scene(unsigned* fetch) {
         __shared__ int s_k;
@@ -180,10 +197,14 @@ struct ClusterGroup {
     __device__ __forceinline__ int rank() const { return (int)cg::this_cluster().block_rank(); }
     __device__ __forceinline__ int ranks() const { return (int)cg::this_cluster().num_blocks(); }
     __device__ __forceinline__ void sync() const { cg::this_cluster().sync(); }
-    __device__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z) {
+    // The slot written at one reduction is written again two reductions later, after a cluster barrier that
+    // every CTA reaches only once it has read the slot.  Lane r of warp 0 loads rank r's slot, and lane 0
+    // adds them in rank order from shuffles: the loads of all ranks are in flight together.
+    template <class T0>
+    __device__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z, T0&& t0) {
         __shared__ double tot[3];
         double bx, by, bz;
-        block_reduce3(a, b, c, bx, by, bz);
+        block_partial3(a, b, c, bx, by, bz);
         cg::cluster_group cl = cg::this_cluster();
         if (threadIdx.x == 0) {
             slots[3 * parity] = bx;
@@ -191,24 +212,33 @@ struct ClusterGroup {
             slots[3 * parity + 2] = bz;
         }
         cl.sync();
-        if (threadIdx.x == 0) {
-            double X = 0.0, Y = 0.0, Z = 0.0;
-            const int n = (int)cl.num_blocks();
-            for (int r = 0; r < n; r++) {
-                const double* rs = cl.map_shared_rank(slots + 3 * parity, r);
-                X += rs[0];
-                Y += rs[1];
-                Z += rs[2];
+        if (threadIdx.x < 32) {
+            const int n = (int)cl.num_blocks(), lane = threadIdx.x;
+            double vx = 0.0, vy = 0.0, vz = 0.0;
+            if (lane < n) {
+                const double* rs = cl.map_shared_rank(slots + 3 * parity, lane);
+                vx = rs[0]; vy = rs[1]; vz = rs[2];
             }
-            tot[0] = X; tot[1] = Y; tot[2] = Z;
+            double X = 0.0, Y = 0.0, Z = 0.0;
+            for (int r = 0; r < n; r++) {
+                X += __shfl_sync(0xffffffffu, vx, r);
+                Y += __shfl_sync(0xffffffffu, vy, r);
+                Z += __shfl_sync(0xffffffffu, vz, r);
+            }
+            if (lane == 0) {
+                t0(X, Y, Z);
+                tot[0] = X; tot[1] = Y; tot[2] = Z;
+            }
         }
         __syncthreads();
         x = tot[0]; y = tot[1]; z = tot[2];
         parity ^= 1;
-        __syncthreads();
     }
-    // The slot written at one reduction (fetch) is written again two reductions (fetches) later, after a
-    // cluster barrier that every CTA reaches only once it has read the slot.
+    __device__ __forceinline__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z) {
+        reduce3(a, b, c, x, y, z, NoEpilogue());
+    }
+    // The slot written at one fetch is written again two fetches later, after a cluster barrier that every
+    // CTA reaches only once it has read the slot.
     __device__ int next_scene(unsigned* fetch) {
         cg::cluster_group cl = cg::this_cluster();
         if (cl.block_rank() == 0 && threadIdx.x == 0) next[fparity] = (int)atomicAdd(fetch, 1u);
@@ -281,83 +311,90 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
                                        reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(e)) & 15u) == 0 &&
                       (reinterpret_cast<uintptr_t>(info) & 7u) == 0;
     const int N4 = N >> 2, W4 = W >> 2, lane = threadIdx.x & 31;
-    if (!conv) {
-        for (it = 0; it < A.max_steps; it++) {
-            BSum dtp, ttp;
-            if (vec4) {
-                // t = L d on rows (same neighbour order and rounding as lap2_f), d.t and t.t
-                const float4* d4 = reinterpret_cast<const float4*>(d);
-                float4* t4 = reinterpret_cast<float4*>(t);
-                for (int gb = i0 - lane; gb < N4; gb += stride) {
-                    const int g = gb + lane;
-                    const uint2 fi = g < N4 ? reinterpret_cast<const uint2*>(info)[g] : make_uint2(0u, 0u);
-                    const unsigned fw[4] = {fi.x & 0xFFFFu, fi.x >> 16, fi.y & 0xFFFFu, fi.y >> 16};
-                    const bool any = ((fw[0] | fw[1] | fw[2] | fw[3]) & 0x8000u) != 0;
-                    float4 xc = make_float4(0.f, 0.f, 0.f, 0.f), ym = xc, yp = xc;
-                    if (any) { xc = d4[g]; ym = d4[g - W4]; yp = d4[g + W4]; }   // rows are interior cells
-                    float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
-                    float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
-                    if (lane == 0 && (fw[0] & 0x8000u) && (fw[0] & 1u)) left = d[4 * g - 1];
-                    if (lane == 31 && (fw[3] & 0x8000u) && (fw[3] & 2u)) right = d[4 * g + 4];
-                    if (!any) continue;
-                    const float cx[4] = {xc.x, xc.y, xc.z, xc.w};
-                    const float cym[4] = {ym.x, ym.y, ym.z, ym.w}, cyp[4] = {yp.x, yp.y, yp.z, yp.w};
-                    float to[4];
+    // t = L d on rows (same neighbour order and rounding as lap2_f), d.t and t.t
+    auto tpass = [&](BSum& dtp, BSum& ttp) {
+        if (vec4) {
+            const float4* d4 = reinterpret_cast<const float4*>(d);
+            float4* t4 = reinterpret_cast<float4*>(t);
+            for (int gb = i0 - lane; gb < N4; gb += stride) {
+                const int g = gb + lane;
+                const uint2 fi = g < N4 ? reinterpret_cast<const uint2*>(info)[g] : make_uint2(0u, 0u);
+                const unsigned fw[4] = {fi.x & 0xFFFFu, fi.x >> 16, fi.y & 0xFFFFu, fi.y >> 16};
+                const bool any = ((fw[0] | fw[1] | fw[2] | fw[3]) & 0x8000u) != 0;
+                float4 xc = make_float4(0.f, 0.f, 0.f, 0.f), ym = xc, yp = xc;
+                if (any) { xc = d4[g]; ym = d4[g - W4]; yp = d4[g + W4]; }   // rows are interior cells
+                float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
+                float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
+                if (lane == 0 && (fw[0] & 0x8000u) && (fw[0] & 1u)) left = d[4 * g - 1];
+                if (lane == 31 && (fw[3] & 0x8000u) && (fw[3] & 2u)) right = d[4 * g + 4];
+                if (!any) continue;
+                const float cx[4] = {xc.x, xc.y, xc.z, xc.w};
+                const float cym[4] = {ym.x, ym.y, ym.z, ym.w}, cyp[4] = {yp.x, yp.y, yp.z, yp.w};
+                float to[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        to[k] = 0.f;
-                        const unsigned f = fw[k];
-                        if (!(f & 0x8000u)) continue;
-                        float sm = 0.f;
-                        if (f & 1u) sm += (k == 0) ? left : cx[k > 0 ? k - 1 : 0];
-                        if (f & 2u) sm += (k == 3) ? right : cx[k < 3 ? k + 1 : 3];
-                        if (f & 4u) sm += cym[k];
-                        if (f & 8u) sm += cyp[k];
-                        const float ti = sm - (float)((f >> 8) & 7) * cx[k];
-                        to[k] = ti;
-                        dtp.add_prod(cx[k], ti);
-                        ttp.add_prod(ti, ti);
-                    }
-                    t4[g] = make_float4(to[0], to[1], to[2], to[3]);
-                }
-            } else {
-                for (int i = i0; i < N; i += stride) {
-                    const uint16_t f = info[i];
+                for (int k = 0; k < 4; k++) {
+                    to[k] = 0.f;
+                    const unsigned f = fw[k];
                     if (!(f & 0x8000u)) continue;
-                    const float ti = lap2_f(d, f, i, W);
-                    t[i] = ti;
-                    dtp.add_prod(d[i], ti);
+                    float sm = 0.f;
+                    if (f & 1u) sm += (k == 0) ? left : cx[k > 0 ? k - 1 : 0];
+                    if (f & 2u) sm += (k == 3) ? right : cx[k < 3 ? k + 1 : 3];
+                    if (f & 4u) sm += cym[k];
+                    if (f & 8u) sm += cyp[k];
+                    const float ti = sm - (float)((f >> 8) & 7) * cx[k];
+                    to[k] = ti;
+                    dtp.add_prod(cx[k], ti);
                     ttp.add_prod(ti, ti);
                 }
+                t4[g] = make_float4(to[0], to[1], to[2], to[3]);
             }
-            double dt, tt, u3;
-            grp.reduce3(dtp, ttp, BSum(), dt, tt, u3);
-            // The FP64 scalar work is one thread's per CTA (GB300 runs FP64 divisions slowly; in every thread
-            // they cost the scene's group microseconds per iteration).  Every CTA of a cluster computes the same
-            // values from the same totals.
-            __shared__ float s_sc[2];
-            __shared__ int s_mode;
-            if (threadIdx.x == 0) {
-                int mode = 0;
-                float al = 0.f, be = 0.f;
-                if (!(dt != 0.0) || !isfinite(rr / dt)) {
-                    mode = -1;                                 // breakdown (singular block): not converged
-                } else {
-                    const double ad = rr / dt;
-                    al = (float)ad;
-                    const double est = ad * ad * tt - rr;     // r'.r' from the CG recurrence
-                    if ((it & 0x3F) && est > 0.0) { mode = 1; be = (float)(est / rr); }
-                }
-                s_sc[0] = al;
-                s_sc[1] = be;
-                s_mode = mode;
+        } else {
+            for (int i = i0; i < N; i += stride) {
+                const uint16_t f = info[i];
+                if (!(f & 0x8000u)) continue;
+                const float ti = lap2_f(d, f, i, W);
+                t[i] = ti;
+                dtp.add_prod(d[i], ti);
+                ttp.add_prod(ti, ti);
             }
-            __syncthreads();
+        }
+    };
+    // The FP64 scalar work of an iteration is thread 0's (GB300 runs FP64 divisions slowly; in every thread
+    // they cost the scene's group microseconds per iteration), done on the totals of the t pass's reduction
+    // and published by its barrier.  Every CTA of a cluster computes the same values from the same totals.
+    __shared__ float s_sc[2];
+    __shared__ int s_mode;
+    auto scalars = [&](double rr_, double dt_, double tt_, int it_) {
+        int mode = 0;
+        float al = 0.f, be = 0.f;
+        if (!(dt_ != 0.0) || !isfinite(rr_ / dt_)) {
+            mode = -1;                                 // breakdown (singular block): not converged
+        } else {
+            const double ad = rr_ / dt_;
+            al = (float)ad;
+            const double est = ad * ad * tt_ - rr_;    // r'.r' from the CG recurrence
+            if ((it_ & 0x3F) && est > 0.0) { mode = 1; be = (float)(est / rr_); }
+        }
+        s_sc[0] = al;
+        s_sc[1] = be;
+        s_mode = mode;
+    };
+    if (!conv) {
+        // Pass 1 (t = L d; d.t, t.t) and pass 2 (e, r, d per cell; exact r.r) alternate.  The r.r of pass 2
+        // travels with the next pass 1's reduction: one reduction and one group barrier per iteration.  The
+        // stop test of iteration k is therefore taken after the pass 1 of iteration k+1, whose t is then
+        // unused; e, r and p are unaffected.
+        double dt, tt, u3;
+        {
+            BSum dtp, ttp;
+            tpass(dtp, ttp);
+            grp.reduce3(BSum(), dtp, ttp, u3, dt, tt, [&](double, double y, double z) { scalars(rr, y, z, 0); });
+        }
+        for (it = 0; it < A.max_steps; it++) {
             const int mode = s_mode;
             const float alpha = s_sc[0];
             if (mode < 0) break;
             const double old = rr;
-            bool replaced = false;
             if (mode == 1) {
                 const float beta = s_sc[1];
                 BSum rp;
@@ -399,14 +436,27 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
                         rp.add_prod(rn, rn);
                     }
                 }
-                double u1, u2;
-                grp.reduce3(rp, BSum(), BSum(), rr, u1, u2);
+                grp.sync();
+                BSum dtp, ttp;
+                tpass(dtp, ttp);
+                grp.reduce3(rp, dtp, ttp, rr, dt, tt, [&](double x, double y, double z) { scalars(x, y, z, it + 1); });
+                if (rr < thr) {
+                    replace(rr);
+                    if (rr < thr) { conv = 1; break; }
+                    // d was formed from the recurrence residual: restart it from the recomputed one
+                    for (int i = i0; i < N; i += stride)
+                        if (info[i] & 0x8000u) d[i] = r[i];
+                    grp.sync();
+                    BSum dtp2, ttp2;
+                    tpass(dtp2, ttp2);
+                    grp.reduce3(BSum(), dtp2, ttp2, u3, dt, tt, [&](double, double y, double z) { scalars(rr, y, z, it + 1); });
+                }
             } else {
                 for (int i = i0; i < N; i += stride)
                     if (info[i] & 0x8000u) e[i] += alpha * d[i];
                 grp.sync();
                 replace(rr);
-                replaced = true;
+                if (rr < thr) { conv = 1; break; }
                 __shared__ float s_b2;
                 if (threadIdx.x == 0) s_b2 = (float)(rr / old);
                 __syncthreads();
@@ -414,18 +464,9 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
                 for (int i = i0; i < N; i += stride)
                     if (info[i] & 0x8000u) d[i] = d[i] * beta + r[i];
                 grp.sync();
-            }
-            if (rr < thr) {
-                if (!replaced) {
-                    replace(rr);
-                    // d was formed from the recurrence residual: restart it from the recomputed one
-                    if (!(rr < thr)) {
-                        for (int i = i0; i < N; i += stride)
-                            if (info[i] & 0x8000u) d[i] = r[i];
-                        grp.sync();
-                    }
-                }
-                if (rr < thr) { conv = 1; break; }
+                BSum dtp, ttp;
+                tpass(dtp, ttp);
+                grp.reduce3(BSum(), dtp, ttp, u3, dt, tt, [&](double, double y, double z) { scalars(rr, y, z, it + 1); });
             }
         }
         it = min(it + 1, A.max_steps);
