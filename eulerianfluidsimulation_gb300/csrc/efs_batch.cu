@@ -90,32 +90,48 @@ struct BSum {
         add(p);
         c += e;
     }
+    __device__ __forceinline__ void add_pair(float s2, float c2) {
+        add(s2);
+        c += c2;
+    }
+    __device__ __forceinline__ double total() const { return (double)s + (double)c; }
 };
 
-// Block totals of up to three pair sums, in thread 0 only (warp partials added in warp order).  One block
-// barrier; the next call writes `sh` only after a barrier every thread reaches after this one's reads.
-__device__ void block_partial3(BSum a, BSum b, BSum c, double& ta, double& tb, double& tc) {
-    __shared__ double sh[3][32];
+// Pair sum over a warp (fixed tree), valid in lane 0.
+__device__ __forceinline__ BSum warp_bsum(BSum v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const float as = __shfl_down_sync(0xffffffffu, a.s, o), ac = __shfl_down_sync(0xffffffffu, a.c, o);
-        const float bs = __shfl_down_sync(0xffffffffu, b.s, o), bc = __shfl_down_sync(0xffffffffu, b.c, o);
-        const float cs = __shfl_down_sync(0xffffffffu, c.s, o), cc = __shfl_down_sync(0xffffffffu, c.c, o);
-        a.add(as); a.c += ac;
-        b.add(bs); b.c += bc;
-        c.add(cs); c.c += cc;
+        const float s2 = __shfl_down_sync(0xffffffffu, v.s, o);
+        const float c2 = __shfl_down_sync(0xffffffffu, v.c, o);
+        v.add_pair(s2, c2);
     }
+    return v;
+}
+
+// Block pair sums of up to three pair sums, valid in thread 0 only: lanes by a fixed tree, then the warps'
+// partials by a second tree in warp 0.  All in float pairs: GB300 runs FP64 at a small fraction of its FP32
+// rate, and a serial chain of FP64 additions on one thread held every other warp at the next barrier.  One
+// block barrier; the next call writes `sw` only after a barrier every thread reaches after this one's reads.
+__device__ void block_pairs3(BSum& a, BSum& b, BSum& c) {
+    __shared__ float sw[6][32];
+    a = warp_bsum(a);
+    b = warp_bsum(b);
+    c = warp_bsum(c);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     if (lane == 0) {
-        sh[0][warp] = (double)a.s + (double)a.c;
-        sh[1][warp] = (double)b.s + (double)b.c;
-        sh[2][warp] = (double)c.s + (double)c.c;
+        sw[0][warp] = a.s; sw[1][warp] = a.c;
+        sw[2][warp] = b.s; sw[3][warp] = b.c;
+        sw[4][warp] = c.s; sw[5][warp] = c.c;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double x = 0, y = 0, z = 0;
-        for (int w = 0; w < nw; w++) { x += sh[0][w]; y += sh[1][w]; z += sh[2][w]; }
-        ta = x; tb = y; tc = z;
+    if (warp == 0) {
+        const bool in = lane < nw;
+        a.s = in ? sw[0][lane] : 0.f; a.c = in ? sw[1][lane] : 0.f;
+        b.s = in ? sw[2][lane] : 0.f; b.c = in ? sw[3][lane] : 0.f;
+        c.s = in ? sw[4][lane] : 0.f; c.c = in ? sw[5][lane] : 0.f;
+        a = warp_bsum(a);
+        b = warp_bsum(b);
+        c = warp_bsum(c);
     }
 }
 
@@ -167,9 +183,9 @@ struct BlockGroup {
     template <class T0>
     __device__ __forceinline__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z, T0&& t0) {
         __shared__ double tot[3];
-        double bx, by, bz;
-        block_partial3(a, b, c, bx, by, bz);
+        block_pairs3(a, b, c);
         if (threadIdx.x == 0) {
+            const double bx = a.total(), by = b.total(), bz = c.total();
             t0(bx, by, bz);
             tot[0] = bx; tot[1] = by; tot[2] = bz;
         }
@@ -191,41 +207,41 @@ struct BlockGroup {
 };
 
 struct ClusterGroup {
-    double* slots;        // this CTA's shared memory: 2 x 3 doubles (alternating per reduction)
+    float* slots;         // this CTA's shared memory: 2 x 3 float pairs (alternating per reduction)
     int* next;            // this CTA's shared memory: 2 ints (alternating per fetch)
     int parity = 0, fparity = 0;
     __device__ __forceinline__ int rank() const { return (int)cg::this_cluster().block_rank(); }
     __device__ __forceinline__ int ranks() const { return (int)cg::this_cluster().num_blocks(); }
     __device__ __forceinline__ void sync() const { cg::this_cluster().sync(); }
     // The slot written at one reduction is written again two reductions later, after a cluster barrier that
-    // every CTA reaches only once it has read the slot.  Lane r of warp 0 loads rank r's slot, and lane 0
-    // adds them in rank order from shuffles: the loads of all ranks are in flight together.
+    // every CTA reaches only once it has read the slot.  Lane r of warp 0 loads rank r's pairs (all loads in
+    // flight together) and a fixed shuffle tree adds them, so every CTA gets bit-identical totals.
     template <class T0>
     __device__ void reduce3(BSum a, BSum b, BSum c, double& x, double& y, double& z, T0&& t0) {
         __shared__ double tot[3];
-        double bx, by, bz;
-        block_partial3(a, b, c, bx, by, bz);
+        block_pairs3(a, b, c);
         cg::cluster_group cl = cg::this_cluster();
         if (threadIdx.x == 0) {
-            slots[3 * parity] = bx;
-            slots[3 * parity + 1] = by;
-            slots[3 * parity + 2] = bz;
+            float* sl = slots + 6 * parity;
+            sl[0] = a.s; sl[1] = a.c;
+            sl[2] = b.s; sl[3] = b.c;
+            sl[4] = c.s; sl[5] = c.c;
         }
         cl.sync();
         if (threadIdx.x < 32) {
-            const int n = (int)cl.num_blocks(), lane = threadIdx.x;
-            double vx = 0.0, vy = 0.0, vz = 0.0;
-            if (lane < n) {
-                const double* rs = cl.map_shared_rank(slots + 3 * parity, lane);
-                vx = rs[0]; vy = rs[1]; vz = rs[2];
+            const int lane = threadIdx.x;
+            BSum px, py, pz;
+            if (lane < (int)cl.num_blocks()) {
+                const float* rs = cl.map_shared_rank(slots + 6 * parity, lane);
+                px.s = rs[0]; px.c = rs[1];
+                py.s = rs[2]; py.c = rs[3];
+                pz.s = rs[4]; pz.c = rs[5];
             }
-            double X = 0.0, Y = 0.0, Z = 0.0;
-            for (int r = 0; r < n; r++) {
-                X += __shfl_sync(0xffffffffu, vx, r);
-                Y += __shfl_sync(0xffffffffu, vy, r);
-                Z += __shfl_sync(0xffffffffu, vz, r);
-            }
+            px = warp_bsum(px);
+            py = warp_bsum(py);
+            pz = warp_bsum(pz);
             if (lane == 0) {
+                const double X = px.total(), Y = py.total(), Z = pz.total();
                 t0(X, Y, Z);
                 tot[0] = X; tot[1] = Y; tot[2] = Z;
             }
@@ -367,13 +383,13 @@ __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
     auto scalars = [&](double rr_, double dt_, double tt_, int it_) {
         int mode = 0;
         float al = 0.f, be = 0.f;
-        if (!(dt_ != 0.0) || !isfinite(rr_ / dt_)) {
+        const double ad = div_fast(rr_, dt_);
+        if (!(dt_ != 0.0) || !isfinite(ad)) {
             mode = -1;                                 // breakdown (singular block): not converged
         } else {
-            const double ad = rr_ / dt_;
             al = (float)ad;
             const double est = ad * ad * tt_ - rr_;    // r'.r' from the CG recurrence
-            if ((it_ & 0x3F) && est > 0.0) { mode = 1; be = (float)(est / rr_); }
+            if ((it_ & 0x3F) && est > 0.0) { mode = 1; be = (float)div_fast(est, rr_); }
         }
         s_sc[0] = al;
         s_sc[1] = be;
@@ -505,7 +521,7 @@ __global__ void __launch_bounds__(1024) k_batch_cg(BCGArgs A) {
 
 // One thread-block cluster per scene; clusters take scenes largest first.
 __global__ void __launch_bounds__(1024) k_batch_cg_cluster(BCGArgs A) {
-    __shared__ double slots[6];
+    __shared__ float slots[12];
     __shared__ int next[2];
     ClusterGroup grp;
     grp.slots = slots;

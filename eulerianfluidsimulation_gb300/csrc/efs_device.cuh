@@ -19,6 +19,19 @@ struct Geo {
     int N;            // W * H * D
 };
 
+// a / b in FP64 without the FP64 division sequence (about 550 cycles of dependent latency on GB300): a
+// float reciprocal refined by two Newton steps in FP64, relative error near 1e-16.  Falls back to the
+// division when b is outside the range where the float reciprocal is finite and normal.
+__device__ __forceinline__ double div_fast(double a, double b) {
+    const float bf = (float)b;
+    float r0 = 1.0f / bf;
+    if (!(fabsf(r0) < 1e37f && fabsf(r0) > 1e-37f)) return a / b;
+    double r = (double)r0;
+    r = fma(r, fma(-b, r, 1.0), r);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+}
+
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (hi < v ? hi : v); }
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
 __device__ __forceinline__ float maxf(float a, float b) { return (a < b) ? b : a; }   // std::max

@@ -155,7 +155,7 @@ def test_scalar_and_vector_solver_passes_in_one_batch():
                 S.close()
 
 
-@pytest.mark.parametrize("cluster,threads", [(4, 256), (8, 512)])
+@pytest.mark.parametrize("cluster,threads", [(2, 128), (4, 256), (8, 512), (8, 1024)])
 def test_cluster_solver_matches_the_single_context(cluster, threads):
     """The pressure solve by a thread-block cluster per scene (partial sums exchanged in distributed shared
     memory) gives the single-context pressure within the same 1e-5 as one block per scene."""
