@@ -5,10 +5,10 @@
 // CGSolver.cpp:32-111) with its own grid size and cell size; the batch shares one set of parameters except
 // GRAVITY_FORCE, which is per scene (9.81 / dx in cells/s^2).  One step of all scenes is one CUDA graph: each
 // stage kernel is a single persistent launch over a table of (scene, block) entries (efs_stages.cu), and the
-// pressure solves are one persistent launch in which each block solves whole scenes (block-level CG, scenes
-// in descending size), so no scene waits on another and no grid-wide barrier is needed.  The tile shape of
-// the stage kernels, their blocks per SM and the solver's block size are chosen by efs_batch_autotune from
-// timed trial steps.
+// pressure solves are one persistent launch in which each block, or each thread-block cluster, solves whole
+// scenes (scenes in descending size), so no scene waits on another and no grid-wide barrier is needed.  The
+// tile shape of the stage kernels, their blocks per SM and the solver's block and cluster size are chosen by
+// efs_batch_autotune from timed trial steps.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -74,8 +74,10 @@ cudaError_t balloc(efs_batch* b, T** p, long long count) {
     return cudaMemset(*p, 0, (size_t)std::max<long long>(count, 1) * sizeof(T));
 }
 
-// ---- block-level CG: EFS_CG_MIXED_RECURRENCE on one scene per block (CGSolver.cpp:32-83 with the mixed
-// precision and recurrence of the persistent solver; see efs_gb300.h) ----------------------------------------
+// ---- group-level CG: EFS_CG_MIXED_RECURRENCE on one scene per block or per thread-block cluster
+// (CGSolver.cpp:32-83 with the mixed precision and recurrence of the persistent solver; see efs_gb300.h).
+// Dot products are compensated float pairs summed by fixed shuffle trees; FP64 appears only in the group
+// totals, the scalars thread 0 derives from them, and the residual replacement every 64 iterations. --------
 struct BSum {
     float s = 0.f, c = 0.f;
     __device__ __forceinline__ void add(float v) {
@@ -267,8 +269,8 @@ struct ClusterGroup {
     __device__ __forceinline__ void finish() const { cg::this_cluster().sync(); }
 };
 
-// Block-level CG (EFS_CG_MIXED_RECURRENCE) of one scene by group G (CGSolver.cpp:32-83 with the mixed precision
-// and recurrence of the persistent solver; see efs_gb300.h).
+// CG (EFS_CG_MIXED_RECURRENCE) of one scene by group G (CGSolver.cpp:32-83 with the mixed precision and
+// recurrence of the persistent solver; see efs_gb300.h).
 template <class G>
 __device__ void solve_scene(const BCGArgs& A, int s, G& grp) {
     const BScene S = A.sc[s];
