@@ -21,6 +21,9 @@ SOLVER_JACOBI = 0
 SOLVER_CG = 1
 SOLVER_FCG_UNET = 2
 
+SHARPEN_PARALLEL = 0
+SHARPEN_SEQUENTIAL = 1
+
 CG_MIXED = 0
 CG_REFERENCE = 1
 CG_MIXED_RECURRENCE = 2

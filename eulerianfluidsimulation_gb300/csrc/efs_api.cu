@@ -41,7 +41,10 @@ bool params_valid(const efs_params* p, std::string& why) {
         why = "unknown cg_variant";
         return false;
     }
-    if (p->sharpen_mode != EFS_SHARPEN_PARALLEL) { why = "unknown sharpen_mode"; return false; }
+    if (p->sharpen_mode != EFS_SHARPEN_PARALLEL && p->sharpen_mode != EFS_SHARPEN_SEQUENTIAL) {
+        why = "unknown sharpen_mode";
+        return false;
+    }
     if (p->max_steps < 0) { why = "max_steps must be >= 0"; return false; }
     if (p->disable_mask & ~EFS_STAGES_ALL) { why = "disable_mask has bits beyond the seven stages"; return false; }
     return true;

@@ -734,6 +734,8 @@ int efs_batch_create(int n_scenes, const int* widths, const int* heights, const 
     if (params->solver != EFS_SOLVER_CG || params->cg_variant != EFS_CG_MIXED_RECURRENCE)
         return bfail(nullptr, EFS_ERR_ARG, "batched scenes use the CG solver (EFS_CG_MIXED_RECURRENCE)");
     if (params->re_calc_div) return bfail(nullptr, EFS_ERR_ARG, "RE_CALC_DIV is not supported in batches");
+    if (params->sharpen_mode != EFS_SHARPEN_PARALLEL)
+        return bfail(nullptr, EFS_ERR_ARG, "batched scenes sharpen in EFS_SHARPEN_PARALLEL mode only");
     if (params->max_steps < 0 || !std::isfinite(params->dt)) return bfail(nullptr, EFS_ERR_ARG, "bad params");
     for (int s = 0; s < n_scenes; s++)
         if (widths[s] < 4 || heights[s] < 4 || (long long)widths[s] * heights[s] > (1LL << 26))

@@ -4,9 +4,9 @@
 // budget and owns every allocation, a real-time loop where the implicit device synchronisation of cudaMalloc /
 // cudaFree is not allowed, or code that records its work into a CUDA graph.  For them this entry point solves
 // on the caller's device buffers and keeps its working vectors in one file-scope __device__ array of fixed
-// size, which every device that loads the library holds until the process exits.  It covers grids up to
-// EFS_NOALLOC_MAX_CELLS cells (larger grids are rejected with EFS_ERR_ARG) and has no counterpart in the
-// reference, whose solvers own heap-allocated fields.
+// size (EFS_NOALLOC_SCRATCH_BYTES, about 13.2 MB), which every device that loads the library holds until the
+// process exits.  It covers grids up to EFS_NOALLOC_MAX_CELLS cells (larger grids are rejected with
+// EFS_ERR_ARG) and has no counterpart in the reference, whose solvers own heap-allocated fields.
 //
 // All calls share the array and find it as the previous call left it: everything the solve reads is written
 // first in the same call (the control block is cleared, the matrix rows and the working vectors are
@@ -48,15 +48,21 @@ constexpr size_t kOffP = align256(kOffE + kVec * sizeof(float));
 constexpr size_t kOffP64 = align256(kOffP + kVec * sizeof(float));
 constexpr size_t kOffT = align256(kOffP64 + kVec * sizeof(double));
 constexpr size_t kScratchBytes = align256(kOffT + kVec * sizeof(float));
+static_assert(kScratchBytes == EFS_NOALLOC_SCRATCH_BYTES, "the header states the fixed scratch size");
 
-// The solver's working memory: about 12 MB, zero at load, shared by every call on a device.
+// The solver's working memory (EFS_NOALLOC_SCRATCH_BYTES), zero at load, shared by every call on a device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Host code cannot use g_noalloc_scratch as an address: its device address is looked up once per device.
+// Host code cannot use g_noalloc_scratch as an address: its device address is looked up once per device, in
+// the context current at that first call (the device's primary context for runtime-API callers).  After a
+// cudaDeviceReset, or from another driver context on the same device, the cached address is not valid; neither
+// is supported.
 std::mutex g_addr_mutex;
 unsigned char* g_addr[64] = {};
 
-std::string g_noalloc_error;
+// Per host thread, so that failing calls on different threads do not race on it; the text returned by
+// efs_noalloc_last_error() stays valid until the next failing call on the same thread.
+thread_local std::string g_noalloc_error;
 
 int nfail(int code, const std::string& msg) {
     g_noalloc_error = msg;
@@ -151,7 +157,7 @@ extern "C" int efs_solve_noalloc(int dim, int width, int height, int depth, cons
 
     DevCtl* ctl = reinterpret_cast<DevCtl*>(base + kOffCtl);
     float* p_s = reinterpret_cast<float*>(base + kOffP) + kMaxHalo;
-    efs::SolverArgs a;
+    efs::SolverArgs a{};      // the FP64-variant vectors stay null: that variant is rejected above
     a.g = g;
     a.dim = dim;
     a.solver = params->solver;

@@ -9,7 +9,8 @@
 //     column (no hash map); row and column sums that the reference forms by iterating over A become passes
 //     over those weights with atomic adds for the scattered part.
 // Density sharpening applies every cell's change, then traces every changed cell on that field, then
-// scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell.
+// scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell, which
+// EFS_SHARPEN_SEQUENTIAL reproduces on one thread for parity.
 #include <mutex>
 
 #include "efs_batch.h"
@@ -225,8 +226,9 @@ __device__ __forceinline__ void sharpen_trace_one(const Geo& g, const float* __r
 }
 
 // Trilinear scatter of `value` at (px, py, pz) onto the non-solid corners (scatter_values,
-// CPUSimulator3D.cpp:609-655).
-template <int DIM>
+// CPUSimulator3D.cpp:609-655).  ATOMIC: many threads scatter at once (parallel mode); otherwise one thread
+// owns rho (sequential mode) and adds in the reference's corner order.
+template <int DIM, bool ATOMIC = true>
 __device__ __forceinline__ void sharpen_scatter_one(const Geo& g, float* __restrict__ rho, const uint8_t* __restrict__ solid,
                                                     float px, float py, float pz, float value) {
     const int x0 = clampi((int)px, 0, g.W - 1), y0 = clampi((int)py, 0, g.H - 1);
@@ -255,7 +257,10 @@ __device__ __forceinline__ void sharpen_scatter_one(const Geo& g, float* __restr
         if (total < 1e-6f) return;
         const float inv = 1.f / total;
 #pragma unroll
-        for (int k = 0; k < 8; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+        for (int k = 0; k < 8; k++) {
+            if (ATOMIC) atomicAdd(&rho[c[k]], value * w[k] * inv);
+            else rho[c[k]] += value * w[k] * inv;
+        }
     } else {
         float w[4];
         w[0] = (1.f - fx) * (1.f - fy); w[1] = fx * (1.f - fy); w[2] = (1.f - fx) * fy; w[3] = fx * fy;
@@ -266,7 +271,10 @@ __device__ __forceinline__ void sharpen_scatter_one(const Geo& g, float* __restr
         if (total < 1e-6f) return;
         const float inv = 1.f / total;
 #pragma unroll
-        for (int k = 0; k < 4; k++) atomicAdd(&rho[c[k]], value * w[k] * inv);
+        for (int k = 0; k < 4; k++) {
+            if (ATOMIC) atomicAdd(&rho[c[k]], value * w[k] * inv);
+            else rho[c[k]] += value * w[k] * inv;
+        }
     }
 }
 
@@ -289,6 +297,63 @@ __global__ void k_sharpen_scatter(Geo g, float* __restrict__ rho, const uint8_t*
     const int n = min(ctl->sh_count, cap);
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
         sharpen_scatter_one<DIM>(g, rho, solid, ends[3 * s], ends[3 * s + 1], ends[3 * s + 2], -val[s]);
+}
+
+// EFS_SHARPEN_SEQUENTIAL: the reference's loop (CPUSimulator3D.cpp:446-455, CPUSimulator2D.cpp:388-401) in its
+// own order.  The changes of every cell were computed from the density before the loop (k_sharpen_calc) and
+// spread into the dense array `del` (zero where a cell does not change).  One block walks the cells in index
+// order, 1024 at a time: its threads compact that slice's changed cells in order into shared memory, and thread
+// 0 then applies, traces and scatters each of them before the next, so every trace sees the density that the
+// cells before it left, as in the reference.  rho is written here, so it is read through plain loads.
+__global__ void k_sharpen_densify(float* __restrict__ del, const int* __restrict__ idx, const float* __restrict__ val,
+                                  const DevCtl* ctl, int cap) {
+    const int n = min(ctl->sh_count, cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) del[idx[s]] = val[s];
+}
+
+constexpr int kSeqThreads = 1024;
+
+template <int DIM>
+__global__ void __launch_bounds__(kSeqThreads) k_sharpen_sequential(Geo g, float* rho, const uint8_t* __restrict__ solid,
+                                                                   const float* __restrict__ del, float Dist) {
+    __shared__ int s_list[kSeqThreads];
+    __shared__ int s_off[kSeqThreads / 32];
+    __shared__ int s_n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int base = 0; base < g.N; base += kSeqThreads) {
+        const int i = base + tid;
+        // cells outside the interior were never listed, so their del is 0; a NaN change counts as changed,
+        // as in the reference's `std::abs(dr) < 1e-6f` test
+        const bool act = i < g.N && !(fabsf(del[i]) < 1e-6f);
+        const unsigned m = __ballot_sync(0xffffffffu, act);
+        if (lane == 0) s_off[warp] = __popc(m);
+        __syncthreads();
+        if (warp == 0) {
+            const int v = s_off[lane];
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            s_off[lane] = incl - v;
+            if (lane == 31) s_n = incl;
+        }
+        __syncthreads();
+        if (act) s_list[s_off[warp] + __popc(m & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        if (tid == 0) {
+            for (int k = 0; k < s_n; k++) {
+                const int c = s_list[k];
+                const float dr = del[c];
+                rho[c] = maxf(rho[c] + dr, 0.f);
+                float px, py, pz;
+                sharpen_trace_one<DIM>(g, rho, solid, c, Dist, px, py, pz);
+                sharpen_scatter_one<DIM, false>(g, rho, solid, px, py, pz, -dr);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1086,6 +1151,16 @@ static cudaError_t stage_sharpen(efs_ctx* c) {
     if (c->dim == 3) k_sharpen_calc<3><<<gr, b, 0, c->stream>>>(g, c->rho, delT, c->sh_idx, c->sh_val, c->ctl, cap);
     else k_sharpen_calc<2><<<gr, b, 0, c->stream>>>(g, c->rho, delT, c->sh_idx, c->sh_val, c->ctl, cap);
     EFS_LAUNCH_CHECK();
+    if (c->prm.sharpen_mode == EFS_SHARPEN_SEQUENTIAL) {
+        // bsum is rho_advect's column-sum scratch, cleared by rho_advect before its first use
+        if ((e = cudaMemsetAsync(c->bsum, 0, (size_t)g.N * sizeof(float), c->stream)) != cudaSuccess) return e;
+        k_sharpen_densify<<<lg, 256, 0, c->stream>>>(c->bsum, c->sh_idx, c->sh_val, c->ctl, cap);
+        EFS_LAUNCH_CHECK();
+        if (c->dim == 3) k_sharpen_sequential<3><<<1, kSeqThreads, 0, c->stream>>>(g, c->rho, c->solid, c->bsum, c->prm.rho_d);
+        else k_sharpen_sequential<2><<<1, kSeqThreads, 0, c->stream>>>(g, c->rho, c->solid, c->bsum, c->prm.rho_d);
+        EFS_LAUNCH_CHECK();
+        return cudaSuccess;
+    }
     k_sharpen_apply<<<lg, 256, 0, c->stream>>>(c->rho, c->sh_idx, c->sh_val, c->ctl, cap);
     EFS_LAUNCH_CHECK();
     if (c->dim == 3) {

@@ -114,10 +114,15 @@ enum efs_field {
 
 /* Density-sharpen scatter semantics.  The reference applies each cell's change and scatters its
  * counter-mass while later cells of the same loop read the updated density
- * (CPUSimulator3D.cpp:446-455).  The GPU applies every cell's change first, then traces all cells
- * on that field, then scatters; the two differ only through the order of those updates. */
+ * (CPUSimulator3D.cpp:446-455, CPUSimulator2D.cpp:388-401).  EFS_SHARPEN_PARALLEL (default, the fast
+ * path) applies every cell's change first, then traces all cells on that field, then scatters; the two
+ * differ only through the order of those updates.  EFS_SHARPEN_SEQUENTIAL is the reference's order, for
+ * parity: one thread walks the changed cells in cell order and applies, traces and scatters each before the
+ * next (bit-exact with the reference's loop; about 0.1-2 s a step at 128^3-256^3, so not a fast path).
+ * Batches (efs_batch_*) run the parallel mode only. */
 enum efs_sharpen_mode {
-    EFS_SHARPEN_PARALLEL = 0
+    EFS_SHARPEN_PARALLEL = 0,
+    EFS_SHARPEN_SEQUENTIAL = 1
 };
 
 /* Values of the reference Properties the step reads (Properties.h:141-162, 186-192). */
@@ -243,13 +248,16 @@ int  efs_timer_elapsed(efs_ctx* ctx, int slot_begin, int slot_end, double* ms);
  * allocation of its plug-ins, a real-time loop that may not synchronise the device, work recorded into a CUDA
  * graph): ISolver::solve on caller-owned device buffers rho, boundary, divergence and pressure (N floats each,
  * reference layout), on `stream` (a cudaStream_t; NULL = the legacy default stream).  Working memory is one
- * fixed file-scope device array of about 10 MB that every device loading the library keeps until exit, so
- * grids are limited to EFS_NOALLOC_MAX_CELLS cells and larger ones are rejected with EFS_ERR_ARG.  The first
- * call on each device looks up that array's address (make it before any stream capture).  All calls share
- * the array: calls whose work overlaps on the GPU race.  With stats == NULL the call returns after queueing
- * its work; otherwise it waits for the stream and fills stats (EFS_ERR_NOT_CONVERGED when max_steps ran out).
- * Errors of this entry point are reported by efs_noalloc_last_error(). */
+ * fixed file-scope device array of EFS_NOALLOC_SCRATCH_BYTES (about 13.2 MB) that every device loading the
+ * library keeps until exit, so grids are limited to EFS_NOALLOC_MAX_CELLS cells and larger ones are rejected
+ * with EFS_ERR_ARG.  The first call on each device looks up that array's address in the context current then
+ * (make it before any stream capture); a cudaDeviceReset or a second driver context on the same device is not
+ * supported afterwards.  All calls share the array: calls whose work overlaps on the GPU race.  With
+ * stats == NULL the call returns after queueing its work; otherwise it waits for the stream and fills stats
+ * (EFS_ERR_NOT_CONVERGED when max_steps ran out).  Errors of this entry point are reported by
+ * efs_noalloc_last_error(), per host thread; its text stays valid until that thread's next failing call. */
 #define EFS_NOALLOC_MAX_CELLS 262144
+#define EFS_NOALLOC_SCRATCH_BYTES 13159168
 int  efs_solve_noalloc(int dim, int width, int height, int depth, const efs_params* params,
                        const float* rho, const float* boundary, const float* divergence, float* pressure,
                        void* stream, efs_stats* stats);

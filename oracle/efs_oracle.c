@@ -13,12 +13,51 @@
  */
 #include "efs_oracle.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
 #define BOUNDARY 1.0f
+
+/* Threads.  When built with OpenMP (oracle/Makefile adds -fopenmp where the compiler has it) the solvers'
+ * per-cell loops (matrix products, vector updates, Jacobi sweeps) run on all host threads; each cell's result
+ * is the same as in the serial loop.  FP64 dot products are summed in fixed blocks of ORC_DOT_BLOCK cells,
+ * each block in cell order and the block sums in block order, so the value does not depend on the thread
+ * count; grids of up to ORC_DOT_BLOCK cells form one block, i.e. the plain serial sum.  The float dot products
+ * of the reference (ScalField3D.h:91-97) and every stage stay serial, in the reference's order. */
+#define ORC_DOT_BLOCK ((size_t)1 << 20)
+#define ORC_PAR_MIN 65536   /* smaller loops stay on the calling thread */
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* sum over [0, n) of f(k) in the fixed block order above; f is an expression in the index variable */
+#define ORC_BLOCKED_SUM(result, n, idx, expr) do { \
+    const size_t n_ = (n); \
+    const size_t nb_ = (n_ + ORC_DOT_BLOCK - 1) / ORC_DOT_BLOCK; \
+    if (nb_ <= 1) { double s_ = 0; for (size_t idx = 0; idx < n_; idx++) s_ += (expr); (result) = s_; break; } \
+    double* part_ = (double*)malloc(nb_ * sizeof(double)); \
+    _Pragma("omp parallel for schedule(static)") \
+    for (long k_ = 0; k_ < (long)nb_; k_++) { \
+        const size_t lo_ = (size_t)k_ * ORC_DOT_BLOCK, hi_ = lo_ + ORC_DOT_BLOCK < n_ ? lo_ + ORC_DOT_BLOCK : n_; \
+        double s_ = 0; \
+        for (size_t idx = lo_; idx < hi_; idx++) s_ += (expr); \
+        part_[k_] = s_; \
+    } \
+    double t_ = 0; \
+    for (size_t k_ = 0; k_ < nb_; k_++) t_ += part_[k_]; \
+    free(part_); \
+    (result) = t_; \
+} while (0)
 
 typedef struct orc_fent { int32_t i, j; float val; } orc_fent;
 
@@ -635,6 +674,7 @@ static void enforce_walls3(orc_grid* g) {
 static void matmul(const orc_grid* g, float* res, const float* xf) {
     const float* rho = g->rho; const float* bnd = g->boundary;
     const int W = g->W, H = g->H, D = g->D;
+    #pragma omp parallel for collapse(2) schedule(static) if (g->N >= ORC_PAR_MIN)
     for (int z = 0; z < D; z++)
     for (int y = 0; y < H; y++)
     for (int x = 0; x < W; x++) {
@@ -664,7 +704,10 @@ static float fdot(const orc_grid* g, const float* a, const float* b) {  /* ScalF
     float s = 0; for (size_t i = 0; i < g->N; i++) s += a[i] * b[i]; return s;
 }
 static double ddot(const orc_grid* g, const float* a, const float* b) {
-    double s = 0; for (size_t i = 0; i < g->N; i++) s += (double)a[i] * (double)b[i]; return s;
+    double s; ORC_BLOCKED_SUM(s, g->N, i, (double)a[i] * (double)b[i]); return s;
+}
+static double dddot(size_t n, const double* a, const double* b) {
+    double s; ORC_BLOCKED_SUM(s, n, i, a[i] * b[i]); return s;
 }
 
 /* the solver threshold the step uses (PROPERTY_F(SOLVER_THRESHOLD), or the relative-residual hook) */
@@ -741,10 +784,12 @@ static float cg_solve_mixed(orc_grid* g, float thr) {
     double* t64 = (double*)malloc(N * sizeof(double));
     double rr;
     #define ORC_REPLACE() do { \
-        for (size_t c = 0; c < N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
+        _Pragma("omp parallel for schedule(static) if (N >= ORC_PAR_MIN)") \
+        for (long c = 0; c < (long)N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
         matmul_d(g, t64, p64); \
-        rr = 0; \
-        for (size_t c = 0; c < N; c++) { r[c] = (float)((double)b[c] - t64[c]); rr += (double)r[c] * (double)r[c]; } \
+        _Pragma("omp parallel for schedule(static) if (N >= ORC_PAR_MIN)") \
+        for (long c = 0; c < (long)N; c++) r[c] = (float)((double)b[c] - t64[c]); \
+        rr = ddot(g, r, r); \
     } while (0)
     for (size_t c = 0; c < N; c++) { p64[c] = (double)b[c]; e[c] = 0.f; }
     ORC_REPLACE();
@@ -756,11 +801,13 @@ static float cg_solve_mixed(orc_grid* g, float thr) {
         for (i = 0; i < steps; i++) {
             matmul(g, t, d);
             const float alpha = (float)(rr / ddot(g, d, t));
-            for (size_t c = 0; c < N; c++) e[c] += alpha * d[c];
+            #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+            for (long c = 0; c < (long)N; c++) e[c] += alpha * d[c];
             const double old = rr;
             int replaced = 0;
             if (i & 0x3F) {
-                for (size_t c = 0; c < N; c++) r[c] += (-alpha) * t[c];
+                #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+                for (long c = 0; c < (long)N; c++) r[c] += (-alpha) * t[c];
                 rr = ddot(g, r, r);
             } else { ORC_REPLACE(); replaced = 1; }
             if (rr < (double)thr) {
@@ -768,7 +815,8 @@ static float cg_solve_mixed(orc_grid* g, float thr) {
                 if (rr < (double)thr) { conv = 1; break; }
             }
             const float beta = (float)(rr / old);
-            for (size_t c = 0; c < N; c++) { d[c] *= beta; d[c] += r[c]; }
+            #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+            for (long c = 0; c < (long)N; c++) { d[c] *= beta; d[c] += r[c]; }
         }
         g->solve_steps = i + 1;
     }
@@ -796,10 +844,12 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
     double* t64 = (double*)malloc(N * sizeof(double));
     double rr;
     #define ORC_REPLACE() do { \
-        for (size_t c = 0; c < N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
+        _Pragma("omp parallel for schedule(static) if (N >= ORC_PAR_MIN)") \
+        for (long c = 0; c < (long)N; c++) { p64[c] += (double)e[c]; e[c] = 0.f; } \
         matmul_d(g, t64, p64); \
-        rr = 0; \
-        for (size_t c = 0; c < N; c++) { r[c] = (float)((double)b[c] - t64[c]); rr += (double)r[c] * (double)r[c]; } \
+        _Pragma("omp parallel for schedule(static) if (N >= ORC_PAR_MIN)") \
+        for (long c = 0; c < (long)N; c++) r[c] = (float)((double)b[c] - t64[c]); \
+        rr = ddot(g, r, r); \
     } while (0)
     for (size_t c = 0; c < N; c++) { p64[c] = (double)b[c]; e[c] = 0.f; }
     ORC_REPLACE();
@@ -819,7 +869,8 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
             int replaced = 0;
             if ((i & 0x3F) && est > 0.0) {
                 const float beta = (float)(est / old);
-                for (size_t c = 0; c < N; c++) {
+                #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+                for (long c = 0; c < (long)N; c++) {
                     e[c] += alpha * d[c];
                     const float rn = r[c] + (-alpha) * t[c];
                     r[c] = rn;
@@ -827,11 +878,13 @@ static float cg_solve_mixed_recurrence(orc_grid* g, float thr) {
                 }
                 rr = ddot(g, r, r);
             } else {
-                for (size_t c = 0; c < N; c++) e[c] += alpha * d[c];
+                #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+                for (long c = 0; c < (long)N; c++) e[c] += alpha * d[c];
                 ORC_REPLACE();
                 replaced = 1;
                 const float beta = (float)(rr / old);
-                for (size_t c = 0; c < N; c++) d[c] = d[c] * beta + r[c];
+                #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+                for (long c = 0; c < (long)N; c++) d[c] = d[c] * beta + r[c];
             }
             if (rr < (double)thr) {
                 if (!replaced) {
@@ -940,6 +993,7 @@ static float jacobi_solve(orc_grid* g) {
     const int W = g->W, H = g->H, D = g->D;
     for (int it = 0; it < iters; it++) {
         float* p = g->p; float* tmp = g->jac_tmp;
+        #pragma omp parallel for collapse(2) schedule(static) if (g->N >= ORC_PAR_MIN)
         for (int z = 0; z < D; z++)
         for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
@@ -1440,6 +1494,7 @@ void orc_step(orc_grid* g, int n) {
 static void matmul_d(const orc_grid* g, double* res, const double* xf) {
     const float* rho = g->rho; const float* bnd = g->boundary;
     const int W = g->W, H = g->H, D = g->D;
+    #pragma omp parallel for collapse(2) schedule(static) if (g->N >= ORC_PAR_MIN)
     for (int z = 0; z < D; z++)
     for (int y = 0; y < H; y++)
     for (int x = 0; x < W; x++) {
@@ -1465,19 +1520,21 @@ static void matmul_d(const orc_grid* g, double* res, const double* xf) {
 int orc_solve_fp64(orc_grid* g, double tol, int maxit, double* p) {
     const size_t N = g->N;
     double* r = (double*)malloc(N * 8); double* d = (double*)malloc(N * 8); double* t = (double*)malloc(N * 8);
-    double bb = 0;
-    for (size_t i = 0; i < N; i++) { p[i] = 0; r[i] = g->div[i]; d[i] = r[i]; bb += r[i] * r[i]; }
+    for (size_t i = 0; i < N; i++) { p[i] = 0; r[i] = g->div[i]; d[i] = r[i]; }
+    const double bb = dddot(N, r, r);
     double rr = bb;
     int it = 0;
     const double thr = tol * tol * bb;
     while (it < maxit && rr > thr && rr > 0) {
         matmul_d(g, t, d);
-        double dt = 0; for (size_t i = 0; i < N; i++) dt += d[i] * t[i];
+        const double dt = dddot(N, d, t);
         const double a = rr / dt;
-        for (size_t i = 0; i < N; i++) { p[i] += a * d[i]; r[i] -= a * t[i]; }
-        double rn = 0; for (size_t i = 0; i < N; i++) rn += r[i] * r[i];
+        #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+        for (long i = 0; i < (long)N; i++) { p[i] += a * d[i]; r[i] -= a * t[i]; }
+        const double rn = dddot(N, r, r);
         const double b = rn / rr; rr = rn;
-        for (size_t i = 0; i < N; i++) d[i] = r[i] + b * d[i];
+        #pragma omp parallel for schedule(static) if (N >= ORC_PAR_MIN)
+        for (long i = 0; i < (long)N; i++) d[i] = r[i] + b * d[i];
         it++;
     }
     free(r); free(d); free(t);

@@ -65,6 +65,8 @@ int       orc_solve_fp64(orc_grid* g, double tol, int maxit, double* p_out);
 double    orc_relres_fp64(orc_grid* g, const float* p);
 /* sum of rho over all cells in FP64 */
 double    orc_total_mass(orc_grid* g);
+/* host threads the solvers' per-cell loops use (1 without OpenMP) */
+int       orc_threads(void);
 
 /* seeded scenes of include/efs_scene.h */
 int       orc_scene_dam3d(int w, int h, int d, int n_min, int n_max, uint64_t seed, float* boundary, float* rho);

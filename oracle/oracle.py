@@ -18,18 +18,35 @@ from eulerianfluidsimulation_gb300.abi import (EfsParams, EfsStats, FIELD_COUNT,
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORC = os.path.join(HERE, "liborc.so")
 LIBREF = os.path.join(HERE, "_ref", "libefs_ref.so")
-REFERENCE_TREE = "/root/reference"
 
 DOTS_FP64 = 1
 SHARPEN_PARALLEL = 2
 REVERSE_SUMS = 4
 
 
+def reference_tree():
+    """Where the reference's source tree is: $EFS_REFERENCE_TREE, else the build recipe's default (the REF
+    variable of oracle/Makefile).  The path may not exist (machines without the reference)."""
+    env = os.environ.get("EFS_REFERENCE_TREE")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as fh:
+        for line in fh:
+            if line.startswith("REF ?="):
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+def reference_tree_present():
+    t = reference_tree()
+    return bool(t) and os.path.isdir(os.path.join(t, "src"))
+
+
 def build(reference=True):
     """Build liborc.so and, when the reference tree is present, _ref/libefs_ref.so."""
     subprocess.check_call(["make", "-s", "-C", HERE, "oracle"])
-    if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "src")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_TREE])
+    if reference and reference_tree_present():
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + reference_tree()])
 
 
 def reference_available():

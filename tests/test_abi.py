@@ -8,8 +8,9 @@ import tempfile
 
 import pytest
 
+from oracle import oracle
+
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
-REFERENCE = "/root/reference"
 
 
 def _lib():
@@ -74,9 +75,10 @@ def test_scene_generators_match_the_oracle():
         assert np.array_equal(c[0], d[0]) and np.array_equal(c[1], d[1])
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "include")), reason="reference tree not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(oracle.reference_tree(), "include")), reason="reference tree not present")
 def test_drop_in_backend_builds_against_reference_headers():
     _lib()
+    REFERENCE = oracle.reference_tree()
     inc = ["-I", os.path.join(ROOT, "oracle", "shim"), "-I", os.path.join(REFERENCE, "include"), "-I", os.path.join(ROOT, "include")]
     srcs = [os.path.join(REFERENCE, "src/simulation/simulator/ISimulator.cpp")] + \
         [os.path.join(REFERENCE, f"src/simulation/data/{k}.cpp") for k in ("ScalField3D", "ScalField2D", "VecField3D", "VecField2D")]

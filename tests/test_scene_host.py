@@ -24,7 +24,7 @@ from oracle import oracle
 from tests.helpers import box_mesh, sphere_mesh, write_obj
 from tests.scene_grid import OracleSceneGrid
 
-REF_SCENES = "/root/reference/assets/scenes"
+REF_SCENES = os.path.join(oracle.reference_tree(), "assets", "scenes")
 
 
 def _centres(shape, center, size):
