@@ -108,10 +108,16 @@ def test_c1_jacobi_one_step(sharpen):
 
 
 # Stated drift bound after 200 steps of the 2D Jacobi dam break (relative L2 of u/v, rho, p against the
-# oracle).  Jacobi itself is deterministic per cell (bit-exact per solve); what drifts is rho_advect's float
-# summation order (atomics against the oracle's cell order), which threshold decisions (the sharpen trace
-# stopping at rho = 0.5, the diffusion's equality test) can amplify.
-DRIFT_C1 = 1e-3
+# oracle).  One step is bit-identical to the oracle in both sharpen modes (test_c1_jacobi_one_step); what
+# drifts is rho_advect's float summation order (atomics against the oracle's cell order), which threshold
+# decisions (the sharpen trace stopping at rho = 0.5, the diffusion's equality test, beta >= 1) turn into
+# relocated mass.  Measured on two runs (the atomics' order changes between runs): GPU against oracle,
+# parallel mode u/v 6.8e-7 and 2.5e-4, rho 4.6e-6 and 9.9e-4, p 9.1e-6 and 9.1e-4; sequential mode u/v 1.3e-2
+# and 9.0e-8, rho 6.8e-4 and 7.2e-7, p 5.7e-4 and 2.2e-7.  The oracle against itself with only its advection
+# summation order reversed reaches u/v 4.1e-3 and p 5.0e-3 (parallel mode, steps 120-160) on the same scene:
+# the bound is a small multiple of that.  After the 200 steps the sharpen stage is still bit-exact (sequential)
+# or within 1e-6 (parallel) from the GPU's state.
+DRIFT_C1 = 5e-2
 
 
 @pytest.mark.parametrize("sharpen", [abi.SHARPEN_PARALLEL, abi.SHARPEN_SEQUENTIAL])
@@ -135,6 +141,17 @@ def test_c1_jacobi_drift_after_200_steps(sharpen):
     print(f"c1 mass {m0:.6f} -> {m1:.6f} (rel {(m1 - m0) / m0:.2e}); oracle {mo:.6f} (rel {(mo - m0) / m0:.2e})")
     assert abs(m1 - m0) / m0 < 5e-6
     assert np.all(np.isfinite(got[abi.FIELD_VEL]))
+    # the stage that differs between the modes, run from the GPU's 200-step state on both
+    o.set_fields(got)
+    with gb.GB300Simulator2D(128, 128, prm) as s:
+        s.set_fields(got)
+        s.stage(abi.STAGE_RHO_SHARPEN)
+        o.stage(abi.STAGE_RHO_SHARPEN)
+        g2, w2 = s.fields(), o.fields()
+    if sharpen == abi.SHARPEN_SEQUENTIAL:
+        assert_exact(g2, w2, range(abi.FIELD_COUNT), "sequential sharpen after 200 steps")
+    else:
+        assert_close(g2, w2, (abi.FIELD_RHO,), 1e-6, "parallel sharpen after 200 steps")
 
 
 # ------------------------------------------------------------------------------------------------
