@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--fcg-train-iters", type=int, default=2000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-alt", action="store_true", help="skip the Jacobi and learned-PCG comparison runs")
+    ap.add_argument("--alt-steps", type=int, default=4, help="timed steps of each comparison run")
     ap.add_argument("--study", default=None, choices=["precision"],
                     help="instead of the throughput line: the precision study (every field against an FP64 "
                          "pressure solve of the same right-hand side) at --size for --steps steps")
@@ -166,38 +168,58 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(a, prm, cg_iters):
-    """Time the CPU oracle (port of the reference CPU step) on the same 256^3 state: stages 0-5 once, the project
-    set-up, and 8 CG iterations; the step time scales the CG part to `cg_iters` iterations."""
+def host_cpu():
+    """The host's CPU model and logical core count (lscpu; /proc/cpuinfo as a fallback)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"model": model or "unknown", "logical_cores": os.cpu_count()}
+
+
+def cpu_sample(a, prm):
+    """Time one whole step of the CPU oracle (the reference CPU step restated: CPUSimulator3D.cpp's stages in the
+    reference's own order, density sharpening sequential as the reference loops) on the same 256^3 scene, the
+    pressure solve included and run to convergence.  The stages run on one thread, as the reference's do; the
+    solver's per-cell loops (matrix products, vector updates) run on all host threads.  The solver is the CG
+    variant of the CUDA path (the reference's FP32 CG stalls above rel-res 1e-6 at this size and would run to
+    MAX_STEPS), so both arms do the same iterations."""
     from eulerianfluidsimulation_gb300 import abi
     from oracle import oracle
     n = a.size
     b, r = oracle.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
-    p = prm.copy()
-    o = oracle.Oracle(3, n, n, n, p)
+    o = oracle.Oracle(3, n, n, n, prm.copy())
     o.set_field(abi.FIELD_BOUNDARY, b)
     o.set_field(abi.FIELD_RHO, r)
+    threads = oracle._load_orc().orc_threads()
     t0 = time.perf_counter()
     for s in range(abi.STAGE_PROJECT):
-        if not (p.disable_mask >> s) & 1:
+        if not (prm.disable_mask >> s) & 1:
             o.stage(s)
     t1 = time.perf_counter()
-    state = o.fields()
-    p0 = p.copy(); p0.max_steps = 0
-    o.set_params(p0)
-    ta = time.perf_counter(); o.stage(abi.STAGE_PROJECT); tb = time.perf_counter()
-    k = 8
-    pk = p.copy(); pk.max_steps = k
-    o.set_fields(state)
-    o.set_params(pk)
-    tc = time.perf_counter(); o.stage(abi.STAGE_PROJECT); td = time.perf_counter()
-    t_stages, t_setup = t1 - t0, tb - ta
-    t_iter = max((td - tc) - t_setup, 0.0) / k
-    step_s = t_stages + t_setup + cg_iters * t_iter
-    return {"value": 1.0 / step_s, "unit": "steps/s", "cores": 1, "kind": "port",
-            "sample": (f"one {n}^3 step on 1 core: stages 0-5 {t_stages:.2f} s, project set-up {t_setup:.2f} s, "
-                       f"{k} CG iterations at {t_iter * 1e3:.1f} ms each scaled to {cg_iters:.0f} iterations/step"),
-            "step_s": step_s}
+    o.stage(abi.STAGE_PROJECT)
+    t2 = time.perf_counter()
+    st = o.stats()
+    step_s = t2 - t0
+    return {"value": 1.0 / step_s, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": (f"one whole {n}^3 step measured (no extrapolation): stages 0-5 {t1 - t0:.2f} s on 1 thread, "
+                       f"project {t2 - t1:.2f} s ({st.solve_steps} CG iterations to rel-res 1e-6, converged="
+                       f"{bool(st.converged)}) with its per-cell loops on {threads} threads"),
+            "step_s": step_s, "stages_s": t1 - t0, "project_s": t2 - t1, "cg_iters": st.solve_steps,
+            "host": host_cpu()}
 
 
 def run_reference(a):
@@ -205,19 +227,97 @@ def run_reference(a):
     if rank != 0:
         return
     prm = workload(a)
-    # unmeasured sizes: plain CG's iteration count grows about linearly with the grid side
-    cg_iters = CG_ITERS_MEASURED.get((a.size, a.spheres), round(CG_ITERS_PER_STEP_REF * a.size / 256))
     t = time.perf_counter()
-    cs = cpu_sample(a, prm, cg_iters)
+    cs = cpu_sample(a, prm)
     wall = time.perf_counter() - t
     line = {"metric": METRIC, "value": cs["value"], "unit": "steps/s", "n_gpus": a.gpus, "steps": 1, "warmup": 0,
             "ms_per_step": cs["step_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "config": config(a), "impl": "reference",
             "cpu_baseline": {"value": cs["value"], "unit": "steps/s", "cores": cs["cores"], "kind": cs["kind"],
-                             "sample": cs["sample"] + f"; CG count = the CUDA path's measured mean ({cg_iters})"},
+                             "sample": cs["sample"], "host": cs["host"]},
             "e2e": {"value": cs["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "sample_wall_s": wall}
+            "sample_wall_s": wall,
+            "note": "one whole step is the bounded sample (about 20-30 s on 16 Grace cores); --steps/--warmup are "
+                    "not repeated on the CPU"}
     print(json.dumps(line), flush=True)
+
+
+def masked_relres(div, p, rho, boundary):
+    """||b - L p|| / ||b|| in FP64 for the reference's pressure matrix (CGSolver.cpp:467-497): rows are liquid
+    (rho > 0.5), non-solid cells; a neighbour counts when it is inside the border and not solid, and adds its p
+    when it is liquid."""
+    div, p, rho, bnd = (np.asarray(x, np.float64) for x in (div, p, rho, boundary))
+    D, H, W = p.shape
+    row = (rho > 0.5) & (bnd != 1.0)
+    inner = np.zeros(p.shape, bool)
+    inner[1:D - 1, 1:H - 1, 1:W - 1] = True
+    ok = inner & (bnd <= 0.5)
+    liq = ok & (rho > 0.5)
+    cnt = np.zeros(p.shape)
+    acc = np.zeros(p.shape)
+    for ax in range(3):
+        for sh in (1, -1):
+            okn = np.roll(ok, sh, axis=ax)
+            pn = np.roll(np.where(liq, p, 0.0), sh, axis=ax)
+            cnt += okn
+            acc += pn
+    Lp = np.where(row, acc - cnt * p, p)
+    res = div - Lp
+    bb = float(np.sum(div * div))
+    return float(np.sqrt(np.sum(res * res) / bb)) if bb > 0 else float(np.sqrt(np.sum(res * res)))
+
+
+def alt_solver_line(a, kind, b, r, cg_ms_step, cg_solve_ms, cg_iters):
+    """One comparison run on the benchmark scene: `kind` = "jacobi" (100 sweeps a step, JacobiSolverCPU3D with
+    MAX_STEPS 200) or "fcg" (flexible PCG with the learned U-Net preconditioner, to the same rel-res 1e-6).
+    Warm-up steps then --alt-steps timed steps with CUDA events on the library's stream."""
+    import eulerianfluidsimulation_gb300 as gb
+    from eulerianfluidsimulation_gb300 import abi, unet_weights
+    n = a.size
+    prm = workload(a)
+    info = {}
+    if kind == "jacobi":
+        prm.solver = abi.SOLVER_JACOBI
+        prm.max_steps = 200
+    else:
+        prm.solver = abi.SOLVER_FCG_UNET
+    sim = gb.GB300Simulator3D(n, n, n, prm)
+    try:
+        sim.set_field(abi.FIELD_BOUNDARY, b)
+        sim.set_field(abi.FIELD_RHO, r)
+        if kind == "fcg":
+            info = unet_weights.load_into(sim)
+        warm = 2
+        for _ in range(warm):
+            sim.update(1)
+        sim.synchronize()
+        st0 = sim.stats()
+        k = max(1, a.alt_steps)
+        sim.solve_timing_arm(k)
+        sim.mark(0)
+        sim.update(k)
+        sim.mark(1)
+        ms = sim.elapsed_ms(0, 1)
+        st1 = sim.stats()
+        launches, solve_ms, _, _ = sim.solve_timing_read()
+        out = {"steps_per_s": k / (ms / 1e3), "ms_per_step": ms / k, "steps": k, "warmup": warm,
+               "solve_iters_per_step": (st1.total_solve_steps - st0.total_solve_steps) / k,
+               "solve_ms_per_step": (solve_ms / launches) if launches else None,
+               "converged": bool(st1.converged), "paused": bool(st1.paused)}
+        if kind == "jacobi":
+            f = sim.fields()
+            out["rel_res_after_100_sweeps"] = masked_relres(f[abi.FIELD_DIVERGENCE], f[abi.FIELD_PRESSURE],
+                                                            f[abi.FIELD_RHO], f[abi.FIELD_BOUNDARY])
+            out["note"] = "Jacobi does not reach rel-res 1e-6; it runs its fixed 100 sweeps (the reference's Jacobi)"
+        else:
+            out["precond_iters_per_step"] = (st1.precond_steps - st0.precond_steps) / k
+            out["network"] = info
+        out["vs_plain_cg"] = {"step_speedup": cg_ms_step / out["ms_per_step"],
+                              "solve_speedup": (cg_solve_ms / out["solve_ms_per_step"]) if out["solve_ms_per_step"] else None,
+                              "cg_iters_per_step": cg_iters}
+        return out
+    finally:
+        sim.close()
 
 
 def run_gb300(a):
@@ -325,11 +425,17 @@ def run_gb300(a):
     st2 = sim.stats()
     sim.close()
 
+    # the metric's comparison on the same scene: Jacobi (100 sweeps a step, the reference's other solver) and
+    # learned-preconditioned FCG, each from the seeded scene, timed like the main line (steps, not solves alone)
+    alt = {}
+    if rank == 0 and world == 1 and prm.solver == abi.SOLVER_CG and not a.no_alt:
+        alt["jacobi"] = alt_solver_line(a, "jacobi", b, r, ms / a.steps, roofline["solve_ms_per_step"], iters / max(a.steps, 1))
+        alt["learned_pcg"] = alt_solver_line(a, "fcg", b, r, ms / a.steps, roofline["solve_ms_per_step"], iters / max(a.steps, 1))
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
-        cg_mean = iters / a.steps if a.steps else CG_ITERS_PER_STEP_REF
-        cs = cpu_sample(a, prm, cg_mean if prm.solver == abi.SOLVER_CG else prm.max_steps // 2)
-        cpu = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cs = cpu_sample(a, prm)
+        cpu = {k: cs[k] for k in ("value", "unit", "cores", "kind", "sample", "host")}
 
     if rank == 0:
         line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world, "steps": a.steps,
@@ -340,6 +446,7 @@ def run_gb300(a):
                 "gpu_launches": kernels * a.steps, "kernels_per_step": kernels,
                 "roofline": roofline, "step_roofline": step_roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks}
+        line.update(alt)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

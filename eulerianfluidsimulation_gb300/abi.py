@@ -21,6 +21,9 @@ SOLVER_JACOBI = 0
 SOLVER_CG = 1
 SOLVER_FCG_UNET = 2
 
+FCG_BOTTOM_UNET = 0
+FCG_BOTTOM_JACOBI = 1
+
 SHARPEN_PARALLEL = 0
 SHARPEN_SEQUENTIAL = 1
 
@@ -73,7 +76,9 @@ class EfsParams(ctypes.Structure):
         ("re_calc_div", ctypes.c_int),
         ("sharpen_mode", ctypes.c_int),
         ("cg_variant", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("fcg_levels", ctypes.c_int),
+        ("fcg_bottom", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
     ]
 
     def as_dict(self):
@@ -164,6 +169,8 @@ def params_default():
     p.re_calc_div = 0
     p.sharpen_mode = 0
     p.cg_variant = CG_MIXED_RECURRENCE
+    p.fcg_levels = -1
+    p.fcg_bottom = FCG_BOTTOM_UNET
     return p
 
 

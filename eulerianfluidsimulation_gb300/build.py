@@ -24,6 +24,7 @@ UNITS = {
     "efs_solver.cu": ["--fmad=false"],
     "efs_noalloc.cu": ["--fmad=false"],
     "efs_unet.cu": [],
+    "efs_mlfcg.cu": [],
     "efs_batch.cu": ["--fmad=false"],
     "efs_scene.cu": ["--fmad=false"],
 }

@@ -46,6 +46,8 @@ bool params_valid(const efs_params* p, std::string& why) {
         return false;
     }
     if (p->max_steps < 0) { why = "max_steps must be >= 0"; return false; }
+    if (p->fcg_levels > 3) { why = "fcg_levels must be at most 3"; return false; }
+    if (p->fcg_bottom != EFS_FCG_BOTTOM_UNET && p->fcg_bottom != EFS_FCG_BOTTOM_JACOBI) { why = "unknown fcg_bottom"; return false; }
     if (p->disable_mask & ~EFS_STAGES_ALL) { why = "disable_mask has bits beyond the seven stages"; return false; }
     return true;
 }
@@ -58,6 +60,19 @@ void drop_graphs(efs_ctx* c) {
     c->timing_nodes_begin.clear();
     c->timing_nodes_end.clear();
     c->kernel_nodes.clear();
+    efs::ml_drop_graph(c);
+}
+
+// FCG's buffers are allocated before any capture of a solve (allocation is not allowed while capturing).
+int prepare_fcg(efs_ctx* c) {
+    if (c->prm.solver != EFS_SOLVER_FCG_UNET) return EFS_OK;
+    if (c->dim != 3) return fail(c, EFS_ERR_STATE, "EFS_SOLVER_FCG_UNET is 3D only");
+    if (c->prm.fcg_bottom == EFS_FCG_BOTTOM_UNET && !c->unet)
+        return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
+    if (c->prm.fcg_bottom == EFS_FCG_BOTTOM_UNET && c->unet && !efs::unet_matches(c))
+        return fail(c, EFS_ERR_STATE, "the U-Net was made for another fcg_levels: efs_unet_init again");
+    CK(efs::ml_alloc(c), "FCG buffers");
+    return EFS_OK;
 }
 
 template <typename T>
@@ -113,6 +128,10 @@ cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
 int build_graph(efs_ctx* c, const efs::GraphKey& key, cudaGraphExec_t* out) {
     auto it = c->graphs.find(key);
     if (it != c->graphs.end()) { *out = it->second; return EFS_OK; }
+    if (key.stages & EFS_STAGE_BIT(EFS_STAGE_PROJECT)) {
+        const int s = prepare_fcg(c);
+        if (s != EFS_OK) return s;
+    }
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t le = enqueue_step(c, key.stages, true);
@@ -183,6 +202,13 @@ int ensure_fp64_vectors(efs_ctx* c) {
 
 }  // namespace
 
+namespace efs {
+void drop_all_graphs(efs_ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+}
+}  // namespace efs
+
 extern "C" {
 
 void efs_params_default(efs_params* p) {
@@ -205,6 +231,8 @@ void efs_params_default(efs_params* p) {
     p->re_calc_div = 0;
     p->sharpen_mode = EFS_SHARPEN_PARALLEL;
     p->cg_variant = EFS_CG_MIXED_RECURRENCE;
+    p->fcg_levels = -1;
+    p->fcg_bottom = EFS_FCG_BOTTOM_UNET;
 }
 
 void efs_params_dam(efs_params* p, float cell_size, float dt, int solver, float tol_rel) {
@@ -236,6 +264,7 @@ void efs_destroy(efs_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
+    efs::ml_free(c);
     efs::unet_free(c);
     void* bufs[] = {c->u, c->v, c->w, c->rho, c->gamma, c->beta, c->fx, c->fy, c->fz, c->solid,
                     c->tvel, c->validA, c->validB, c->wb, c->wf, c->bb, c->fb, c->bsum, c->gsum, c->rho_acc,
@@ -570,8 +599,10 @@ int efs_reset_fields(efs_ctx* c) {
 int efs_stage(efs_ctx* c, int stage) {
     if (!c) return EFS_ERR_ARG;
     if (stage < 0 || stage >= EFS_STAGE_COUNT) return fail(c, EFS_ERR_ARG, "unknown stage");
-    if (stage == EFS_STAGE_PROJECT && c->prm.solver == EFS_SOLVER_FCG_UNET && !c->unet)
-        return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
+    if (stage == EFS_STAGE_PROJECT) {
+        const int s = prepare_fcg(c);
+        if (s != EFS_OK) return s;
+    }
     CK(efs::launch_stage(c, stage, false), "stage launch");
     return EFS_OK;
 }
@@ -580,13 +611,6 @@ int efs_step(efs_ctx* c, int n_steps) {
     if (!c) return EFS_ERR_ARG;
     if (n_steps < 0) return fail(c, EFS_ERR_ARG, "n_steps < 0");
     if (n_steps == 0) return EFS_OK;
-    if (c->prm.solver == EFS_SOLVER_FCG_UNET) {
-        // FCG reads its scalars on the host every iteration, so the step runs as direct launches
-        if (!c->unet) return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
-        for (int k = 0; k < n_steps; k++) CK(enqueue_step(c, EFS_STAGES_ALL & ~c->prm.disable_mask, false), "step");
-        c->frames += n_steps;
-        return EFS_OK;
-    }
     efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
     cudaGraphExec_t exec = nullptr;
     int s = build_graph(c, key, &exec);
@@ -610,7 +634,6 @@ int efs_step(efs_ctx* c, int n_steps) {
 
 int efs_step_kernel_count(efs_ctx* c, int* count) {
     if (!c || !count) return EFS_ERR_ARG;
-    if (c->prm.solver == EFS_SOLVER_FCG_UNET) return fail(c, EFS_ERR_STATE, "FCG steps are not captured in a graph");
     efs::GraphKey key{EFS_STAGES_ALL & ~c->prm.disable_mask, c->prm.solver, c->prm.cg_variant};
     cudaGraphExec_t exec = nullptr;
     int s = build_graph(c, key, &exec);
@@ -621,8 +644,8 @@ int efs_step_kernel_count(efs_ctx* c, int* count) {
 
 int efs_solve(efs_ctx* c, efs_stats* out) {
     if (!c) return EFS_ERR_ARG;
-    if (c->prm.solver == EFS_SOLVER_FCG_UNET && !c->unet)
-        return fail(c, EFS_ERR_STATE, "FCG needs a U-Net: efs_unet_init or efs_unet_set_weights");
+    const int ps = prepare_fcg(c);
+    if (ps != EFS_OK) return ps;
     CK(efs::launch_solver_prep(c), "solver prep");
     CK(efs::launch_solver(c), "solver launch");
     int s = efs_get_stats(c, out);

@@ -68,6 +68,18 @@ struct SolverArgs {
     double* t64;
     double* partials;          // 2 slots x 3 values per block
     DevCtl* ctl;
+    const double* thr_dev;     // when set: the absolute r.r threshold, read from device memory (FCG fallback)
+};
+
+// A matrix level of the FCG preconditioner's hierarchy (efs_mlfcg.cu): grid dims, per-cell row flag in bit 15
+// of info; level 0 (w == nullptr) reads its stencil from the solver's rowinfo bits, coarser levels from a
+// float diagonal and six byte face weights (w[k * V + i], k = -x, +x, -y, +y, -z, +z).
+struct LvView {
+    int W, H, D;
+    long long V;
+    const uint16_t* info;
+    const uint8_t* w;
+    const float* diag;
 };
 
 struct GraphKey {
@@ -84,6 +96,7 @@ struct GraphKey {
 
 namespace efs {
 struct UNetState;
+struct MLState;
 }
 
 struct efs_ctx {
@@ -147,6 +160,7 @@ struct efs_ctx {
     std::string err;
 
     efs::UNetState* unet = nullptr;         // learned preconditioner (efs_unet.cu)
+    efs::MLState* ml = nullptr;             // FCG and its multilevel hierarchy (efs_mlfcg.cu)
     void* query_scratch = nullptr;          // efs_query_box block partials and result (efs_scene.cu)
     // efs_step_host: transfers that overlap the step run on `xfer`; the step graph waits for `ev_late` (late
     // inputs) before rho_advect and records `ev_advected` after it
@@ -168,9 +182,29 @@ cudaError_t launch_solver_prep(efs_ctx* c);
 // efs_solver.cu
 cudaError_t solver_configure(efs_ctx* c);
 cudaError_t launch_solver(efs_ctx* c);
-// efs_unet.cu: FCG with the U-Net preconditioner (host-driven, not graph-capturable), and teardown
+// persistent CG on right-hand side b (not the context's divergence) with the absolute threshold *thr_dev, on
+// stream st; the context's solver vectors, pressure and control block (efs_solver.cu)
+cudaError_t launch_solver_on(efs_ctx* c, const float* b, const double* thr_dev, cudaStream_t st);
+// efs_mlfcg.cu: FCG with the multilevel preconditioner; inside a stream capture it adds its nodes, otherwise
+// it replays a cached solve graph.  ml_alloc (outside any capture) sizes the hierarchy for the current params.
 cudaError_t fcg_solve(efs_ctx* c);
+cudaError_t ml_alloc(efs_ctx* c);
+void ml_free(efs_ctx* c);
+void ml_drop_graph(efs_ctx* c);
+int ml_resolve_levels(const efs_ctx* c);
+int ml_levels(const efs_ctx* c);
+void ml_level_dims(const efs_ctx* c, int level, int* W, int* H, int* D);
+LvView ml_view(const efs_ctx* c, int level);
+cudaError_t ml_build(efs_ctx* c, cudaStream_t st);
+cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st);
+cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out);
+int ml_level_cg(efs_ctx* c, const LvView& L, const float* r0, float* e, float* t1, float* t2, float* t3, double tol,
+                int maxit, cudaStream_t st);
+// efs_unet.cu: the network's correction z for residual r on the bottom level B (rows; unscaled), teardown
+cudaError_t unet_correction(efs_ctx* c, const LvView& B, const float* r, float* z, cudaStream_t st);
+bool unet_matches(const efs_ctx* c);   // the network was made for the context's current fcg_levels
 void unet_free(efs_ctx* c);
+void drop_all_graphs(efs_ctx* c);
 // efs_fields.cu
 cudaError_t launch_upload_vec(efs_ctx* c, const float* staged, float* a, float* b, float* cc, cudaStream_t st = nullptr);
 cudaError_t launch_download_vec(efs_ctx* c, float* staged, const float* a, const float* b, const float* cc,

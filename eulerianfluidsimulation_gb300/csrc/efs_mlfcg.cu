@@ -1,0 +1,853 @@
+// efs_mlfcg.cu — flexible preconditioned CG (EFS_SOLVER_FCG_UNET) with a multilevel preconditioner whose
+// coarsest level is solved by the learned U-Net (efs_unet.cu), run entirely on the device.
+//
+// No counterpart in the reference: its solvers are CGSolverCPU3D / JacobiSolverCPU3D
+// (src/simulation/solver/CGSolver.cpp:416-497, JacobiSolver.cpp:154-212).  FCG solves the same matrix L p = b
+// (rows: liquid, non-solid cells, as built by k_solver_prep) to the same stop rule.
+//
+// Hierarchy.  Level 0 is L itself, read from rowinfo (bit 15 row, bits 0-5 the liquid neighbours in the
+// order -x, +x, -y, +y, -z, +z, bits 8-10 the neighbour count: row i of L is sum of its liquid neighbours
+// minus count x_i).  Level l+1 merges 2x2x2 cells of level l (the last cell of an odd side alone); its matrix
+// is P^T A P for the piecewise-constant prolongation P, again a 7-point stencil: per coarse cell a diagonal
+// (the children's diagonals plus the couplings between children) and six face weights (the couplings that
+// cross that face, at most 4^l), stored as one float and six bytes.
+//
+// V-cycle M(r) (one preconditioner application), at each level above the bottom: two damped Jacobi sweeps
+// (weight 0.8) from zero, the residual restricted (summed over the merged cells), the next level's
+// correction, prolongation (added to the merged cells), two more sweeps.  At the bottom level: the U-Net's
+// output e scaled by the line search (e.r)/(e.Ae) on that level, or (for comparison without the network)
+// 20 Jacobi sweeps.
+//
+// FCG(1) (Notay 2000, truncation 1): beta = -(z.q_old)/(d_old.q_old), d = z + beta d, q = A d,
+// alpha = (r.z)/(d.q), x += alpha d, r -= alpha q.  x is FP64 and starts at 0; the true residual b - A x is
+// recomputed in FP64 every 32 iterations and before stopping.  Every scalar lives in device memory: the
+// iteration is the body of a CUDA graph WHILE node whose condition the convergence test sets, with the
+// residual recomputation in an IF node inside it; after the loop an IF node hands a stalled solve (residual
+// not halved over 10 iterations, or d.Ad >= 0) to the persistent CG kernel on the residual system.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "efs_internal.h"
+
+namespace efs {
+
+namespace {
+
+constexpr float kOmega = 0.8f;        // Jacobi damping
+constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the network
+constexpr int kRedGrid = 304;         // blocks of every reduction kernel (2 per SM on 152 SMs)
+constexpr int kThreads = 256;
+
+// device scalars of one FCG solve
+struct FcgDev {
+    double rr, rz, dq, zq, bb, thr, alpha, beta, rr_window, rows;
+    double ls_alpha;                  // bottom-level line search factor of the current V-cycle
+    int it, conv, stall, verify, fallback, pad;
+};
+
+inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
+inline unsigned red_blocks(long long n) { return (unsigned)std::min<long long>(kRedGrid, blocks_for(n)); }
+
+// ---- matrix rows at a level -----------------------------------------------------------------------------------
+template <bool FINE>
+__device__ __forceinline__ bool lrow(const LvView& L, long long i, float& dg, float (&w)[6]) {
+    const uint16_t f = L.info[i];
+    if (!(f & 0x8000u)) return false;
+    if (FINE) {
+        dg = -(float)((f >> 8) & 7);
+#pragma unroll
+        for (int k = 0; k < 6; k++) w[k] = ((f >> k) & 1u) ? 1.f : 0.f;
+    } else {
+        dg = L.diag[i];
+#pragma unroll
+        for (int k = 0; k < 6; k++) w[k] = (float)L.w[k * L.V + i];
+    }
+    return true;
+}
+__device__ __forceinline__ long long noff(const LvView& L, int k) {
+    const long long W = L.W, WH = (long long)L.W * L.H;
+    return k == 0 ? -1 : k == 1 ? 1 : k == 2 ? -W : k == 3 ? W : k == 4 ? -WH : WH;
+}
+// (A x)_i for a row (neighbours are read only where the weight is non-zero, i.e. inside the grid)
+template <typename T>
+__device__ __forceinline__ T lapply(const LvView& L, long long i, const T* x, float dg, const float (&w)[6]) {
+    T s = (T)dg * x[i];
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        if (w[k] != 0.f) s += (T)w[k] * x[i + noff(L, k)];
+    return s;
+}
+
+// ---- block reduction of three doubles into partials[3 * blockIdx.x + j] ----------------------------------------
+__device__ __forceinline__ void block_partials(double a, double b, double c, double* part) {
+    __shared__ double sh[3][kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int k = 0; k < kThreads / 32; k++) { s0 += sh[0][k]; s1 += sh[1][k]; s2 += sh[2][k]; }
+        part[3 * blockIdx.x] = s0;
+        part[3 * blockIdx.x + 1] = s1;
+        part[3 * blockIdx.x + 2] = s2;
+    }
+}
+// the totals of `nparts` block partials, summed in block order (run by one thread)
+__device__ __forceinline__ void sum_partials(const double* part, int nparts, double (&t)[3]) {
+    t[0] = t[1] = t[2] = 0;
+    for (int b = 0; b < nparts; b++) { t[0] += part[3 * b]; t[1] += part[3 * b + 1]; t[2] += part[3 * b + 2]; }
+}
+
+// ---- hierarchy -------------------------------------------------------------------------------------------------
+struct LvOut {
+    int W, H, D;
+    long long V;
+    uint16_t* info;
+    uint8_t* w;
+    float* diag;
+};
+template <bool FINE>
+__global__ void k_ml_build(LvView src, LvOut dst) {
+    const long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (C >= dst.V) return;
+    const int X = (int)(C % dst.W), Y = (int)((C / dst.W) % dst.H), Z = (int)(C / ((long long)dst.W * dst.H));
+    bool row = false;
+    float dg = 0.f, w[6] = {0, 0, 0, 0, 0, 0};
+    for (int c8 = 0; c8 < 8; c8++) {
+        const int dx = c8 & 1, dy = (c8 >> 1) & 1, dz = c8 >> 2;
+        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
+        if (x >= src.W || y >= src.H || z >= src.D) continue;
+        const long long i = ((long long)z * src.H + y) * src.W + x;
+        float cd, cw[6];
+        if (!lrow<FINE>(src, i, cd, cw)) continue;
+        row = true;
+        dg += cd;
+        // 1 where the neighbour in direction k lies in the same merged cell
+        const int same[6] = {dx, 1 - dx, dy, 1 - dy, dz, 1 - dz};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (cw[k] == 0.f) continue;
+            if (same[k]) dg += cw[k]; else w[k] += cw[k];
+        }
+    }
+    dst.info[C] = row ? (uint16_t)0x8000u : (uint16_t)0;
+    dst.diag[C] = row ? dg : 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) dst.w[k * dst.V + C] = row ? (uint8_t)w[k] : (uint8_t)0;
+}
+
+// ---- level operators ------------------------------------------------------------------------------------------
+// zout = zin + w (r - A zin) / diag on rows (zin null: zout = w r / diag), 0 elsewhere
+template <bool FINE>
+__global__ void k_ml_smooth(LvView L, const float* __restrict__ r, const float* __restrict__ zin, float* __restrict__ zout,
+                            float omega) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= L.V) return;
+    float dg, w[6];
+    if (!lrow<FINE>(L, i, dg, w) || dg == 0.f) { zout[i] = 0.f; return; }
+    if (!zin) { zout[i] = omega * r[i] / dg; return; }
+    const float az = lapply<float>(L, i, zin, dg, w);
+    zout[i] = zin[i] + omega * (r[i] - az) / dg;
+}
+// rc[C] = sum over the merged rows i of C of (r - A z)_i (z null: of r_i)
+template <bool FINE>
+__global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float* __restrict__ z, LvView Cv,
+                              float* __restrict__ rc) {
+    const long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (C >= Cv.V) return;
+    const int X = (int)(C % Cv.W), Y = (int)((C / Cv.W) % Cv.H), Z = (int)(C / ((long long)Cv.W * Cv.H));
+    float s = 0.f;
+    for (int c8 = 0; c8 < 8; c8++) {
+        const int x = 2 * X + (c8 & 1), y = 2 * Y + ((c8 >> 1) & 1), zz = 2 * Z + (c8 >> 2);
+        if (x >= F.W || y >= F.H || zz >= F.D) continue;
+        const long long i = ((long long)zz * F.H + y) * F.W + x;
+        float dg, w[6];
+        if (!lrow<FINE>(F, i, dg, w)) continue;
+        s += z ? r[i] - lapply<float>(F, i, z, dg, w) : r[i];
+    }
+    rc[C] = s;
+}
+// z_i += ec[parent(i)] on rows
+template <bool FINE>
+__global__ void k_ml_prolong(LvView F, float* __restrict__ z, const float* __restrict__ ec, LvView Cv) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= F.V) return;
+    if (!(F.info[i] & 0x8000u)) return;
+    const int x = (int)(i % F.W), y = (int)((i / F.W) % F.H), zz = (int)(i / ((long long)F.W * F.H));
+    z[i] += ec[((long long)(zz >> 1) * Cv.H + (y >> 1)) * Cv.W + (x >> 1)];
+}
+template <bool FINE>
+__global__ void k_ml_matvec(LvView L, const float* __restrict__ x, float* __restrict__ y) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= L.V) return;
+    float dg, w[6];
+    y[i] = lrow<FINE>(L, i, dg, w) ? lapply<float>(L, i, x, dg, w) : 0.f;
+}
+// bottom line search: partials of e.r and e.(A e)
+template <bool FINE>
+__global__ void k_ml_ls_dots(LvView L, const float* __restrict__ e, const float* __restrict__ r, double* __restrict__ part) {
+    double a = 0, b = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < L.V; i += (long long)gridDim.x * blockDim.x) {
+        float dg, w[6];
+        if (!lrow<FINE>(L, i, dg, w)) continue;
+        const double ei = e[i];
+        a += ei * (double)r[i];
+        b += ei * (double)lapply<float>(L, i, e, dg, w);
+    }
+    block_partials(a, b, 0.0, part);
+}
+__global__ void k_ml_ls_finish(const double* __restrict__ part, int nparts, FcgDev* s) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    const double a = (t[1] != 0.0) ? t[0] / t[1] : 0.0;
+    s->ls_alpha = std::isfinite(a) ? a : 0.0;
+}
+__global__ void k_ml_scale(long long n, float* __restrict__ z, const FcgDev* __restrict__ s) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) z[i] = (float)((double)z[i] * s->ls_alpha);
+}
+
+// ---- FCG ------------------------------------------------------------------------------------------------------
+// x = 0, r = b on rows (0 elsewhere), d = q = 0; partials of b.b and the row count
+__global__ void k_fcg_init(LvView F, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
+                           float* __restrict__ d, float* __restrict__ q, double* __restrict__ part) {
+    double bb = 0, rows = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+        const bool row = F.info[i] & 0x8000u;
+        const float bi = row ? b[i] : 0.f;
+        x[i] = 0.0;
+        r[i] = bi;
+        d[i] = 0.f;
+        q[i] = 0.f;
+        bb += (double)bi * bi;
+        rows += row ? 1.0 : 0.0;
+    }
+    block_partials(bb, rows, 0.0, part);
+}
+// the stop threshold as the CG solvers form it (k_solver): tol_rel^2 b.b rounded to float, or the absolute one
+__global__ void k_fcg_init_finish(const double* __restrict__ part, int nparts, FcgDev* s, float tol_rel, float abs_thr,
+                                  int max_it, cudaGraphConditionalHandle loop) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    s->bb = t[0];
+    s->rows = t[1];
+    s->rr = t[0];
+    double thr;
+    if (tol_rel > 0) {
+        float tf = (float)((double)tol_rel * (double)tol_rel * t[0]);
+        if (!(tf > 0)) tf = FLT_MIN;
+        thr = (double)tf;
+    } else {
+        thr = (double)abs_thr;
+    }
+    s->thr = thr;
+    s->conv = s->rr < thr;
+    s->it = 0;
+    s->stall = 0;
+    s->verify = 0;
+    s->fallback = 0;
+    s->rr_window = s->rr;
+    s->rz = s->dq = s->zq = s->alpha = s->beta = 0;
+    cudaGraphSetConditional(loop, (!s->conv && max_it > 0) ? 1u : 0u);
+}
+// partials of z.q (q = A d of the previous iteration) and r.z
+__global__ void k_fcg_dots_zq_rz(LvView F, const float* __restrict__ z, const float* __restrict__ q,
+                                 const float* __restrict__ r, double* __restrict__ part) {
+    double zq = 0, rz = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+        const double zi = z[i];
+        zq += zi * (double)q[i];
+        rz += zi * (double)r[i];
+    }
+    block_partials(zq, rz, 0.0, part);
+}
+__global__ void k_fcg_beta(const double* __restrict__ part, int nparts, FcgDev* s) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    s->zq = t[0];
+    s->rz = t[1];
+    double beta = 0.0;
+    if (s->it > 0 && s->dq != 0.0) beta = -t[0] / s->dq;
+    s->beta = std::isfinite(beta) ? beta : 0.0;
+}
+__global__ void k_fcg_dir(long long n, float* __restrict__ d, const float* __restrict__ z, const FcgDev* __restrict__ s) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) d[i] = (float)((double)z[i] + s->beta * (double)d[i]);
+}
+// q = A d and the partials of d.q
+__global__ void k_fcg_matvec_dot(LvView F, const float* __restrict__ d, float* __restrict__ q, double* __restrict__ part) {
+    double dq = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+        float dg, w[6];
+        float qi = 0.f;
+        if (lrow<true>(F, i, dg, w)) qi = lapply<float>(F, i, d, dg, w);
+        q[i] = qi;
+        dq += (double)d[i] * qi;
+    }
+    block_partials(dq, 0.0, 0.0, part);
+}
+// alpha = (r.z) / (d.q); L is negative definite on the rows, so d.q >= 0 (or a non-finite alpha) is a breakdown
+__global__ void k_fcg_alpha(const double* __restrict__ part, int nparts, FcgDev* s) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    s->dq = t[0];
+    const double a = s->rz / t[0];
+    if (!(t[0] < 0.0) || !std::isfinite(a)) {
+        s->stall = 1;
+        s->alpha = 0.0;
+    } else {
+        s->alpha = a;
+    }
+}
+// x += alpha d, r -= alpha q; partials of r.r
+__global__ void k_fcg_update(long long n, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ d,
+                             const float* __restrict__ q, const FcgDev* __restrict__ s, double* __restrict__ part) {
+    const double a = s->alpha;
+    double rr = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        x[i] += a * (double)d[i];
+        const float ri = (float)((double)r[i] - a * (double)q[i]);
+        r[i] = ri;
+        rr += (double)ri * ri;
+    }
+    block_partials(rr, 0.0, 0.0, part);
+}
+// r.r, the iteration count, the stall window and whether the true residual is recomputed now
+__global__ void k_fcg_check(const double* __restrict__ part, int nparts, FcgDev* s, cudaGraphConditionalHandle verify) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    s->rr = t[0];
+    s->it += 1;
+    const bool below = s->rr < s->thr;
+    if (!below && !s->stall && (s->it % 10) == 0) {
+        if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
+        s->rr_window = s->rr;
+    }
+    s->verify = !s->stall && (below || (s->it % 32) == 0);
+    if (!s->verify) s->conv = 0;
+    cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
+}
+// r = b - A x in FP64 (rows), partials of r.r
+__global__ void k_fcg_true_resid(LvView F, const float* __restrict__ b, const double* __restrict__ x, float* __restrict__ r,
+                                 double* __restrict__ part) {
+    double rr = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+        float dg, w[6];
+        float ri = 0.f;
+        if (lrow<true>(F, i, dg, w)) ri = (float)((double)b[i] - lapply<double>(F, i, x, dg, w));
+        r[i] = ri;
+        rr += (double)ri * ri;
+    }
+    block_partials(rr, 0.0, 0.0, part);
+}
+__global__ void k_fcg_verify(const double* __restrict__ part, int nparts, FcgDev* s) {
+    if (threadIdx.x != 0) return;
+    double t[3];
+    sum_partials(part, nparts, t);
+    s->rr = t[0];
+    s->conv = s->rr < s->thr;
+}
+// the loop condition for the next iteration
+__global__ void k_fcg_loop(const FcgDev* __restrict__ s, int max_it, cudaGraphConditionalHandle loop) {
+    if (threadIdx.x != 0) return;
+    cudaGraphSetConditional(loop, (!s->conv && !s->stall && s->it < max_it) ? 1u : 0u);
+}
+// after the loop: hand a stalled, unconverged solve to plain CG
+__global__ void k_fcg_post(FcgDev* s, cudaGraphConditionalHandle fallback) {
+    if (threadIdx.x != 0) return;
+    cudaGraphSetConditional(fallback, (s->stall && !s->conv) ? 1u : 0u);
+}
+// fb = b - A x in FP64 (rows; the right-hand side of the fallback CG)
+__global__ void k_fcg_fb_rhs(LvView F, const float* __restrict__ b, const double* __restrict__ x, float* __restrict__ fb) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= F.V) return;
+    float dg, w[6];
+    fb[i] = lrow<true>(F, i, dg, w) ? (float)((double)b[i] - lapply<double>(F, i, x, dg, w)) : 0.f;
+}
+__global__ void k_fcg_fb_add(LvView F, double* __restrict__ x, const float* __restrict__ p) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < F.V && (F.info[i] & 0x8000u)) x[i] += (double)p[i];
+}
+__global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
+    if (threadIdx.x != 0) return;
+    s->fallback = 1;
+    s->conv = ctl->converged;
+}
+__global__ void k_fcg_out(LvView F, const double* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= F.V) return;
+    if (F.info[i] & 0x8000u) {
+        p[i] = (float)x[i];
+        p64[i] = x[i];
+    }
+}
+// solve statistics into the control block; after a fallback the CG launch has counted the solve and its own
+// iterations and convergence, to which the FCG iterations are added
+__global__ void k_fcg_stats(const FcgDev* __restrict__ s, DevCtl* ctl) {
+    if (threadIdx.x != 0) return;
+    const int it = s->it;
+    ctl->precond_iterations = it;
+    if (s->fallback) {
+        ctl->iterations += it;
+        ctl->bb = s->bb;
+    } else {
+        ctl->converged = s->conv;
+        ctl->iterations = it;
+        ctl->rr = s->rr;
+        ctl->bb = s->bb;
+        ctl->thr = s->thr;
+        ctl->active_cells = (long long)s->rows;
+        ctl->solves += 1;
+        ctl->sum_rows += s->rows;
+    }
+    ctl->total_iterations += it;
+    ctl->sum_iter_rows += (double)it * s->rows;
+}
+
+// host-side CG on one level (training samples): dots through these partials
+__global__ void k_lv_dot3(long long n, const float* a0, const float* b0, const float* a1, const float* b1,
+                          double* __restrict__ part) {
+    double s0 = 0, s1 = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        s0 += (double)a0[i] * b0[i];
+        if (a1) s1 += (double)a1[i] * b1[i];
+    }
+    block_partials(s0, s1, 0.0, part);
+}
+__global__ void k_lv_axpy2(long long n, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ d,
+                           const float* __restrict__ q, double alpha) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = (float)((double)x[i] + alpha * d[i]);
+    r[i] = (float)((double)r[i] - alpha * q[i]);
+}
+__global__ void k_lv_xpby(long long n, float* __restrict__ d, const float* __restrict__ r, double beta) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) d[i] = (float)((double)r[i] + beta * d[i]);
+}
+
+#define MCK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return e_; } while (0)
+
+}  // namespace
+
+// ---- state -----------------------------------------------------------------------------------------------------
+struct MLLevel {
+    int W = 0, H = 0, D = 0;
+    long long V = 0;
+    uint16_t* info = nullptr;
+    uint8_t* w = nullptr;
+    float* diag = nullptr;
+    float *r = nullptr, *z = nullptr, *t = nullptr;
+};
+
+struct MLState {
+    int nlev = 0;                 // aggregation levels of the allocated hierarchy
+    MLLevel lv[4];                // lv[1..nlev]
+    double* x64 = nullptr;        // FCG vectors (fine grid)
+    float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *q = nullptr, *fb = nullptr;
+    double* part = nullptr;       // 3 * kRedGrid block partials
+    FcgDev* s = nullptr;
+    double* hpart = nullptr;      // pinned: partials of the host-driven level CG
+    cudaStream_t cap1 = nullptr, cap2 = nullptr;   // streams for capturing conditional bodies
+    cudaGraph_t solve_graph = nullptr;
+    cudaGraphExec_t solve_exec = nullptr;          // efs_solve / efs_stage outside a step graph
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+template <typename T>
+cudaError_t malloc_ml(MLState* m, T** p, long long count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), (size_t)std::max(1LL, count) * sizeof(T));
+    if (e == cudaSuccess) m->allocs.push_back(*p);
+    return e;
+}
+
+LvView fine_view(const efs_ctx* c) {
+    return LvView{c->g.W, c->g.H, c->g.D, (long long)c->g.N, c->rowinfo, nullptr, nullptr};
+}
+LvView level_view(const efs_ctx* c, const MLState* m, int l) {
+    if (l == 0) return fine_view(c);
+    const MLLevel& L = m->lv[l];
+    return LvView{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
+}
+
+}  // namespace
+
+int ml_resolve_levels(const efs_ctx* c) {
+    if (c->dim != 3) return 0;
+    int l = c->prm.fcg_levels;
+    if (l >= 0) return std::min(l, 3);
+    int W = c->g.W, H = c->g.H, D = c->g.D;
+    l = 0;
+    while (l < 3 && std::max(W, std::max(H, D)) > 32) {
+        W = (W + 1) / 2; H = (H + 1) / 2; D = (D + 1) / 2;
+        l++;
+    }
+    return l;
+}
+
+void ml_level_dims(const efs_ctx* c, int level, int* W, int* H, int* D) {
+    int w = c->g.W, h = c->g.H, d = c->g.D;
+    for (int k = 0; k < level; k++) { w = (w + 1) / 2; h = (h + 1) / 2; d = (d + 1) / 2; }
+    *W = w; *H = h; *D = d;
+}
+
+void ml_free(efs_ctx* c) {
+    MLState* m = c->ml;
+    if (!m) return;
+    if (m->solve_exec) cudaGraphExecDestroy(m->solve_exec);
+    if (m->solve_graph) cudaGraphDestroy(m->solve_graph);
+    for (void* p : m->allocs) cudaFree(p);
+    if (m->hpart) cudaFreeHost(m->hpart);
+    if (m->cap1) cudaStreamDestroy(m->cap1);
+    if (m->cap2) cudaStreamDestroy(m->cap2);
+    delete m;
+    c->ml = nullptr;
+}
+
+void ml_drop_graph(efs_ctx* c) {
+    MLState* m = c->ml;
+    if (!m) return;
+    if (m->solve_exec) cudaGraphExecDestroy(m->solve_exec);
+    if (m->solve_graph) cudaGraphDestroy(m->solve_graph);
+    m->solve_exec = nullptr;
+    m->solve_graph = nullptr;
+}
+
+// Buffers for the context's current level count (outside any stream capture; kept while the count holds).
+cudaError_t ml_alloc(efs_ctx* c) {
+    const int nlev = ml_resolve_levels(c);
+    if (c->ml && c->ml->nlev == nlev) return cudaSuccess;
+    ml_free(c);
+    MLState* m = new MLState();
+    c->ml = m;
+    m->nlev = nlev;
+    const long long N = c->g.N;
+    MCK(malloc_ml(m, &m->x64, N));
+    MCK(malloc_ml(m, &m->r, N));
+    MCK(malloc_ml(m, &m->z, N));
+    MCK(malloc_ml(m, &m->zt, N));
+    MCK(malloc_ml(m, &m->d, N));
+    MCK(malloc_ml(m, &m->q, N));
+    MCK(malloc_ml(m, &m->fb, N));
+    MCK(malloc_ml(m, &m->part, 3LL * kRedGrid));
+    MCK(malloc_ml(m, &m->s, 1));
+    MCK(cudaMemset(m->s, 0, sizeof(FcgDev)));
+    for (int l = 1; l <= nlev; l++) {
+        MLLevel& L = m->lv[l];
+        ml_level_dims(c, l, &L.W, &L.H, &L.D);
+        L.V = (long long)L.W * L.H * L.D;
+        MCK(malloc_ml(m, &L.info, L.V));
+        MCK(malloc_ml(m, &L.w, 6 * L.V));
+        MCK(malloc_ml(m, &L.diag, L.V));
+        MCK(malloc_ml(m, &L.r, L.V));
+        MCK(malloc_ml(m, &L.z, L.V));
+        MCK(malloc_ml(m, &L.t, L.V));
+    }
+    MCK(cudaMallocHost(reinterpret_cast<void**>(&m->hpart), 3 * kRedGrid * sizeof(double)));
+    MCK(cudaStreamCreateWithFlags(&m->cap1, cudaStreamNonBlocking));
+    MCK(cudaStreamCreateWithFlags(&m->cap2, cudaStreamNonBlocking));
+    return cudaSuccess;
+}
+
+int ml_levels(const efs_ctx* c) { return c->ml ? c->ml->nlev : ml_resolve_levels(c); }
+
+LvView ml_view(const efs_ctx* c, int level) { return level_view(c, c->ml, level); }
+
+// The hierarchy's matrices from the current rowinfo.
+cudaError_t ml_build(efs_ctx* c, cudaStream_t st) {
+    MLState* m = c->ml;
+    for (int l = 1; l <= m->nlev; l++) {
+        const MLLevel& L = m->lv[l];
+        const LvOut out{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
+        if (l == 1) k_ml_build<true><<<blocks_for(L.V), kThreads, 0, st>>>(level_view(c, m, 0), out);
+        else k_ml_build<false><<<blocks_for(L.V), kThreads, 0, st>>>(level_view(c, m, l - 1), out);
+        MCK(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st) {
+    if (!L.w) k_ml_matvec<true><<<blocks_for(L.V), kThreads, 0, st>>>(L, x, y);
+    else k_ml_matvec<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, x, y);
+    return cudaGetLastError();
+}
+
+namespace {
+
+template <bool FINE>
+cudaError_t smooth(const LvView& L, const float* r, const float* zin, float* zout, cudaStream_t st) {
+    k_ml_smooth<FINE><<<blocks_for(L.V), kThreads, 0, st>>>(L, r, zin, zout, kOmega);
+    return cudaGetLastError();
+}
+cudaError_t smooth_any(const LvView& L, const float* r, const float* zin, float* zout, cudaStream_t st) {
+    return L.w ? smooth<false>(L, r, zin, zout, st) : smooth<true>(L, r, zin, zout, st);
+}
+
+// pre-smoothing at level l: z = S(S(0)) with t as the intermediate
+cudaError_t pre_smooth(const LvView& L, const float* r, float* z, float* t, cudaStream_t st) {
+    MCK(smooth_any(L, r, nullptr, t, st));
+    return smooth_any(L, r, t, z, st);
+}
+cudaError_t post_smooth(const LvView& L, const float* r, float* z, float* t, cudaStream_t st) {
+    MCK(smooth_any(L, r, z, t, st));
+    return smooth_any(L, r, t, z, st);
+}
+cudaError_t restrict_to(const LvView& F, const float* r, const float* z, const LvView& Cv, float* rc, cudaStream_t st) {
+    if (!F.w) k_ml_restrict<true><<<blocks_for(Cv.V), kThreads, 0, st>>>(F, r, z, Cv, rc);
+    else k_ml_restrict<false><<<blocks_for(Cv.V), kThreads, 0, st>>>(F, r, z, Cv, rc);
+    return cudaGetLastError();
+}
+cudaError_t prolong_add(const LvView& F, float* z, const float* ec, const LvView& Cv, cudaStream_t st) {
+    if (!F.w) k_ml_prolong<true><<<blocks_for(F.V), kThreads, 0, st>>>(F, z, ec, Cv);
+    else k_ml_prolong<false><<<blocks_for(F.V), kThreads, 0, st>>>(F, z, ec, Cv);
+    return cudaGetLastError();
+}
+
+// The bottom solve: z = the network's correction for r, scaled by the line search on this level (or Jacobi
+// sweeps without the network).
+cudaError_t bottom_solve(efs_ctx* c, const LvView& B, const float* r, float* z, float* t, cudaStream_t st) {
+    MLState* m = c->ml;
+    if (c->prm.fcg_bottom == EFS_FCG_BOTTOM_JACOBI || !c->unet) {
+        float* a = z;
+        float* o = t;
+        MCK(smooth_any(B, r, nullptr, a, st));
+        for (int k = 1; k < kBottomJacobi; k++) {
+            MCK(smooth_any(B, r, a, o, st));
+            std::swap(a, o);
+        }
+        if (a != z) MCK(cudaMemcpyAsync(z, a, B.V * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        return cudaSuccess;
+    }
+    MCK(unet_correction(c, B, r, z, st));
+    const unsigned rb = red_blocks(B.V);
+    if (!B.w) k_ml_ls_dots<true><<<rb, kThreads, 0, st>>>(B, z, r, m->part);
+    else k_ml_ls_dots<false><<<rb, kThreads, 0, st>>>(B, z, r, m->part);
+    MCK(cudaGetLastError());
+    k_ml_ls_finish<<<1, 32, 0, st>>>(m->part, (int)rb, m->s);
+    MCK(cudaGetLastError());
+    k_ml_scale<<<blocks_for(B.V), kThreads, 0, st>>>(B.V, z, m->s);
+    return cudaGetLastError();
+}
+
+// z = M(r) at level l (r, z, t: that level's vectors)
+cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaStream_t st) {
+    MLState* m = c->ml;
+    const LvView L = level_view(c, m, l);
+    if (l == m->nlev) return bottom_solve(c, L, r, z, t, st);
+    const LvView Cv = level_view(c, m, l + 1);
+    MLLevel& N = m->lv[l + 1];
+    MCK(pre_smooth(L, r, z, t, st));
+    MCK(restrict_to(L, r, z, Cv, N.r, st));
+    MCK(vcycle(c, l + 1, N.r, N.z, N.t, st));
+    MCK(prolong_add(L, z, N.z, Cv, st));
+    return post_smooth(L, r, z, t, st);
+}
+
+// a conditional handle on the graph `st` is capturing into
+cudaError_t make_handle(cudaStream_t st, cudaGraphConditionalHandle* h) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    MCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive || !g) return cudaErrorStreamCaptureUnmatched;
+    return cudaGraphConditionalHandleCreate(h, g, 0, 0);
+}
+// a conditional node after `st`'s current capture dependencies; `st` continues after it; *body to be filled
+cudaError_t add_conditional(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                            cudaGraph_t* body) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    MCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    MCK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    *body = p.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// The whole solve on `st`, which is capturing into a graph.
+cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
+    MLState* m = c->ml;
+    const LvView F = fine_view(c);
+    const long long N = F.V;
+    const unsigned rb = red_blocks(N);
+    const int max_it = c->prm.max_steps;
+    MCK(ml_build(c, st));
+    cudaGraphConditionalHandle h_loop, h_verify, h_fb;
+    MCK(make_handle(st, &h_loop));
+    k_fcg_init<<<rb, kThreads, 0, st>>>(F, c->div, m->x64, m->r, m->d, m->q, m->part);
+    MCK(cudaGetLastError());
+    k_fcg_init_finish<<<1, 32, 0, st>>>(m->part, (int)rb, m->s, c->prm.tol_rel, c->prm.solver_threshold, max_it, h_loop);
+    MCK(cudaGetLastError());
+
+    // ---- WHILE: one FCG iteration ----
+    cudaGraph_t body = nullptr;
+    MCK(add_conditional(st, h_loop, cudaGraphCondTypeWhile, &body));
+    {
+        cudaStream_t b = m->cap1;
+        MCK(cudaStreamBeginCaptureToGraph(b, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        do {
+            if ((e = vcycle(c, 0, m->r, m->z, m->zt, b)) != cudaSuccess) break;
+            k_fcg_dots_zq_rz<<<rb, kThreads, 0, b>>>(F, m->z, m->q, m->r, m->part);
+            k_fcg_beta<<<1, 32, 0, b>>>(m->part, (int)rb, m->s);
+            k_fcg_dir<<<blocks_for(N), kThreads, 0, b>>>(N, m->d, m->z, m->s);
+            k_fcg_matvec_dot<<<rb, kThreads, 0, b>>>(F, m->d, m->q, m->part);
+            k_fcg_alpha<<<1, 32, 0, b>>>(m->part, (int)rb, m->s);
+            k_fcg_update<<<rb, kThreads, 0, b>>>(N, m->x64, m->r, m->d, m->q, m->s, m->part);
+            if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
+            k_fcg_check<<<1, 32, 0, b>>>(m->part, (int)rb, m->s, h_verify);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
+            cudaGraph_t vbody = nullptr;
+            if ((e = add_conditional(b, h_verify, cudaGraphCondTypeIf, &vbody)) != cudaSuccess) break;
+            cudaStream_t v = m->cap2;
+            if ((e = cudaStreamBeginCaptureToGraph(v, vbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+            k_fcg_true_resid<<<rb, kThreads, 0, v>>>(F, c->div, m->x64, m->r, m->part);
+            k_fcg_verify<<<1, 32, 0, v>>>(m->part, (int)rb, m->s);
+            cudaError_t ve = cudaGetLastError();
+            cudaGraph_t dummy = nullptr;
+            cudaError_t ee = cudaStreamEndCapture(v, &dummy);
+            if ((e = ve) != cudaSuccess || (e = ee) != cudaSuccess) break;
+            k_fcg_loop<<<1, 32, 0, b>>>(m->s, max_it, h_loop);
+            e = cudaGetLastError();
+        } while (0);
+        cudaGraph_t dummy = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(b, &dummy);
+        MCK(e);
+        MCK(ee);
+    }
+
+    // ---- IF: the plain-CG fallback on the residual system ----
+    MCK(make_handle(st, &h_fb));
+    k_fcg_post<<<1, 32, 0, st>>>(m->s, h_fb);
+    MCK(cudaGetLastError());
+    cudaGraph_t fbody = nullptr;
+    MCK(add_conditional(st, h_fb, cudaGraphCondTypeIf, &fbody));
+    {
+        cudaStream_t b = m->cap1;
+        MCK(cudaStreamBeginCaptureToGraph(b, fbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        do {
+            k_fcg_fb_rhs<<<blocks_for(N), kThreads, 0, b>>>(F, c->div, m->x64, m->fb);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            if ((e = launch_solver_on(c, m->fb, &m->s->thr, b)) != cudaSuccess) break;
+            k_fcg_fb_add<<<blocks_for(N), kThreads, 0, b>>>(F, m->x64, c->p);
+            k_fcg_fb_done<<<1, 32, 0, b>>>(m->s, c->ctl);
+            e = cudaGetLastError();
+        } while (0);
+        cudaGraph_t dummy = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(b, &dummy);
+        MCK(e);
+        MCK(ee);
+    }
+    k_fcg_out<<<blocks_for(N), kThreads, 0, st>>>(F, m->x64, c->p, c->p64);
+    k_fcg_stats<<<1, 32, 0, st>>>(m->s, c->ctl);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t fcg_solve(efs_ctx* c) {
+    if (!c->ml || c->ml->nlev != ml_resolve_levels(c)) return cudaErrorNotReady;   // ml_alloc runs before any capture
+    cudaStreamCaptureStatus cs;
+    MCK(cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) return fcg_enqueue(c, c->stream);
+    MLState* m = c->ml;
+    if (!m->solve_exec) {
+        MCK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = fcg_enqueue(c, c->stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        if (e != cudaSuccess || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return e != cudaSuccess ? e : ee;
+        }
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); return e; }
+        m->solve_graph = g;
+        m->solve_exec = x;
+    }
+    return cudaGraphLaunch(m->solve_exec, c->stream);
+}
+
+// r (fine) carried down the pre-smoothing and restriction chain to the bottom level: out = the bottom residual
+cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out) {
+    MLState* m = c->ml;
+    MCK(ml_build(c, st));
+    const float* r = r0;
+    for (int l = 0; l < m->nlev; l++) {
+        const LvView L = level_view(c, m, l);
+        float* z = (l == 0) ? m->z : m->lv[l].z;
+        float* t = (l == 0) ? m->zt : m->lv[l].t;
+        MCK(pre_smooth(L, r, z, t, st));
+        MCK(restrict_to(L, r, z, level_view(c, m, l + 1), m->lv[l + 1].r, st));
+        r = m->lv[l + 1].r;
+    }
+    *out = r;
+    return cudaSuccess;
+}
+
+// CG on level matrix L (negative definite on its rows) for L e = r from e = 0, to ||r|| <= tol ||r0||, host-driven
+// (training samples only).  t1, t2, t3: scratch vectors of L.V floats.  Returns the iterations, or -1.
+int ml_level_cg(efs_ctx* c, const LvView& L, const float* r0, float* e, float* t1, float* t2, float* t3, double tol,
+                int maxit, cudaStream_t st) {
+    MLState* m = c->ml;
+    const long long n = L.V;
+    const unsigned rb = red_blocks(n), nb = blocks_for(n);
+    float *r = t1, *d = t2, *q = t3;
+    auto dot2 = [&](const float* a0, const float* b0, const float* a1, const float* b1, double& s0, double& s1) -> bool {
+        k_lv_dot3<<<rb, kThreads, 0, st>>>(n, a0, b0, a1, b1, m->part);
+        if (cudaMemcpyAsync(m->hpart, m->part, 3 * rb * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+        s0 = s1 = 0;
+        for (unsigned k = 0; k < rb; k++) { s0 += m->hpart[3 * k]; s1 += m->hpart[3 * k + 1]; }
+        return true;
+    };
+    if (cudaMemsetAsync(e, 0, n * sizeof(float), st) != cudaSuccess) return -1;
+    if (cudaMemcpyAsync(r, r0, n * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return -1;
+    if (cudaMemcpyAsync(d, r0, n * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return -1;
+    double rr, unused;
+    if (!dot2(r, r, nullptr, nullptr, rr, unused)) return -1;
+    const double thr = tol * tol * rr;
+    int it = 0;
+    while (it < maxit && rr > thr && rr > 0) {
+        if (ml_matvec(L, d, q, st) != cudaSuccess) return -1;
+        double dq;
+        if (!dot2(d, q, nullptr, nullptr, dq, unused)) return -1;
+        if (!(dq != 0.0)) break;
+        const double a = rr / dq;
+        k_lv_axpy2<<<nb, kThreads, 0, st>>>(n, e, r, d, q, a);
+        double rn;
+        if (!dot2(r, r, nullptr, nullptr, rn, unused)) return -1;
+        k_lv_xpby<<<nb, kThreads, 0, st>>>(n, d, r, rn / rr);
+        rr = rn;
+        it++;
+    }
+    return it;
+}
+
+}  // namespace efs

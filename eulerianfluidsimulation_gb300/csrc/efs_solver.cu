@@ -992,7 +992,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         if (!red.run(ctl, rr_p, bb_p, rows, rr, bb, nrows)) return;
     }
     float thr_f;
-    if (a.tol_rel > 0) {
+    if (a.thr_dev) {
+        thr_f = (float)*a.thr_dev;
+    } else if (a.tol_rel > 0) {
         thr_f = (float)((double)a.tol_rel * (double)a.tol_rel * bb);
         if (!(thr_f > 0)) thr_f = FLT_MIN;
     } else {
@@ -1234,9 +1236,9 @@ cudaError_t solver_configure(efs_ctx* c) {
     return solver_shape(n_chunks, c->sm_count, &c->solver_blocks, &c->solver_smem);
 }
 
-cudaError_t launch_solver(efs_ctx* c) {
-    if (c->prm.solver == EFS_SOLVER_FCG_UNET) return fcg_solve(c);
-    SolverArgs a;
+namespace {
+SolverArgs context_solver_args(efs_ctx* c) {
+    SolverArgs a{};
     a.g = c->g;
     a.dim = c->dim;
     a.solver = c->prm.solver;
@@ -1262,20 +1264,40 @@ cudaError_t launch_solver(efs_ctx* c) {
     a.t64 = c->t64;
     a.partials = c->partials;
     a.ctl = c->ctl;
+    a.thr_dev = nullptr;
+    return a;
+}
+
+cudaError_t launch_context_solver(efs_ctx* c, const SolverArgs& a, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c->solver_blocks);
     cfg.blockDim = dim3(SOLVER_THREADS);
     cfg.dynamicSmemBytes = c->solver_smem;
-    cfg.stream = c->stream;
+    cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     // a fresh barrier for this launch (a previous launch may have aborted mid-barrier)
-    cudaError_t e = cudaMemsetAsync(c->ctl, 0, 2 * sizeof(int), c->stream);
+    cudaError_t e = cudaMemsetAsync(c->ctl, 0, 2 * sizeof(int), st);
     if (e != cudaSuccess) return e;
     return cudaLaunchKernelEx(&cfg, a.cg_variant == EFS_CG_FP64 && a.solver == EFS_SOLVER_CG ? k_solver_fp64 : k_solver, a);
+}
+}  // namespace
+
+cudaError_t launch_solver(efs_ctx* c) {
+    if (c->prm.solver == EFS_SOLVER_FCG_UNET) return fcg_solve(c);
+    return launch_context_solver(c, context_solver_args(c), c->stream);
+}
+
+cudaError_t launch_solver_on(efs_ctx* c, const float* b, const double* thr_dev, cudaStream_t st) {
+    SolverArgs a = context_solver_args(c);
+    a.solver = EFS_SOLVER_CG;
+    a.cg_variant = EFS_CG_MIXED_RECURRENCE;
+    a.b = b;
+    a.thr_dev = thr_dev;
+    return launch_context_solver(c, a, st);
 }
 
 // Launch shape of the solver for a grid of n_chunks 32-cell chunks (the same rule as solver_configure),

@@ -1,13 +1,17 @@
 // efs_unet.cu — the learned preconditioner: a 3-level 3D convolutional U-Net (16/32/64 channels, BF16
-// weights and activations, FP32 accumulation in tensor memory), its training on the GPU with the project's
-// own forward and backward kernels, and flexible preconditioned CG (FCG) with plain CG as the fallback.
+// weights and activations, FP32 accumulation in tensor memory) and its training on the GPU with the
+// project's own forward and backward kernels.  FCG applies it as the coarsest-level solve of its multilevel
+// preconditioner (efs_mlfcg.cu).
 //
 // No counterpart in the reference (its solvers are CGSolverCPU3D / JacobiSolverCPU3D,
-// src/simulation/solver/CGSolver.cpp:416-497, JacobiSolver.cpp:154-212); FCG solves the same matrix
-// L p = b as those (rows: liquid, non-solid cells; see k_solver_prep) to the same stop rule.
+// src/simulation/solver/CGSolver.cpp:416-497, JacobiSolver.cpp:154-212).
 //
-// Network (all convolutions 3x3x3, zero padding; level l has the grid dimensions halved l times, rounded up):
-//   x0  = [r / rms(r), row mask, 0 x 14]                   level 0, 16 channels (BF16)
+// The network works on one level of FCG's hierarchy (the bottom one; level 0 is the pressure matrix's own
+// grid).  Network (all convolutions 3x3x3, zero padding; network level k has that grid's dimensions halved k
+// times, rounded up):
+//   x0  = [r / rms(r), row mask, geometry, 0...]          network level 0, 16 channels (BF16); geometry (only
+//                                                        above hierarchy level 0): -diag / (6 4^l) and the six
+//                                                        face weights / 4^l of the level-l matrix
 //   e0  = relu(conv0(x0))            16 -> 16              level 0
 //   e1  = relu(conv1(pool(e0)))      16 -> 32              level 1 (pool: 2x2x2 mean)
 //   e2  = relu(conv2(pool(e1)))      32 -> 64              level 2
@@ -53,6 +57,7 @@ struct Level {
 }  // namespace
 
 struct UNetState {
+    int level = 0;               // hierarchy level the network works on (0: the context's grid)
     Level L[3];
     long long woff[kLayers], boff[kLayers], nparam = 0;
     float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
@@ -74,17 +79,17 @@ struct UNetState {
     double* dpart = nullptr;     // block partials
     double* dloss = nullptr;     // [0] loss
     int* err = nullptr;
-    // training set: (b, p, rowinfo) per sample
+    // training set per sample: input r, its exact correction e (A e = r), row info and, above level 0, the
+    // level's matrix (face weights, diagonal)
     int cap = 0, count = 0, next = 0;
     float *sb = nullptr, *sp = nullptr;
     uint16_t* srow = nullptr;
+    uint8_t* sw = nullptr;
+    float* sdiag = nullptr;
     float* tmp_in = nullptr;     // one scalar field: input staging
     float* tmp_t = nullptr;
     float *tz = nullptr, *tq = nullptr;   // training: z = net output and L z (energy loss)
-    // FCG vectors
-    double* x64 = nullptr;
-    float *fr = nullptr, *fz = nullptr, *fd = nullptr, *fq = nullptr;
-    double* hdots = nullptr;     // pinned host copy of the dot products
+    float *c1 = nullptr, *c2 = nullptr, *c3 = nullptr;   // bottom-level CG vectors (training samples)
     std::vector<void*> allocs;
 };
 
@@ -133,9 +138,11 @@ __global__ void k_finish_scale(const double* __restrict__ part, int nb, double* 
     }
 }
 
-// x0[v] = [r * inv, mask, 0...] on rows, 0 elsewhere
+// x0[v] = [r * inv, mask, geometry, 0...] on rows, 0 elsewhere; geometry (gw non-null: a level above 0) is
+// -diag * gnorm / 6 and the six face weights * gnorm, gnorm = 4^-level
 __global__ void k_pack(const float* __restrict__ r, const uint16_t* __restrict__ rowinfo, const double* __restrict__ scal,
-                       long long n, bf16* __restrict__ x0) {
+                       long long n, bf16* __restrict__ x0, const uint8_t* __restrict__ gw, const float* __restrict__ gdiag,
+                       float gnorm) {
     const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (v >= n) return;
     const bool row = rowinfo[v] & 0x8000u;
@@ -145,6 +152,11 @@ __global__ void k_pack(const float* __restrict__ r, const uint16_t* __restrict__
     if (row) {
         o[0] = __float2bfloat16((float)((double)r[v] * scal[2]));
         o[1] = __float2bfloat16(1.f);
+        if (gw) {
+            o[2] = __float2bfloat16(-gdiag[v] * gnorm * (1.f / 6.f));
+#pragma unroll
+            for (int k = 0; k < 6; k++) o[3 + k] = __float2bfloat16((float)gw[k * n + v] * gnorm);
+        }
     }
     uint4* dst = reinterpret_cast<uint4*>(x0 + v * 16);
     dst[0] = reinterpret_cast<const uint4*>(o)[0];
@@ -416,36 +428,6 @@ __global__ void k_unpack(const float* __restrict__ y32, const uint16_t* __restri
     z[v] = (rowinfo[v] & 0x8000u) ? y32[v] : 0.f;
 }
 
-// ---- FCG kernels (matrix of k_solver_prep: rowinfo bits x-1, x+1, y-1, y+1, z-1, z+1) -------------------------
-struct Off6 {
-    long long o[6];
-};
-__device__ __forceinline__ int fcg_bit(int k) { return (k == 4) ? 5 : (k == 5 ? 4 : k); }   // order x-1,x+1,y-1,y+1,z+1,z-1
-__global__ void k_fcg_matvec(const float* __restrict__ d, const uint16_t* __restrict__ rowinfo, long long n, Off6 off,
-                             float* __restrict__ q) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint16_t f = rowinfo[i];
-    if (!(f & 0x8000u)) { q[i] = 0.f; return; }
-    float s = 0.f;
-#pragma unroll
-    for (int k = 0; k < 6; k++)
-        if (f & (1u << fcg_bit(k))) s += d[i + off.o[fcg_bit(k)]];
-    q[i] = s - (float)((f >> 8) & 7) * d[i];
-}
-// r = b - L x in FP64, rounded to FP32 (rows), 0 elsewhere
-__global__ void k_fcg_resid(const float* __restrict__ b, const double* __restrict__ x, const uint16_t* __restrict__ rowinfo,
-                            long long n, Off6 off, float* __restrict__ r) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint16_t f = rowinfo[i];
-    if (!(f & 0x8000u)) { r[i] = 0.f; return; }
-    double s = 0.0;
-#pragma unroll
-    for (int k = 0; k < 6; k++)
-        if (f & (1u << fcg_bit(k))) s += x[i + off.o[fcg_bit(k)]];
-    r[i] = (float)((double)b[i] - (s - (double)((f >> 8) & 7) * x[i]));
-}
 // three dot products at once (pairs (a0,b0), (a1,b1), (a2,b2); null pairs give 0) -> block partials
 __global__ void k_dots3(const float* a0, const float* b0, const float* a1, const float* b1, const float* a2, const float* b2,
                         long long n, double* __restrict__ part) {
@@ -492,57 +474,6 @@ __global__ void k_dots3_finish(const double* __restrict__ part, int nb, double* 
     }
     if (threadIdx.x == 0) { out[0] = sh[0][0]; out[1] = sh[1][0]; out[2] = sh[2][0]; }
 }
-__global__ void k_fcg_xr(double* __restrict__ x, float* __restrict__ r, const float* __restrict__ d, const float* __restrict__ q,
-                         long long n, double alpha) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    x[i] += alpha * (double)d[i];
-    r[i] = (float)((double)r[i] - alpha * (double)q[i]);
-}
-__global__ void k_fcg_dir(float* __restrict__ d, const float* __restrict__ z, long long n, double beta) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    d[i] = (float)((double)z[i] + beta * (double)d[i]);
-}
-__global__ void k_fcg_init(const float* __restrict__ b, const uint16_t* __restrict__ rowinfo, long long n, double* __restrict__ x) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    x[i] = 0.0;   // FCG starts from 0: its first residual is b, the kind of field the network was trained on
-}
-__global__ void k_fcg_out(const double* __restrict__ x, const uint16_t* __restrict__ rowinfo, long long n, float* __restrict__ p,
-                          double* __restrict__ p64) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (rowinfo[i] & 0x8000u) {
-        p[i] = (float)x[i];
-        p64[i] = x[i];
-    }
-}
-// statistics of an FCG solve; after a CG fallback (cg = 1) the CG launch has already counted the solve, its
-// iterations and its convergence, which are folded in here
-__global__ void k_fcg_stats(DevCtl* ctl, int conv, int iters, double rr, double bb, double thr, double rows, int cg) {
-    ctl->precond_iterations = iters;
-    if (cg) {
-        ctl->iterations += iters;
-        ctl->bb = bb;
-    } else {
-        ctl->converged = conv;
-        ctl->iterations = iters;
-        ctl->rr = rr;
-        ctl->bb = bb;
-        ctl->thr = thr;
-        ctl->active_cells = (long long)rows;
-        ctl->solves += 1;
-        ctl->sum_rows += rows;
-    }
-    ctl->total_iterations += iters;
-    ctl->sum_iter_rows += (double)iters * rows;
-}
-__global__ void k_add_rows(double* __restrict__ x, const float* __restrict__ e, const uint16_t* __restrict__ rowinfo, long long n) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n && (rowinfo[i] & 0x8000u)) x[i] += (double)e[i];
-}
-
 // ---- host helpers -------------------------------------------------------------------------------------------
 inline unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
@@ -553,17 +484,14 @@ cudaError_t ualloc(UNetState* u, T** p, long long count) {
     return e;
 }
 
-Level level_of(const efs_ctx* c, int l) {
+// network level l of a network on hierarchy level `base` (grid sides halved base + l times, rounded up)
+Level level_of(const efs_ctx* c, int base, int l) {
     Level L{c->g.D, c->g.H, c->g.W, 0};
-    for (int k = 0; k < l; k++) L = Level{(L.D + 1) / 2, (L.H + 1) / 2, (L.W + 1) / 2, 0};
+    for (int k = 0; k < base + l; k++) L = Level{(L.D + 1) / 2, (L.H + 1) / 2, (L.W + 1) / 2, 0};
     L.V = (long long)L.D * L.H * L.W;
     return L;
 }
 
-Off6 offsets(const efs_ctx* c) {
-    const long long W = c->g.W, WH = (long long)c->g.W * c->g.H;
-    return Off6{{-1, 1, -W, W, c->dim == 3 ? -WH : 0, c->dim == 3 ? WH : 0}};
-}
 
 // cuTensorMapEncodeTiled from the driver, through the runtime (no link against the driver library).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -682,13 +610,15 @@ cudaError_t scale_rows(UNetState* u, const float* x, const uint16_t* rowinfo, lo
 
 // forward pass on the input field `r` (FP32, reference layout) with matrix rows `rowinfo`; y32 holds the output.
 // train: keep the pre-activations for the backward pass.
-cudaError_t forward(UNetState* u, const float* r, const uint16_t* rowinfo, bool train, cudaStream_t st,
+cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, cudaStream_t st,
                     cudaEvent_t* ev = nullptr) {
     const Level *L = u->L;
+    const uint16_t* rowinfo = M.info;
     // ev (optional): 12 events recorded before and after each of the six convolutions
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
-    k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0);
+    k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0, M.w, M.diag,
+                                          1.f / (float)(1 << (2 * u->level)));
     UCK(cudaGetLastError());
     const float* B[kLayers];
     for (int k = 0; k < kLayers; k++) B[k] = u->w32 + u->boff[k];
@@ -724,8 +654,9 @@ cudaError_t forward(UNetState* u, const float* r, const uint16_t* rowinfo, bool 
 // The training losses (kind 0: mean squared error against the target field p normalised by its rms over
 // rows; kind 1: energy-norm alignment with the error p for input r, see k_energy_grad) and the gradients of
 // every parameter, accumulated into u->grad.  Requires a forward(train = true) on input r just before.
-cudaError_t backward(UNetState* u, const float* r, const float* p, const uint16_t* rowinfo, int kind, Off6 off,
-                     int sm_count, cudaStream_t st) {
+cudaError_t backward(UNetState* u, const float* r, const float* p, const LvView& M, int kind, int sm_count,
+                     cudaStream_t st) {
+    const uint16_t* rowinfo = M.info;
     const Level* L = u->L;
     float* G = u->grad;
     const unsigned nb = nblk(L[0].V);
@@ -738,8 +669,7 @@ cudaError_t backward(UNetState* u, const float* r, const float* p, const uint16_
     } else {
         k_unpack<<<nb, 256, 0, st>>>(u->y32, rowinfo, L[0].V, u->tz);
         UCK(cudaGetLastError());
-        k_fcg_matvec<<<nb, 256, 0, st>>>(u->tz, rowinfo, L[0].V, off, u->tq);
-        UCK(cudaGetLastError());
+        UCK(ml_matvec(M, u->tz, u->tq, st));
         k_dots3<<<kRedBlocks, 256, 0, st>>>(u->tz, r, u->tz, u->tq, p, r, L[0].V, u->dpart);
         UCK(cudaGetLastError());
         k_dots3_finish<<<1, 256, 0, st>>>(u->dpart, kRedBlocks, u->dscal + 8);
@@ -835,7 +765,8 @@ cudaError_t alloc_train(UNetState* u) {
 cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
     UNetState* u = new UNetState();
     *out = u;
-    for (int l = 0; l < 3; l++) u->L[l] = level_of(c, l);
+    u->level = ml_resolve_levels(c);
+    for (int l = 0; l < 3; l++) u->L[l] = level_of(c, u->level, l);
     long long off = 0;
     for (int k = 0; k < kLayers; k++) {
         u->woff[k] = off;
@@ -891,136 +822,38 @@ int ucuda(efs_ctx* c, cudaError_t e, const char* what) {
 }
 #define ACK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return efs::ucuda(c, e_, what); } while (0)
 
-// One dot-product round: up to three pairs, result in u->hdots[0..2] (host, after a synchronisation).
-cudaError_t dots3(efs_ctx* c, UNetState* u, const float* a0, const float* b0, const float* a1, const float* b1,
-                  const float* a2, const float* b2) {
-    const long long n = c->g.N;
-    k_dots3<<<kRedBlocks, 256, 0, c->stream>>>(a0, b0, a1, b1, a2, b2, n, u->dpart);
-    UCK(cudaGetLastError());
-    k_dots3_finish<<<1, 256, 0, c->stream>>>(u->dpart, kRedBlocks, u->dscal + 8);
-    UCK(cudaGetLastError());
-    UCK(cudaMemcpyAsync(u->hdots, u->dscal + 8, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    return cudaStreamSynchronize(c->stream);
-}
-
 }  // namespace
 
 void unet_free(efs_ctx* c) {
     if (!c || !c->unet) return;
     for (void* p : c->unet->allocs) cudaFree(p);
-    if (c->unet->hdots) cudaFreeHost(c->unet->hdots);
     delete c->unet;
     c->unet = nullptr;
 }
 
-// Flexible preconditioned CG (Notay's FCG with truncation 1: beta = -(z'.q) / (d.q)) on the matrix of the
-// current rowinfo, from p0 = 0 (the CG solvers start from b), to the stop rule of the CG solvers
-// (r.r < tol_rel^2 b.b, or the absolute threshold), with x in FP64 and the true residual recomputed in FP64
-// every 32 iterations and before stopping.  Plain CG is the fallback: when the residual norm has not halved
-// over 10 iterations, or d.Ld is not negative (L is negative definite on the rows), the rest of the solve is
-// handed to the
-// persistent CG kernel (EFS_CG_MIXED_RECURRENCE) on the residual system L e = r with the same absolute
-// threshold, and x += e.
-cudaError_t fcg_solve(efs_ctx* c) {
+// The network's correction for residual r on the bottom level B: z = net(r) on B's rows, 0 elsewhere.
+cudaError_t unet_correction(efs_ctx* c, const LvView& B, const float* r, float* z, cudaStream_t st) {
     UNetState* u = c->unet;
-    if (!u) return cudaErrorInvalidValue;
-    const long long n = c->g.N;
-    if (!u->x64) {
-        UCK(ualloc(u, &u->x64, n));
-        UCK(ualloc(u, &u->fr, n));
-        UCK(ualloc(u, &u->fz, n));
-        UCK(ualloc(u, &u->fd, n));
-        UCK(ualloc(u, &u->fq, n));
-        UCK(cudaMallocHost(reinterpret_cast<void**>(&u->hdots), 4 * sizeof(double)));
+    if (!u || u->L[0].V != B.V) return cudaErrorInvalidValue;
+    UCK(forward(u, r, B, false, st));
+    k_unpack<<<nblk(B.V), 256, 0, st>>>(u->y32, B.info, B.V, z);
+    return cudaGetLastError();
+}
+
+bool unet_matches(const efs_ctx* c) { return c->unet && c->unet->level == ml_resolve_levels(c); }
+
+// The matrix the network works on: the context's grid (level 0) or the FCG hierarchy's bottom level, built
+// from the current rowinfo (launch_solver_prep first).
+cudaError_t net_matrix(efs_ctx* c, LvView* M) {
+    UNetState* u = c->unet;
+    if (u->level == 0) {
+        *M = ml_view(c, 0);
+        return cudaSuccess;
     }
-    cudaStream_t st = c->stream;
-    const Off6 off = offsets(c);
-    const unsigned nb = nblk(n);
-    const uint16_t* R = c->rowinfo;
-    k_fcg_init<<<nb, 256, 0, st>>>(c->div, R, n, u->x64);
-    UCK(cudaGetLastError());
-    k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
-    UCK(cudaGetLastError());
-    UCK(dots3(c, u, u->fr, u->fr, c->div, c->div, nullptr, nullptr));
-    double rr = u->hdots[0];
-    const double bb = u->hdots[1];
-    UCK(scale_rows(u, c->div, R, n, u->dscal, st));
-    double hs[2];
-    UCK(cudaMemcpyAsync(hs, u->dscal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    UCK(cudaStreamSynchronize(st));
-    const double rows = hs[1];
-    double thr = c->prm.tol_rel > 0 ? (double)(float)((double)c->prm.tol_rel * c->prm.tol_rel * bb)
-                                    : (double)c->prm.solver_threshold;
-    int conv = rr < thr, it = 0;
-    bool fallback = false;
-    if (!conv) {
-        UCK(forward(u, u->fr, R, false, st));
-        k_unpack<<<nb, 256, 0, st>>>(u->y32, R, n, u->fz);
-        UCK(cudaGetLastError());
-        UCK(cudaMemcpyAsync(u->fd, u->fz, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        UCK(dots3(c, u, u->fr, u->fz, nullptr, nullptr, nullptr, nullptr));
-        double rz = u->hdots[0];
-        double rr_window = rr;
-        for (it = 0; it < c->prm.max_steps; it++) {
-            k_fcg_matvec<<<nb, 256, 0, st>>>(u->fd, R, n, off, u->fq);
-            UCK(cudaGetLastError());
-            UCK(dots3(c, u, u->fd, u->fq, nullptr, nullptr, nullptr, nullptr));
-            const double dq = u->hdots[0];
-            // d.Ld < 0 for any direction on the rows; the sign of r.z does not matter (alpha follows it)
-            if (!(dq < 0.0) || !std::isfinite(rz / dq)) { fallback = true; break; }
-            const double alpha = rz / dq;
-            k_fcg_xr<<<nb, 256, 0, st>>>(u->x64, u->fr, u->fd, u->fq, n, alpha);
-            UCK(cudaGetLastError());
-            if (((it + 1) & 31) == 0) {
-                k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
-                UCK(cudaGetLastError());
-            }
-            UCK(dots3(c, u, u->fr, u->fr, nullptr, nullptr, nullptr, nullptr));
-            rr = u->hdots[0];
-            if (rr < thr) {
-                k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
-                UCK(cudaGetLastError());
-                UCK(dots3(c, u, u->fr, u->fr, nullptr, nullptr, nullptr, nullptr));
-                rr = u->hdots[0];
-                if (rr < thr) { conv = 1; it++; break; }
-            }
-            if (((it + 1) % 10) == 0) {
-                if (rr > 0.5 * rr_window) { fallback = true; it++; break; }
-                rr_window = rr;
-            }
-            UCK(forward(u, u->fr, R, false, st));
-            k_unpack<<<nb, 256, 0, st>>>(u->y32, R, n, u->fz);
-            UCK(cudaGetLastError());
-            UCK(dots3(c, u, u->fz, u->fq, u->fr, u->fz, nullptr, nullptr));
-            const double beta = -u->hdots[0] / dq;
-            rz = u->hdots[1];
-            k_fcg_dir<<<nb, 256, 0, st>>>(u->fd, u->fz, n, beta);
-            UCK(cudaGetLastError());
-        }
-    }
-    if (fallback) {
-        // plain CG on L e = r (true residual of x), absolute threshold thr; then x += e
-        k_fcg_resid<<<nb, 256, 0, st>>>(c->div, u->x64, R, n, off, u->fr);
-        UCK(cudaGetLastError());
-        UCK(cudaMemcpyAsync(u->tmp_t, c->div, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        UCK(cudaMemcpyAsync(c->div, u->fr, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        const efs_params saved = c->prm;
-        c->prm.solver = EFS_SOLVER_CG;
-        c->prm.cg_variant = EFS_CG_MIXED_RECURRENCE;
-        c->prm.tol_rel = 0.f;
-        c->prm.solver_threshold = (float)thr;
-        c->prm.max_steps = std::max(0, saved.max_steps - it);
-        cudaError_t e = launch_solver(c);
-        c->prm = saved;
-        UCK(e);
-        k_add_rows<<<nb, 256, 0, st>>>(u->x64, c->p, R, n);
-        UCK(cudaGetLastError());
-        UCK(cudaMemcpyAsync(c->div, u->tmp_t, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    }
-    k_fcg_out<<<nb, 256, 0, st>>>(u->x64, R, n, c->p, c->p64);
-    UCK(cudaGetLastError());
-    k_fcg_stats<<<1, 1, 0, st>>>(c->ctl, conv, it, rr, bb, thr, rows, fallback ? 1 : 0);
-    UCK(cudaGetLastError());
+    if (ml_resolve_levels(c) != u->level) return cudaErrorInvalidValue;
+    UCK(ml_alloc(c));
+    UCK(ml_build(c, c->stream));
+    *M = ml_view(c, u->level);
     return cudaSuccess;
 }
 
@@ -1041,6 +874,7 @@ int efs_unet_init(efs_ctx* c, uint64_t seed, int sample_capacity) {
     if (c->dim != 3) return efs::ufail(c, EFS_ERR_ARG, "the U-Net preconditioner is 3D only");
     if (sample_capacity < 0) return efs::ufail(c, EFS_ERR_ARG, "sample_capacity < 0");
     ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    efs::drop_all_graphs(c);      // captured solves address the old network's buffers
     efs::unet_free(c);
     UNetState* u = nullptr;
     cudaError_t e = efs::alloc_net(c, &u);
@@ -1055,10 +889,14 @@ int efs_unet_init(efs_ctx* c, uint64_t seed, int sample_capacity) {
     }
     ACK(efs::refresh_bf16(u, c->stream), "U-Net weights");
     if (sample_capacity > 0) {
-        const long long N = c->g.N;
-        ACK(efs::ualloc(u, &u->sb, N * sample_capacity), "sample buffer");
-        ACK(efs::ualloc(u, &u->sp, N * sample_capacity), "sample buffer");
-        ACK(efs::ualloc(u, &u->srow, N * sample_capacity), "sample buffer");
+        const long long V = u->L[0].V;
+        ACK(efs::ualloc(u, &u->sb, V * sample_capacity), "sample buffer");
+        ACK(efs::ualloc(u, &u->sp, V * sample_capacity), "sample buffer");
+        ACK(efs::ualloc(u, &u->srow, V * sample_capacity), "sample buffer");
+        if (u->level > 0) {
+            ACK(efs::ualloc(u, &u->sw, 6 * V * sample_capacity), "sample buffer");
+            ACK(efs::ualloc(u, &u->sdiag, V * sample_capacity), "sample buffer");
+        }
         u->cap = sample_capacity;
     }
     ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
@@ -1096,11 +934,13 @@ int efs_unet_apply(efs_ctx* c, const float* r_host, float* z_host) {
     UNetState* u = c->unet;
     if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
     if (!r_host || !z_host) return efs::ufail(c, EFS_ERR_ARG, "NULL field");
-    const long long N = c->g.N;
+    const long long N = u->L[0].V;
     ACK(efs::launch_solver_prep(c), "solver prep");
+    efs::LvView M;
+    ACK(efs::net_matrix(c, &M), "hierarchy (efs_unet_init again after changing fcg_levels)");
     ACK(cudaMemcpyAsync(u->tmp_in, r_host, N * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload");
-    ACK(efs::forward(u, u->tmp_in, c->rowinfo, false, c->stream), "U-Net forward");
-    efs::k_unpack<<<efs::nblk(N), 256, 0, c->stream>>>(u->y32, c->rowinfo, N, u->tmp_t);
+    ACK(efs::forward(u, u->tmp_in, M, false, c->stream), "U-Net forward");
+    efs::k_unpack<<<efs::nblk(N), 256, 0, c->stream>>>(u->y32, M.info, N, u->tmp_t);
     ACK(cudaGetLastError(), "unpack");
     ACK(cudaMemcpyAsync(z_host, u->tmp_t, N * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "download");
     ACK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
@@ -1113,16 +953,18 @@ int efs_unet_loss_grad(efs_ctx* c, int loss_kind, const float* b_host, const flo
     if (!u) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
     if (!b_host || !p_host) return efs::ufail(c, EFS_ERR_ARG, "NULL field");
     if (loss_kind != 0 && loss_kind != 1) return efs::ufail(c, EFS_ERR_ARG, "loss_kind: 0 (pressure MSE) or 1 (energy)");
-    const long long N = c->g.N;
+    const long long N = u->L[0].V;
     cudaStream_t st = c->stream;
     ACK(efs::alloc_train(u), "U-Net training buffers");
     ACK(efs::launch_solver_prep(c), "solver prep");
+    efs::LvView M;
+    ACK(efs::net_matrix(c, &M), "hierarchy (efs_unet_init again after changing fcg_levels)");
     ACK(cudaMemcpyAsync(u->tmp_in, b_host, N * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
     ACK(cudaMemcpyAsync(u->tmp_t, p_host, N * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
     ACK(cudaMemsetAsync(u->grad, 0, u->nparam * sizeof(float), st), "memset");
     ACK(cudaMemsetAsync(u->dloss, 0, sizeof(double), st), "memset");
-    ACK(efs::forward(u, u->tmp_in, c->rowinfo, true, st), "U-Net forward");
-    ACK(efs::backward(u, u->tmp_in, u->tmp_t, c->rowinfo, loss_kind, efs::offsets(c), c->sm_count, st), "U-Net backward");
+    ACK(efs::forward(u, u->tmp_in, M, true, st), "U-Net forward");
+    ACK(efs::backward(u, u->tmp_in, u->tmp_t, M, loss_kind, c->sm_count, st), "U-Net backward");
     double l = 0;
     ACK(cudaMemcpyAsync(&l, u->dloss, sizeof(double), cudaMemcpyDeviceToHost, st), "download");
     if (grads_host) ACK(cudaMemcpyAsync(grads_host, u->grad, u->nparam * sizeof(float), cudaMemcpyDeviceToHost, st), "download");
@@ -1142,13 +984,18 @@ int efs_unet_time_forward(efs_ctx* c, int reps, float* ms_forward, float* ms_lay
     ACK(cudaEventCreate(&e0), "cudaEventCreate");
     ACK(cudaEventCreate(&e1), "cudaEventCreate");
     ACK(efs::launch_solver_prep(c), "solver prep");
-    ACK(efs::forward(u, c->div, c->rowinfo, false, st), "U-Net forward");   // warm-up
+    efs::LvView M;
+    ACK(efs::net_matrix(c, &M), "hierarchy (efs_unet_init again after changing fcg_levels)");
+    // the input: the divergence itself, or carried down to the network's level as the V-cycle carries it
+    const float* in = c->div;
+    if (u->level > 0) ACK(efs::ml_descend(c, c->div, st, &in), "descend");
+    ACK(efs::forward(u, in, M, false, st), "U-Net forward");   // warm-up
     double lay[6] = {0, 0, 0, 0, 0, 0};
     float total = 0.f;
     cudaError_t err = cudaSuccess;
     for (int k = 0; k < reps && err == cudaSuccess; k++) {
         cudaEventRecord(e0, st);
-        err = efs::forward(u, c->div, c->rowinfo, false, st, ev);
+        err = efs::forward(u, in, M, false, st, ev);
         cudaEventRecord(e1, st);
         if (err == cudaSuccess) err = cudaEventSynchronize(e1);
         float ms = 0.f;
@@ -1173,14 +1020,47 @@ int efs_unet_add_sample(efs_ctx* c) {
     if (!c) return EFS_ERR_ARG;
     UNetState* u = c->unet;
     if (!u || u->cap == 0) return efs::ufail(c, EFS_ERR_STATE, "no sample buffer: efs_unet_init with sample_capacity > 0");
-    const long long N = c->g.N;
+    const long long V = u->L[0].V;
     const int slot = u->next;
-    ACK(cudaMemcpyAsync(u->sb + (size_t)slot * N, c->div, N * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "sample");
-    ACK(cudaMemcpyAsync(u->sp + (size_t)slot * N, c->p, N * sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "sample");
-    ACK(cudaMemcpyAsync(u->srow + (size_t)slot * N, c->rowinfo, N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, c->stream),
-        "sample");
+    cudaStream_t st = c->stream;
+    if (u->level == 0) {
+        ACK(cudaMemcpyAsync(u->sb + (size_t)slot * V, c->div, V * sizeof(float), cudaMemcpyDeviceToDevice, st), "sample");
+        ACK(cudaMemcpyAsync(u->sp + (size_t)slot * V, c->p, V * sizeof(float), cudaMemcpyDeviceToDevice, st), "sample");
+        ACK(cudaMemcpyAsync(u->srow + (size_t)slot * V, c->rowinfo, V * sizeof(uint16_t), cudaMemcpyDeviceToDevice, st),
+            "sample");
+    } else {
+        // the divergence as the first V-cycle carries it to the network's level, and its exact correction there
+        efs::LvView M;
+        ACK(efs::launch_solver_prep(c), "solver prep");
+        ACK(efs::net_matrix(c, &M), "hierarchy (efs_unet_init again after changing fcg_levels)");
+        const float* rb = nullptr;
+        ACK(efs::ml_descend(c, c->div, st, &rb), "descend");
+        if (!u->c1) {
+            ACK(efs::ualloc(u, &u->c1, V), "sample CG");
+            ACK(efs::ualloc(u, &u->c2, V), "sample CG");
+            ACK(efs::ualloc(u, &u->c3, V), "sample CG");
+        }
+        float* sb = u->sb + (size_t)slot * V;
+        float* sp = u->sp + (size_t)slot * V;
+        ACK(cudaMemcpyAsync(sb, rb, V * sizeof(float), cudaMemcpyDeviceToDevice, st), "sample");
+        if (efs::ml_level_cg(c, M, sb, sp, u->c1, u->c2, u->c3, 1e-8, 20000, st) < 0)
+            return efs::ufail(c, EFS_ERR_CUDA, "bottom-level CG of a training sample failed");
+        ACK(cudaMemcpyAsync(u->srow + (size_t)slot * V, M.info, V * sizeof(uint16_t), cudaMemcpyDeviceToDevice, st), "sample");
+        ACK(cudaMemcpyAsync(u->sw + (size_t)slot * 6 * V, M.w, 6 * V, cudaMemcpyDeviceToDevice, st), "sample");
+        ACK(cudaMemcpyAsync(u->sdiag + (size_t)slot * V, M.diag, V * sizeof(float), cudaMemcpyDeviceToDevice, st), "sample");
+    }
     u->next = (u->next + 1) % u->cap;
     u->count = std::min(u->count + 1, u->cap);
+    return EFS_OK;
+}
+
+int efs_unet_grid(efs_ctx* c, int* width, int* height, int* depth, int* level) {
+    if (!c) return EFS_ERR_ARG;
+    if (!c->unet) return efs::ufail(c, EFS_ERR_STATE, "no U-Net: call efs_unet_init first");
+    if (width) *width = c->unet->L[0].W;
+    if (height) *height = c->unet->L[0].H;
+    if (depth) *depth = c->unet->L[0].D;
+    if (level) *level = c->unet->level;
     return EFS_OK;
 }
 
@@ -1200,7 +1080,7 @@ int efs_unet_train(efs_ctx* c, int loss_kind, int iterations, int batch, float l
         (loss_kind != 0 && loss_kind != 1))
         return efs::ufail(c, EFS_ERR_ARG, "loss_kind 0/1, iterations >= 0, batch >= 1, lr > 0, 0 <= synthetic <= 1");
     cudaStream_t st = c->stream;
-    const long long N = c->g.N;
+    const long long N = u->L[0].V;
     ACK(efs::alloc_train(u), "U-Net training buffers");
     unsigned long long rng = seed * 6364136223846793005ull + 1442695040888963407ull;
     double l = 0;
@@ -1213,6 +1093,8 @@ int efs_unet_train(efs_ctx* c, int loss_kind, int iterations, int batch, float l
             const float* sb = u->sb + (size_t)s * N;
             const float* sp = u->sp + (size_t)s * N;
             const uint16_t* sr = u->srow + (size_t)s * N;
+            efs::LvView M{u->L[0].W, u->L[0].H, u->L[0].D, N, sr, u->sw ? u->sw + (size_t)s * 6 * N : nullptr,
+                          u->sdiag ? u->sdiag + (size_t)s * N : nullptr};
             rng = rng * 6364136223846793005ull + 1442695040888963407ull;
             if ((float)((rng >> 40) * (1.0 / 16777216.0)) < synthetic) {
                 // synthetic pair on this sample's geometry: e random and multi-scale, input L e, target e
@@ -1225,13 +1107,12 @@ int efs_unet_train(efs_ctx* c, int loss_kind, int iterations, int batch, float l
                 }
                 efs::k_synth_error<<<efs::nblk(N), 256, 0, st>>>(u->L[0], sr, rng, amp, u->tmp_t);
                 ACK(cudaGetLastError(), "synthetic error");
-                efs::k_fcg_matvec<<<efs::nblk(N), 256, 0, st>>>(u->tmp_t, sr, N, efs::offsets(c), u->tmp_in);
-                ACK(cudaGetLastError(), "synthetic residual");
+                ACK(efs::ml_matvec(M, u->tmp_t, u->tmp_in, st), "synthetic residual");
                 sb = u->tmp_in;
                 sp = u->tmp_t;
             }
-            ACK(efs::forward(u, sb, sr, true, st), "U-Net forward");
-            ACK(efs::backward(u, sb, sp, sr, loss_kind, efs::offsets(c), c->sm_count, st), "U-Net backward");
+            ACK(efs::forward(u, sb, M, true, st), "U-Net forward");
+            ACK(efs::backward(u, sb, sp, M, loss_kind, c->sm_count, st), "U-Net backward");
         }
         u->adam_t += 1;
         const float b1 = 0.9f, b2 = 0.999f;

@@ -255,6 +255,13 @@ class _GB300Simulator:
     def unet_init(self, seed=0, sample_capacity=0):
         check(lib().efs_unet_init(self._h, seed, sample_capacity), self._h)
 
+    def unet_grid(self):
+        """(width, height, depth, level): the grid the network works on, `level` aggregation levels below the
+        context's grid (the FCG preconditioner's bottom level; 0 = the context's own grid)."""
+        v = [ctypes.c_int() for _ in range(4)]
+        check(lib().efs_unet_grid(self._h, *[ctypes.byref(x) for x in v]), self._h)
+        return tuple(x.value for x in v)
+
     def unet_weights(self):
         out = np.empty(unet_param_count(), np.float32)
         check(lib().efs_unet_get_weights(self._h, fptr(out), out.size), self._h)
@@ -265,6 +272,7 @@ class _GB300Simulator:
         check(lib().efs_unet_set_weights(self._h, fptr(a), a.size), self._h)
 
     def unet_apply(self, r):
+        """z = net(r) for a field of the network's grid (unet_grid)."""
         a = np.ascontiguousarray(r, dtype=np.float32)
         z = np.empty_like(a)
         check(lib().efs_unet_apply(self._h, fptr(a), fptr(z)), self._h)

@@ -61,10 +61,14 @@ enum efs_stage {
 enum efs_solver {
     EFS_SOLVER_JACOBI = 0,      /* JacobiSolverCPU3D: max_steps/2 sweeps from p = 0                */
     EFS_SOLVER_CG = 1,          /* CGSolverCPU3D: p0 = b, true residual every 64 iterations        */
-    /* No counterpart in the reference: flexible preconditioned CG with the context's learned U-Net
-     * preconditioner (3D; efs_unet_*), same matrix, start p0 = b and stop rule as EFS_SOLVER_CG; when the
-     * residual stalls it hands the remaining residual system to plain CG.  Steps with this solver run as
-     * direct launches (the iteration reads scalars on the host), not as a replayed graph. */
+    /* No counterpart in the reference: flexible preconditioned CG (Notay's FCG(1)) on the same matrix and
+     * to the same stop rule as EFS_SOLVER_CG, from p0 = 0, with the pressure accumulated in FP64 and the true
+     * residual recomputed every 32 iterations and before stopping.  Its preconditioner is a multigrid
+     * V-cycle whose coarsest level is solved by the context's learned U-Net (3D; efs_unet_*, fcg_levels and
+     * fcg_bottom below).  When the residual stalls (not halved over 10 iterations) or a direction breaks
+     * down, the remaining residual system goes to plain CG (EFS_CG_MIXED_RECURRENCE).  The whole solve is
+     * device-resident: CUDA graph conditional (while / if) nodes run the iteration, so steps with this solver
+     * replay one graph like the others. */
     EFS_SOLVER_FCG_UNET = 2
 };
 
@@ -144,8 +148,25 @@ typedef struct efs_params {
     int   re_calc_div;        /* RE_CALC_DIV (2D only)                                    */
     int   sharpen_mode;       /* enum efs_sharpen_mode                                    */
     int   cg_variant;         /* enum efs_cg_variant                                      */
-    int   reserved[5];
+    int   fcg_levels;         /* EFS_SOLVER_FCG_UNET: aggregation levels of its preconditioner (below) */
+    int   fcg_bottom;         /* EFS_SOLVER_FCG_UNET: enum efs_fcg_bottom                 */
+    int   reserved[3];
 } efs_params;
+
+/* The preconditioner of EFS_SOLVER_FCG_UNET (no counterpart in the reference) is one V-cycle over a hierarchy
+ * of aggregated grids: level 0 is the pressure matrix itself; level l+1 merges 2x2x2 cells of level l, its
+ * matrix the Galerkin product P^T A P of the piecewise-constant prolongation P (matrix rows where any merged
+ * cell is a row).  At every level above the bottom: 2 damped Jacobi sweeps (weight 0.8), the residual
+ * restricted to the next level, the correction prolonged back, 2 more sweeps.  At the bottom level the
+ * correction comes from the U-Net (fcg_bottom EFS_FCG_BOTTOM_UNET), scaled by the line search
+ * (e.r)/(e.Ae) on that level, or, for comparison without the network, from 20 Jacobi sweeps
+ * (EFS_FCG_BOTTOM_JACOBI).  fcg_levels is the number of aggregation levels (0..3); a negative value picks the
+ * fewest levels whose bottom grid is at most 32 cells on every side.  The network works on the bottom grid
+ * (efs_unet_grid). */
+enum efs_fcg_bottom {
+    EFS_FCG_BOTTOM_UNET = 0,
+    EFS_FCG_BOTTOM_JACOBI = 1
+};
 
 /* Per-context statistics (Properties SOLVE_STEPS / SOLVE_ERRORS / PAUSED / SIMULATION_FRAMES). */
 typedef struct efs_stats {
@@ -264,20 +285,26 @@ int  efs_solve_noalloc(int dim, int width, int height, int depth, const efs_para
 const char* efs_noalloc_last_error(void);
 
 /* ---- learned preconditioner: 3D U-Net (3 levels, 16/32/64 channels, BF16 weights, FP32 accumulation) ----
- * No counterpart in the reference.  A context holds at most one network, sized for its grid; the FP32
- * master parameters are laid out layer by layer as weights [27 taps][cin][cout] then bias [cout] (layers:
- * 16->16, 16->32, 32->64, 64->32, 32->16, 16->16).  The network maps a residual field r to z on the matrix
- * rows; FCG (EFS_SOLVER_FCG_UNET) applies it every iteration.  Training runs on the device on samples
- * (divergence, pressure, matrix rows) the context stored after its own projections.  The matrix rows used
- * by efs_unet_apply and efs_unet_loss_grad are those of the context's current rho and boundary; both
- * entry points overwrite the pressure field with the divergence (the solver's start). */
+ * No counterpart in the reference.  A context holds at most one network, sized for the bottom grid of the
+ * FCG preconditioner's hierarchy (efs_params.fcg_levels at efs_unet_init; with 0 levels, the context's own
+ * grid).  The FP32 master parameters are laid out layer by layer as weights [27 taps][cin][cout] then bias
+ * [cout] (layers: 16->16, 16->32, 32->64, 64->32, 32->16, 16->16).  The network maps a residual field r on
+ * the bottom grid to a correction on that grid's matrix rows; its input channels are r / rms(r), the row
+ * mask and, above level 0, the aggregated matrix (diagonal and the six face weights, normalised).  FCG
+ * (EFS_SOLVER_FCG_UNET) applies it once per iteration.  Training runs on the device on samples the context
+ * stored after its own projections.  The matrix used by efs_unet_apply and efs_unet_loss_grad is the bottom
+ * level's, built from the context's current rho and boundary; both entry points overwrite the pressure
+ * field with the divergence (the solver's start). */
 int  efs_unet_param_count(int64_t* count);
-/* Fresh network with He-normal weights from `seed`; room for `sample_capacity` training samples (0: none). */
+/* Fresh network with He-normal weights from `seed` on the bottom grid of the current fcg_levels; room for
+ * `sample_capacity` training samples (0: none). */
 int  efs_unet_init(efs_ctx* ctx, uint64_t seed, int sample_capacity);
+/* The network's grid (cells per axis) and its aggregation level below the context's grid. */
+int  efs_unet_grid(efs_ctx* ctx, int* width, int* height, int* depth, int* level);
 int  efs_unet_get_weights(efs_ctx* ctx, float* host, int64_t count);
 /* Loading weights also resets the optimiser state of efs_unet_train. */
 int  efs_unet_set_weights(efs_ctx* ctx, const float* host, int64_t count);
-/* z = net(r) on host fields (N floats each). */
+/* z = net(r) on host fields of the network's grid (its cells' count of floats each). */
 int  efs_unet_apply(efs_ctx* ctx, const float* r, float* z);
 /* Training losses, for input b and target p (p solves L p = b; host fields):
  *   loss_kind 0: sum over rows of (net(b)_v - p_v / rms(p))^2 / rows (the pressure, normalised);
@@ -289,7 +316,10 @@ int  efs_unet_loss_grad(efs_ctx* ctx, int loss_kind, const float* b, const float
  * stream, `reps` passes after one warm-up): mean ms per pass and per convolution layer (ms_layers[6], may
  * be NULL).  A measurement entry point: the pressure field is overwritten with the divergence. */
 int  efs_unet_time_forward(efs_ctx* ctx, int reps, float* ms_forward, float* ms_layers);
-/* Stores the current (divergence, pressure, matrix rows) as a training sample (ring buffer). */
+/* Stores a training sample (ring buffer).  With 0 aggregation levels: the current (divergence, pressure,
+ * matrix rows).  Otherwise: the current divergence carried down the V-cycle's pre-smoothing and restriction
+ * chain to the bottom grid (what the network receives in the first FCG iteration), the bottom matrix, and
+ * that residual's exact correction on the bottom grid (a CG solve there, relative residual 1e-8). */
 int  efs_unet_add_sample(efs_ctx* ctx);
 int  efs_unet_sample_count(efs_ctx* ctx, int* count);
 /* `iterations` Adam steps (beta 0.9/0.999) of `batch` samples drawn with `seed`; mean loss of the last batch.

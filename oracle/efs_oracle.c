@@ -1564,6 +1564,7 @@ void orc_params_default(efs_params* p) {
     p->solver = EFS_SOLVER_CG; p->max_steps = 2000; p->solver_threshold = 1e-5f; p->tol_rel = 0.f;
     p->disable_mask = 0; p->re_calc_div = 0; p->sharpen_mode = EFS_SHARPEN_PARALLEL;
     p->cg_variant = EFS_CG_MIXED_RECURRENCE;
+    p->fcg_levels = -1; p->fcg_bottom = EFS_FCG_BOTTOM_UNET;
 }
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -82,6 +82,7 @@ def test_unet_halo_tile_path_matches_oracle():
     p = np.where(rows, rng.normal(size=(D, H, W)), 0.0).astype(np.float32)
     b = apply_L(p).astype(np.float32)
     prm = abi.params_dam(1.0 / W, 0.004, abi.SOLVER_CG, 1e-6)
+    prm.fcg_levels = 0                      # the network on the context's own grid
     with gb.GB300Simulator3D(W, H, D, prm) as s:
         s.unet_init(13, 0)
         s.set_field(abi.FIELD_BOUNDARY, bnd)
