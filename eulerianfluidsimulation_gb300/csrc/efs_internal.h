@@ -200,8 +200,12 @@ cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st
 cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out);
 int ml_level_cg(efs_ctx* c, const LvView& L, const float* r0, float* e, float* t1, float* t2, float* t3, double tol,
                 int maxit, cudaStream_t st);
-// efs_unet.cu: the network's correction z for residual r on the bottom level B (rows; unscaled), teardown
-cudaError_t unet_correction(efs_ctx* c, const LvView& B, const float* r, float* z, cudaStream_t st);
+// efs_unet.cu: the network's forward pass on bottom-level residual r with its input scale already in
+// unet_scale_slot(c) ([0] sum of squares, [1] rows, [2] 1 / rms); output channel 0 in unet_output(c); teardown
+cudaError_t unet_forward_prescaled(efs_ctx* c, const LvView& B, const float* r, cudaStream_t st);
+double* unet_scale_slot(efs_ctx* c);
+cudaError_t unet_scale_rows(efs_ctx* c, const LvView& B, const float* r, cudaStream_t st);   // the slot from r
+const float* unet_output(efs_ctx* c);
 bool unet_matches(const efs_ctx* c);   // the network was made for the context's current fcg_levels
 void unet_free(efs_ctx* c);
 void drop_all_graphs(efs_ctx* c);

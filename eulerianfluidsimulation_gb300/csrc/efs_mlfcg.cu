@@ -39,18 +39,20 @@ namespace {
 
 constexpr float kOmega = 0.8f;        // Jacobi damping
 constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the network
-constexpr int kRedGrid = 304;         // blocks of every reduction kernel (2 per SM on 152 SMs)
 constexpr int kThreads = 256;
+constexpr int kGrid = 608;            // blocks of the fine-level and reduction kernels (4 per SM on 152 SMs)
 
 // device scalars of one FCG solve
 struct FcgDev {
     double rr, rz, dq, zq, bb, thr, alpha, beta, rr_window, rows;
-    double ls_alpha;                  // bottom-level line search factor of the current V-cycle
-    int it, conv, stall, verify, fallback, pad;
+    double ls_alpha;                  // bottom-level line search factor of the current V-cycle (1 without the network)
+    int it, conv, stall, verify, fallback, nchunks;
+    unsigned count;                   // arrival counter of the last-block reductions (back to 0 after each)
+    unsigned pad;
 };
 
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
-inline unsigned red_blocks(long long n) { return (unsigned)std::min<long long>(kRedGrid, blocks_for(n)); }
+inline unsigned grid_for(long long n) { return (unsigned)std::min<long long>(kGrid, blocks_for(n)); }
 
 // ---- matrix rows at a level -----------------------------------------------------------------------------------
 template <bool FINE>
@@ -82,7 +84,26 @@ __device__ __forceinline__ T lapply(const LvView& L, long long i, const T* x, fl
     return s;
 }
 
-// ---- block reduction of three doubles into partials[3 * blockIdx.x + j] ----------------------------------------
+// The cells a level kernel visits: at level 0 the 32-cell chunks that hold a matrix row (the list built at the
+// start of the solve, warp-aligned), at coarser levels every cell.  item -> cell, or -1 past the end.
+struct Walk {
+    const int* chunks;                // level 0 only
+    const FcgDev* s;
+    long long V;
+    __device__ __forceinline__ long long items() const { return chunks ? (long long)s->nchunks * 32 : V; }
+    __device__ __forceinline__ long long cell(long long t) const {
+        if (!chunks) return t;
+        const long long i = (long long)chunks[t >> 5] * 32 + (t & 31);
+        return i < V ? i : -1;
+    }
+};
+#define WALK(wk, t, i)                                                                                        \
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x, n_items_ = (wk).items(); t < n_items_; \
+         t += (long long)gridDim.x * blockDim.x)                                                              \
+        if (const long long i = (wk).cell(t); i >= 0)
+
+// ---- reductions ------------------------------------------------------------------------------------------------
+// block partials of (a, b, c) into part[3 * blockIdx.x + j]
 __device__ __forceinline__ void block_partials(double a, double b, double c, double* part) {
     __shared__ double sh[3][kThreads / 32];
 #pragma unroll
@@ -102,10 +123,108 @@ __device__ __forceinline__ void block_partials(double a, double b, double c, dou
         part[3 * blockIdx.x + 2] = s2;
     }
 }
-// the totals of `nparts` block partials, summed in block order (run by one thread)
-__device__ __forceinline__ void sum_partials(const double* part, int nparts, double (&t)[3]) {
-    t[0] = t[1] = t[2] = 0;
-    for (int b = 0; b < nparts; b++) { t[0] += part[3 * b]; t[1] += part[3 * b + 1]; t[2] += part[3 * b + 2]; }
+// Every block stores its partials; the block that arrives last sums them all in a fixed order (lane-strided over
+// the blocks, then a fixed shuffle tree) and returns true on its thread 0, with the totals in tot.
+__device__ bool reduce_last(double a, double b, double c, double* part, unsigned* counter, double (&tot)[3]) {
+    block_partials(a, b, c, part);
+    __shared__ unsigned s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = (atomicAdd(counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last || threadIdx.x >= 32) return false;
+    __threadfence();
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += 32) {
+        t0 += __ldcg(part + 3 * k);
+        t1 += __ldcg(part + 3 * k + 1);
+        t2 += __ldcg(part + 3 * k + 2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        t0 += __shfl_down_sync(0xffffffffu, t0, o);
+        t1 += __shfl_down_sync(0xffffffffu, t1, o);
+        t2 += __shfl_down_sync(0xffffffffu, t2, o);
+    }
+    if (threadIdx.x != 0) return false;
+    tot[0] = t0; tot[1] = t1; tot[2] = t2;
+    *counter = 0u;
+    return true;
+}
+
+// ---- the level-0 chunk list (ordered compaction of the chunks that hold a row) ---------------------------------
+__device__ __forceinline__ bool chunk_has_row(const uint16_t* info, long long N, long long ch) {
+    const long long i0 = ch * 32;
+    if (i0 + 32 <= N) {
+        const uint4* q = reinterpret_cast<const uint4*>(info + i0);
+        unsigned any = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint4 v = q[k];
+            any |= (v.x | v.y | v.z | v.w);
+        }
+        return (any & 0x80008000u) != 0;
+    }
+    for (long long i = i0; i < N; i++)
+        if (info[i] & 0x8000u) return true;
+    return false;
+}
+__global__ void k_chunks_count(const uint16_t* __restrict__ info, long long N, long long nch, int* __restrict__ bcount) {
+    const long long ch = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int f = (ch < nch) && chunk_has_row(info, N, ch);
+    const int n = __syncthreads_count(f);
+    if (threadIdx.x == 0) bcount[blockIdx.x] = n;
+}
+// exclusive scan of the block counts (one block of 1024 threads), total into s->nchunks
+__global__ void k_chunks_scan(int* __restrict__ bcount, int nb, FcgDev* s) {
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = 0; base < nb; base += 1024) {
+        const int k = base + threadIdx.x;
+        const int v = k < nb ? bcount[k] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int wv = warp_tot[lane];
+            int wi = wv;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            warp_tot[lane] = wi - wv;
+        }
+        __syncthreads();
+        const int excl = carry + warp_tot[warp] + incl - v;
+        if (k < nb) bcount[k] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) s->nchunks = carry;
+}
+__global__ void k_chunks_write(const uint16_t* __restrict__ info, long long N, long long nch, const int* __restrict__ boff,
+                               int* __restrict__ chunks) {
+    __shared__ int wcount[kThreads / 32];
+    const long long ch = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool f = (ch < nch) && chunk_has_row(info, N, ch);
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wcount[warp] = __popc(m);
+    __syncthreads();
+    int off = boff[blockIdx.x];
+    for (int k = 0; k < warp; k++) off += wcount[k];
+    if (f) chunks[off + __popc(m & ((1u << lane) - 1u))] = (int)ch;
 }
 
 // ---- hierarchy -------------------------------------------------------------------------------------------------
@@ -147,44 +266,94 @@ __global__ void k_ml_build(LvView src, LvOut dst) {
 }
 
 // ---- level operators ------------------------------------------------------------------------------------------
-// zout = zin + w (r - A zin) / diag on rows (zin null: zout = w r / diag), 0 elsewhere
-template <bool FINE>
-__global__ void k_ml_smooth(LvView L, const float* __restrict__ r, const float* __restrict__ zin, float* __restrict__ zout,
-                            float omega) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= L.V) return;
-    float dg, w[6];
-    if (!lrow<FINE>(L, i, dg, w) || dg == 0.f) { zout[i] = 0.f; return; }
-    if (!zin) { zout[i] = omega * r[i] / dg; return; }
-    const float az = lapply<float>(L, i, zin, dg, w);
-    zout[i] = zin[i] + omega * (r[i] - az) / dg;
+// zout = zin + w (r - A zin) / diag on rows (zin null: zout = w r / diag), 0 on the other visited cells.
+// DOTS (level 0, the last sweep of the V-cycle): also the partials of z.q and r.z, and in the last block
+// beta = -(z.q) / (d.q) of FCG(1) (0 in the first iteration) and r.z.
+template <bool FINE, bool DOTS>
+__global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, const float* __restrict__ zin,
+                            float* __restrict__ zout, float omega, const float* __restrict__ q, FcgDev* s,
+                            double* __restrict__ part) {
+    double zq = 0, rz = 0;
+    WALK(wk, t, i) {
+        float dg, w[6];
+        float zi = 0.f;
+        if (lrow<FINE>(L, i, dg, w) && dg != 0.f)
+            zi = zin ? zin[i] + omega * (r[i] - lapply<float>(L, i, zin, dg, w)) / dg : omega * r[i] / dg;
+        zout[i] = zi;
+        if (DOTS) {
+            zq += (double)zi * q[i];
+            rz += (double)zi * r[i];
+        }
+    }
+    if (DOTS) {
+        double tot[3];
+        if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+            s->zq = tot[0];
+            s->rz = tot[1];
+            double beta = 0.0;
+            if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
+            s->beta = isfinite(beta) ? beta : 0.0;
+        }
+    }
 }
-// rc[C] = sum over the merged rows i of C of (r - A z)_i (z null: of r_i)
+// rc[C] = sum over the merged rows i of C of (r - A z)_i.  scal (non-null: the level below is the network's):
+// the sum of rc^2 over the coarse rows, their count and 1 / rms into scal[0..2].
 template <bool FINE>
 __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float* __restrict__ z, LvView Cv,
-                              float* __restrict__ rc) {
-    const long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (C >= Cv.V) return;
-    const int X = (int)(C % Cv.W), Y = (int)((C / Cv.W) % Cv.H), Z = (int)(C / ((long long)Cv.W * Cv.H));
-    float s = 0.f;
-    for (int c8 = 0; c8 < 8; c8++) {
-        const int x = 2 * X + (c8 & 1), y = 2 * Y + ((c8 >> 1) & 1), zz = 2 * Z + (c8 >> 2);
-        if (x >= F.W || y >= F.H || zz >= F.D) continue;
-        const long long i = ((long long)zz * F.H + y) * F.W + x;
-        float dg, w[6];
-        if (!lrow<FINE>(F, i, dg, w)) continue;
-        s += z ? r[i] - lapply<float>(F, i, z, dg, w) : r[i];
+                              float* __restrict__ rc, double* __restrict__ scal, FcgDev* s, double* __restrict__ part) {
+    double ss = 0, cnt = 0;
+    for (long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x; C < Cv.V; C += (long long)gridDim.x * blockDim.x) {
+        const int X = (int)(C % Cv.W), Y = (int)((C / Cv.W) % Cv.H), Z = (int)(C / ((long long)Cv.W * Cv.H));
+        float acc = 0.f;
+        for (int c8 = 0; c8 < 8; c8++) {
+            const int x = 2 * X + (c8 & 1), y = 2 * Y + ((c8 >> 1) & 1), zz = 2 * Z + (c8 >> 2);
+            if (x >= F.W || y >= F.H || zz >= F.D) continue;
+            const long long i = ((long long)zz * F.H + y) * F.W + x;
+            float dg, w[6];
+            if (!lrow<FINE>(F, i, dg, w)) continue;
+            acc += r[i] - lapply<float>(F, i, z, dg, w);
+        }
+        rc[C] = acc;
+        if (scal && (Cv.info[C] & 0x8000u)) {
+            ss += (double)acc * acc;
+            cnt += 1.0;
+        }
     }
-    rc[C] = s;
+    if (scal) {
+        double tot[3];
+        if (reduce_last(ss, cnt, 0.0, part, &s->count, tot)) {
+            scal[0] = tot[0];
+            scal[1] = tot[1];
+            scal[2] = (tot[0] > 0 && tot[1] > 0) ? 1.0 / sqrt(tot[0] / tot[1]) : 1.0;
+        }
+    }
 }
-// z_i += ec[parent(i)] on rows
+// The first sweep after the coarse correction, with the prolongation folded in: with zp = z + a ec(parent) on
+// the rows (a = *alpha, or 1), tout = zp + w (r - A zp) / diag.
 template <bool FINE>
-__global__ void k_ml_prolong(LvView F, float* __restrict__ z, const float* __restrict__ ec, LvView Cv) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= F.V) return;
-    if (!(F.info[i] & 0x8000u)) return;
-    const int x = (int)(i % F.W), y = (int)((i / F.W) % F.H), zz = (int)(i / ((long long)F.W * F.H));
-    z[i] += ec[((long long)(zz >> 1) * Cv.H + (y >> 1)) * Cv.W + (x >> 1)];
+__global__ void k_ml_prolong_smooth(LvView L, Walk wk, const float* __restrict__ r, const float* __restrict__ z,
+                                    const float* __restrict__ ec, LvView Cv, const double* __restrict__ alpha,
+                                    float* __restrict__ tout, float omega) {
+    const float a = alpha ? (float)*alpha : 1.f;
+    const int W = L.W, H = L.H;
+    WALK(wk, t, i) {
+        float dg, w[6];
+        if (!lrow<FINE>(L, i, dg, w) || dg == 0.f) { tout[i] = 0.f; continue; }
+        const int x = (int)(i % W), y = (int)((i / W) % H), zz = (int)(i / ((long long)W * H));
+        auto parent = [&](int px, int py, int pz) {
+            return ec[((long long)(pz >> 1) * Cv.H + (py >> 1)) * Cv.W + (px >> 1)];
+        };
+        const float zi = z[i] + a * parent(x, y, zz);
+        float s = dg * zi;
+        if (w[0] != 0.f) s += w[0] * (z[i - 1] + a * parent(x - 1, y, zz));
+        if (w[1] != 0.f) s += w[1] * (z[i + 1] + a * parent(x + 1, y, zz));
+        if (w[2] != 0.f) s += w[2] * (z[i - W] + a * parent(x, y - 1, zz));
+        if (w[3] != 0.f) s += w[3] * (z[i + W] + a * parent(x, y + 1, zz));
+        const long long WH = (long long)W * H;
+        if (w[4] != 0.f) s += w[4] * (z[i - WH] + a * parent(x, y, zz - 1));
+        if (w[5] != 0.f) s += w[5] * (z[i + WH] + a * parent(x, y, zz + 1));
+        tout[i] = zi + omega * (r[i] - s) / dg;
+    }
 }
 template <bool FINE>
 __global__ void k_ml_matvec(LvView L, const float* __restrict__ x, float* __restrict__ y) {
@@ -193,37 +362,53 @@ __global__ void k_ml_matvec(LvView L, const float* __restrict__ x, float* __rest
     float dg, w[6];
     y[i] = lrow<FINE>(L, i, dg, w) ? lapply<float>(L, i, x, dg, w) : 0.f;
 }
-// bottom line search: partials of e.r and e.(A e)
+// bottom line search for the network's output e (read on the rows): a = (e.r) / (e.Ae) into s->ls_alpha
 template <bool FINE>
-__global__ void k_ml_ls_dots(LvView L, const float* __restrict__ e, const float* __restrict__ r, double* __restrict__ part) {
-    double a = 0, b = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < L.V; i += (long long)gridDim.x * blockDim.x) {
+__global__ void k_ml_line_search(LvView L, Walk wk, const float* __restrict__ e, const float* __restrict__ r, FcgDev* s,
+                                 double* __restrict__ part) {
+    double er = 0, eae = 0;
+    WALK(wk, t, i) {
         float dg, w[6];
         if (!lrow<FINE>(L, i, dg, w)) continue;
         const double ei = e[i];
-        a += ei * (double)r[i];
-        b += ei * (double)lapply<float>(L, i, e, dg, w);
+        er += ei * (double)r[i];
+        eae += ei * (double)lapply<float>(L, i, e, dg, w);
     }
-    block_partials(a, b, 0.0, part);
+    double tot[3];
+    if (reduce_last(er, eae, 0.0, part, &s->count, tot)) {
+        const double a = (tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
+        s->ls_alpha = isfinite(a) ? a : 0.0;
+    }
 }
-__global__ void k_ml_ls_finish(const double* __restrict__ part, int nparts, FcgDev* s) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    const double a = (t[1] != 0.0) ? t[0] / t[1] : 0.0;
-    s->ls_alpha = std::isfinite(a) ? a : 0.0;
-}
-__global__ void k_ml_scale(long long n, float* __restrict__ z, const FcgDev* __restrict__ s) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) z[i] = (float)((double)z[i] * s->ls_alpha);
+// level 0 is the bottom: z = a e on the rows, with FCG's dots and beta as in the last sweep (k_ml_smooth DOTS)
+__global__ void k_take_dots(LvView F, Walk wk, const float* __restrict__ e, const float* __restrict__ q,
+                            const float* __restrict__ r, float* __restrict__ z, FcgDev* s, double* __restrict__ part) {
+    const double a = s->ls_alpha;
+    double zq = 0, rz = 0;
+    WALK(wk, t, i) {
+        const float zi = (F.info[i] & 0x8000u) ? (float)(a * (double)e[i]) : 0.f;
+        z[i] = zi;
+        zq += (double)zi * q[i];
+        rz += (double)zi * r[i];
+    }
+    double tot[3];
+    if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+        s->zq = tot[0];
+        s->rz = tot[1];
+        double beta = 0.0;
+        if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
+        s->beta = isfinite(beta) ? beta : 0.0;
+    }
 }
 
 // ---- FCG ------------------------------------------------------------------------------------------------------
-// x = 0, r = b on rows (0 elsewhere), d = q = 0; partials of b.b and the row count
-__global__ void k_fcg_init(LvView F, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
-                           float* __restrict__ d, float* __restrict__ q, double* __restrict__ part) {
+// x = 0, r = b on rows (0 on the other visited cells), d = q = 0; b.b and the row count; the stop threshold as
+// the CG solvers form it (k_solver): tol_rel^2 b.b rounded to float, or the absolute one
+__global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
+                           float* __restrict__ d, float* __restrict__ q, FcgDev* s, double* __restrict__ part,
+                           float tol_rel, float abs_thr, int max_it, cudaGraphConditionalHandle loop) {
     double bb = 0, rows = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+    WALK(wk, t, i) {
         const bool row = F.info[i] & 0x8000u;
         const float bi = row ? b[i] : 0.f;
         x[i] = 0.0;
@@ -233,134 +418,110 @@ __global__ void k_fcg_init(LvView F, const float* __restrict__ b, double* __rest
         bb += (double)bi * bi;
         rows += row ? 1.0 : 0.0;
     }
-    block_partials(bb, rows, 0.0, part);
-}
-// the stop threshold as the CG solvers form it (k_solver): tol_rel^2 b.b rounded to float, or the absolute one
-__global__ void k_fcg_init_finish(const double* __restrict__ part, int nparts, FcgDev* s, float tol_rel, float abs_thr,
-                                  int max_it, cudaGraphConditionalHandle loop) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    s->bb = t[0];
-    s->rows = t[1];
-    s->rr = t[0];
-    double thr;
-    if (tol_rel > 0) {
-        float tf = (float)((double)tol_rel * (double)tol_rel * t[0]);
-        if (!(tf > 0)) tf = FLT_MIN;
-        thr = (double)tf;
-    } else {
-        thr = (double)abs_thr;
+    double tot[3];
+    if (reduce_last(bb, rows, 0.0, part, &s->count, tot)) {
+        s->bb = tot[0];
+        s->rows = tot[1];
+        s->rr = tot[0];
+        double thr;
+        if (tol_rel > 0) {
+            float tf = (float)((double)tol_rel * (double)tol_rel * tot[0]);
+            if (!(tf > 0)) tf = FLT_MIN;
+            thr = (double)tf;
+        } else {
+            thr = (double)abs_thr;
+        }
+        s->thr = thr;
+        s->conv = s->rr < thr;
+        s->it = 0;
+        s->stall = 0;
+        s->verify = 0;
+        s->fallback = 0;
+        s->rr_window = s->rr;
+        s->rz = s->dq = s->zq = s->alpha = s->beta = 0;
+        s->ls_alpha = 1.0;
+        cudaGraphSetConditional(loop, (!s->conv && max_it > 0) ? 1u : 0u);
     }
-    s->thr = thr;
-    s->conv = s->rr < thr;
-    s->it = 0;
-    s->stall = 0;
-    s->verify = 0;
-    s->fallback = 0;
-    s->rr_window = s->rr;
-    s->rz = s->dq = s->zq = s->alpha = s->beta = 0;
-    cudaGraphSetConditional(loop, (!s->conv && max_it > 0) ? 1u : 0u);
 }
-// partials of z.q (q = A d of the previous iteration) and r.z
-__global__ void k_fcg_dots_zq_rz(LvView F, const float* __restrict__ z, const float* __restrict__ q,
-                                 const float* __restrict__ r, double* __restrict__ part) {
-    double zq = 0, rz = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
-        const double zi = z[i];
-        zq += zi * (double)q[i];
-        rz += zi * (double)r[i];
-    }
-    block_partials(zq, rz, 0.0, part);
-}
-__global__ void k_fcg_beta(const double* __restrict__ part, int nparts, FcgDev* s) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    s->zq = t[0];
-    s->rz = t[1];
-    double beta = 0.0;
-    if (s->it > 0 && s->dq != 0.0) beta = -t[0] / s->dq;
-    s->beta = std::isfinite(beta) ? beta : 0.0;
-}
-__global__ void k_fcg_dir(long long n, float* __restrict__ d, const float* __restrict__ z, const FcgDev* __restrict__ s) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) d[i] = (float)((double)z[i] + s->beta * (double)d[i]);
-}
-// q = A d and the partials of d.q
-__global__ void k_fcg_matvec_dot(LvView F, const float* __restrict__ d, float* __restrict__ q, double* __restrict__ part) {
+// dn = z + beta d (on the fly for the stencil's neighbours), q = A dn; d.q and alpha = (r.z) / (dn.q).  L is
+// negative definite on the rows, so dn.q >= 0 (or a non-finite alpha) is a breakdown: the solve stalls.
+__global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z, const float* __restrict__ d,
+                                 float* __restrict__ dn, float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
+    const float beta = (float)s->beta;
     double dq = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+    WALK(wk, t, i) {
         float dg, w[6];
+        const float di = z[i] + beta * d[i];
         float qi = 0.f;
-        if (lrow<true>(F, i, dg, w)) qi = lapply<float>(F, i, d, dg, w);
+        if (lrow<true>(F, i, dg, w)) {
+            qi = dg * di;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (w[k] != 0.f) {
+                    const long long j = i + noff(F, k);
+                    qi += z[j] + beta * d[j];
+                }
+        }
+        dn[i] = di;
         q[i] = qi;
-        dq += (double)d[i] * qi;
+        dq += (double)di * qi;
     }
-    block_partials(dq, 0.0, 0.0, part);
-}
-// alpha = (r.z) / (d.q); L is negative definite on the rows, so d.q >= 0 (or a non-finite alpha) is a breakdown
-__global__ void k_fcg_alpha(const double* __restrict__ part, int nparts, FcgDev* s) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    s->dq = t[0];
-    const double a = s->rz / t[0];
-    if (!(t[0] < 0.0) || !std::isfinite(a)) {
-        s->stall = 1;
-        s->alpha = 0.0;
-    } else {
-        s->alpha = a;
+    double tot[3];
+    if (reduce_last(dq, 0.0, 0.0, part, &s->count, tot)) {
+        s->dq = tot[0];
+        const double a = s->rz / tot[0];
+        if (!(tot[0] < 0.0) || !isfinite(a)) {
+            s->stall = 1;
+            s->alpha = 0.0;
+        } else {
+            s->alpha = a;
+        }
     }
 }
-// x += alpha d, r -= alpha q; partials of r.r
-__global__ void k_fcg_update(long long n, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ d,
-                             const float* __restrict__ q, const FcgDev* __restrict__ s, double* __restrict__ part) {
+// x += alpha dn, r -= alpha q, d = dn; r.r, the iteration count, the stall window and whether the true residual
+// is recomputed now (every 32 iterations and when the recurrence residual meets the threshold)
+__global__ void k_fcg_update(Walk wk, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
+                             float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
+                             cudaGraphConditionalHandle verify) {
     const double a = s->alpha;
     double rr = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        x[i] += a * (double)d[i];
+    WALK(wk, t, i) {
+        const float di = dn[i];
+        x[i] += a * (double)di;
         const float ri = (float)((double)r[i] - a * (double)q[i]);
         r[i] = ri;
+        d[i] = di;
         rr += (double)ri * ri;
     }
-    block_partials(rr, 0.0, 0.0, part);
-}
-// r.r, the iteration count, the stall window and whether the true residual is recomputed now
-__global__ void k_fcg_check(const double* __restrict__ part, int nparts, FcgDev* s, cudaGraphConditionalHandle verify) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    s->rr = t[0];
-    s->it += 1;
-    const bool below = s->rr < s->thr;
-    if (!below && !s->stall && (s->it % 10) == 0) {
-        if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
-        s->rr_window = s->rr;
+    double tot[3];
+    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+        s->rr = tot[0];
+        s->it += 1;
+        const bool below = s->rr < s->thr;
+        if (!below && !s->stall && (s->it % 10) == 0) {
+            if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
+            s->rr_window = s->rr;
+        }
+        s->verify = !s->stall && (below || (s->it % 32) == 0);
+        cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
     }
-    s->verify = !s->stall && (below || (s->it % 32) == 0);
-    if (!s->verify) s->conv = 0;
-    cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
 }
-// r = b - A x in FP64 (rows), partials of r.r
-__global__ void k_fcg_true_resid(LvView F, const float* __restrict__ b, const double* __restrict__ x, float* __restrict__ r,
-                                 double* __restrict__ part) {
+// r = b - A x in FP64 (rows); r.r and the convergence decision
+__global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b, const double* __restrict__ x,
+                                 float* __restrict__ r, FcgDev* s, double* __restrict__ part) {
     double rr = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < F.V; i += (long long)gridDim.x * blockDim.x) {
+    WALK(wk, t, i) {
         float dg, w[6];
         float ri = 0.f;
         if (lrow<true>(F, i, dg, w)) ri = (float)((double)b[i] - lapply<double>(F, i, x, dg, w));
         r[i] = ri;
         rr += (double)ri * ri;
     }
-    block_partials(rr, 0.0, 0.0, part);
-}
-__global__ void k_fcg_verify(const double* __restrict__ part, int nparts, FcgDev* s) {
-    if (threadIdx.x != 0) return;
-    double t[3];
-    sum_partials(part, nparts, t);
-    s->rr = t[0];
-    s->conv = s->rr < s->thr;
+    double tot[3];
+    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+        s->rr = tot[0];
+        s->conv = s->rr < s->thr;
+    }
 }
 // the loop condition for the next iteration
 __global__ void k_fcg_loop(const FcgDev* __restrict__ s, int max_it, cudaGraphConditionalHandle loop) {
@@ -372,28 +533,29 @@ __global__ void k_fcg_post(FcgDev* s, cudaGraphConditionalHandle fallback) {
     if (threadIdx.x != 0) return;
     cudaGraphSetConditional(fallback, (s->stall && !s->conv) ? 1u : 0u);
 }
-// fb = b - A x in FP64 (rows; the right-hand side of the fallback CG)
+// fb = b - A x in FP64 on rows, 0 elsewhere (the right-hand side of the fallback CG; every cell written)
 __global__ void k_fcg_fb_rhs(LvView F, const float* __restrict__ b, const double* __restrict__ x, float* __restrict__ fb) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= F.V) return;
     float dg, w[6];
     fb[i] = lrow<true>(F, i, dg, w) ? (float)((double)b[i] - lapply<double>(F, i, x, dg, w)) : 0.f;
 }
-__global__ void k_fcg_fb_add(LvView F, double* __restrict__ x, const float* __restrict__ p) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < F.V && (F.info[i] & 0x8000u)) x[i] += (double)p[i];
+__global__ void k_fcg_fb_add(LvView F, Walk wk, double* __restrict__ x, const float* __restrict__ p) {
+    WALK(wk, t, i) {
+        if (F.info[i] & 0x8000u) x[i] += (double)p[i];
+    }
 }
 __global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
     if (threadIdx.x != 0) return;
     s->fallback = 1;
     s->conv = ctl->converged;
 }
-__global__ void k_fcg_out(LvView F, const double* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= F.V) return;
-    if (F.info[i] & 0x8000u) {
-        p[i] = (float)x[i];
-        p64[i] = x[i];
+__global__ void k_fcg_out(LvView F, Walk wk, const double* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
+    WALK(wk, t, i) {
+        if (F.info[i] & 0x8000u) {
+            p[i] = (float)x[i];
+            p64[i] = x[i];
+        }
     }
 }
 // solve statistics into the control block; after a fallback the CG launch has counted the solve and its own
@@ -419,7 +581,7 @@ __global__ void k_fcg_stats(const FcgDev* __restrict__ s, DevCtl* ctl) {
     ctl->sum_iter_rows += (double)it * s->rows;
 }
 
-// host-side CG on one level (training samples): dots through these partials
+// host-driven CG on one level (training samples): dots through these partials
 __global__ void k_lv_dot3(long long n, const float* a0, const float* b0, const float* a1, const float* b1,
                           double* __restrict__ part) {
     double s0 = 0, s1 = 0;
@@ -459,8 +621,11 @@ struct MLState {
     int nlev = 0;                 // aggregation levels of the allocated hierarchy
     MLLevel lv[4];                // lv[1..nlev]
     double* x64 = nullptr;        // FCG vectors (fine grid)
-    float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *q = nullptr, *fb = nullptr;
-    double* part = nullptr;       // 3 * kRedGrid block partials
+    float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *dn = nullptr, *q = nullptr, *fb = nullptr;
+    int* chunks = nullptr;        // level 0: the 32-cell chunks that hold a matrix row, in order
+    int* bcount = nullptr;        // their per-block counts / offsets
+    long long nch = 0;            // chunks of the fine grid
+    double* part = nullptr;       // 3 * kGrid block partials
     FcgDev* s = nullptr;
     double* hpart = nullptr;      // pinned: partials of the host-driven level CG
     cudaStream_t cap1 = nullptr, cap2 = nullptr;   // streams for capturing conditional bodies
@@ -485,6 +650,11 @@ LvView level_view(const efs_ctx* c, const MLState* m, int l) {
     if (l == 0) return fine_view(c);
     const MLLevel& L = m->lv[l];
     return LvView{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
+}
+// level 0 visits the chunk list, coarser levels every cell
+Walk walk_of(const efs_ctx* c, const MLState* m, int l) {
+    if (l == 0) return Walk{m->chunks, m->s, (long long)c->g.N};
+    return Walk{nullptr, m->s, m->lv[l].V};
 }
 
 }  // namespace
@@ -539,14 +709,18 @@ cudaError_t ml_alloc(efs_ctx* c) {
     c->ml = m;
     m->nlev = nlev;
     const long long N = c->g.N;
+    m->nch = (N + 31) / 32;
     MCK(malloc_ml(m, &m->x64, N));
     MCK(malloc_ml(m, &m->r, N));
     MCK(malloc_ml(m, &m->z, N));
     MCK(malloc_ml(m, &m->zt, N));
     MCK(malloc_ml(m, &m->d, N));
+    MCK(malloc_ml(m, &m->dn, N));
     MCK(malloc_ml(m, &m->q, N));
     MCK(malloc_ml(m, &m->fb, N));
-    MCK(malloc_ml(m, &m->part, 3LL * kRedGrid));
+    MCK(malloc_ml(m, &m->chunks, m->nch));
+    MCK(malloc_ml(m, &m->bcount, (long long)blocks_for(m->nch)));
+    MCK(malloc_ml(m, &m->part, 3LL * kGrid));
     MCK(malloc_ml(m, &m->s, 1));
     MCK(cudaMemset(m->s, 0, sizeof(FcgDev)));
     for (int l = 1; l <= nlev; l++) {
@@ -560,7 +734,7 @@ cudaError_t ml_alloc(efs_ctx* c) {
         MCK(malloc_ml(m, &L.z, L.V));
         MCK(malloc_ml(m, &L.t, L.V));
     }
-    MCK(cudaMallocHost(reinterpret_cast<void**>(&m->hpart), 3 * kRedGrid * sizeof(double)));
+    MCK(cudaMallocHost(reinterpret_cast<void**>(&m->hpart), 3 * kGrid * sizeof(double)));
     MCK(cudaStreamCreateWithFlags(&m->cap1, cudaStreamNonBlocking));
     MCK(cudaStreamCreateWithFlags(&m->cap2, cudaStreamNonBlocking));
     return cudaSuccess;
@@ -570,9 +744,15 @@ int ml_levels(const efs_ctx* c) { return c->ml ? c->ml->nlev : ml_resolve_levels
 
 LvView ml_view(const efs_ctx* c, int level) { return level_view(c, c->ml, level); }
 
-// The hierarchy's matrices from the current rowinfo.
+// The hierarchy's matrices and the level-0 chunk list from the current rowinfo.
 cudaError_t ml_build(efs_ctx* c, cudaStream_t st) {
     MLState* m = c->ml;
+    const long long N = c->g.N;
+    const unsigned nb = blocks_for(m->nch);
+    k_chunks_count<<<nb, kThreads, 0, st>>>(c->rowinfo, N, m->nch, m->bcount);
+    k_chunks_scan<<<1, 1024, 0, st>>>(m->bcount, (int)nb, m->s);
+    k_chunks_write<<<nb, kThreads, 0, st>>>(c->rowinfo, N, m->nch, m->bcount, m->chunks);
+    MCK(cudaGetLastError());
     for (int l = 1; l <= m->nlev; l++) {
         const MLLevel& L = m->lv[l];
         const LvOut out{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
@@ -591,73 +771,76 @@ cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st
 
 namespace {
 
-template <bool FINE>
-cudaError_t smooth(const LvView& L, const float* r, const float* zin, float* zout, cudaStream_t st) {
-    k_ml_smooth<FINE><<<blocks_for(L.V), kThreads, 0, st>>>(L, r, zin, zout, kOmega);
-    return cudaGetLastError();
-}
-cudaError_t smooth_any(const LvView& L, const float* r, const float* zin, float* zout, cudaStream_t st) {
-    return L.w ? smooth<false>(L, r, zin, zout, st) : smooth<true>(L, r, zin, zout, st);
-}
-
-// pre-smoothing at level l: z = S(S(0)) with t as the intermediate
-cudaError_t pre_smooth(const LvView& L, const float* r, float* z, float* t, cudaStream_t st) {
-    MCK(smooth_any(L, r, nullptr, t, st));
-    return smooth_any(L, r, t, z, st);
-}
-cudaError_t post_smooth(const LvView& L, const float* r, float* z, float* t, cudaStream_t st) {
-    MCK(smooth_any(L, r, z, t, st));
-    return smooth_any(L, r, t, z, st);
-}
-cudaError_t restrict_to(const LvView& F, const float* r, const float* z, const LvView& Cv, float* rc, cudaStream_t st) {
-    if (!F.w) k_ml_restrict<true><<<blocks_for(Cv.V), kThreads, 0, st>>>(F, r, z, Cv, rc);
-    else k_ml_restrict<false><<<blocks_for(Cv.V), kThreads, 0, st>>>(F, r, z, Cv, rc);
-    return cudaGetLastError();
-}
-cudaError_t prolong_add(const LvView& F, float* z, const float* ec, const LvView& Cv, cudaStream_t st) {
-    if (!F.w) k_ml_prolong<true><<<blocks_for(F.V), kThreads, 0, st>>>(F, z, ec, Cv);
-    else k_ml_prolong<false><<<blocks_for(F.V), kThreads, 0, st>>>(F, z, ec, Cv);
-    return cudaGetLastError();
-}
-
-// The bottom solve: z = the network's correction for r, scaled by the line search on this level (or Jacobi
-// sweeps without the network).
-cudaError_t bottom_solve(efs_ctx* c, const LvView& B, const float* r, float* z, float* t, cudaStream_t st) {
+// one damped Jacobi sweep at level l (zin null: from zero); dots: FCG's z.q and r.z with beta (level 0 only)
+cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zout, cudaStream_t st, bool dots = false) {
     MLState* m = c->ml;
-    if (c->prm.fcg_bottom == EFS_FCG_BOTTOM_JACOBI || !c->unet) {
-        float* a = z;
-        float* o = t;
-        MCK(smooth_any(B, r, nullptr, a, st));
-        for (int k = 1; k < kBottomJacobi; k++) {
-            MCK(smooth_any(B, r, a, o, st));
-            std::swap(a, o);
-        }
-        if (a != z) MCK(cudaMemcpyAsync(z, a, B.V * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        return cudaSuccess;
+    const LvView L = level_view(c, m, l);
+    const Walk wk = walk_of(c, m, l);
+    const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
+    if (l == 0) {
+        if (dots) k_ml_smooth<true, true><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, m->q, m->s, m->part);
+        else k_ml_smooth<true, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
+    } else {
+        k_ml_smooth<false, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     }
-    MCK(unet_correction(c, B, r, z, st));
-    const unsigned rb = red_blocks(B.V);
-    if (!B.w) k_ml_ls_dots<true><<<rb, kThreads, 0, st>>>(B, z, r, m->part);
-    else k_ml_ls_dots<false><<<rb, kThreads, 0, st>>>(B, z, r, m->part);
-    MCK(cudaGetLastError());
-    k_ml_ls_finish<<<1, 32, 0, st>>>(m->part, (int)rb, m->s);
-    MCK(cudaGetLastError());
-    k_ml_scale<<<blocks_for(B.V), kThreads, 0, st>>>(B.V, z, m->s);
     return cudaGetLastError();
 }
 
-// z = M(r) at level l (r, z, t: that level's vectors)
+bool net_bottom(const efs_ctx* c) { return c->prm.fcg_bottom == EFS_FCG_BOTTOM_UNET && c->unet; }
+
+// z = M(r) at level l (r, z, t: that level's vectors).  Level 0 ends with FCG's z.q, r.z and beta.  At the
+// bottom level with the network the correction stays in the network's output buffer, scaled by s->ls_alpha when
+// the level above prolongs it.
 cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaStream_t st) {
     MLState* m = c->ml;
     const LvView L = level_view(c, m, l);
-    if (l == m->nlev) return bottom_solve(c, L, r, z, t, st);
+    const Walk wk = walk_of(c, m, l);
+    const int nb = m->nlev;
+    if (l == nb) {
+        // bottom solve
+        if (net_bottom(c)) {
+            if (l == 0) MCK(unet_scale_rows(c, L, r, st));
+            MCK(unet_forward_prescaled(c, L, r, st));
+            const float* e = unet_output(c);
+            const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
+            if (l == 0) k_ml_line_search<true><<<g, kThreads, 0, st>>>(L, wk, e, r, m->s, m->part);
+            else k_ml_line_search<false><<<g, kThreads, 0, st>>>(L, wk, e, r, m->s, m->part);
+            MCK(cudaGetLastError());
+            if (l == 0) {
+                k_take_dots<<<g, kThreads, 0, st>>>(L, wk, e, m->q, r, z, m->s, m->part);
+                MCK(cudaGetLastError());
+            }
+            return cudaSuccess;
+        }
+        float* a = z;
+        float* o = t;
+        MCK(sweep(c, l, r, nullptr, a, st, l == 0 && kBottomJacobi == 1));
+        for (int k = 1; k < kBottomJacobi; k++) {
+            MCK(sweep(c, l, r, a, o, st, l == 0 && k == kBottomJacobi - 1));
+            std::swap(a, o);
+        }
+        if (a != z) MCK(cudaMemcpyAsync(z, a, L.V * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        return cudaSuccess;
+    }
     const LvView Cv = level_view(c, m, l + 1);
     MLLevel& N = m->lv[l + 1];
-    MCK(pre_smooth(L, r, z, t, st));
-    MCK(restrict_to(L, r, z, Cv, N.r, st));
+    const bool to_net = (l + 1 == nb) && net_bottom(c);
+    // pre-smoothing, restriction
+    MCK(sweep(c, l, r, nullptr, t, st));
+    MCK(sweep(c, l, r, t, z, st));
+    const unsigned gc = grid_for(Cv.V);
+    if (l == 0) k_ml_restrict<true><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
+    else k_ml_restrict<false><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
+    MCK(cudaGetLastError());
     MCK(vcycle(c, l + 1, N.r, N.z, N.t, st));
-    MCK(prolong_add(L, z, N.z, Cv, st));
-    return post_smooth(L, r, z, t, st);
+    // prolongation folded into the first post-smoothing sweep, then the second sweep
+    const float* ec = to_net ? unet_output(c) : N.z;
+    const double* a = to_net ? &m->s->ls_alpha : nullptr;
+    const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
+    if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
+    else k_ml_prolong_smooth<false><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
+    MCK(cudaGetLastError());
+    return sweep(c, l, r, t, z, st, l == 0);
 }
 
 // a conditional handle on the graph `st` is capturing into
@@ -691,15 +874,15 @@ cudaError_t add_conditional(cudaStream_t st, cudaGraphConditionalHandle h, cudaG
 cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
     MLState* m = c->ml;
     const LvView F = fine_view(c);
+    const Walk wk = walk_of(c, m, 0);
     const long long N = F.V;
-    const unsigned rb = red_blocks(N);
+    const unsigned g = grid_for(N);
     const int max_it = c->prm.max_steps;
     MCK(ml_build(c, st));
     cudaGraphConditionalHandle h_loop, h_verify, h_fb;
     MCK(make_handle(st, &h_loop));
-    k_fcg_init<<<rb, kThreads, 0, st>>>(F, c->div, m->x64, m->r, m->d, m->q, m->part);
-    MCK(cudaGetLastError());
-    k_fcg_init_finish<<<1, 32, 0, st>>>(m->part, (int)rb, m->s, c->prm.tol_rel, c->prm.solver_threshold, max_it, h_loop);
+    k_fcg_init<<<g, kThreads, 0, st>>>(F, wk, c->div, m->x64, m->r, m->d, m->q, m->s, m->part, c->prm.tol_rel,
+                                      c->prm.solver_threshold, max_it, h_loop);
     MCK(cudaGetLastError());
 
     // ---- WHILE: one FCG iteration ----
@@ -710,23 +893,18 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         MCK(cudaStreamBeginCaptureToGraph(b, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;
         do {
+            // z = M(r), with z.q, r.z and beta at its end
             if ((e = vcycle(c, 0, m->r, m->z, m->zt, b)) != cudaSuccess) break;
-            k_fcg_dots_zq_rz<<<rb, kThreads, 0, b>>>(F, m->z, m->q, m->r, m->part);
-            k_fcg_beta<<<1, 32, 0, b>>>(m->part, (int)rb, m->s);
-            k_fcg_dir<<<blocks_for(N), kThreads, 0, b>>>(N, m->d, m->z, m->s);
-            k_fcg_matvec_dot<<<rb, kThreads, 0, b>>>(F, m->d, m->q, m->part);
-            k_fcg_alpha<<<1, 32, 0, b>>>(m->part, (int)rb, m->s);
-            k_fcg_update<<<rb, kThreads, 0, b>>>(N, m->x64, m->r, m->d, m->q, m->s, m->part);
+            k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
-            k_fcg_check<<<1, 32, 0, b>>>(m->part, (int)rb, m->s, h_verify);
+            k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
             cudaGraph_t vbody = nullptr;
             if ((e = add_conditional(b, h_verify, cudaGraphCondTypeIf, &vbody)) != cudaSuccess) break;
             cudaStream_t v = m->cap2;
             if ((e = cudaStreamBeginCaptureToGraph(v, vbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-            k_fcg_true_resid<<<rb, kThreads, 0, v>>>(F, c->div, m->x64, m->r, m->part);
-            k_fcg_verify<<<1, 32, 0, v>>>(m->part, (int)rb, m->s);
+            k_fcg_true_resid<<<g, kThreads, 0, v>>>(F, wk, c->div, m->x64, m->r, m->s, m->part);
             cudaError_t ve = cudaGetLastError();
             cudaGraph_t dummy = nullptr;
             cudaError_t ee = cudaStreamEndCapture(v, &dummy);
@@ -754,7 +932,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             k_fcg_fb_rhs<<<blocks_for(N), kThreads, 0, b>>>(F, c->div, m->x64, m->fb);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             if ((e = launch_solver_on(c, m->fb, &m->s->thr, b)) != cudaSuccess) break;
-            k_fcg_fb_add<<<blocks_for(N), kThreads, 0, b>>>(F, m->x64, c->p);
+            k_fcg_fb_add<<<g, kThreads, 0, b>>>(F, wk, m->x64, c->p);
             k_fcg_fb_done<<<1, 32, 0, b>>>(m->s, c->ctl);
             e = cudaGetLastError();
         } while (0);
@@ -763,7 +941,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         MCK(e);
         MCK(ee);
     }
-    k_fcg_out<<<blocks_for(N), kThreads, 0, st>>>(F, m->x64, c->p, c->p64);
+    k_fcg_out<<<g, kThreads, 0, st>>>(F, wk, m->x64, c->p, c->p64);
     k_fcg_stats<<<1, 32, 0, st>>>(m->s, c->ctl);
     return cudaGetLastError();
 }
@@ -795,6 +973,7 @@ cudaError_t fcg_solve(efs_ctx* c) {
 }
 
 // r (fine) carried down the pre-smoothing and restriction chain to the bottom level: out = the bottom residual
+// (outside any capture; builds the hierarchy first)
 cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out) {
     MLState* m = c->ml;
     MCK(ml_build(c, st));
@@ -803,8 +982,12 @@ cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float
         const LvView L = level_view(c, m, l);
         float* z = (l == 0) ? m->z : m->lv[l].z;
         float* t = (l == 0) ? m->zt : m->lv[l].t;
-        MCK(pre_smooth(L, r, z, t, st));
-        MCK(restrict_to(L, r, z, level_view(c, m, l + 1), m->lv[l + 1].r, st));
+        const LvView Cv = level_view(c, m, l + 1);
+        MCK(sweep(c, l, r, nullptr, t, st));
+        MCK(sweep(c, l, r, t, z, st));
+        if (l == 0) k_ml_restrict<true><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[1].r, nullptr, m->s, m->part);
+        else k_ml_restrict<false><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[l + 1].r, nullptr, m->s, m->part);
+        MCK(cudaGetLastError());
         r = m->lv[l + 1].r;
     }
     *out = r;
@@ -817,7 +1000,7 @@ int ml_level_cg(efs_ctx* c, const LvView& L, const float* r0, float* e, float* t
                 int maxit, cudaStream_t st) {
     MLState* m = c->ml;
     const long long n = L.V;
-    const unsigned rb = red_blocks(n), nb = blocks_for(n);
+    const unsigned rb = grid_for(n), nb = blocks_for(n);
     float *r = t1, *d = t2, *q = t3;
     auto dot2 = [&](const float* a0, const float* b0, const float* a1, const float* b1, double& s0, double& s1) -> bool {
         k_lv_dot3<<<rb, kThreads, 0, st>>>(n, a0, b0, a1, b1, m->part);

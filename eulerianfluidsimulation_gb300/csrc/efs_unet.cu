@@ -610,13 +610,15 @@ cudaError_t scale_rows(UNetState* u, const float* x, const uint16_t* rowinfo, lo
 
 // forward pass on the input field `r` (FP32, reference layout) with matrix rows `rowinfo`; y32 holds the output.
 // train: keep the pre-activations for the backward pass.
+// prescaled: u->dscal[0..2] already hold the input's sum of squares, row count and 1 / rms (FCG's restriction
+// kernel computes them on the way down).
 cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, cudaStream_t st,
-                    cudaEvent_t* ev = nullptr) {
+                    cudaEvent_t* ev = nullptr, bool prescaled = false) {
     const Level *L = u->L;
     const uint16_t* rowinfo = M.info;
     // ev (optional): 12 events recorded before and after each of the six convolutions
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
-    UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
+    if (!prescaled) UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
     k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0, M.w, M.diag,
                                           1.f / (float)(1 << (2 * u->level)));
     UCK(cudaGetLastError());
@@ -831,14 +833,19 @@ void unet_free(efs_ctx* c) {
     c->unet = nullptr;
 }
 
-// The network's correction for residual r on the bottom level B: z = net(r) on B's rows, 0 elsewhere.
-cudaError_t unet_correction(efs_ctx* c, const LvView& B, const float* r, float* z, cudaStream_t st) {
+// The network's correction for residual r on the bottom level B, left in unet_output(c) (channel 0 of the last
+// convolution, to be read on B's rows).  The input scale (1 / rms of r over the rows) must already be in
+// unet_scale_slot(c)[2], as FCG's restriction kernel leaves it.
+cudaError_t unet_forward_prescaled(efs_ctx* c, const LvView& B, const float* r, cudaStream_t st) {
     UNetState* u = c->unet;
     if (!u || u->L[0].V != B.V) return cudaErrorInvalidValue;
-    UCK(forward(u, r, B, false, st));
-    k_unpack<<<nblk(B.V), 256, 0, st>>>(u->y32, B.info, B.V, z);
-    return cudaGetLastError();
+    return forward(u, r, B, false, st, nullptr, true);
 }
+double* unet_scale_slot(efs_ctx* c) { return c->unet ? c->unet->dscal : nullptr; }
+cudaError_t unet_scale_rows(efs_ctx* c, const LvView& B, const float* r, cudaStream_t st) {
+    return scale_rows(c->unet, r, B.info, B.V, c->unet->dscal, st);
+}
+const float* unet_output(efs_ctx* c) { return c->unet ? c->unet->y32 : nullptr; }
 
 bool unet_matches(const efs_ctx* c) { return c->unet && c->unet->level == ml_resolve_levels(c); }
 
