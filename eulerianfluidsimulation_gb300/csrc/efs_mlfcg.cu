@@ -239,7 +239,8 @@ template <bool FINE>
 __global__ void k_ml_build(LvView src, LvOut dst) {
     const long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (C >= dst.V) return;
-    const int X = (int)(C % dst.W), Y = (int)((C / dst.W) % dst.H), Z = (int)(C / ((long long)dst.W * dst.H));
+    const int c32 = (int)C;           // grids stay below 2^31 cells
+    const int X = c32 % dst.W, Y = (c32 / dst.W) % dst.H, Z = c32 / (dst.W * dst.H);
     bool row = false;
     float dg = 0.f, w[6] = {0, 0, 0, 0, 0, 0};
     for (int c8 = 0; c8 < 8; c8++) {
@@ -303,7 +304,8 @@ __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float
                               float* __restrict__ rc, double* __restrict__ scal, FcgDev* s, double* __restrict__ part) {
     double ss = 0, cnt = 0;
     for (long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x; C < Cv.V; C += (long long)gridDim.x * blockDim.x) {
-        const int X = (int)(C % Cv.W), Y = (int)((C / Cv.W) % Cv.H), Z = (int)(C / ((long long)Cv.W * Cv.H));
+        const int c32 = (int)C;
+        const int X = c32 % Cv.W, Y = (c32 / Cv.W) % Cv.H, Z = c32 / (Cv.W * Cv.H);
         float acc = 0.f;
         for (int c8 = 0; c8 < 8; c8++) {
             const int x = 2 * X + (c8 & 1), y = 2 * Y + ((c8 >> 1) & 1), zz = 2 * Z + (c8 >> 2);
@@ -339,7 +341,8 @@ __global__ void k_ml_prolong_smooth(LvView L, Walk wk, const float* __restrict__
     WALK(wk, t, i) {
         float dg, w[6];
         if (!lrow<FINE>(L, i, dg, w) || dg == 0.f) { tout[i] = 0.f; continue; }
-        const int x = (int)(i % W), y = (int)((i / W) % H), zz = (int)(i / ((long long)W * H));
+        const int i32 = (int)i;
+        const int x = i32 % W, y = (i32 / W) % H, zz = i32 / (W * H);
         auto parent = [&](int px, int py, int pz) {
             return ec[((long long)(pz >> 1) * Cv.H + (py >> 1)) * Cv.W + (px >> 1)];
         };
@@ -398,6 +401,212 @@ __global__ void k_take_dots(LvView F, Walk wk, const float* __restrict__ e, cons
         double beta = 0.0;
         if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
         s->beta = isfinite(beta) ? beta : 0.0;
+    }
+}
+
+// ---- level 0 with 128-bit accesses ----------------------------------------------------------------------------
+// When the grid's width is a multiple of 32, every 32-cell chunk is one piece of one grid row, and the chunks in
+// the list lie inside the border (rows are interior cells), so for every 4-cell group of a listed chunk the
+// loads at +-1, +-W and +-W*H stay inside the grid.  Thread t of a level-0 kernel takes the 4-cell group
+// t & 7 of listed chunk t >> 3: a warp covers four chunks, each vector load is 16 bytes a lane.
+struct QWalk {
+    const int* chunks;
+    const FcgDev* s;
+};
+#define QWALK(qw, i)                                                                                            \
+    for (long long t_ = blockIdx.x * (long long)blockDim.x + threadIdx.x, n_ = (long long)(qw).s->nchunks * 8; \
+         t_ < n_; t_ += (long long)gridDim.x * blockDim.x)                                                      \
+        if (const int i = (qw).chunks[t_ >> 3] * 32 + ((int)t_ & 7) * 4; true)
+
+__device__ __forceinline__ void ld4(const float* __restrict__ p, int i, float (&v)[4]) {
+    const float4 a = *reinterpret_cast<const float4*>(p + i);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, int i, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p + i) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void info4(const uint16_t* __restrict__ info, int i, unsigned (&f)[4]) {
+    const uint2 u = *reinterpret_cast<const uint2*>(info + i);
+    f[0] = u.x & 0xFFFFu; f[1] = u.x >> 16; f[2] = u.y & 0xFFFFu; f[3] = u.y >> 16;
+}
+// x at the group's 4 cells (c) and at their six neighbours (nb[k][n], n = -x, +x, -y, +y, -z, +z)
+__device__ __forceinline__ void stencil4(const float* __restrict__ x, int i, int W, int WH, float (&c)[4],
+                                         float (&nb)[4][6]) {
+    float ym[4], yp[4], zm[4], zp[4];
+    ld4(x, i, c);
+    ld4(x, i - W, ym);
+    ld4(x, i + W, yp);
+    ld4(x, i - WH, zm);
+    ld4(x, i + WH, zp);
+    const float left = x[i - 1], right = x[i + 4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        nb[k][0] = k == 0 ? left : c[k - 1 < 0 ? 0 : k - 1];
+        nb[k][1] = k == 3 ? right : c[k + 1 > 3 ? 3 : k + 1];
+        nb[k][2] = ym[k]; nb[k][3] = yp[k]; nb[k][4] = zm[k]; nb[k][5] = zp[k];
+    }
+}
+__device__ __forceinline__ float lap4(unsigned f, float c, const float (&nb)[6]) {
+    float s = -(float)((f >> 8) & 7) * c;
+#pragma unroll
+    for (int n = 0; n < 6; n++)
+        if (f & (1u << n)) s += nb[n];
+    return s;
+}
+
+// k_ml_smooth at level 0
+template <bool DOTS>
+__global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ r,
+                           const float* __restrict__ zin, float* __restrict__ zout, float omega,
+                           const float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
+    double zq = 0, rz = 0;
+    QWALK(qw, i) {
+        unsigned f[4];
+        float rv[4], out[4];
+        info4(info, i, f);
+        ld4(r, i, rv);
+        if (zin) {
+            float c[4], nb[4][6];
+            stencil4(zin, i, W, WH, c, nb);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float dg = -(float)((f[k] >> 8) & 7);
+                out[k] = ((f[k] & 0x8000u) && dg != 0.f) ? c[k] + omega * (rv[k] - lap4(f[k], c[k], nb[k])) / dg : 0.f;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float dg = -(float)((f[k] >> 8) & 7);
+                out[k] = ((f[k] & 0x8000u) && dg != 0.f) ? omega * rv[k] / dg : 0.f;
+            }
+        }
+        st4(zout, i, out);
+        if (DOTS) {
+            float qv[4];
+            ld4(q, i, qv);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                zq += (double)out[k] * qv[k];
+                rz += (double)out[k] * rv[k];
+            }
+        }
+    }
+    if (DOTS) {
+        double tot[3];
+        if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+            s->zq = tot[0];
+            s->rz = tot[1];
+            double beta = 0.0;
+            if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
+            s->beta = isfinite(beta) ? beta : 0.0;
+        }
+    }
+}
+// k_ml_prolong_smooth at level 0 (its coarse level is level 1 or the network's grid)
+__global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int H, const float* __restrict__ r,
+                                   const float* __restrict__ z, const float* __restrict__ ec, int CW, int CH,
+                                   const double* __restrict__ alpha, float* __restrict__ tout, float omega) {
+    const float a = alpha ? (float)*alpha : 1.f;
+    const int WH = W * H;
+    QWALK(qw, i) {
+        unsigned f[4];
+        float rv[4], c[4], nb[4][6], out[4];
+        info4(info, i, f);
+        ld4(r, i, rv);
+        stencil4(z, i, W, WH, c, nb);
+        const int x0 = i % W, y = (i / W) % H, zz = i / WH;
+        auto par = [&](int px, int py, int pz) { return ec[((pz >> 1) * CH + (py >> 1)) * CW + (px >> 1)]; };
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const unsigned fk = f[k];
+            const float dg = -(float)((fk >> 8) & 7);
+            if (!(fk & 0x8000u) || dg == 0.f) { out[k] = 0.f; continue; }
+            const int x = x0 + k;
+            const float zc = c[k] + a * par(x, y, zz);
+            float sum = dg * zc;
+            if (fk & 1u) sum += nb[k][0] + a * par(x - 1, y, zz);
+            if (fk & 2u) sum += nb[k][1] + a * par(x + 1, y, zz);
+            if (fk & 4u) sum += nb[k][2] + a * par(x, y - 1, zz);
+            if (fk & 8u) sum += nb[k][3] + a * par(x, y + 1, zz);
+            if (fk & 16u) sum += nb[k][4] + a * par(x, y, zz - 1);
+            if (fk & 32u) sum += nb[k][5] + a * par(x, y, zz + 1);
+            out[k] = zc + omega * (rv[k] - sum) / dg;
+        }
+        st4(tout, i, out);
+    }
+}
+// k_fcg_dir_matvec at level 0
+__global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ z,
+                               const float* __restrict__ d, float* __restrict__ dn, float* __restrict__ q, FcgDev* s,
+                               double* __restrict__ part) {
+    const float beta = (float)s->beta;
+    double dq = 0;
+    QWALK(qw, i) {
+        unsigned f[4];
+        float zc[4], zn[4][6], dc[4], dnb[4][6], dv[4], qv[4];
+        info4(info, i, f);
+        stencil4(z, i, W, WH, zc, zn);
+        stencil4(d, i, W, WH, dc, dnb);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            dv[k] = zc[k] + beta * dc[k];
+            float nbv[6];
+#pragma unroll
+            for (int n = 0; n < 6; n++) nbv[n] = zn[k][n] + beta * dnb[k][n];
+            qv[k] = (f[k] & 0x8000u) ? lap4(f[k], dv[k], nbv) : 0.f;
+            dq += (double)dv[k] * qv[k];
+        }
+        st4(dn, i, dv);
+        st4(q, i, qv);
+    }
+    double tot[3];
+    if (reduce_last(dq, 0.0, 0.0, part, &s->count, tot)) {
+        s->dq = tot[0];
+        const double al = s->rz / tot[0];
+        if (!(tot[0] < 0.0) || !isfinite(al)) {
+            s->stall = 1;
+            s->alpha = 0.0;
+        } else {
+            s->alpha = al;
+        }
+    }
+}
+// k_fcg_update at level 0
+__global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
+                           float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
+                           cudaGraphConditionalHandle verify) {
+    const double a = s->alpha;
+    double rr = 0;
+    QWALK(qw, i) {
+        float dv[4], rv[4], qv[4];
+        ld4(dn, i, dv);
+        ld4(r, i, rv);
+        ld4(q, i, qv);
+        double2* x2 = reinterpret_cast<double2*>(x + i);
+        double2 x01 = x2[0], x23 = x2[1];
+        x01.x += a * (double)dv[0]; x01.y += a * (double)dv[1];
+        x23.x += a * (double)dv[2]; x23.y += a * (double)dv[3];
+        x2[0] = x01;
+        x2[1] = x23;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            rv[k] = (float)((double)rv[k] - a * (double)qv[k]);
+            rr += (double)rv[k] * rv[k];
+        }
+        st4(r, i, rv);
+        st4(d, i, dv);
+    }
+    double tot[3];
+    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+        s->rr = tot[0];
+        s->it += 1;
+        const bool below = s->rr < s->thr;
+        if (!below && !s->stall && (s->it % 10) == 0) {
+            if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
+            s->rr_window = s->rr;
+        }
+        s->verify = !s->stall && (below || (s->it % 32) == 0);
+        cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
     }
 }
 
@@ -771,12 +980,22 @@ cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st
 
 namespace {
 
+// level 0 takes the 128-bit kernels when its rows are whole 32-cell chunks of grid rows
+bool quad_level0(const efs_ctx* c) { return (c->g.W % 32) == 0; }
+QWalk qwalk_of(const MLState* m) { return QWalk{m->chunks, m->s}; }
+
 // one damped Jacobi sweep at level l (zin null: from zero); dots: FCG's z.q and r.z with beta (level 0 only)
 cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zout, cudaStream_t st, bool dots = false) {
     MLState* m = c->ml;
     const LvView L = level_view(c, m, l);
     const Walk wk = walk_of(c, m, l);
     const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
+    if (l == 0 && quad_level0(c)) {
+        const unsigned gq = grid_for(c->g.N / 4);
+        if (dots) k_q_smooth<true><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, m->q, m->s, m->part);
+        else k_q_smooth<false><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, nullptr, m->s, m->part);
+        return cudaGetLastError();
+    }
     if (l == 0) {
         if (dots) k_ml_smooth<true, true><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, m->q, m->s, m->part);
         else k_ml_smooth<true, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
@@ -837,7 +1056,10 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
     const float* ec = to_net ? unet_output(c) : N.z;
     const double* a = to_net ? &m->s->ls_alpha : nullptr;
     const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
-    if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
+    if (l == 0 && quad_level0(c))
+        k_q_prolong_smooth<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.H, r, z, ec, Cv.W,
+                                                                     Cv.H, a, t, kOmega);
+    else if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     else k_ml_prolong_smooth<false><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     MCK(cudaGetLastError());
     return sweep(c, l, r, t, z, st, l == 0);
@@ -895,9 +1117,13 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         do {
             // z = M(r), with z.q, r.z and beta at its end
             if ((e = vcycle(c, 0, m->r, m->z, m->zt, b)) != cudaSuccess) break;
-            k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
+            const bool quad = quad_level0(c);
+            const unsigned gq = grid_for(N / 4);
+            if (quad) k_q_dir_matvec<<<gq, kThreads, 0, b>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, m->z, m->d, m->dn, m->q, m->s, m->part);
+            else k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
-            k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+            if (quad) k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+            else k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
             cudaGraph_t vbody = nullptr;

@@ -6,7 +6,12 @@
   relative L2 of the oracle's;
 - training on the device lowers the loss on the samples it was given;
 - FCG with the trained network reaches the same stop rule as CG, its pressure within 1e-5 of CG's, in
-  fewer iterations than plain CG (the gain of the network over the method without it).
+  fewer iterations than plain CG;
+- FCG with the multilevel preconditioner (the network as its coarsest-level solve): the same stop rule and
+  pressure bound; with a trained network it takes fewer iterations than the same V-cycle without the network
+  (20 Jacobi sweeps at the bottom), which is the network's gain; a network that outputs zeros makes FCG break
+  down at once and the plain-CG fallback finishes the solve; steps with FCG replay one captured graph and
+  match the CG steps.
 """
 import numpy as np
 import pytest
@@ -146,3 +151,107 @@ def test_fcg_converges_and_the_trained_network_saves_iterations():
     assert rel_l2(p_fcg[rows], p_cg[rows]) < 1e-5
     print(f"\nFCG {st_fcg.solve_steps} iterations ({st_fcg.precond_steps} preconditioned), CG {st_cg.solve_steps}")
     assert st_fcg.solve_steps < st_cg.solve_steps, (st_fcg.solve_steps, st_fcg.precond_steps, st_cg.solve_steps)
+
+
+def _dam_ctx(n, spheres=4, seed=4, levels=-1, bottom=abi.FCG_BOTTOM_UNET, solver=abi.SOLVER_CG):
+    prm = abi.params_dam(1.0 / n, 0.004, solver, 1e-6)
+    prm.max_steps = 20000
+    prm.fcg_levels = levels
+    prm.fcg_bottom = bottom
+    s = gb.GB300Simulator3D(n, n, n, prm)
+    b, r = oracle.scene_dam3d(n, n, n, spheres, spheres, seed)
+    s.set_field(abi.FIELD_BOUNDARY, b)
+    s.set_field(abi.FIELD_RHO, r)
+    return s
+
+
+def _solve_with(s, state, **kw):
+    p = s.params.copy()
+    for k, v in kw.items():
+        setattr(p, k, v)
+    s.set_params(p)
+    s.set_fields(state)
+    s.project()
+    return s.stats(), s.pressure()
+
+
+def test_multilevel_fcg_without_network_matches_cg():
+    """64^3 (one aggregation level, 32^3 bottom solved by Jacobi sweeps): FCG meets CG's stop rule, its
+    pressure within 1e-5 of CG's on the rows, in a fraction of CG's iterations."""
+    n = 64
+    with _dam_ctx(n, bottom=abi.FCG_BOTTOM_JACOBI) as s:
+        s.update(3)
+        state = s.fields()
+        st_cg, p_cg = _solve_with(s, state, solver=abi.SOLVER_CG)
+        st, p = _solve_with(s, state, solver=abi.SOLVER_FCG_UNET)
+    rows = (state[abi.FIELD_RHO] > 0.5) & (state[abi.FIELD_BOUNDARY] == 0.0)
+    print(f"\nFCG (V-cycle, Jacobi bottom) {st.solve_steps} iterations, CG {st_cg.solve_steps}")
+    assert st.converged and st_cg.converged and st.rr < st.threshold
+    assert rel_l2(p[rows], p_cg[rows]) < 1e-5
+    assert st.solve_steps * 4 < st_cg.solve_steps
+
+
+def test_fcg_breakdown_falls_back_to_cg():
+    """A network whose output is zero gives z = 0, so d.Ad = 0 in the first iteration: FCG stops there and the
+    persistent CG kernel solves the remaining system; the pressure still meets the stop rule."""
+    n = 32
+    with _dam_ctx(n, levels=0) as s:
+        s.update(2)
+        state = s.fields()
+        st_cg, p_cg = _solve_with(s, state, solver=abi.SOLVER_CG)
+        s.unet_init(3, 0)
+        s.unet_set_weights(np.zeros(gb.unet_param_count(), np.float32))
+        st, p = _solve_with(s, state, solver=abi.SOLVER_FCG_UNET)
+    rows = (state[abi.FIELD_RHO] > 0.5) & (state[abi.FIELD_BOUNDARY] == 0.0)
+    assert st.converged and st.precond_steps == 1 and st.solve_steps > 1
+    assert rel_l2(p[rows], p_cg[rows]) < 1e-5
+
+
+def test_trained_network_beats_the_v_cycle_without_it():
+    """64^3 with the network on the 32^3 bottom grid, trained on samples of another seed's trajectory: on a state
+    it was not trained on, FCG takes fewer iterations with the network than with 20 Jacobi sweeps in its place,
+    and both meet the stop rule with the CG pressure's accuracy."""
+    n = 64
+    with _dam_ctx(n, seed=9) as t:
+        t.unet_init(5, 24)
+        assert t.unet_grid() == (32, 32, 32, 1)
+        for _ in range(24):
+            t.update(1)
+            t.unet_add_sample()
+        t.unet_train(600, batch=8, lr=1e-3, synthetic=0.5, seed=3)
+        w = t.unet_weights()
+    with _dam_ctx(n, seed=4) as s:
+        s.update(3)
+        state = s.fields()
+        st_cg, p_cg = _solve_with(s, state, solver=abi.SOLVER_CG)
+        st_j, p_j = _solve_with(s, state, solver=abi.SOLVER_FCG_UNET, fcg_bottom=abi.FCG_BOTTOM_JACOBI)
+        s.unet_init(0, 0)
+        s.unet_set_weights(w)
+        st_n, p_n = _solve_with(s, state, solver=abi.SOLVER_FCG_UNET, fcg_bottom=abi.FCG_BOTTOM_UNET)
+    rows = (state[abi.FIELD_RHO] > 0.5) & (state[abi.FIELD_BOUNDARY] == 0.0)
+    print(f"\nFCG: network bottom {st_n.solve_steps}, Jacobi bottom {st_j.solve_steps}, plain CG {st_cg.solve_steps}")
+    assert st_n.converged and st_j.converged
+    assert rel_l2(p_n[rows], p_cg[rows]) < 1e-5 and rel_l2(p_j[rows], p_cg[rows]) < 1e-5
+    assert st_n.solve_steps < st_j.solve_steps < st_cg.solve_steps
+
+
+def test_fcg_steps_replay_one_graph_and_match_cg_steps():
+    """Whole steps with FCG (Jacobi bottom, no network needed) through efs_step: the step is one captured graph
+    (the solve's conditional nodes inside it) and two steps match two CG steps within 1e-5."""
+    n = 48
+    with _dam_ctx(n, bottom=abi.FCG_BOTTOM_JACOBI) as s:
+        s.update(1)
+        state = s.fields()
+        s.update(2)
+        want = s.fields()
+        p = s.params.copy()
+        p.solver = abi.SOLVER_FCG_UNET
+        s.set_params(p)
+        assert s.kernels_per_step() > 0
+        s.set_fields(state)
+        s.update(2)
+        got = s.fields()
+        st = s.stats()
+    assert st.converged and not st.paused and st.precond_steps == st.solve_steps
+    for f in (abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_PRESSURE):
+        assert rel_l2(got[f], want[f]) < 1e-5, (abi.FIELD_NAMES[f], rel_l2(got[f], want[f]))
