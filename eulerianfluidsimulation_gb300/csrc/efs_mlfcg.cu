@@ -40,7 +40,7 @@ namespace {
 constexpr float kOmega = 0.8f;        // Jacobi damping
 constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the network
 constexpr int kThreads = 256;
-constexpr int kGrid = 608;            // blocks of the fine-level and reduction kernels (4 per SM on 152 SMs)
+constexpr int kGrid = 4096;           // most blocks of a reduction kernel (the partials buffer holds one per block)
 
 // device scalars of one FCG solve
 struct FcgDev {
@@ -52,6 +52,7 @@ struct FcgDev {
 };
 
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
+// reduction kernels: at most kGrid blocks, looping over the rest
 inline unsigned grid_for(long long n) { return (unsigned)std::min<long long>(kGrid, blocks_for(n)); }
 
 // ---- matrix rows at a level -----------------------------------------------------------------------------------
@@ -135,12 +136,22 @@ __device__ bool reduce_last(double a, double b, double c, double* part, unsigned
     __syncthreads();
     if (!s_last || threadIdx.x >= 32) return false;
     __threadfence();
-    double t0 = 0, t1 = 0, t2 = 0;
-    for (unsigned k = threadIdx.x; k < gridDim.x; k += 32) {
-        t0 += __ldcg(part + 3 * k);
-        t1 += __ldcg(part + 3 * k + 1);
-        t2 += __ldcg(part + 3 * k + 2);
+    // four independent chains per lane (FP64 adds have a long latency), combined in a fixed order
+    double a0[4] = {0, 0, 0, 0}, a1[4] = {0, 0, 0, 0}, a2[4] = {0, 0, 0, 0};
+    for (unsigned k = threadIdx.x; k < gridDim.x; k += 128) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const unsigned kk = k + 32u * u;
+            if (kk < gridDim.x) {
+                a0[u] += __ldcg(part + 3 * kk);
+                a1[u] += __ldcg(part + 3 * kk + 1);
+                a2[u] += __ldcg(part + 3 * kk + 2);
+            }
+        }
     }
+    double t0 = (a0[0] + a0[1]) + (a0[2] + a0[3]);
+    double t1 = (a1[0] + a1[1]) + (a1[2] + a1[3]);
+    double t2 = (a2[0] + a2[1]) + (a2[2] + a2[3]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         t0 += __shfl_down_sync(0xffffffffu, t0, o);
@@ -1000,7 +1011,7 @@ cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zo
         if (dots) k_ml_smooth<true, true><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, m->q, m->s, m->part);
         else k_ml_smooth<true, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     } else {
-        k_ml_smooth<false, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
+        k_ml_smooth<false, false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     }
     return cudaGetLastError();
 }
@@ -1047,7 +1058,7 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
     // pre-smoothing, restriction
     MCK(sweep(c, l, r, nullptr, t, st));
     MCK(sweep(c, l, r, t, z, st));
-    const unsigned gc = grid_for(Cv.V);
+    const unsigned gc = to_net ? grid_for(Cv.V) : blocks_for(Cv.V);
     if (l == 0) k_ml_restrict<true><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
     else k_ml_restrict<false><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
     MCK(cudaGetLastError());
@@ -1060,7 +1071,7 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
         k_q_prolong_smooth<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.H, r, z, ec, Cv.W,
                                                                      Cv.H, a, t, kOmega);
     else if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
-    else k_ml_prolong_smooth<false><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
+    else k_ml_prolong_smooth<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     MCK(cudaGetLastError());
     return sweep(c, l, r, t, z, st, l == 0);
 }

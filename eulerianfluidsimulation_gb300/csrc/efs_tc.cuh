@@ -148,6 +148,11 @@ struct ConvArgs {
     int D, H, W, cin;
     int relu;
     int* err;                   // error word: bit 0 = an mbarrier wait gave up
+    // split over the K steps (taps x 16-channel chunks): CTA (x, y) runs steps [y * split_per, (y + 1) * split_per)
+    // and stores its raw FP32 accumulators in partial[y][V][COUT]; k_conv_split_reduce finishes the layer.
+    // partial null: one CTA per 128 voxels runs every step and finishes the layer itself.
+    float* partial;
+    int split_per;
 };
 
 constexpr int kConvThreads = 128;
@@ -170,7 +175,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     const bool vin = v < V;
     const int x = vin ? v % a.W : 0, y = vin ? (v / a.W) % a.H : 0, z = vin ? v / (a.W * a.H) : 0;
     const int chunks = a.cin >> 4;
-    const int S = 27 * chunks;
+    const int s_all = 27 * chunks;
+    const int s0 = a.partial ? (int)blockIdx.y * a.split_per : 0;
+    const int S = a.partial ? min(a.split_per, s_all - s0) : s_all;   // >= 1: the host sizes the split so
 
     if (warp == 0) tmem_alloc(tslot, kCols);
     if (tid == 0) {
@@ -184,7 +191,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     const uint32_t tmem = *tslot;
 
     auto load = [&](int s, int b) {
-        const int tap = s / chunks, cc = s - tap * chunks;
+        const int sg = s0 + s;
+        const int tap = sg / chunks, cc = sg - tap * chunks;
         const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
         const int nx = x + dx, ny = y + dy, nz = z + dz;
         const bool ok = vin && nx >= 0 && nx < a.W && ny >= 0 && ny < a.H && nz >= 0 && nz < a.D;
@@ -231,7 +239,19 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
         mbar_wait(&mbar[last & 1], (last >> 1) & 1);   // bounded: let MMAs in flight finish before freeing TMEM
     }
     tc_fence_after();
-    if (ok) {
+    if (ok && a.partial) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)c0, acc);
+            if (vin) {
+                float4* dst = reinterpret_cast<float4*>(a.partial + ((size_t)blockIdx.y * V + v) * COUT + c0);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+            }
+        }
+    } else if (ok) {
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 #pragma unroll
         for (int c0 = 0; c0 < COUT; c0 += 16) {
@@ -264,6 +284,34 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+// Finishes a split convolution: per voxel and 8 channels, the splits' partial sums in split order, then bias,
+// ReLU, the skip addition and the stores of k_conv3_tc's epilogue.
+template <int COUT>
+__global__ void k_conv_split_reduce(const float* __restrict__ partial, int splits, int V, const float* __restrict__ bias,
+                                    const __nv_bfloat16* __restrict__ skip, __nv_bfloat16* __restrict__ out,
+                                    float* __restrict__ out32, int relu) {
+    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (item >= (long long)V * (COUT / 8)) return;
+    const int v = (int)(item / (COUT / 8)), c0 = (int)(item % (COUT / 8)) * 8;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < splits; k++) {
+        const float4* src = reinterpret_cast<const float4*>(partial + ((size_t)k * V + v) * COUT + c0);
+        const float4 p0 = src[0], p1 = src[1];
+        acc[0] += p0.x; acc[1] += p0.y; acc[2] += p0.z; acc[3] += p0.w;
+        acc[4] += p1.x; acc[5] += p1.y; acc[6] += p1.z; acc[7] += p1.w;
+    }
+    __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float t = acc[j] + (bias ? bias[c0 + j] : 0.f);
+        if (relu) t = fmaxf(t, 0.f);
+        if (skip) t += __bfloat162float(skip[(size_t)v * COUT + c0 + j]);
+        o[j] = __float2bfloat16(t);
+        if (out32 && c0 + j == 0) out32[v] = t;
+    }
+    if (out) *reinterpret_cast<uint4*>(out + (size_t)v * COUT + c0) = *reinterpret_cast<const uint4*>(o);
 }
 
 // ============================================================================================================

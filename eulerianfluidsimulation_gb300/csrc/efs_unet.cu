@@ -58,6 +58,9 @@ struct Level {
 
 struct UNetState {
     int level = 0;               // hierarchy level the network works on (0: the context's grid)
+    int sm = 0;                  // SMs of the device (the split convolutions' target CTA count)
+    float* split = nullptr;      // FP32 partial sums of split convolutions
+    long long split_cap = 0;     // floats in split
     Level L[3];
     long long woff[kLayers], boff[kLayers], nparam = 0;
     float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
@@ -563,9 +566,36 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
     const Level& L = u->L[level];
     if (L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64)
         return conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st);
-    tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err};
+    tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0};
     const unsigned grid = (unsigned)((L.V + 127) / 128);
     (void)layer;
+    // Small grids (the coarse levels of the network, and the whole network on FCG's bottom grid) give too few
+    // CTAs, each running all 27 x cin/16 MMA steps in sequence: split the steps over more CTAs, then sum.
+    const int s_all = 27 * (cin / 16);
+    int ks = 1, per = s_all;
+    if (!pre && u->split && (int)grid < 2 * u->sm) {
+        ks = std::min(s_all, (2 * u->sm + (int)grid - 1) / (int)grid);
+        per = (s_all + ks - 1) / ks;
+        ks = (s_all + per - 1) / per;   // every split gets at least one step
+        if ((long long)ks * L.V * cout > u->split_cap) ks = 1;
+    }
+    if (ks > 1) {
+        a.partial = u->split;
+        a.split_per = per;
+        const dim3 g2(grid, (unsigned)ks);
+        if (cout == 16) tc::k_conv3_tc<16><<<g2, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+        else if (cout == 32) tc::k_conv3_tc<32><<<g2, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+        else tc::k_conv3_tc<64><<<g2, tc::kConvThreads, tc::kConvSmem, st>>>(a);
+        {
+            const cudaError_t ce = cudaGetLastError();
+            if (ce != cudaSuccess) return ce;
+        }
+        const unsigned rg = nblk(L.V * (cout / 8));
+        if (cout == 16) tc::k_conv_split_reduce<16><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
+        else if (cout == 32) tc::k_conv_split_reduce<32><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
+        else tc::k_conv_split_reduce<64><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
+        return cudaGetLastError();
+    }
     if (cout == 16) tc::k_conv3_tc<16><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
     else if (cout == 32) tc::k_conv3_tc<32><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
     else tc::k_conv3_tc<64><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
@@ -784,6 +814,11 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
         UCK(ualloc(u, &u->wb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
     }
     UCK(ualloc(u, &u->wh, 27LL * 64 * 64));
+    // split convolutions run on grids of fewer than 2 x SMs CTAs of 128 voxels, into at most 2 x SMs + CTAs more
+    // partial tiles: (2 x SMs + 2 x SMs) x 128 voxels x 64 channels bounds every layer
+    u->sm = c->sm_count > 0 ? c->sm_count : 152;
+    u->split_cap = 4LL * u->sm * 128 * 64;
+    UCK(ualloc(u, &u->split, u->split_cap));
     UCK(ualloc(u, &u->x0, L[0].V * 16));
     UCK(ualloc(u, &u->e0, L[0].V * 16));
     UCK(ualloc(u, &u->p0, L[1].V * 16));
