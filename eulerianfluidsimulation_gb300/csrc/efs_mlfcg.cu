@@ -466,11 +466,13 @@ __device__ __forceinline__ float lap4(unsigned f, float c, const float (&nb)[6])
 }
 
 // k_ml_smooth at level 0
+// (the level-0 kernels sum their few cells per thread in FP32, and the block and grid sums in FP64: GB300's FP64
+// pipe is a small fraction of its FP32 one)
 template <bool DOTS>
 __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ r,
                            const float* __restrict__ zin, float* __restrict__ zout, float omega,
                            const float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
-    double zq = 0, rz = 0;
+    float zq = 0.f, rz = 0.f;
     QWALK(qw, i) {
         unsigned f[4];
         float rv[4], out[4];
@@ -497,8 +499,8 @@ __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, i
             ld4(q, i, qv);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                zq += (double)out[k] * qv[k];
-                rz += (double)out[k] * rv[k];
+                zq += out[k] * qv[k];
+                rz += out[k] * rv[k];
             }
         }
     }
@@ -551,7 +553,7 @@ __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int 
                                const float* __restrict__ d, float* __restrict__ dn, float* __restrict__ q, FcgDev* s,
                                double* __restrict__ part) {
     const float beta = (float)s->beta;
-    double dq = 0;
+    float dq = 0.f;
     QWALK(qw, i) {
         unsigned f[4];
         float zc[4], zn[4][6], dc[4], dnb[4][6], dv[4], qv[4];
@@ -565,7 +567,7 @@ __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int 
 #pragma unroll
             for (int n = 0; n < 6; n++) nbv[n] = zn[k][n] + beta * dnb[k][n];
             qv[k] = (f[k] & 0x8000u) ? lap4(f[k], dv[k], nbv) : 0.f;
-            dq += (double)dv[k] * qv[k];
+            dq += dv[k] * qv[k];
         }
         st4(dn, i, dv);
         st4(q, i, qv);
@@ -587,7 +589,8 @@ __global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__
                            float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
                            cudaGraphConditionalHandle verify) {
     const double a = s->alpha;
-    double rr = 0;
+    const float af = (float)a;
+    float rr = 0.f;
     QWALK(qw, i) {
         float dv[4], rv[4], qv[4];
         ld4(dn, i, dv);
@@ -601,8 +604,8 @@ __global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__
         x2[1] = x23;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            rv[k] = (float)((double)rv[k] - a * (double)qv[k]);
-            rr += (double)rv[k] * rv[k];
+            rv[k] = rv[k] - af * qv[k];
+            rr += rv[k] * rv[k];
         }
         st4(r, i, rv);
         st4(d, i, dv);

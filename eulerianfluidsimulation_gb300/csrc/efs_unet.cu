@@ -573,8 +573,8 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
     // CTAs, each running all 27 x cin/16 MMA steps in sequence: split the steps over more CTAs, then sum.
     const int s_all = 27 * (cin / 16);
     int ks = 1, per = s_all;
-    if (!pre && u->split && (int)grid < 2 * u->sm) {
-        ks = std::min(s_all, (2 * u->sm + (int)grid - 1) / (int)grid);
+    if (!pre && u->split && (int)grid < 8 * u->sm) {
+        ks = std::min(s_all, (8 * u->sm + (int)grid - 1) / (int)grid);
         per = (s_all + ks - 1) / ks;
         ks = (s_all + per - 1) / per;   // every split gets at least one step
         if ((long long)ks * L.V * cout > u->split_cap) ks = 1;
@@ -814,10 +814,10 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
         UCK(ualloc(u, &u->wb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
     }
     UCK(ualloc(u, &u->wh, 27LL * 64 * 64));
-    // split convolutions run on grids of fewer than 2 x SMs CTAs of 128 voxels, into at most 2 x SMs + CTAs more
-    // partial tiles: (2 x SMs + 2 x SMs) x 128 voxels x 64 channels bounds every layer
+    // split convolutions run on grids of fewer than 8 x SMs CTAs of 128 voxels, into at most 8 x SMs + CTAs more
+    // partial tiles: (8 x SMs + 8 x SMs) x 128 voxels x 64 channels bounds every layer (the launch also checks)
     u->sm = c->sm_count > 0 ? c->sm_count : 152;
-    u->split_cap = 4LL * u->sm * 128 * 64;
+    u->split_cap = 16LL * u->sm * 128 * 64;
     UCK(ualloc(u, &u->split, u->split_cap));
     UCK(ualloc(u, &u->x0, L[0].V * 16));
     UCK(ualloc(u, &u->e0, L[0].V * 16));
