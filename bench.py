@@ -7,11 +7,13 @@ the reference's dam-break scene) with the pressure solved by CG to relative resi
 
 Lines printed (rank 0, one JSON object):
   --impl gb300 (default): `value` = steps/s with the fields resident in HBM (CUDA events on the library's
-      stream around K replayed step graphs); `e2e` = the same through efs_upload_fields / efs_step /
-      efs_download_fields with pinned host buffers every step; `roofline` for the pressure solve (the
-      dominant kernel); `cpu_baseline` = the CPU oracle (a port of the reference CPU step) on a bounded sample.
+      stream around K replayed step graphs); `e2e` = the same through efs_step_host with pinned host buffers
+      every step; `roofline` for the pressure solve (the dominant kernel); `jacobi` and `learned_pcg` = the same
+      scene stepped with Jacobi (100 sweeps) and with FCG and the committed trained network (steps/s,
+      iterations and solve ms per step); `cpu_baseline` = one whole CPU step of the oracle (a port of the
+      reference CPU step), measured.
   --impl reference: the reference's CPU step on the host cores (the oracle port; the reference's own sources
-      need its build tree) on the same workload, bounded sample.
+      need its build tree) on the same workload: one whole step, its pressure solve run to convergence.
 With --gpus N (torchrun), every rank advances its own replica (weak scaling; the step has no data exchange).
 """
 import argparse
@@ -48,12 +50,6 @@ SOLVE_DRAM_BYTES_PER_ROW_ITER = 68.23e9 / (950 * 3778175)
 STEP_BYTES_PER_CELL_3D = 693.0
 # The same for 2D (vel 8 B, 4 advection weights; the 2D diffusion runs 7 iterations x 2 axes).
 STEP_BYTES_PER_CELL_2D = 618.0
-# Mean CG iterations per step the CUDA path needs on this workload (measured by the gb300 arm over the first
-# steps of the dam break; printed in its JSON line as cg_iters_per_step).  The CPU-baseline sample times a
-# few CG iterations and scales them to this count instead of solving at 256^3 on one core for minutes.
-CG_ITERS_PER_STEP_REF = 934
-# The same for the other dam-break workloads the gb300 arm has measured (grid side, spheres) -> iterations/step.
-CG_ITERS_MEASURED = {(256, 16): 934, (128, 8): 459}
 
 
 def parse():
@@ -67,9 +63,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--dt", type=float, default=0.004)
     ap.add_argument("--solver", default=None, choices=["cg", "jacobi", "fcg"],
-                    help="fcg: learned U-Net preconditioner (trained first at --fcg-train-size, outside the timed region)")
-    ap.add_argument("--fcg-train-size", type=int, default=64)
-    ap.add_argument("--fcg-train-iters", type=int, default=2000)
+                    help="fcg: flexible PCG with the learned preconditioner (the committed trained network)")
+    ap.add_argument("--fcg-levels", type=int, default=0,
+                    help="unet workload: aggregation levels below the grid for the network (0: the whole grid; -1: FCG's "
+                         "bottom grid, timed after one V-cycle descent)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-alt", action="store_true", help="skip the Jacobi and learned-PCG comparison runs")
@@ -467,43 +464,21 @@ def unet_flops(n):
 
 
 def run_fcg(a):
-    """The learned-preconditioner line: FCG with the U-Net on the same 256^3 dam break.  The network is trained
-    first on the device (outside the timed region) on samples of other seeds at --fcg-train-size."""
+    """The learned-preconditioner line: FCG (multilevel preconditioner, the committed trained network as its
+    coarsest-level solve) on the same 256^3 dam break, each step one replayed graph."""
     import eulerianfluidsimulation_gb300 as gb
-    from eulerianfluidsimulation_gb300 import abi
+    from eulerianfluidsimulation_gb300 import abi, unet_weights
     rank, world, local = dist_env()
     if rank != 0:
         return
-    n, nt = a.size, a.fcg_train_size
-    prm_t = abi.params_dam(1.0 / nt, a.dt, abi.SOLVER_CG, 1e-6)
-    prm_t.max_steps = 20000
-    T = gb.GB300Simulator3D(nt, nt, nt, prm_t)
-    T.unet_init(a.seed + 7, 48)
-    t0 = time.perf_counter()
-    for sd in (a.seed + 1, a.seed + 2):
-        bt, rt = gb.scene_dam3d(nt, nt, nt, a.spheres, a.spheres, sd)
-        T.reset()
-        T.set_field(abi.FIELD_BOUNDARY, bt)
-        T.set_field(abi.FIELD_RHO, rt)
-        for _ in range(24):
-            T.update(1)
-            T.unet_add_sample()
-    T.synchronize()
-    t1 = time.perf_counter()
-    loss0 = T.unet_train(1, 8, 1e-3, 0.5, 1, loss_kind=1)
-    loss = T.unet_train(a.fcg_train_iters, 4, 1e-3, 0.5, 2, loss_kind=1)
-    t2 = time.perf_counter()
-    W = T.unet_weights()
-    T.close()
-
+    n = a.size
     prm = workload(a)
     prm.solver = abi.SOLVER_FCG_UNET
     b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
     sim = gb.GB300Simulator3D(n, n, n, prm)
     sim.set_field(abi.FIELD_BOUNDARY, b)
     sim.set_field(abi.FIELD_RHO, r)
-    sim.unet_init(0, 0)
-    sim.unet_set_weights(W)
+    net = unet_weights.load_into(sim)
     for _ in range(a.warmup):
         sim.update(1)
     sim.synchronize()
@@ -534,8 +509,9 @@ def run_fcg(a):
     # the dominant kernel: the implicit-GEMM convolutions of one forward pass, timed on the device
     sim.set_params(prm)
     ms_fwd, ms_layers = sim.unet_time_forward(3)
+    nw = sim.unet_grid()[0]
     sim.close()
-    flops = unet_flops(n)
+    flops = unet_flops(nw)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -551,7 +527,8 @@ def run_fcg(a):
                 "ms_per_layer": [round(float(x), 4) for x in ms_layers]}
     steps_per_s = a.steps / (ms / 1e3)
     cfg = config(a)
-    cfg["solver"] = "fcg_unet rel-res 1e-6 (flexible PCG, U-Net 16/32/64 BF16, FP64 x, CG fallback on stall)"
+    cfg["solver"] = ("fcg_unet rel-res 1e-6 (flexible PCG, multigrid V-cycle with the U-Net 16/32/64 BF16 as its "
+                     "coarsest-level solve, FP64 x, CG fallback on stall)")
     line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": 1, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
@@ -560,9 +537,7 @@ def run_fcg(a):
             "fcg_converged": bool(st1.converged),
             "plain_cg_same_trajectory": {"iters_per_step": (sc1.total_solve_steps - sc0.total_solve_steps) / 3,
                                          "ms_per_step": ms_cg},
-            "training": {"grid": [nt] * 3, "samples": 48, "scenes": 2, "iterations": a.fcg_train_iters, "batch": 4,
-                         "loss": "energy-norm alignment", "synthetic_fraction": 0.5, "loss_first": loss0,
-                         "loss_last": loss, "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)},
+            "network": net,
             "roofline": roofline, "clocks": clocks, "cpu_baseline": None, "e2e": None}
     print(json.dumps(line), flush=True)
 
@@ -805,16 +780,19 @@ def run_unet(a):
         return
     n = a.size
     b, r = gb.scene_dam3d(n, n, n, a.spheres, a.spheres, a.seed)
-    sim = gb.GB300Simulator3D(n, n, n, workload(a))
+    prm = workload(a)
+    prm.fcg_levels = a.fcg_levels       # 0: the network on the whole grid; < 0: on FCG's bottom grid
+    sim = gb.GB300Simulator3D(n, n, n, prm)
     sim.set_field(abi.FIELD_BOUNDARY, b)
     sim.set_field(abi.FIELD_RHO, r)
     sim.update(1)
     sim.unet_init(a.seed + 7, 0)
+    nw, nh, nd, level = sim.unet_grid()
     with Clocks(local) as clk:
         ms_fwd, ms_layers = sim.unet_time_forward(max(1, a.steps))
     clocks = clk.summary()
     sim.close()
-    flops = unet_flops(n)
+    flops = unet_flops(nw)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -826,10 +804,11 @@ def run_unet(a):
     per_layer = [{"layer": k, "cin_cout": list(UNET_LAYERS[k][:2]), "level": UNET_LAYERS[k][2], "ms": float(ms_layers[k]),
                   "TFLOP/s": flops[k] / (float(ms_layers[k]) / 1e3) / 1e12 if ms_layers[k] > 0 else None}
                  for k in range(len(UNET_LAYERS))]
-    line = {"metric": f"U-Net forward TFLOP/s at {n}^3 (implicit-GEMM tcgen05 convolutions)", "value": achieved,
+    line = {"metric": f"U-Net forward TFLOP/s at {nw}^3 (implicit-GEMM tcgen05 convolutions)", "value": achieved,
             "unit": "TFLOP/s", "n_gpus": 1, "steps": max(1, a.steps), "warmup": 1, "ms_per_step": ms_fwd,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"unet_{n}", "channels": [16, 32, 64], "levels": 3, "kernel": "3x3x3"},
+            "config": {"workload": f"unet_{n}", "network_grid": [nw, nh, nd], "hierarchy_level": level,
+                       "channels": [16, 32, 64], "levels": 3, "kernel": "3x3x3"},
             "layers": per_layer,
             "roofline": {"kernel": "k_conv3_tc (6 convolutions of one forward pass)", "bound": "tensor",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
