@@ -307,7 +307,7 @@ def alt_solver_line(a, kind, b, r, cg_ms_step, cg_solve_ms, cg_iters):
                                                             f[abi.FIELD_RHO], f[abi.FIELD_BOUNDARY])
             out["note"] = "Jacobi does not reach rel-res 1e-6; it runs its fixed 100 sweeps (the reference's Jacobi)"
         else:
-            out["precond_iters_per_step"] = (st1.precond_steps - st0.precond_steps) / k
+            out["precond_iters_last_solve"] = st1.precond_steps
             out["network"] = info
         out["vs_plain_cg"] = {"step_speedup": cg_ms_step / out["ms_per_step"],
                               "solve_speedup": (cg_solve_ms / out["solve_ms_per_step"]) if out["solve_ms_per_step"] else None,
