@@ -169,10 +169,6 @@ struct efs_ctx {
     cudaEvent_t ev_projected = nullptr;   // recorded after project_pre: the divergence is final
     cudaEvent_t ev_early = nullptr;         // the first stages' inputs are on the device
     float* fstage = nullptr;                // efs_step_host: staging of the forces (dim floats a cell)
-    // TMA tensor maps of the velocity-extrapolation ping-pong fields (u, v, w, validA, then the tvel thirds and
-    // validB; CUtensorMap is 64-byte aligned, 128 bytes each), built on first use; state -1 unknown, 0 not used
-    alignas(64) unsigned char extrap_maps[8 * 128] = {};
-    int extrap_tma = -1;
 };
 
 namespace efs {

@@ -11,12 +11,7 @@
 // Density sharpening applies every cell's change, then traces every changed cell on that field, then
 // scatters (EFS_SHARPEN_PARALLEL); the reference interleaves the three per cell, which
 // EFS_SHARPEN_SEQUENTIAL reproduces on one thread for parity.
-#include <cstdlib>
-#include <cstring>
 #include <mutex>
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
 
 #include "efs_batch.h"
 #include "efs_internal.h"
@@ -122,120 +117,6 @@ __global__ void k_extrap_pass(Geo g, const float* __restrict__ su, const float* 
                               float* __restrict__ dv, float* __restrict__ dw, uint8_t* __restrict__ dV,
                               const uint8_t* __restrict__ solid, int settled) {
     d_extrap_pass<DIM>(g, blockIdx.x, blockIdx.y, blockIdx.z, su, sv, sw, sV, du, dv, dw, dV, solid, settled != 0);
-}
-
-// The same pass (3D) with each CTA's inputs staged in shared memory by TMA: one 3D tensor load per source field
-// of an output tile of 32 x 8 x 4 cells with a one-cell halo, waited on through one mbarrier, then every cell's
-// six neighbours read from shared memory.  Each cell's arithmetic and the order of its neighbour sums are those
-// of d_extrap_pass, so the results are identical.  The x start of a box is rounded down to a 16-byte boundary
-// (floats from x0 - 4, 40 wide; validity bytes from x0 - 16, 64 wide); loads outside the grid read zeros.
-constexpr int kEXT = 32, kEYT = 8, kEZT = 4;
-constexpr int kEFX = kEXT + 8, kEFY = kEYT + 2, kEFZ = kEZT + 2;     // float box 40 x 10 x 6
-constexpr int kEMX = kEXT + 32;                                      // validity box 64 x 10 x 6
-constexpr int kEFBox = kEFX * kEFY * kEFZ, kEMBox = kEMX * kEFY * kEFZ;
-constexpr int kExtrapSmem = 3 * kEFBox * 4 + kEMBox + 16;
-constexpr unsigned long long kExtrapWaitNs = 2000000000ull;          // a wait gives up after 2 s
-
-struct ExtrapTmaArgs {
-    CUtensorMap mu, mv, mw, mV;
-    Geo g;
-    float *du, *dv, *dw;
-    uint8_t* dV;
-    const uint8_t* solid;
-    int settled;
-    DevCtl* ctl;
-};
-
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ bool ex_mbar_test(uint64_t* bar, uint32_t parity) {
-    uint32_t done;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(done) : "r"(su32(bar)), "r"(parity) : "memory");
-    return done != 0;
-}
-__device__ __forceinline__ bool ex_mbar_wait(uint64_t* bar, uint32_t parity) {
-    if (ex_mbar_test(bar, parity)) return true;
-    unsigned long long t0, t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-    while (!ex_mbar_test(bar, parity)) {
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > kExtrapWaitNs) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void ex_tma3(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
-    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-                 ::"r"(su32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(su32(bar)) : "memory");
-}
-
-__global__ void __launch_bounds__(256) k_extrap_pass_tma(const __grid_constant__ ExtrapTmaArgs a) {
-    extern __shared__ __align__(128) unsigned char esm[];
-    float* tu = reinterpret_cast<float*>(esm);
-    float* tv = tu + kEFBox;
-    float* tw = tv + kEFBox;
-    uint8_t* tV = esm + 3 * kEFBox * 4;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(esm + 3 * kEFBox * 4 + kEMBox);
-    const int x0 = blockIdx.x * kEXT, y0 = blockIdx.y * kEYT, z0 = blockIdx.z * kEZT;
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
-                     "r"((unsigned)(3 * kEFBox * 4 + kEMBox)) : "memory");
-        ex_tma3(tu, &a.mu, x0 - 4, y0 - 1, z0 - 1, bar);
-        ex_tma3(tv, &a.mv, x0 - 4, y0 - 1, z0 - 1, bar);
-        ex_tma3(tw, &a.mw, x0 - 4, y0 - 1, z0 - 1, bar);
-        ex_tma3(tV, &a.mV, x0 - 16, y0 - 1, z0 - 1, bar);
-    }
-    if (!ex_mbar_wait(bar, 0)) {
-        // give up on this tile: flag it, and wait (bounded) for the copies in flight before leaving
-        if (threadIdx.x == 0) atomicOr(&a.ctl->error, DEV_ERR_BARRIER_TIMEOUT);
-        ex_mbar_wait(bar, 0);
-        return;
-    }
-    const Geo& g = a.g;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int x = x0 + tx, y = y0 + ty;
-    if (x < 1 || x > g.W - 2 || y < 1 || y > g.H - 2) return;
-#pragma unroll
-    for (int tz = 0; tz < kEZT; tz++) {
-        const int z = z0 + tz;
-        if (z < 1 || z > g.D - 2) continue;
-        const int i = z * g.WH + y * g.W + x;
-        const int f = ((tz + 1) * kEFY + (ty + 1)) * kEFX + (tx + 4);
-        const int m = ((tz + 1) * kEFY + (ty + 1)) * kEMX + (tx + 16);
-        if (a.solid[i]) {
-            if (a.settled) continue;
-            a.du[i] = tu[f]; a.dv[i] = tv[f]; a.dw[i] = tw[f];
-            a.dV[i] = 0;
-            continue;
-        }
-        if (tV[m]) {
-            if (a.settled && a.dV[i]) continue;
-            a.du[i] = tu[f]; a.dv[i] = tv[f]; a.dw[i] = tw[f];
-            a.dV[i] = 1;
-            continue;
-        }
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f, n = 0;
-        const int fo[6] = {-1, 1, -kEFX, kEFX, -kEFX * kEFY, kEFX * kEFY};
-        const int mo[6] = {-1, 1, -kEMX, kEMX, -kEMX * kEFY, kEMX * kEFY};
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-            if (tV[m + mo[k]]) {
-                s0 += tu[f + fo[k]]; s1 += tv[f + fo[k]]; s2 += tw[f + fo[k]];
-                n++;
-            }
-        }
-        if (n > 0) {
-            a.du[i] = s0 / n; a.dv[i] = s1 / n; a.dw[i] = s2 / n;
-        } else {
-            if (a.settled) continue;
-            a.du[i] = tu[f]; a.dv[i] = tv[f]; a.dw[i] = tw[f];
-        }
-        a.dV[i] = (n > 0) ? 1 : 0;
-    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1240,75 +1121,20 @@ static cudaError_t stage_decay(efs_ctx* c) {
     return cudaSuccess;
 }
 
-// The tensor maps of the TMA extrapolation pass (3D grids whose width is a multiple of 16, so that every row
-// pitch is a multiple of 16 bytes for floats and bytes).  EFS_EXTRAP_TMA=0 in the environment keeps the plain
-// kernel.  Returns whether the TMA pass is used.
-static bool extrap_tma_ready(efs_ctx* c) {
-    if (c->extrap_tma >= 0) return c->extrap_tma == 1;
-    c->extrap_tma = 0;
-    const char* env = std::getenv("EFS_EXTRAP_TMA");
-    if (env && env[0] == '0') return false;
-    const Geo& g = c->g;
-    if (c->dim != 3 || (g.W % 16) != 0) return false;
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess || !fn)
-        return false;
-    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(c->extrap_maps);
-    const float* fsrc[6] = {c->u, c->v, c->w, c->tvel, c->tvel + g.N, c->tvel + 2 * (size_t)g.N};
-    const uint8_t* vsrc[2] = {c->validA, c->validB};
-    const cuuint64_t dims[3] = {(cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.D};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    for (int side = 0; side < 2; side++) {
-        for (int k = 0; k < 3; k++) {
-            const cuuint64_t str[2] = {(cuuint64_t)g.W * 4, (cuuint64_t)g.WH * 4};
-            const cuuint32_t box[3] = {(cuuint32_t)kEFX, (cuuint32_t)kEFY, (cuuint32_t)kEFZ};
-            if (encode(&maps[4 * side + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)fsrc[3 * side + k], dims, str, box,
-                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-                return false;
-        }
-        const cuuint64_t str[2] = {(cuuint64_t)g.W, (cuuint64_t)g.WH};
-        const cuuint32_t box[3] = {(cuuint32_t)kEMX, (cuuint32_t)kEFY, (cuuint32_t)kEFZ};
-        if (encode(&maps[4 * side + 3], CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void*)vsrc[side], dims, str, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return false;
-    }
-    c->extrap_tma = 1;
-    return true;
-}
-
 static cudaError_t stage_extrapolate(efs_ctx* c) {
     const Geo& g = c->g;
     float* tu = c->tvel; float* tv = c->tvel + g.N; float* tw = c->tvel + 2 * (size_t)g.N;
     k_extrap_init<<<grid_linear(g.N, 256), 256, 0, c->stream>>>(g, c->dim, c->rho, c->solid, c->validA);
     EFS_LAUNCH_CHECK();
     const dim3 b(BX, BY), gr = grid_interior(g, c->dim);
-    const bool tma = extrap_tma_ready(c);
-    const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(c->extrap_maps);
-    const dim3 gt((g.W + kEXT - 1) / kEXT, (g.H + kEYT - 1) / kEYT, (g.D + kEZT - 1) / kEZT);
     for (int it = 0; it < 6; it++) {
         const bool odd = it & 1;
         const float* su = odd ? tu : c->u; const float* sv = odd ? tv : c->v; const float* sw = odd ? tw : c->w;
         float* du = odd ? c->u : tu; float* dv = odd ? c->v : tv; float* dw = odd ? c->w : tw;
         const uint8_t* sV = odd ? c->validB : c->validA;
         uint8_t* dV = odd ? c->validA : c->validB;
-        if (tma) {
-            ExtrapTmaArgs a;
-            std::memcpy(&a.mu, &maps[4 * (odd ? 1 : 0) + 0], sizeof(CUtensorMap));
-            std::memcpy(&a.mv, &maps[4 * (odd ? 1 : 0) + 1], sizeof(CUtensorMap));
-            std::memcpy(&a.mw, &maps[4 * (odd ? 1 : 0) + 2], sizeof(CUtensorMap));
-            std::memcpy(&a.mV, &maps[4 * (odd ? 1 : 0) + 3], sizeof(CUtensorMap));
-            a.g = g; a.du = du; a.dv = dv; a.dw = dw; a.dV = dV; a.solid = c->solid; a.settled = it >= 1; a.ctl = c->ctl;
-            k_extrap_pass_tma<<<gt, 256, kExtrapSmem, c->stream>>>(a);
-        } else if (c->dim == 3) {
-            k_extrap_pass<3><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
-        } else {
-            k_extrap_pass<2><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
-        }
+        if (c->dim == 3) k_extrap_pass<3><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
+        else k_extrap_pass<2><<<gr, b, 0, c->stream>>>(g, su, sv, sw, sV, du, dv, dw, dV, c->solid, it >= 1);
         EFS_LAUNCH_CHECK();
     }
     return cudaSuccess;
