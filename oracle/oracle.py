@@ -112,6 +112,8 @@ def _load_ref():
         lib.ref_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.ref_stage.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.ref_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(EfsStats)]
+        lib.ref_query_box.restype = ctypes.c_longlong
+        lib.ref_query_box.argtypes = [ctypes.c_void_p, _FP, _FP, ctypes.c_int, _FP]
         _ref = lib
     return _ref
 
@@ -274,6 +276,16 @@ class RefOracle(_Base):
         s = EfsStats()
         self._lib.ref_stats(self._h, ctypes.byref(s))
         return s
+
+    def query_box(self, position, scale, only_fluid=True):
+        """QueryNode::update's metric loop (the reference's own lines) on this 3D grid -> (metrics, count)."""
+        pos = np.asarray(position, np.float32)
+        scl = np.asarray(scale, np.float32)
+        out = np.zeros(13, np.float32)
+        n = self._lib.ref_query_box(self._h, _fptr(pos), _fptr(scl), int(only_fluid), _fptr(out))
+        m = {"max_position": out[0:3].copy(), "min_position": out[3:6].copy(), "avg_position": out[6:9].copy(),
+             "velocity": out[9:12].copy(), "pressure": float(out[12])}
+        return m, int(n)
 
 
 def mesh_label(shape, triangles, center, size, value_inside=1.0, value_outside=0.0, out=None):

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <cmath>
 #include <cfloat>
+#include <limits>
 
 #include "simulation/Properties.h"
 #include "simulation/data/StorageBuffer.h"
@@ -154,5 +155,27 @@ void ref_stats(void* h, efs_stats* s) {
 }
 
 void ref_clear_paused(void) { SET_PROPERTY_B(PAUSED, false); SET_PROPERTY_I(SOLVE_STEPS, 0); }
+
+// QueryNode::update's metric loop (src/simulation/scene/nodes/QueryNode.cpp:52-81) on this simulator's 3D grid:
+// the reference's own lines, cut from its source file by oracle/Makefile into _ref/query_loop.inc and compiled
+// here with the names they use (position, scale, _only_fluid, grid, w, h, d).  QueryNode.cpp itself cannot be
+// compiled: its scene-node headers need GL, JSON and UI types.  out: max, min, avg position, velocity (3 each),
+// pressure; returns the count.
+long long ref_query_box(void* handle, const float* pos, const float* scl, int only_fluid, float* out) {
+    RefSim* r = static_cast<RefSim*>(handle);
+    IGrid3D* grid = r->g3;
+    const glm::vec3 position(pos[0], pos[1], pos[2]);
+    const glm::vec3 scale(scl[0], scl[1], scl[2]);
+    const bool _only_fluid = only_fluid != 0;
+    const int w = r->w;
+    const int h = r->h;
+    const int d = r->d;
+#include "query_loop.inc"
+    const glm::vec3 res[4] = {maxPos, minPos, avgPos, vel};
+    for (int k = 0; k < 4; k++)
+        for (int c = 0; c < 3; c++) out[3 * k + c] = res[k][c];
+    out[12] = pres;
+    return count;
+}
 
 }  // extern "C"

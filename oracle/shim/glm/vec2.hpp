@@ -40,6 +40,14 @@ inline vec3 operator*(float s, const vec3& a) { return vec3(s * a.x, s * a.y, s 
 inline vec3 operator/(const vec3& a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
 inline float length(const vec3& v) { float t0 = v.x * v.x, t1 = v.y * v.y, t2 = v.z * v.z; return std::sqrt(t0 + t1 + t2); }
 
+// component-wise glm::max / glm::min (x < y ? y : x and y < x ? y : x per component)
+inline vec3 max(const vec3& a, const vec3& b) {
+    return vec3(a.x < b.x ? b.x : a.x, a.y < b.y ? b.y : a.y, a.z < b.z ? b.z : a.z);
+}
+inline vec3 min(const vec3& a, const vec3& b) {
+    return vec3(b.x < a.x ? b.x : a.x, b.y < a.y ? b.y : a.y, b.z < a.z ? b.z : a.z);
+}
+
 struct vec4 { float x, y, z, w; };
 struct mat4 { float m[16]; };
 static_assert(sizeof(vec2) == 8 && sizeof(vec3) == 12, "glm vectors are packed floats");

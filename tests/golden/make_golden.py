@@ -8,7 +8,10 @@ needs the reference tree) on small seeded scenes and stores, per case:
 plus the parameters used.  Sizes are chosen so the reference's 32-bit advection-matrix key cannot wrap
 (3D: cells^2 < 2^32; 2D: side <= 256).
 
-Usage: python tests/golden/make_golden.py      (writes ref_3d_cg.npz, ref_2d_jacobi.npz, ref_2d_cg.npz)
+Also ``ref_query.npz``: the reference's QueryNode metric loop (its own lines, compiled into the reference build by
+oracle/Makefile) on a stepped 32^3 state, for a set of boxes.
+
+Usage: python tests/golden/make_golden.py      (writes ref_3d_cg.npz, ref_2d_jacobi.npz, ref_2d_cg.npz, ref_query.npz)
 """
 import os
 import sys
@@ -69,9 +72,41 @@ def make(name):
     print(path, os.path.getsize(path), "bytes")
 
 
+# QueryNode metric boxes (position, scale, only_fluid) on a 32^3 dam break after 6 steps: the whole grid, a box in
+# the liquid, one crossing the far faces (clipped), one at negative coordinates, one without liquid, the whole grid
+# counting every cell, and an empty box
+QUERIES = [((0, 0, 0), (32, 32, 32), 1), ((2, 2, 2), (8, 10, 12), 1), ((6, 1, 20), (40, 40, 40), 1),
+           ((-3, -2, -5), (10, 12, 9), 1), ((28, 28, 28), (3, 3, 3), 1), ((0, 0, 0), (32, 32, 32), 0),
+           ((5, 5, 5), (0, 4, 4), 0)]
+
+
+def make_query():
+    """ref_query.npz: the reference's own QueryNode metric loop (compiled into the reference build) on a stepped
+    3D state, for each box of QUERIES."""
+    n = 32
+    prm = case_params(3, n, abi.SOLVER_CG, 0.004, 1e-6)
+    b, r = scene(3, n, 8, seed=2)
+    ref = oracle.RefOracle(3, n, n, n, prm)
+    ref.set_field(abi.FIELD_BOUNDARY, b)
+    ref.set_field(abi.FIELD_RHO, r)
+    ref.step(6)
+    out = {"rho": ref.field(abi.FIELD_RHO), "vel": ref.field(abi.FIELD_VEL), "pressure": ref.field(abi.FIELD_PRESSURE),
+           "queries": np.array([list(p) + list(s) + [f] for p, s, f in QUERIES], np.int32)}
+    res = []
+    for p, s, f in QUERIES:
+        m, cnt = ref.query_box(p, s, bool(f))
+        res.append(np.concatenate([m["max_position"], m["min_position"], m["avg_position"], m["velocity"],
+                                   [m["pressure"], cnt]]).astype(np.float64))
+    out["results"] = np.array(res)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_query.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     oracle.build(reference=True)
     if not oracle.reference_available():
         sys.exit("the reference tree is needed to generate golden fixtures")
     for n in CASES:
         make(n)
+    make_query()
