@@ -5,10 +5,8 @@
 
 #include "simulation/Properties.h"
 
-namespace {
-
 // The Properties values the step reads (include/simulation/Properties.h:141-162, 186-192), as efs_params.
-efs_params params_from_properties() {
+efs_params GB300ParamsFromProperties() {
     efs_params p;
     efs_params_default(&p);
     p.dt = PROPERTY_F(DT);
@@ -37,6 +35,8 @@ efs_params params_from_properties() {
     p.re_calc_div = PROPERTY_B(RE_CALC_DIV) ? 1 : 0;
     return p;
 }
+
+namespace {
 
 void report(efs_ctx* ctx, int status, const char* what) {
     if (status != EFS_OK) std::fprintf(stderr, "GB300 backend: %s failed: %s\n", what, efs_last_error(ctx));
@@ -83,7 +83,7 @@ GB300Simulator3D::GB300Simulator3D(unsigned int width, unsigned int height, unsi
     : ISimulator3D(width, height, depth) {
     availableSolvers(std::vector({Properties::SELF_CG, Properties::JACOBI}));
     _grid = new GB300Grid3D(width, height, depth);
-    const efs_params p = params_from_properties();
+    const efs_params p = GB300ParamsFromProperties();
     report(nullptr, efs_create(3, (int)width, (int)height, (int)depth, &p, &_ctx), "efs_create");
     _data = new SimulationDisplay3D::RenderData3D;
     _data->grid = _grid;
@@ -99,7 +99,7 @@ void* GB300Simulator3D::getRenderData() { return _data; }
 const char* GB300Simulator3D::lastError() const { return _ctx ? efs_last_error(_ctx) : efs_last_error(nullptr); }
 
 void GB300Simulator3D::syncParams() {
-    const efs_params p = params_from_properties();
+    const efs_params p = GB300ParamsFromProperties();
     report(_ctx, efs_set_params(_ctx, &p), "efs_set_params");
 }
 
@@ -165,7 +165,7 @@ void GB300Simulator3D::project() { stage(EFS_STAGE_PROJECT); }
 GB300Simulator2D::GB300Simulator2D(unsigned int width, unsigned int height) : ISimulator2D(width, height) {
     availableSolvers(std::vector({Properties::SELF_CG, Properties::JACOBI}));
     _grid = new GB300Grid2D(width, height);
-    const efs_params p = params_from_properties();
+    const efs_params p = GB300ParamsFromProperties();
     report(nullptr, efs_create(2, (int)width, (int)height, 1, &p, &_ctx), "efs_create");
     _data = new SimulationDisplay2D::RenderData2D();
     _data->grid = _grid;
@@ -181,7 +181,7 @@ void* GB300Simulator2D::getRenderData() { return _data; }
 const char* GB300Simulator2D::lastError() const { return _ctx ? efs_last_error(_ctx) : efs_last_error(nullptr); }
 
 void GB300Simulator2D::syncParams() {
-    const efs_params p = params_from_properties();
+    const efs_params p = GB300ParamsFromProperties();
     report(_ctx, efs_set_params(_ctx, &p), "efs_set_params");
 }
 

@@ -21,6 +21,10 @@
 
 #include "efs_gb300.h"
 
+// The Properties values the step reads (Properties.h:141-162, 186-192) as the C ABI's parameters: what every
+// update() and stage call passes to the device backend.
+efs_params GB300ParamsFromProperties();
+
 // Host mirrors of the device fields; the accessors hand out the mirrors as the reference's grids do.
 class GB300Grid3D final : public IGrid3D {
 public:

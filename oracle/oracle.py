@@ -53,6 +53,44 @@ def reference_available():
     return os.path.exists(LIBREF)
 
 
+def dropin_driver():
+    """Build _ref/dropin_driver (tests/dropin_driver.cpp: the C++ drop-in backend and the reference's
+    CPUSimulator3D behind its ISimulator3D interface) and return its path.  Needs the reference tree and
+    libefs_gb300.so."""
+    build(reference=True)
+    subprocess.check_call(["make", "-s", "-C", HERE, "dropin", "REF=" + reference_tree()])
+    return os.path.join(HERE, "_ref", "dropin_driver")
+
+
+def dropin_reference(n, frames):
+    """The reference's CPUSimulator3D::update() for `frames` frames on the driver's seeded n^3 dam break, with
+    the Properties set as the application does: {"steps", "paused"} per frame, "params" (the efs_params the C++
+    drop-in derives from those Properties) and the fields after the last frame, keyed by field id."""
+    import tempfile
+    from eulerianfluidsimulation_gb300 import abi
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "ref.bin")
+        subprocess.check_call([dropin_driver(), "reference", str(n), str(frames), out])
+        raw = open(out, "rb").read()
+    head = np.frombuffer(raw[:8], np.int32)
+    assert head[0] == n and head[1] == frames
+    off = 8
+    steps = np.frombuffer(raw[off:off + 4 * frames], np.int32).copy()
+    off += 4 * frames
+    paused = np.frombuffer(raw[off:off + 4 * frames], np.int32).copy()
+    off += 4 * frames
+    psize = ctypes.sizeof(EfsParams)
+    prm = EfsParams.from_buffer_copy(raw[off:off + psize])
+    off += psize
+    N = n * n * n
+    fl = np.frombuffer(raw[off:], np.float32)
+    assert fl.size == 8 * N
+    fields = {abi.FIELD_VEL: fl[:3 * N].reshape(n, n, n, 3).copy()}
+    for k, f in enumerate((abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA, abi.FIELD_DIVERGENCE, abi.FIELD_PRESSURE)):
+        fields[f] = fl[(3 + k) * N:(4 + k) * N].reshape(n, n, n).copy()
+    return {"steps": steps, "paused": paused, "params": prm, "fields": fields}
+
+
 _orc = None
 _ref = None
 _FP = ctypes.POINTER(ctypes.c_float)

@@ -11,7 +11,11 @@ plus the parameters used.  Sizes are chosen so the reference's 32-bit advection-
 Also ``ref_query.npz``: the reference's QueryNode metric loop (its own lines, compiled into the reference build by
 oracle/Makefile) on a stepped 32^3 state, for a set of boxes.
 
-Usage: python tests/golden/make_golden.py      (writes ref_3d_cg.npz, ref_2d_jacobi.npz, ref_2d_cg.npz, ref_query.npz)
+Also ``ref_dropin_dam32.npz``: the reference's CPUSimulator3D driven through its ISimulator3D interface by
+tests/dropin_driver.cpp (oracle/Makefile's ``dropin`` target, which needs libefs_gb300.so built first).
+
+Usage: python tests/golden/make_golden.py      (writes ref_3d_cg.npz, ref_2d_jacobi.npz, ref_2d_cg.npz, ref_query.npz,
+                                                ref_dropin_dam32.npz)
 """
 import os
 import sys
@@ -103,6 +107,26 @@ def make_query():
     print(path, os.path.getsize(path), "bytes")
 
 
+# the C++ drop-in's comparison case: tests/dropin_driver.cpp's seeded 32^3 dam break (4 spheres, seed 3), frames
+DROPIN = (32, 4)
+
+
+def make_dropin():
+    """ref_dropin_dam32.npz: the reference's CPUSimulator3D::update(), called through its ISimulator3D interface
+    with the Properties set as the application sets them (tests/dropin_driver.cpp), for DROPIN frames; SOLVE_STEPS
+    and PAUSED after each frame, the efs_params the C++ drop-in backend derives from the same Properties, and the
+    fields after the last frame."""
+    n, frames = DROPIN
+    r = oracle.dropin_reference(n, frames)
+    out = {"params": np.frombuffer(bytes(r["params"]), np.uint8).copy(), "steps": r["steps"], "paused": r["paused"],
+           "meta": np.array([n, frames, 4, 4, 3])}
+    for f, a in r["fields"].items():
+        out[f"field_{f}"] = a
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_dropin_dam32.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     oracle.build(reference=True)
     if not oracle.reference_available():
@@ -110,3 +134,4 @@ if __name__ == "__main__":
     for n in CASES:
         make(n)
     make_query()
+    make_dropin()

@@ -89,3 +89,48 @@ def test_drop_in_backend_builds_against_reference_headers():
               ["-L", os.path.join(ROOT, "eulerianfluidsimulation_gb300"), "-lefs_gb300"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         assert res.returncode == 0, res.stderr[-2000:]
+
+
+def _dropin_expected(n):
+    """The efs_params the C++ drop-in must derive from tests/dropin_driver.cpp's Properties (an n^3 dam break
+    with the reference's CG): the reference semantics of the solver (absolute r.r threshold, float dot products)
+    and velocity decay disabled."""
+    from eulerianfluidsimulation_gb300 import abi
+    p = abi.params_dam(1.0 / n, 0.004, abi.SOLVER_CG, 1e-5)
+    p.tol_rel = 0.0
+    p.cg_variant = abi.CG_REFERENCE
+    p.max_steps = 2000
+    p.disable_mask = 1 << abi.STAGE_VEL_DECAY
+    return p
+
+
+def test_dropin_fixture_params_are_the_adapter_mapping():
+    """ref_dropin_dam32.npz holds the efs_params GB300ParamsFromProperties() returned beside the reference's run."""
+    import numpy as np
+    from eulerianfluidsimulation_gb300 import abi
+    from tests.helpers import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "ref_dropin_dam32.npz"))
+    got = abi.EfsParams.from_buffer_copy(z["params"].tobytes()).as_dict()
+    assert got == _dropin_expected(int(z["meta"][0])).as_dict()
+    assert not z["paused"].any() and (z["steps"] > 0).all()
+
+
+@pytest.mark.skipif(not oracle.reference_tree_present(), reason="reference tree not present")
+def test_dropin_driver_runs_the_adapter():
+    """tests/dropin_driver.cpp, built against the reference's headers and its CPU build: the Properties the
+    application sets map to the expected efs_params, and without a CUDA device GB300Simulator3D reports the
+    backend's error instead of stepping (the reference-side construction and update() calls still run)."""
+    _lib()
+    exe = oracle.dropin_driver()
+    res = subprocess.run([exe, "params"], capture_output=True, text=True, timeout=60)
+    assert res.returncode == 0, res.stderr
+    got = dict(kv.split("=") for kv in res.stdout.split())
+    want = _dropin_expected(64).as_dict()
+    for k, v in got.items():
+        assert float(v) == pytest.approx(float(want[k]), rel=1e-7), (k, v, want[k])
+    assert set(got) <= set(want)
+    import torch
+    if not torch.cuda.is_available():
+        res = subprocess.run([exe, "run", "32", "2"], capture_output=True, text=True, timeout=120)
+        assert res.returncode == 0, res.stderr
+        assert res.stdout.startswith("no-device"), res.stdout
