@@ -309,6 +309,8 @@ def alt_solver_line(a, kind, b, r, cg_ms_step, cg_solve_ms, cg_iters):
         else:
             out["precond_iters_last_solve"] = st1.precond_steps
             out["network"] = info
+            direct, graph = sim.fcg_time_vcycle(5)
+            out["preconditioner_ms"] = {"kernel_by_kernel": direct, "graph_replay": graph}
         out["vs_plain_cg"] = {"step_speedup": cg_ms_step / out["ms_per_step"],
                               "solve_speedup": (cg_solve_ms / out["solve_ms_per_step"]) if out["solve_ms_per_step"] else None,
                               "cg_iters_per_step": cg_iters}
@@ -509,6 +511,8 @@ def run_fcg(a):
     # the dominant kernel: the implicit-GEMM convolutions of one forward pass, timed on the device
     sim.set_params(prm)
     ms_fwd, ms_layers = sim.unet_time_forward(3)
+    # one preconditioner application (V-cycle + network), kernel by kernel and as a graph replay
+    vc_direct, vc_graph = sim.fcg_time_vcycle(5)
     nw = sim.unet_grid()[0]
     sim.close()
     flops = unet_flops(nw)
@@ -537,7 +541,7 @@ def run_fcg(a):
             "fcg_converged": bool(st1.converged),
             "plain_cg_same_trajectory": {"iters_per_step": (sc1.total_solve_steps - sc0.total_solve_steps) / 3,
                                          "ms_per_step": ms_cg},
-            "network": net,
+            "network": net, "preconditioner_ms": {"kernel_by_kernel": vc_direct, "graph_replay": vc_graph},
             "roofline": roofline, "clocks": clocks, "cpu_baseline": None, "e2e": None}
     print(json.dumps(line), flush=True)
 

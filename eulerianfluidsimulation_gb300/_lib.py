@@ -56,6 +56,7 @@ SIGNATURES = {
     "efs_unet_add_sample": (ctypes.c_int, [_CTX]),
     "efs_unet_grid": (ctypes.c_int, [_CTX] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "efs_unet_time_forward": (ctypes.c_int, [_CTX, ctypes.c_int, _FP, _FP]),
+    "efs_fcg_time_vcycle": (ctypes.c_int, [_CTX, ctypes.c_int, _FP, _FP]),
     "efs_unet_sample_count": (ctypes.c_int, [_CTX, ctypes.POINTER(ctypes.c_int)]),
     "efs_unet_train": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_uint64, _FP]),

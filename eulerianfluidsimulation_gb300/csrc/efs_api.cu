@@ -654,6 +654,16 @@ int efs_solve(efs_ctx* c, efs_stats* out) {
     return EFS_OK;
 }
 
+int efs_fcg_time_vcycle(efs_ctx* c, int reps, float* ms_direct, float* ms_graph) {
+    if (!c || reps < 1 || !ms_direct || !ms_graph) return EFS_ERR_ARG;
+    if (c->prm.solver != EFS_SOLVER_FCG_UNET) return fail(c, EFS_ERR_STATE, "solver is not EFS_SOLVER_FCG_UNET");
+    const int ps = prepare_fcg(c);
+    if (ps != EFS_OK) return ps;
+    CK(efs::launch_solver_prep(c), "solver prep");
+    CK(efs::ml_time_vcycle(c, reps, ms_direct, ms_graph), "V-cycle timing");
+    return check_device_status(c);
+}
+
 int efs_synchronize(efs_ctx* c) {
     if (!c) return EFS_ERR_ARG;
     return check_device_status(c);

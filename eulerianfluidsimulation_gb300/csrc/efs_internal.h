@@ -198,6 +198,7 @@ LvView ml_view(const efs_ctx* c, int level);
 cudaError_t ml_build(efs_ctx* c, cudaStream_t st);
 cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st);
 cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out);
+cudaError_t ml_time_vcycle(efs_ctx* c, int reps, float* ms_direct, float* ms_graph);
 int ml_level_cg(efs_ctx* c, const LvView& L, const float* r0, float* e, float* t1, float* t2, float* t3, double tol,
                 int maxit, cudaStream_t st);
 // efs_unet.cu: the network's forward pass on bottom-level residual r with its input scale already in

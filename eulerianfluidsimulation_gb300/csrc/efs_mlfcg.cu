@@ -1212,6 +1212,50 @@ cudaError_t fcg_solve(efs_ctx* c) {
     return cudaGraphLaunch(m->solve_exec, c->stream);
 }
 
+// Device time of one application of the preconditioner (the V-cycle, with the network or the Jacobi sweeps at the
+// bottom) on r = the current divergence: `reps` applications as direct launches, then `reps` replays of one
+// captured application (what a solve's loop body pays).  Builds the hierarchy from the current rowinfo first.
+cudaError_t ml_time_vcycle(efs_ctx* c, int reps, float* ms_direct, float* ms_graph) {
+    MLState* m = c->ml;
+    cudaStream_t st = c->stream;
+    const size_t bytes = (size_t)c->g.N * sizeof(float);
+    MCK(ml_build(c, st));
+    MCK(cudaMemcpyAsync(m->r, c->div, bytes, cudaMemcpyDeviceToDevice, st));
+    MCK(cudaMemsetAsync(m->q, 0, bytes, st));   // the previous direction's A d, read by the closing sweep's dots
+    MCK(vcycle(c, 0, m->r, m->z, m->zt, st));   // warm-up
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int k = 0; k < reps && e == cudaSuccess; k++) e = vcycle(c, 0, m->r, m->z, m->zt, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess) *ms_direct = ms / reps;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t ce = vcycle(c, 0, m->r, m->z, m->zt, st);
+        cudaError_t ee = cudaStreamEndCapture(st, &g);
+        e = ce != cudaSuccess ? ce : ee;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(x, st);            // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int k = 0; k < reps && e == cudaSuccess; k++) e = cudaGraphLaunch(x, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess) *ms_graph = ms / reps;
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return e;
+}
+
 // r (fine) carried down the pre-smoothing and restriction chain to the bottom level: out = the bottom residual
 // (outside any capture; builds the hierarchy first)
 cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float** out) {

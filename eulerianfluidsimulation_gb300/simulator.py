@@ -293,6 +293,14 @@ class _GB300Simulator:
         check(lib().efs_unet_time_forward(self._h, reps, fptr(ms), fptr(lay)), self._h)
         return float(ms[0]), lay
 
+    def fcg_time_vcycle(self, reps=5):
+        """efs_fcg_time_vcycle: (ms per preconditioner application launched kernel by kernel, ms per replay of
+        one captured application) on the current divergence."""
+        d = np.zeros(1, np.float32)
+        g = np.zeros(1, np.float32)
+        check(lib().efs_fcg_time_vcycle(self._h, reps, fptr(d), fptr(g)), self._h)
+        return float(d[0]), float(g[0])
+
     def unet_add_sample(self):
         check(lib().efs_unet_add_sample(self._h), self._h)
 

@@ -260,6 +260,12 @@ int  efs_solve_timing_arm(efs_ctx* ctx, int capacity);
 int  efs_solve_timing_read(efs_ctx* ctx, int* launches, double* total_ms, double* row_iterations,
                            double* row_setups);
 
+/* Device time of one application of FCG's preconditioner (EFS_SOLVER_FCG_UNET; the V-cycle with its bottom
+ * solve) on r = the current divergence, after the solve's set-up: mean ms over `reps` applications launched
+ * kernel by kernel, and over `reps` replays of one application captured as a graph (the cost inside a solve).
+ * A measurement entry point: the pressure field is overwritten with the divergence. */
+int  efs_fcg_time_vcycle(efs_ctx* ctx, int reps, float* ms_direct, float* ms_graph);
+
 /* CUDA events on the context's stream: record slot (0..7); elapsed ms between two recorded slots (waits). */
 int  efs_timer_mark(efs_ctx* ctx, int slot);
 int  efs_timer_elapsed(efs_ctx* ctx, int slot_begin, int slot_end, double* ms);

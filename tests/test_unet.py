@@ -255,3 +255,28 @@ def test_fcg_steps_replay_one_graph_and_match_cg_steps():
     assert st.converged and not st.paused and st.precond_steps == st.solve_steps
     for f in (abi.FIELD_VEL, abi.FIELD_RHO, abi.FIELD_PRESSURE):
         assert rel_l2(got[f], want[f]) < 1e-5, (abi.FIELD_NAMES[f], rel_l2(got[f], want[f]))
+
+
+def test_preconditioner_timing_entry_point():
+    """efs_fcg_time_vcycle times one preconditioner application (64^3: one aggregation level, the committed
+    network's grid at the bottom) kernel by kernel and as a graph replay; it refuses a context whose solver is
+    not FCG, and a solve afterwards still converges."""
+    from eulerianfluidsimulation_gb300 import unet_weights
+    n = 64
+    with _dam_ctx(n, solver=abi.SOLVER_CG) as s:
+        s.update(2)
+        with pytest.raises(gb.EfsError) as ei:
+            s.fcg_time_vcycle(2)
+        assert ei.value.status == abi.EFS_ERR_STATE
+        p = s.params.copy()
+        p.solver = abi.SOLVER_FCG_UNET
+        s.set_params(p)
+        if unet_weights.available():
+            unet_weights.load_into(s)
+        else:
+            s.unet_init(1, 0)
+        direct, graph = s.fcg_time_vcycle(3)
+        print(f"\npreconditioner at 64^3: {direct:.3f} ms kernel by kernel, {graph:.3f} ms as a graph replay")
+        assert np.isfinite(direct) and np.isfinite(graph) and direct > 0 and graph > 0
+        s.update(1)
+        assert s.stats().converged
