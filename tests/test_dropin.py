@@ -63,11 +63,14 @@ def _run_adapter_sequence(n, frames, scene, prm, pinned):
     return got, np.array(steps), np.array(paused)
 
 
-# relative L2 after the fixture's 4 frames; the oracle (same float dot products and stopping rule as the
-# reference, other summation order) lands at <= 1.2e-6 on the first five and 2.7e-5 on the divergence, which the
-# last frame's projection leaves at the level of the solve's residual
-TOL = {abi.FIELD_VEL: 1e-5, abi.FIELD_RHO: 1e-5, abi.FIELD_GAMMA: 1e-5, abi.FIELD_BETA: 1e-5, abi.FIELD_PRESSURE: 1e-5,
-       abi.FIELD_DIVERGENCE: 2e-4}
+# Relative L2 after the fixture's 4 frames.  The CG stops at the reference's absolute threshold (r.r < 1e-5), so
+# two correct solves whose dot products round differently stop at different points, and the frames carry that on.
+# The oracle with the reference's summation order lands within 1.2e-6 of the fixture; the oracle with FP64 dot
+# products (another valid order) at vel 4.4e-6, beta 6.5e-5, pressure 2.0e-5, divergence 8.3e-5; the GPU's tree
+# ordered float dot products at vel 1.5e-5, rho 3.8e-6, gamma 1.8e-6, beta 9.7e-5, pressure 4.6e-5, divergence
+# 1.5e-4.  The bounds are about 3x the larger of the two spreads.
+TOL = {abi.FIELD_VEL: 5e-5, abi.FIELD_RHO: 2e-5, abi.FIELD_GAMMA: 1e-5, abi.FIELD_BETA: 3e-4, abi.FIELD_PRESSURE: 1.5e-4,
+       abi.FIELD_DIVERGENCE: 5e-4}
 
 
 @pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "page-locked"])
