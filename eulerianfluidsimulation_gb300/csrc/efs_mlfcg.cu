@@ -104,30 +104,35 @@ struct Walk {
         if (const long long i = (wk).cell(t); i >= 0)
 
 // ---- reductions ------------------------------------------------------------------------------------------------
-// block partials of (a, b, c) into part[3 * blockIdx.x + j]
-__device__ __forceinline__ void block_partials(double a, double b, double c, double* part) {
-    __shared__ double sh[3][kThreads / 32];
+// Block partials of the NV values v into part[3 * blockIdx.x + j]: the warp sums in the threads' accumulator type T
+// (FP32 for the level-0 kernels, whose threads sum a few cells each), the block's eight warp sums in FP64 by
+// thread 0 in warp order.  GB300's FP64 pipe runs at a small fraction of its FP32 rate: a shuffle tree in FP64
+// over every warp of a 4096-block launch cost more than the sweep it finished.
+template <int NV, typename T>
+__device__ __forceinline__ void block_partials(T (&v)[NV], double* part) {
+    __shared__ double sh[NV][kThreads / 32];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-        c += __shfl_down_sync(0xffffffffu, c, o);
-    }
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < NV; j++) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = c; }
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) sh[j][warp] = (double)v[j];
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double s0 = 0, s1 = 0, s2 = 0;
-        for (int k = 0; k < kThreads / 32; k++) { s0 += sh[0][k]; s1 += sh[1][k]; s2 += sh[2][k]; }
-        part[3 * blockIdx.x] = s0;
-        part[3 * blockIdx.x + 1] = s1;
-        part[3 * blockIdx.x + 2] = s2;
-    }
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            double t = 0;
+            for (int k = 0; k < kThreads / 32; k++) t += sh[j][k];
+            part[3 * blockIdx.x + j] = t;
+        }
 }
 // Every block stores its partials; the block that arrives last sums them all in a fixed order (lane-strided over
-// the blocks, then a fixed shuffle tree) and returns true on its thread 0, with the totals in tot.
-__device__ bool reduce_last(double a, double b, double c, double* part, unsigned* counter, double (&tot)[3]) {
-    block_partials(a, b, c, part);
+// the blocks, then a fixed shuffle tree) and returns true on its thread 0, with the NV totals in tot (the rest 0).
+template <int NV, typename T>
+__device__ bool reduce_last(T (&v)[NV], double* part, unsigned* counter, double (&tot)[3]) {
+    block_partials<NV>(v, part);
     __shared__ unsigned s_last;
     if (threadIdx.x == 0) {
         __threadfence();
@@ -137,29 +142,29 @@ __device__ bool reduce_last(double a, double b, double c, double* part, unsigned
     if (!s_last || threadIdx.x >= 32) return false;
     __threadfence();
     // four independent chains per lane (FP64 adds have a long latency), combined in a fixed order
-    double a0[4] = {0, 0, 0, 0}, a1[4] = {0, 0, 0, 0}, a2[4] = {0, 0, 0, 0};
+    double acc[NV][4];
+#pragma unroll
+    for (int j = 0; j < NV; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0;
     for (unsigned k = threadIdx.x; k < gridDim.x; k += 128) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const unsigned kk = k + 32u * u;
-            if (kk < gridDim.x) {
-                a0[u] += __ldcg(part + 3 * kk);
-                a1[u] += __ldcg(part + 3 * kk + 1);
-                a2[u] += __ldcg(part + 3 * kk + 2);
-            }
+            if (kk < gridDim.x)
+#pragma unroll
+                for (int j = 0; j < NV; j++) acc[j][u] += __ldcg(part + 3 * kk + j);
         }
     }
-    double t0 = (a0[0] + a0[1]) + (a0[2] + a0[3]);
-    double t1 = (a1[0] + a1[1]) + (a1[2] + a1[3]);
-    double t2 = (a2[0] + a2[1]) + (a2[2] + a2[3]);
+    double t[NV];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        t0 += __shfl_down_sync(0xffffffffu, t0, o);
-        t1 += __shfl_down_sync(0xffffffffu, t1, o);
-        t2 += __shfl_down_sync(0xffffffffu, t2, o);
-    }
+    for (int j = 0; j < NV; j++) t[j] = (acc[j][0] + acc[j][1]) + (acc[j][2] + acc[j][3]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < NV; j++) t[j] += __shfl_down_sync(0xffffffffu, t[j], o);
     if (threadIdx.x != 0) return false;
-    tot[0] = t0; tot[1] = t1; tot[2] = t2;
+    tot[0] = tot[1] = tot[2] = 0.0;
+#pragma unroll
+    for (int j = 0; j < NV; j++) tot[j] = t[j];
     *counter = 0u;
     return true;
 }
@@ -285,7 +290,7 @@ template <bool FINE, bool DOTS>
 __global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, const float* __restrict__ zin,
                             float* __restrict__ zout, float omega, const float* __restrict__ q, FcgDev* s,
                             double* __restrict__ part) {
-    double zq = 0, rz = 0;
+    float zq = 0.f, rz = 0.f;
     WALK(wk, t, i) {
         float dg, w[6];
         float zi = 0.f;
@@ -293,13 +298,14 @@ __global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, cons
             zi = zin ? zin[i] + omega * (r[i] - lapply<float>(L, i, zin, dg, w)) / dg : omega * r[i] / dg;
         zout[i] = zi;
         if (DOTS) {
-            zq += (double)zi * q[i];
-            rz += (double)zi * r[i];
+            zq += zi * q[i];
+            rz += zi * r[i];
         }
     }
     if (DOTS) {
         double tot[3];
-        if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+        float v[2] = {zq, rz};
+        if (reduce_last(v, part, &s->count, tot)) {
             s->zq = tot[0];
             s->rz = tot[1];
             double beta = 0.0;
@@ -315,6 +321,8 @@ __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float
                               float* __restrict__ rc, double* __restrict__ scal, FcgDev* s, double* __restrict__ part) {
     double ss = 0, cnt = 0;
     for (long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x; C < Cv.V; C += (long long)gridDim.x * blockDim.x) {
+        // a coarse cell is a row exactly when one of its children is (k_ml_build): the others sum nothing
+        if (!(Cv.info[C] & 0x8000u)) { rc[C] = 0.f; continue; }
         const int c32 = (int)C;
         const int X = c32 % Cv.W, Y = (c32 / Cv.W) % Cv.H, Z = c32 / (Cv.W * Cv.H);
         float acc = 0.f;
@@ -327,14 +335,15 @@ __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float
             acc += r[i] - lapply<float>(F, i, z, dg, w);
         }
         rc[C] = acc;
-        if (scal && (Cv.info[C] & 0x8000u)) {
+        if (scal) {
             ss += (double)acc * acc;
             cnt += 1.0;
         }
     }
     if (scal) {
         double tot[3];
-        if (reduce_last(ss, cnt, 0.0, part, &s->count, tot)) {
+        double v[2] = {ss, cnt};
+        if (reduce_last(v, part, &s->count, tot)) {
             scal[0] = tot[0];
             scal[1] = tot[1];
             scal[2] = (tot[0] > 0 && tot[1] > 0) ? 1.0 / sqrt(tot[0] / tot[1]) : 1.0;
@@ -389,7 +398,8 @@ __global__ void k_ml_line_search(LvView L, Walk wk, const float* __restrict__ e,
         eae += ei * (double)lapply<float>(L, i, e, dg, w);
     }
     double tot[3];
-    if (reduce_last(er, eae, 0.0, part, &s->count, tot)) {
+    double v[2] = {er, eae};
+    if (reduce_last(v, part, &s->count, tot)) {
         const double a = (tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
         s->ls_alpha = isfinite(a) ? a : 0.0;
     }
@@ -398,15 +408,16 @@ __global__ void k_ml_line_search(LvView L, Walk wk, const float* __restrict__ e,
 __global__ void k_take_dots(LvView F, Walk wk, const float* __restrict__ e, const float* __restrict__ q,
                             const float* __restrict__ r, float* __restrict__ z, FcgDev* s, double* __restrict__ part) {
     const double a = s->ls_alpha;
-    double zq = 0, rz = 0;
+    float zq = 0.f, rz = 0.f;
     WALK(wk, t, i) {
         const float zi = (F.info[i] & 0x8000u) ? (float)(a * (double)e[i]) : 0.f;
         z[i] = zi;
-        zq += (double)zi * q[i];
-        rz += (double)zi * r[i];
+        zq += zi * q[i];
+        rz += zi * r[i];
     }
     double tot[3];
-    if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+    float v[2] = {zq, rz};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->zq = tot[0];
         s->rz = tot[1];
         double beta = 0.0;
@@ -506,7 +517,8 @@ __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, i
     }
     if (DOTS) {
         double tot[3];
-        if (reduce_last(zq, rz, 0.0, part, &s->count, tot)) {
+        float v[2] = {zq, rz};
+        if (reduce_last(v, part, &s->count, tot)) {
             s->zq = tot[0];
             s->rz = tot[1];
             double beta = 0.0;
@@ -573,7 +585,8 @@ __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int 
         st4(q, i, qv);
     }
     double tot[3];
-    if (reduce_last(dq, 0.0, 0.0, part, &s->count, tot)) {
+    float v[1] = {dq};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->dq = tot[0];
         const double al = s->rz / tot[0];
         if (!(tot[0] < 0.0) || !isfinite(al)) {
@@ -611,7 +624,8 @@ __global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__
         st4(d, i, dv);
     }
     double tot[3];
-    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+    float v[1] = {rr};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->rr = tot[0];
         s->it += 1;
         const bool below = s->rr < s->thr;
@@ -642,7 +656,8 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, doubl
         rows += row ? 1.0 : 0.0;
     }
     double tot[3];
-    if (reduce_last(bb, rows, 0.0, part, &s->count, tot)) {
+    double v[2] = {bb, rows};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->bb = tot[0];
         s->rows = tot[1];
         s->rr = tot[0];
@@ -671,7 +686,7 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, doubl
 __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z, const float* __restrict__ d,
                                  float* __restrict__ dn, float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
     const float beta = (float)s->beta;
-    double dq = 0;
+    float dq = 0.f;
     WALK(wk, t, i) {
         float dg, w[6];
         const float di = z[i] + beta * d[i];
@@ -687,10 +702,11 @@ __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z,
         }
         dn[i] = di;
         q[i] = qi;
-        dq += (double)di * qi;
+        dq += di * qi;
     }
     double tot[3];
-    if (reduce_last(dq, 0.0, 0.0, part, &s->count, tot)) {
+    float v[1] = {dq};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->dq = tot[0];
         const double a = s->rz / tot[0];
         if (!(tot[0] < 0.0) || !isfinite(a)) {
@@ -707,17 +723,18 @@ __global__ void k_fcg_update(Walk wk, double* __restrict__ x, float* __restrict_
                              float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
                              cudaGraphConditionalHandle verify) {
     const double a = s->alpha;
-    double rr = 0;
+    float rr = 0.f;
     WALK(wk, t, i) {
         const float di = dn[i];
         x[i] += a * (double)di;
         const float ri = (float)((double)r[i] - a * (double)q[i]);
         r[i] = ri;
         d[i] = di;
-        rr += (double)ri * ri;
+        rr += ri * ri;
     }
     double tot[3];
-    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+    float v[1] = {rr};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->rr = tot[0];
         s->it += 1;
         const bool below = s->rr < s->thr;
@@ -741,7 +758,8 @@ __global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b,
         rr += (double)ri * ri;
     }
     double tot[3];
-    if (reduce_last(rr, 0.0, 0.0, part, &s->count, tot)) {
+    double v[1] = {rr};
+    if (reduce_last(v, part, &s->count, tot)) {
         s->rr = tot[0];
         s->conv = s->rr < s->thr;
     }
@@ -812,7 +830,8 @@ __global__ void k_lv_dot3(long long n, const float* a0, const float* b0, const f
         s0 += (double)a0[i] * b0[i];
         if (a1) s1 += (double)a1[i] * b1[i];
     }
-    block_partials(s0, s1, 0.0, part);
+    double v[2] = {s0, s1};
+    block_partials<2>(v, part);
 }
 __global__ void k_lv_axpy2(long long n, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ d,
                            const float* __restrict__ q, double alpha) {
@@ -848,6 +867,7 @@ struct MLState {
     int* chunks = nullptr;        // level 0: the 32-cell chunks that hold a matrix row, in order
     int* bcount = nullptr;        // their per-block counts / offsets
     long long nch = 0;            // chunks of the fine grid
+    unsigned qred_grid = 0;       // blocks of the level-0 reduction kernels (one wave)
     double* part = nullptr;       // 3 * kGrid block partials
     FcgDev* s = nullptr;
     double* hpart = nullptr;      // pinned: partials of the host-driven level CG
@@ -960,6 +980,11 @@ cudaError_t ml_alloc(efs_ctx* c) {
     MCK(cudaMallocHost(reinterpret_cast<void**>(&m->hpart), 3 * kGrid * sizeof(double)));
     MCK(cudaStreamCreateWithFlags(&m->cap1, cudaStreamNonBlocking));
     MCK(cudaStreamCreateWithFlags(&m->cap2, cudaStreamNonBlocking));
+    // the level-0 reduction kernels run one wave of resident blocks (each thread loops over several 4-cell
+    // groups): fewer block partials to order and sum at the end
+    int occ = 0;
+    MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_q_smooth<true>, kThreads, 0));
+    m->qred_grid = (unsigned)std::max(1, occ) * (unsigned)std::max(1, c->sm_count);
     return cudaSuccess;
 }
 
@@ -1006,7 +1031,7 @@ cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zo
     const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
     if (l == 0 && quad_level0(c)) {
         const unsigned gq = grid_for(c->g.N / 4);
-        if (dots) k_q_smooth<true><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, m->q, m->s, m->part);
+        if (dots) k_q_smooth<true><<<std::min(gq, m->qred_grid), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, m->q, m->s, m->part);
         else k_q_smooth<false><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, nullptr, m->s, m->part);
         return cudaGetLastError();
     }
@@ -1132,7 +1157,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             // z = M(r), with z.q, r.z and beta at its end
             if ((e = vcycle(c, 0, m->r, m->z, m->zt, b)) != cudaSuccess) break;
             const bool quad = quad_level0(c);
-            const unsigned gq = grid_for(N / 4);
+            const unsigned gq = std::min(grid_for(N / 4), m->qred_grid);
             if (quad) k_q_dir_matvec<<<gq, kThreads, 0, b>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, m->z, m->d, m->dn, m->q, m->s, m->part);
             else k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
