@@ -80,6 +80,7 @@ struct LvView {
     const uint16_t* info;
     const uint8_t* w;
     const float* diag;
+    const float* wd = nullptr;   // coarse levels: the smoother's damping over the diagonal (0 off the rows)
 };
 
 struct GraphKey {

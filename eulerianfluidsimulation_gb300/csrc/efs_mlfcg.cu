@@ -42,13 +42,20 @@ constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the 
 constexpr int kThreads = 256;
 constexpr int kGrid = 4096;           // most blocks of a reduction kernel (the partials buffer holds one per block)
 
+// Arrival counters of the last-block reductions: a block counts itself in group blockIdx.x % kArriveGroups, and
+// the last block of each group in the top counter.  One 128-byte line per counter: same-address atomics from
+// thousands of blocks queue at one L2 slice (4096 arrivals cost tens of microseconds), 32 lines do not.
+constexpr int kArriveGroups = 32;
+constexpr int kArriveStride = 32;     // unsigned per counter line
+
 // device scalars of one FCG solve
 struct FcgDev {
     double rr, rz, dq, zq, bb, thr, alpha, beta, rr_window, rows;
     double ls_alpha;                  // bottom-level line search factor of the current V-cycle (1 without the network)
     int it, conv, stall, verify, fallback, nchunks;
-    unsigned count;                   // arrival counter of the last-block reductions (back to 0 after each)
-    unsigned pad;
+    int ncchunks;                     // level 1's 32-cell chunks that hold a row (the restriction's list)
+    // arrival counters (groups, then the top), back to 0 after each reduction
+    alignas(128) unsigned count[(kArriveGroups + 1) * kArriveStride];
 };
 
 inline unsigned blocks_for(long long n) { return (unsigned)std::max(1LL, (n + kThreads - 1) / kThreads); }
@@ -104,10 +111,10 @@ struct Walk {
         if (const long long i = (wk).cell(t); i >= 0)
 
 // ---- reductions ------------------------------------------------------------------------------------------------
-// Block partials of the NV values v into part[3 * blockIdx.x + j]: the warp sums in the threads' accumulator type T
-// (FP32 for the level-0 kernels, whose threads sum a few cells each), the block's eight warp sums in FP64 by
-// thread 0 in warp order.  GB300's FP64 pipe runs at a small fraction of its FP32 rate: a shuffle tree in FP64
-// over every warp of a 4096-block launch cost more than the sweep it finished.
+// Block partials of the NV values v into part[3 * blockIdx.x + j]: the warp sums and the block's eight warp sums
+// (thread 0, warp order) in the threads' accumulator type T (FP32 for the level-0 kernels, whose threads sum a
+// few cells each).  GB300's FP64 pipe runs at a small fraction of its FP32 rate: a shuffle tree in FP64 over every
+// warp of a 4096-block launch cost more than the sweep it finished.
 template <int NV, typename T>
 __device__ __forceinline__ void block_partials(T (&v)[NV], double* part) {
     __shared__ double sh[NV][kThreads / 32];
@@ -123,9 +130,9 @@ __device__ __forceinline__ void block_partials(T (&v)[NV], double* part) {
     if (threadIdx.x == 0)
 #pragma unroll
         for (int j = 0; j < NV; j++) {
-            double t = 0;
-            for (int k = 0; k < kThreads / 32; k++) t += sh[j][k];
-            part[3 * blockIdx.x + j] = t;
+            T t = 0;
+            for (int k = 0; k < kThreads / 32; k++) t += (T)sh[j][k];
+            part[3 * blockIdx.x + j] = (double)t;
         }
 }
 // Every block stores its partials; the block that arrives last sums them all in a fixed order (lane-strided over
@@ -134,9 +141,17 @@ template <int NV, typename T>
 __device__ bool reduce_last(T (&v)[NV], double* part, unsigned* counter, double (&tot)[3]) {
     block_partials<NV>(v, part);
     __shared__ unsigned s_last;
+    const unsigned ngroups = min(gridDim.x, (unsigned)kArriveGroups);
     if (threadIdx.x == 0) {
         __threadfence();
-        s_last = (atomicAdd(counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+        const unsigned g = blockIdx.x % kArriveGroups;
+        const unsigned gsize = (gridDim.x - g + kArriveGroups - 1) / kArriveGroups;
+        unsigned last = 0u;
+        if (atomicAdd(counter + g * kArriveStride, 1u) == gsize - 1) {
+            __threadfence();
+            last = (atomicAdd(counter + kArriveGroups * kArriveStride, 1u) == ngroups - 1) ? 1u : 0u;
+        }
+        s_last = last;
     }
     __syncthreads();
     if (!s_last || threadIdx.x >= 32) return false;
@@ -161,11 +176,59 @@ __device__ bool reduce_last(T (&v)[NV], double* part, unsigned* counter, double 
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
         for (int j = 0; j < NV; j++) t[j] += __shfl_down_sync(0xffffffffu, t[j], o);
+    // every block has arrived: the counters go back to 0 for the next reduction
+    if (threadIdx.x < ngroups) counter[threadIdx.x * kArriveStride] = 0u;
+    if (threadIdx.x == 0) counter[kArriveGroups * kArriveStride] = 0u;
     if (threadIdx.x != 0) return false;
     tot[0] = tot[1] = tot[2] = 0.0;
 #pragma unroll
     for (int j = 0; j < NV; j++) tot[j] = t[j];
-    *counter = 0u;
+    return true;
+}
+
+// The level-0 reduction kernels (thousands of blocks) only store their FP32 block partials; one block then sums
+// them: thread t adds blocks t, t + 256, ... with a compensated FP32 sum (Kahan), the 256 results go through a
+// fixed FP64 tree.  Blocks that waited for their own fence and arrival atomic before exiting had cost about
+// 20 us per 4096-block launch.
+constexpr int kFinishPer = kGrid / kThreads;   // partials per thread of a finisher block
+template <int NV>
+__device__ bool finish_partials(const double* __restrict__ part, int n, double (&tot)[NV]) {
+    __shared__ double sh[NV][kThreads / 32];
+    double a[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        float v[kFinishPer];
+#pragma unroll
+        for (int u = 0; u < kFinishPer; u++) {      // all loads first: one round trip
+            const int k = (int)threadIdx.x + u * kThreads;
+            v[u] = k < n ? (float)__ldcg(part + 3 * k + j) : 0.f;
+        }
+        float sum = 0.f, comp = 0.f;
+#pragma unroll
+        for (int u = 0; u < kFinishPer; u++) {
+            const float y = v[u] - comp;
+            const float t = sum + y;
+            comp = (t - sum) - y;
+            sum = t;
+        }
+        a[j] = (double)sum;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < NV; j++) a[j] += __shfl_down_sync(0xffffffffu, a[j], o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; j++) sh[j][warp] = a[j];
+    __syncthreads();
+    if (threadIdx.x != 0) return false;
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+        double t = 0;
+        for (int k = 0; k < kThreads / 32; k++) t += sh[j][k];
+        tot[j] = t;
+    }
     return true;
 }
 
@@ -192,8 +255,8 @@ __global__ void k_chunks_count(const uint16_t* __restrict__ info, long long N, l
     const int n = __syncthreads_count(f);
     if (threadIdx.x == 0) bcount[blockIdx.x] = n;
 }
-// exclusive scan of the block counts (one block of 1024 threads), total into s->nchunks
-__global__ void k_chunks_scan(int* __restrict__ bcount, int nb, FcgDev* s) {
+// exclusive scan of the block counts (one block of 1024 threads), total into *total
+__global__ void k_chunks_scan(int* __restrict__ bcount, int nb, int* __restrict__ total) {
     __shared__ int warp_tot[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -227,7 +290,7 @@ __global__ void k_chunks_scan(int* __restrict__ bcount, int nb, FcgDev* s) {
         if (threadIdx.x == 1023) carry = excl + v;
         __syncthreads();
     }
-    if (threadIdx.x == 0) s->nchunks = carry;
+    if (threadIdx.x == 0) *total = carry;
 }
 __global__ void k_chunks_write(const uint16_t* __restrict__ info, long long N, long long nch, const int* __restrict__ boff,
                                int* __restrict__ chunks) {
@@ -250,6 +313,7 @@ struct LvOut {
     uint16_t* info;
     uint8_t* w;
     float* diag;
+    float* wd;
 };
 template <bool FINE>
 __global__ void k_ml_build(LvView src, LvOut dst) {
@@ -278,6 +342,7 @@ __global__ void k_ml_build(LvView src, LvOut dst) {
     }
     dst.info[C] = row ? (uint16_t)0x8000u : (uint16_t)0;
     dst.diag[C] = row ? dg : 0.f;
+    dst.wd[C] = (row && dg != 0.f) ? kOmega / dg : 0.f;
 #pragma unroll
     for (int k = 0; k < 6; k++) dst.w[k * dst.V + C] = row ? (uint8_t)w[k] : (uint8_t)0;
 }
@@ -294,8 +359,10 @@ __global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, cons
     WALK(wk, t, i) {
         float dg, w[6];
         float zi = 0.f;
-        if (lrow<FINE>(L, i, dg, w) && dg != 0.f)
-            zi = zin ? zin[i] + omega * (r[i] - lapply<float>(L, i, zin, dg, w)) / dg : omega * r[i] / dg;
+        if (lrow<FINE>(L, i, dg, w) && dg != 0.f) {
+            if (FINE) zi = zin ? zin[i] + omega * (r[i] - lapply<float>(L, i, zin, dg, w)) / dg : omega * r[i] / dg;
+            else zi = zin ? zin[i] + (r[i] - lapply<float>(L, i, zin, dg, w)) * L.wd[i] : r[i] * L.wd[i];
+        }
         zout[i] = zi;
         if (DOTS) {
             zq += zi * q[i];
@@ -305,13 +372,38 @@ __global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, cons
     if (DOTS) {
         double tot[3];
         float v[2] = {zq, rz};
-        if (reduce_last(v, part, &s->count, tot)) {
+        if (reduce_last(v, part, s->count, tot)) {
             s->zq = tot[0];
             s->rz = tot[1];
             double beta = 0.0;
             if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
             s->beta = isfinite(beta) ? beta : 0.0;
         }
+    }
+}
+// The first damped Jacobi sweep from zero is pointwise (z1 = w r / diag on the rows), so the two pre-smoothing
+// sweeps are one pass: zout = z1 + w (r - A z1) / diag, with z1 formed at the row and at its neighbours exactly as
+// the first sweep would store it (a neighbour with a non-zero weight is a row).
+template <bool FINE>
+__device__ __forceinline__ float z1_at(const LvView& L, long long j, const float* __restrict__ r, float omega) {
+    if (!FINE) return r[j] * L.wd[j];
+    const float dj = -(float)((L.info[j] >> 8) & 7);
+    return dj != 0.f ? omega * r[j] / dj : 0.f;
+}
+template <bool FINE>
+__global__ void k_ml_smooth2(LvView L, Walk wk, const float* __restrict__ r, float* __restrict__ zout, float omega) {
+    WALK(wk, t, i) {
+        float dg, w[6];
+        float zi = 0.f;
+        if (lrow<FINE>(L, i, dg, w) && dg != 0.f) {
+            const float z1 = z1_at<FINE>(L, i, r, omega);
+            float s = dg * z1;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (w[k] != 0.f) s += w[k] * z1_at<FINE>(L, i + noff(L, k), r, omega);
+            zi = FINE ? z1 + omega * (r[i] - s) / dg : z1 + (r[i] - s) * L.wd[i];
+        }
+        zout[i] = zi;
     }
 }
 // rc[C] = sum over the merged rows i of C of (r - A z)_i.  scal (non-null: the level below is the network's):
@@ -343,7 +435,7 @@ __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float
     if (scal) {
         double tot[3];
         double v[2] = {ss, cnt};
-        if (reduce_last(v, part, &s->count, tot)) {
+        if (reduce_last(v, part, s->count, tot)) {
             scal[0] = tot[0];
             scal[1] = tot[1];
             scal[2] = (tot[0] > 0 && tot[1] > 0) ? 1.0 / sqrt(tot[0] / tot[1]) : 1.0;
@@ -375,7 +467,7 @@ __global__ void k_ml_prolong_smooth(LvView L, Walk wk, const float* __restrict__
         const long long WH = (long long)W * H;
         if (w[4] != 0.f) s += w[4] * (z[i - WH] + a * parent(x, y, zz - 1));
         if (w[5] != 0.f) s += w[5] * (z[i + WH] + a * parent(x, y, zz + 1));
-        tout[i] = zi + omega * (r[i] - s) / dg;
+        tout[i] = FINE ? zi + omega * (r[i] - s) / dg : zi + (r[i] - s) * L.wd[i];
     }
 }
 template <bool FINE>
@@ -399,7 +491,7 @@ __global__ void k_ml_line_search(LvView L, Walk wk, const float* __restrict__ e,
     }
     double tot[3];
     double v[2] = {er, eae};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         const double a = (tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
         s->ls_alpha = isfinite(a) ? a : 0.0;
     }
@@ -417,7 +509,7 @@ __global__ void k_take_dots(LvView F, Walk wk, const float* __restrict__ e, cons
     }
     double tot[3];
     float v[2] = {zq, rz};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         s->zq = tot[0];
         s->rz = tot[1];
         double beta = 0.0;
@@ -476,13 +568,27 @@ __device__ __forceinline__ float lap4(unsigned f, float c, const float (&nb)[6])
     return s;
 }
 
-// k_ml_smooth at level 0
+// The level-0 diagonal is -(count of non-solid neighbours), count 0..6: the sweeps multiply by omega / diagonal,
+// taken per block from a table of the eight counts (0 for count 0 and for the unused 7), instead of dividing.
+__device__ __forceinline__ void init_wod(float* wod) {
+    if (threadIdx.x < 8) {
+        const unsigned k = threadIdx.x;
+        wod[k] = (k == 0 || k == 7) ? 0.f : kOmega / -(float)k;
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ unsigned q_count(unsigned f) { return (f >> 8) & 7u; }
+__device__ __forceinline__ bool q_live(unsigned f) { return (f & 0x8000u) && q_count(f) != 0; }
+
+// k_ml_smooth at level 0 (damping omega = kOmega)
 // (the level-0 kernels sum their few cells per thread in FP32, and the block and grid sums in FP64: GB300's FP64
 // pipe is a small fraction of its FP32 one)
 template <bool DOTS>
 __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ r,
-                           const float* __restrict__ zin, float* __restrict__ zout, float omega,
-                           const float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
+                           const float* __restrict__ zin, float* __restrict__ zout, const float* __restrict__ q,
+                           double* __restrict__ part) {
+    __shared__ float wod[8];
+    init_wod(wod);
     float zq = 0.f, rz = 0.f;
     QWALK(qw, i) {
         unsigned f[4];
@@ -493,16 +599,11 @@ __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, i
             float c[4], nb[4][6];
             stencil4(zin, i, W, WH, c, nb);
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const float dg = -(float)((f[k] >> 8) & 7);
-                out[k] = ((f[k] & 0x8000u) && dg != 0.f) ? c[k] + omega * (rv[k] - lap4(f[k], c[k], nb[k])) / dg : 0.f;
-            }
+            for (int k = 0; k < 4; k++)
+                out[k] = q_live(f[k]) ? c[k] + (rv[k] - lap4(f[k], c[k], nb[k])) * wod[q_count(f[k])] : 0.f;
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const float dg = -(float)((f[k] >> 8) & 7);
-                out[k] = ((f[k] & 0x8000u) && dg != 0.f) ? omega * rv[k] / dg : 0.f;
-            }
+            for (int k = 0; k < 4; k++) out[k] = q_live(f[k]) ? rv[k] * wod[q_count(f[k])] : 0.f;
         }
         st4(zout, i, out);
         if (DOTS) {
@@ -516,21 +617,142 @@ __global__ void k_q_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, i
         }
     }
     if (DOTS) {
-        double tot[3];
         float v[2] = {zq, rz};
-        if (reduce_last(v, part, &s->count, tot)) {
-            s->zq = tot[0];
-            s->rz = tot[1];
-            double beta = 0.0;
-            if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
-            s->beta = isfinite(beta) ? beta : 0.0;
+        block_partials<2>(v, part);
+    }
+}
+// the dots of k_q_smooth<true> (its n block partials): FCG's z.q, r.z and beta, as k_ml_smooth DOTS
+__global__ void k_q_finish_dots(const double* __restrict__ part, int n, FcgDev* s) {
+    double tot[2];
+    if (!finish_partials<2>(part, n, tot)) return;
+    s->zq = tot[0];
+    s->rz = tot[1];
+    double beta = 0.0;
+    if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
+    s->beta = isfinite(beta) ? beta : 0.0;
+}
+// k_ml_smooth2 at level 0: the first sweep's values at the group and at its six neighbours from r and the
+// neighbours' counts (a neighbour with its stencil bit set is a row)
+__global__ void k_q_smooth2(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ r,
+                            float* __restrict__ zout) {
+    __shared__ float wod[8];
+    init_wod(wod);
+    QWALK(qw, i) {
+        unsigned f[4], fym[4], fyp[4], fzm[4], fzp[4];
+        float rv[4], rym[4], ryp[4], rzm[4], rzp[4], c[4], out[4];
+        info4(info, i, f);
+        info4(info, i - W, fym);
+        info4(info, i + W, fyp);
+        info4(info, i - WH, fzm);
+        info4(info, i + WH, fzp);
+        ld4(r, i, rv);
+        ld4(r, i - W, rym);
+        ld4(r, i + W, ryp);
+        ld4(r, i - WH, rzm);
+        ld4(r, i + WH, rzp);
+        const float left = r[i - 1] * wod[q_count(info[i - 1])], right = r[i + 4] * wod[q_count(info[i + 4])];
+#pragma unroll
+        for (int k = 0; k < 4; k++) c[k] = q_live(f[k]) ? rv[k] * wod[q_count(f[k])] : 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!q_live(f[k])) { out[k] = 0.f; continue; }
+            float nb[6];
+            nb[0] = k == 0 ? left : c[k - 1 < 0 ? 0 : k - 1];
+            nb[1] = k == 3 ? right : c[k + 1 > 3 ? 3 : k + 1];
+            nb[2] = rym[k] * wod[q_count(fym[k])];
+            nb[3] = ryp[k] * wod[q_count(fyp[k])];
+            nb[4] = rzm[k] * wod[q_count(fzm[k])];
+            nb[5] = rzp[k] * wod[q_count(fzp[k])];
+            out[k] = c[k] + (rv[k] - lap4(f[k], c[k], nb)) * wod[q_count(f[k])];
+        }
+        st4(zout, i, out);
+    }
+}
+// k_ml_restrict at level 0 (width a multiple of 64): one warp per listed level-1 chunk, i.e. 32 coarse cells of a
+// coarse row that hold a row, and the 64 x 4 fine cells below them.  Lane 8 j + g takes the 4-cell groups g and
+// g + 8 of fine row j ((dy, dz) = (j & 1, j >> 1)) and sums each group's residuals into the two coarse cells the
+// group covers; a fixed butterfly over the four rows finishes the coarse sums, which lanes 0-7 store.  A group's
+// stencil is read where the group holds a row, and so lies in the grid's interior rows (the loads stay inside the
+// grid); a group without rows reads the interior group at WH + W + 4 (the grid has at least 4 cells on each side)
+// and adds nothing.  Coarse cells outside the listed chunks hold no row and stay 0 from the solve's set-up.
+// scal: as k_ml_restrict.
+__global__ void k_q_restrict(const int* __restrict__ cchunks, const FcgDev* s, const uint16_t* __restrict__ info, int W,
+                             int H, int D, const float* __restrict__ r, const float* __restrict__ z, LvView Cv,
+                             float* __restrict__ rc, double* __restrict__ scal, FcgDev* sw, double* __restrict__ part) {
+    const int lane = threadIdx.x & 31, j = lane >> 3, g = lane & 7;
+    const long long items = s->ncchunks;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int WH = W * H, cpr = Cv.W / 32;
+    double ss = 0, cnt = 0;
+    for (long long it = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; it < items; it += nwarps) {
+        const int ch = cchunks[it];
+        const int crow = ch / cpr, cx0 = (ch - crow * cpr) * 32, Y = crow % Cv.H, Z = crow / Cv.H;
+        const long long C0 = (long long)ch * 32;
+        const int y = 2 * Y + (j & 1), zz = 2 * Z + (j >> 1);
+        const bool inside = y < H && zz < D;
+        const int i0 = inside ? (zz * H + y) * W + 2 * cx0 + 4 * g : 0, i1 = inside ? i0 + 32 : 0;
+        unsigned f0[4], f1[4];
+        info4(info, i0, f0);
+        info4(info, i1, f1);
+        const bool h0 = inside && ((f0[0] | f0[1] | f0[2] | f0[3]) & 0x8000u);
+        const bool h1 = inside && ((f1[0] | f1[1] | f1[2] | f1[3]) & 0x8000u);
+        const int safe = WH + W + 4;
+        float rv0[4], rv1[4], c0[4], c1[4], nb0[4][6], nb1[4][6];
+        ld4(r, h0 ? i0 : safe, rv0);
+        ld4(r, h1 ? i1 : safe, rv1);
+        stencil4(z, h0 ? i0 : safe, W, WH, c0, nb0);
+        stencil4(z, h1 ? i1 : safe, W, WH, c1, nb1);
+        float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;   // coarse cells 2g, 2g + 1 and 16 + 2g, 17 + 2g
+        if (h0) {
+            if (f0[0] & 0x8000u) a0 += rv0[0] - lap4(f0[0], c0[0], nb0[0]);
+            if (f0[1] & 0x8000u) a0 += rv0[1] - lap4(f0[1], c0[1], nb0[1]);
+            if (f0[2] & 0x8000u) a1 += rv0[2] - lap4(f0[2], c0[2], nb0[2]);
+            if (f0[3] & 0x8000u) a1 += rv0[3] - lap4(f0[3], c0[3], nb0[3]);
+        }
+        if (h1) {
+            if (f1[0] & 0x8000u) b0 += rv1[0] - lap4(f1[0], c1[0], nb1[0]);
+            if (f1[1] & 0x8000u) b0 += rv1[1] - lap4(f1[1], c1[1], nb1[1]);
+            if (f1[2] & 0x8000u) b1 += rv1[2] - lap4(f1[2], c1[2], nb1[2]);
+            if (f1[3] & 0x8000u) b1 += rv1[3] - lap4(f1[3], c1[3], nb1[3]);
+        }
+#pragma unroll
+        for (int o = 8; o <= 16; o <<= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            b0 += __shfl_xor_sync(0xffffffffu, b0, o);
+            b1 += __shfl_xor_sync(0xffffffffu, b1, o);
+        }
+        if (j == 0) {
+            *reinterpret_cast<float2*>(rc + C0 + 2 * g) = make_float2(a0, a1);
+            *reinterpret_cast<float2*>(rc + C0 + 16 + 2 * g) = make_float2(b0, b1);
+            if (scal) {
+                const unsigned ca = *reinterpret_cast<const unsigned*>(Cv.info + C0 + 2 * g);
+                const unsigned cb = *reinterpret_cast<const unsigned*>(Cv.info + C0 + 16 + 2 * g);
+                if (ca & 0x8000u) { ss += (double)a0 * a0; cnt += 1.0; }
+                if (ca & 0x80000000u) { ss += (double)a1 * a1; cnt += 1.0; }
+                if (cb & 0x8000u) { ss += (double)b0 * b0; cnt += 1.0; }
+                if (cb & 0x80000000u) { ss += (double)b1 * b1; cnt += 1.0; }
+            }
+        }
+    }
+    if (scal) {
+        double tot[3], v[2] = {ss, cnt};
+        if (reduce_last(v, part, sw->count, tot)) {
+            scal[0] = tot[0];
+            scal[1] = tot[1];
+            scal[2] = (tot[0] > 0 && tot[1] > 0) ? 1.0 / sqrt(tot[0] / tot[1]) : 1.0;
         }
     }
 }
-// k_ml_prolong_smooth at level 0 (its coarse level is level 1 or the network's grid)
-__global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int H, const float* __restrict__ r,
-                                   const float* __restrict__ z, const float* __restrict__ ec, int CW, int CH,
-                                   const double* __restrict__ alpha, float* __restrict__ tout, float omega) {
+// k_ml_prolong_smooth at level 0 (its coarse level is level 1 or the network's grid, CW x CH x CD).  The group's
+// cells x0 .. x0 + 3 have the parents px = x0 / 2 (cells 0, 1) and px + 1 (cells 2, 3); their x neighbours add
+// px - 1 and px + 2, their y and z neighbours the same two parents in the neighbouring parent rows (clamped to the
+// grid: a neighbour outside it has no stencil bit).
+__global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, int W, int H, int D,
+                                   const float* __restrict__ r, const float* __restrict__ z, const float* __restrict__ ec,
+                                   int CW, int CH, const double* __restrict__ alpha, float* __restrict__ tout) {
+    __shared__ float wod[8];
+    init_wod(wod);
     const float a = alpha ? (float)*alpha : 1.f;
     const int WH = W * H;
     QWALK(qw, i) {
@@ -539,23 +761,32 @@ __global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, 
         info4(info, i, f);
         ld4(r, i, rv);
         stencil4(z, i, W, WH, c, nb);
-        const int x0 = i % W, y = (i / W) % H, zz = i / WH;
-        auto par = [&](int px, int py, int pz) { return ec[((pz >> 1) * CH + (py >> 1)) * CW + (px >> 1)]; };
+        const int row = i / W, x0 = i - row * W, y = row % H, zz = row / H;
+        const int px = x0 >> 1;
+        auto prow = [&](int py, int pz) { return ec + ((long long)(pz >> 1) * CH + (py >> 1)) * CW; };
+        const float* pc = prow(y, zz);
+        const float2 pcc = *reinterpret_cast<const float2*>(pc + px);
+        const float pl = pc[px > 0 ? px - 1 : 0], pr = pc[px + 2 < CW ? px + 2 : CW - 1];
+        const float2 pym = *reinterpret_cast<const float2*>(prow(y > 0 ? y - 1 : 0, zz) + px);
+        const float2 pyp = *reinterpret_cast<const float2*>(prow(y + 1 < H ? y + 1 : H - 1, zz) + px);
+        const float2 pzm = *reinterpret_cast<const float2*>(prow(y, zz > 0 ? zz - 1 : 0) + px);
+        const float2 pzp = *reinterpret_cast<const float2*>(prow(y, zz + 1 < D ? zz + 1 : D - 1) + px);
+        const float P[4] = {pcc.x, pcc.x, pcc.y, pcc.y};
+        const float PL[4] = {pl, pcc.x, pcc.x, pcc.y};
+        const float PR[4] = {pcc.x, pcc.y, pcc.y, pr};
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const unsigned fk = f[k];
-            const float dg = -(float)((fk >> 8) & 7);
-            if (!(fk & 0x8000u) || dg == 0.f) { out[k] = 0.f; continue; }
-            const int x = x0 + k;
-            const float zc = c[k] + a * par(x, y, zz);
-            float sum = dg * zc;
-            if (fk & 1u) sum += nb[k][0] + a * par(x - 1, y, zz);
-            if (fk & 2u) sum += nb[k][1] + a * par(x + 1, y, zz);
-            if (fk & 4u) sum += nb[k][2] + a * par(x, y - 1, zz);
-            if (fk & 8u) sum += nb[k][3] + a * par(x, y + 1, zz);
-            if (fk & 16u) sum += nb[k][4] + a * par(x, y, zz - 1);
-            if (fk & 32u) sum += nb[k][5] + a * par(x, y, zz + 1);
-            out[k] = zc + omega * (rv[k] - sum) / dg;
+            if (!q_live(fk)) { out[k] = 0.f; continue; }
+            const float zc = c[k] + a * P[k];
+            float sum = -(float)q_count(fk) * zc;
+            if (fk & 1u) sum += nb[k][0] + a * PL[k];
+            if (fk & 2u) sum += nb[k][1] + a * PR[k];
+            if (fk & 4u) sum += nb[k][2] + a * (k < 2 ? pym.x : pym.y);
+            if (fk & 8u) sum += nb[k][3] + a * (k < 2 ? pyp.x : pyp.y);
+            if (fk & 16u) sum += nb[k][4] + a * (k < 2 ? pzm.x : pzm.y);
+            if (fk & 32u) sum += nb[k][5] + a * (k < 2 ? pzp.x : pzp.y);
+            out[k] = zc + (rv[k] - sum) * wod[q_count(fk)];
         }
         st4(tout, i, out);
     }
@@ -584,23 +815,25 @@ __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int 
         st4(dn, i, dv);
         st4(q, i, qv);
     }
-    double tot[3];
     float v[1] = {dq};
-    if (reduce_last(v, part, &s->count, tot)) {
-        s->dq = tot[0];
-        const double al = s->rz / tot[0];
-        if (!(tot[0] < 0.0) || !isfinite(al)) {
-            s->stall = 1;
-            s->alpha = 0.0;
-        } else {
-            s->alpha = al;
-        }
+    block_partials<1>(v, part);
+}
+// d.q of k_q_dir_matvec and alpha, as k_fcg_dir_matvec
+__global__ void k_q_finish_dq(const double* __restrict__ part, int n, FcgDev* s) {
+    double tot[1];
+    if (!finish_partials<1>(part, n, tot)) return;
+    s->dq = tot[0];
+    const double al = s->rz / tot[0];
+    if (!(tot[0] < 0.0) || !isfinite(al)) {
+        s->stall = 1;
+        s->alpha = 0.0;
+    } else {
+        s->alpha = al;
     }
 }
 // k_fcg_update at level 0
 __global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
-                           float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
-                           cudaGraphConditionalHandle verify) {
+                           float* __restrict__ d, const float* __restrict__ q, const FcgDev* s, double* __restrict__ part) {
     const double a = s->alpha;
     const float af = (float)a;
     float rr = 0.f;
@@ -623,19 +856,22 @@ __global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__
         st4(r, i, rv);
         st4(d, i, dv);
     }
-    double tot[3];
     float v[1] = {rr};
-    if (reduce_last(v, part, &s->count, tot)) {
-        s->rr = tot[0];
-        s->it += 1;
-        const bool below = s->rr < s->thr;
-        if (!below && !s->stall && (s->it % 10) == 0) {
-            if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
-            s->rr_window = s->rr;
-        }
-        s->verify = !s->stall && (below || (s->it % 32) == 0);
-        cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
+    block_partials<1>(v, part);
+}
+// r.r of k_q_update, the iteration count, the stall window and the verification decision, as k_fcg_update
+__global__ void k_q_finish_rr(const double* __restrict__ part, int n, FcgDev* s, cudaGraphConditionalHandle verify) {
+    double tot[1];
+    if (!finish_partials<1>(part, n, tot)) return;
+    s->rr = tot[0];
+    s->it += 1;
+    const bool below = s->rr < s->thr;
+    if (!below && !s->stall && (s->it % 10) == 0) {
+        if (!(s->rr <= 0.5 * s->rr_window)) s->stall = 1;
+        s->rr_window = s->rr;
     }
+    s->verify = !s->stall && (below || (s->it % 32) == 0);
+    cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
 }
 
 // ---- FCG ------------------------------------------------------------------------------------------------------
@@ -657,7 +893,7 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, doubl
     }
     double tot[3];
     double v[2] = {bb, rows};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         s->bb = tot[0];
         s->rows = tot[1];
         s->rr = tot[0];
@@ -706,7 +942,7 @@ __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z,
     }
     double tot[3];
     float v[1] = {dq};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         s->dq = tot[0];
         const double a = s->rz / tot[0];
         if (!(tot[0] < 0.0) || !isfinite(a)) {
@@ -734,7 +970,7 @@ __global__ void k_fcg_update(Walk wk, double* __restrict__ x, float* __restrict_
     }
     double tot[3];
     float v[1] = {rr};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         s->rr = tot[0];
         s->it += 1;
         const bool below = s->rr < s->thr;
@@ -759,7 +995,7 @@ __global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b,
     }
     double tot[3];
     double v[1] = {rr};
-    if (reduce_last(v, part, &s->count, tot)) {
+    if (reduce_last(v, part, s->count, tot)) {
         s->rr = tot[0];
         s->conv = s->rr < s->thr;
     }
@@ -856,6 +1092,7 @@ struct MLLevel {
     uint16_t* info = nullptr;
     uint8_t* w = nullptr;
     float* diag = nullptr;
+    float* wd = nullptr;          // kOmega / diag on the rows, 0 elsewhere
     float *r = nullptr, *z = nullptr, *t = nullptr;
 };
 
@@ -866,8 +1103,10 @@ struct MLState {
     float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *dn = nullptr, *q = nullptr, *fb = nullptr;
     int* chunks = nullptr;        // level 0: the 32-cell chunks that hold a matrix row, in order
     int* bcount = nullptr;        // their per-block counts / offsets
+    int* cchunks = nullptr;       // level 1: the 32-cell chunks that hold a row, in order (k_q_restrict)
+    int* cbcount = nullptr;
+    long long cnch = 0;           // chunks of level 1
     long long nch = 0;            // chunks of the fine grid
-    unsigned qred_grid = 0;       // blocks of the level-0 reduction kernels (one wave)
     double* part = nullptr;       // 3 * kGrid block partials
     FcgDev* s = nullptr;
     double* hpart = nullptr;      // pinned: partials of the host-driven level CG
@@ -892,7 +1131,7 @@ LvView fine_view(const efs_ctx* c) {
 LvView level_view(const efs_ctx* c, const MLState* m, int l) {
     if (l == 0) return fine_view(c);
     const MLLevel& L = m->lv[l];
-    return LvView{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
+    return LvView{L.W, L.H, L.D, L.V, L.info, L.w, L.diag, L.wd};
 }
 // level 0 visits the chunk list, coarser levels every cell
 Walk walk_of(const efs_ctx* c, const MLState* m, int l) {
@@ -963,6 +1202,13 @@ cudaError_t ml_alloc(efs_ctx* c) {
     MCK(malloc_ml(m, &m->fb, N));
     MCK(malloc_ml(m, &m->chunks, m->nch));
     MCK(malloc_ml(m, &m->bcount, (long long)blocks_for(m->nch)));
+    if (nlev >= 1) {
+        long long W1 = 0;
+        { int w, h, d; ml_level_dims(c, 1, &w, &h, &d); W1 = (long long)w * h * d; }
+        m->cnch = (W1 + 31) / 32;
+        MCK(malloc_ml(m, &m->cchunks, m->cnch));
+        MCK(malloc_ml(m, &m->cbcount, (long long)blocks_for(m->cnch)));
+    }
     MCK(malloc_ml(m, &m->part, 3LL * kGrid));
     MCK(malloc_ml(m, &m->s, 1));
     MCK(cudaMemset(m->s, 0, sizeof(FcgDev)));
@@ -973,6 +1219,7 @@ cudaError_t ml_alloc(efs_ctx* c) {
         MCK(malloc_ml(m, &L.info, L.V));
         MCK(malloc_ml(m, &L.w, 6 * L.V));
         MCK(malloc_ml(m, &L.diag, L.V));
+        MCK(malloc_ml(m, &L.wd, L.V));
         MCK(malloc_ml(m, &L.r, L.V));
         MCK(malloc_ml(m, &L.z, L.V));
         MCK(malloc_ml(m, &L.t, L.V));
@@ -980,11 +1227,6 @@ cudaError_t ml_alloc(efs_ctx* c) {
     MCK(cudaMallocHost(reinterpret_cast<void**>(&m->hpart), 3 * kGrid * sizeof(double)));
     MCK(cudaStreamCreateWithFlags(&m->cap1, cudaStreamNonBlocking));
     MCK(cudaStreamCreateWithFlags(&m->cap2, cudaStreamNonBlocking));
-    // the level-0 reduction kernels run one wave of resident blocks (each thread loops over several 4-cell
-    // groups): fewer block partials to order and sum at the end
-    int occ = 0;
-    MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_q_smooth<true>, kThreads, 0));
-    m->qred_grid = (unsigned)std::max(1, occ) * (unsigned)std::max(1, c->sm_count);
     return cudaSuccess;
 }
 
@@ -992,21 +1234,34 @@ int ml_levels(const efs_ctx* c) { return c->ml ? c->ml->nlev : ml_resolve_levels
 
 LvView ml_view(const efs_ctx* c, int level) { return level_view(c, c->ml, level); }
 
-// The hierarchy's matrices and the level-0 chunk list from the current rowinfo.
+// the level-0 restriction walks level 1's chunk list when level 1's rows are whole 32-cell chunks of its grid rows
+static bool restrict_list(const efs_ctx* c) { return c->g.W % 64 == 0 && c->g.H >= 4 && c->g.D >= 4; }
+
+// The hierarchy's matrices and the level-0 chunk list from the current rowinfo; with restrict_list, level 1's
+// chunk list, and level 1's right-hand side zeroed (k_q_restrict writes only the listed chunks).
 cudaError_t ml_build(efs_ctx* c, cudaStream_t st) {
     MLState* m = c->ml;
     const long long N = c->g.N;
     const unsigned nb = blocks_for(m->nch);
     k_chunks_count<<<nb, kThreads, 0, st>>>(c->rowinfo, N, m->nch, m->bcount);
-    k_chunks_scan<<<1, 1024, 0, st>>>(m->bcount, (int)nb, m->s);
+    k_chunks_scan<<<1, 1024, 0, st>>>(m->bcount, (int)nb, &m->s->nchunks);
     k_chunks_write<<<nb, kThreads, 0, st>>>(c->rowinfo, N, m->nch, m->bcount, m->chunks);
     MCK(cudaGetLastError());
     for (int l = 1; l <= m->nlev; l++) {
         const MLLevel& L = m->lv[l];
-        const LvOut out{L.W, L.H, L.D, L.V, L.info, L.w, L.diag};
+        const LvOut out{L.W, L.H, L.D, L.V, L.info, L.w, L.diag, L.wd};
         if (l == 1) k_ml_build<true><<<blocks_for(L.V), kThreads, 0, st>>>(level_view(c, m, 0), out);
         else k_ml_build<false><<<blocks_for(L.V), kThreads, 0, st>>>(level_view(c, m, l - 1), out);
         MCK(cudaGetLastError());
+    }
+    if (m->nlev >= 1 && restrict_list(c)) {
+        const MLLevel& L1 = m->lv[1];
+        const unsigned nb1 = blocks_for(m->cnch);
+        k_chunks_count<<<nb1, kThreads, 0, st>>>(L1.info, L1.V, m->cnch, m->cbcount);
+        k_chunks_scan<<<1, 1024, 0, st>>>(m->cbcount, (int)nb1, &m->s->ncchunks);
+        k_chunks_write<<<nb1, kThreads, 0, st>>>(L1.info, L1.V, m->cnch, m->cbcount, m->cchunks);
+        MCK(cudaGetLastError());
+        MCK(cudaMemsetAsync(L1.r, 0, (size_t)L1.V * sizeof(float), st));
     }
     return cudaSuccess;
 }
@@ -1020,8 +1275,10 @@ cudaError_t ml_matvec(const LvView& L, const float* x, float* y, cudaStream_t st
 namespace {
 
 // level 0 takes the 128-bit kernels when its rows are whole 32-cell chunks of grid rows
-bool quad_level0(const efs_ctx* c) { return (c->g.W % 32) == 0; }
+bool quad_level0(const efs_ctx* c) { return (c->g.W % 32) == 0 && c->g.H >= 4 && c->g.D >= 4; }
 QWalk qwalk_of(const MLState* m) { return QWalk{m->chunks, m->s}; }
+// k_q_restrict: one warp per listed level-1 chunk (at most all of them)
+unsigned q_restrict_grid(const MLState* m) { return grid_for(m->cnch * 32); }
 
 // one damped Jacobi sweep at level l (zin null: from zero); dots: FCG's z.q and r.z with beta (level 0 only)
 cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zout, cudaStream_t st, bool dots = false) {
@@ -1031,8 +1288,12 @@ cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zo
     const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
     if (l == 0 && quad_level0(c)) {
         const unsigned gq = grid_for(c->g.N / 4);
-        if (dots) k_q_smooth<true><<<std::min(gq, m->qred_grid), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, m->q, m->s, m->part);
-        else k_q_smooth<false><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, kOmega, nullptr, m->s, m->part);
+        if (dots) {
+            k_q_smooth<true><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, m->q, m->part);
+            k_q_finish_dots<<<1, kThreads, 0, st>>>(m->part, (int)gq, m->s);
+        } else {
+            k_q_smooth<false><<<gq, kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zin, zout, nullptr, m->part);
+        }
         return cudaGetLastError();
     }
     if (l == 0) {
@@ -1041,6 +1302,18 @@ cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zo
     } else {
         k_ml_smooth<false, false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     }
+    return cudaGetLastError();
+}
+
+// the two pre-smoothing sweeps from zero at level l, in one pass
+cudaError_t sweep2(efs_ctx* c, int l, const float* r, float* zout, cudaStream_t st) {
+    MLState* m = c->ml;
+    const LvView L = level_view(c, m, l);
+    const Walk wk = walk_of(c, m, l);
+    if (l == 0 && quad_level0(c))
+        k_q_smooth2<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zout);
+    else if (l == 0) k_ml_smooth2<true><<<grid_for(c->g.N), kThreads, 0, st>>>(L, wk, r, zout, kOmega);
+    else k_ml_smooth2<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, zout, kOmega);
     return cudaGetLastError();
 }
 
@@ -1084,10 +1357,12 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
     MLLevel& N = m->lv[l + 1];
     const bool to_net = (l + 1 == nb) && net_bottom(c);
     // pre-smoothing, restriction
-    MCK(sweep(c, l, r, nullptr, t, st));
-    MCK(sweep(c, l, r, t, z, st));
+    MCK(sweep2(c, l, r, z, st));
     const unsigned gc = to_net ? grid_for(Cv.V) : blocks_for(Cv.V);
-    if (l == 0) k_ml_restrict<true><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
+    if (l == 0 && restrict_list(c))
+        k_q_restrict<<<q_restrict_grid(m), kThreads, 0, st>>>(m->cchunks, m->s, c->rowinfo, c->g.W, c->g.H, c->g.D, r, z,
+                                                              Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
+    else if (l == 0) k_ml_restrict<true><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
     else k_ml_restrict<false><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
     MCK(cudaGetLastError());
     MCK(vcycle(c, l + 1, N.r, N.z, N.t, st));
@@ -1096,8 +1371,8 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
     const double* a = to_net ? &m->s->ls_alpha : nullptr;
     const unsigned g = grid_for(l == 0 ? c->g.N : L.V);
     if (l == 0 && quad_level0(c))
-        k_q_prolong_smooth<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.H, r, z, ec, Cv.W,
-                                                                     Cv.H, a, t, kOmega);
+        k_q_prolong_smooth<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.H, c->g.D, r, z,
+                                                                     ec, Cv.W, Cv.H, a, t);
     else if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     else k_ml_prolong_smooth<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     MCK(cudaGetLastError());
@@ -1157,12 +1432,20 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             // z = M(r), with z.q, r.z and beta at its end
             if ((e = vcycle(c, 0, m->r, m->z, m->zt, b)) != cudaSuccess) break;
             const bool quad = quad_level0(c);
-            const unsigned gq = std::min(grid_for(N / 4), m->qred_grid);
-            if (quad) k_q_dir_matvec<<<gq, kThreads, 0, b>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, m->z, m->d, m->dn, m->q, m->s, m->part);
-            else k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
+            const unsigned gq = grid_for(N / 4);
+            if (quad) {
+                k_q_dir_matvec<<<gq, kThreads, 0, b>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, m->z, m->d, m->dn, m->q, m->s, m->part);
+                k_q_finish_dq<<<1, kThreads, 0, b>>>(m->part, (int)gq, m->s);
+            } else {
+                k_fcg_dir_matvec<<<g, kThreads, 0, b>>>(F, wk, m->z, m->d, m->dn, m->q, m->s, m->part);
+            }
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
-            if (quad) k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
-            else k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+            if (quad) {
+                k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->x64, m->r, m->dn, m->d, m->q, m->s, m->part);
+                k_q_finish_rr<<<1, kThreads, 0, b>>>(m->part, (int)gq, m->s, h_verify);
+            } else {
+                k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+            }
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
             cudaGraph_t vbody = nullptr;
@@ -1290,11 +1573,12 @@ cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float
     for (int l = 0; l < m->nlev; l++) {
         const LvView L = level_view(c, m, l);
         float* z = (l == 0) ? m->z : m->lv[l].z;
-        float* t = (l == 0) ? m->zt : m->lv[l].t;
         const LvView Cv = level_view(c, m, l + 1);
-        MCK(sweep(c, l, r, nullptr, t, st));
-        MCK(sweep(c, l, r, t, z, st));
-        if (l == 0) k_ml_restrict<true><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[1].r, nullptr, m->s, m->part);
+        MCK(sweep2(c, l, r, z, st));
+        if (l == 0 && restrict_list(c))
+            k_q_restrict<<<q_restrict_grid(m), kThreads, 0, st>>>(m->cchunks, m->s, c->rowinfo, c->g.W, c->g.H, c->g.D, r,
+                                                                  z, Cv, m->lv[1].r, nullptr, m->s, m->part);
+        else if (l == 0) k_ml_restrict<true><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[1].r, nullptr, m->s, m->part);
         else k_ml_restrict<false><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[l + 1].r, nullptr, m->s, m->part);
         MCK(cudaGetLastError());
         r = m->lv[l + 1].r;

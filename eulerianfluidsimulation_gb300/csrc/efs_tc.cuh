@@ -286,32 +286,49 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     if (warp == 0) tmem_dealloc(tmem, kCols);
 }
 
-// Finishes a split convolution: per voxel and 8 channels, the splits' partial sums in split order, then bias,
-// ReLU, the skip addition and the stores of k_conv3_tc's epilogue.
-template <int COUT>
+// Finishes a split convolution: per voxel and 4 channels, LANES lanes of one warp sum the splits k = lane,
+// lane + LANES, ... in order, then a fixed butterfly over the LANES lanes (every lane ends with the same sum);
+// bias, ReLU, the skip addition and the stores of k_conv3_tc's epilogue.  With many splits (the coarse layers run
+// 27-54 over a few thousand items) 8 lanes keep 8 loads in flight per item; with few, one lane per item.
+template <int LANES>
+__host__ __device__ constexpr int split_lanes_ok() { return LANES == 1 || LANES == 8; }
+inline int split_lanes(int splits) { return splits >= 16 ? 8 : 1; }
+template <int COUT, int LANES>
 __global__ void k_conv_split_reduce(const float* __restrict__ partial, int splits, int V, const float* __restrict__ bias,
                                     const __nv_bfloat16* __restrict__ skip, __nv_bfloat16* __restrict__ out,
                                     float* __restrict__ out32, int relu) {
-    const long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (item >= (long long)V * (COUT / 8)) return;
-    const int v = (int)(item / (COUT / 8)), c0 = (int)(item % (COUT / 8)) * 8;
-    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < splits; k++) {
-        const float4* src = reinterpret_cast<const float4*>(partial + ((size_t)k * V + v) * COUT + c0);
-        const float4 p0 = src[0], p1 = src[1];
-        acc[0] += p0.x; acc[1] += p0.y; acc[2] += p0.z; acc[3] += p0.w;
-        acc[4] += p1.x; acc[5] += p1.y; acc[6] += p1.z; acc[7] += p1.w;
+    static_assert(split_lanes_ok<LANES>(), "LANES");
+    const long long item = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / LANES;
+    const int lane = (int)(threadIdx.x % LANES);
+    const bool live = item < (long long)V * (COUT / 4);
+    const int v = live ? (int)(item / (COUT / 4)) : 0, c0 = live ? (int)(item % (COUT / 4)) * 4 : 0;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live) {
+#pragma unroll 4
+        for (int k = lane; k < splits; k += LANES) {
+            const float4 p = *reinterpret_cast<const float4*>(partial + ((size_t)k * V + v) * COUT + c0);
+            acc.x += p.x; acc.y += p.y; acc.z += p.z; acc.w += p.w;
+        }
     }
-    __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-        float t = acc[j] + (bias ? bias[c0 + j] : 0.f);
+    for (int o = LANES / 2; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+        acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
+    }
+    if (!live || lane != 0) return;
+    const float a4[4] = {acc.x, acc.y, acc.z, acc.w};
+    __align__(8) __nv_bfloat16 o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        float t = a4[j] + (bias ? bias[c0 + j] : 0.f);
         if (relu) t = fmaxf(t, 0.f);
         if (skip) t += __bfloat162float(skip[(size_t)v * COUT + c0 + j]);
         o[j] = __float2bfloat16(t);
         if (out32 && c0 + j == 0) out32[v] = t;
     }
-    if (out) *reinterpret_cast<uint4*>(out + (size_t)v * COUT + c0) = *reinterpret_cast<const uint4*>(o);
+    if (out) *reinterpret_cast<uint2*>(out + (size_t)v * COUT + c0) = *reinterpret_cast<const uint2*>(o);
 }
 
 // ============================================================================================================

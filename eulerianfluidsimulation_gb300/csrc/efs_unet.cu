@@ -590,10 +590,19 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
             const cudaError_t ce = cudaGetLastError();
             if (ce != cudaSuccess) return ce;
         }
-        const unsigned rg = nblk(L.V * (cout / 8));
-        if (cout == 16) tc::k_conv_split_reduce<16><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
-        else if (cout == 32) tc::k_conv_split_reduce<32><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
-        else tc::k_conv_split_reduce<64><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu);
+        const int lanes = tc::split_lanes(ks);
+        const unsigned rg = nblk(L.V * (cout / 4) * lanes);
+#define EFS_SPLIT_REDUCE(CO, LN) tc::k_conv_split_reduce<CO, LN><<<rg, 256, 0, st>>>(u->split, ks, (int)L.V, bias, skip, out, out32, relu)
+        if (lanes == 8) {
+            if (cout == 16) EFS_SPLIT_REDUCE(16, 8);
+            else if (cout == 32) EFS_SPLIT_REDUCE(32, 8);
+            else EFS_SPLIT_REDUCE(64, 8);
+        } else {
+            if (cout == 16) EFS_SPLIT_REDUCE(16, 1);
+            else if (cout == 32) EFS_SPLIT_REDUCE(32, 1);
+            else EFS_SPLIT_REDUCE(64, 1);
+        }
+#undef EFS_SPLIT_REDUCE
         return cudaGetLastError();
     }
     if (cout == 16) tc::k_conv3_tc<16><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
