@@ -92,13 +92,14 @@ __device__ __forceinline__ T lapply(const LvView& L, long long i, const T* x, fl
     return s;
 }
 
-// The cells a level kernel visits: at level 0 the 32-cell chunks that hold a matrix row (the list built at the
-// start of the solve, warp-aligned), at coarser levels every cell.  item -> cell, or -1 past the end.
+// The cells a level kernel visits: at level 0 (and at level 1 when its list is built) the 32-cell chunks that hold a
+// matrix row (the list built at the start of the solve, warp-aligned, *count of them), at coarser levels every
+// cell.  item -> cell, or -1 past the end.  Only rows are read at a level, so unvisited cells are never needed.
 struct Walk {
-    const int* chunks;                // level 0 only
-    const FcgDev* s;
+    const int* chunks;
+    const int* count;
     long long V;
-    __device__ __forceinline__ long long items() const { return chunks ? (long long)s->nchunks * 32 : V; }
+    __device__ __forceinline__ long long items() const { return chunks ? (long long)*count * 32 : V; }
     __device__ __forceinline__ long long cell(long long t) const {
         if (!chunks) return t;
         const long long i = (long long)chunks[t >> 5] * 32 + (t & 31);
@@ -481,16 +482,16 @@ __global__ void k_ml_matvec(LvView L, const float* __restrict__ x, float* __rest
 template <bool FINE>
 __global__ void k_ml_line_search(LvView L, Walk wk, const float* __restrict__ e, const float* __restrict__ r, FcgDev* s,
                                  double* __restrict__ part) {
-    double er = 0, eae = 0;
+    float er = 0.f, eae = 0.f;
     WALK(wk, t, i) {
         float dg, w[6];
         if (!lrow<FINE>(L, i, dg, w)) continue;
-        const double ei = e[i];
-        er += ei * (double)r[i];
-        eae += ei * (double)lapply<float>(L, i, e, dg, w);
+        const float ei = e[i];
+        er += ei * r[i];
+        eae += ei * lapply<float>(L, i, e, dg, w);
     }
     double tot[3];
-    double v[2] = {er, eae};
+    float v[2] = {er, eae};
     if (reduce_last(v, part, s->count, tot)) {
         const double a = (tot[1] != 0.0) ? tot[0] / tot[1] : 0.0;
         s->ls_alpha = isfinite(a) ? a : 0.0;
@@ -1125,6 +1126,10 @@ cudaError_t malloc_ml(MLState* m, T** p, long long count) {
     return e;
 }
 
+// Level 1's chunk list is built (and walked by level 1's kernels and the level-0 restriction) when level 1's rows
+// are whole 32-cell chunks of its grid rows.
+bool restrict_list(const efs_ctx* c) { return c->g.W % 64 == 0 && c->g.H >= 4 && c->g.D >= 4; }
+
 LvView fine_view(const efs_ctx* c) {
     return LvView{c->g.W, c->g.H, c->g.D, (long long)c->g.N, c->rowinfo, nullptr, nullptr};
 }
@@ -1135,8 +1140,9 @@ LvView level_view(const efs_ctx* c, const MLState* m, int l) {
 }
 // level 0 visits the chunk list, coarser levels every cell
 Walk walk_of(const efs_ctx* c, const MLState* m, int l) {
-    if (l == 0) return Walk{m->chunks, m->s, (long long)c->g.N};
-    return Walk{nullptr, m->s, m->lv[l].V};
+    if (l == 0) return Walk{m->chunks, &m->s->nchunks, (long long)c->g.N};
+    if (l == 1 && m->cchunks && restrict_list(c)) return Walk{m->cchunks, &m->s->ncchunks, m->lv[1].V};
+    return Walk{nullptr, nullptr, m->lv[l].V};
 }
 
 }  // namespace
@@ -1234,9 +1240,6 @@ int ml_levels(const efs_ctx* c) { return c->ml ? c->ml->nlev : ml_resolve_levels
 
 LvView ml_view(const efs_ctx* c, int level) { return level_view(c, c->ml, level); }
 
-// the level-0 restriction walks level 1's chunk list when level 1's rows are whole 32-cell chunks of its grid rows
-static bool restrict_list(const efs_ctx* c) { return c->g.W % 64 == 0 && c->g.H >= 4 && c->g.D >= 4; }
-
 // The hierarchy's matrices and the level-0 chunk list from the current rowinfo; with restrict_list, level 1's
 // chunk list, and level 1's right-hand side zeroed (k_q_restrict writes only the listed chunks).
 cudaError_t ml_build(efs_ctx* c, cudaStream_t st) {
@@ -1300,7 +1303,7 @@ cudaError_t sweep(efs_ctx* c, int l, const float* r, const float* zin, float* zo
         if (dots) k_ml_smooth<true, true><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, m->q, m->s, m->part);
         else k_ml_smooth<true, false><<<g, kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     } else {
-        k_ml_smooth<false, false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
+        k_ml_smooth<false, false><<<grid_for(L.V), kThreads, 0, st>>>(L, wk, r, zin, zout, kOmega, nullptr, m->s, m->part);
     }
     return cudaGetLastError();
 }
@@ -1313,7 +1316,7 @@ cudaError_t sweep2(efs_ctx* c, int l, const float* r, float* zout, cudaStream_t 
     if (l == 0 && quad_level0(c))
         k_q_smooth2<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.WH, r, zout);
     else if (l == 0) k_ml_smooth2<true><<<grid_for(c->g.N), kThreads, 0, st>>>(L, wk, r, zout, kOmega);
-    else k_ml_smooth2<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, zout, kOmega);
+    else k_ml_smooth2<false><<<grid_for(L.V), kThreads, 0, st>>>(L, wk, r, zout, kOmega);
     return cudaGetLastError();
 }
 
@@ -1374,7 +1377,7 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
         k_q_prolong_smooth<<<grid_for(c->g.N / 4), kThreads, 0, st>>>(qwalk_of(m), c->rowinfo, c->g.W, c->g.H, c->g.D, r, z,
                                                                      ec, Cv.W, Cv.H, a, t);
     else if (l == 0) k_ml_prolong_smooth<true><<<g, kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
-    else k_ml_prolong_smooth<false><<<blocks_for(L.V), kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
+    else k_ml_prolong_smooth<false><<<grid_for(L.V), kThreads, 0, st>>>(L, wk, r, z, ec, Cv, a, t, kOmega);
     MCK(cudaGetLastError());
     return sweep(c, l, r, t, z, st, l == 0);
 }

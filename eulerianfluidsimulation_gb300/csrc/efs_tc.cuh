@@ -153,6 +153,9 @@ struct ConvArgs {
     // partial null: one CTA per 128 voxels runs every step and finishes the layer itself.
     float* partial;
     int split_per;
+    // up != 0: the input is the grid of half the resolution (ceil(W/2) x ceil(H/2) x ceil(D/2) voxels) read as its
+    // nearest up-sampling: voxel (x, y, z) takes the input voxel (x/2, y/2, z/2)
+    int up;
 };
 
 constexpr int kConvThreads = 128;
@@ -196,7 +199,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
         const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
         const int nx = x + dx, ny = y + dy, nz = z + dz;
         const bool ok = vin && nx >= 0 && nx < a.W && ny >= 0 && ny < a.H && nz >= 0 && nz < a.D;
-        const __nv_bfloat16* src = ok ? a.in + ((size_t)((nz * a.H + ny) * a.W + nx) * a.cin + cc * 16) : a.in;
+        const int iv = a.up ? (((nz >> 1) * ((a.H + 1) >> 1) + (ny >> 1)) * ((a.W + 1) >> 1) + (nx >> 1))
+                            : ((nz * a.H + ny) * a.W + nx);
+        const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + cc * 16) : a.in;
         cp_async16(bufA[b] + tile_off(tid, 0), src, ok);
         cp_async16(bufA[b] + tile_off(tid, 8), src + 8, ok);
         if (tid < 2 * COUT) {

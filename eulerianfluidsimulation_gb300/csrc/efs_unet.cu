@@ -561,20 +561,32 @@ cudaError_t conv_halo(UNetState* u, const bf16* in, const bf16* wt, int cin, int
     return launch_halo<64>(a, L.W, L.H, L.D, sm_count, st);
 }
 
-cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
-                 const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st) {
+// the implicit-GEMM (im2col) kernel serves the level; it can read an up-sampled input in place
+bool conv_im2col(const UNetState* u, int level, int cin) {
     const Level& L = u->L[level];
-    if (L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64)
+    return !(L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64);
+}
+
+// up: `in` is the next coarser level's tensor, read as its nearest up-sampling (im2col levels only)
+cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
+                 const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st, bool up = false) {
+    const Level& L = u->L[level];
+    if (!conv_im2col(u, level, cin)) {
+        if (up) return cudaErrorInvalidValue;
         return conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st);
-    tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0};
+    }
+    tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0, up ? 1 : 0};
     const unsigned grid = (unsigned)((L.V + 127) / 128);
     (void)layer;
     // Small grids (the coarse levels of the network, and the whole network on FCG's bottom grid) give too few
     // CTAs, each running all 27 x cin/16 MMA steps in sequence: split the steps over more CTAs, then sum.
     const int s_all = 27 * (cin / 16);
     int ks = 1, per = s_all;
-    if (!pre && u->split && (int)grid < 8 * u->sm) {
-        ks = std::min(s_all, (8 * u->sm + (int)grid - 1) / (int)grid);
+    // as many splits as fill one wave of resident CTAs (7 per SM: kConvSmem and the TMEM columns): a second,
+    // mostly empty wave costs a whole CTA lifetime
+    const int slots = 7 * u->sm;
+    if (!pre && u->split && (int)grid < slots) {
+        ks = std::min(s_all, slots / (int)grid);
         per = (s_all + ks - 1) / ks;
         ks = (s_all + per - 1) / per;   // every split gets at least one step
         if ((long long)ks * L.V * cout > u->split_cap) ks = 1;
@@ -676,15 +688,24 @@ cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, c
     mark(4);
     UCK(conv(u, 2, u->p1, u->wf[2], 32, 64, 2, B[2], nullptr, u->e2, nullptr, train ? u->a2 : nullptr, 1, st));
     mark(5);
-    k_up<<<nblk(L[1].V * 8), 256, 0, st>>>(u->e2, L[2], u->u2, L[1], 64);
-    UCK(cudaGetLastError());
+    // the up-samplings: read in place by the next convolution where it is the implicit-GEMM kernel and nothing
+    // keeps the up-sampled tensor (training's weight gradients read it)
+    const bool up3 = !train && conv_im2col(u, 1, 64), up4 = !train && conv_im2col(u, 0, 32);
+    if (!up3) {
+        k_up<<<nblk(L[1].V * 8), 256, 0, st>>>(u->e2, L[2], u->u2, L[1], 64);
+        UCK(cudaGetLastError());
+    }
     mark(6);
-    UCK(conv(u, 3, u->u2, u->wf[3], 64, 32, 1, B[3], u->e1, u->d1, nullptr, train ? u->a3 : nullptr, 1, st));
+    UCK(conv(u, 3, up3 ? u->e2 : u->u2, u->wf[3], 64, 32, 1, B[3], u->e1, u->d1, nullptr, train ? u->a3 : nullptr, 1, st,
+             up3));
     mark(7);
-    k_up<<<nblk(L[0].V * 4), 256, 0, st>>>(u->d1, L[1], u->u1, L[0], 32);
-    UCK(cudaGetLastError());
+    if (!up4) {
+        k_up<<<nblk(L[0].V * 4), 256, 0, st>>>(u->d1, L[1], u->u1, L[0], 32);
+        UCK(cudaGetLastError());
+    }
     mark(8);
-    UCK(conv(u, 4, u->u1, u->wf[4], 32, 16, 0, B[4], u->e0, u->d0, nullptr, train ? u->a4 : nullptr, 1, st));
+    UCK(conv(u, 4, up4 ? u->d1 : u->u1, u->wf[4], 32, 16, 0, B[4], u->e0, u->d0, nullptr, train ? u->a4 : nullptr, 1, st,
+             up4));
     mark(9);
     mark(10);
     UCK(conv(u, 5, u->d0, u->wf[5], 16, 16, 0, B[5], nullptr, nullptr, u->y32, nullptr, 0, st));
