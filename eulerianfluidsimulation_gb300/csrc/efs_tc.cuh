@@ -160,17 +160,21 @@ struct ConvArgs {
 
 constexpr int kConvThreads = 128;
 constexpr int kConvSmem = 32 * 1024;   // also caps residency at 7 blocks/SM: 7 x 64 TMEM columns <= 512
+constexpr int kConvStages = 4;         // operand buffers of k_conv3_tc
+constexpr int kConvAhead = 2;          // steps its gathers run ahead of its MMAs
+static_assert(kConvAhead == 2 && kConvStages >= kConvAhead + 2, "the refill waits for the MMA two steps back");
 
 template <int COUT>
 __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
     constexpr int kABytes = 128 * 32, kBBytes = COUT * 32;
     constexpr uint32_t kCols = COUT < 32 ? 32 : COUT;
+    static_assert(kConvStages * (kABytes + kBBytes + 8) + 4 <= kConvSmem, "stages fit the shared memory");
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* bufA[2] = {smem, smem + kABytes};
-    unsigned char* bufB[2] = {smem + 2 * kABytes, smem + 2 * kABytes + kBBytes};
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * kABytes + 2 * kBBytes);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    auto bufA = [&](int b) { return smem + b * kABytes; };
+    auto bufB = [&](int b) { return smem + kConvStages * kABytes + b * kBBytes; };
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kConvStages * (kABytes + kBBytes));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + kConvStages);
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int V = a.D * a.H * a.W;
@@ -184,8 +188,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
 
     if (warp == 0) tmem_alloc(tslot, kCols);
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int b = 0; b < kConvStages; b++) mbar_init(&mbar[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     tc_fence_before();
@@ -202,46 +205,58 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
         const int iv = a.up ? (((nz >> 1) * ((a.H + 1) >> 1) + (ny >> 1)) * ((a.W + 1) >> 1) + (nx >> 1))
                             : ((nz * a.H + ny) * a.W + nx);
         const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + cc * 16) : a.in;
-        cp_async16(bufA[b] + tile_off(tid, 0), src, ok);
-        cp_async16(bufA[b] + tile_off(tid, 8), src + 8, ok);
+        cp_async16(bufA(b) + tile_off(tid, 0), src, ok);
+        cp_async16(bufA(b) + tile_off(tid, 8), src + 8, ok);
         if (tid < 2 * COUT) {
             const int n = tid >> 1, kg = tid & 1;
             const __nv_bfloat16* w = a.wt + ((size_t)(tap * chunks + cc) * COUT + n) * 16 + kg * 8;
-            cp_async16(bufB[b] + tile_off(n, kg * 8), w, true);
+            cp_async16(bufB(b) + tile_off(n, kg * 8), w, true);
         }
         cp_async_commit();
     };
 
+    // kConvStages buffers, the gathers kConvAhead steps ahead: while MMA s runs the gathers of steps s + 1 ..
+    // s + kConvAhead fly, and a buffer is refilled two steps after its MMA was issued, so a CTA does not wait for
+    // each MMA's completion in turn.  Buffer b serves steps b, b + kConvStages, ...; its mbarrier completes once
+    // per step, when that step's MMA has read it.
     bool ok = true;
-    load(0, 0);
+    for (int p = 0; p < kConvAhead && p < S; p++) load(p, p);
     for (int s = 0; s < S && ok; s++) {
-        const int b = s & 1;
-        if (s + 1 < S) {
-            // buffer b^1 was read by MMA s-1: wait for it before refilling
-            if (s >= 1 && !mbar_wait(&mbar[b ^ 1], ((s - 1) >> 1) & 1)) { ok = false; break; }
-            load(s + 1, b ^ 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
+        const int b = s % kConvStages;
+        const int next = s + kConvAhead;
+        if (next < S) {
+            // its buffer was read by MMA next - kConvStages (= s - 2): wait for that before refilling
+            const int pb = next % kConvStages, prev = next - kConvStages;
+            if (prev >= 0 && !mbar_wait(&mbar[pb], (uint32_t)((prev / kConvStages) & 1))) { ok = false; break; }
+            load(next, pb);
+        }
+        // step s's group is complete when at most (loads issued after it) groups are pending
+        switch (min(S - 1, next) - s) {
+            case 0: cp_async_wait<0>(); break;
+            case 1: cp_async_wait<1>(); break;
+            default: cp_async_wait<kConvAhead>(); break;
         }
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
-            const uint64_t ad = sdesc(smem_u32(bufA[b]), 128, 256);
-            const uint64_t bd = sdesc(smem_u32(bufB[b]), 128, 256);
+            const uint64_t ad = sdesc(smem_u32(bufA(b)), 128, 256);
+            const uint64_t bd = sdesc(smem_u32(bufB(b)), 128, 256);
             mma_bf16(tmem, ad, bd, idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
             mma_commit(&mbar[b]);
         }
     }
     cp_async_wait<0>();
-    // all MMAs (the last commit covers every earlier one), and the other buffer's last arrival
+    // all MMAs (the last commit covers every earlier one), and every buffer's last arrival
     const int last = S - 1;
-    if (ok && !mbar_wait(&mbar[last & 1], (last >> 1) & 1)) ok = false;
-    if (ok && last >= 1 && !mbar_wait(&mbar[(last - 1) & 1], ((last - 1) >> 1) & 1)) ok = false;
+    for (int b = 0; b < kConvStages && ok; b++) {
+        const int sl = last - ((last - b) % kConvStages + kConvStages) % kConvStages;   // last step on buffer b
+        if (sl >= 0 && !mbar_wait(&mbar[b], (uint32_t)((sl / kConvStages) & 1))) ok = false;
+    }
     if (!ok) {
         if (tid == 0) atomicOr(a.err, 1);
-        mbar_wait(&mbar[last & 1], (last >> 1) & 1);   // bounded: let MMAs in flight finish before freeing TMEM
+        // bounded: let MMAs in flight finish before freeing TMEM
+        mbar_wait(&mbar[last % kConvStages], (uint32_t)((last / kConvStages) & 1));
     }
     tc_fence_after();
     if (ok && a.partial) {
