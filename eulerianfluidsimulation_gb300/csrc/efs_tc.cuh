@@ -162,7 +162,7 @@ constexpr int kConvThreads = 128;
 constexpr int kConvSmem = 32 * 1024;   // also caps residency at 7 blocks/SM: 7 x 64 TMEM columns <= 512
 constexpr int kConvStages = 4;         // operand buffers of k_conv3_tc
 constexpr int kConvAhead = 2;          // steps its gathers run ahead of its MMAs
-static_assert(kConvAhead == 2 && kConvStages >= kConvAhead + 2, "the refill waits for the MMA two steps back");
+static_assert(kConvAhead == 2 && kConvStages == kConvAhead + 2, "the refill waits for the MMA two steps back");
 
 template <int COUT>
 __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
@@ -196,48 +196,55 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    auto load = [&](int s, int b) {
-        const int sg = s0 + s;
-        const int tap = sg / chunks, cc = sg - tap * chunks;
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    // The gathers walk the K steps in order, so a cursor carries the step's tap offset (dx, dy, dz), channel
+    // chunk and weight tile from one gather to the next instead of decomposing the step index each time.
+    const int clog = __ffs(chunks) - 1;   // chunks = cin / 16 is 1, 2 or 4
+    const int tap0 = s0 >> clog;
+    int ccur = s0 & (chunks - 1), dz = tap0 / 9 - 1, dy = (tap0 / 3) % 3 - 1, dx = tap0 % 3 - 1;
+    // which of the three offsets along each axis stay inside the grid (bit d + 1)
+    const unsigned mx = vin ? ((x > 0) | 2u | ((x < a.W - 1) << 2)) : 0u;
+    const unsigned my = (y > 0) | 2u | ((y < a.H - 1) << 2), mz = (z > 0) | 2u | ((z < a.D - 1) << 2);
+    const int PW = (a.W + 1) >> 1, PH = (a.H + 1) >> 1;
+    const uint32_t aoff0 = tile_off(tid, 0), aoff8 = tile_off(tid, 8);
+    const int wn = tid >> 1, wkg = tid & 1;
+    const __nv_bfloat16* wcur = a.wt + ((size_t)s0 * COUT + wn) * 16 + wkg * 8;
+    auto load = [&](int bi) {
+        const bool ok = (mx >> (dx + 1)) & (my >> (dy + 1)) & (mz >> (dz + 1)) & 1u;
         const int nx = x + dx, ny = y + dy, nz = z + dz;
-        const bool ok = vin && nx >= 0 && nx < a.W && ny >= 0 && ny < a.H && nz >= 0 && nz < a.D;
-        const int iv = a.up ? (((nz >> 1) * ((a.H + 1) >> 1) + (ny >> 1)) * ((a.W + 1) >> 1) + (nx >> 1))
-                            : ((nz * a.H + ny) * a.W + nx);
-        const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + cc * 16) : a.in;
-        cp_async16(bufA(b) + tile_off(tid, 0), src, ok);
-        cp_async16(bufA(b) + tile_off(tid, 8), src + 8, ok);
-        if (tid < 2 * COUT) {
-            const int n = tid >> 1, kg = tid & 1;
-            const __nv_bfloat16* w = a.wt + ((size_t)(tap * chunks + cc) * COUT + n) * 16 + kg * 8;
-            cp_async16(bufB(b) + tile_off(n, kg * 8), w, true);
-        }
+        const int iv = a.up ? (((nz >> 1) * PH + (ny >> 1)) * PW + (nx >> 1)) : ((nz * a.H + ny) * a.W + nx);
+        const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + ccur * 16) : a.in;
+        cp_async16(bufA(bi) + aoff0, src, ok);
+        cp_async16(bufA(bi) + aoff8, src + 8, ok);
+        if (tid < 2 * COUT) cp_async16(bufB(bi) + tile_off(wn, wkg * 8), wcur, true);
         cp_async_commit();
+        // advance the cursor by one step
+        wcur += COUT * 16;
+        if (++ccur == chunks) {
+            ccur = 0;
+            if (++dx > 1) {
+                dx = -1;
+                if (++dy > 1) { dy = -1; ++dz; }
+            }
+        }
     };
 
     // kConvStages buffers, the gathers kConvAhead steps ahead: while MMA s runs the gathers of steps s + 1 ..
     // s + kConvAhead fly, and a buffer is refilled two steps after its MMA was issued, so a CTA does not wait for
     // each MMA's completion in turn.  Buffer b serves steps b, b + kConvStages, ...; its mbarrier completes once
-    // per step, when that step's MMA has read it.
+    // per step, when that step's MMA has read it.  Thread 0 alone polls that mbarrier; the step's barrier tells
+    // the others.
     bool ok = true;
-    for (int p = 0; p < kConvAhead && p < S; p++) load(p, p);
-    for (int s = 0; s < S && ok; s++) {
+    for (int p = 0; p < kConvAhead && p < S; p++) load(p);
+    for (int s = 0; s < S; s++) {
         const int b = s % kConvStages;
-        const int next = s + kConvAhead;
-        if (next < S) {
-            // its buffer was read by MMA next - kConvStages (= s - 2): wait for that before refilling
-            const int pb = next % kConvStages, prev = next - kConvStages;
-            if (prev >= 0 && !mbar_wait(&mbar[pb], (uint32_t)((prev / kConvStages) & 1))) { ok = false; break; }
-            load(next, pb);
-        }
-        // step s's group is complete when at most (loads issued after it) groups are pending
-        switch (min(S - 1, next) - s) {
-            case 0: cp_async_wait<0>(); break;
-            case 1: cp_async_wait<1>(); break;
-            default: cp_async_wait<kConvAhead>(); break;
-        }
+        // step s's gather is complete when at most the later steps' gathers already issued are pending
+        if (s + 1 < S) cp_async_wait<kConvAhead - 1>();
+        else cp_async_wait<0>();
         fence_async_smem();
-        __syncthreads();
+        const int next = s + kConvAhead, prev = next - kConvStages;
+        const bool gave_up = tid == 0 && next < S && prev >= 0 &&
+                             !mbar_wait(&mbar[next % kConvStages], (uint32_t)((prev / kConvStages) & 1));
+        if (__syncthreads_or(gave_up)) { ok = false; break; }
         if (tid == 0) {
             tc_fence_after();
             const uint64_t ad = sdesc(smem_u32(bufA(b)), 128, 256);
@@ -245,6 +252,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_tc(ConvArgs a) {
             mma_bf16(tmem, ad, bd, idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
             mma_commit(&mbar[b]);
         }
+        if (next < S) load(next % kConvStages);
     }
     cp_async_wait<0>();
     // all MMAs (the last commit covers every earlier one), and every buffer's last arrival
