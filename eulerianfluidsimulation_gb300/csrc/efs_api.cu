@@ -618,11 +618,11 @@ int efs_step(efs_ctx* c, int n_steps) {
     auto nb = c->timing_nodes_begin.find(key), ne = c->timing_nodes_end.find(key);
     const bool can_time = nb != c->timing_nodes_begin.end() && ne != c->timing_nodes_end.end();
     for (int k = 0; k < n_steps; k++) {
-        if (can_time && c->ev_used < (int)c->ev_begin.size()) {
+        if (can_time && c->ev_used < c->ev_capacity) {
             CK(cudaGraphExecEventRecordNodeSetEvent(exec, nb->second, c->ev_begin[c->ev_used]), "timing event");
             CK(cudaGraphExecEventRecordNodeSetEvent(exec, ne->second, c->ev_end[c->ev_used]), "timing event");
             c->ev_used++;
-        } else if (can_time && !c->ev_begin.empty()) {
+        } else if (can_time && c->ev_capacity > 0) {
             CK(cudaGraphExecEventRecordNodeSetEvent(exec, nb->second, c->ev_solve_begin), "timing event");
             CK(cudaGraphExecEventRecordNodeSetEvent(exec, ne->second, c->ev_solve_end), "timing event");
         }
@@ -707,18 +707,16 @@ int efs_total_mass(efs_ctx* c, double* out) {
 int efs_solve_timing_arm(efs_ctx* c, int capacity) {
     if (!c || capacity < 0) return EFS_ERR_ARG;
     CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
-    for (auto ev : c->ev_begin) cudaEventDestroy(ev);
-    for (auto ev : c->ev_end) cudaEventDestroy(ev);
-    c->ev_begin.clear();
-    c->ev_end.clear();
-    c->ev_used = 0;
-    for (int k = 0; k < capacity; k++) {
+    // the pool only grows (events stay alive while a graph's event-record nodes may refer to them)
+    while ((int)c->ev_begin.size() < capacity) {
         cudaEvent_t a, b;
         CK(cudaEventCreate(&a), "cudaEventCreate");
         CK(cudaEventCreate(&b), "cudaEventCreate");
         c->ev_begin.push_back(a);
         c->ev_end.push_back(b);
     }
+    c->ev_capacity = capacity;
+    c->ev_used = 0;
     // work counters restart with the pool
     CK(cudaMemset(&c->ctl->sum_iter_rows, 0, 2 * sizeof(double)), "cudaMemset");
     return EFS_OK;

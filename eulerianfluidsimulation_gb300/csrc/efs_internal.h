@@ -152,8 +152,9 @@ struct efs_ctx {
     std::map<efs::GraphKey, int> kernel_nodes;
 
     // solve timing pool
-    std::vector<cudaEvent_t> ev_begin, ev_end;
+    std::vector<cudaEvent_t> ev_begin, ev_end;   // only grows: a replayed graph's event nodes may hold any of them
     int ev_used = 0;
+    int ev_capacity = 0;                         // pairs armed by efs_solve_timing_arm
     cudaEvent_t ev_solve_begin = nullptr, ev_solve_end = nullptr;   // recorded inside the graph
 
     cudaEvent_t marks[8] = {};
