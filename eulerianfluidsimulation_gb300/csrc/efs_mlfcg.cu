@@ -52,6 +52,7 @@ constexpr int kArriveStride = 32;     // unsigned per counter line
 struct FcgDev {
     double rr, rz, dq, zq, bb, thr, alpha, beta, rr_window, rows;
     double ls_alpha;                  // bottom-level line search factor of the current V-cycle (1 without the network)
+    float alpha_hi, alpha_lo, beta_f; // alpha as a float pair and beta in float, for the level-0 kernels
     int it, conv, stall, verify, fallback, nchunks;
     int ncchunks;                     // level 1's 32-cell chunks that hold a row (the restriction's list)
     // arrival counters (groups, then the top), back to 0 after each reduction
@@ -90,6 +91,39 @@ __device__ __forceinline__ T lapply(const LvView& L, long long i, const T* x, fl
     for (int k = 0; k < 6; k++)
         if (w[k] != 0.f) s += (T)w[k] * x[i + noff(L, k)];
     return s;
+}
+
+// FCG's x as a pair of floats, x.x + x.y with |x.y| below half an ulp of x.x: about 48 significant bits, updated
+// on the FP32 pipe (GB300's FP64 rate made the FP64 update of every row a sixth of the vector update's time).
+// pair_add returns x + (ah + al) d: the product's rounding error by FMA, the sum's by TwoSum, renormalised.
+__device__ __forceinline__ float2 pair_add(float2 x, float ah, float al, float d) {
+    const float p = __fmul_rn(ah, d);
+    const float pe = fmaf(al, d, fmaf(ah, d, -p));
+    const float s = __fadd_rn(x.x, p);
+    const float bb = __fsub_rn(s, x.x);
+    const float t = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    const float lo = __fadd_rn(__fadd_rn(t, x.y), pe);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+__device__ __forceinline__ double pair_val(float2 x) { return (double)x.x + (double)x.y; }
+// (A x)_i in FP64 for x held as float pairs (lapply's order)
+__device__ __forceinline__ double lapply_pair(const LvView& L, long long i, const float2* x, float dg, const float (&w)[6]) {
+    double s = (double)dg * pair_val(x[i]);
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        if (w[k] != 0.f) s += (double)w[k] * pair_val(x[i + noff(L, k)]);
+    return s;
+}
+// alpha / beta for the float kernels
+__device__ __forceinline__ void set_alpha(FcgDev* s, double a) {
+    s->alpha = a;
+    s->alpha_hi = (float)a;
+    s->alpha_lo = (float)(a - (double)s->alpha_hi);
+}
+__device__ __forceinline__ void set_beta(FcgDev* s, double b) {
+    s->beta = b;
+    s->beta_f = (float)b;
 }
 
 // The cells a level kernel visits: at level 0 (and at level 1 when its list is built) the 32-cell chunks that hold a
@@ -378,7 +412,7 @@ __global__ void k_ml_smooth(LvView L, Walk wk, const float* __restrict__ r, cons
             s->rz = tot[1];
             double beta = 0.0;
             if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
-            s->beta = isfinite(beta) ? beta : 0.0;
+            set_beta(s, isfinite(beta) ? beta : 0.0);
         }
     }
 }
@@ -515,7 +549,7 @@ __global__ void k_take_dots(LvView F, Walk wk, const float* __restrict__ e, cons
         s->rz = tot[1];
         double beta = 0.0;
         if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
-        s->beta = isfinite(beta) ? beta : 0.0;
+        set_beta(s, isfinite(beta) ? beta : 0.0);
     }
 }
 
@@ -630,7 +664,7 @@ __global__ void k_q_finish_dots(const double* __restrict__ part, int n, FcgDev* 
     s->rz = tot[1];
     double beta = 0.0;
     if (s->it > 0 && s->dq != 0.0) beta = -tot[0] / s->dq;
-    s->beta = isfinite(beta) ? beta : 0.0;
+    set_beta(s, isfinite(beta) ? beta : 0.0);
 }
 // k_ml_smooth2 at level 0: the first sweep's values at the group and at its six neighbours from r and the
 // neighbours' counts (a neighbour with its stencil bit set is a row)
@@ -796,7 +830,7 @@ __global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, 
 __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ z,
                                const float* __restrict__ d, float* __restrict__ dn, float* __restrict__ q, FcgDev* s,
                                double* __restrict__ part) {
-    const float beta = (float)s->beta;
+    const float beta = s->beta_f;
     float dq = 0.f;
     QWALK(qw, i) {
         unsigned f[4];
@@ -827,28 +861,29 @@ __global__ void k_q_finish_dq(const double* __restrict__ part, int n, FcgDev* s)
     const double al = s->rz / tot[0];
     if (!(tot[0] < 0.0) || !isfinite(al)) {
         s->stall = 1;
-        s->alpha = 0.0;
+        set_alpha(s, 0.0);
     } else {
-        s->alpha = al;
+        set_alpha(s, al);
     }
 }
 // k_fcg_update at level 0
-__global__ void k_q_update(QWalk qw, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
+__global__ void k_q_update(QWalk qw, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
                            float* __restrict__ d, const float* __restrict__ q, const FcgDev* s, double* __restrict__ part) {
-    const double a = s->alpha;
-    const float af = (float)a;
+    const float af = s->alpha_hi, al = s->alpha_lo;
     float rr = 0.f;
     QWALK(qw, i) {
         float dv[4], rv[4], qv[4];
         ld4(dn, i, dv);
         ld4(r, i, rv);
         ld4(q, i, qv);
-        double2* x2 = reinterpret_cast<double2*>(x + i);
-        double2 x01 = x2[0], x23 = x2[1];
-        x01.x += a * (double)dv[0]; x01.y += a * (double)dv[1];
-        x23.x += a * (double)dv[2]; x23.y += a * (double)dv[3];
-        x2[0] = x01;
-        x2[1] = x23;
+        float4* x4 = reinterpret_cast<float4*>(x + i);
+        float4 x01 = x4[0], x23 = x4[1];
+        float2 p0 = pair_add(make_float2(x01.x, x01.y), af, al, dv[0]);
+        float2 p1 = pair_add(make_float2(x01.z, x01.w), af, al, dv[1]);
+        float2 p2 = pair_add(make_float2(x23.x, x23.y), af, al, dv[2]);
+        float2 p3 = pair_add(make_float2(x23.z, x23.w), af, al, dv[3]);
+        x4[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
+        x4[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             rv[k] = rv[k] - af * qv[k];
@@ -878,14 +913,14 @@ __global__ void k_q_finish_rr(const double* __restrict__ part, int n, FcgDev* s,
 // ---- FCG ------------------------------------------------------------------------------------------------------
 // x = 0, r = b on rows (0 on the other visited cells), d = q = 0; b.b and the row count; the stop threshold as
 // the CG solvers form it (k_solver): tol_rel^2 b.b rounded to float, or the absolute one
-__global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
+__global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, float2* __restrict__ x, float* __restrict__ r,
                            float* __restrict__ d, float* __restrict__ q, FcgDev* s, double* __restrict__ part,
                            float tol_rel, float abs_thr, int max_it, cudaGraphConditionalHandle loop) {
     double bb = 0, rows = 0;
     WALK(wk, t, i) {
         const bool row = F.info[i] & 0x8000u;
         const float bi = row ? b[i] : 0.f;
-        x[i] = 0.0;
+        x[i] = make_float2(0.f, 0.f);
         r[i] = bi;
         d[i] = 0.f;
         q[i] = 0.f;
@@ -913,7 +948,9 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, doubl
         s->verify = 0;
         s->fallback = 0;
         s->rr_window = s->rr;
-        s->rz = s->dq = s->zq = s->alpha = s->beta = 0;
+        s->rz = s->dq = s->zq = 0;
+        set_alpha(s, 0.0);
+        set_beta(s, 0.0);
         s->ls_alpha = 1.0;
         cudaGraphSetConditional(loop, (!s->conv && max_it > 0) ? 1u : 0u);
     }
@@ -922,7 +959,7 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, doubl
 // negative definite on the rows, so dn.q >= 0 (or a non-finite alpha) is a breakdown: the solve stalls.
 __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z, const float* __restrict__ d,
                                  float* __restrict__ dn, float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
-    const float beta = (float)s->beta;
+    const float beta = s->beta_f;
     float dq = 0.f;
     WALK(wk, t, i) {
         float dg, w[6];
@@ -948,23 +985,23 @@ __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z,
         const double a = s->rz / tot[0];
         if (!(tot[0] < 0.0) || !isfinite(a)) {
             s->stall = 1;
-            s->alpha = 0.0;
+            set_alpha(s, 0.0);
         } else {
-            s->alpha = a;
+            set_alpha(s, a);
         }
     }
 }
 // x += alpha dn, r -= alpha q, d = dn; r.r, the iteration count, the stall window and whether the true residual
 // is recomputed now (every 32 iterations and when the recurrence residual meets the threshold)
-__global__ void k_fcg_update(Walk wk, double* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
+__global__ void k_fcg_update(Walk wk, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
                              float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
                              cudaGraphConditionalHandle verify) {
-    const double a = s->alpha;
+    const float af = s->alpha_hi, al = s->alpha_lo;
     float rr = 0.f;
     WALK(wk, t, i) {
         const float di = dn[i];
-        x[i] += a * (double)di;
-        const float ri = (float)((double)r[i] - a * (double)q[i]);
+        x[i] = pair_add(x[i], af, al, di);
+        const float ri = r[i] - af * q[i];
         r[i] = ri;
         d[i] = di;
         rr += ri * ri;
@@ -984,13 +1021,13 @@ __global__ void k_fcg_update(Walk wk, double* __restrict__ x, float* __restrict_
     }
 }
 // r = b - A x in FP64 (rows); r.r and the convergence decision
-__global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b, const double* __restrict__ x,
+__global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b, const float2* __restrict__ x,
                                  float* __restrict__ r, FcgDev* s, double* __restrict__ part) {
     double rr = 0;
     WALK(wk, t, i) {
         float dg, w[6];
         float ri = 0.f;
-        if (lrow<true>(F, i, dg, w)) ri = (float)((double)b[i] - lapply<double>(F, i, x, dg, w));
+        if (lrow<true>(F, i, dg, w)) ri = (float)((double)b[i] - lapply_pair(F, i, x, dg, w));
         r[i] = ri;
         rr += (double)ri * ri;
     }
@@ -1012,15 +1049,15 @@ __global__ void k_fcg_post(FcgDev* s, cudaGraphConditionalHandle fallback) {
     cudaGraphSetConditional(fallback, (s->stall && !s->conv) ? 1u : 0u);
 }
 // fb = b - A x in FP64 on rows, 0 elsewhere (the right-hand side of the fallback CG; every cell written)
-__global__ void k_fcg_fb_rhs(LvView F, const float* __restrict__ b, const double* __restrict__ x, float* __restrict__ fb) {
+__global__ void k_fcg_fb_rhs(LvView F, const float* __restrict__ b, const float2* __restrict__ x, float* __restrict__ fb) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= F.V) return;
     float dg, w[6];
-    fb[i] = lrow<true>(F, i, dg, w) ? (float)((double)b[i] - lapply<double>(F, i, x, dg, w)) : 0.f;
+    fb[i] = lrow<true>(F, i, dg, w) ? (float)((double)b[i] - lapply_pair(F, i, x, dg, w)) : 0.f;
 }
-__global__ void k_fcg_fb_add(LvView F, Walk wk, double* __restrict__ x, const float* __restrict__ p) {
+__global__ void k_fcg_fb_add(LvView F, Walk wk, float2* __restrict__ x, const float* __restrict__ p) {
     WALK(wk, t, i) {
-        if (F.info[i] & 0x8000u) x[i] += (double)p[i];
+        if (F.info[i] & 0x8000u) x[i] = pair_add(x[i], 1.f, 0.f, p[i]);
     }
 }
 __global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
@@ -1028,11 +1065,12 @@ __global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
     s->fallback = 1;
     s->conv = ctl->converged;
 }
-__global__ void k_fcg_out(LvView F, Walk wk, const double* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
+__global__ void k_fcg_out(LvView F, Walk wk, const float2* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
     WALK(wk, t, i) {
         if (F.info[i] & 0x8000u) {
-            p[i] = (float)x[i];
-            p64[i] = x[i];
+            const double v = pair_val(x[i]);
+            p[i] = (float)v;
+            p64[i] = v;
         }
     }
 }
@@ -1100,7 +1138,7 @@ struct MLLevel {
 struct MLState {
     int nlev = 0;                 // aggregation levels of the allocated hierarchy
     MLLevel lv[4];                // lv[1..nlev]
-    double* x64 = nullptr;        // FCG vectors (fine grid)
+    float2* xp = nullptr;         // FCG's x as float pairs (pair_add), and its other vectors (fine grid)
     float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *dn = nullptr, *q = nullptr, *fb = nullptr;
     int* chunks = nullptr;        // level 0: the 32-cell chunks that hold a matrix row, in order
     int* bcount = nullptr;        // their per-block counts / offsets
@@ -1198,7 +1236,7 @@ cudaError_t ml_alloc(efs_ctx* c) {
     m->nlev = nlev;
     const long long N = c->g.N;
     m->nch = (N + 31) / 32;
-    MCK(malloc_ml(m, &m->x64, N));
+    MCK(malloc_ml(m, &m->xp, N));
     MCK(malloc_ml(m, &m->r, N));
     MCK(malloc_ml(m, &m->z, N));
     MCK(malloc_ml(m, &m->zt, N));
@@ -1420,7 +1458,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
     MCK(ml_build(c, st));
     cudaGraphConditionalHandle h_loop, h_verify, h_fb;
     MCK(make_handle(st, &h_loop));
-    k_fcg_init<<<g, kThreads, 0, st>>>(F, wk, c->div, m->x64, m->r, m->d, m->q, m->s, m->part, c->prm.tol_rel,
+    k_fcg_init<<<g, kThreads, 0, st>>>(F, wk, c->div, m->xp, m->r, m->d, m->q, m->s, m->part, c->prm.tol_rel,
                                       c->prm.solver_threshold, max_it, h_loop);
     MCK(cudaGetLastError());
 
@@ -1444,10 +1482,10 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             }
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
             if (quad) {
-                k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->x64, m->r, m->dn, m->d, m->q, m->s, m->part);
+                k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->xp, m->r, m->dn, m->d, m->q, m->s, m->part);
                 k_q_finish_rr<<<1, kThreads, 0, b>>>(m->part, (int)gq, m->s, h_verify);
             } else {
-                k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->x64, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+                k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->xp, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
             }
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
@@ -1455,7 +1493,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             if ((e = add_conditional(b, h_verify, cudaGraphCondTypeIf, &vbody)) != cudaSuccess) break;
             cudaStream_t v = m->cap2;
             if ((e = cudaStreamBeginCaptureToGraph(v, vbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-            k_fcg_true_resid<<<g, kThreads, 0, v>>>(F, wk, c->div, m->x64, m->r, m->s, m->part);
+            k_fcg_true_resid<<<g, kThreads, 0, v>>>(F, wk, c->div, m->xp, m->r, m->s, m->part);
             cudaError_t ve = cudaGetLastError();
             cudaGraph_t dummy = nullptr;
             cudaError_t ee = cudaStreamEndCapture(v, &dummy);
@@ -1480,10 +1518,10 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         MCK(cudaStreamBeginCaptureToGraph(b, fbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;
         do {
-            k_fcg_fb_rhs<<<blocks_for(N), kThreads, 0, b>>>(F, c->div, m->x64, m->fb);
+            k_fcg_fb_rhs<<<blocks_for(N), kThreads, 0, b>>>(F, c->div, m->xp, m->fb);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             if ((e = launch_solver_on(c, m->fb, &m->s->thr, b)) != cudaSuccess) break;
-            k_fcg_fb_add<<<g, kThreads, 0, b>>>(F, wk, m->x64, c->p);
+            k_fcg_fb_add<<<g, kThreads, 0, b>>>(F, wk, m->xp, c->p);
             k_fcg_fb_done<<<1, 32, 0, b>>>(m->s, c->ctl);
             e = cudaGetLastError();
         } while (0);
@@ -1492,7 +1530,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         MCK(e);
         MCK(ee);
     }
-    k_fcg_out<<<g, kThreads, 0, st>>>(F, wk, m->x64, c->p, c->p64);
+    k_fcg_out<<<g, kThreads, 0, st>>>(F, wk, m->xp, c->p, c->p64);
     k_fcg_stats<<<1, 32, 0, st>>>(m->s, c->ctl);
     return cudaGetLastError();
 }
