@@ -225,7 +225,7 @@ __device__ bool reduce_last(T (&v)[NV], double* part, unsigned* counter, double 
 // them: thread t adds blocks t, t + 256, ... with a compensated FP32 sum (Kahan), the 256 results go through a
 // fixed FP64 tree.  Blocks that waited for their own fence and arrival atomic before exiting had cost about
 // 20 us per 4096-block launch.
-constexpr int kFinishPer = kGrid / kThreads;   // partials per thread of a finisher block
+constexpr int kFinishPer = (kGrid + kThreads - 1) / kThreads;   // partials per thread of a finisher block
 template <int NV>
 __device__ bool finish_partials(const double* __restrict__ part, int n, double (&tot)[NV]) {
     __shared__ double sh[NV][kThreads / 32];
