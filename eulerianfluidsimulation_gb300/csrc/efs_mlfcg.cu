@@ -40,7 +40,11 @@ namespace {
 constexpr float kOmega = 0.8f;        // Jacobi damping
 constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the network
 constexpr int kThreads = 256;
-constexpr int kGrid = 4096;           // most blocks of a reduction kernel (the partials buffer holds one per block)
+// Most blocks of a level kernel (threads loop over the rest; the partials buffer holds one per block): 8 per SM
+// of GB300's 152.  A 4096-block launch of these short kernels spends microseconds distributing blocks (a trivial
+// 4096-block kernel takes 4.9 µs); at 1216 the preconditioner took 280 instead of 297 µs and the 256^3 solve
+// 12.8 instead of 13.7 ms (608, 912 and 1520 blocks were slower or equal).
+constexpr int kGrid = 1216;
 
 // Arrival counters of the last-block reductions: a block counts itself in group blockIdx.x % kArriveGroups, and
 // the last block of each group in the top counter.  One 128-byte line per counter: same-address atomics from
