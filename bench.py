@@ -385,7 +385,10 @@ def run_gb300(a):
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_solver launch on this "
                                   "workload, scaled by row-iterations" if traffic else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
-                "solve_ms_per_step": solve_ms / max(launches, 1), "algorithmic_bytes_per_launch": solve_bytes / max(launches, 1)}
+                "solve_ms_per_step": solve_ms / max(launches, 1), "algorithmic_bytes_per_launch": solve_bytes / max(launches, 1),
+                # the DRAM bytes per launch over the launch's time: what HBM actually moves (L2 keeps about half of the
+                # algorithmic bytes on chip), beside the algorithmic rate that `achieved` reports
+                "dram_gbs": (traffic / ((solve_ms / launches) / 1e3) / 1e9) if traffic and solve_ms > 0 else None}
     # the whole step: the stages' algorithmic bytes per interior cell plus the solve's per matrix row
     step_bytes = STEP_BYTES_PER_CELL_3D * (n - 2) ** 3 + solve_bytes / max(launches, 1)
     step_achieved = step_bytes / (ms / a.steps / 1e3) / 1e9
@@ -408,6 +411,8 @@ def run_gb300(a):
         h["forces"][...] = 0
         k_e2e = max(2, a.steps // 2)
         sim.synchronize()
+        se0 = sim.stats()
+        sim.solve_timing_arm(k_e2e)
         barrier()
         sim.mark(2)
         for _ in range(k_e2e):
@@ -417,8 +422,14 @@ def run_gb300(a):
         sim.mark(3)
         ms_e2e = sim.elapsed_ms(2, 3)
         barrier()
+        se1 = sim.stats()
+        e_launches, e_solve_ms, _, _ = sim.solve_timing_read()
+        # the e2e steps continue the trajectory after the timed steps: their solves may take other iteration
+        # counts than the main line's, so the line carries them
         e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
-               "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e,
+               "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e, "ms_per_step": ms_e2e / k_e2e,
+               "solve_iters_per_step": (se1.total_solve_steps - se0.total_solve_steps) / k_e2e,
+               "solve_ms_per_step": (e_solve_ms / e_launches) if e_launches else None,
                "api": "efs_step_host: upload vel,rho,gamma,boundary,forces + one step + download vel,rho,gamma,beta,div,p "
                       "(page-locked buffers; gamma/forces up and rho/gamma/beta/div down overlap the step)"}
     st2 = sim.stats()
