@@ -62,8 +62,9 @@ enum efs_solver {
     EFS_SOLVER_JACOBI = 0,      /* JacobiSolverCPU3D: max_steps/2 sweeps from p = 0                */
     EFS_SOLVER_CG = 1,          /* CGSolverCPU3D: p0 = b, true residual every 64 iterations        */
     /* No counterpart in the reference: flexible preconditioned CG (Notay's FCG(1)) on the same matrix and
-     * to the same stop rule as EFS_SOLVER_CG, from p0 = 0, with the pressure accumulated in FP64 and the true
-     * residual recomputed every 32 iterations and before stopping.  Its preconditioner is a multigrid
+     * to the same stop rule as EFS_SOLVER_CG, from p0 = 0, with the pressure accumulated as float pairs (about
+     * 48 significant bits; efs_download_pressure_fp64 gives their sum) and the true residual recomputed in
+     * FP64 every 32 iterations and before stopping.  Its preconditioner is a multigrid
      * V-cycle whose coarsest level is solved by the context's learned U-Net (3D; efs_unet_*, fcg_levels and
      * fcg_bottom below).  When the residual stalls (not halved over 10 iterations) or a direction breaks
      * down, the remaining residual system goes to plain CG (EFS_CG_MIXED_RECURRENCE).  The whole solve is
@@ -231,7 +232,8 @@ int  efs_step_host(efs_ctx* ctx, const float* vel, const float* rho, const float
 int  efs_reset_fields(efs_ctx* ctx);
 /* No counterpart in the reference.  The FP64 pressure of the last CG solve (N doubles, reference layout):
  * the FP64 iterate for EFS_CG_FP64, the FP64 accumulator with its increment folded in for the mixed
- * variants (the FP32 pressure field is this value rounded).  Matrix rows only; other cells hold stale
+ * variants, the float-pair iterate's sum for EFS_SOLVER_FCG_UNET (the FP32 pressure field is this value
+ * rounded).  Matrix rows only; other cells hold stale
  * values.  EFS_ERR_STATE for Jacobi and EFS_CG_REFERENCE, which keep no FP64 pressure. */
 int  efs_download_pressure_fp64(efs_ctx* ctx, double* host);
 
