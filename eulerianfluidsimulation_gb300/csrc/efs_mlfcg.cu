@@ -445,26 +445,43 @@ __global__ void k_ml_smooth2(LvView L, Walk wk, const float* __restrict__ r, flo
         zout[i] = zi;
     }
 }
-// rc[C] = sum over the merged rows i of C of (r - A z)_i.  scal (non-null: the level below is the network's):
-// the sum of rc^2 over the coarse rows, their count and 1 / rms into scal[0..2].
+// Restriction rc[C] = sum over the merged rows i of C of (r - A z)_i, in two passes whose threads each make one
+// load round trip (a thread gathering its eight children's stencils in sequence made the coarse levels'
+// restriction a chain of dependent loads): res = r - A z on the level's rows (visited cells), then per coarse
+// row the sum of its row children's res, children in the order x fastest, then y, then z.  scal (non-null: the
+// level below is the network's): the sum of rc^2 over the coarse rows, their count and 1 / rms into scal[0..2].
 template <bool FINE>
-__global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float* __restrict__ z, LvView Cv,
-                              float* __restrict__ rc, double* __restrict__ scal, FcgDev* s, double* __restrict__ part) {
+__global__ void k_ml_resid(LvView L, Walk wk, const float* __restrict__ r, const float* __restrict__ z,
+                           float* __restrict__ res) {
+    WALK(wk, t, i) {
+        float dg, w[6];
+        res[i] = lrow<FINE>(L, i, dg, w) ? r[i] - lapply<float>(L, i, z, dg, w) : 0.f;
+    }
+}
+template <bool FINE>
+__global__ void k_ml_sum8(LvView F, const float* __restrict__ res, LvView Cv, float* __restrict__ rc,
+                          double* __restrict__ scal, FcgDev* s, double* __restrict__ part) {
     double ss = 0, cnt = 0;
     for (long long C = blockIdx.x * (long long)blockDim.x + threadIdx.x; C < Cv.V; C += (long long)gridDim.x * blockDim.x) {
-        // a coarse cell is a row exactly when one of its children is (k_ml_build): the others sum nothing
         if (!(Cv.info[C] & 0x8000u)) { rc[C] = 0.f; continue; }
         const int c32 = (int)C;
         const int X = c32 % Cv.W, Y = (c32 / Cv.W) % Cv.H, Z = c32 / (Cv.W * Cv.H);
-        float acc = 0.f;
+        long long ch[8];
+        bool ok[8];
+#pragma unroll
         for (int c8 = 0; c8 < 8; c8++) {
             const int x = 2 * X + (c8 & 1), y = 2 * Y + ((c8 >> 1) & 1), zz = 2 * Z + (c8 >> 2);
-            if (x >= F.W || y >= F.H || zz >= F.D) continue;
-            const long long i = ((long long)zz * F.H + y) * F.W + x;
-            float dg, w[6];
-            if (!lrow<FINE>(F, i, dg, w)) continue;
-            acc += r[i] - lapply<float>(F, i, z, dg, w);
+            ok[c8] = x < F.W && y < F.H && zz < F.D;
+            ch[c8] = ok[c8] ? ((long long)zz * F.H + y) * F.W + x : 0;
         }
+        uint16_t f[8];
+        float v[8];
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++) { f[c8] = F.info[ch[c8]]; v[c8] = res[ch[c8]]; }
+        float acc = 0.f;
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++)
+            if (ok[c8] && (f[c8] & 0x8000u)) acc += v[c8];
         rc[C] = acc;
         if (scal) {
             ss += (double)acc * acc;
@@ -472,9 +489,8 @@ __global__ void k_ml_restrict(LvView F, const float* __restrict__ r, const float
         }
     }
     if (scal) {
-        double tot[3];
-        double v[2] = {ss, cnt};
-        if (reduce_last(v, part, s->count, tot)) {
+        double tot[3], v2[2] = {ss, cnt};
+        if (reduce_last(v2, part, s->count, tot)) {
             scal[0] = tot[0];
             scal[1] = tot[1];
             scal[2] = (tot[0] > 0 && tot[1] > 0) ? 1.0 / sqrt(tot[0] / tot[1]) : 1.0;
@@ -707,14 +723,14 @@ __global__ void k_q_smooth2(QWalk qw, const uint16_t* __restrict__ info, int W, 
         st4(zout, i, out);
     }
 }
-// k_ml_restrict at level 0 (width a multiple of 64): one warp per listed level-1 chunk, i.e. 32 coarse cells of a
+// The restriction at level 0 (width a multiple of 64): one warp per listed level-1 chunk, i.e. 32 coarse cells of a
 // coarse row that hold a row, and the 64 x 4 fine cells below them.  Lane 8 j + g takes the 4-cell groups g and
 // g + 8 of fine row j ((dy, dz) = (j & 1, j >> 1)) and sums each group's residuals into the two coarse cells the
 // group covers; a fixed butterfly over the four rows finishes the coarse sums, which lanes 0-7 store.  A group's
 // stencil is read where the group holds a row, and so lies in the grid's interior rows (the loads stay inside the
 // grid); a group without rows reads the interior group at WH + W + 4 (the grid has at least 4 cells on each side)
 // and adds nothing.  Coarse cells outside the listed chunks hold no row and stay 0 from the solve's set-up.
-// scal: as k_ml_restrict.
+// scal: as k_ml_sum8.
 __global__ void k_q_restrict(const int* __restrict__ cchunks, const FcgDev* s, const uint16_t* __restrict__ info, int W,
                              int H, int D, const float* __restrict__ r, const float* __restrict__ z, LvView Cv,
                              float* __restrict__ rc, double* __restrict__ scal, FcgDev* sw, double* __restrict__ part) {
@@ -1362,6 +1378,20 @@ cudaError_t sweep2(efs_ctx* c, int l, const float* r, float* zout, cudaStream_t 
     return cudaGetLastError();
 }
 
+// restriction from level l to l + 1 (the non-128-bit paths): residual into the level's scratch t, then the sums
+cudaError_t restrict2(efs_ctx* c, int l, const float* r, const float* z, float* t, float* rc, double* scal,
+                      cudaStream_t st) {
+    MLState* m = c->ml;
+    const LvView L = level_view(c, m, l), Cv = level_view(c, m, l + 1);
+    const Walk wk = walk_of(c, m, l);
+    if (l == 0) k_ml_resid<true><<<grid_for(c->g.N), kThreads, 0, st>>>(L, wk, r, z, t);
+    else k_ml_resid<false><<<grid_for(L.V), kThreads, 0, st>>>(L, wk, r, z, t);
+    MCK(cudaGetLastError());
+    if (l == 0) k_ml_sum8<true><<<grid_for(Cv.V), kThreads, 0, st>>>(L, t, Cv, rc, scal, m->s, m->part);
+    else k_ml_sum8<false><<<grid_for(Cv.V), kThreads, 0, st>>>(L, t, Cv, rc, scal, m->s, m->part);
+    return cudaGetLastError();
+}
+
 bool net_bottom(const efs_ctx* c) { return c->prm.fcg_bottom == EFS_FCG_BOTTOM_UNET && c->unet; }
 
 // z = M(r) at level l (r, z, t: that level's vectors).  Level 0 ends with FCG's z.q, r.z and beta.  At the
@@ -1403,12 +1433,10 @@ cudaError_t vcycle(efs_ctx* c, int l, const float* r, float* z, float* t, cudaSt
     const bool to_net = (l + 1 == nb) && net_bottom(c);
     // pre-smoothing, restriction
     MCK(sweep2(c, l, r, z, st));
-    const unsigned gc = to_net ? grid_for(Cv.V) : blocks_for(Cv.V);
     if (l == 0 && restrict_list(c))
         k_q_restrict<<<q_restrict_grid(m), kThreads, 0, st>>>(m->cchunks, m->s, c->rowinfo, c->g.W, c->g.H, c->g.D, r, z,
                                                               Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
-    else if (l == 0) k_ml_restrict<true><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
-    else k_ml_restrict<false><<<gc, kThreads, 0, st>>>(L, r, z, Cv, N.r, to_net ? unet_scale_slot(c) : nullptr, m->s, m->part);
+    else MCK(restrict2(c, l, r, z, t, N.r, to_net ? unet_scale_slot(c) : nullptr, st));
     MCK(cudaGetLastError());
     MCK(vcycle(c, l + 1, N.r, N.z, N.t, st));
     // prolongation folded into the first post-smoothing sweep, then the second sweep
@@ -1623,8 +1651,7 @@ cudaError_t ml_descend(efs_ctx* c, const float* r0, cudaStream_t st, const float
         if (l == 0 && restrict_list(c))
             k_q_restrict<<<q_restrict_grid(m), kThreads, 0, st>>>(m->cchunks, m->s, c->rowinfo, c->g.W, c->g.H, c->g.D, r,
                                                                   z, Cv, m->lv[1].r, nullptr, m->s, m->part);
-        else if (l == 0) k_ml_restrict<true><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[1].r, nullptr, m->s, m->part);
-        else k_ml_restrict<false><<<grid_for(Cv.V), kThreads, 0, st>>>(L, r, z, Cv, m->lv[l + 1].r, nullptr, m->s, m->part);
+        else MCK(restrict2(c, l, r, z, (l == 0) ? m->zt : m->lv[l].t, m->lv[l + 1].r, nullptr, st));
         MCK(cudaGetLastError());
         r = m->lv[l + 1].r;
     }
