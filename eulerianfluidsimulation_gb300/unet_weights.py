@@ -51,7 +51,7 @@ def _params(n, abi):
     return p
 
 
-def train(sizes=(128, 256), samples=(10000, 10000), trajectory=250, rounds=4, iters_per_round=1500, batch=8,
+def train(sizes=(128, 256), samples=(10000, 10000), trajectory=250, rounds=6, iters_per_round=3000, batch=8,
           lr=1e-3, synthetic=0.5, seed=0, log=print):
     """Collect samples along plain-CG trajectories at each grid size (`trajectory` steps per seeded scene, new
     scene after that), then train for `rounds` rounds of `iters_per_round` Adam steps on each size's samples
@@ -105,8 +105,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", action="store_true")
     ap.add_argument("--samples", type=int, default=10000, help="samples per grid size")
-    ap.add_argument("--rounds", type=int, default=4)
-    ap.add_argument("--iters", type=int, default=1500)
+    ap.add_argument("--rounds", type=int, default=6)
+    ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--out", default=WEIGHTS_PATH)
     a = ap.parse_args()
     if not a.train:
