@@ -244,13 +244,45 @@ __device__ __forceinline__ double lap_d(const double* x, uint16_t info, int i, c
         if (info & (1u << cg_bit(k))) sum += x[i + nb.o[k]];
     return sum - (double)((info >> 8) & 7) * x[i];
 }
-// L b in FP64 (p64 == b at the start)
-__device__ __forceinline__ double lap_df(const float* x, uint16_t info, int i, const Nb& nb) {
-    double sum = 0.0;
+
+// The mixed variants' pressure accumulator as float pairs (hi + lo, about 48 significant bits) in the memory of
+// a.p64, computed on the FP32 pipe with error-free transformations; GB300 runs FP64 at a small fraction of its
+// FP32 rate, and the FP64 residual replacement had cost about 70 µs at 256^3 each time.  Converted to doubles in
+// place at the end of the solve (efs_download_pressure_fp64).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ float2 df_renorm(float s, float e) {
+    const float hi = __fadd_rn(s, e);
+    return make_float2(hi, __fsub_rn(e, __fsub_rn(hi, s)));
+}
+__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
+    float s, e;
+    two_sum(x.x, y.x, s, e);
+    return df_renorm(s, __fadd_rn(e, __fadd_rn(x.y, y.y)));
+}
+__device__ __forceinline__ float2 df_add_f(float2 x, float y) {
+    float s, e;
+    two_sum(x.x, y, s, e);
+    return df_renorm(s, __fadd_rn(e, x.y));
+}
+// x times a small integer k (the diagonal count): the product's rounding error by FMA
+__device__ __forceinline__ float2 df_mul_k(float2 x, float k) {
+    const float ph = __fmul_rn(k, x.x);
+    return df_renorm(ph, fmaf(k, x.y, fmaf(k, x.x, -ph)));
+}
+// b - L x for the pair field x (lap_d's neighbour order), rounded to float
+__device__ __forceinline__ float df_resid(float b, const float2 (&xv)[7], uint16_t f) {
+    float2 sum = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 6; k++)
-        if (info & (1u << cg_bit(k))) sum += (double)x[i + nb.o[k]];
-    return sum - (double)((info >> 8) & 7) * (double)x[i];
+        if (f & (1u << cg_bit(k))) sum = df_add(sum, xv[k]);
+    const float2 dc = df_mul_k(xv[6], (float)((f >> 8) & 7));
+    const float2 lap = df_add(sum, make_float2(-dc.x, -dc.y));
+    const float2 t = df_add_f(make_float2(-lap.x, -lap.y), b);
+    return __fadd_rn(t.x, t.y);
 }
 
 // This block's share of the active chunks, cached in shared memory for the whole solve (the compacted list
@@ -638,8 +670,8 @@ __device__ __forceinline__ FSum phase_update4(const SolverArgs& a, const Chunks&
 
 // Residual replacement of the mixed-precision variants, in rounds of several chunks per warp whose loads do not
 // depend on rowinfo (a chunk at a time, each row's loads waiting for its rowinfo, made every replacement a
-// chain of dependent L2 round trips: about 145 µs at 256^3, 16 times a solve).  Same per-row arithmetic as
-// the per-row loops: p64 += e, e = 0, then r = b - L p64 in FP64 with the neighbours summed in order.
+// chain of dependent L2 round trips: about 145 µs at 256^3, 16 times a solve): p += e, e = 0, then r = b - L p
+// with the neighbours summed in order, p as float pairs (df_resid).
 #ifndef EFS_SOLVER_UR
 #define EFS_SOLVER_UR 1
 #endif
@@ -655,14 +687,15 @@ __device__ __forceinline__ void fold_rows(const SolverArgs& a, const Chunks& ch)
             act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
             idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
         }
-        double pv[UA];
+        float2* pp = reinterpret_cast<float2*>(a.p64);
+        float2 pv[UA];
         float ev[UA];
 #pragma unroll
-        for (int u = 0; u < UA; u++) { pv[u] = a.p64[idx[u]]; ev[u] = a.e[idx[u]]; }
+        for (int u = 0; u < UA; u++) { pv[u] = pp[idx[u]]; ev[u] = a.e[idx[u]]; }
 #pragma unroll
         for (int u = 0; u < UA; u++) {
             if (!act[u]) continue;
-            a.p64[idx[u]] = pv[u] + (double)ev[u];
+            pp[idx[u]] = df_add_f(pv[u], ev[u]);
             a.e[idx[u]] = 0.f;
         }
     }
@@ -679,27 +712,23 @@ __device__ __forceinline__ FSum residual_rows(const SolverArgs& a, const Chunks&
             act[u] = c < ch.n && ((ch.mask[c] >> lane) & 1u);
             idx[u] = act[u] ? ch.ids[c] * 32 + lane : 0;
         }
+        const float2* pp = reinterpret_cast<const float2*>(a.p64);
         uint16_t f[UR];
         float bv[UR];
-        double xv[UR][7];
+        float2 xv[UR][7];
 #pragma unroll
         for (int u = 0; u < UR; u++) {
             const int i = idx[u];
             f[u] = a.rowinfo[i];
             bv[u] = a.b[i];
-            xv[u][6] = a.p64[i];
+            xv[u][6] = pp[i];
 #pragma unroll
-            for (int k = 0; k < 6; k++) xv[u][k] = a.p64[i + nb.o[k]];
+            for (int k = 0; k < 6; k++) xv[u][k] = pp[i + nb.o[k]];
         }
 #pragma unroll
         for (int u = 0; u < UR; u++) {
             if (!act[u]) continue;
-            double sum = 0.0;
-#pragma unroll
-            for (int k = 0; k < 6; k++)
-                if (f[u] & (1u << cg_bit(k))) sum += xv[u][k];
-            const double lap = sum - (double)((f[u] >> 8) & 7) * xv[u][6];
-            const float ri = (float)((double)bv[u] - lap);
+            const float ri = df_resid(bv[u], xv[u], f[u]);
             a.r[idx[u]] = ri;
             acc.add_prod(ri, ri);
         }
@@ -979,9 +1008,13 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
             rows += 1;
             float ri;
             if (mixed) {
-                p64[i] = (double)bi;
+                reinterpret_cast<float2*>(p64)[i] = make_float2(bi, 0.f);
                 e[i] = 0.f;
-                ri = (float)((double)bi - lap_df(b, f, i, nb));
+                float2 bv[7];
+#pragma unroll
+                for (int k = 0; k < 6; k++) bv[k] = make_float2(b[i + nb.o[k]], 0.f);
+                bv[6] = make_float2(bi, 0.f);
+                ri = df_resid(bi, bv, f);
             } else {
                 ri = bi - lap_f(b, f, i, nb);
             }
@@ -1003,7 +1036,8 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
     const double thr = (double)thr_f;
     red.below = thr;
 
-    // residual recomputation (CGSolver.cpp:447-451): fold e into p64 and r = b - L p64 in FP64 (mixed), or
+    // residual recomputation (CGSolver.cpp:447-451): fold e into the pair accumulator and r = b - L p in float
+    // pairs (mixed), or
     // r = b - L p in FP32 (reference)
     auto replace = [&](double& rr_out) -> bool {
         // the fold reads e with its own chunk-to-warp mapping: every warp's update of e comes first
@@ -1139,10 +1173,12 @@ __global__ void __launch_bounds__(SOLVER_THREADS, SOLVER_MIN_BLOCKS) k_solver(So
         iters = it + 1;
     }
     if (mixed) {
-        // fold the increment: p64 then holds the FP64 solution (efs_download_pressure_fp64)
+        // fold the increment and convert the pairs in place: p64 then holds the FP64 solution
+        // (efs_download_pressure_fp64)
         for_rows(a, ch, [&](int i) {
             if (!(info[i] & 0x8000u)) return;
-            const double v = p64[i] + (double)e[i];
+            const float2 pv = reinterpret_cast<const float2*>(p64)[i];
+            const double v = ((double)pv.x + (double)pv.y) + (double)e[i];
             p64[i] = v;
             e[i] = 0.f;
             p[i] = (float)v;

@@ -75,8 +75,10 @@ enum efs_solver {
 
 /* CG variants.  Both follow CGSolverCPU3D::solve (CGSolver.cpp:416-465): p0 = b, recurrence residual, the
  * true residual recomputed when (i & 63) == 0, stop when r.r < threshold or after max_steps, FP64 dot
- * products.  EFS_CG_MIXED keeps the pressure as an FP64 accumulator plus an FP32 increment that is folded in
- * at every recomputation, and computes that true residual in FP64 (group-wise reliable updates); before
+ * products.  EFS_CG_MIXED keeps the pressure as an extended-precision accumulator (a pair of floats, about
+ * 48 significant bits, computed on the FP32 pipe) plus an FP32 increment that is folded in at every
+ * recomputation, and computes that true residual in the same pair arithmetic (group-wise reliable updates;
+ * the CPU oracle uses FP64 for both); before
  * stopping it recomputes the true residual once more and continues if it is above the threshold.  This
  * reaches relative residuals below what any FP32 pressure field can represent (the rounded exact solution
  * sits near 1e-5 on these grids).  EFS_CG_REFERENCE keeps the pressure in FP32 and recomputes the residual in
@@ -88,7 +90,7 @@ enum efs_cg_variant {
      * residual-norm recurrence r'.r' = alpha^2 t.t - r.r (an exact CG identity), so that alpha and beta both
      * follow from one reduction of d.t and t.t.  The iteration then updates the increment, r and d per cell
      * and sums the exact r'.r' for the stop test (on the GPU that sum travels with the next iteration's
-     * reduction).  Every 64th iteration recomputes the residual in FP64 as the other variants do, and takes
+     * reduction).  Every 64th iteration recomputes the residual as EFS_CG_MIXED does, and takes
      * that iteration's beta from it. */
     EFS_CG_MIXED_RECURRENCE = 2,
     /* EFS_CG_FP64: a study solver, not a fast path.  The reference iteration with p, r, d and L d in FP64 and
