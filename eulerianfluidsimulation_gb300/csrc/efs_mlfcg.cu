@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "efs_internal.h"
+#include "efs_pair.cuh"
 
 namespace efs {
 
@@ -97,27 +98,18 @@ __device__ __forceinline__ T lapply(const LvView& L, long long i, const T* x, fl
     return s;
 }
 
-// FCG's x as a pair of floats, x.x + x.y with |x.y| below half an ulp of x.x: about 48 significant bits, updated
-// on the FP32 pipe (GB300's FP64 rate made the FP64 update of every row a sixth of the vector update's time).
-// pair_add returns x + (ah + al) d: the product's rounding error by FMA, the sum's by TwoSum, renormalised.
-__device__ __forceinline__ float2 pair_add(float2 x, float ah, float al, float d) {
-    const float p = __fmul_rn(ah, d);
-    const float pe = fmaf(al, d, fmaf(ah, d, -p));
-    const float s = __fadd_rn(x.x, p);
-    const float bb = __fsub_rn(s, x.x);
-    const float t = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    const float lo = __fadd_rn(__fadd_rn(t, x.y), pe);
-    const float hi = __fadd_rn(s, lo);
-    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
-}
-__device__ __forceinline__ double pair_val(float2 x) { return (double)x.x + (double)x.y; }
-// (A x)_i in FP64 for x held as float pairs (lapply's order)
-__device__ __forceinline__ double lapply_pair(const LvView& L, long long i, const float2* x, float dg, const float (&w)[6]) {
-    double s = (double)dg * pair_val(x[i]);
+// FCG's x as a pair of floats (efs_pair.cuh), updated on the FP32 pipe: GB300's FP64 rate made the FP64 update
+// of every row a sixth of the vector update's time.
+// b_i - (A x)_i for x held as float pairs, on a level-0 row with flags f (lapply's neighbour order), in pair
+// arithmetic, rounded to float
+__device__ __forceinline__ float resid_pair(const LvView& L, long long i, const float2* x, float b, unsigned f) {
+    float2 sum = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 6; k++)
-        if (w[k] != 0.f) s += (double)w[k] * pair_val(x[i + noff(L, k)]);
-    return s;
+        if ((f >> k) & 1u) sum = df_add(sum, x[i + noff(L, k)]);
+    const float2 lap = df_add(sum, df_neg(df_mul_k(x[i], (float)((f >> 8) & 7))));
+    const float2 t = df_add_f(df_neg(lap), b);
+    return __fadd_rn(t.x, t.y);
 }
 // alpha / beta for the float kernels
 __device__ __forceinline__ void set_alpha(FcgDev* s, double a) {
@@ -898,10 +890,10 @@ __global__ void k_q_update(QWalk qw, float2* __restrict__ x, float* __restrict__
         ld4(q, i, qv);
         float4* x4 = reinterpret_cast<float4*>(x + i);
         float4 x01 = x4[0], x23 = x4[1];
-        float2 p0 = pair_add(make_float2(x01.x, x01.y), af, al, dv[0]);
-        float2 p1 = pair_add(make_float2(x01.z, x01.w), af, al, dv[1]);
-        float2 p2 = pair_add(make_float2(x23.x, x23.y), af, al, dv[2]);
-        float2 p3 = pair_add(make_float2(x23.z, x23.w), af, al, dv[3]);
+        float2 p0 = df_axpy(make_float2(x01.x, x01.y), af, al, dv[0]);
+        float2 p1 = df_axpy(make_float2(x01.z, x01.w), af, al, dv[1]);
+        float2 p2 = df_axpy(make_float2(x23.x, x23.y), af, al, dv[2]);
+        float2 p3 = df_axpy(make_float2(x23.z, x23.w), af, al, dv[3]);
         x4[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
         x4[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
 #pragma unroll
@@ -1020,7 +1012,7 @@ __global__ void k_fcg_update(Walk wk, float2* __restrict__ x, float* __restrict_
     float rr = 0.f;
     WALK(wk, t, i) {
         const float di = dn[i];
-        x[i] = pair_add(x[i], af, al, di);
+        x[i] = df_axpy(x[i], af, al, di);
         const float ri = r[i] - af * q[i];
         r[i] = ri;
         d[i] = di;
@@ -1047,7 +1039,7 @@ __global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b,
     WALK(wk, t, i) {
         float dg, w[6];
         float ri = 0.f;
-        if (lrow<true>(F, i, dg, w)) ri = (float)((double)b[i] - lapply_pair(F, i, x, dg, w));
+        if (lrow<true>(F, i, dg, w)) ri = resid_pair(F, i, x, b[i], F.info[i]);
         r[i] = ri;
         rr += (double)ri * ri;
     }
@@ -1073,11 +1065,11 @@ __global__ void k_fcg_fb_rhs(LvView F, const float* __restrict__ b, const float2
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= F.V) return;
     float dg, w[6];
-    fb[i] = lrow<true>(F, i, dg, w) ? (float)((double)b[i] - lapply_pair(F, i, x, dg, w)) : 0.f;
+    fb[i] = lrow<true>(F, i, dg, w) ? resid_pair(F, i, x, b[i], F.info[i]) : 0.f;
 }
 __global__ void k_fcg_fb_add(LvView F, Walk wk, float2* __restrict__ x, const float* __restrict__ p) {
     WALK(wk, t, i) {
-        if (F.info[i] & 0x8000u) x[i] = pair_add(x[i], 1.f, 0.f, p[i]);
+        if (F.info[i] & 0x8000u) x[i] = df_axpy(x[i], 1.f, 0.f, p[i]);
     }
 }
 __global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
@@ -1088,7 +1080,7 @@ __global__ void k_fcg_fb_done(FcgDev* s, const DevCtl* ctl) {
 __global__ void k_fcg_out(LvView F, Walk wk, const float2* __restrict__ x, float* __restrict__ p, double* __restrict__ p64) {
     WALK(wk, t, i) {
         if (F.info[i] & 0x8000u) {
-            const double v = pair_val(x[i]);
+            const double v = df_val(x[i]);
             p[i] = (float)v;
             p64[i] = v;
         }
@@ -1158,7 +1150,7 @@ struct MLLevel {
 struct MLState {
     int nlev = 0;                 // aggregation levels of the allocated hierarchy
     MLLevel lv[4];                // lv[1..nlev]
-    float2* xp = nullptr;         // FCG's x as float pairs (pair_add), and its other vectors (fine grid)
+    float2* xp = nullptr;         // FCG's x as float pairs (df_axpy), and its other vectors (fine grid)
     float *r = nullptr, *z = nullptr, *zt = nullptr, *d = nullptr, *dn = nullptr, *q = nullptr, *fb = nullptr;
     int* chunks = nullptr;        // level 0: the 32-cell chunks that hold a matrix row, in order
     int* bcount = nullptr;        // their per-block counts / offsets

@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "efs_internal.h"
+#include "efs_pair.cuh"
 
 namespace efs {
 
@@ -249,30 +250,6 @@ __device__ __forceinline__ double lap_d(const double* x, uint16_t info, int i, c
 // a.p64, computed on the FP32 pipe with error-free transformations; GB300 runs FP64 at a small fraction of its
 // FP32 rate, and the FP64 residual replacement had cost about 70 µs at 256^3 each time.  Converted to doubles in
 // place at the end of the solve (efs_download_pressure_fp64).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-__device__ __forceinline__ float2 df_renorm(float s, float e) {
-    const float hi = __fadd_rn(s, e);
-    return make_float2(hi, __fsub_rn(e, __fsub_rn(hi, s)));
-}
-__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
-    float s, e;
-    two_sum(x.x, y.x, s, e);
-    return df_renorm(s, __fadd_rn(e, __fadd_rn(x.y, y.y)));
-}
-__device__ __forceinline__ float2 df_add_f(float2 x, float y) {
-    float s, e;
-    two_sum(x.x, y, s, e);
-    return df_renorm(s, __fadd_rn(e, x.y));
-}
-// x times a small integer k (the diagonal count): the product's rounding error by FMA
-__device__ __forceinline__ float2 df_mul_k(float2 x, float k) {
-    const float ph = __fmul_rn(k, x.x);
-    return df_renorm(ph, fmaf(k, x.y, fmaf(k, x.x, -ph)));
-}
 // b - L x for the pair field x (lap_d's neighbour order), rounded to float
 __device__ __forceinline__ float df_resid(float b, const float2 (&xv)[7], uint16_t f) {
     float2 sum = make_float2(0.f, 0.f);
@@ -280,8 +257,8 @@ __device__ __forceinline__ float df_resid(float b, const float2 (&xv)[7], uint16
     for (int k = 0; k < 6; k++)
         if (f & (1u << cg_bit(k))) sum = df_add(sum, xv[k]);
     const float2 dc = df_mul_k(xv[6], (float)((f >> 8) & 7));
-    const float2 lap = df_add(sum, make_float2(-dc.x, -dc.y));
-    const float2 t = df_add_f(make_float2(-lap.x, -lap.y), b);
+    const float2 lap = df_add(sum, df_neg(dc));
+    const float2 t = df_add_f(df_neg(lap), b);
     return __fadd_rn(t.x, t.y);
 }
 
