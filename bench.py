@@ -41,9 +41,9 @@ SOLVE_BYTES_PER_ROW_SETUP = 30.0
 # Jacobi (ping-pong): per row and sweep read rowinfo, p, b and write the other p (14 B).
 JACOBI_BYTES_PER_ROW_ITER = 14.0
 # DRAM bytes (read + write) the solver moved per matrix row and CG iteration in one ncu capture of k_solver on
-# this workload (one launch: 950 iterations over 3,778,175 rows, 27.37 GB read + 40.87 GB written; the
+# this workload (one launch: 950 iterations over 3,778,175 rows, 27.29 GB read + 40.74 GB written; the
 # active vectors only partly fit in L2 at 256^3).  `traffic` scales it by this run's row-iterations per launch.
-SOLVE_DRAM_BYTES_PER_ROW_ITER = 68.23e9 / (950 * 3778175)
+SOLVE_DRAM_BYTES_PER_ROW_ITER = 68.03e9 / (950 * 3778175)
 # Algorithmic bytes per interior cell of the stages other than the pressure solve, 3D (each field read once and
 # written once per pass: extrapolation 30 + 162, sharpen 21, advection 61 + 12 + 76 + 52, diffusion 153,
 # velocity advection 50, add_force 25, divergence 22, gradient and walls 29).
