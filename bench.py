@@ -410,15 +410,23 @@ def run_gb300(a):
         h["boundary"][...] = b
         h["forces"][...] = 0
         k_e2e = max(2, a.steps // 2)
+
+        def step_host():
+            sim.step_host(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"],
+                          vel_out=h["vel"], rho_out=h["rho"], gamma_out=h["gamma"], beta_out=h["beta"],
+                          divergence_out=h["div"], pressure_out=h["p"])
+        # untimed warm-up calls: the first call that passes a forces field recaptures the step graph with the
+        # forces read (a one-time cost of the context, not of a step)
+        w_e2e = 2
+        for _ in range(w_e2e):
+            step_host()
         sim.synchronize()
         se0 = sim.stats()
         sim.solve_timing_arm(k_e2e)
         barrier()
         sim.mark(2)
         for _ in range(k_e2e):
-            sim.step_host(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"],
-                          vel_out=h["vel"], rho_out=h["rho"], gamma_out=h["gamma"], beta_out=h["beta"],
-                          divergence_out=h["div"], pressure_out=h["p"])
+            step_host()
         sim.mark(3)
         ms_e2e = sim.elapsed_ms(2, 3)
         barrier()
@@ -427,7 +435,7 @@ def run_gb300(a):
         # the e2e steps continue the trajectory after the timed steps: their solves may take other iteration
         # counts than the main line's, so the line carries them
         e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
-               "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e, "ms_per_step": ms_e2e / k_e2e,
+               "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e, "warmup": w_e2e, "ms_per_step": ms_e2e / k_e2e,
                "solve_iters_per_step": (se1.total_solve_steps - se0.total_solve_steps) / k_e2e,
                "solve_ms_per_step": (e_solve_ms / e_launches) if e_launches else None,
                "api": "efs_step_host: upload vel,rho,gamma,boundary,forces + one step + download vel,rho,gamma,beta,div,p "
@@ -731,16 +739,21 @@ def run_dam2d(a):
         sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
         h["boundary"][...] = b
         h["forces"][...] = 0
-        sim.synchronize()
-        sim.mark(2)
-        for _ in range(a.steps):
+
+        def step_host():
             sim.upload_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], boundary=h["boundary"], forces=h["forces"])
             sim.update(1)
             sim.download_fields(vel=h["vel"], rho=h["rho"], gamma=h["gamma"], beta=h["beta"], divergence=h["div"], pressure=h["p"])
+        # untimed warm-up call: the first upload of a forces field recaptures the step graph with the forces read
+        step_host()
+        sim.synchronize()
+        sim.mark(2)
+        for _ in range(a.steps):
+            step_host()
         sim.mark(3)
         ms_e2e = sim.elapsed_ms(2, 3)
         e2e = {"value": a.steps / (ms_e2e / 1e3), "unit": "steps/s", "h2d_bytes_per_step": 4 * n * n * 7,
-               "d2h_bytes_per_step": 4 * n * n * 7, "steps": a.steps,
+               "d2h_bytes_per_step": 4 * n * n * 7, "steps": a.steps, "warmup": 1,
                "api": "efs_upload_fields(vel,rho,gamma,boundary,forces) + efs_step + efs_download_fields(vel,rho,gamma,beta,div,p)"}
     sim.close()
     cpu = None

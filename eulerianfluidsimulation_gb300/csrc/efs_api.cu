@@ -98,14 +98,16 @@ cudaError_t enqueue_step(efs_ctx* c, unsigned stages, bool timing_events) {
     const bool fuse = (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_ADD_FORCE));
     const bool chain = (stages & EFS_STAGE_BIT(EFS_STAGE_RHO_ADVECT)) && (stages & EFS_STAGE_BIT(EFS_STAGE_VEL_ADVECT));
     for (int s = 0; s < EFS_STAGE_COUNT; s++) {
-        // captured steps: gamma and forces uploaded by efs_step_host on the transfer stream are first read by
-        // rho_advect; rho, gamma and beta are final after it (the later stages do not write them)
+        // captured steps: efs_step_host uploads gamma and forces on the transfer stream; gamma is first read by
+        // rho_advect, the forces by vel_advect's averaging pass (or add_force after it).  rho, gamma and beta
+        // are final after rho_advect (the later stages do not write them).
         if (timing_events && s == EFS_STAGE_RHO_ADVECT) {
-            cudaError_t e = cudaStreamWaitEvent(c->stream, c->ev_late, cudaEventWaitExternal);
+            cudaError_t e = cudaStreamWaitEvent(c->stream, c->ev_gamma, cudaEventWaitExternal);
             if (e != cudaSuccess) return e;
         }
         if (timing_events && s == EFS_STAGE_VEL_ADVECT) {
             cudaError_t e = cudaEventRecordWithFlags(c->ev_advected, c->stream, cudaEventRecordExternal);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_forces, cudaEventWaitExternal);
             if (e != cudaSuccess) return e;
         }
         if (!(stages & EFS_STAGE_BIT(s))) continue;
@@ -278,7 +280,8 @@ void efs_destroy(efs_ctx* c) {
     for (auto ev : c->marks) if (ev) cudaEventDestroy(ev);
     if (c->ev_solve_begin) cudaEventDestroy(c->ev_solve_begin);
     if (c->xfer) { cudaStreamSynchronize(c->xfer); cudaStreamDestroy(c->xfer); }
-    if (c->ev_late) cudaEventDestroy(c->ev_late);
+    if (c->ev_gamma) cudaEventDestroy(c->ev_gamma);
+    if (c->ev_forces) cudaEventDestroy(c->ev_forces);
     if (c->ev_advected) cudaEventDestroy(c->ev_advected);
     if (c->ev_projected) cudaEventDestroy(c->ev_projected);
     if (c->ev_early) cudaEventDestroy(c->ev_early);
@@ -341,7 +344,8 @@ int efs_create(int dim, int width, int height, int depth, const efs_params* para
     if ((e = dalloc(&c->partials, 6 * (size_t)c->solver_blocks)) != cudaSuccess) return bail(e, "cudaMalloc partials");
     if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->ctl_host), sizeof(DevCtl))) != cudaSuccess) return bail(e, "cudaMallocHost");
     if ((e = cudaEventCreate(&c->ev_solve_begin)) != cudaSuccess) return bail(e, "cudaEventCreate");
-    if ((e = cudaEventCreateWithFlags(&c->ev_late, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_gamma, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreateWithFlags(&c->ev_forces, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_advected, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_projected, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "cudaEventCreate");
@@ -559,11 +563,13 @@ int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* g
     if (boundary && (s = enqueue_upload(c, EFS_FIELD_BOUNDARY, boundary)) != EFS_OK) return s;
     if (vel && (s = enqueue_upload(c, EFS_FIELD_VEL, vel)) != EFS_OK) return s;
     if (rho && (s = enqueue_upload(c, EFS_FIELD_RHO, rho)) != EFS_OK) return s;
-    // inputs first read by rho_advect (gamma) and add_force (forces), on the transfer stream once the first
-    // stages' inputs are up (the host link is the bottleneck: sharing it would delay the first stage)
+    // inputs first read by rho_advect (gamma) and vel_advect (forces), on the transfer stream once the first
+    // stages' inputs are up (the host link is the bottleneck: sharing it would delay the first stage); the
+    // step waits for each where it first reads it, so the forces move while rho_advect runs
     CK(cudaEventRecord(c->ev_early, c->stream), "cudaEventRecord");
     CK(cudaStreamWaitEvent(c->xfer, c->ev_early, 0), "cudaStreamWaitEvent");
     if (gamma) CK(cudaMemcpyAsync(c->gamma, gamma, bytes, cudaMemcpyHostToDevice, c->xfer), "upload gamma");
+    CK(cudaEventRecord(c->ev_gamma, c->xfer), "cudaEventRecord");
     if (forces) {
         // the copy engine brings the interleaved forces up; a short split kernel follows (a kernel reading the
         // host buffer itself would wait for SMs behind the first stages)
@@ -571,7 +577,7 @@ int efs_step_host(efs_ctx* c, const float* vel, const float* rho, const float* g
         CK(cudaMemcpyAsync(c->fstage, forces, bytes * c->dim, cudaMemcpyHostToDevice, c->xfer), "upload forces");
         CK(efs::launch_upload_vec(c, c->fstage, c->fx, c->fy, c->fz, c->xfer), "split forces");
     }
-    CK(cudaEventRecord(c->ev_late, c->xfer), "cudaEventRecord");
+    CK(cudaEventRecord(c->ev_forces, c->xfer), "cudaEventRecord");
     if ((s = efs_step(c, 1)) != EFS_OK) return s;
     // rho, gamma, beta: on the transfer stream once rho_advect is done
     CK(cudaStreamWaitEvent(c->xfer, c->ev_advected, 0), "cudaStreamWaitEvent");

@@ -164,10 +164,10 @@ struct efs_ctx {
     efs::UNetState* unet = nullptr;         // learned preconditioner (efs_unet.cu)
     efs::MLState* ml = nullptr;             // FCG and its multilevel hierarchy (efs_mlfcg.cu)
     void* query_scratch = nullptr;          // efs_query_box block partials and result (efs_scene.cu)
-    // efs_step_host: transfers that overlap the step run on `xfer`; the step graph waits for `ev_late` (late
-    // inputs) before rho_advect and records `ev_advected` after it
+    // efs_step_host: transfers that overlap the step run on `xfer`; the step graph waits for `ev_gamma` before
+    // rho_advect and for `ev_forces` before vel_advect, and records `ev_advected` after rho_advect
     cudaStream_t xfer = nullptr;
-    cudaEvent_t ev_late = nullptr, ev_advected = nullptr;
+    cudaEvent_t ev_gamma = nullptr, ev_forces = nullptr, ev_advected = nullptr;
     cudaEvent_t ev_projected = nullptr;   // recorded after project_pre: the divergence is final
     cudaEvent_t ev_early = nullptr;         // the first stages' inputs are on the device
     float* fstage = nullptr;                // efs_step_host: staging of the forces (dim floats a cell)
