@@ -360,6 +360,136 @@ __global__ void k_conv_split_reduce(const float* __restrict__ partial, int split
 }
 
 // ============================================================================================================
+// Slab 3x3x3 convolution for narrow grids: the same function as k_conv3_tc.  A CTA computes M = 128 voxels, an
+// 8 (x) x 16 (y) x 1 (z) slab (slabs reaching past the grid's width or height compute zeros there and store
+// only the voxels inside).  It copies the slab's input with a
+// one-voxel halo (10 x 18 x 3 voxels; zero outside the grid; with `up`, voxel (x, y, z) of the half-resolution
+// input at (x/2, y/2, z/2)) into shared memory once, as planes of 8 channels ([cin/8][z][y][x] x 16 bytes),
+// together with every K step's weight tile.  The A operand of step (tap, chunk) is then a descriptor into that
+// copy: 8 x-consecutive voxels of one y row are a 128-byte core matrix, the slab's 16 rows follow at the row
+// pitch (stride byte offset 160), and the chunk's upper 8 channels one plane further (leading byte offset).
+// A tap only moves the start address, so one thread issues all 27 x cin/16 MMAs back to back: no gathers
+// between the MMAs and no split of the steps over CTAs.  M row m = TMEM lane m is voxel (x0 + m % 8,
+// y0 + m / 8, z0).
+// ============================================================================================================
+constexpr int kSlabX = 8, kSlabY = 16;
+constexpr int kSlabHX = kSlabX + 2, kSlabHY = kSlabY + 2, kSlabHZ = 3;
+constexpr int kSlabVox = kSlabHX * kSlabHY * kSlabHZ;   // voxels of the halo brick
+constexpr uint32_t kSlabPlane = kSlabVox * 16;            // bytes of one 8-channel plane of the brick
+constexpr uint32_t kSlabRow = kSlabHX * 16;               // bytes of one brick row: the A stride byte offset
+__host__ __device__ constexpr size_t slab_smem_bytes(int cin, int cout) {
+    return (size_t)(cin / 8) * kSlabPlane + (size_t)27 * (cin / 16) * cout * 32 + 16;
+}
+__host__ __device__ constexpr bool slab_fits(int cin) { return cin == 16 || cin == 32 || cin == 64; }
+__host__ __device__ constexpr long long slab_count(int W, int H, int D) {
+    return (long long)((W + kSlabX - 1) / kSlabX) * ((H + kSlabY - 1) / kSlabY) * D;
+}
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
+    static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
+    constexpr uint32_t kCols = COUT < 32 ? 32 : COUT;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int chunks = a.cin >> 4, planes = a.cin >> 3;
+    const int S = 27 * chunks;
+    unsigned char* brick = smem;
+    unsigned char* wsm = smem + (size_t)planes * kSlabPlane;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(wsm + (size_t)S * COUT * 32);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+    const int nsx = (a.W + kSlabX - 1) / kSlabX, nsy = (a.H + kSlabY - 1) / kSlabY;
+    const int x0 = (blockIdx.x % nsx) * kSlabX, y0 = ((blockIdx.x / nsx) % nsy) * kSlabY, z0 = blockIdx.x / (nsx * nsy);
+    const int PW = (a.W + 1) >> 1, PH = (a.H + 1) >> 1;
+
+    // the brick: piece p = voxel * planes + plane (the planes of one voxel are adjacent in global memory)
+    const int pieces = kSlabVox * planes;
+    for (int p = tid; p < pieces; p += kConvThreads) {
+        const int vox = p / planes, pl = p - vox * planes;
+        const int hx = vox % kSlabHX, hy = (vox / kSlabHX) % kSlabHY, hz = vox / (kSlabHX * kSlabHY);
+        const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+        const bool ok = gx >= 0 && gx < a.W && gy >= 0 && gy < a.H && gz >= 0 && gz < a.D;
+        const int iv = a.up ? (((gz >> 1) * PH + (gy >> 1)) * PW + (gx >> 1)) : ((gz * a.H + gy) * a.W + gx);
+        const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + pl * 8) : a.in;
+        cp_async16(brick + (size_t)pl * kSlabPlane + (size_t)vox * 16, src, ok);
+    }
+    // every step's weight tile in k_conv3_tc's B layout; step s's tile at s * COUT * 32 bytes
+    const int wpieces = S * COUT * 2;
+    for (int q = tid; q < wpieces; q += kConvThreads) {
+        const int s = q / (2 * COUT), r = q - s * 2 * COUT, n = r >> 1, kh = r & 1;
+        cp_async16(wsm + (size_t)s * COUT * 32 + tile_off(n, kh * 8), a.wt + ((size_t)(s * COUT + n) * 16 + kh * 8),
+                   true);
+    }
+    cp_async_commit();
+    if (warp == 0) tmem_alloc(tslot, kCols);
+    if (tid == 0) {
+        mbar_init(mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    cp_async_wait<0>();
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        // steps in k_conv3_tc's order: s = tap * chunks + chunk, tap = ((dz + 1) * 3 + dy + 1) * 3 + dx + 1
+        const uint32_t b0 = smem_u32(brick), w0 = smem_u32(wsm);
+        const int clog = __ffs(chunks) - 1;
+        for (int s = 0; s < S; s++) {
+            const int tap = s >> clog, c = s & (chunks - 1);
+            const int hz = tap / 9, hy = (tap / 3) % 3, hx = tap % 3;   // the tap's offsets + 1
+            const uint32_t aaddr = b0 + (uint32_t)(2 * c) * kSlabPlane + (uint32_t)((hz * kSlabHY + hy) * kSlabHX + hx) * 16;
+            mma_bf16(tmem, sdesc(aaddr, kSlabPlane, kSlabRow), sdesc(w0 + (uint32_t)s * COUT * 32, 128, 256),
+                     idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
+        }
+        mma_commit(mbar);
+    }
+    bool ok = mbar_wait(mbar, 0);
+    if (!ok) {
+        if (tid == 0) atomicOr(a.err, 1);
+        // bounded: let MMAs in flight finish before freeing TMEM
+        mbar_wait(mbar, 0);
+    }
+    tc_fence_after();
+    const int vx = x0 + (tid & 7), vy = y0 + (tid >> 3);
+    if (ok) {
+        const bool vin = vx < a.W && vy < a.H;
+        const int v = vin ? (z0 * a.H + vy) * a.W + vx : 0;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)c0, acc);   // every lane of the warp takes part
+            if (!vin) continue;
+            __align__(16) __nv_bfloat16 o[16], pr[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
+                pr[j] = __float2bfloat16(t);
+                if (a.relu) t = fmaxf(t, 0.f);
+                if (a.skip) t += __bfloat162float(a.skip[(size_t)v * COUT + c0 + j]);
+                o[j] = __float2bfloat16(t);
+                if (a.out32 && c0 + j == 0) a.out32[v] = t;
+            }
+            if (a.out) {
+                uint4* dst = reinterpret_cast<uint4*>(a.out + (size_t)v * COUT + c0);
+                dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                dst[1] = reinterpret_cast<const uint4*>(o)[1];
+            }
+            if (a.pre) {
+                uint4* dst = reinterpret_cast<uint4*>(a.pre + (size_t)v * COUT + c0);
+                dst[0] = reinterpret_cast<const uint4*>(pr)[0];
+                dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kCols);
+}
+
+// ============================================================================================================
 // Weight gradient:  dw[tap][c][n] += sum_v in[v + off(tap)][c] * g[v][n]
 // GEMM view: M = 27 * CIN rows (row = tap * CIN + c), tiles of 128 (blockIdx.x); N = COUT; K = voxels, in
 // steps of 16, over the voxel range of blockIdx.y.  Operands are transposed into the K-major tiles with

@@ -59,6 +59,7 @@ struct Level {
 struct UNetState {
     int level = 0;               // hierarchy level the network works on (0: the context's grid)
     int sm = 0;                  // SMs of the device (the split convolutions' target CTA count)
+    int slab_smem = 0;           // dynamic shared memory k_conv3_slab may take (0: the slab kernel is not used)
     float* split = nullptr;      // FP32 partial sums of split convolutions
     long long split_cap = 0;     // floats in split
     Level L[3];
@@ -561,6 +562,19 @@ cudaError_t conv_halo(UNetState* u, const bf16* in, const bf16* wt, int cin, int
     return launch_halo<64>(a, L.W, L.H, L.D, sm_count, st);
 }
 
+// k_conv3_slab's shared memory ceiling: the device's opt-in maximum per block, set once for every instantiation
+// (outside any stream capture)
+cudaError_t slab_setup(UNetState* u) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) u->slab_smem = optin;
+    return e;
+}
+
 // the implicit-GEMM (im2col) kernel serves the level; it can read an up-sampled input in place
 bool conv_im2col(const UNetState* u, int level, int cin) {
     const Level& L = u->L[level];
@@ -576,8 +590,17 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
         return conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st);
     }
     tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0, up ? 1 : 0};
-    const unsigned grid = (unsigned)((L.V + 127) / 128);
     (void)layer;
+    // narrow grids: one CTA per 8 x 16 slab, its input brick and weights in shared memory
+    const size_t slab_bytes = tc::slab_smem_bytes(cin, cout);
+    if (tc::slab_fits(cin) && slab_bytes <= (size_t)u->slab_smem) {
+        const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D);
+        if (cout == 16) tc::k_conv3_slab<16><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
+        else if (cout == 32) tc::k_conv3_slab<32><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
+        else tc::k_conv3_slab<64><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
+        return cudaGetLastError();
+    }
+    const unsigned grid = (unsigned)((L.V + 127) / 128);
     // Small grids (the coarse levels of the network, and the whole network on FCG's bottom grid) give too few
     // CTAs, each running all 27 x cin/16 MMA steps in sequence: split the steps over more CTAs, then sum.
     const int s_all = 27 * (cin / 16);
@@ -847,6 +870,7 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
     // split convolutions run on grids of fewer than 8 x SMs CTAs of 128 voxels, into at most 8 x SMs + CTAs more
     // partial tiles: (8 x SMs + 8 x SMs) x 128 voxels x 64 channels bounds every layer (the launch also checks)
     u->sm = c->sm_count > 0 ? c->sm_count : 152;
+    UCK(slab_setup(u));
     u->split_cap = 16LL * u->sm * 128 * 64;
     UCK(ualloc(u, &u->split, u->split_cap));
     UCK(ualloc(u, &u->x0, L[0].V * 16));

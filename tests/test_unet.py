@@ -77,7 +77,7 @@ def test_unet_gradients_match_oracle(kind):
 def test_unet_halo_tile_path_matches_oracle():
     """Grids at least 96 voxels wide take the halo-tile convolution (TMA input box, one descriptor per tap):
     here levels 0 and 1 (widths 200 and 100: a partial second segment, 16/32/64 input channels, COUT
-    16/32/64 in the forward and input-gradient passes); level 2 (width 50) keeps the im2col kernel."""
+    16/32/64 in the forward and input-gradient passes); level 2 (width 50) takes the slab kernel."""
     W, H, D = 200, 12, 10
     bnd, rho = oracle.scene_dam3d(W, H, D, 3, 3, 6)
     rows = (rho > 0.5) & (bnd == 0.0)
@@ -90,6 +90,38 @@ def test_unet_halo_tile_path_matches_oracle():
     prm.fcg_levels = 0                      # the network on the context's own grid
     with gb.GB300Simulator3D(W, H, D, prm) as s:
         s.unet_init(13, 0)
+        s.set_field(abi.FIELD_BOUNDARY, bnd)
+        s.set_field(abi.FIELD_RHO, rho)
+        z = s.unet_apply(r)
+        loss, g = s.unet_loss_grad(b, p, loss_kind=1)
+        w = s.unet_weights()
+    y, _ = U.forward(w, r, rows, bf16=True)
+    assert np.all(z[~rows] == 0)
+    assert rel_l2(z[rows], y[rows]) < 1e-2, rel_l2(z[rows], y[rows])
+    lo, go = U.loss_grad(w, b, p, rows, bf16=True, kind=1, apply_L=apply_L)
+    assert abs(loss - lo) <= 1e-3 * lo, (loss, lo)
+    for name, sl in U.layer_slices():
+        assert rel_l2(g[sl], go[sl]) < 3e-2, (name, rel_l2(g[sl], go[sl]))
+
+
+def test_unet_slab_path_matches_oracle():
+    """Grids narrower than the halo-tile kernel's take the slab convolution (input brick and weights in shared
+    memory, one descriptor per tap): here levels 0 and 1 in whole 8 x 16 slabs (16 x 32 x 6 and 8 x 16 x 3:
+    16/32/64 input channels, COUT 16/32/64, the up-sampled inputs read in place, the forward and
+    input-gradient passes) and level 2 (4 x 8 x 2) in one partial slab.  The 12^3 tests above run every
+    level in partial slabs."""
+    W, H, D = 16, 32, 6
+    bnd, rho = oracle.scene_dam3d(W, H, D, 2, 2, 8)
+    rows = (rho > 0.5) & (bnd == 0.0)
+    apply_L, _ = U.matrix(rho, bnd)
+    rng = np.random.default_rng(17)
+    r = rng.normal(size=(D, H, W)).astype(np.float32)
+    p = np.where(rows, rng.normal(size=(D, H, W)), 0.0).astype(np.float32)
+    b = apply_L(p).astype(np.float32)
+    prm = abi.params_dam(1.0 / W, 0.004, abi.SOLVER_CG, 1e-6)
+    prm.fcg_levels = 0                      # the network on the context's own grid
+    with gb.GB300Simulator3D(W, H, D, prm) as s:
+        s.unet_init(19, 0)
         s.set_field(abi.FIELD_BOUNDARY, bnd)
         s.set_field(abi.FIELD_RHO, rho)
         z = s.unet_apply(r)
