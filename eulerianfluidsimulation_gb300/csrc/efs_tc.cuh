@@ -156,6 +156,8 @@ struct ConvArgs {
     // up != 0: the input is the grid of half the resolution (ceil(W/2) x ceil(H/2) x ceil(D/2) voxels) read as its
     // nearest up-sampling: voxel (x, y, z) takes the input voxel (x/2, y/2, z/2)
     int up;
+    // k_conv3_slab with two z slabs: the 2x2x2 mean of the outputs ([ceil(D/2)][ceil(H/2)][ceil(W/2)][COUT]), or null
+    __nv_bfloat16* pool;
 };
 
 constexpr int kConvThreads = 128;
@@ -360,50 +362,56 @@ __global__ void k_conv_split_reduce(const float* __restrict__ partial, int split
 }
 
 // ============================================================================================================
-// Slab 3x3x3 convolution for narrow grids: the same function as k_conv3_tc.  A CTA computes M = 128 voxels, an
-// 8 (x) x 16 (y) x 1 (z) slab (slabs reaching past the grid's width or height compute zeros there and store
-// only the voxels inside).  It copies the slab's input with a
-// one-voxel halo (10 x 18 x 3 voxels; zero outside the grid; with `up`, voxel (x, y, z) of the half-resolution
-// input at (x/2, y/2, z/2)) into shared memory once, as planes of 8 channels ([cin/8][z][y][x] x 16 bytes),
-// together with every K step's weight tile.  The A operand of step (tap, chunk) is then a descriptor into that
-// copy: 8 x-consecutive voxels of one y row are a 128-byte core matrix, the slab's 16 rows follow at the row
-// pitch (stride byte offset 160), and the chunk's upper 8 channels one plane further (leading byte offset).
-// A tap only moves the start address, so one thread issues all 27 x cin/16 MMAs back to back: no gathers
-// between the MMAs and no split of the steps over CTAs.  M row m = TMEM lane m is voxel (x0 + m % 8,
-// y0 + m / 8, z0).
+// Slab 3x3x3 convolution for narrow grids: the same function as k_conv3_tc.  A CTA computes ZS slabs of M = 128
+// voxels, each 8 (x) x 16 (y) x 1 (z); slabs reaching past the grid compute zeros there and store only the
+// voxels inside.  It copies their input with a one-voxel halo (10 x 18 x (ZS + 2) voxels; zero outside the grid;
+// with `up`, voxel (x, y, z) of the half-resolution input at (x/2, y/2, z/2)) into shared memory once, as planes
+// of 8 channels ([cin/8][z][y][x] x 16 bytes), together with every K step's weight tile.  The A operand of step
+// (tap, chunk) of slab k is a descriptor into that copy: 8 x-consecutive voxels of one y row are a 128-byte core
+// matrix, the slab's 16 rows follow at the row pitch (stride byte offset 160), and the chunk's upper 8 channels
+// one plane further (leading byte offset).  A tap or a slab only moves the start address, so one thread issues
+// all ZS x 27 x cin/16 MMAs back to back, slab k into TMEM columns k COUT .. k COUT + COUT - 1: no gathers
+// between the MMAs and no split of the steps over CTAs.  M row m = TMEM lane m is voxel (x0 + m % 8, y0 + m / 8)
+// of each slab.
+// With ZS = 2 and `pool`, the epilogue also writes the 2x2x2 mean of the stored (BF16) outputs in k_pool's
+// order (z, then y, then x), taking the x and y neighbours from lanes m ^ 1 and m ^ 8 of the same warp.
 // ============================================================================================================
 constexpr int kSlabX = 8, kSlabY = 16;
-constexpr int kSlabHX = kSlabX + 2, kSlabHY = kSlabY + 2, kSlabHZ = 3;
-constexpr int kSlabVox = kSlabHX * kSlabHY * kSlabHZ;   // voxels of the halo brick
-constexpr uint32_t kSlabPlane = kSlabVox * 16;            // bytes of one 8-channel plane of the brick
+constexpr int kSlabHX = kSlabX + 2, kSlabHY = kSlabY + 2;
 constexpr uint32_t kSlabRow = kSlabHX * 16;               // bytes of one brick row: the A stride byte offset
-__host__ __device__ constexpr size_t slab_smem_bytes(int cin, int cout) {
-    return (size_t)(cin / 8) * kSlabPlane + (size_t)27 * (cin / 16) * cout * 32 + 16;
+constexpr uint32_t kSlabZ = kSlabHY * kSlabRow;           // bytes of one z plane of one channel plane
+__host__ __device__ constexpr int slab_vox(int zs) { return kSlabHX * kSlabHY * (zs + 2); }
+__host__ __device__ constexpr size_t slab_smem_bytes(int cin, int cout, int zs) {
+    return (size_t)(cin / 8) * slab_vox(zs) * 16 + (size_t)27 * (cin / 16) * cout * 32 + 16;
 }
 __host__ __device__ constexpr bool slab_fits(int cin) { return cin == 16 || cin == 32 || cin == 64; }
-__host__ __device__ constexpr long long slab_count(int W, int H, int D) {
-    return (long long)((W + kSlabX - 1) / kSlabX) * ((H + kSlabY - 1) / kSlabY) * D;
+__host__ __device__ constexpr long long slab_count(int W, int H, int D, int zs) {
+    return (long long)((W + kSlabX - 1) / kSlabX) * ((H + kSlabY - 1) / kSlabY) * ((D + zs - 1) / zs);
 }
 
-template <int COUT>
+template <int COUT, int ZS>
 __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
     static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
-    constexpr uint32_t kCols = COUT < 32 ? 32 : COUT;
+    static_assert(ZS == 1 || ZS == 2, "ZS");
+    constexpr uint32_t kCols = ZS * COUT < 32 ? 32 : ZS * COUT;
+    constexpr int kVox = slab_vox(ZS);
+    constexpr uint32_t kPlane = kVox * 16;                  // bytes of one 8-channel plane of the brick
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int chunks = a.cin >> 4, planes = a.cin >> 3;
     const int S = 27 * chunks;
     unsigned char* brick = smem;
-    unsigned char* wsm = smem + (size_t)planes * kSlabPlane;
+    unsigned char* wsm = smem + (size_t)planes * kPlane;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(wsm + (size_t)S * COUT * 32);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int nsx = (a.W + kSlabX - 1) / kSlabX, nsy = (a.H + kSlabY - 1) / kSlabY;
-    const int x0 = (blockIdx.x % nsx) * kSlabX, y0 = ((blockIdx.x / nsx) % nsy) * kSlabY, z0 = blockIdx.x / (nsx * nsy);
+    const int x0 = (blockIdx.x % nsx) * kSlabX, y0 = ((blockIdx.x / nsx) % nsy) * kSlabY;
+    const int z0 = (blockIdx.x / (nsx * nsy)) * ZS;
     const int PW = (a.W + 1) >> 1, PH = (a.H + 1) >> 1;
 
     // the brick: piece p = voxel * planes + plane (the planes of one voxel are adjacent in global memory)
-    const int pieces = kSlabVox * planes;
+    const int pieces = kVox * planes;
     for (int p = tid; p < pieces; p += kConvThreads) {
         const int vox = p / planes, pl = p - vox * planes;
         const int hx = vox % kSlabHX, hy = (vox / kSlabHX) % kSlabHY, hz = vox / (kSlabHX * kSlabHY);
@@ -411,7 +419,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
         const bool ok = gx >= 0 && gx < a.W && gy >= 0 && gy < a.H && gz >= 0 && gz < a.D;
         const int iv = a.up ? (((gz >> 1) * PH + (gy >> 1)) * PW + (gx >> 1)) : ((gz * a.H + gy) * a.W + gx);
         const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + pl * 8) : a.in;
-        cp_async16(brick + (size_t)pl * kSlabPlane + (size_t)vox * 16, src, ok);
+        cp_async16(brick + (size_t)pl * kPlane + (size_t)vox * 16, src, ok);
     }
     // every step's weight tile in k_conv3_tc's B layout; step s's tile at s * COUT * 32 bytes
     const int wpieces = S * COUT * 2;
@@ -436,12 +444,16 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
         // steps in k_conv3_tc's order: s = tap * chunks + chunk, tap = ((dz + 1) * 3 + dy + 1) * 3 + dx + 1
         const uint32_t b0 = smem_u32(brick), w0 = smem_u32(wsm);
         const int clog = __ffs(chunks) - 1;
-        for (int s = 0; s < S; s++) {
-            const int tap = s >> clog, c = s & (chunks - 1);
-            const int hz = tap / 9, hy = (tap / 3) % 3, hx = tap % 3;   // the tap's offsets + 1
-            const uint32_t aaddr = b0 + (uint32_t)(2 * c) * kSlabPlane + (uint32_t)((hz * kSlabHY + hy) * kSlabHX + hx) * 16;
-            mma_bf16(tmem, sdesc(aaddr, kSlabPlane, kSlabRow), sdesc(w0 + (uint32_t)s * COUT * 32, 128, 256),
-                     idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
+#pragma unroll
+        for (int k = 0; k < ZS; k++) {
+            for (int s = 0; s < S; s++) {
+                const int tap = s >> clog, c = s & (chunks - 1);
+                const int hz = tap / 9 + k, hy = (tap / 3) % 3, hx = tap % 3;   // the tap's offsets + 1, slab k
+                const uint32_t aaddr = b0 + (uint32_t)(2 * c) * kPlane + (uint32_t)hz * kSlabZ + (uint32_t)hy * kSlabRow +
+                                       (uint32_t)hx * 16;
+                mma_bf16(tmem + (uint32_t)(k * COUT), sdesc(aaddr, kPlane, kSlabRow),
+                         sdesc(w0 + (uint32_t)s * COUT * 32, 128, 256), idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
+            }
         }
         mma_commit(mbar);
     }
@@ -455,32 +467,67 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
     const int vx = x0 + (tid & 7), vy = y0 + (tid >> 3);
     if (ok) {
         const bool vin = vx < a.W && vy < a.H;
-        const int v = vin ? (z0 * a.H + vy) * a.W + vx : 0;
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        const bool pool = ZS == 2 && a.pool != nullptr;
 #pragma unroll
         for (int c0 = 0; c0 < COUT; c0 += 16) {
-            float acc[16];
-            tmem_ld16(tmem + lane_base + (uint32_t)c0, acc);   // every lane of the warp takes part
-            if (!vin) continue;
-            __align__(16) __nv_bfloat16 o[16], pr[16];
+            float st[ZS][16];   // the stored values, for the pooling
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
-                pr[j] = __float2bfloat16(t);
-                if (a.relu) t = fmaxf(t, 0.f);
-                if (a.skip) t += __bfloat162float(a.skip[(size_t)v * COUT + c0 + j]);
-                o[j] = __float2bfloat16(t);
-                if (a.out32 && c0 + j == 0) a.out32[v] = t;
+            for (int k = 0; k < ZS; k++) {
+                float acc[16];
+                tmem_ld16(tmem + lane_base + (uint32_t)(k * COUT + c0), acc);   // every lane of the warp takes part
+                const bool in = vin && z0 + k < a.D;
+                const size_t v = in ? ((size_t)(z0 + k) * a.H + vy) * a.W + vx : 0;
+                __align__(16) __nv_bfloat16 o[16], pr[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    float t = acc[j] + (a.bias ? a.bias[c0 + j] : 0.f);
+                    pr[j] = __float2bfloat16(t);
+                    if (a.relu) t = fmaxf(t, 0.f);
+                    if (in && a.skip) t += __bfloat162float(a.skip[v * COUT + c0 + j]);
+                    o[j] = __float2bfloat16(t);
+                    st[k][j] = __bfloat162float(o[j]);
+                    if (in && a.out32 && c0 + j == 0) a.out32[v] = t;
+                }
+                if (in && a.out) {
+                    uint4* dst = reinterpret_cast<uint4*>(a.out + v * COUT + c0);
+                    dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                }
+                if (in && a.pre) {
+                    uint4* dst = reinterpret_cast<uint4*>(a.pre + v * COUT + c0);
+                    dst[0] = reinterpret_cast<const uint4*>(pr)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+                }
             }
-            if (a.out) {
-                uint4* dst = reinterpret_cast<uint4*>(a.out + (size_t)v * COUT + c0);
-                dst[0] = reinterpret_cast<const uint4*>(o)[0];
-                dst[1] = reinterpret_cast<const uint4*>(o)[1];
-            }
-            if (a.pre) {
-                uint4* dst = reinterpret_cast<uint4*>(a.pre + (size_t)v * COUT + c0);
-                dst[0] = reinterpret_cast<const uint4*>(pr)[0];
-                dst[1] = reinterpret_cast<const uint4*>(pr)[1];
+            if (pool) {
+                // the pooled voxel of the lane at even (x, y): its own value, then x + 1, y + 1, x + 1 and y + 1,
+                // for z0 and then z0 + 1, as k_pool sums them
+                const bool hx1 = vx + 1 < a.W, hy1 = vy + 1 < a.H, hz1 = z0 + 1 < a.D;
+                const float inv = 1.f / (float)((hx1 ? 2 : 1) * (hy1 ? 2 : 1) * (hz1 ? 2 : 1));
+                __align__(16) __nv_bfloat16 po[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    float sum = 0.f;
+#pragma unroll
+                    for (int k = 0; k < ZS; k++) {
+                        const float sx = __shfl_xor_sync(0xffffffffu, st[k][j], 1);
+                        const float sy = __shfl_xor_sync(0xffffffffu, st[k][j], 8);
+                        const float sxy = __shfl_xor_sync(0xffffffffu, st[k][j], 9);
+                        if (k == 1 && !hz1) continue;
+                        sum += st[k][j];
+                        if (hx1) sum += sx;
+                        if (hy1) sum += sy;
+                        if (hx1 && hy1) sum += sxy;
+                    }
+                    po[j] = __float2bfloat16(sum * inv);
+                }
+                if (vin && !(vx & 1) && !(vy & 1)) {
+                    const size_t pv = ((size_t)(z0 >> 1) * PH + (vy >> 1)) * PW + (vx >> 1);
+                    uint4* dst = reinterpret_cast<uint4*>(a.pool + pv * COUT + c0);
+                    dst[0] = reinterpret_cast<const uint4*>(po)[0];
+                    dst[1] = reinterpret_cast<const uint4*>(po)[1];
+                }
             }
         }
     }

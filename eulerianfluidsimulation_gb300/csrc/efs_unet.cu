@@ -568,9 +568,11 @@ cudaError_t slab_setup(UNetState* u) {
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(tc::k_conv3_slab<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e == cudaSuccess) u->slab_smem = optin;
     return e;
 }
@@ -581,24 +583,40 @@ bool conv_im2col(const UNetState* u, int level, int cin) {
     return !(L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64);
 }
 
-// up: `in` is the next coarser level's tensor, read as its nearest up-sampling (im2col levels only)
+// up: `in` is the next coarser level's tensor, read as its nearest up-sampling (not on halo-tile levels).
+// pool: also the 2x2x2 mean of `out` on the next coarser level (fused into the slab kernel where it serves).
 cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int cin, int cout, int level, const float* bias,
-                 const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st, bool up = false) {
+                 const bf16* skip, bf16* out, float* out32, bf16* pre, int relu, cudaStream_t st, bool up = false,
+                 bf16* pool = nullptr) {
     const Level& L = u->L[level];
+    auto pool_after = [&](cudaError_t e) -> cudaError_t {
+        if (e != cudaSuccess || !pool) return e;
+        const Level& P = u->L[level + 1];
+        k_pool<<<nblk(P.V * (cout / 8)), 256, 0, st>>>(out, L, pool, P, cout);
+        return cudaGetLastError();
+    };
     if (!conv_im2col(u, level, cin)) {
         if (up) return cudaErrorInvalidValue;
-        return conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st);
+        return pool_after(conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st));
     }
     tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0, up ? 1 : 0};
     (void)layer;
-    // narrow grids: one CTA per 8 x 16 slab, its input brick and weights in shared memory
-    const size_t slab_bytes = tc::slab_smem_bytes(cin, cout);
-    if (tc::slab_fits(cin) && slab_bytes <= (size_t)u->slab_smem) {
-        const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D);
-        if (cout == 16) tc::k_conv3_slab<16><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
-        else if (cout == 32) tc::k_conv3_slab<32><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
-        else tc::k_conv3_slab<64><<<gs, tc::kConvThreads, slab_bytes, st>>>(a);
+    // narrow grids: one CTA per 8 x 16 slab (two z slabs where the pooling is fused), its input brick and
+    // weights in shared memory
+    const size_t slab1 = tc::slab_smem_bytes(cin, cout, 1), slab2 = tc::slab_smem_bytes(cin, cout, 2);
+    if (tc::slab_fits(cin) && pool && cout <= 32 && slab2 <= (size_t)u->slab_smem) {
+        a.pool = pool;
+        const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D, 2);
+        if (cout == 16) tc::k_conv3_slab<16, 2><<<gs, tc::kConvThreads, slab2, st>>>(a);
+        else tc::k_conv3_slab<32, 2><<<gs, tc::kConvThreads, slab2, st>>>(a);
         return cudaGetLastError();
+    }
+    if (tc::slab_fits(cin) && slab1 <= (size_t)u->slab_smem) {
+        const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D, 1);
+        if (cout == 16) tc::k_conv3_slab<16, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
+        else if (cout == 32) tc::k_conv3_slab<32, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
+        else tc::k_conv3_slab<64, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
+        return pool_after(cudaGetLastError());
     }
     const unsigned grid = (unsigned)((L.V + 127) / 128);
     // Small grids (the coarse levels of the network, and the whole network on FCG's bottom grid) give too few
@@ -638,12 +656,12 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
             else EFS_SPLIT_REDUCE(64, 1);
         }
 #undef EFS_SPLIT_REDUCE
-        return cudaGetLastError();
+        return pool_after(cudaGetLastError());
     }
     if (cout == 16) tc::k_conv3_tc<16><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
     else if (cout == 32) tc::k_conv3_tc<32><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
     else tc::k_conv3_tc<64><<<grid, tc::kConvThreads, tc::kConvSmem, st>>>(a);
-    return cudaGetLastError();
+    return pool_after(cudaGetLastError());
 }
 
 cudaError_t wgrad(UNetState* u, const bf16* in, const bf16* g, int cin, int cout, int level, float* dw, int sm_count,
@@ -690,7 +708,8 @@ cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, c
                     cudaEvent_t* ev = nullptr, bool prescaled = false) {
     const Level *L = u->L;
     const uint16_t* rowinfo = M.info;
-    // ev (optional): 12 events recorded before and after each of the six convolutions
+    // ev (optional): 12 events recorded before and after each of the six convolutions (layers 0 and 1 with their
+    // pooling)
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     if (!prescaled) UCK(scale_rows(u, r, rowinfo, L[0].V, u->dscal, st));
     k_pack<<<nblk(L[0].V), 256, 0, st>>>(r, rowinfo, u->dscal, L[0].V, u->x0, M.w, M.diag,
@@ -699,15 +718,14 @@ cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, c
     const float* B[kLayers];
     for (int k = 0; k < kLayers; k++) B[k] = u->w32 + u->boff[k];
     mark(0);
-    UCK(conv(u, 0, u->x0, u->wf[0], 16, 16, 0, B[0], nullptr, u->e0, nullptr, train ? u->a0 : nullptr, 1, st));
+    // layers 0 and 1 with the 2x2x2 mean pooling of their outputs (p0, p1)
+    UCK(conv(u, 0, u->x0, u->wf[0], 16, 16, 0, B[0], nullptr, u->e0, nullptr, train ? u->a0 : nullptr, 1, st, false,
+             u->p0));
     mark(1);
-    k_pool<<<nblk(L[1].V * 2), 256, 0, st>>>(u->e0, L[0], u->p0, L[1], 16);
-    UCK(cudaGetLastError());
     mark(2);
-    UCK(conv(u, 1, u->p0, u->wf[1], 16, 32, 1, B[1], nullptr, u->e1, nullptr, train ? u->a1 : nullptr, 1, st));
+    UCK(conv(u, 1, u->p0, u->wf[1], 16, 32, 1, B[1], nullptr, u->e1, nullptr, train ? u->a1 : nullptr, 1, st, false,
+             u->p1));
     mark(3);
-    k_pool<<<nblk(L[2].V * 4), 256, 0, st>>>(u->e1, L[1], u->p1, L[2], 32);
-    UCK(cudaGetLastError());
     mark(4);
     UCK(conv(u, 2, u->p1, u->wf[2], 32, 64, 2, B[2], nullptr, u->e2, nullptr, train ? u->a2 : nullptr, 1, st));
     mark(5);
