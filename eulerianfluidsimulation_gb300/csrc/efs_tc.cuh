@@ -125,6 +125,27 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// ---- TMA and bulk copies ------------------------------------------------------------------------------------
+// The arrival of this thread plus `bytes` of expected transaction count on the mbarrier.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Tiled 4D tensor load (box of the tensor map) into shared memory; elements outside the tensor read as zero.
+// The innermost coordinate c0 is always 0 here (whole 16-byte channel groups).
+__device__ __forceinline__ void tma_load_4d(void* sdst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        ::"r"(smem_u32(sdst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+// Contiguous global -> shared copy (addresses and size multiples of 16 bytes).
+__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // Byte offset of element (row, k) (k < 16) in a K-major no-swizzle tile (see the top of this file).
 __host__ __device__ __forceinline__ uint32_t tile_off(int row, int k) {
     return (uint32_t)((row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
@@ -158,6 +179,9 @@ struct ConvArgs {
     int up;
     // k_conv3_slab with two z slabs: the 2x2x2 mean of the outputs ([ceil(D/2)][ceil(H/2)][ceil(W/2)][COUT]), or null
     __nv_bfloat16* pool;
+    // k_conv3_slab: the weights already in its shared-memory order (step s's B tile at s * COUT * 32 bytes), read
+    // by one bulk copy; null: the kernel arranges `wt` itself
+    const __nv_bfloat16* wslab;
 };
 
 constexpr int kConvThreads = 128;
@@ -382,7 +406,7 @@ constexpr uint32_t kSlabRow = kSlabHX * 16;               // bytes of one brick 
 constexpr uint32_t kSlabZ = kSlabHY * kSlabRow;           // bytes of one z plane of one channel plane
 __host__ __device__ constexpr int slab_vox(int zs) { return kSlabHX * kSlabHY * (zs + 2); }
 __host__ __device__ constexpr size_t slab_smem_bytes(int cin, int cout, int zs) {
-    return (size_t)(cin / 8) * slab_vox(zs) * 16 + (size_t)27 * (cin / 16) * cout * 32 + 16;
+    return (size_t)(cin / 8) * slab_vox(zs) * 16 + (size_t)27 * (cin / 16) * cout * 32 + 32;
 }
 __host__ __device__ constexpr bool slab_fits(int cin) { return cin == 16 || cin == 32 || cin == 64; }
 __host__ __device__ constexpr long long slab_count(int W, int H, int D, int zs) {
@@ -402,12 +426,22 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
     const int S = 27 * chunks;
     unsigned char* brick = smem;
     unsigned char* wsm = smem + (size_t)planes * kPlane;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(wsm + (size_t)S * COUT * 32);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(wsm + (size_t)S * COUT * 32);   // [0] the MMAs, [1] the weights
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    const uint32_t wbytes = (uint32_t)S * COUT * 32;
 
     const int nsx = (a.W + kSlabX - 1) / kSlabX, nsy = (a.H + kSlabY - 1) / kSlabY;
     const int x0 = (blockIdx.x % nsx) * kSlabX, y0 = ((blockIdx.x / nsx) % nsy) * kSlabY;
     const int z0 = (blockIdx.x / (nsx * nsy)) * ZS;
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (a.wslab) {   // the packed weights: one bulk copy, complete on mbar[1]
+            mbar_expect_tx(&mbar[1], wbytes);
+            bulk_load(wsm, a.wslab, wbytes, &mbar[1]);
+        }
+    }
     const int PW = (a.W + 1) >> 1, PH = (a.H + 1) >> 1;
 
     // the brick: piece p = voxel * planes + plane (the planes of one voxel are adjacent in global memory)
@@ -421,8 +455,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
         const __nv_bfloat16* src = ok ? a.in + ((size_t)iv * a.cin + pl * 8) : a.in;
         cp_async16(brick + (size_t)pl * kPlane + (size_t)vox * 16, src, ok);
     }
-    // every step's weight tile in k_conv3_tc's B layout; step s's tile at s * COUT * 32 bytes
-    const int wpieces = S * COUT * 2;
+    // without packed weights: every step's weight tile in k_conv3_tc's B layout, step s's tile at s * COUT * 32
+    // bytes, one 16-byte piece at a time
+    const int wpieces = a.wslab ? 0 : S * COUT * 2;
     for (int q = tid; q < wpieces; q += kConvThreads) {
         const int s = q / (2 * COUT), r = q - s * 2 * COUT, n = r >> 1, kh = r & 1;
         cp_async16(wsm + (size_t)s * COUT * 32 + tile_off(n, kh * 8), a.wt + ((size_t)(s * COUT + n) * 16 + kh * 8),
@@ -430,10 +465,6 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
     }
     cp_async_commit();
     if (warp == 0) tmem_alloc(tslot, kCols);
-    if (tid == 0) {
-        mbar_init(mbar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
     cp_async_wait<0>();
     fence_async_smem();
     tc_fence_before();
@@ -444,8 +475,13 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
         // steps in k_conv3_tc's order: s = tap * chunks + chunk, tap = ((dz + 1) * 3 + dy + 1) * 3 + dx + 1
         const uint32_t b0 = smem_u32(brick), w0 = smem_u32(wsm);
         const int clog = __ffs(chunks) - 1;
+        // the bulk copy of the weights (bounded); without it no MMA is issued, the error word says why, and
+        // the commit below still completes mbar[0]
+        const bool wok = !a.wslab || mbar_wait(&mbar[1], 0);
+        if (!wok) atomicOr(a.err, 1);
+        tc_fence_after();
 #pragma unroll
-        for (int k = 0; k < ZS; k++) {
+        for (int k = 0; k < (wok ? ZS : 0); k++) {
             for (int s = 0; s < S; s++) {
                 const int tap = s >> clog, c = s & (chunks - 1);
                 const int hz = tap / 9 + k, hy = (tap / 3) % 3, hx = tap % 3;   // the tap's offsets + 1, slab k
@@ -455,13 +491,13 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
                          sdesc(w0 + (uint32_t)s * COUT * 32, 128, 256), idesc_bf16(128, COUT), s > 0 ? 1u : 0u);
             }
         }
-        mma_commit(mbar);
+        mma_commit(&mbar[0]);
     }
-    bool ok = mbar_wait(mbar, 0);
+    bool ok = mbar_wait(&mbar[0], 0);
     if (!ok) {
         if (tid == 0) atomicOr(a.err, 1);
         // bounded: let MMAs in flight finish before freeing TMEM
-        mbar_wait(mbar, 0);
+        mbar_wait(&mbar[0], 0);
     }
     tc_fence_after();
     const int vx = x0 + (tid & 7), vy = y0 + (tid >> 3);
@@ -652,27 +688,6 @@ __global__ void __launch_bounds__(kConvThreads) k_wgrad3_tc(WgradArgs a) {
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, kCols);
-}
-
-// ---- TMA and bulk copies ------------------------------------------------------------------------------------
-// The arrival of this thread plus `bytes` of expected transaction count on the mbarrier.
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-// Tiled 4D tensor load (box of the tensor map) into shared memory; elements outside the tensor read as zero.
-// The innermost coordinate c0 is always 0 here (whole 16-byte channel groups).
-__device__ __forceinline__ void tma_load_4d(void* sdst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
-                                            uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
-        ::"r"(smem_u32(sdst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
-        : "memory");
-}
-// Contiguous global -> shared copy (addresses and size multiples of 16 bytes).
-__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
 }
 
 // ============================================================================================================

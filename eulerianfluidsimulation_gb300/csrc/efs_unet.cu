@@ -67,6 +67,7 @@ struct UNetState {
     float *w32 = nullptr, *grad = nullptr, *am = nullptr, *av = nullptr;
     int adam_t = 0;
     bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
+    bf16 *wsf[kLayers] = {}, *wsb[kLayers] = {};   // wf, wb in k_conv3_slab's shared-memory order
     bf16* wh = nullptr;          // weights of the convolution in flight, packed for k_conv3_halo_ws
     // activations (level of each in brackets)
     bf16 *x0 = nullptr, *e0 = nullptr, *p0 = nullptr, *e1 = nullptr, *p1 = nullptr, *e2 = nullptr, *u2 = nullptr,
@@ -354,13 +355,20 @@ __global__ void k_sum_partials(const double* __restrict__ part, int nb, const do
 }
 // FP32 master weights -> BF16 operand layouts: forward wf[tap][cin/16][cout][16]; input gradient
 // wb[tap'][cout/16][cin][16] with tap' = 26 - tap (negated offsets) and the channel roles swapped.
-__global__ void k_w_to_bf16(const float* __restrict__ w, int cin, int cout, bf16* __restrict__ wf, bf16* __restrict__ wb) {
+// wf: the forward weights [tap][cin/16][cout][16]; wb: the input gradient's (taps flipped, cin and cout swapped)
+// [26 - tap][cout/16][cin][16]; wsf, wsb: the same as k_conv3_slab keeps them in shared memory, step s's
+// K-major no-swizzle B tile (rows = output channels) at s * rows * 16 elements
+__global__ void k_w_to_bf16(const float* __restrict__ w, int cin, int cout, bf16* __restrict__ wf, bf16* __restrict__ wb,
+                            bf16* __restrict__ wsf, bf16* __restrict__ wsb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 27 * cin * cout) return;
     const int co = i % cout, ci = (i / cout) % cin, tap = i / (cout * cin);
     const bf16 v = __float2bfloat16(w[i]);
-    wf[(((size_t)tap * (cin / 16) + ci / 16) * cout + co) * 16 + ci % 16] = v;
-    wb[(((size_t)(26 - tap) * (cout / 16) + co / 16) * cin + ci) * 16 + co % 16] = v;
+    const size_t sf = (size_t)tap * (cin / 16) + ci / 16, sb = (size_t)(26 - tap) * (cout / 16) + co / 16;
+    wf[(sf * cout + co) * 16 + ci % 16] = v;
+    wb[(sb * cin + ci) * 16 + co % 16] = v;
+    wsf[sf * cout * 16 + tc::tile_off(co, ci % 16) / 2] = v;
+    wsb[sb * cin * 16 + tc::tile_off(ci, co % 16) / 2] = v;
 }
 __global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2, float gscale) {
@@ -600,9 +608,9 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
         return pool_after(conv_halo(u, in, wt, cin, cout, L, bias, skip, out, out32, pre, relu, st));
     }
     tc::ConvArgs a{in, wt, bias, skip, out, out32, pre, L.D, L.H, L.W, cin, relu, u->err, nullptr, 0, up ? 1 : 0};
-    (void)layer;
     // narrow grids: one CTA per 8 x 16 slab (two z slabs where the pooling is fused), its input brick and
-    // weights in shared memory
+    // weights in shared memory; the layer's weights come packed in that order where `wt` is one of its copies
+    a.wslab = wt == u->wf[layer] ? u->wsf[layer] : wt == u->wb[layer] ? u->wsb[layer] : nullptr;
     const size_t slab1 = tc::slab_smem_bytes(cin, cout, 1), slab2 = tc::slab_smem_bytes(cin, cout, 2);
     if (tc::slab_fits(cin) && pool && cout <= 32 && slab2 <= (size_t)u->slab_smem) {
         a.pool = pool;
@@ -686,7 +694,8 @@ cudaError_t wgrad(UNetState* u, const bf16* in, const bf16* g, int cin, int cout
 cudaError_t refresh_bf16(UNetState* u, cudaStream_t st) {
     for (int k = 0; k < kLayers; k++) {
         const int n = 27 * kSpec[k].cin * kSpec[k].cout;
-        k_w_to_bf16<<<nblk(n), 256, 0, st>>>(u->w32 + u->woff[k], kSpec[k].cin, kSpec[k].cout, u->wf[k], u->wb[k]);
+        k_w_to_bf16<<<nblk(n), 256, 0, st>>>(u->w32 + u->woff[k], kSpec[k].cin, kSpec[k].cout, u->wf[k], u->wb[k],
+                                              u->wsf[k], u->wsb[k]);
         UCK(cudaGetLastError());
     }
     return cudaSuccess;
@@ -883,6 +892,8 @@ cudaError_t alloc_net(efs_ctx* c, UNetState** out) {
     for (int k = 0; k < kLayers; k++) {
         UCK(ualloc(u, &u->wf[k], 27LL * kSpec[k].cin * kSpec[k].cout));
         UCK(ualloc(u, &u->wb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
+        UCK(ualloc(u, &u->wsf[k], 27LL * kSpec[k].cin * kSpec[k].cout));
+        UCK(ualloc(u, &u->wsb[k], 27LL * kSpec[k].cin * kSpec[k].cout));
     }
     UCK(ualloc(u, &u->wh, 27LL * 64 * 64));
     // split convolutions run on grids of fewer than 8 x SMs CTAs of 128 voxels, into at most 8 x SMs + CTAs more
