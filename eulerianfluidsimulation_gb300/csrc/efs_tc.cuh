@@ -405,21 +405,31 @@ constexpr int kSlabHX = kSlabX + 2, kSlabHY = kSlabY + 2;
 constexpr uint32_t kSlabRow = kSlabHX * 16;               // bytes of one brick row: the A stride byte offset
 constexpr uint32_t kSlabZ = kSlabHY * kSlabRow;           // bytes of one z plane of one channel plane
 __host__ __device__ constexpr int slab_vox(int zs) { return kSlabHX * kSlabHY * (zs + 2); }
+// bytes of one 8-channel plane of the brick, padded to 128 (the alignment of a tensor copy's destination)
+__host__ __device__ constexpr uint32_t slab_plane(int zs) { return ((uint32_t)slab_vox(zs) * 16 + 127) / 128 * 128; }
 __host__ __device__ constexpr size_t slab_smem_bytes(int cin, int cout, int zs) {
-    return (size_t)(cin / 8) * slab_vox(zs) * 16 + (size_t)27 * (cin / 16) * cout * 32 + 32;
+    return (size_t)(cin / 8) * slab_plane(zs) + (size_t)27 * (cin / 16) * cout * 32 + 32;
 }
 __host__ __device__ constexpr bool slab_fits(int cin) { return cin == 16 || cin == 32 || cin == 64; }
 __host__ __device__ constexpr long long slab_count(int W, int H, int D, int zs) {
     return (long long)((W + kSlabX - 1) / kSlabX) * ((H + kSlabY - 1) / kSlabY) * ((D + zs - 1) / zs);
 }
 
+// TMA maps of the input's 8-channel planes for k_conv3_slab (n = cin / 8 maps, box 8 x 10 x 18 x (ZS + 2) at
+// (0, x0 - 1, y0 - 1, z0 - 1), zero outside the grid); n = 0: the brick is gathered by cp.async (the up-sampled
+// inputs, which no tensor map describes)
+struct SlabMaps {
+    CUtensorMap map[8];
+    int n;
+};
+
 template <int COUT, int ZS>
-__global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
+__global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a, const __grid_constant__ SlabMaps m) {
     static_assert(COUT == 16 || COUT == 32 || COUT == 64, "COUT");
     static_assert(ZS == 1 || ZS == 2, "ZS");
     constexpr uint32_t kCols = ZS * COUT < 32 ? 32 : ZS * COUT;
     constexpr int kVox = slab_vox(ZS);
-    constexpr uint32_t kPlane = kVox * 16;                  // bytes of one 8-channel plane of the brick
+    constexpr uint32_t kPlane = slab_plane(ZS);            // bytes of one 8-channel plane of the brick
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int chunks = a.cin >> 4, planes = a.cin >> 3;
@@ -433,19 +443,27 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
     const int nsx = (a.W + kSlabX - 1) / kSlabX, nsy = (a.H + kSlabY - 1) / kSlabY;
     const int x0 = (blockIdx.x % nsx) * kSlabX, y0 = ((blockIdx.x / nsx) % nsy) * kSlabY;
     const int z0 = (blockIdx.x / (nsx * nsy)) * ZS;
+    const bool tma = m.n == planes;
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (a.wslab) {   // the packed weights: one bulk copy, complete on mbar[1]
-            mbar_expect_tx(&mbar[1], wbytes);
-            bulk_load(wsm, a.wslab, wbytes, &mbar[1]);
+        // the packed weights (one bulk copy) and the brick's planes (one tensor load each), complete on mbar[1]
+        // (a tensor load delivers its box, kVox x 16 bytes, into a plane padded to kPlane)
+        const uint32_t tx = (a.wslab ? wbytes : 0u) + (tma ? (uint32_t)planes * (uint32_t)(kVox * 16) : 0u);
+        if (tx) {
+            mbar_expect_tx(&mbar[1], tx);
+            if (a.wslab) bulk_load(wsm, a.wslab, wbytes, &mbar[1]);
+            if (tma)
+                for (int pl = 0; pl < planes; pl++)
+                    tma_load_4d(brick + (size_t)pl * kPlane, &m.map[pl], 0, x0 - 1, y0 - 1, z0 - 1, &mbar[1]);
         }
     }
     const int PW = (a.W + 1) >> 1, PH = (a.H + 1) >> 1;
 
-    // the brick: piece p = voxel * planes + plane (the planes of one voxel are adjacent in global memory)
-    const int pieces = kVox * planes;
+    // without tensor maps, the brick by cp.async: piece p = voxel * planes + plane (the planes of one voxel are
+    // adjacent in global memory)
+    const int pieces = tma ? 0 : kVox * planes;
     for (int p = tid; p < pieces; p += kConvThreads) {
         const int vox = p / planes, pl = p - vox * planes;
         const int hx = vox % kSlabHX, hy = (vox / kSlabHX) % kSlabHY, hz = vox / (kSlabHX * kSlabHY);
@@ -475,9 +493,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3_slab(ConvArgs a) {
         // steps in k_conv3_tc's order: s = tap * chunks + chunk, tap = ((dz + 1) * 3 + dy + 1) * 3 + dx + 1
         const uint32_t b0 = smem_u32(brick), w0 = smem_u32(wsm);
         const int clog = __ffs(chunks) - 1;
-        // the bulk copy of the weights (bounded); without it no MMA is issued, the error word says why, and
-        // the commit below still completes mbar[0]
-        const bool wok = !a.wslab || mbar_wait(&mbar[1], 0);
+        // the bulk and tensor copies (bounded); without them no MMA is issued, the error word says why, and the
+        // commit below still completes mbar[0]
+        const bool wok = !(a.wslab || tma) || mbar_wait(&mbar[1], 0);
         if (!wok) atomicOr(a.err, 1);
         tc_fence_after();
 #pragma unroll

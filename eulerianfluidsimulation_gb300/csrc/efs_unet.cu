@@ -585,6 +585,26 @@ cudaError_t slab_setup(UNetState* u) {
     return e;
 }
 
+// k_conv3_slab's tensor maps of `in` (channels-last, cin channels on level L): plane g covers channels 8 g ..
+// 8 g + 7; the box is one slab's brick.  Left empty (maps->n = 0, the kernel then gathers by cp.async) when the
+// driver's encoder is unavailable or refuses a map.
+void slab_maps(const bf16* in, int cin, const Level& L, int zs, tc::SlabMaps* maps) {
+    maps->n = 0;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode || cin / 8 > 8) return;
+    const cuuint64_t dims[4] = {8, (cuuint64_t)L.W, (cuuint64_t)L.H, (cuuint64_t)L.D};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)L.W * cin * 2, (cuuint64_t)L.H * L.W * cin * 2};
+    const cuuint32_t boxd[4] = {8, (cuuint32_t)tc::kSlabHX, (cuuint32_t)tc::kSlabHY, (cuuint32_t)(zs + 2)};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    for (int g = 0; g < cin / 8; g++) {
+        const CUresult r = encode(&maps->map[g], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)(in + 8 * g), dims, strides,
+                                  boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return;
+    }
+    maps->n = cin / 8;
+}
+
 // the implicit-GEMM (im2col) kernel serves the level; it can read an up-sampled input in place
 bool conv_im2col(const UNetState* u, int level, int cin) {
     const Level& L = u->L[level];
@@ -612,18 +632,22 @@ cudaError_t conv(UNetState* u, int layer, const bf16* in, const bf16* wt, int ci
     // weights in shared memory; the layer's weights come packed in that order where `wt` is one of its copies
     a.wslab = wt == u->wf[layer] ? u->wsf[layer] : wt == u->wb[layer] ? u->wsb[layer] : nullptr;
     const size_t slab1 = tc::slab_smem_bytes(cin, cout, 1), slab2 = tc::slab_smem_bytes(cin, cout, 2);
+    tc::SlabMaps maps;
+    std::memset(&maps, 0, sizeof(maps));
     if (tc::slab_fits(cin) && pool && cout <= 32 && slab2 <= (size_t)u->slab_smem) {
         a.pool = pool;
+        if (!up) slab_maps(in, cin, L, 2, &maps);
         const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D, 2);
-        if (cout == 16) tc::k_conv3_slab<16, 2><<<gs, tc::kConvThreads, slab2, st>>>(a);
-        else tc::k_conv3_slab<32, 2><<<gs, tc::kConvThreads, slab2, st>>>(a);
+        if (cout == 16) tc::k_conv3_slab<16, 2><<<gs, tc::kConvThreads, slab2, st>>>(a, maps);
+        else tc::k_conv3_slab<32, 2><<<gs, tc::kConvThreads, slab2, st>>>(a, maps);
         return cudaGetLastError();
     }
     if (tc::slab_fits(cin) && slab1 <= (size_t)u->slab_smem) {
+        if (!up) slab_maps(in, cin, L, 1, &maps);
         const unsigned gs = (unsigned)tc::slab_count(L.W, L.H, L.D, 1);
-        if (cout == 16) tc::k_conv3_slab<16, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
-        else if (cout == 32) tc::k_conv3_slab<32, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
-        else tc::k_conv3_slab<64, 1><<<gs, tc::kConvThreads, slab1, st>>>(a);
+        if (cout == 16) tc::k_conv3_slab<16, 1><<<gs, tc::kConvThreads, slab1, st>>>(a, maps);
+        else if (cout == 32) tc::k_conv3_slab<32, 1><<<gs, tc::kConvThreads, slab1, st>>>(a, maps);
+        else tc::k_conv3_slab<64, 1><<<gs, tc::kConvThreads, slab1, st>>>(a, maps);
         return pool_after(cudaGetLastError());
     }
     const unsigned grid = (unsigned)((L.V + 127) / 128);
