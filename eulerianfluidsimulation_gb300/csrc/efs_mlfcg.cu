@@ -58,6 +58,11 @@ struct FcgDev {
     double rr, rz, dq, zq, bb, thr, alpha, beta, rr_window, rows;
     double ls_alpha;                  // bottom-level line search factor of the current V-cycle (1 without the network)
     float alpha_hi, alpha_lo, beta_f; // alpha as a float pair and beta in float, for the level-0 kernels
+    float alpha_prev_hi, alpha_prev_lo;   // the previous iteration's alpha (x may still lack its step)
+    // The two direction buffers (d0, d1) alternate: the direction of iteration k is written to buffer par ^ 1 and
+    // becomes buffer par when the iteration's last finisher toggles par.  x takes its steps two iterations at a
+    // time: xlag = 1 while it lacks alpha d of the direction in buffer par.
+    int par, xlag;
     int it, conv, stall, verify, fallback, nchunks;
     int ncchunks;                     // level 1's 32-cell chunks that hold a row (the restriction's list)
     // arrival counters (groups, then the top), back to 0 after each reduction
@@ -110,6 +115,25 @@ __device__ __forceinline__ float resid_pair(const LvView& L, long long i, const 
     const float2 lap = df_add(sum, df_neg(df_mul_k(x[i], (float)((f >> 8) & 7))));
     const float2 t = df_add_f(df_neg(lap), b);
     return __fadd_rn(t.x, t.y);
+}
+// resid_pair of x + (ah + al) d, the pending step formed at each of the seven points as the vector update forms it
+__device__ __forceinline__ float resid_pair_step(const LvView& L, long long i, const float2* x, const float* d, float ah,
+                                                 float al, float b, unsigned f) {
+    float2 sum = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        if ((f >> k) & 1u) {
+            const long long j = i + noff(L, k);
+            sum = df_add(sum, df_axpy(x[j], ah, al, d[j]));
+        }
+    const float2 lap = df_add(sum, df_neg(df_mul_k(df_axpy(x[i], ah, al, d[i]), (float)((f >> 8) & 7))));
+    const float2 t = df_add_f(df_neg(lap), b);
+    return __fadd_rn(t.x, t.y);
+}
+// the start of an iteration's vector step: the old alpha becomes the previous one
+__device__ __forceinline__ void shift_alpha(FcgDev* s) {
+    s->alpha_prev_hi = s->alpha_hi;
+    s->alpha_prev_lo = s->alpha_lo;
 }
 // alpha / beta for the float kernels
 __device__ __forceinline__ void set_alpha(FcgDev* s, double a) {
@@ -840,9 +864,11 @@ __global__ void k_q_prolong_smooth(QWalk qw, const uint16_t* __restrict__ info, 
 }
 // k_fcg_dir_matvec at level 0
 __global__ void k_q_dir_matvec(QWalk qw, const uint16_t* __restrict__ info, int W, int WH, const float* __restrict__ z,
-                               const float* __restrict__ d, float* __restrict__ dn, float* __restrict__ q, FcgDev* s,
+                               float* __restrict__ d0, float* __restrict__ d1, float* __restrict__ q, FcgDev* s,
                                double* __restrict__ part) {
     const float beta = s->beta_f;
+    const float* d = s->par ? d1 : d0;
+    float* dn = s->par ? d0 : d1;
     float dq = 0.f;
     QWALK(qw, i) {
         unsigned f[4];
@@ -870,6 +896,7 @@ __global__ void k_q_finish_dq(const double* __restrict__ part, int n, FcgDev* s)
     double tot[1];
     if (!finish_partials<1>(part, n, tot)) return;
     s->dq = tot[0];
+    shift_alpha(s);
     const double al = s->rz / tot[0];
     if (!(tot[0] < 0.0) || !isfinite(al)) {
         s->stall = 1;
@@ -879,30 +906,38 @@ __global__ void k_q_finish_dq(const double* __restrict__ part, int n, FcgDev* s)
     }
 }
 // k_fcg_update at level 0
-__global__ void k_q_update(QWalk qw, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
-                           float* __restrict__ d, const float* __restrict__ q, const FcgDev* s, double* __restrict__ part) {
-    const float af = s->alpha_hi, al = s->alpha_lo;
+__global__ void k_q_update(QWalk qw, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ d0,
+                           const float* __restrict__ d1, const float* __restrict__ q, const FcgDev* s,
+                           double* __restrict__ part) {
+    const float af = s->alpha_hi, al = s->alpha_lo, pf = s->alpha_prev_hi, pl = s->alpha_prev_lo;
+    const bool lag = s->xlag;
+    const float* dprev = s->par ? d1 : d0;   // the previous direction, whose step x lacks when lag
+    const float* dcur = s->par ? d0 : d1;    // this iteration's
     float rr = 0.f;
     QWALK(qw, i) {
-        float dv[4], rv[4], qv[4];
-        ld4(dn, i, dv);
+        float rv[4], qv[4];
         ld4(r, i, rv);
         ld4(q, i, qv);
-        float4* x4 = reinterpret_cast<float4*>(x + i);
-        float4 x01 = x4[0], x23 = x4[1];
-        float2 p0 = df_axpy(make_float2(x01.x, x01.y), af, al, dv[0]);
-        float2 p1 = df_axpy(make_float2(x01.z, x01.w), af, al, dv[1]);
-        float2 p2 = df_axpy(make_float2(x23.x, x23.y), af, al, dv[2]);
-        float2 p3 = df_axpy(make_float2(x23.z, x23.w), af, al, dv[3]);
-        x4[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
-        x4[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
+        if (lag) {
+            // both steps, in the order the iterations take them
+            float dp[4], dv[4];
+            ld4(dprev, i, dp);
+            ld4(dcur, i, dv);
+            float4* x4 = reinterpret_cast<float4*>(x + i);
+            float4 x01 = x4[0], x23 = x4[1];
+            float2 p0 = df_axpy(df_axpy(make_float2(x01.x, x01.y), pf, pl, dp[0]), af, al, dv[0]);
+            float2 p1 = df_axpy(df_axpy(make_float2(x01.z, x01.w), pf, pl, dp[1]), af, al, dv[1]);
+            float2 p2 = df_axpy(df_axpy(make_float2(x23.x, x23.y), pf, pl, dp[2]), af, al, dv[2]);
+            float2 p3 = df_axpy(df_axpy(make_float2(x23.z, x23.w), pf, pl, dp[3]), af, al, dv[3]);
+            x4[0] = make_float4(p0.x, p0.y, p1.x, p1.y);
+            x4[1] = make_float4(p2.x, p2.y, p3.x, p3.y);
+        }
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             rv[k] = rv[k] - af * qv[k];
             rr += rv[k] * rv[k];
         }
         st4(r, i, rv);
-        st4(d, i, dv);
     }
     float v[1] = {rr};
     block_partials<1>(v, part);
@@ -919,6 +954,8 @@ __global__ void k_q_finish_rr(const double* __restrict__ part, int n, FcgDev* s,
         s->rr_window = s->rr;
     }
     s->verify = !s->stall && (below || (s->it % 32) == 0);
+    s->par ^= 1;
+    s->xlag ^= 1;
     cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
 }
 
@@ -962,16 +999,22 @@ __global__ void k_fcg_init(LvView F, Walk wk, const float* __restrict__ b, float
         s->rr_window = s->rr;
         s->rz = s->dq = s->zq = 0;
         set_alpha(s, 0.0);
+        shift_alpha(s);
         set_beta(s, 0.0);
+        s->par = 0;          // d (zeroed above) is buffer 0
+        s->xlag = 0;
         s->ls_alpha = 1.0;
         cudaGraphSetConditional(loop, (!s->conv && max_it > 0) ? 1u : 0u);
     }
 }
 // dn = z + beta d (on the fly for the stencil's neighbours), q = A dn; d.q and alpha = (r.z) / (dn.q).  L is
 // negative definite on the rows, so dn.q >= 0 (or a non-finite alpha) is a breakdown: the solve stalls.
-__global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z, const float* __restrict__ d,
-                                 float* __restrict__ dn, float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
+// d is direction buffer par, dn the other.
+__global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z, float* __restrict__ d0,
+                                 float* __restrict__ d1, float* __restrict__ q, FcgDev* s, double* __restrict__ part) {
     const float beta = s->beta_f;
+    const float* d = s->par ? d1 : d0;
+    float* dn = s->par ? d0 : d1;
     float dq = 0.f;
     WALK(wk, t, i) {
         float dg, w[6];
@@ -994,6 +1037,7 @@ __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z,
     float v[1] = {dq};
     if (reduce_last(v, part, s->count, tot)) {
         s->dq = tot[0];
+        shift_alpha(s);
         const double a = s->rz / tot[0];
         if (!(tot[0] < 0.0) || !isfinite(a)) {
             s->stall = 1;
@@ -1003,19 +1047,21 @@ __global__ void k_fcg_dir_matvec(LvView F, Walk wk, const float* __restrict__ z,
         }
     }
 }
-// x += alpha dn, r -= alpha q, d = dn; r.r, the iteration count, the stall window and whether the true residual
-// is recomputed now (every 32 iterations and when the recurrence residual meets the threshold)
-__global__ void k_fcg_update(Walk wk, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ dn,
-                             float* __restrict__ d, const float* __restrict__ q, FcgDev* s, double* __restrict__ part,
-                             cudaGraphConditionalHandle verify) {
-    const float af = s->alpha_hi, al = s->alpha_lo;
+// r -= alpha q and, every other iteration, x += alpha' d' + alpha dn (the previous step and this one, in that
+// order); r.r, the iteration count, the stall window and whether the true residual is recomputed now (every 32
+// iterations and when the recurrence residual meets the threshold); the direction buffers swap
+__global__ void k_fcg_update(Walk wk, float2* __restrict__ x, float* __restrict__ r, const float* __restrict__ d0,
+                             const float* __restrict__ d1, const float* __restrict__ q, FcgDev* s,
+                             double* __restrict__ part, cudaGraphConditionalHandle verify) {
+    const float af = s->alpha_hi, al = s->alpha_lo, pf = s->alpha_prev_hi, pl = s->alpha_prev_lo;
+    const bool lag = s->xlag;
+    const float* dprev = s->par ? d1 : d0;
+    const float* dcur = s->par ? d0 : d1;
     float rr = 0.f;
     WALK(wk, t, i) {
-        const float di = dn[i];
-        x[i] = df_axpy(x[i], af, al, di);
+        if (lag) x[i] = df_axpy(df_axpy(x[i], pf, pl, dprev[i]), af, al, dcur[i]);
         const float ri = r[i] - af * q[i];
         r[i] = ri;
-        d[i] = di;
         rr += ri * ri;
     }
     double tot[3];
@@ -1029,17 +1075,25 @@ __global__ void k_fcg_update(Walk wk, float2* __restrict__ x, float* __restrict_
             s->rr_window = s->rr;
         }
         s->verify = !s->stall && (below || (s->it % 32) == 0);
+        s->par ^= 1;
+        s->xlag ^= 1;
         cudaGraphSetConditional(verify, s->verify ? 1u : 0u);
     }
 }
-// r = b - A x in FP64 (rows); r.r and the convergence decision
+// r = b - A x in float pairs (rows), with x's pending step alpha d (d: direction buffer par) formed on the fly;
+// r.r and the convergence decision
 __global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b, const float2* __restrict__ x,
-                                 float* __restrict__ r, FcgDev* s, double* __restrict__ part) {
+                                 const float* __restrict__ d0, const float* __restrict__ d1, float* __restrict__ r,
+                                 FcgDev* s, double* __restrict__ part) {
+    const bool lag = s->xlag;
+    const float* d = s->par ? d1 : d0;
+    const float ah = s->alpha_hi, al = s->alpha_lo;
     double rr = 0;
     WALK(wk, t, i) {
         float dg, w[6];
         float ri = 0.f;
-        if (lrow<true>(F, i, dg, w)) ri = resid_pair(F, i, x, b[i], F.info[i]);
+        if (lrow<true>(F, i, dg, w))
+            ri = lag ? resid_pair_step(F, i, x, d, ah, al, b[i], F.info[i]) : resid_pair(F, i, x, b[i], F.info[i]);
         r[i] = ri;
         rr += (double)ri * ri;
     }
@@ -1049,6 +1103,14 @@ __global__ void k_fcg_true_resid(LvView F, Walk wk, const float* __restrict__ b,
         s->rr = tot[0];
         s->conv = s->rr < s->thr;
     }
+}
+// after the loop: x's pending step, if any (x += alpha d, d: direction buffer par)
+__global__ void k_fcg_flush(Walk wk, float2* __restrict__ x, const float* __restrict__ d0, const float* __restrict__ d1,
+                            const FcgDev* __restrict__ s) {
+    if (!s->xlag) return;
+    const float* d = s->par ? d1 : d0;
+    const float ah = s->alpha_hi, al = s->alpha_lo;
+    WALK(wk, t, i) { x[i] = df_axpy(x[i], ah, al, d[i]); }
 }
 // the loop condition for the next iteration
 __global__ void k_fcg_loop(const FcgDev* __restrict__ s, int max_it, cudaGraphConditionalHandle loop) {
@@ -1506,10 +1568,10 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             }
             if ((e = make_handle(b, &h_verify)) != cudaSuccess) break;
             if (quad) {
-                k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->xp, m->r, m->dn, m->d, m->q, m->s, m->part);
+                k_q_update<<<gq, kThreads, 0, b>>>(qwalk_of(m), m->xp, m->r, m->d, m->dn, m->q, m->s, m->part);
                 k_q_finish_rr<<<1, kThreads, 0, b>>>(m->part, (int)gq, m->s, h_verify);
             } else {
-                k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->xp, m->r, m->dn, m->d, m->q, m->s, m->part, h_verify);
+                k_fcg_update<<<g, kThreads, 0, b>>>(wk, m->xp, m->r, m->d, m->dn, m->q, m->s, m->part, h_verify);
             }
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             // ---- IF: the true residual in FP64 (every 32 iterations and before stopping) ----
@@ -1517,7 +1579,7 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
             if ((e = add_conditional(b, h_verify, cudaGraphCondTypeIf, &vbody)) != cudaSuccess) break;
             cudaStream_t v = m->cap2;
             if ((e = cudaStreamBeginCaptureToGraph(v, vbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-            k_fcg_true_resid<<<g, kThreads, 0, v>>>(F, wk, c->div, m->xp, m->r, m->s, m->part);
+            k_fcg_true_resid<<<g, kThreads, 0, v>>>(F, wk, c->div, m->xp, m->d, m->dn, m->r, m->s, m->part);
             cudaError_t ve = cudaGetLastError();
             cudaGraph_t dummy = nullptr;
             cudaError_t ee = cudaStreamEndCapture(v, &dummy);
@@ -1531,6 +1593,8 @@ cudaError_t fcg_enqueue(efs_ctx* c, cudaStream_t st) {
         MCK(ee);
     }
 
+    k_fcg_flush<<<g, kThreads, 0, st>>>(wk, m->xp, m->d, m->dn, m->s);
+    MCK(cudaGetLastError());
     // ---- IF: the plain-CG fallback on the residual system ----
     MCK(make_handle(st, &h_fb));
     k_fcg_post<<<1, 32, 0, st>>>(m->s, h_fb);
