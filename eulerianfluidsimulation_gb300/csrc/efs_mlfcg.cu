@@ -38,7 +38,7 @@ namespace efs {
 
 namespace {
 
-constexpr float kOmega = 0.8f;        // Jacobi damping
+constexpr float kOmega = 6.0f / 7.0f;  // Jacobi damping (the smoothing optimum of the 3D 7-point stencil)
 constexpr int kBottomJacobi = 20;     // sweeps of the bottom solve without the network
 constexpr int kThreads = 256;
 // Most blocks of a level kernel (threads loop over the rest; the partials buffer holds one per block): 8 per SM

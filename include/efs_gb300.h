@@ -159,7 +159,7 @@ typedef struct efs_params {
 /* The preconditioner of EFS_SOLVER_FCG_UNET (no counterpart in the reference) is one V-cycle over a hierarchy
  * of aggregated grids: level 0 is the pressure matrix itself; level l+1 merges 2x2x2 cells of level l, its
  * matrix the Galerkin product P^T A P of the piecewise-constant prolongation P (matrix rows where any merged
- * cell is a row).  At every level above the bottom: 2 damped Jacobi sweeps (weight 0.8), the residual
+ * cell is a row).  At every level above the bottom: 2 damped Jacobi sweeps (weight 6/7), the residual
  * restricted to the next level, the correction prolonged back, 2 more sweeps.  At the bottom level the
  * correction comes from the U-Net (fcg_bottom EFS_FCG_BOTTOM_UNET), scaled by the line search
  * (e.r)/(e.Ae) on that level, or, for comparison without the network, from 20 Jacobi sweeps
