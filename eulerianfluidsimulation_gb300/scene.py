@@ -391,6 +391,22 @@ class Scene2D:
         return cls(doc.get("width", 0), doc.get("height", 0), doc.get("boundary", []), doc.get("fluid", []),
                    doc.get("properties", {}))
 
+    @classmethod
+    def from_image(cls, path, threshold, properties=None):
+        """Scene2D::loadImage (Scene2D.cpp:87-121): the image, read as one 8-bit grey channel (image.read_grey8),
+        becomes a grid of the image's width x height.  Pixel i = x + y W (row 0 the image's top row) is fluid
+        when it is below `threshold` (threshold > 0), or when it is at least |threshold| (threshold <= 0); the
+        outermost cells are boundary (fluid there stays fluid, as in the reference)."""
+        from .image import read_grey8
+        px = read_grey8(path)
+        h, w = px.shape
+        flat = px.reshape(-1).astype(np.int64)
+        fluid = (flat < threshold) if threshold > 0 else ~(flat < abs(threshold))
+        x = np.arange(w)[None, :]
+        y = np.arange(h)[:, None]
+        border = ((x == 0) | (x == w - 1) | (y == 0) | (y == h - 1)).reshape(-1)
+        return cls(w, h, np.nonzero(border)[0], np.nonzero(fluid)[0], properties)
+
     def params(self, base=None):
         return params_from_properties(self.properties, base)
 

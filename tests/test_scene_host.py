@@ -252,3 +252,157 @@ def test_scene2d_roundtrip(tmp_path):
     sc.save(_Sim(), str(tmp_path / "t.scene2D"))
     back = S.Scene2D.load(str(tmp_path / "t.scene2D"))
     assert sorted(back.boundary.tolist()) == sorted(b) and back.fluid.tolist() == fl
+
+
+# ---- Scene2D::loadImage (Scene2D.cpp:87-121) and the 8-bit grey reading it relies on ----------------------------
+def _png_chunk(kind, body):
+    import struct
+    import zlib
+    return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+
+def _png_filter_rows(raw, bpp):
+    """PNG's five row filters applied in turn (row y uses filter y % 5), written from the PNG specification."""
+    out = bytearray()
+    prev = np.zeros(raw.shape[1], np.int64)
+    for y, line in enumerate(raw.astype(np.int64)):
+        f = y % 5
+        left = np.concatenate([np.zeros(bpp, np.int64), line[:-bpp]])
+        upleft = np.concatenate([np.zeros(bpp, np.int64), prev[:-bpp]])
+        if f == 0:
+            pred = np.zeros_like(line)
+        elif f == 1:
+            pred = left
+        elif f == 2:
+            pred = prev
+        elif f == 3:
+            pred = (left + prev) // 2
+        else:
+            p = left + prev - upleft
+            pa, pb, pc = np.abs(p - left), np.abs(p - prev), np.abs(p - upleft)
+            pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, upleft))
+        out.append(f)
+        out += ((line - pred) & 0xFF).astype(np.uint8).tobytes()
+        prev = line
+    return bytes(out)
+
+
+def _pack_rows(samples, bits):
+    """(h, w * channels) integer samples -> (h, row_bytes) uint8 scanlines at `bits` per sample."""
+    if bits == 8:
+        return samples.astype(np.uint8)
+    if bits == 16:
+        s = samples.astype(np.int64)
+        return np.stack([s >> 8, s & 0xFF], -1).reshape(s.shape[0], -1).astype(np.uint8)
+    bitsarr = ((samples[..., None] >> np.arange(bits - 1, -1, -1)) & 1).reshape(samples.shape[0], -1)
+    return np.packbits(bitsarr.astype(np.uint8), axis=1)
+
+
+def _write_png(path, samples, ctype, bits, palette=None, adam7=False):
+    """samples: (h, w, channels) integers; every row filter is used; Adam7 writes the seven passes in turn."""
+    import struct
+    import zlib
+    h, w, ch = samples.shape
+    bpp = max(1, ch * bits // 8)
+    if adam7:
+        data = b""
+        for x0, y0, dx, dy in ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+                               (0, 1, 1, 2)):
+            part = samples[y0::dy, x0::dx]
+            if part.size == 0:
+                continue
+            data += _png_filter_rows(_pack_rows(part.reshape(part.shape[0], -1), bits), bpp)
+    else:
+        data = _png_filter_rows(_pack_rows(samples.reshape(h, -1), bits), bpp)
+    png = b"\x89PNG\r\n\x1a\n" + _png_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, bits, ctype, 0, 0, 1 if adam7 else 0))
+    if palette is not None:
+        png += _png_chunk(b"PLTE", np.asarray(palette, np.uint8).tobytes())
+    png += _png_chunk(b"IDAT", zlib.compress(data)) + _png_chunk(b"IEND", b"")
+    path.write_bytes(png)
+
+
+def _luma(rgb):
+    rgb = rgb.astype(np.int64)
+    return (rgb[..., 0] * 77 + rgb[..., 1] * 150 + rgb[..., 2] * 29) >> 8
+
+
+def test_read_grey8_png_all_colour_types(tmp_path):
+    from eulerianfluidsimulation_gb300.image import read_grey8
+    rng = np.random.default_rng(3)
+    h, w = 13, 17
+    grey = rng.integers(0, 256, (h, w, 1))
+    _write_png(tmp_path / "g8.png", grey, 0, 8)
+    assert np.array_equal(read_grey8(str(tmp_path / "g8.png")), grey[..., 0])
+    _write_png(tmp_path / "g8i.png", grey, 0, 8, adam7=True)
+    assert np.array_equal(read_grey8(str(tmp_path / "g8i.png")), grey[..., 0])
+    rgb = rng.integers(0, 256, (h, w, 3))
+    _write_png(tmp_path / "rgb.png", rgb, 2, 8)
+    assert np.array_equal(read_grey8(str(tmp_path / "rgb.png")), _luma(rgb))
+    rgba = rng.integers(0, 256, (h, w, 4))
+    _write_png(tmp_path / "rgba.png", rgba, 6, 8)
+    assert np.array_equal(read_grey8(str(tmp_path / "rgba.png")), _luma(rgba))
+    ga = rng.integers(0, 256, (h, w, 2))
+    _write_png(tmp_path / "ga.png", ga, 4, 8)
+    assert np.array_equal(read_grey8(str(tmp_path / "ga.png")), ga[..., 0])
+    g16 = rng.integers(0, 65536, (h, w, 1))
+    _write_png(tmp_path / "g16.png", g16, 0, 16)
+    assert np.array_equal(read_grey8(str(tmp_path / "g16.png")), g16[..., 0] >> 8)
+    rgb16 = rng.integers(0, 65536, (h, w, 3))
+    _write_png(tmp_path / "rgb16.png", rgb16, 2, 16, adam7=True)
+    assert np.array_equal(read_grey8(str(tmp_path / "rgb16.png")), _luma(rgb16) >> 8)
+    for bits, scale in ((1, 255), (2, 85), (4, 17)):
+        low = rng.integers(0, 1 << bits, (h, w, 1))
+        _write_png(tmp_path / f"g{bits}.png", low, 0, bits)
+        assert np.array_equal(read_grey8(str(tmp_path / f"g{bits}.png")), low[..., 0] * scale), bits
+    pal = rng.integers(0, 256, (16, 3))
+    idx = rng.integers(0, 16, (h, w, 1))
+    _write_png(tmp_path / "p4.png", idx, 3, 4, palette=pal)
+    assert np.array_equal(read_grey8(str(tmp_path / "p4.png")), _luma(pal[idx[..., 0]]))
+
+
+def test_read_grey8_netpbm_and_bmp(tmp_path):
+    import struct
+    from eulerianfluidsimulation_gb300.image import read_grey8
+    rng = np.random.default_rng(4)
+    h, w = 7, 10
+    g = rng.integers(0, 256, (h, w)).astype(np.uint8)
+    (tmp_path / "a.pgm").write_bytes(b"P5\n# comment\n%d %d\n255\n" % (w, h) + g.tobytes())
+    assert np.array_equal(read_grey8(str(tmp_path / "a.pgm")), g)
+    rgb = rng.integers(0, 256, (h, w, 3)).astype(np.uint8)
+    (tmp_path / "a.ppm").write_bytes(b"P6 %d %d 255\n" % (w, h) + rgb.tobytes())
+    assert np.array_equal(read_grey8(str(tmp_path / "a.ppm")), _luma(rgb))
+    # 24-bit BMP, rows bottom-up and padded to 4 bytes
+    stride = (w * 3 + 3) // 4 * 4
+    rows = b"".join(rgb[y][:, ::-1].tobytes() + b"\0" * (stride - w * 3) for y in range(h - 1, -1, -1))
+    hdr = b"BM" + struct.pack("<IHHI", 54 + len(rows), 0, 0, 54) + struct.pack("<IiiHHIIiiII", 40, w, h, 1, 24, 0,
+                                                                                len(rows), 0, 0, 0, 0)
+    (tmp_path / "a.bmp").write_bytes(hdr + rows)
+    assert np.array_equal(read_grey8(str(tmp_path / "a.bmp")), _luma(rgb))
+
+
+@pytest.mark.parametrize("threshold", [128, -128, 1])
+def test_scene2d_from_image(tmp_path, threshold):
+    """The reference's loop: pixel i = x + y W is rho 1 when below the threshold (threshold > 0), or when at
+    least |threshold| (threshold <= 0); boundary 1 on the outermost cells; the grid is the image's size."""
+    rng = np.random.default_rng(5)
+    h, w = 11, 16
+    g = rng.integers(0, 256, (h, w, 1))
+    _write_png(tmp_path / "scene.png", g, 0, 8)
+    sc = S.Scene2D.from_image(str(tmp_path / "scene.png"), threshold)
+    assert (sc.width, sc.height) == (w, h)
+    want_rho = np.zeros(w * h, np.float32)
+    want_b = np.zeros(w * h, np.float32)
+    for x in range(w):
+        for y in range(h):
+            i = x + y * w
+            p = int(g[y, x, 0])
+            if threshold > 0:
+                want_rho[i] = 1.0 if p < threshold else 0.0
+            else:
+                want_rho[i] = 0.0 if p < abs(threshold) else 1.0
+            if x == 0 or x == w - 1 or y == 0 or y == h - 1:
+                want_b[i] = 1.0
+    grid = OracleSceneGrid((h, w))
+    sc.reset(grid)
+    assert np.array_equal(grid.field(abi.FIELD_RHO).ravel(), want_rho)
+    assert np.array_equal(grid.field(abi.FIELD_BOUNDARY).ravel(), want_b)
