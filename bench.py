@@ -96,6 +96,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(ms, world):
+    """The slowest rank's time (a collective: every rank calls it with its own time)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, ms, world):
+    """Whole-job throughput: the units all ranks processed (each rank its own replica) over the slowest rank's
+    time."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 def workload(a):
     from eulerianfluidsimulation_gb300 import abi
     solver = abi.SOLVER_JACOBI if a.solver == "jacobi" else abi.SOLVER_CG
@@ -359,13 +377,8 @@ def run_gb300(a):
     st1 = sim.stats()
     launches, solve_ms, row_iters, row_setups = sim.solve_timing_read()
     iters = st1.total_solve_steps - st0.total_solve_steps
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    steps_per_s = a.steps / (ms / 1e3) * world
+    ms = max_over_ranks(ms, world)
+    steps_per_s = job_throughput(a.steps, ms, world)
     if prm.solver == abi.SOLVER_JACOBI:
         solve_bytes = row_iters * JACOBI_BYTES_PER_ROW_ITER
     else:
@@ -428,13 +441,13 @@ def run_gb300(a):
         for _ in range(k_e2e):
             step_host()
         sim.mark(3)
-        ms_e2e = sim.elapsed_ms(2, 3)
+        ms_e2e = max_over_ranks(sim.elapsed_ms(2, 3), world)
         barrier()
         se1 = sim.stats()
         e_launches, e_solve_ms, _, _ = sim.solve_timing_read()
         # the e2e steps continue the trajectory after the timed steps: their solves may take other iteration
         # counts than the main line's, so the line carries them
-        e2e = {"value": k_e2e / (ms_e2e / 1e3) * world, "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
+        e2e = {"value": job_throughput(k_e2e, ms_e2e, world), "unit": "steps/s", "h2d_bytes_per_step": 4 * N * 9,
                "d2h_bytes_per_step": 4 * N * 8, "steps": k_e2e, "warmup": w_e2e, "ms_per_step": ms_e2e / k_e2e,
                "solve_iters_per_step": (se1.total_solve_steps - se0.total_solve_steps) / k_e2e,
                "solve_ms_per_step": (e_solve_ms / e_launches) if e_launches else None,
