@@ -164,7 +164,12 @@ def test_one_step_matches_oracle(dim, n):
 @pytest.mark.parametrize("dim,n,steps", [(3, 32, 12), (2, 96, 12)])
 def test_every_stage_exact_along_gpu_trajectory(dim, n, steps):
     """After `steps` GPU steps, each stage run from that GPU state matches the oracle run from the same state:
-    bit-exact, except rho_advect's atomically summed fields (relative L2 1e-6)."""
+    bit-exact, except rho_advect's atomically summed fields (relative L2 1e-6) and, rarely, project's pressure
+    and velocity.  Both solves round alpha and beta to float each iteration, the GPU from dot products summed
+    as float pairs (about 48 bits), the oracle from FP64 ones: when one of those roundings falls on the other
+    side of a float boundary, the iterates from there on differ in the last bits (seen once: 103 of 32^3
+    velocity cells, relative 9.5e-12).  Those two fields are held to 1e-9 in that case; everything else of the
+    stage stays bit-exact."""
     prm, b, r, _ = run_pair(dim, n, steps)
     with gpu_sim(dim, n, prm) as s:
         s.set_field(abi.FIELD_BOUNDARY, b)
@@ -181,6 +186,15 @@ def test_every_stage_exact_along_gpu_trajectory(dim, n, steps):
             if stage == abi.STAGE_RHO_ADVECT:
                 assert_fields(got, want, 1e-6, fields=(abi.FIELD_RHO, abi.FIELD_GAMMA, abi.FIELD_BETA), what="advect")
                 assert_fields(got, want, 0, fields=(abi.FIELD_VEL, abi.FIELD_PRESSURE), what="advect")
+            elif stage == abi.STAGE_PROJECT:
+                solved = (abi.FIELD_VEL, abi.FIELD_PRESSURE)
+                assert_fields(got, want, 0, fields=[f for f in range(abi.FIELD_COUNT) if f not in solved],
+                              what="project")
+                exact = all(np.array_equal(got[f], want[f]) for f in solved)
+                if not exact:
+                    print("project: the solves' float roundings of alpha or beta parted; " +
+                          ", ".join(f"{abi.FIELD_NAMES[f]} rel {rel_l2(got[f], want[f]):.2e}" for f in solved))
+                    assert_fields(got, want, 1e-9, fields=solved, what="project")
             else:
                 assert_fields(got, want, 0, what=abi.STAGE_NAMES[stage])
 
