@@ -605,10 +605,13 @@ void slab_maps(const bf16* in, int cin, const Level& L, int zs, tc::SlabMaps* ma
     maps->n = cin / 8;
 }
 
-// the implicit-GEMM (im2col) kernel serves the level; it can read an up-sampled input in place
+// whether the level's convolution of cin input channels runs below the halo-tile kernel (the slab kernel, or
+// the implicit-GEMM one where the slab does not fit).  Wide levels take the halo-tile kernel for 32 and 64 input
+// channels; with 16 the slab kernel is faster there too (at 256^3 layer 0 0.60 against 0.89 ms, at 192^3 0.26
+// against 0.50 ms), with 32 and 64 slower (one to three CTAs an SM).
 bool conv_im2col(const UNetState* u, int level, int cin) {
     const Level& L = u->L[level];
-    return !(L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64);
+    return !(L.W >= kHaloMinWidth && cin % 16 == 0 && cin <= 64 && cin > 16);
 }
 
 // up: `in` is the next coarser level's tensor, read as its nearest up-sampling (not on halo-tile levels).
@@ -764,7 +767,9 @@ cudaError_t forward(UNetState* u, const float* r, const LvView& M, bool train, c
     mark(5);
     // the up-samplings: read in place by the next convolution where it is the implicit-GEMM kernel and nothing
     // keeps the up-sampled tensor (training's weight gradients read it)
-    const bool up3 = !train && conv_im2col(u, 1, 64), up4 = !train && conv_im2col(u, 0, 32);
+    // (wide levels materialise the up-sampling: a gather of it per brick there is slower than the copy)
+    const bool up3 = !train && conv_im2col(u, 1, 64) && u->L[1].W < kHaloMinWidth,
+               up4 = !train && conv_im2col(u, 0, 32) && u->L[0].W < kHaloMinWidth;
     if (!up3) {
         k_up<<<nblk(L[1].V * 8), 256, 0, st>>>(u->e2, L[2], u->u2, L[1], 64);
         UCK(cudaGetLastError());

@@ -75,9 +75,10 @@ def test_unet_gradients_match_oracle(kind):
 
 
 def test_unet_halo_tile_path_matches_oracle():
-    """Grids at least 96 voxels wide take the halo-tile convolution (TMA input box, one descriptor per tap):
-    here levels 0 and 1 (widths 200 and 100: a partial second segment, 16/32/64 input channels, COUT
-    16/32/64 in the forward and input-gradient passes); level 2 (width 50) takes the slab kernel."""
+    """Grids at least 96 voxels wide take the halo-tile convolution (TMA input box, one descriptor per tap) for
+    32 and 64 input channels: here levels 0 and 1 (widths 200 and 100: a partial second segment, COUT 16/32/64
+    in the forward and input-gradient passes).  Their 16-channel convolutions, and level 2 (width 50), take the
+    slab kernel on these wide grids."""
     W, H, D = 200, 12, 10
     bnd, rho = oracle.scene_dam3d(W, H, D, 3, 3, 6)
     rows = (rho > 0.5) & (bnd == 0.0)
