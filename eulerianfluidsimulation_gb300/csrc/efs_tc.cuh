@@ -390,7 +390,9 @@ __global__ void k_conv_split_reduce(const float* __restrict__ partial, int split
 // voxels, each 8 (x) x 16 (y) x 1 (z); slabs reaching past the grid compute zeros there and store only the
 // voxels inside.  It copies their input with a one-voxel halo (10 x 18 x (ZS + 2) voxels; zero outside the grid;
 // with `up`, voxel (x, y, z) of the half-resolution input at (x/2, y/2, z/2)) into shared memory once, as planes
-// of 8 channels ([cin/8][z][y][x] x 16 bytes), together with every K step's weight tile.  The A operand of step
+// of 8 channels ([cin/8][z][y][x] x 16 bytes, each padded to 128 bytes), together with every K step's weight
+// tile.  The planes arrive by one tensor load each (SlabMaps) or, for an up-sampled input, by a cp.async gather;
+// the weights, pre-packed in this order (ConvArgs::wslab), by one bulk copy.  The A operand of step
 // (tap, chunk) of slab k is a descriptor into that copy: 8 x-consecutive voxels of one y row are a 128-byte core
 // matrix, the slab's 16 rows follow at the row pitch (stride byte offset 160), and the chunk's upper 8 channels
 // one plane further (leading byte offset).  A tap or a slab only moves the start address, so one thread issues
