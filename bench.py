@@ -564,7 +564,7 @@ def run_fcg(a):
     steps_per_s = a.steps / (ms / 1e3)
     cfg = config(a)
     cfg["solver"] = ("fcg_unet rel-res 1e-6 (flexible PCG, multigrid V-cycle with the U-Net 16/32/64 BF16 as its "
-                     "coarsest-level solve, x as float pairs, FP64 true residual, CG fallback on stall)")
+                     "coarsest-level solve, x as float pairs, true residual in pair arithmetic, CG fallback on stall)")
     line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": 1, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,

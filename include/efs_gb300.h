@@ -64,7 +64,7 @@ enum efs_solver {
     /* No counterpart in the reference: flexible preconditioned CG (Notay's FCG(1)) on the same matrix and
      * to the same stop rule as EFS_SOLVER_CG, from p0 = 0, with the pressure accumulated as float pairs (about
      * 48 significant bits; efs_download_pressure_fp64 gives their sum) and the true residual recomputed in
-     * FP64 every 32 iterations and before stopping.  Its preconditioner is a multigrid
+     * the same pair arithmetic every 32 iterations and before stopping.  Its preconditioner is a multigrid
      * V-cycle whose coarsest level is solved by the context's learned U-Net (3D; efs_unet_*, fcg_levels and
      * fcg_bottom below).  When the residual stalls (not halved over 10 iterations) or a direction breaks
      * down, the remaining residual system goes to plain CG (EFS_CG_MIXED_RECURRENCE).  The whole solve is
@@ -74,8 +74,8 @@ enum efs_solver {
 };
 
 /* CG variants.  Both follow CGSolverCPU3D::solve (CGSolver.cpp:416-465): p0 = b, recurrence residual, the
- * true residual recomputed when (i & 63) == 0, stop when r.r < threshold or after max_steps, FP64 dot
- * products.  EFS_CG_MIXED keeps the pressure as an extended-precision accumulator (a pair of floats, about
+ * true residual recomputed when (i & 63) == 0, stop when r.r < threshold or after max_steps, FP64-class dot
+ * products (summed as float pairs on the GPU, in FP64 by the CPU oracle).  EFS_CG_MIXED keeps the pressure as an extended-precision accumulator (a pair of floats, about
  * 48 significant bits, computed on the FP32 pipe) plus an FP32 increment that is folded in at every
  * recomputation, and computes that true residual in the same pair arithmetic (group-wise reliable updates;
  * the CPU oracle uses FP64 for both); before
